@@ -1,0 +1,104 @@
+/* C interface of the CPU oracle (test infrastructure; see oracle_common.h).
+ *
+ * Layouts: mosaics are row-major f32 or u16 with an explicit row stride in
+ * samples; RGB images are interleaved f32 [h][3*w]. CFA codes: 0 RGGB, 1 BGGR,
+ * 2 GRBG, 3 GBRG. Every function is a restatement of one reference stage; the
+ * file that implements it cites the reference file:line it follows.
+ */
+#ifndef RD_ORACLE_H
+#define RD_ORACLE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- demosaic (demosaic.cpp, amaze.cpp) ---- */
+void ro_bilinear_reconstruct(const float* mosaic, int w, int h, int stride, int pattern, const float gains[3],
+                             float* out, int out_stride);
+void ro_mhc_reconstruct(const float* mosaic, int w, int h, int stride, int pattern, const float gains[3],
+                        float* out, int out_stride);
+int ro_rcd_reconstruct(const float* mosaic, int w, int h, int stride, int pattern, const float gains[3],
+                       float* out, int out_stride);
+int ro_amaze_reconstruct(const float* mosaic, int w, int h, int stride, int pattern, const float gains[3],
+                         float clip_point, float* out, int out_stride);
+int ro_amaze_probe_tile(const float* mosaic, int w, int h, int stride, int pattern, float clip_point,
+                        const char* plane, float* out);
+/* algorithm: 0 bilinear, 1 MHC, 2 RCD, 3 AMaZE; balance = as-shot gains. */
+int ro_demosaic(const float* mosaic, int w, int h, int pattern, const float balance[3], int algorithm,
+                float* out);
+
+/* ---- sensor contract + highlight (sensor.cpp) ---- */
+typedef struct ro_sensor {
+  int sensor_w, sensor_h, row_stride;
+  int crop_x, crop_y, crop_w, crop_h;
+  int pattern;                /* sensor CFA pattern at sensor (0,0) */
+  int black_w, black_h;       /* black repeat pattern */
+  const float* black;         /* black_w*black_h values */
+  int white_count;            /* 1, 3 or black_w*black_h */
+  const float* white;
+} ro_sensor;
+
+/* NormalizationContract::normalize at full crop size. Returns crop pattern. */
+int ro_normalize(const uint16_t* mosaic, const ro_sensor* s, float* out);
+/* clip_cancellable: stats = {affected, changed, over_white, aff_r, aff_g, aff_b}. */
+int ro_clip(float* mosaic, int w, int h, int pattern, const float levels[3], uint64_t stats[6]);
+/* reconstruct_opposed_cancellable. ceiling may be NULL. stats = {suspected, reconstructed,
+ * changed, fallback, unsupported, neutralised, susp_r, susp_g, susp_b}. labels_out (optional,
+ * ceil(w/2)*ceil(h/2) u32) receives the compact region labels. */
+int ro_opposed(float* mosaic, int w, int h, int pattern, const float levels[3], const float* ceiling,
+               uint64_t stats[9], uint32_t* labels_out, uint32_t* region_count);
+/* label_components on a 0/1 grid (regions.rs:188-281); returns count. */
+uint32_t ro_label_components(uint32_t* labels, int w, int h);
+
+/* ---- capture sharpening (capture.cpp) ---- */
+/* Gaussian kernel weights (crates/detail/src/gaussian.rs:9-17); returns tap count. */
+int ro_gaussian_kernel(float sigma, float* weights, int max_taps);
+int ro_capture_sharpen(float* rgb, int w, int h, float amount, float radius, float noise,
+                       const float ceilings[3], int iterations);
+
+/* ---- optics (optics.cpp) ---- */
+typedef struct ro_optics {
+  int width, height;
+  double norm_scale, norm_unscale, center_x, center_y;
+  float scale;
+  int distortion_model; /* 0 none, 1 poly3, 2 poly5, 3 ptlens */
+  float distortion[3];
+  int tca_model;        /* 0 none, 1 linear, 2 poly3 */
+  float tca_red[3], tca_blue[3];
+  int vignetting_model; /* 0 none, 1 pa */
+  float vignetting[3];
+} ro_optics;
+/* build_plan's geometry for a 36x24-normalised sensor: fills norm/center/scale. */
+int ro_optics_plan(ro_optics* plan, float crop_factor, float real_focal, float lens_center_x,
+                   float lens_center_y);
+int ro_optics_apply(const ro_optics* plan, const float* rgb_in, float* rgb_out);
+int ro_optics_map(const ro_optics* plan, int x, int y, float coords[6]);
+
+/* ---- area reduction (spatial.cpp) ---- */
+int ro_area_reduce(const float* rgb, int w, int h, int tw, int th, float* out);
+
+/* ---- colour + output (color.cpp) ---- */
+void ro_white_balance(float* rgb, size_t pixels, const float gains[3]);
+void ro_camera_matrix(float* rgb, size_t pixels, const float m[9]);
+typedef struct ro_adjust {
+  float exposure_ev;
+  const float* base_lut;    /* 4096 entries or NULL */
+  const float* tone_lut;    /* 4096 entries or NULL */
+  float saturation, vibrance;
+  int has_hsl;
+  float hsl[8][3];          /* hue, saturation, luminance per band */
+  int has_grading;
+  float grading[3][3];      /* shadows, midtones, highlights x RGB */
+} ro_adjust;
+void ro_adjust_apply(float* rgb, size_t pixels, const ro_adjust* a);
+void ro_standard_base_lut(float* lut4096);
+void ro_display_srgb8(const float* rgb, size_t pixels, uint8_t* out);
+void ro_histogram(const uint8_t* rgb8, size_t pixels, uint64_t hist[4 * 256], uint64_t clipped[6]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
