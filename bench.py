@@ -1,0 +1,410 @@
+"""Benchmark: full-sensor 24 MP develops per second on one GB300.
+
+Workload (the reference's full-sensor configuration): 6048x4024 RGGB u16
+14-bit synthetic mosaic, ~5% clipped in Gaussian blobs; Opposed highlight;
+AMaZE; masked RL capture sharpening, 10 iterations, sigma 0.7; optics (Poly5
+distortion -0.02/0.005, PA vignetting, linear TCA 1.0003/0.9997); exact area
+reduction to 2560x1703; WB + camera matrix; exposure +0.5 EV, 16-knot tone
+curve, 8-band HSL; sRGB 8-bit + histogram.
+
+A step is one complete develop of one mosaic. `value` is measured with the
+mosaic already resident in HBM (rd_develop_device -> rd_spatial ->
+rd_render_device); `e2e` goes through the host-buffer C ABI (rd_develop from
+pinned host memory -> rd_spatial -> rd_render into host memory), copies
+included. L2 is flushed before every timed step (outside the step's events).
+
+Multi-GPU: images are independent, so N GPUs run N replicas; value = N x
+per-GPU develops/s (max step time over ranks).
+
+`--impl reference` times the reference algorithm on the host cores: the
+reference is Rust and cannot be built here, so its CPU restatement (the
+oracle) runs on a bounded band of the same workload per step.
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "24MP develops/s"
+UNIT = "develops/s"
+
+
+def dist_setup(gpus: int):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo", init_method="env://")
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, value: float) -> float:
+    if pg is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.thread.join(timeout=2)
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# Algorithmic bytes per launch of each kernel family, per pixel of the image it covers.
+def family_bytes(name: str, N: int, n: int, H: int, tw: int) -> float | None:
+    table = {
+        "amaze": 14.0 * N,          # u16 mosaic in, planar f32 RGB out
+        "rl_iteration": 12.0 * N,   # estimate in, guide in, estimate out
+        "rl_mask": 12.0 * N,
+        "rl_init": 24.0 * N,
+        "rl_apply": 36.0 * N,
+        "vignetting": 4.0 * N,
+        "optics_gather": 28.0 * N,  # RGB + multiplier in, RGB out
+        "area_horizontal": 12.0 * N + 12.0 * tw * H,
+        "area_vertical": 12.0 * tw * H + 12.0 * n,
+        "wb_matrix": 24.0 * n,
+        "color_output": 15.0 * n,
+        "opposed": 6.0 * N,
+        "mhc_bilinear": 14.0 * N,
+        "rcd": 14.0 * N,
+    }
+    return table.get(name)
+
+
+def run_ours(args, world, rank, local, pg):
+    from rohditor_gb300 import Device
+    from rohditor_gb300 import _ffi
+    from rohditor_gb300.workloads import full_24mp
+
+    dev = Device(local)
+    lib = dev.lib
+    h = dev.handle
+    wl = full_24mp(demosaic=args.demosaic, iterations=args.iterations, highlight=args.highlight,
+                   width=args.width, height=args.height)
+    W, H = wl.width, wl.height
+    tw, th = wl.target
+    N, n = W * H, tw * th
+    sensor = wl.sensor.to_c()
+    detail = wl.capture.to_c()
+    optics = wl.optics.to_c()
+    color = wl.color.to_c()
+    wb = np.ascontiguousarray(wl.color.wb_gains, dtype=np.float32)
+    cam = np.ascontiguousarray(wl.color.camera_to_rec2020, dtype=np.float32)
+    wbp = wb.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    camp = cam.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    d_mosaic = wl.mosaic_device(dev)
+    # Pinned host copy of the same mosaic and pinned host outputs for the end-to-end leg.
+    mos_bytes = 2 * N
+    h_mosaic = ctypes.c_void_p()
+    dev.check(lib.rd_host_alloc(mos_bytes, ctypes.byref(h_mosaic)))
+    dev.check(lib.rd_copy_to_host(h, h_mosaic, ctypes.c_void_p(d_mosaic), mos_bytes))
+    h_out = ctypes.c_void_p()
+    dev.check(lib.rd_host_alloc(3 * n, ctypes.byref(h_out)))
+    hist = np.zeros(1024, dtype=np.uint64)
+    clipped = np.zeros(6, dtype=np.uint64)
+
+    def step_device():
+        src, base = ctypes.c_void_p(), ctypes.c_void_p()
+        dev.check(lib.rd_develop_device(h, ctypes.c_void_p(d_mosaic), W, ctypes.byref(sensor), ctypes.byref(detail),
+                                        None, ctypes.byref(src), None))
+        dev.check(lib.rd_spatial(h, src, ctypes.byref(optics), tw, th, wbp, camp, ctypes.byref(base), None))
+        dev.check(lib.rd_render_device(h, base, ctypes.byref(color), None))
+        lib.rd_source_release(src)
+        lib.rd_base_release(base)
+
+    def step_e2e():
+        src, base = ctypes.c_void_p(), ctypes.c_void_p()
+        dev.check(lib.rd_develop(h, ctypes.cast(h_mosaic, ctypes.POINTER(ctypes.c_uint16)), W, ctypes.byref(sensor),
+                                 ctypes.byref(detail), None, ctypes.byref(src), None))
+        dev.check(lib.rd_spatial(h, src, ctypes.byref(optics), tw, th, wbp, camp, ctypes.byref(base), None))
+        dev.check(lib.rd_render(h, base, ctypes.byref(color), ctypes.cast(h_out, ctypes.POINTER(ctypes.c_uint8)),
+                                hist.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                clipped.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), None))
+        lib.rd_source_release(src)
+        lib.rd_base_release(base)
+
+    def timed(step, steps):
+        total = 0.0
+        per = []
+        for _ in range(steps):
+            dev.check(lib.rd_ctx_flush_l2(h))
+            dev.check(lib.rd_ctx_event_record(h, 0))
+            step()
+            dev.check(lib.rd_ctx_event_record(h, 1))
+            ms = ctypes.c_float()
+            dev.check(lib.rd_ctx_event_elapsed(h, 0, 1, ctypes.byref(ms)))
+            per.append(ms.value)
+            total += ms.value
+        return total, per
+
+    for _ in range(args.warmup):
+        step_device()
+    dev.synchronize()
+    lib.rd_ctx_reset_kernel_timing(h)
+    lib.rd_ctx_enable_kernel_timing(h, 1)
+    launches0 = dev.kernel_launches
+    barrier(pg)
+    dev.synchronize()
+    with ClockSampler(local) as clocks:
+        total_ms, per = timed(step_device, args.steps)
+    dev.synchronize()
+    launches = dev.kernel_launches - launches0
+    lib.rd_ctx_enable_kernel_timing(h, 0)
+    barrier(pg)
+    total_ms = max_over_ranks(pg, total_ms)
+    families = {}
+    for f in range(16):
+        name = ctypes.c_char_p()
+        ms = ctypes.c_double()
+        cnt = ctypes.c_uint64()
+        lib.rd_ctx_kernel_timing(h, f, ctypes.byref(name), ctypes.byref(ms), ctypes.byref(cnt))
+        if ms.value > 0:
+            families[name.value.decode()] = {"ms": ms.value, "launches": int(cnt.value)}
+    # e2e through host buffers
+    for _ in range(max(1, args.warmup // 2)):
+        step_e2e()
+    barrier(pg)
+    e2e_ms, e2e_per = timed(step_e2e, args.steps)
+    e2e_ms = max_over_ranks(pg, e2e_ms)
+
+    ms_per_step = total_ms / args.steps
+    value = world * args.steps / (total_ms / 1e3)
+    e2e_value = world * args.steps / (e2e_ms / 1e3)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    # Dominant HBM-bound kernel (largest device time among the bandwidth-bound families).
+    kernels = {}
+    for name, rec in families.items():
+        b = family_bytes(name, N, n, H, tw)
+        per_launch_ms = rec["ms"] / max(rec["launches"], 1)
+        entry = {"total_ms": round(rec["ms"], 3), "launches": rec["launches"],
+                 "ms_per_launch": round(per_launch_ms, 4)}
+        if b is not None:
+            gbs = b / (per_launch_ms / 1e3) / 1e9
+            entry["algorithmic_gbs"] = round(gbs, 1)
+            entry["hbm_frac"] = round(gbs / hbm_peak, 3)
+        kernels[name] = entry
+    step_kernel_ms = sum(r["ms"] for r in families.values()) / args.steps
+    dominant = max(families.items(), key=lambda kv: kv[1]["ms"])[0] if families else None
+    hbm_families = [k for k in families if k not in ("amaze", "rcd", "opposed", "synth")]
+    dom_hbm = max(hbm_families, key=lambda k: families[k]["ms"]) if hbm_families else None
+    roofline = None
+    if dom_hbm:
+        rec = families[dom_hbm]
+        per_launch_s = rec["ms"] / rec["launches"] / 1e3
+        achieved = family_bytes(dom_hbm, N, n, H, tw) / per_launch_s / 1e9
+        roofline = {"bound": "hbm", "kernel": dom_hbm, "achieved": round(achieved, 1), "peak": hbm_peak,
+                    "unit": "GB/s", "frac": round(achieved / hbm_peak, 3), "traffic": None,
+                    "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
+                    else "fallback 6.8 TB/s"}
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
+        "config": {"workload": f"full_24mp {W}x{H} RGGB 14-bit, {args.highlight} + {args.demosaic} + "
+                               f"RL{args.iterations} + optics(poly5, PA vignetting, linear TCA) + area->{tw}x{th} "
+                               f"+ WB/matrix + exposure/tone/HSL + sRGB8 + histogram",
+                   "mp_per_s": round(value * N / 1e6, 1), "parallelism": f"replicas x{world}",
+                   "l2": "flushed before every timed step (256 MB write outside the step events)"},
+        "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": mos_bytes,
+                "d2h_bytes_per_step": 3 * n + 1024 * 8 + 6 * 8, "ms_per_step": round(e2e_ms / args.steps, 3)},
+        "gpu_launches": int(launches),
+        "roofline": roofline,
+        "kernels": kernels,
+        "dominant_kernel": dominant,
+        "kernel_ms_per_step": round(step_kernel_ms, 3),
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args, sample_rows=args.cpu_baseline_rows)
+    lib.rd_host_free(h_mosaic)
+    lib.rd_host_free(h_out)
+    dev.check(lib.rd_device_free(h, ctypes.c_void_p(d_mosaic)))
+    dev.close()
+    return line
+
+
+def cpu_develop_band(rows: int, args) -> tuple[float, float]:
+    """Run the oracle pipeline on a `rows`-high band of the 24 MP workload; returns (seconds, fraction)."""
+    from oracle import oracle as o
+    from rohditor_gb300.workloads import full_24mp, preview_dimensions
+
+    wl = full_24mp(demosaic=args.demosaic, iterations=args.iterations, highlight=args.highlight)
+    W, H = wl.width, wl.height
+    rng = np.random.default_rng(5)
+    # A band with the workload's statistics: smooth scene, ~5% clipped blobs, 14-bit levels.
+    yy, xx = np.mgrid[0:rows, 0:W].astype(np.float32)
+    scene = 0.35 + 0.2 * np.sin(xx / 97.0) * np.cos(yy / 61.0)
+    blobs = ((xx % 900 - 450) ** 2 + (yy % 700 - 350) ** 2) < 110 ** 2
+    scene[blobs] = 2.0
+    raw = np.clip(512 + scene * 15871 + rng.normal(0, 20, scene.shape), 0, 16383).astype(np.uint16)
+    odesc = o.sensor_desc(W, rows, W, (0, 0, W, rows), 0, [512.0], (1, 1), [16383.0])
+    t0 = time.perf_counter()
+    m, pattern = o.normalize(raw, odesc)
+    if args.highlight == "opposed":
+        m, _, _, _ = o.opposed(m, pattern, wl.sensor.detection_levels, wl.sensor.neutral_ceiling)
+    else:
+        m, _ = o.clip(m, pattern, wl.sensor.clip_levels)
+    algo = {"bilinear": 0, "mhc": 1, "rcd": 2, "amaze": 3}[args.demosaic]
+    rgb = o.demosaic(m, pattern, wl.sensor.demosaic_balance, algo)
+    cap = wl.capture
+    rgb = o.capture(rgb, cap.amount, cap.radius, cap.noise_protection, cap.ceilings, cap.iterations)
+    plan = o.optics_plan(W, rows, 2, (-0.02, 0.005, 0.0), 1, (1.0003, 0, 0), (0.9997, 0, 0))
+    plan.vignetting_model = 1
+    for k, v in enumerate(wl.optics.vignetting_k):
+        plan.vignetting[k] = v
+    rgb = o.optics_apply(plan, rgb)
+    tw, th = preview_dimensions(W, rows, 2560)
+    base = o.camera_matrix(o.white_balance(o.area_reduce(rgb, (tw, th)), wl.color.wb_gains),
+                           wl.color.camera_to_rec2020)
+    c = wl.color
+    x = o.adjust(base, c.exposure_ev, c.base_lut, c.tone_lut, c.saturation, c.vibrance, c.hsl, c.grading)
+    o.histogram(o.display_srgb8(x))
+    return time.perf_counter() - t0, rows / H
+
+
+def cpu_baseline(args, sample_rows: int) -> dict:
+    secs, frac = cpu_develop_band(sample_rows, args)
+    cores = os.cpu_count() or 1
+    return {"value": round(frac / secs, 4), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"oracle (C++ restatement of the reference CPU pipeline, OpenMP on {cores} threads) on a "
+                      f"6048x{sample_rows} band of the 24 MP workload ({frac:.3f} of a develop) in {secs:.1f} s; "
+                      f"value = develop-fraction / seconds"}
+
+
+def run_reference(args, world, rank, pg):
+    if rank != 0:
+        return None
+    rows = args.cpu_rows
+    times = []
+    for i in range(args.warmup + args.steps):
+        secs, frac = cpu_develop_band(rows, args)
+        if i >= args.warmup:
+            times.append(secs)
+    total = sum(times)
+    value = args.steps * frac / total
+    cores = os.cpu_count() or 1
+    cpu = {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": "port",
+           "sample": f"6048x{rows} band ({frac:.3f} of a 24 MP develop) per step through the oracle"}
+    return {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps / frac, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": {"workload": f"full_24mp 6048x4024, {args.highlight} + {args.demosaic} + RL{args.iterations} + "
+                               f"optics + area->2560x1703 + colour + sRGB8 + histogram (CPU restatement; the Rust "
+                               f"reference cannot be built on this image)"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--highlight", default="opposed", choices=["opposed", "clip"])
+    p.add_argument("--demosaic", default="amaze", choices=["amaze", "rcd", "mhc"])
+    p.add_argument("--iterations", type=int, default=10)
+    p.add_argument("--cpu-rows", type=int, default=256)
+    p.add_argument("--width", type=int, default=6048, help="mosaic width (smaller cases for profiling)")
+    p.add_argument("--height", type=int, default=4024)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-baseline-rows", type=int, default=2048,
+                   help="band height of the CPU baseline sample (2048 rows = half a 24 MP develop)")
+    args = p.parse_args()
+    world, rank, local, pg = dist_setup(args.gpus)
+    if args.impl == "reference":
+        line = run_reference(args, world, rank, pg)
+    else:
+        line = run_ours(args, world, rank, local, pg)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

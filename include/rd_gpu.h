@@ -1,0 +1,263 @@
+/* rd_gpu.h - C ABI of the GB300 sensor-development library.
+ *
+ * This is the drop-in boundary that replaces the wgpu executors of the
+ * reference's `rohditor-gpu` crate (crates/gpu). Only plain-old-data, opaque
+ * handles and plain pointers cross it; no exception and no C++ or torch type.
+ * Every call is ordered on the context's CUDA stream. Host pointers are
+ * borrowed only for the duration of the call. Device objects (rd_source,
+ * rd_base) are owned by their handles and must be released.
+ *
+ * Reference interface each entry point stands in for (file:line in the
+ * reference project):
+ *   rd_status                GpuPreviewError            crates/gpu/src/lib.rs:55-111
+ *   rd_ctx_create            GpuSensorProcessor::new    crates/gpu/src/sensor/normalize.rs:91
+ *   rd_ctx_set_budget        GpuSensorProcessor::set_budget  crates/gpu/src/sensor/normalize.rs:157
+ *   rd_supports              GpuSensorProcessor::supports    crates/gpu/src/sensor/develop.rs:55
+ *   rd_develop               GpuSensorProcessor::develop     crates/gpu/src/sensor/develop.rs:68
+ *   rd_spatial               GpuSpatialProcessor::reduce_preview crates/gpu/src/spatial/reduction.rs:15
+ *   rd_render                GpuPreviewProcessor::render + begin_histogram
+ *                                                       crates/gpu/src/preview/processor.rs:1011,1518
+ *   stage entry points       the crates' stage APIs the CPU pipeline calls:
+ *     rd_stage_normalize     NormalizationContract::normalize crates/core/src/pipeline/sensor.rs:221
+ *     rd_stage_highlight     HighlightExecution::apply_cancellable crates/highlight/src/lib.rs:172
+ *     rd_stage_demosaic      demosaic_cancellable        crates/demosaic/src/lib.rs:302
+ *     rd_stage_capture       sharpening::apply_cancellable crates/core/src/sharpening.rs:87
+ *     rd_stage_optics        OpticsExecution::apply_cancellable crates/optics/src/correction.rs:49
+ *     rd_stage_area_reduce   resize_area_with_plan_cancellable crates/core/src/resample.rs:235
+ *     rd_stage_color         apply_white_balance + apply_camera_color_transform +
+ *                            apply_adjustments_with_local + render_display8 + Histogram
+ *                            crates/core/src/cpu/stages.rs:250-308,380-528,1028-1094;
+ *                            crates/core/src/analysis/histogram.rs:92-128
+ */
+#ifndef RD_GPU_H
+#define RD_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* GpuPreviewError variants (crates/gpu/src/lib.rs:55-111). */
+typedef enum rd_status {
+  RD_OK = 0,
+  RD_CANCELLED = 1,
+  RD_UNSUPPORTED = 2,
+  RD_OVER_BUDGET = 3,
+  RD_INVALID_DIMENSIONS = 4,
+  RD_BASE_MISMATCH = 5,
+  RD_UNSUPPORTED_EDITS = 6,
+  RD_SYNCHRONIZATION = 7,
+  RD_INVALID_INPUT = 8,
+  RD_READBACK = 9
+} rd_status;
+
+/* 1 for the routing answers that keep the device usable (UnsupportedEdits,
+ * OverBudget; GpuPreviewError::is_routing), else 0. */
+int rd_status_is_routing(rd_status status);
+const char* rd_status_name(rd_status status);
+
+typedef struct rd_ctx rd_ctx;
+typedef struct rd_source rd_source; /* full-resolution camera RGB resident on the device */
+typedef struct rd_base rd_base;     /* reduced Rec.2020 base resident on the device */
+
+/* ---- descriptors: the CPU-resolved contracts, never raw recipe fields ---- */
+
+enum { RD_CFA_RGGB = 0, RD_CFA_BGGR = 1, RD_CFA_GRBG = 2, RD_CFA_GBRG = 3 };
+enum { RD_HIGHLIGHT_OFF = 0, RD_HIGHLIGHT_CLIP = 1, RD_HIGHLIGHT_OPPOSED = 2 };
+enum { RD_DEMOSAIC_BILINEAR = 0, RD_DEMOSAIC_MHC = 1, RD_DEMOSAIC_RCD = 2, RD_DEMOSAIC_AMAZE = 3 };
+#define RD_MAX_LEVEL_PATTERN 64
+
+/* NormalizationContract + SensorDevelopmentDescription
+ * (crates/core/src/pipeline/sensor.rs:56-67, 280-298). Levels are indexed at
+ * SENSOR coordinates; the crop's CFA phase is derived from `cfa` by the shift. */
+typedef struct rd_sensor_desc {
+  uint32_t sensor_width, sensor_height;
+  uint32_t crop_x, crop_y, crop_width, crop_height;
+  int32_t cfa;                       /* pattern at sensor (0,0): RD_CFA_* */
+  uint32_t black_repeat_w, black_repeat_h;
+  float black[RD_MAX_LEVEL_PATTERN]; /* black_repeat_w*black_repeat_h values */
+  uint32_t white_count;              /* 1, 3 (per channel) or black_repeat_w*black_repeat_h */
+  float white[RD_MAX_LEVEL_PATTERN];
+  int32_t highlight;                 /* RD_HIGHLIGHT_* */
+  float clip_levels[3];              /* Clip: per-channel ceilings */
+  float detection_levels[3];         /* Opposed: detection levels */
+  int32_t has_neutral_ceiling;
+  float neutral_ceiling[3];          /* Opposed: WB-aware neutral ceiling */
+  int32_t demosaic;                  /* RD_DEMOSAIC_* */
+  float demosaic_balance[3];         /* as-shot gains the demosaic reconstructs under */
+} rd_sensor_desc;
+
+/* CaptureSharpeningContract (crates/core/src/sharpening.rs:17-68). The
+ * iteration count is explicit (the reference fixes it at 8). */
+typedef struct rd_detail_desc {
+  int32_t enabled;
+  float amount, radius, noise_protection;
+  float ceilings[3];
+  int32_t iterations;
+} rd_detail_desc;
+
+enum { RD_DISTORTION_NONE = 0, RD_DISTORTION_POLY3 = 1, RD_DISTORTION_POLY5 = 2, RD_DISTORTION_PTLENS = 3 };
+enum { RD_TCA_NONE = 0, RD_TCA_LINEAR = 1, RD_TCA_POLY3 = 2 };
+
+/* OpticsExecution (crates/optics/src/plan.rs:37-50): the resolved, lensfun-free
+ * correction contract. */
+typedef struct rd_optics_desc {
+  uint32_t width, height;
+  double norm_scale, norm_unscale, center_x, center_y;
+  float scale;
+  int32_t distortion_model;
+  float distortion[3];
+  int32_t tca_model;
+  float tca_red[3], tca_blue[3];
+  int32_t vignetting;     /* 0 none, 1 PA */
+  float vignetting_k[3];
+} rd_optics_desc;
+
+/* White balance, camera matrix and the global adjustment chain
+ * (crates/core/src/cpu/stages.rs:380-528) with LUTs resolved on the host. */
+typedef struct rd_color_desc {
+  float wb_gains[3];
+  float camera_to_rec2020[9];   /* row-major */
+  float exposure_ev;
+  int32_t has_base_lut;
+  float base_lut[4096];         /* BaseRenderingLut values */
+  int32_t has_tone_lut;
+  float tone_lut[4096];         /* ToneCurveLut values */
+  float saturation, vibrance;
+  int32_t has_hsl;
+  float hsl[8][3];              /* hue, saturation, luminance per band */
+  int32_t has_grading;
+  float grading[3][3];          /* shadows, midtones, highlights x RGB */
+} rd_color_desc;
+
+/* StageTimings-style device timings (ms) and counters. */
+typedef struct rd_metrics {
+  float normalize_highlight_ms, demosaic_ms, capture_ms, optics_ms, reduce_ms, color_ms, total_ms;
+  uint64_t highlight_stats[9]; /* Clip: affected, changed, over_white, aff_r,g,b.
+                                  Opposed: suspected, reconstructed, changed, fallback,
+                                  unsupported, neutralised, susp_r,g,b */
+  uint64_t kernel_launches;
+  uint64_t device_bytes;
+} rd_metrics;
+
+/* ---- context ---- */
+rd_status rd_ctx_create(int device, uint64_t budget_bytes, rd_ctx** out);
+/* Every rd_source and rd_base of the context must be released first. */
+void rd_ctx_destroy(rd_ctx* ctx);
+rd_status rd_ctx_set_budget(rd_ctx* ctx, uint64_t budget_bytes);
+const char* rd_ctx_last_error(const rd_ctx* ctx);
+rd_status rd_ctx_synchronize(rd_ctx* ctx);
+/* Number of this library's kernels launched on the context so far. */
+uint64_t rd_ctx_kernel_launches(const rd_ctx* ctx);
+
+/* ---- routing ---- */
+int rd_supports(const rd_sensor_desc* sensor);
+
+/* ---- processor API (resident objects) ----
+ * `cancel` (optional) is a host word polled between stages; non-zero ends the
+ * call with RD_CANCELLED and returns no device state. */
+rd_status rd_develop(rd_ctx* ctx, const uint16_t* mosaic, size_t row_stride, const rd_sensor_desc* sensor,
+                     const rd_detail_desc* detail, const volatile uint32_t* cancel, rd_source** out,
+                     rd_metrics* metrics);
+/* Same, with the mosaic already resident on the device (d_mosaic is a device
+ * pointer of sensor_height*row_stride u16). */
+rd_status rd_develop_device(rd_ctx* ctx, const uint16_t* d_mosaic, size_t row_stride,
+                            const rd_sensor_desc* sensor, const rd_detail_desc* detail,
+                            const volatile uint32_t* cancel, rd_source** out, rd_metrics* metrics);
+rd_status rd_spatial(rd_ctx* ctx, const rd_source* source, const rd_optics_desc* optics, uint32_t target_width,
+                     uint32_t target_height, const float wb_gains[3], const float camera_to_rec2020[9],
+                     rd_base** out, rd_metrics* metrics);
+/* srgb_out: host [h][3w] u8, or NULL. hist: 4*256 u64 (R, G, B, luma) or NULL.
+ * clipped: 6 u64 (shadow r,g,b, highlight r,g,b) or NULL. */
+rd_status rd_render(rd_ctx* ctx, const rd_base* base, const rd_color_desc* color, uint8_t* srgb_out,
+                    uint64_t* hist, uint64_t* clipped, rd_metrics* metrics);
+/* Device-resident render: writes u8 output and histogram into device memory
+ * owned by the base; nothing is copied to the host. */
+rd_status rd_render_device(rd_ctx* ctx, rd_base* base, const rd_color_desc* color, rd_metrics* metrics);
+
+rd_status rd_source_dimensions(const rd_source* source, uint32_t* width, uint32_t* height);
+rd_status rd_source_download(rd_ctx* ctx, const rd_source* source, float* rgb_interleaved);
+rd_status rd_base_dimensions(const rd_base* base, uint32_t* width, uint32_t* height);
+rd_status rd_base_download(rd_ctx* ctx, const rd_base* base, float* rgb_interleaved);
+void rd_source_release(rd_source* source);
+void rd_base_release(rd_base* base);
+
+/* ---- stage entry points (host buffers in and out) ---- */
+/* Normalize + highlight at full crop size. out: crop_h*crop_w f32. stats: 9 u64. */
+rd_status rd_stage_highlight(rd_ctx* ctx, const uint16_t* mosaic, size_t row_stride, const rd_sensor_desc* sensor,
+                             float* out, uint64_t* stats);
+/* Opposed reconstruction of a normalized mosaic (crop-local CFA `cfa`), as
+ * reconstruct_opposed (crates/highlight/src/opposed.rs:63). ceiling may be
+ * NULL. stats: 9 u64 (OpposedStats order). labels (optional): the compact
+ * region label of every 2x2 cell, ceil(w/2)*ceil(h/2) u32. */
+rd_status rd_stage_opposed(rd_ctx* ctx, const float* mosaic, uint32_t width, uint32_t height, int32_t cfa,
+                           const float levels[3], const float* ceiling, float* out, uint64_t* stats,
+                           uint32_t* labels, uint32_t* region_count);
+/* Demosaic a normalized mosaic (crop-local CFA `cfa`). out: interleaved [h][3w]. */
+rd_status rd_stage_demosaic(rd_ctx* ctx, const float* mosaic, uint32_t width, uint32_t height, int32_t cfa,
+                            int32_t algorithm, const float balance[3], float* out);
+rd_status rd_stage_capture(rd_ctx* ctx, float* rgb_interleaved, uint32_t width, uint32_t height,
+                           const rd_detail_desc* detail);
+rd_status rd_stage_optics(rd_ctx* ctx, const rd_optics_desc* optics, const float* rgb_in, float* rgb_out);
+rd_status rd_stage_area_reduce(rd_ctx* ctx, const float* rgb_in, uint32_t width, uint32_t height,
+                               uint32_t target_width, uint32_t target_height, float* rgb_out);
+/* Camera-native RGB -> WB -> matrix -> adjustments -> sRGB8 + histogram. */
+rd_status rd_stage_color(rd_ctx* ctx, const float* rgb_in, uint32_t width, uint32_t height,
+                         const rd_color_desc* color, uint8_t* srgb_out, uint64_t* hist, uint64_t* clipped);
+
+/* ---- host-side contract helpers ---- */
+/* build_plan geometry + automatic scale (crates/optics/src/plan.rs:173-231,521-559)
+ * for a lens given crop factor, real focal length and lens centre offsets. */
+rd_status rd_optics_plan(rd_optics_desc* optics, float crop_factor, float real_focal, float lens_center_x,
+                         float lens_center_y);
+/* BaseRenderingLut::standard_v1 (crates/core/src/rendering.rs:36-50). */
+void rd_standard_base_lut(float* lut4096);
+
+/* ---- synthetic scene generator (seeded, counter-based; identical on CPU and GPU) ---- */
+typedef struct rd_synth_desc {
+  uint32_t width, height;
+  int32_t cfa;
+  uint32_t bits;          /* 12, 14 or 16 */
+  float black;            /* DN */
+  float white;            /* DN */
+  float clip_fraction;    /* target fraction of clipped sites (0..1) */
+  float gains[3];         /* camera channel response (as-shot WB is its inverse) */
+  uint64_t seed;
+  int32_t highlight_blobs; /* 1: clipped regions are Gaussian blobs */
+  float hot_pixel_fraction;
+} rd_synth_desc;
+/* Generate on the device into d_out (height*width u16, row stride = width). */
+rd_status rd_synth_mosaic_device(rd_ctx* ctx, const rd_synth_desc* desc, uint16_t* d_out);
+/* Generate into host memory (runs on the device, then copies). */
+rd_status rd_synth_mosaic(rd_ctx* ctx, const rd_synth_desc* desc, uint16_t* out);
+
+/* ---- measurement ---- */
+/* Record CUDA event `slot` (0..63) on the context stream; elapsed ms between two slots. */
+rd_status rd_ctx_event_record(rd_ctx* ctx, int slot);
+rd_status rd_ctx_event_elapsed(rd_ctx* ctx, int start_slot, int stop_slot, float* ms);
+/* Overwrite a buffer larger than L2 on the context stream (cold-cache timing). */
+rd_status rd_ctx_flush_l2(rd_ctx* ctx);
+/* Per-kernel-family device time: when enabled, every launch of the library is
+ * bracketed by CUDA events; totals are resolved at each call's final sync. */
+rd_status rd_ctx_enable_kernel_timing(rd_ctx* ctx, int enable);
+/* family: index 0..RD_KERNEL_FAMILIES-1; returns its name, total ms and launch count. */
+#define RD_KERNEL_FAMILIES 16
+rd_status rd_ctx_kernel_timing(const rd_ctx* ctx, int family, const char** name, double* total_ms,
+                               uint64_t* launches);
+rd_status rd_ctx_reset_kernel_timing(rd_ctx* ctx);
+
+/* ---- device memory helpers for callers without a CUDA runtime of their own ---- */
+/* Page-locked host memory for fast host<->device copies. */
+rd_status rd_host_alloc(size_t bytes, void** out);
+void rd_host_free(void* ptr);
+rd_status rd_device_alloc(rd_ctx* ctx, size_t bytes, void** out);
+rd_status rd_device_free(rd_ctx* ctx, void* ptr);
+rd_status rd_copy_to_device(rd_ctx* ctx, void* dst, const void* src, size_t bytes);
+rd_status rd_copy_to_host(rd_ctx* ctx, void* dst, const void* src, size_t bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RD_GPU_H */

@@ -172,3 +172,177 @@ def amaze_probe_plane(mosaic: np.ndarray, pattern: int, clip_point: float, plane
 
 
 os.environ.setdefault("OMP_WAIT_POLICY", "PASSIVE")
+
+
+# ---------------------------------------------------------------- stage wrappers
+def sensor_desc(sensor_w, sensor_h, row_stride, crop, pattern, black, black_repeat, white):
+    """Build the oracle's sensor struct; keeps the level arrays alive on the struct."""
+    d = SensorDesc()
+    d.sensor_w, d.sensor_h, d.row_stride = sensor_w, sensor_h, row_stride
+    d.crop_x, d.crop_y, d.crop_w, d.crop_h = crop
+    d.pattern = pattern
+    d.black_w, d.black_h = black_repeat
+    d._black = f32(np.asarray(black))
+    d._white = f32(np.asarray(white))
+    d.black = ptr(d._black)
+    d.white_count = d._white.size
+    d.white = ptr(d._white)
+    return d
+
+
+def normalize(mosaic_u16: np.ndarray, desc: SensorDesc) -> tuple[np.ndarray, int]:
+    mosaic_u16 = np.ascontiguousarray(mosaic_u16, dtype=np.uint16)
+    out = np.zeros((desc.crop_h, desc.crop_w), dtype=np.float32)
+    pattern = load().ro_normalize(ptr(mosaic_u16, ctypes.c_uint16), ctypes.byref(desc), ptr(out))
+    return out, pattern
+
+
+def clip(mosaic: np.ndarray, pattern: int, levels) -> tuple[np.ndarray, np.ndarray]:
+    m = f32(mosaic).copy()
+    h, w = m.shape
+    stats = np.zeros(6, dtype=np.uint64)
+    lv = f32(np.asarray(levels))
+    if load().ro_clip(ptr(m), w, h, pattern, ptr(lv), ptr(stats, ctypes.c_uint64)) != 0:
+        raise ValueError("non-finite sample")
+    return m, stats
+
+
+def opposed(mosaic: np.ndarray, pattern: int, levels, ceiling=None):
+    m = f32(mosaic).copy()
+    h, w = m.shape
+    stats = np.zeros(9, dtype=np.uint64)
+    lv = f32(np.asarray(levels))
+    ce = f32(np.asarray(ceiling)) if ceiling is not None else None
+    labels = np.zeros(((h + 1) // 2, (w + 1) // 2), dtype=np.uint32)
+    count = ctypes.c_uint32()
+    rc = load().ro_opposed(ptr(m), w, h, pattern, ptr(lv), ptr(ce) if ce is not None else None,
+                           ptr(stats, ctypes.c_uint64), ptr(labels, ctypes.c_uint32), ctypes.byref(count))
+    if rc != 0:
+        raise ValueError("non-finite sample")
+    return m, stats, labels, count.value
+
+
+def label_components(grid: np.ndarray) -> tuple[np.ndarray, int]:
+    g = np.ascontiguousarray(grid, dtype=np.uint32).copy()
+    h, w = g.shape
+    count = load().ro_label_components(ptr(g, ctypes.c_uint32), w, h)
+    return g, int(count)
+
+
+def capture(rgb: np.ndarray, amount, radius, noise, ceilings, iterations) -> np.ndarray:
+    out = f32(rgb).copy()
+    h, w3 = out.shape
+    ce = f32(np.asarray(ceilings))
+    if load().ro_capture_sharpen(ptr(out), w3 // 3, h, amount, radius, noise, ptr(ce), iterations) != 0:
+        raise ValueError("capture failed")
+    return out
+
+
+def optics_desc_from(c) -> OpticsDesc:
+    """Copy a product optics descriptor (same field meaning) into the oracle struct."""
+    d = OpticsDesc()
+    d.width, d.height = c.width, c.height
+    d.norm_scale, d.norm_unscale, d.center_x, d.center_y = c.norm_scale, c.norm_unscale, c.center_x, c.center_y
+    d.scale = c.scale
+    d.distortion_model = c.distortion_model
+    d.tca_model = c.tca_model
+    d.vignetting_model = c.vignetting
+    for k in range(3):
+        d.distortion[k] = c.distortion[k]
+        d.tca_red[k] = c.tca_red[k]
+        d.tca_blue[k] = c.tca_blue[k]
+        d.vignetting[k] = c.vignetting_k[k]
+    return d
+
+
+def optics_plan(width, height, distortion_model, distortion, tca_model, tca_red, tca_blue, crop=1.0,
+                focal=35.0, center=(0.0, 0.0)) -> OpticsDesc:
+    d = OpticsDesc()
+    d.width, d.height = width, height
+    d.distortion_model, d.tca_model = distortion_model, tca_model
+    for k in range(3):
+        d.distortion[k] = distortion[k]
+        d.tca_red[k] = tca_red[k]
+        d.tca_blue[k] = tca_blue[k]
+    if load().ro_optics_plan(ctypes.byref(d), crop, focal, center[0], center[1]) != 0:
+        raise ValueError("no safe scale")
+    return d
+
+
+def optics_apply(desc: OpticsDesc, rgb: np.ndarray) -> np.ndarray:
+    rgb = f32(rgb)
+    out = np.zeros_like(rgb)
+    rc = load().ro_optics_apply(ctypes.byref(desc), ptr(rgb), ptr(out))
+    if rc != 0:
+        raise ValueError(f"optics failed: {rc}")
+    return out
+
+
+def area_reduce(rgb: np.ndarray, target) -> np.ndarray:
+    rgb = f32(rgb)
+    h, w3 = rgb.shape
+    out = np.zeros((target[1], 3 * target[0]), dtype=np.float32)
+    if load().ro_area_reduce(ptr(rgb), w3 // 3, h, target[0], target[1], ptr(out)) != 0:
+        raise ValueError("bad reduction")
+    return out
+
+
+def white_balance(rgb: np.ndarray, gains) -> np.ndarray:
+    out = f32(rgb).copy()
+    g = f32(np.asarray(gains))
+    load().ro_white_balance(ptr(out), out.size // 3, ptr(g))
+    return out
+
+
+def camera_matrix(rgb: np.ndarray, m) -> np.ndarray:
+    out = f32(rgb).copy()
+    mm = f32(np.asarray(m)).reshape(-1)
+    load().ro_camera_matrix(ptr(out), out.size // 3, ptr(mm))
+    return out
+
+
+def adjust(rgb: np.ndarray, exposure_ev=0.0, base_lut=None, tone_lut=None, saturation=1.0, vibrance=0.0,
+           hsl=None, grading=None) -> np.ndarray:
+    out = f32(rgb).copy()
+    a = AdjustDesc()
+    a.exposure_ev = exposure_ev
+    keep = []
+    if base_lut is not None:
+        b = f32(base_lut)
+        keep.append(b)
+        a.base_lut = ptr(b)
+    if tone_lut is not None:
+        t = f32(tone_lut)
+        keep.append(t)
+        a.tone_lut = ptr(t)
+    a.saturation, a.vibrance = saturation, vibrance
+    if hsl is not None:
+        a.has_hsl = 1
+        ctypes.memmove(a.hsl, f32(hsl).ctypes.data, 24 * 4)
+    if grading is not None:
+        a.has_grading = 1
+        ctypes.memmove(a.grading, f32(grading).ctypes.data, 9 * 4)
+    load().ro_adjust_apply(ptr(out), out.size // 3, ctypes.byref(a))
+    return out
+
+
+def standard_base_lut() -> np.ndarray:
+    out = np.zeros(4096, dtype=np.float32)
+    load().ro_standard_base_lut(ptr(out))
+    return out
+
+
+def display_srgb8(rgb: np.ndarray) -> np.ndarray:
+    rgb = f32(rgb)
+    out = np.zeros(rgb.shape, dtype=np.uint8)
+    load().ro_display_srgb8(ptr(rgb), rgb.size // 3, ptr(out, ctypes.c_uint8))
+    return out
+
+
+def histogram(rgb8: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    rgb8 = np.ascontiguousarray(rgb8, dtype=np.uint8)
+    hist = np.zeros(1024, dtype=np.uint64)
+    clipped = np.zeros(6, dtype=np.uint64)
+    load().ro_histogram(ptr(rgb8, ctypes.c_uint8), rgb8.size // 3, ptr(hist, ctypes.c_uint64),
+                        ptr(clipped, ctypes.c_uint64))
+    return hist, clipped

@@ -1,0 +1,13 @@
+"""GB300 (sm_103a) sensor-development library: the C ABI in include/rd_gpu.h,
+built from csrc/ into _lib/librd_gpu.so, with a host-side mirror of the
+reference's `rohditor-gpu` processor interface."""
+
+from .processor import (CaptureContract, ColorContract, Device, GpuBase, GpuDevelopedSource, GpuPreviewError,
+                        GpuPreviewProcessor, GpuSensorProcessor, GpuSpatialProcessor, Histogram, OpticsExecution,
+                        SensorDescription, Stages, clip_levels, opposed_levels, standard_base_lut)
+
+__all__ = [
+    "CaptureContract", "ColorContract", "Device", "GpuBase", "GpuDevelopedSource", "GpuPreviewError",
+    "GpuPreviewProcessor", "GpuSensorProcessor", "GpuSpatialProcessor", "Histogram", "OpticsExecution",
+    "SensorDescription", "Stages", "clip_levels", "opposed_levels", "standard_base_lut",
+]

@@ -1,0 +1,1192 @@
+// The C ABI (include/rd_gpu.h): context, processor API, stage entry points and
+// host contract helpers. Everything device-side is ordered on the context's
+// stream; device memory comes from the stream-ordered pool (cudaMallocAsync)
+// and is charged against the context's byte budget before it is taken, like
+// the reference's logical reservations (crates/gpu/src/memory.rs:44-60).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "rd_internal.cuh"
+
+struct rd_ctx {
+  rd::Context c;
+};
+struct rd_source {
+  rd_ctx* ctx;
+  float* rgb;  // planar camera-native RGB
+  int W, H;
+  size_t bytes;
+};
+struct rd_base {
+  rd_ctx* ctx;
+  float* rgb;  // planar linear Rec.2020 RGB
+  int W, H;
+  size_t bytes;
+  uint8_t* d_srgb;             // device output of rd_render_device
+  unsigned long long* d_hist;  // 1024 bins
+  size_t out_bytes;
+};
+
+namespace rd {
+
+Status run_amaze(Context& ctx, const MosaicSource& src, const float gains[3], float clip_point, float* rgb,
+                 int count_clip, unsigned long long* clip_stats);
+
+Status reserve(Context& ctx, size_t bytes) {
+  if (ctx.budget && ctx.reserved + bytes > ctx.budget)
+    return Status{RD_OVER_BUDGET, "device working set of " + std::to_string(ctx.reserved + bytes) +
+                                      " bytes exceeds the budget of " + std::to_string(ctx.budget)};
+  ctx.reserved += bytes;
+  return Status{};
+}
+void release(Context& ctx, size_t bytes) { ctx.reserved -= std::min<uint64_t>(bytes, ctx.reserved); }
+
+Status device_alloc(Context& ctx, size_t bytes, void** out) {
+  *out = nullptr;
+  if (bytes == 0) bytes = 16;
+  RD_TRY(reserve(ctx, bytes));
+  const cudaError_t e = cudaMallocAsync(out, bytes, ctx.stream);
+  if (e != cudaSuccess) {
+    release(ctx, bytes);
+    cudaGetLastError();
+    return Status{RD_OVER_BUDGET, std::string("device allocation failed: ") + cudaGetErrorString(e)};
+  }
+  return Status{};
+}
+void device_free(Context& ctx, void* ptr, size_t bytes) {
+  if (!ptr) return;
+  cudaFreeAsync(ptr, ctx.stream);
+  release(ctx, bytes == 0 ? 16 : bytes);
+}
+
+const char* kernel_family_name(int family) {
+  static const char* names[K_FAMILY_COUNT] = {
+      "normalize", "opposed", "mhc_bilinear", "rcd", "amaze", "rl_init", "rl_mask", "rl_iteration",
+      "rl_apply", "vignetting", "optics_gather", "area_horizontal", "area_vertical", "wb_matrix",
+      "color_output", "synth"};
+  return family >= 0 && family < K_FAMILY_COUNT ? names[family] : "unknown";
+}
+
+LaunchScope::LaunchScope(Context& c, int f) : ctx(c), family(f) {
+  ctx.launches++;
+  ctx.family_launches[f]++;
+  if (!ctx.timing) return;
+  auto take = [&]() {
+    cudaEvent_t e = nullptr;
+    if (!ctx.event_pool.empty()) {
+      e = ctx.event_pool.back();
+      ctx.event_pool.pop_back();
+    } else {
+      cudaEventCreate(&e);
+    }
+    return e;
+  };
+  a = take();
+  b = take();
+  cudaEventRecord(a, ctx.stream);
+}
+
+LaunchScope::~LaunchScope() {
+  if (!a) return;
+  cudaEventRecord(b, ctx.stream);
+  ctx.pending.push_back({family, {a, b}});
+}
+
+void resolve_kernel_timing(Context& ctx) {
+  for (auto& p : ctx.pending) {
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, p.second.first, p.second.second) == cudaSuccess) ctx.family_ms[p.first] += ms;
+    ctx.event_pool.push_back(p.second.first);
+    ctx.event_pool.push_back(p.second.second);
+  }
+  ctx.pending.clear();
+  cudaGetLastError();
+}
+
+// Reads and clears the kernels' error word; one synchronization point per call.
+Status check_kernel_error(Context& ctx, const char* stage) {
+  uint32_t word = 0;
+  RD_CUDA_TRY(cudaMemcpyAsync(&word, ctx.d_error, sizeof(word), cudaMemcpyDeviceToHost, ctx.stream));
+  RD_CUDA_TRY(cudaStreamSynchronize(ctx.stream));
+  if (!ctx.pending.empty()) resolve_kernel_timing(ctx);
+  if (word) {
+    RD_CUDA_TRY(cudaMemsetAsync(ctx.d_error, 0, sizeof(uint32_t), ctx.stream));
+    std::string what;
+    if (word & 1u) what += " non-finite demosaic output;";
+    if (word & 2u) what += " non-finite capture input;";
+    if (word & 4u) what += " invalid vignetting gain;";
+    if (word & 8u) what += " optics footprint outside the image or non-finite coordinate;";
+    if (word & 16u) what += " highlight reconstruction failed;";
+    return Status{RD_INVALID_INPUT, std::string(stage) + ":" + what};
+  }
+  return Status{};
+}
+
+// ------------------------------------------------------------- host contracts
+static void validate_sensor(const rd_sensor_desc& s, Status& st) {
+  auto bad = [&](const char* why) {
+    if (st.ok()) st = Status{RD_INVALID_INPUT, why};
+  };
+  if (s.sensor_width < 2 || s.sensor_height < 2) bad("sensor must be at least 2x2");
+  if (s.crop_width < 2 || s.crop_height < 2) bad("crop must be at least 2x2");
+  if ((uint64_t)s.crop_x + s.crop_width > s.sensor_width || (uint64_t)s.crop_y + s.crop_height > s.sensor_height)
+    bad("crop lies outside the sensor");
+  if (s.cfa < 0 || s.cfa > 3) bad("unknown CFA pattern");
+  const uint64_t n = (uint64_t)s.black_repeat_w * s.black_repeat_h;
+  if (n == 0 || n > RD_MAX_LEVEL_PATTERN) bad("black repeat pattern must hold 1..64 values");
+  if (!(s.white_count == 1 || s.white_count == 3 || s.white_count == n)) bad("white levels must be 1, 3 or per pattern");
+  for (uint64_t k = 0; k < n && k < RD_MAX_LEVEL_PATTERN; ++k)
+    if (!std::isfinite(s.black[k])) bad("black levels must be finite");
+  for (uint32_t k = 0; k < s.white_count && k < RD_MAX_LEVEL_PATTERN; ++k)
+    if (!std::isfinite(s.white[k])) bad("white levels must be finite");
+  if (st.ok()) {
+    // validate_levels (sensor.rs:532-561): white must exceed black over the pattern.
+    for (uint32_t y = 0; y < s.black_repeat_h; ++y)
+      for (uint32_t x = 0; x < s.black_repeat_w; ++x) {
+        const uint32_t i = y * s.black_repeat_w + x;
+        const float black = s.black[i];
+        const float white = s.white_count == 1 ? s.white[0]
+                            : s.white_count == 3 ? s.white[color_at(s.cfa, (int)x, (int)y)]
+                                                 : s.white[i];
+        if (!(white > black)) bad("white level must exceed black level");
+      }
+  }
+  if (s.highlight < 0 || s.highlight > 2) bad("unknown highlight method");
+  const float* lv = s.highlight == RD_HIGHLIGHT_CLIP ? s.clip_levels : s.detection_levels;
+  if (s.highlight != RD_HIGHLIGHT_OFF)
+    for (int c = 0; c < 3; ++c)
+      if (!std::isfinite(lv[c]) || !(lv[c] > 0.0f)) bad("highlight levels must be finite and positive");
+  if (s.highlight == RD_HIGHLIGHT_OPPOSED && s.has_neutral_ceiling)
+    for (int c = 0; c < 3; ++c)
+      if (!std::isfinite(s.neutral_ceiling[c]) || !(s.neutral_ceiling[c] > 0.0f))
+        bad("neutral ceiling must be finite and positive");
+  if (s.demosaic < 0 || s.demosaic > 3) bad("unknown demosaic algorithm");
+  for (int c = 0; c < 3; ++c)
+    if (!std::isfinite(s.demosaic_balance[c]) || !(s.demosaic_balance[c] > 0.0f))
+      bad("demosaic balance must be finite and positive");
+}
+
+static MosaicSource make_source(const rd_sensor_desc& s, const uint16_t* d_raw, size_t row_stride) {
+  MosaicSource m{};
+  m.raw = d_raw;
+  m.f32 = nullptr;
+  m.row_stride = (long long)row_stride;
+  m.crop_x = (int)s.crop_x;
+  m.crop_y = (int)s.crop_y;
+  m.sensor_cfa = s.cfa;
+  m.width = (int)s.crop_width;
+  m.height = (int)s.crop_height;
+  m.cfa = shifted_cfa(s.cfa, (int)s.crop_x, (int)s.crop_y);
+  m.black_w = (int)s.black_repeat_w;
+  m.black_h = (int)s.black_repeat_h;
+  m.white_count = (int)s.white_count;
+  m.clip = s.highlight == RD_HIGHLIGHT_CLIP ? 1 : 0;
+  for (int c = 0; c < 3; ++c) {
+    m.clip_levels[c] = s.clip_levels[c];
+    m.fwd[c] = s.demosaic_balance[c];  // run_demosaic normalizes it
+  }
+  for (int k = 0; k < RD_MAX_LEVEL_PATTERN; ++k) {
+    m.black[k] = s.black[k];
+    m.white[k] = s.white[k];
+  }
+  return m;
+}
+
+// build_plan (crates/optics/src/plan.rs:173-231) and find_scale (:521-559).
+namespace {
+bool map_coords(const rd_optics_desc& p, double x, double y, float scale, float out[6]);
+}
+
+Status optics_plan(rd_optics_desc& p, float crop, float real_focal, float lens_cx, float lens_cy) {
+  if (p.width < 4 || p.height < 4) return Status{RD_INVALID_DIMENSIONS, "optics needs at least 4x4 pixels"};
+  if (!(crop > 0.0f) || !std::isfinite(crop) || !(real_focal > 0.0f) || !std::isfinite(real_focal))
+    return Status{RD_INVALID_INPUT, "crop factor and focal length must be finite and positive"};
+  const double wf = p.width >= 2 ? (double)(p.width - 1) : 1.0;
+  const double hf = p.height >= 2 ? (double)(p.height - 1) : 1.0;
+  p.norm_scale = std::hypot(36.0, 24.0) / (double)crop / std::hypot(wf + 1.0, hf + 1.0) / (double)real_focal;
+  p.norm_unscale = 1.0 / p.norm_scale;
+  const double lens_size = std::min(wf, hf);
+  p.center_x = (wf / 2.0 + lens_size / 2.0 * (double)lens_cx) * p.norm_scale;
+  p.center_y = (hf / 2.0 + lens_size / 2.0 * (double)lens_cy) * p.norm_scale;
+  p.scale = 1.0f;
+  if (p.distortion_model == RD_DISTORTION_NONE && p.tca_model == RD_TCA_NONE) return Status{};
+  float scale = 1.0f;
+  for (int i = 0; i < 160; ++i) {
+    bool safe = true;
+    const int max_x = (int)p.width - 1, max_y = (int)p.height - 1;
+    for (int index = 0; index < 64 && safe; ++index) {
+      const float t = (float)index / 63.0f;
+      const float pts[4][2] = {{t * (float)max_x, 0.0f},
+                               {t * (float)max_x, (float)max_y},
+                               {0.0f, t * (float)max_y},
+                               {(float)max_x, t * (float)max_y}};
+      for (auto& pt : pts) {
+        float c[6];
+        if (!map_coords(p, (double)(size_t)pt[0], (double)(size_t)pt[1], scale, c)) {
+          safe = false;
+          break;
+        }
+        for (int k = 0; k < 3; ++k)
+          if (!(c[2 * k] >= 1.0f && c[2 * k + 1] >= 1.0f && c[2 * k] <= (float)(p.width - 2) &&
+                c[2 * k + 1] <= (float)(p.height - 2)))
+            safe = false;
+        if (!safe) break;
+      }
+    }
+    if (safe) {
+      p.scale = scale;
+      return Status{};
+    }
+    scale *= 1.025f;
+  }
+  return Status{RD_INVALID_INPUT, "no automatic scale keeps the cubic footprint inside the image"};
+}
+
+namespace {
+constexpr double NEWTON_EPS = 0.00001;
+void undist(const rd_optics_desc& p, float x, float y, float* ox, float* oy) {
+  *ox = x;
+  *oy = y;
+  if (p.distortion_model == RD_DISTORTION_NONE) return;
+  const double rd = std::sqrt((double)(x * x + y * y));
+  if (rd == 0.0) return;
+  const double a = p.distortion[0], b = p.distortion[1], c = p.distortion[2];
+  double ru = rd;
+  bool converged = false;
+  if (p.distortion_model == RD_DISTORTION_POLY3) {
+    const double inv_k1 = (double)(1.0f / p.distortion[0]);
+    const double rd_div_k1 = (double)(float)(rd * inv_k1);
+    for (int s = 0; s < 7; ++s) {
+      const double f = ru * ru * ru + ru * inv_k1 - rd_div_k1;
+      if (std::fabs(f) < NEWTON_EPS) { converged = true; break; }
+      ru -= f / (3.0 * ru * ru + inv_k1);
+    }
+    if (!converged || ru < 0.0) { *ox = NAN; *oy = NAN; return; }
+  } else if (p.distortion_model == RD_DISTORTION_POLY5) {
+    for (int s = 0; s < 7; ++s) {
+      const double ru2 = ru * ru;
+      const double f = ru * (1.0 + a * ru2 + b * ru2 * ru2) - rd;
+      if (std::fabs(f) < NEWTON_EPS) { converged = true; break; }
+      ru -= f / (1.0 + 3.0 * a * ru2 + 5.0 * b * ru2 * ru2);
+    }
+    if (!converged || ru < 0.0) return;
+  } else {
+    for (int s = 0; s < 7; ++s) {
+      const double f = ru * (a * ru * ru * ru + b * ru * ru + c * ru + 1.0) - rd;
+      if (std::fabs(f) < NEWTON_EPS) { converged = true; break; }
+      ru -= f / (4.0 * a * ru * ru * ru + 3.0 * b * ru * ru + 2.0 * c * ru + 1.0);
+    }
+    if (!converged || ru < 0.0) return;
+  }
+  const double ratio = ru / rd;
+  *ox = (float)((double)x * ratio);
+  *oy = (float)((double)y * ratio);
+}
+void tca3(const float* ch, float x, float y, float* ox, float* oy) {
+  *ox = x;
+  *oy = y;
+  const double rd = std::sqrt((double)(x * x + y * y));
+  if (rd == 0.0) return;
+  const double v = ch[0], c = ch[1], b = ch[2];
+  double ru = rd;
+  bool converged = false;
+  for (int s = 0; s < 7; ++s) {
+    const double ru2 = ru * ru;
+    const double f = b * ru2 * ru + c * ru2 + v * ru - rd;
+    if (std::fabs(f) < NEWTON_EPS) { converged = true; break; }
+    ru -= f / (3.0 * b * ru2 + 2.0 * c * ru + v);
+  }
+  if (!converged || ru <= 0.0) return;
+  const double ratio = ru / rd;
+  *ox = (float)((double)x * ratio);
+  *oy = (float)((double)y * ratio);
+}
+bool map_coords(const rd_optics_desc& p, double x, double y, float scale, float out[6]) {
+  const double cpx = p.center_x * p.norm_unscale, cpy = p.center_y * p.norm_unscale;
+  const double mx = cpx + (x - cpx) / (double)scale, my = cpy + (y - cpy) / (double)scale;
+  const double ix = mx * p.norm_scale - p.center_x, iy = my * p.norm_scale - p.center_y;
+  float gx, gy;
+  undist(p, (float)ix, (float)iy, &gx, &gy);
+  if (!std::isfinite(gx) || !std::isfinite(gy)) return false;
+  float n[6] = {gx, gy, gx, gy, gx, gy};
+  if (p.tca_model == RD_TCA_LINEAR) {
+    n[0] = gx * p.tca_red[0];
+    n[1] = gy * p.tca_red[0];
+    n[4] = gx * p.tca_blue[0];
+    n[5] = gy * p.tca_blue[0];
+  } else if (p.tca_model == RD_TCA_POLY3) {
+    tca3(p.tca_red, gx, gy, &n[0], &n[1]);
+    tca3(p.tca_blue, gx, gy, &n[4], &n[5]);
+  }
+  for (int c = 0; c < 3; ++c) {
+    out[2 * c] = (float)(((double)n[2 * c] + p.center_x) * p.norm_unscale);
+    out[2 * c + 1] = (float)(((double)n[2 * c + 1] + p.center_y) * p.norm_unscale);
+    if (!std::isfinite(out[2 * c]) || !std::isfinite(out[2 * c + 1])) return false;
+  }
+  return true;
+}
+}  // namespace
+
+// BaseRenderingLut::standard_v1 (crates/core/src/rendering.rs:36-50, 223-234).
+void standard_base_lut(float* lut) {
+  const float anchor = std::pow(0.18f, 1.45f - 1.0f) * (1.0f - 0.18f);
+  for (int i = 0; i < 4096; ++i) {
+    if (i == 4095) {
+      lut[i] = 1.0f;
+      continue;
+    }
+    const float coordinate = (float)i / 4095.0f;
+    const float input = coordinate / (1.0f - coordinate);
+    if (input == 0.0f) {
+      lut[i] = 0.0f;
+      continue;
+    }
+    const float numerator = std::pow(input, 1.45f);
+    lut[i] = numerator / (numerator + anchor);
+  }
+}
+
+}  // namespace rd
+
+using rd::Status;
+
+namespace {
+
+rd_status finish(rd_ctx* ctx, const Status& st) {
+  if (ctx) ctx->c.last_error = st.message;
+  return st.code;
+}
+
+struct Timer {
+  rd::Context& c;
+  int n = 0;
+  explicit Timer(rd::Context& ctx) : c(ctx) {}
+  void mark() {
+    if (n < 8) cudaEventRecord(c.ev[n++], c.stream);
+  }
+  float span(int a, int b) const {
+    float ms = 0.0f;
+    if (a < n && b < n) cudaEventElapsedTime(&ms, c.ev[a], c.ev[b]);
+    return ms;
+  }
+};
+
+// Sensor development on a resident mosaic: normalize + highlight + demosaic,
+// then capture sharpening. Returns a new rd_source.
+Status develop_impl(rd_ctx* h, const uint16_t* d_raw, size_t row_stride, const rd_sensor_desc& s,
+                    const rd_detail_desc* detail, const volatile uint32_t* cancel, rd_source** out,
+                    rd_metrics* metrics) {
+  rd::Context& ctx = h->c;
+  Status st;
+  validate_sensor(s, st);
+  if (!st.ok()) return st;
+  if (row_stride < s.sensor_width) return Status{RD_INVALID_DIMENSIONS, "row stride is shorter than the sensor width"};
+  if (cancel && *cancel) return Status{RD_CANCELLED, "cancelled"};
+  const int W = (int)s.crop_width, H = (int)s.crop_height;
+  const long long plane = (long long)W * H;
+  rd::MosaicSource src = rd::make_source(s, d_raw, row_stride);
+  Timer tm(ctx);
+  tm.mark();
+  unsigned long long* d_stats = nullptr;
+  void* p = nullptr;
+  RD_TRY(rd::device_alloc(ctx, sizeof(unsigned long long) * 16, &p));
+  d_stats = static_cast<unsigned long long*>(p);
+  RD_CUDA_TRY(cudaMemsetAsync(d_stats, 0, sizeof(unsigned long long) * 16, ctx.stream));
+  float* d_mosaic = nullptr;
+  const size_t mosaic_bytes = sizeof(float) * (size_t)plane;
+  if (s.highlight == RD_HIGHLIGHT_OPPOSED) {
+    st = rd::device_alloc(ctx, mosaic_bytes, &p);
+    if (st.ok()) {
+      d_mosaic = static_cast<float*>(p);
+      rd::MosaicSource norm = src;
+      norm.clip = 0;
+      st = rd::launch_normalize(ctx, norm, d_mosaic, nullptr);
+    }
+    if (st.ok())
+      st = rd::run_opposed(ctx, d_mosaic, W, H, src.cfa, s.detection_levels,
+                           s.has_neutral_ceiling ? s.neutral_ceiling : nullptr, d_stats, nullptr);
+    src.f32 = d_mosaic;
+    src.clip = 0;
+  }
+  tm.mark();
+  rd_source* result = nullptr;
+  if (st.ok() && cancel && *cancel) st = Status{RD_CANCELLED, "cancelled"};
+  if (st.ok()) {
+    result = new (std::nothrow) rd_source{h, nullptr, W, H, sizeof(float) * 3 * (size_t)plane};
+    if (!result) st = Status{RD_OVER_BUDGET, "host allocation failed"};
+  }
+  if (st.ok()) {
+    st = rd::device_alloc(ctx, result->bytes, &p);
+    if (st.ok()) result->rgb = static_cast<float*>(p);
+  }
+  if (st.ok()) st = rd::run_demosaic(ctx, src, s.demosaic, result->rgb, d_stats);
+  tm.mark();
+  if (st.ok() && cancel && *cancel) st = Status{RD_CANCELLED, "cancelled"};
+  if (st.ok() && detail) st = rd::run_capture(ctx, result->rgb, W, H, *detail, nullptr);
+  tm.mark();
+  if (d_mosaic) rd::device_free(ctx, d_mosaic, mosaic_bytes);
+  uint64_t host_stats[16] = {};
+  if (st.ok()) {
+    const cudaError_t e = cudaMemcpyAsync(host_stats, d_stats, sizeof(host_stats), cudaMemcpyDeviceToHost, ctx.stream);
+    if (e != cudaSuccess) st = Status{RD_READBACK, cudaGetErrorString(e)};
+  }
+  rd::device_free(ctx, d_stats, sizeof(unsigned long long) * 16);
+  if (st.ok()) st = rd::check_kernel_error(ctx, "develop");
+  if (st.ok() && cancel && *cancel) st = Status{RD_CANCELLED, "cancelled"};
+  if (!st.ok()) {
+    if (result) {
+      if (result->rgb) rd::device_free(ctx, result->rgb, result->bytes);
+      delete result;
+    }
+    cudaStreamSynchronize(ctx.stream);
+    return st;
+  }
+  if (metrics) {
+    metrics->normalize_highlight_ms = tm.span(0, 1);
+    metrics->demosaic_ms = tm.span(1, 2);
+    metrics->capture_ms = tm.span(2, 3);
+    metrics->total_ms = tm.span(0, 3);
+    for (int k = 0; k < 9; ++k) metrics->highlight_stats[k] = host_stats[k];
+    metrics->kernel_launches = ctx.launches;
+    metrics->device_bytes = ctx.reserved;
+  }
+  *out = result;
+  return Status{};
+}
+
+}  // namespace
+
+extern "C" {
+
+int rd_status_is_routing(rd_status status) {
+  return status == RD_UNSUPPORTED_EDITS || status == RD_OVER_BUDGET;
+}
+
+const char* rd_status_name(rd_status status) {
+  switch (status) {
+    case RD_OK: return "Ok";
+    case RD_CANCELLED: return "Cancelled";
+    case RD_UNSUPPORTED: return "Unsupported";
+    case RD_OVER_BUDGET: return "OverBudget";
+    case RD_INVALID_DIMENSIONS: return "InvalidDimensions";
+    case RD_BASE_MISMATCH: return "BaseMismatch";
+    case RD_UNSUPPORTED_EDITS: return "UnsupportedEdits";
+    case RD_SYNCHRONIZATION: return "Synchronization";
+    case RD_INVALID_INPUT: return "InvalidInput";
+    case RD_READBACK: return "Readback";
+  }
+  return "Unknown";
+}
+
+rd_status rd_ctx_create(int device, uint64_t budget_bytes, rd_ctx** out) {
+  if (!out) return RD_INVALID_INPUT;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
+    cudaGetLastError();
+    return RD_UNSUPPORTED;
+  }
+  if (cudaSetDevice(device) != cudaSuccess) return RD_SYNCHRONIZATION;
+  rd_ctx* h = new (std::nothrow) rd_ctx();
+  if (!h) return RD_OVER_BUDGET;
+  rd::Context& c = h->c;
+  c.device = device;
+  c.budget = budget_bytes;
+  cudaDeviceGetAttribute(&c.sm_count, cudaDevAttrMultiProcessorCount, device);
+  if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete h;
+    return RD_SYNCHRONIZATION;
+  }
+  for (auto& e : c.ev) cudaEventCreate(&e);
+  if (cudaMalloc(&c.d_error, sizeof(uint32_t)) != cudaSuccess ||
+      cudaMemsetAsync(c.d_error, 0, sizeof(uint32_t), c.stream) != cudaSuccess) {
+    cudaStreamDestroy(c.stream);
+    delete h;
+    return RD_SYNCHRONIZATION;
+  }
+  // Keep freed pool memory cached between calls instead of returning it to the driver.
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t threshold = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+  }
+  cudaStreamSynchronize(c.stream);
+  *out = h;
+  return RD_OK;
+}
+
+void rd_ctx_destroy(rd_ctx* h) {
+  if (!h) return;
+  rd::Context& c = h->c;
+  cudaSetDevice(c.device);
+  if (c.amaze_scratch) rd::device_free(c, c.amaze_scratch, 0);
+  if (c.flush_buf) rd::device_free(c, c.flush_buf, c.flush_bytes);
+  cudaStreamSynchronize(c.stream);
+  rd::resolve_kernel_timing(c);
+  for (auto e : c.event_pool) cudaEventDestroy(e);
+  for (auto& e : c.user_ev)
+    if (e) cudaEventDestroy(e);
+  cudaFree(c.d_error);
+  for (auto& e : c.ev) cudaEventDestroy(e);
+  cudaStreamDestroy(c.stream);
+  delete h;
+}
+
+rd_status rd_ctx_set_budget(rd_ctx* h, uint64_t budget_bytes) {
+  if (!h) return RD_INVALID_INPUT;
+  h->c.budget = budget_bytes;
+  return RD_OK;
+}
+
+const char* rd_ctx_last_error(const rd_ctx* h) { return h ? h->c.last_error.c_str() : "no context"; }
+
+rd_status rd_ctx_synchronize(rd_ctx* h) {
+  if (!h) return RD_INVALID_INPUT;
+  return cudaStreamSynchronize(h->c.stream) == cudaSuccess ? RD_OK : RD_SYNCHRONIZATION;
+}
+
+uint64_t rd_ctx_kernel_launches(const rd_ctx* h) { return h ? h->c.launches : 0; }
+
+int rd_supports(const rd_sensor_desc* s) {
+  if (!s) return 0;
+  Status st;
+  rd::validate_sensor(*s, st);
+  return st.ok() ? 1 : 0;
+}
+
+rd_status rd_develop(rd_ctx* h, const uint16_t* mosaic, size_t row_stride, const rd_sensor_desc* sensor,
+                     const rd_detail_desc* detail, const volatile uint32_t* cancel, rd_source** out,
+                     rd_metrics* metrics) {
+  if (!h || !mosaic || !sensor || !out) return finish(h, Status{RD_INVALID_INPUT, "null argument"});
+  *out = nullptr;
+  rd::Context& ctx = h->c;
+  cudaSetDevice(ctx.device);
+  const size_t bytes = sizeof(uint16_t) * row_stride * sensor->sensor_height;
+  void* p = nullptr;
+  Status st = rd::device_alloc(ctx, bytes, &p);
+  if (!st.ok()) return finish(h, st);
+  if (cudaMemcpyAsync(p, mosaic, bytes, cudaMemcpyHostToDevice, ctx.stream) != cudaSuccess)
+    st = Status{RD_SYNCHRONIZATION, "mosaic upload failed"};
+  if (st.ok()) st = develop_impl(h, static_cast<const uint16_t*>(p), row_stride, *sensor, detail, cancel, out, metrics);
+  rd::device_free(ctx, p, bytes);
+  return finish(h, st);
+}
+
+rd_status rd_develop_device(rd_ctx* h, const uint16_t* d_mosaic, size_t row_stride, const rd_sensor_desc* sensor,
+                            const rd_detail_desc* detail, const volatile uint32_t* cancel, rd_source** out,
+                            rd_metrics* metrics) {
+  if (!h || !d_mosaic || !sensor || !out) return finish(h, Status{RD_INVALID_INPUT, "null argument"});
+  *out = nullptr;
+  cudaSetDevice(h->c.device);
+  return finish(h, develop_impl(h, d_mosaic, row_stride, *sensor, detail, cancel, out, metrics));
+}
+
+rd_status rd_spatial(rd_ctx* h, const rd_source* source, const rd_optics_desc* optics, uint32_t tw, uint32_t th,
+                     const float wb_gains[3], const float cam[9], rd_base** out, rd_metrics* metrics) {
+  if (!h || !source || !out || !wb_gains || !cam) return finish(h, Status{RD_INVALID_INPUT, "null argument"});
+  *out = nullptr;
+  rd::Context& ctx = h->c;
+  cudaSetDevice(ctx.device);
+  const int W = source->W, H = source->H;
+  if (tw == 0 || th == 0 || (int)tw > W || (int)th > H)
+    return finish(h, Status{RD_INVALID_DIMENSIONS, "area reduction cannot upscale or produce an empty image"});
+  if (optics && ((int)optics->width != W || (int)optics->height != H))
+    return finish(h, Status{RD_BASE_MISMATCH, "optics execution was resolved for another image size"});
+  for (int c = 0; c < 3; ++c)
+    if (!std::isfinite(wb_gains[c]) || !(wb_gains[c] > 0.0f))
+      return finish(h, Status{RD_INVALID_INPUT, "white-balance gains must be finite and positive"});
+  const long long plane = (long long)W * H;
+  Timer tm(ctx);
+  tm.mark();
+  Status st;
+  const bool vig = optics && optics->vignetting == 1;
+  const bool warp = optics && (optics->distortion_model != RD_DISTORTION_NONE || optics->tca_model != RD_TCA_NONE);
+  void* p = nullptr;
+  float* mult = nullptr;
+  float* warped = nullptr;
+  if (vig) {
+    st = rd::device_alloc(ctx, sizeof(float) * plane, &p);
+    if (st.ok()) {
+      mult = static_cast<float*>(p);
+      st = rd::run_vignette_plane(ctx, *optics, mult);
+    }
+  }
+  const float* reduce_in = source->rgb;
+  const float* reduce_mult = mult;
+  if (st.ok() && warp) {
+    st = rd::device_alloc(ctx, sizeof(float) * 3 * plane, &p);
+    if (st.ok()) {
+      warped = static_cast<float*>(p);
+      st = rd::run_optics_gather(ctx, *optics, source->rgb, mult, warped);
+      reduce_in = warped;
+      reduce_mult = nullptr;
+    }
+  }
+  tm.mark();
+  rd_base* base = nullptr;
+  if (st.ok()) {
+    base = new (std::nothrow) rd_base{h, nullptr, (int)tw, (int)th, sizeof(float) * 3 * (size_t)tw * th, nullptr, nullptr, 0};
+    if (!base) st = Status{RD_OVER_BUDGET, "host allocation failed"};
+  }
+  if (st.ok()) {
+    st = rd::device_alloc(ctx, base->bytes, &p);
+    if (st.ok()) base->rgb = static_cast<float*>(p);
+  }
+  if (st.ok()) {
+    if ((int)tw == W && (int)th == H && !reduce_mult) {
+      if (cudaMemcpyAsync(base->rgb, reduce_in, base->bytes, cudaMemcpyDeviceToDevice, ctx.stream) != cudaSuccess)
+        st = Status{RD_SYNCHRONIZATION, "copy failed"};
+    } else {
+      const size_t mid_bytes = sizeof(float) * rd::area_reduce_scratch_floats(W, H, (int)tw, (int)th);
+      st = rd::device_alloc(ctx, mid_bytes, &p);
+      if (st.ok()) {
+        st = rd::run_area_reduce(ctx, reduce_in, reduce_mult, W, H, (int)tw, (int)th, base->rgb, static_cast<float*>(p));
+        rd::device_free(ctx, p, mid_bytes);
+      }
+    }
+  }
+  tm.mark();
+  if (st.ok()) st = rd::run_wb_matrix(ctx, base->rgb, (size_t)tw * th, wb_gains, cam);
+  tm.mark();
+  if (mult) rd::device_free(ctx, mult, sizeof(float) * plane);
+  if (warped) rd::device_free(ctx, warped, sizeof(float) * 3 * plane);
+  if (st.ok()) st = rd::check_kernel_error(ctx, "spatial");
+  if (!st.ok()) {
+    if (base) {
+      if (base->rgb) rd::device_free(ctx, base->rgb, base->bytes);
+      delete base;
+    }
+    cudaStreamSynchronize(ctx.stream);
+    return finish(h, st);
+  }
+  if (metrics) {
+    metrics->optics_ms = tm.span(0, 1);
+    metrics->reduce_ms = tm.span(1, 2);
+    metrics->color_ms = tm.span(2, 3);
+    metrics->total_ms = tm.span(0, 3);
+    metrics->kernel_launches = ctx.launches;
+    metrics->device_bytes = ctx.reserved;
+  }
+  *out = base;
+  return finish(h, Status{});
+}
+
+static Status ensure_outputs(rd_base* base) {
+  rd::Context& ctx = base->ctx->c;
+  if (base->d_srgb) return Status{};
+  base->out_bytes = (size_t)3 * base->W * base->H + 1024 * sizeof(unsigned long long) + 16;
+  void* p = nullptr;
+  RD_TRY(rd::device_alloc(ctx, base->out_bytes, &p));
+  base->d_hist = static_cast<unsigned long long*>(p);
+  base->d_srgb = reinterpret_cast<uint8_t*>(base->d_hist + 1024);
+  return Status{};
+}
+
+rd_status rd_render_device(rd_ctx* h, rd_base* base, const rd_color_desc* color, rd_metrics* metrics) {
+  if (!h || !base || !color) return finish(h, Status{RD_INVALID_INPUT, "null argument"});
+  if (base->ctx != h) return finish(h, Status{RD_BASE_MISMATCH, "base belongs to another context"});
+  rd::Context& ctx = h->c;
+  cudaSetDevice(ctx.device);
+  Status st = ensure_outputs(base);
+  if (!st.ok()) return finish(h, st);
+  Timer tm(ctx);
+  tm.mark();
+  if (cudaMemsetAsync(base->d_hist, 0, 1024 * sizeof(unsigned long long), ctx.stream) != cudaSuccess)
+    return finish(h, Status{RD_SYNCHRONIZATION, "memset failed"});
+  st = rd::run_color_output(ctx, base->rgb, base->W, base->H, *color, false, base->d_srgb, base->d_hist);
+  tm.mark();
+  if (st.ok()) st = rd::check_kernel_error(ctx, "render");
+  if (st.ok() && metrics) {
+    metrics->color_ms = tm.span(0, 1);
+    metrics->total_ms = metrics->color_ms;
+    metrics->kernel_launches = ctx.launches;
+  }
+  return finish(h, st);
+}
+
+rd_status rd_render(rd_ctx* h, const rd_base* cbase, const rd_color_desc* color, uint8_t* srgb_out, uint64_t* hist,
+                    uint64_t* clipped, rd_metrics* metrics) {
+  rd_base* base = const_cast<rd_base*>(cbase);
+  rd_status s = rd_render_device(h, base, color, metrics);
+  if (s != RD_OK) return s;
+  rd::Context& ctx = h->c;
+  uint64_t bins[1024];
+  Status st;
+  if (srgb_out &&
+      cudaMemcpyAsync(srgb_out, base->d_srgb, (size_t)3 * base->W * base->H, cudaMemcpyDeviceToHost, ctx.stream) !=
+          cudaSuccess)
+    st = Status{RD_READBACK, "output readback failed"};
+  if (st.ok() && cudaMemcpyAsync(bins, base->d_hist, sizeof(bins), cudaMemcpyDeviceToHost, ctx.stream) != cudaSuccess)
+    st = Status{RD_READBACK, "histogram readback failed"};
+  if (st.ok() && cudaStreamSynchronize(ctx.stream) != cudaSuccess) st = Status{RD_READBACK, "readback failed"};
+  if (st.ok()) {
+    if (hist) std::memcpy(hist, bins, sizeof(bins));
+    // Histogram::count_clipped (histogram.rs:110-121): bins 0 and 255.
+    if (clipped)
+      for (int c = 0; c < 3; ++c) {
+        clipped[c] = bins[256 * c];
+        clipped[3 + c] = bins[256 * c + 255];
+      }
+  }
+  return finish(h, st);
+}
+
+rd_status rd_source_dimensions(const rd_source* s, uint32_t* w, uint32_t* hgt) {
+  if (!s || !w || !hgt) return RD_INVALID_INPUT;
+  *w = (uint32_t)s->W;
+  *hgt = (uint32_t)s->H;
+  return RD_OK;
+}
+rd_status rd_base_dimensions(const rd_base* b, uint32_t* w, uint32_t* hgt) {
+  if (!b || !w || !hgt) return RD_INVALID_INPUT;
+  *w = (uint32_t)b->W;
+  *hgt = (uint32_t)b->H;
+  return RD_OK;
+}
+
+static rd_status download_planar(rd_ctx* h, const float* d, int W, int H, float* out) {
+  rd::Context& ctx = h->c;
+  const size_t plane = (size_t)W * H;
+  std::vector<float> tmp(3 * plane);
+  if (cudaMemcpyAsync(tmp.data(), d, sizeof(float) * 3 * plane, cudaMemcpyDeviceToHost, ctx.stream) != cudaSuccess ||
+      cudaStreamSynchronize(ctx.stream) != cudaSuccess)
+    return finish(h, Status{RD_READBACK, "readback failed"});
+  for (size_t i = 0; i < plane; ++i) {
+    out[3 * i] = tmp[i];
+    out[3 * i + 1] = tmp[plane + i];
+    out[3 * i + 2] = tmp[2 * plane + i];
+  }
+  return RD_OK;
+}
+
+rd_status rd_source_download(rd_ctx* h, const rd_source* s, float* out) {
+  if (!h || !s || !out) return RD_INVALID_INPUT;
+  return download_planar(h, s->rgb, s->W, s->H, out);
+}
+rd_status rd_base_download(rd_ctx* h, const rd_base* b, float* out) {
+  if (!h || !b || !out) return RD_INVALID_INPUT;
+  return download_planar(h, b->rgb, b->W, b->H, out);
+}
+void rd_source_release(rd_source* s) {
+  if (!s) return;
+  rd::device_free(s->ctx->c, s->rgb, s->bytes);
+  delete s;
+}
+void rd_base_release(rd_base* b) {
+  if (!b) return;
+  rd::device_free(b->ctx->c, b->rgb, b->bytes);
+  if (b->d_hist) rd::device_free(b->ctx->c, b->d_hist, b->out_bytes);
+  delete b;
+}
+
+// ------------------------------------------------------------------ stages
+static Status upload_planar(rd::Context& ctx, const float* interleaved, int W, int H, float** out, size_t* bytes) {
+  const size_t plane = (size_t)W * H;
+  std::vector<float> tmp(3 * plane);
+  for (size_t i = 0; i < plane; ++i) {
+    tmp[i] = interleaved[3 * i];
+    tmp[plane + i] = interleaved[3 * i + 1];
+    tmp[2 * plane + i] = interleaved[3 * i + 2];
+  }
+  *bytes = sizeof(float) * 3 * plane;
+  void* p = nullptr;
+  RD_TRY(rd::device_alloc(ctx, *bytes, &p));
+  *out = static_cast<float*>(p);
+  RD_CUDA_TRY(cudaMemcpyAsync(*out, tmp.data(), *bytes, cudaMemcpyHostToDevice, ctx.stream));
+  RD_CUDA_TRY(cudaStreamSynchronize(ctx.stream));
+  return Status{};
+}
+
+rd_status rd_stage_highlight(rd_ctx* h, const uint16_t* mosaic, size_t row_stride, const rd_sensor_desc* s,
+                             float* out, uint64_t* stats) {
+  if (!h || !mosaic || !s || !out) return finish(h, Status{RD_INVALID_INPUT, "null argument"});
+  rd::Context& ctx = h->c;
+  cudaSetDevice(ctx.device);
+  Status st;
+  rd::validate_sensor(*s, st);
+  if (!st.ok()) return finish(h, st);
+  const size_t raw_bytes = sizeof(uint16_t) * row_stride * s->sensor_height;
+  const int W = (int)s->crop_width, H = (int)s->crop_height;
+  const size_t out_bytes = sizeof(float) * (size_t)W * H;
+  void *praw = nullptr, *pout = nullptr, *pst = nullptr;
+  st = rd::device_alloc(ctx, raw_bytes, &praw);
+  if (st.ok()) st = rd::device_alloc(ctx, out_bytes, &pout);
+  if (st.ok()) st = rd::device_alloc(ctx, 16 * sizeof(unsigned long long), &pst);
+  if (st.ok() && cudaMemcpyAsync(praw, mosaic, raw_bytes, cudaMemcpyHostToDevice, ctx.stream) != cudaSuccess)
+    st = Status{RD_SYNCHRONIZATION, "upload failed"};
+  if (st.ok() && cudaMemsetAsync(pst, 0, 16 * sizeof(unsigned long long), ctx.stream) != cudaSuccess)
+    st = Status{RD_SYNCHRONIZATION, "memset failed"};
+  if (st.ok()) {
+    rd::MosaicSource src = rd::make_source(*s, static_cast<const uint16_t*>(praw), row_stride);
+    if (s->highlight == RD_HIGHLIGHT_OPPOSED) src.clip = 0;
+    st = rd::launch_normalize(ctx, src, static_cast<float*>(pout), static_cast<unsigned long long*>(pst));
+    if (st.ok() && s->highlight == RD_HIGHLIGHT_OPPOSED)
+      st = rd::run_opposed(ctx, static_cast<float*>(pout), W, H, src.cfa, s->detection_levels,
+                           s->has_neutral_ceiling ? s->neutral_ceiling : nullptr,
+                           static_cast<unsigned long long*>(pst), nullptr);
+  }
+  uint64_t host_stats[16] = {};
+  if (st.ok() && (cudaMemcpyAsync(out, pout, out_bytes, cudaMemcpyDeviceToHost, ctx.stream) != cudaSuccess ||
+                  cudaMemcpyAsync(host_stats, pst, sizeof(host_stats), cudaMemcpyDeviceToHost, ctx.stream) !=
+                      cudaSuccess))
+    st = Status{RD_READBACK, "readback failed"};
+  if (st.ok()) st = rd::check_kernel_error(ctx, "highlight");
+  if (st.ok() && stats) std::memcpy(stats, host_stats, sizeof(uint64_t) * 9);
+  rd::device_free(ctx, praw, raw_bytes);
+  rd::device_free(ctx, pout, out_bytes);
+  rd::device_free(ctx, pst, 16 * sizeof(unsigned long long));
+  cudaStreamSynchronize(ctx.stream);
+  return finish(h, st);
+}
+
+rd_status rd_stage_opposed(rd_ctx* h, const float* mosaic, uint32_t W, uint32_t H, int32_t cfa,
+                           const float levels[3], const float* ceiling, float* out, uint64_t* stats,
+                           uint32_t* labels, uint32_t* region_count) {
+  if (!h || !mosaic || !levels || !out) return finish(h, Status{RD_INVALID_INPUT, "null argument"});
+  if (W < 1 || H < 1 || cfa < 0 || cfa > 3) return finish(h, Status{RD_INVALID_DIMENSIONS, "bad mosaic"});
+  for (int c = 0; c < 3; ++c) {
+    if (!std::isfinite(levels[c]) || !(levels[c] > 0.0f))
+      return finish(h, Status{RD_INVALID_INPUT, "detection levels must be finite and positive"});
+    if (ceiling && (!std::isfinite(ceiling[c]) || !(ceiling[c] > 0.0f)))
+      return finish(h, Status{RD_INVALID_INPUT, "neutral ceiling must be finite and positive"});
+  }
+  for (size_t i = 0; i < (size_t)W * H; ++i)
+    if (!std::isfinite(mosaic[i])) return finish(h, Status{RD_INVALID_INPUT, "non-finite sample"});
+  rd::Context& ctx = h->c;
+  cudaSetDevice(ctx.device);
+  const size_t bytes = sizeof(float) * (size_t)W * H;
+  const size_t cells = (size_t)(W / 2 + W % 2) * (H / 2 + H % 2);
+  void *pm = nullptr, *ps = nullptr, *pl = nullptr;
+  Status st = rd::device_alloc(ctx, bytes, &pm);
+  if (st.ok()) st = rd::device_alloc(ctx, 16 * sizeof(unsigned long long), &ps);
+  if (st.ok() && labels) st = rd::device_alloc(ctx, sizeof(uint32_t) * cells, &pl);
+  if (st.ok() && (cudaMemcpyAsync(pm, mosaic, bytes, cudaMemcpyHostToDevice, ctx.stream) != cudaSuccess ||
+                  cudaMemsetAsync(ps, 0, 16 * sizeof(unsigned long long), ctx.stream) != cudaSuccess))
+    st = Status{RD_SYNCHRONIZATION, "upload failed"};
+  uint32_t count = 0;
+  if (st.ok())
+    st = rd::run_opposed_labels(ctx, static_cast<float*>(pm), (int)W, (int)H, cfa, levels, ceiling,
+                                static_cast<unsigned long long*>(ps), static_cast<uint32_t*>(pl), &count);
+  uint64_t host_stats[16] = {};
+  if (st.ok() && (cudaMemcpyAsync(out, pm, bytes, cudaMemcpyDeviceToHost, ctx.stream) != cudaSuccess ||
+                  cudaMemcpyAsync(host_stats, ps, sizeof(host_stats), cudaMemcpyDeviceToHost, ctx.stream) !=
+                      cudaSuccess ||
+                  (labels && cudaMemcpyAsync(labels, pl, sizeof(uint32_t) * cells, cudaMemcpyDeviceToHost,
+                                             ctx.stream) != cudaSuccess)))
+    st = Status{RD_READBACK, "readback failed"};
+  if (st.ok()) st = rd::check_kernel_error(ctx, "opposed");
+  if (st.ok()) {
+    if (stats) std::memcpy(stats, host_stats, sizeof(uint64_t) * 9);
+    if (region_count) *region_count = count;
+  }
+  rd::device_free(ctx, pm, bytes);
+  rd::device_free(ctx, ps, 16 * sizeof(unsigned long long));
+  if (pl) rd::device_free(ctx, pl, sizeof(uint32_t) * cells);
+  cudaStreamSynchronize(ctx.stream);
+  return finish(h, st);
+}
+
+rd_status rd_stage_demosaic(rd_ctx* h, const float* mosaic, uint32_t W, uint32_t H, int32_t cfa, int32_t algorithm,
+                            const float balance[3], float* out) {
+  if (!h || !mosaic || !balance || !out) return finish(h, Status{RD_INVALID_INPUT, "null argument"});
+  if (W < 2 || H < 2) return finish(h, Status{RD_INVALID_DIMENSIONS, "demosaicing requires at least 2x2 samples"});
+  if (cfa < 0 || cfa > 3 || algorithm < 0 || algorithm > 3)
+    return finish(h, Status{RD_INVALID_INPUT, "unknown CFA or algorithm"});
+  for (int c = 0; c < 3; ++c)
+    if (!std::isfinite(balance[c]) || !(balance[c] > 0.0f))
+      return finish(h, Status{RD_INVALID_INPUT, "balance must be finite and positive"});
+  rd::Context& ctx = h->c;
+  cudaSetDevice(ctx.device);
+  const size_t in_bytes = sizeof(float) * (size_t)W * H, out_bytes = 3 * in_bytes;
+  void *pin = nullptr, *pout = nullptr;
+  Status st = rd::device_alloc(ctx, in_bytes, &pin);
+  if (st.ok()) st = rd::device_alloc(ctx, out_bytes, &pout);
+  if (st.ok() && cudaMemcpyAsync(pin, mosaic, in_bytes, cudaMemcpyHostToDevice, ctx.stream) != cudaSuccess)
+    st = Status{RD_SYNCHRONIZATION, "upload failed"};
+  if (st.ok()) {
+    rd::MosaicSource src{};
+    src.f32 = static_cast<const float*>(pin);
+    src.width = (int)W;
+    src.height = (int)H;
+    src.cfa = cfa;
+    src.black_w = src.black_h = 1;
+    src.white_count = 1;
+    for (int c = 0; c < 3; ++c) src.fwd[c] = balance[c];
+    st = rd::run_demosaic(ctx, src, algorithm, static_cast<float*>(pout), nullptr);
+  }
+  if (st.ok()) st = rd::check_kernel_error(ctx, "demosaic");
+  rd_status rs = st.code;
+  if (st.ok()) rs = download_planar(h, static_cast<float*>(pout), (int)W, (int)H, out);
+  rd::device_free(ctx, pin, in_bytes);
+  rd::device_free(ctx, pout, out_bytes);
+  cudaStreamSynchronize(ctx.stream);
+  if (rs != RD_OK && st.ok()) return rs;
+  return finish(h, st);
+}
+
+rd_status rd_stage_capture(rd_ctx* h, float* rgb, uint32_t W, uint32_t H, const rd_detail_desc* detail) {
+  if (!h || !rgb || !detail) return finish(h, Status{RD_INVALID_INPUT, "null argument"});
+  rd::Context& ctx = h->c;
+  cudaSetDevice(ctx.device);
+  float* d = nullptr;
+  size_t bytes = 0;
+  Status st = upload_planar(ctx, rgb, (int)W, (int)H, &d, &bytes);
+  if (st.ok()) st = rd::run_capture(ctx, d, (int)W, (int)H, *detail, nullptr);
+  if (st.ok()) st = rd::check_kernel_error(ctx, "capture");
+  if (st.ok() && download_planar(h, d, (int)W, (int)H, rgb) != RD_OK) st = Status{RD_READBACK, "readback failed"};
+  if (d) rd::device_free(ctx, d, bytes);
+  cudaStreamSynchronize(ctx.stream);
+  return finish(h, st);
+}
+
+rd_status rd_stage_optics(rd_ctx* h, const rd_optics_desc* o, const float* rgb_in, float* rgb_out) {
+  if (!h || !o || !rgb_in || !rgb_out) return finish(h, Status{RD_INVALID_INPUT, "null argument"});
+  if (o->width < 4 || o->height < 4) return finish(h, Status{RD_INVALID_DIMENSIONS, "optics needs at least 4x4"});
+  rd::Context& ctx = h->c;
+  cudaSetDevice(ctx.device);
+  const int W = (int)o->width, H = (int)o->height;
+  const size_t plane = (size_t)W * H;
+  float* d = nullptr;
+  size_t bytes = 0;
+  void* p = nullptr;
+  float* mult = nullptr;
+  float* warped = nullptr;
+  Status st = upload_planar(ctx, rgb_in, W, H, &d, &bytes);
+  if (st.ok() && o->vignetting == 1) {
+    st = rd::device_alloc(ctx, sizeof(float) * plane, &p);
+    if (st.ok()) {
+      mult = static_cast<float*>(p);
+      st = rd::run_vignette_plane(ctx, *o, mult);
+    }
+  }
+  const bool warp = o->distortion_model != RD_DISTORTION_NONE || o->tca_model != RD_TCA_NONE;
+  if (st.ok()) {
+    st = rd::device_alloc(ctx, bytes, &p);
+    if (st.ok()) warped = static_cast<float*>(p);
+  }
+  if (st.ok()) {
+    if (warp) {
+      st = rd::run_optics_gather(ctx, *o, d, mult, warped);
+    } else {
+      // Vignetting only: the reduction kernel at 1:1 applies the multiplier exactly.
+      const size_t mid_bytes = sizeof(float) * rd::area_reduce_scratch_floats(W, H, W, H);
+      st = rd::device_alloc(ctx, mid_bytes, &p);
+      if (st.ok()) {
+        st = rd::run_area_reduce(ctx, d, mult, W, H, W, H, warped, static_cast<float*>(p));
+        rd::device_free(ctx, p, mid_bytes);
+      }
+    }
+  }
+  if (st.ok()) st = rd::check_kernel_error(ctx, "optics");
+  if (st.ok() && download_planar(h, warped, W, H, rgb_out) != RD_OK) st = Status{RD_READBACK, "readback failed"};
+  if (d) rd::device_free(ctx, d, bytes);
+  if (warped) rd::device_free(ctx, warped, bytes);
+  if (mult) rd::device_free(ctx, mult, sizeof(float) * plane);
+  cudaStreamSynchronize(ctx.stream);
+  return finish(h, st);
+}
+
+rd_status rd_stage_area_reduce(rd_ctx* h, const float* rgb_in, uint32_t W, uint32_t H, uint32_t tw, uint32_t th,
+                               float* rgb_out) {
+  if (!h || !rgb_in || !rgb_out) return finish(h, Status{RD_INVALID_INPUT, "null argument"});
+  if (tw == 0 || th == 0 || tw > W || th > H)
+    return finish(h, Status{RD_INVALID_DIMENSIONS, "area reduction cannot upscale or produce an empty image"});
+  rd::Context& ctx = h->c;
+  cudaSetDevice(ctx.device);
+  float* d = nullptr;
+  size_t bytes = 0;
+  void* p = nullptr;
+  void* pm = nullptr;
+  const size_t out_bytes = sizeof(float) * 3 * (size_t)tw * th;
+  const size_t mid_bytes = sizeof(float) * rd::area_reduce_scratch_floats((int)W, (int)H, (int)tw, (int)th);
+  Status st = upload_planar(ctx, rgb_in, (int)W, (int)H, &d, &bytes);
+  if (st.ok()) st = rd::device_alloc(ctx, out_bytes, &p);
+  if (st.ok()) st = rd::device_alloc(ctx, mid_bytes, &pm);
+  if (st.ok())
+    st = rd::run_area_reduce(ctx, d, nullptr, (int)W, (int)H, (int)tw, (int)th, static_cast<float*>(p),
+                             static_cast<float*>(pm));
+  if (st.ok()) st = rd::check_kernel_error(ctx, "area reduce");
+  if (st.ok() && download_planar(h, static_cast<float*>(p), (int)tw, (int)th, rgb_out) != RD_OK)
+    st = Status{RD_READBACK, "readback failed"};
+  if (d) rd::device_free(ctx, d, bytes);
+  if (p) rd::device_free(ctx, p, out_bytes);
+  if (pm) rd::device_free(ctx, pm, mid_bytes);
+  cudaStreamSynchronize(ctx.stream);
+  return finish(h, st);
+}
+
+rd_status rd_stage_color(rd_ctx* h, const float* rgb_in, uint32_t W, uint32_t H, const rd_color_desc* color,
+                         uint8_t* srgb_out, uint64_t* hist, uint64_t* clipped) {
+  if (!h || !rgb_in || !color || !srgb_out) return finish(h, Status{RD_INVALID_INPUT, "null argument"});
+  rd::Context& ctx = h->c;
+  cudaSetDevice(ctx.device);
+  float* d = nullptr;
+  size_t bytes = 0;
+  void* p = nullptr;
+  const size_t out_bytes = (size_t)3 * W * H + 1024 * sizeof(unsigned long long);
+  Status st = upload_planar(ctx, rgb_in, (int)W, (int)H, &d, &bytes);
+  if (st.ok()) st = rd::device_alloc(ctx, out_bytes, &p);
+  unsigned long long* d_hist = static_cast<unsigned long long*>(p);
+  uint8_t* d_out = reinterpret_cast<uint8_t*>(d_hist + 1024);
+  if (st.ok() && cudaMemsetAsync(d_hist, 0, 1024 * sizeof(unsigned long long), ctx.stream) != cudaSuccess)
+    st = Status{RD_SYNCHRONIZATION, "memset failed"};
+  if (st.ok()) st = rd::run_color_output(ctx, d, (int)W, (int)H, *color, true, d_out, d_hist);
+  uint64_t bins[1024];
+  if (st.ok() && (cudaMemcpyAsync(srgb_out, d_out, (size_t)3 * W * H, cudaMemcpyDeviceToHost, ctx.stream) !=
+                      cudaSuccess ||
+                  cudaMemcpyAsync(bins, d_hist, sizeof(bins), cudaMemcpyDeviceToHost, ctx.stream) != cudaSuccess))
+    st = Status{RD_READBACK, "readback failed"};
+  if (st.ok()) st = rd::check_kernel_error(ctx, "color");
+  if (st.ok()) {
+    if (hist) std::memcpy(hist, bins, sizeof(bins));
+    if (clipped)
+      for (int c = 0; c < 3; ++c) {
+        clipped[c] = bins[256 * c];
+        clipped[3 + c] = bins[256 * c + 255];
+      }
+  }
+  if (d) rd::device_free(ctx, d, bytes);
+  if (p) rd::device_free(ctx, p, out_bytes);
+  cudaStreamSynchronize(ctx.stream);
+  return finish(h, st);
+}
+
+rd_status rd_optics_plan(rd_optics_desc* o, float crop, float real_focal, float cx, float cy) {
+  if (!o) return RD_INVALID_INPUT;
+  return rd::optics_plan(*o, crop, real_focal, cx, cy).code;
+}
+
+void rd_standard_base_lut(float* lut) {
+  if (lut) rd::standard_base_lut(lut);
+}
+
+rd_status rd_synth_mosaic_device(rd_ctx* h, const rd_synth_desc* d, uint16_t* d_out) {
+  if (!h || !d || !d_out) return finish(h, Status{RD_INVALID_INPUT, "null argument"});
+  cudaSetDevice(h->c.device);
+  Status st = rd::run_synth(h->c, *d, d_out);
+  if (st.ok() && cudaStreamSynchronize(h->c.stream) != cudaSuccess) st = Status{RD_SYNCHRONIZATION, "sync failed"};
+  return finish(h, st);
+}
+
+rd_status rd_synth_mosaic(rd_ctx* h, const rd_synth_desc* d, uint16_t* out) {
+  if (!h || !d || !out) return finish(h, Status{RD_INVALID_INPUT, "null argument"});
+  rd::Context& ctx = h->c;
+  cudaSetDevice(ctx.device);
+  const size_t bytes = sizeof(uint16_t) * d->width * d->height;
+  void* p = nullptr;
+  Status st = rd::device_alloc(ctx, bytes, &p);
+  if (st.ok()) st = rd::run_synth(ctx, *d, static_cast<uint16_t*>(p));
+  if (st.ok() && (cudaMemcpyAsync(out, p, bytes, cudaMemcpyDeviceToHost, ctx.stream) != cudaSuccess ||
+                  cudaStreamSynchronize(ctx.stream) != cudaSuccess))
+    st = Status{RD_READBACK, "readback failed"};
+  if (p) rd::device_free(ctx, p, bytes);
+  cudaStreamSynchronize(ctx.stream);
+  return finish(h, st);
+}
+
+rd_status rd_ctx_event_record(rd_ctx* h, int slot) {
+  if (!h || slot < 0 || slot >= 64) return RD_INVALID_INPUT;
+  rd::Context& c = h->c;
+  if (!c.user_ev[slot] && cudaEventCreate(&c.user_ev[slot]) != cudaSuccess) return RD_SYNCHRONIZATION;
+  return cudaEventRecord(c.user_ev[slot], c.stream) == cudaSuccess ? RD_OK : RD_SYNCHRONIZATION;
+}
+
+rd_status rd_ctx_event_elapsed(rd_ctx* h, int a, int b, float* ms) {
+  if (!h || !ms || a < 0 || b < 0 || a >= 64 || b >= 64 || !h->c.user_ev[a] || !h->c.user_ev[b])
+    return RD_INVALID_INPUT;
+  if (cudaEventSynchronize(h->c.user_ev[b]) != cudaSuccess) return RD_SYNCHRONIZATION;
+  return cudaEventElapsedTime(ms, h->c.user_ev[a], h->c.user_ev[b]) == cudaSuccess ? RD_OK : RD_SYNCHRONIZATION;
+}
+
+rd_status rd_ctx_flush_l2(rd_ctx* h) {
+  if (!h) return RD_INVALID_INPUT;
+  rd::Context& c = h->c;
+  if (!c.flush_buf) {
+    int l2 = 0;
+    cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, c.device);
+    c.flush_bytes = std::max<size_t>((size_t)l2 * 2, (size_t)256 << 20);
+    Status st = rd::device_alloc(c, c.flush_bytes, &c.flush_buf);
+    if (!st.ok()) return finish(h, st);
+  }
+  return cudaMemsetAsync(c.flush_buf, 0x5a, c.flush_bytes, c.stream) == cudaSuccess ? RD_OK : RD_SYNCHRONIZATION;
+}
+
+rd_status rd_ctx_enable_kernel_timing(rd_ctx* h, int enable) {
+  if (!h) return RD_INVALID_INPUT;
+  cudaStreamSynchronize(h->c.stream);
+  rd::resolve_kernel_timing(h->c);
+  h->c.timing = enable != 0;
+  return RD_OK;
+}
+
+rd_status rd_ctx_kernel_timing(const rd_ctx* h, int family, const char** name, double* total_ms,
+                               uint64_t* launches) {
+  if (!h || family < 0 || family >= RD_KERNEL_FAMILIES) return RD_INVALID_INPUT;
+  if (name) *name = rd::kernel_family_name(family);
+  if (total_ms) *total_ms = h->c.family_ms[family];
+  if (launches) *launches = h->c.family_launches[family];
+  return RD_OK;
+}
+
+rd_status rd_ctx_reset_kernel_timing(rd_ctx* h) {
+  if (!h) return RD_INVALID_INPUT;
+  cudaStreamSynchronize(h->c.stream);
+  rd::resolve_kernel_timing(h->c);
+  for (int k = 0; k < RD_KERNEL_FAMILIES; ++k) {
+    h->c.family_ms[k] = 0.0;
+    h->c.family_launches[k] = 0;
+  }
+  return RD_OK;
+}
+
+rd_status rd_host_alloc(size_t bytes, void** out) {
+  if (!out) return RD_INVALID_INPUT;
+  return cudaMallocHost(out, bytes) == cudaSuccess ? RD_OK : RD_OVER_BUDGET;
+}
+
+void rd_host_free(void* ptr) {
+  if (ptr) cudaFreeHost(ptr);
+}
+
+rd_status rd_device_alloc(rd_ctx* h, size_t bytes, void** out) {
+  if (!h || !out) return RD_INVALID_INPUT;
+  cudaSetDevice(h->c.device);
+  Status st = rd::device_alloc(h->c, bytes, out);
+  if (st.ok()) {
+    h->c.user_allocs[*out] = bytes;
+    cudaStreamSynchronize(h->c.stream);
+  }
+  return finish(h, st);
+}
+rd_status rd_device_free(rd_ctx* h, void* ptr) {
+  if (!h) return RD_INVALID_INPUT;
+  if (!ptr) return RD_OK;
+  auto it = h->c.user_allocs.find(ptr);
+  if (it == h->c.user_allocs.end()) return finish(h, Status{RD_INVALID_INPUT, "pointer was not allocated here"});
+  rd::device_free(h->c, ptr, it->second);
+  h->c.user_allocs.erase(it);
+  cudaStreamSynchronize(h->c.stream);
+  return RD_OK;
+}
+rd_status rd_copy_to_device(rd_ctx* h, void* dst, const void* src, size_t bytes) {
+  if (!h) return RD_INVALID_INPUT;
+  if (cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->c.stream) != cudaSuccess ||
+      cudaStreamSynchronize(h->c.stream) != cudaSuccess)
+    return RD_SYNCHRONIZATION;
+  return RD_OK;
+}
+rd_status rd_copy_to_host(rd_ctx* h, void* dst, const void* src, size_t bytes) {
+  if (!h) return RD_INVALID_INPUT;
+  if (cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->c.stream) != cudaSuccess ||
+      cudaStreamSynchronize(h->c.stream) != cudaSuccess)
+    return RD_READBACK;
+  return RD_OK;
+}
+
+}  // extern "C"

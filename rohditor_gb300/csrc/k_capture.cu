@@ -1,0 +1,508 @@
+// Masked Richardson-Lucy capture sharpening (crates/core/src/sharpening.rs:
+// 87-389) and lens vignetting (crates/optics/src/correction.rs:213-267) on
+// sm_103a.
+//
+// Data layout: planar RGB plus four full-resolution f32 planes (guide, mask,
+// and a ping-pong pair for the estimate). Kernels:
+//   rl_init      guide = max(sum max(c,0)/3, 1e-6), mask = 1 - smoothstep(peak)
+//   rl_mask      blur(mask) and blur(guide) on one tile, refines the mask
+//   rl_iter      one whole RL iteration per tile in shared memory:
+//                blur(estimate) -> ratio = guide / max(b, 1e-6) -> blur(ratio)
+//                -> estimate = clamp(estimate * b, guide/2, 2 guide)
+//                so an iteration reads the estimate and guide once and writes
+//                the estimate once (12 bytes per pixel of compulsory traffic);
+//   rl_apply     the bounded common RGB gain, fused with vignetting.
+// Every blur keeps the reference's tap order (horizontal pass, then vertical,
+// each tap added in kernel order from 0; border columns start from -0.0 as
+// Iterator::sum does) and its half-sample mirror at the image edges. Field
+// values outside the image are filled from their mirror position, so every
+// stencil read equals the reference's mirrored read bit for bit.
+#include <cuda_runtime.h>
+
+#include "rd_internal.cuh"
+
+namespace rd {
+namespace {
+
+constexpr float FLOOR = 1.0e-6f;
+constexpr int MAX_TAPS = 9;  // radius <= 4 for sigma <= 1.2 (CAPTURE_RADIUS_RANGE)
+__constant__ float c_kernel[MAX_TAPS];
+
+__device__ __forceinline__ float smoothstep(float low, float high, float value) {
+  float t = (value - low) / (high - low);
+  t = t < 0.0f ? 0.0f : (t > 1.0f ? 1.0f : t);
+  return t * t * (3.0f - 2.0f * t);
+}
+__device__ __forceinline__ float rmax(float a, float b) {
+  if (isnan(a)) return b;
+  if (isnan(b)) return a;
+  return a > b ? a : b;
+}
+__device__ __forceinline__ float rmin(float a, float b) {
+  if (isnan(a)) return b;
+  if (isnan(b)) return a;
+  return a < b ? a : b;
+}
+// sharpening.rs:318-326: reflect about the outer pixel boundary.
+__device__ __forceinline__ int mirror_half(int index, int length) {
+  const int period = 2 * length;
+  int f = index % period;
+  if (f < 0) f += period;
+  return f < length ? f : 2 * length - 1 - f;
+}
+
+__global__ void rl_init_kernel(const float* __restrict__ rgb, long long plane, float c0, float c1, float c2,
+                               float* __restrict__ guide, float* __restrict__ mask, float* __restrict__ est,
+                               unsigned* error) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= plane) return;
+  const float r = rgb[i], g = rgb[plane + i], b = rgb[2 * plane + i];
+  if (!isfinite(r) || !isfinite(g) || !isfinite(b)) atomicOr(error, 2u);
+  float s = -0.0f;
+  s += rmax(r, 0.0f) / 3.0f;
+  s += rmax(g, 0.0f) / 3.0f;
+  s += rmax(b, 0.0f) / 3.0f;
+  const float gd = rmax(s, FLOOR);
+  float peak = 0.0f;
+  peak = rmax(peak, r / c0);
+  peak = rmax(peak, g / c1);
+  peak = rmax(peak, b / c2);
+  guide[i] = gd;
+  est[i] = gd;
+  mask[i] = 1.0f - smoothstep(0.85f, 0.98f, peak);
+}
+
+// Tile geometry of the fused kernels: a TX x TY core with radius-r halos.
+constexpr int TX = 64, TY = 32, RMAX = 4;
+constexpr int EW = TX + 4 * RMAX, EH = TY + 4 * RMAX;  // estimate window (two blurs)
+constexpr int RWX = TX + 2 * RMAX, RWY = TY + 2 * RMAX; // ratio window (one blur)
+
+// Load a real field into a window whose origin is (ox, oy): every entry holds
+// the field at the mirrored (in-image) position.
+__device__ __forceinline__ void load_window(float* dst, int ww, int wh, const float* __restrict__ src, int W, int H,
+                                            int ox, int oy) {
+  for (int k = threadIdx.x; k < ww * wh; k += blockDim.x) {
+    const int qy = k / ww, qx = k % ww;
+    dst[k] = src[(long long)mirror_half(oy + qy, H) * W + mirror_half(ox + qx, W)];
+  }
+}
+
+// Horizontal taps at image column x (in-image) of window row `row` whose
+// window column of x is qx: the reference's interior/border split.
+__device__ __forceinline__ float hblur(const float* row, int qx, int x, int W, int r, int taps) {
+  const bool border = W <= 2 * r || x < r || x >= W - r;
+  float v = border ? -0.0f : 0.0f;
+  for (int k = 0; k < taps; ++k) v += row[qx - r + k] * c_kernel[k];
+  return v;
+}
+
+struct RlIterSmem {
+  float e[EH * EW];       // estimate window, origin (x0 - 2r, y0 - 2r)
+  float t1[EH * RWX];     // horizontal blur of e, window columns x0 - r ..
+  float q[RWY * RWX];     // blur(e) then the ratio, origin (x0 - r, y0 - r)
+  float t2[RWY * TX];     // horizontal blur of the ratio, core columns
+};
+
+__global__ void __launch_bounds__(256) rl_iter_kernel(const float* __restrict__ est_in, const float* __restrict__ guide,
+                                                      float* __restrict__ est_out, int W, int H, int r) {
+  extern __shared__ float4 rl_smem_raw[];
+  RlIterSmem& S = *reinterpret_cast<RlIterSmem*>(rl_smem_raw);
+  const int taps = 2 * r + 1;
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+  const int ew = TX + 4 * r, eh = TY + 4 * r, qw = TX + 2 * r, qh = TY + 2 * r;
+  load_window(S.e, ew, eh, est_in, W, H, x0 - 2 * r, y0 - 2 * r);
+  __syncthreads();
+  // Horizontal pass of blur #1 at window columns x0 - r .. x0 + TX + r (in-image
+  // columns only; the rest are filled from their mirror after the ratio).
+  for (int k = threadIdx.x; k < eh * qw; k += blockDim.x) {
+    const int qy = k / qw, qx = k % qw;
+    const int x = x0 - r + qx;
+    if (x < 0 || x >= W) continue;
+    S.t1[qy * qw + qx] = hblur(S.e + qy * ew, qx + r, x, W, r, taps);
+  }
+  __syncthreads();
+  // Vertical pass of blur #1 and the ratio at in-image positions of the ratio window.
+  for (int k = threadIdx.x; k < qh * qw; k += blockDim.x) {
+    const int qy = k / qw, qx = k % qw;
+    const int x = x0 - r + qx, y = y0 - r + qy;
+    if (x < 0 || x >= W || y < 0 || y >= H) continue;
+    float b = 0.0f;
+    for (int j = 0; j < taps; ++j) b += S.t1[(qy + j) * qw + qx] * c_kernel[j];
+    S.q[k] = guide[(long long)y * W + x] / rmax(b, FLOOR);
+  }
+  __syncthreads();
+  // Out-of-image ratio entries within the blur radius of the image take the
+  // value at their mirror position, which lies inside this window. Entries
+  // further out are never read.
+  for (int k = threadIdx.x; k < qh * qw; k += blockDim.x) {
+    const int qy = k / qw, qx = k % qw;
+    const int x = x0 - r + qx, y = y0 - r + qy;
+    if (x >= 0 && x < W && y >= 0 && y < H) continue;
+    if (x < -r || x >= W + r || y < -r || y >= H + r) continue;
+    const int mx = mirror_half(x, W) - (x0 - r), my = mirror_half(y, H) - (y0 - r);
+    S.q[k] = S.q[my * qw + mx];
+  }
+  __syncthreads();
+  // Horizontal pass of blur #2 on the core columns.
+  for (int k = threadIdx.x; k < qh * TX; k += blockDim.x) {
+    const int qy = k / TX, cx = k % TX;
+    const int x = x0 + cx;
+    if (x >= W) continue;
+    S.t2[k] = hblur(S.q + qy * qw, cx + r, x, W, r, taps);
+  }
+  __syncthreads();
+  // Vertical pass of blur #2 and the bounded update.
+  for (int k = threadIdx.x; k < TY * TX; k += blockDim.x) {
+    const int cy = k / TX, cx = k % TX;
+    const int x = x0 + cx, y = y0 + cy;
+    if (x >= W || y >= H) continue;
+    float b = 0.0f;
+    for (int j = 0; j < taps; ++j) b += S.t2[(cy + j) * TX + cx] * c_kernel[j];
+    const long long o = (long long)y * W + x;
+    const float g = guide[o];
+    float e = S.e[(cy + 2 * r) * ew + cx + 2 * r] * b;
+    const float lo = g * 0.5f, hi = g * 2.0f;
+    if (e < lo) e = lo;
+    if (e > hi) e = hi;
+    est_out[o] = e;
+  }
+}
+
+// Mask refinement: blur(mask) and blur(guide) of one tile, then
+//   mask = min(mask, blur(mask)^4) * smoothstep(thr, 3 thr, |g - blur(g)|) * smoothstep(0.001, 0.01, g).
+struct RlMaskSmem {
+  float m[RWY * RWX];
+  float g[RWY * RWX];
+  float tm[RWY * TX];
+  float tg[RWY * TX];
+};
+
+__global__ void __launch_bounds__(256) rl_mask_kernel(const float* __restrict__ mask_in, const float* __restrict__ guide,
+                                                      float* __restrict__ mask_out, int W, int H, int r, float noise) {
+  extern __shared__ float4 rl_smem_raw[];
+  RlMaskSmem& S = *reinterpret_cast<RlMaskSmem*>(rl_smem_raw);
+  const int taps = 2 * r + 1;
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+  const int qw = TX + 2 * r, qh = TY + 2 * r;
+  load_window(S.m, qw, qh, mask_in, W, H, x0 - r, y0 - r);
+  load_window(S.g, qw, qh, guide, W, H, x0 - r, y0 - r);
+  __syncthreads();
+  for (int k = threadIdx.x; k < qh * TX; k += blockDim.x) {
+    const int qy = k / TX, cx = k % TX;
+    const int x = x0 + cx;
+    if (x >= W) continue;
+    S.tm[k] = hblur(S.m + qy * qw, cx + r, x, W, r, taps);
+    S.tg[k] = hblur(S.g + qy * qw, cx + r, x, W, r, taps);
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < TY * TX; k += blockDim.x) {
+    const int cy = k / TX, cx = k % TX;
+    const int x = x0 + cx, y = y0 + cy;
+    if (x >= W || y >= H) continue;
+    float bm = 0.0f, bg = 0.0f;
+    for (int j = 0; j < taps; ++j) {
+      bm += S.tm[(cy + j) * TX + cx] * c_kernel[j];
+      bg += S.tg[(cy + j) * TX + cx] * c_kernel[j];
+    }
+    const float m0 = S.m[(cy + r) * qw + cx + r];
+    const float g = S.g[(cy + r) * qw + cx + r];
+    const float b2 = bm * bm;
+    float m = rmin(m0, b2 * b2);
+    const float threshold = 0.0005f + noise * 0.008f + bg * noise * 0.02f;
+    const float detail = fabsf(g - bg);
+    m *= smoothstep(threshold, threshold * 3.0f, detail) * smoothstep(0.001f, 0.01f, g);
+    mask_out[(long long)y * W + x] = m;
+  }
+}
+
+// Vignetting radius scan (correction.rs:239-262): r2 advances along each row
+// by the row-independent increment d[k] = 2 ns x_k + ns^2 with f32 rounding at
+// every step, so the value at a column depends on the whole row prefix. One
+// thread per row walks the row and records r2 at every SEG-th column; the
+// apply kernel resumes each SEG-column segment from its checkpoint exactly.
+constexpr int SEG = 32;
+
+__global__ void vignette_scan_kernel(const float* __restrict__ incr, const float* __restrict__ r2_start, int W, int H,
+                                     float* __restrict__ checkpoints, int segs) {
+  const int y = blockIdx.x * blockDim.x + threadIdx.x;
+  if (y >= H) return;
+  float r2 = r2_start[y];
+  float* cp = checkpoints + (long long)y * segs;
+  for (int s = 0; s < segs; ++s) {
+    cp[s] = r2;
+    const int end = min(W, (s + 1) * SEG);
+    for (int x = s * SEG; x < end; ++x) r2 += incr[x];
+  }
+}
+
+struct ApplyParams {
+  float* rgb;
+  long long plane;
+  int W, H;
+  // capture gain
+  int capture;
+  float amount;
+  const float* mask;
+  const float* est;
+  const float* guide;
+  // vignetting
+  int vignetting;
+  const float* incr;
+  const float* checkpoints;
+  int segs;
+  float k1, k2, k3;
+  unsigned* error;
+};
+
+// One warp per (row, 32 segments): each lane resumes the radius scan of one
+// SEG-column segment from its checkpoint, multipliers go through shared
+// memory, and the warp then sweeps the 1024 pixels with coalesced accesses.
+__global__ void __launch_bounds__(256) rl_apply_kernel(const ApplyParams p) {
+  __shared__ float mult[8][32][SEG + 1];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int y = blockIdx.y;
+  const int seg0 = (blockIdx.x * 8 + warp) * 32;  // first segment of this warp
+  if (seg0 * SEG >= p.W) return;
+  bool bad = false;
+  if (p.vignetting) {
+    const int s = seg0 + lane;
+    if (s < p.segs) {
+      float r2 = p.checkpoints[(long long)y * p.segs + s];
+      const int xs = s * SEG;
+      for (int j = 0; j < SEG; ++j) {
+        const int x = xs + j;
+        float m = 1.0f;
+        if (x < p.W) {
+          const float r4 = r2 * r2, r6 = r4 * r2;
+          const float gain = 1.0f + p.k1 * r2 + p.k2 * r4 + p.k3 * r6;
+          if (!isfinite(gain) || gain == 0.0f) bad = true;
+          m = 1.0f / gain;
+          r2 += p.incr[x];
+        }
+        mult[warp][lane][j] = m;
+      }
+    }
+    __syncwarp();
+  }
+  for (int j = 0; j < 32; ++j) {
+    const int s = seg0 + j;
+    const int x = s * SEG + lane;
+    if (s >= p.segs || x >= p.W) continue;
+    const long long o = (long long)y * p.W + x;
+    float v0 = p.rgb[o], v1 = p.rgb[p.plane + o], v2 = p.rgb[2 * p.plane + o];
+    if (p.capture) {
+      // sharpening.rs:110-118
+      const float gain = 1.0f + p.amount * p.mask[o] * (p.est[o] / p.guide[o] - 1.0f);
+      if (gain != 1.0f && isfinite(v0 * gain) && isfinite(v1 * gain) && isfinite(v2 * gain)) {
+        v0 *= gain;
+        v1 *= gain;
+        v2 *= gain;
+      }
+    }
+    if (p.vignetting) {
+      const float m = mult[warp][j][lane];
+      v0 *= m;
+      v1 *= m;
+      v2 *= m;
+      if (!isfinite(v0) || !isfinite(v1) || !isfinite(v2)) bad = true;
+    }
+    p.rgb[o] = v0;
+    p.rgb[p.plane + o] = v1;
+    p.rgb[2 * p.plane + o] = v2;
+  }
+  if (bad) atomicOr(p.error, 4u);
+}
+
+}  // namespace
+
+// Host contract: Gaussian kernel weights (crates/detail/src/gaussian.rs:9-17).
+int gaussian_kernel(float sigma, float* weights, int max_taps) {
+  const int radius = (int)std::ceil(3.0f * sigma);
+  const int taps = 2 * radius + 1;
+  if (taps > max_taps) return -1;
+  float sum = -0.0f;
+  for (int i = 0; i < taps; ++i) {
+    const float t = (float)(i - radius) / sigma;
+    weights[i] = std::exp(-0.5f * (t * t));
+    sum += weights[i];
+  }
+  for (int i = 0; i < taps; ++i) weights[i] /= sum;
+  return taps;
+}
+
+namespace {
+struct VignetteTables {
+  float* incr = nullptr;
+  float* r2_start = nullptr;
+  float* checkpoints = nullptr;
+  int segs = 0;
+  size_t bytes = 0;
+};
+
+// Host side of the vignetting scan: the column increments and the row starts
+// follow correction.rs:226-243 operation by operation in f32.
+Status prepare_vignetting(Context& ctx, const rd_optics_desc& o, int W, int H, VignetteTables& t) {
+  const float ns = (float)o.norm_scale;
+  const float step = 2.0f * ns, step_sq = ns * ns;
+  const float start_x = (float)(-o.center_x), start_y = (float)(-o.center_y);
+  std::vector<float> incr(W), r2s(H);
+  float x = start_x;
+  for (int k = 0; k < W; ++k) {
+    incr[k] = step * x + step_sq;
+    x += ns;
+  }
+  for (int row = 0; row < H; ++row) {
+    const float y = start_y + ns * (float)row;
+    r2s[row] = start_x * start_x + y * y;
+  }
+  t.segs = (W + SEG - 1) / SEG;
+  t.bytes = sizeof(float) * ((size_t)W + H + (size_t)H * t.segs);
+  void* p = nullptr;
+  RD_TRY(device_alloc(ctx, t.bytes, &p));
+  t.incr = static_cast<float*>(p);
+  t.r2_start = t.incr + W;
+  t.checkpoints = t.r2_start + H;
+  RD_CUDA_TRY(cudaMemcpyAsync(t.incr, incr.data(), sizeof(float) * W, cudaMemcpyHostToDevice, ctx.stream));
+  RD_CUDA_TRY(cudaMemcpyAsync(t.r2_start, r2s.data(), sizeof(float) * H, cudaMemcpyHostToDevice, ctx.stream));
+  RD_LAUNCH(ctx, K_VIGNETTE, vignette_scan_kernel<<<(H + 127) / 128, 128, 0, ctx.stream>>>(t.incr, t.r2_start, W, H, t.checkpoints, t.segs));
+  RD_CUDA_TRY(cudaGetLastError());
+  return Status{};
+}
+}  // namespace
+
+// Vignetting multiplier plane: mult[y][x] = 1 / (1 + k1 r2 + k2 r2^2 + k3 r2^3)
+// with r2 from the exact incremental scan. The optics gather and the area
+// reduction multiply each source sample by it on load, so the resident source
+// itself is never modified.
+__global__ void __launch_bounds__(256) vignette_plane_kernel(const float* __restrict__ incr,
+                                                             const float* __restrict__ checkpoints, int W, int H,
+                                                             int segs, float k1, float k2, float k3,
+                                                             float* __restrict__ mult, unsigned* error) {
+  __shared__ float m[8][32][SEG + 1];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int y = blockIdx.y;
+  const int seg0 = (blockIdx.x * 8 + warp) * 32;
+  if (seg0 >= segs) return;
+  bool bad = false;
+  const int s = seg0 + lane;
+  if (s < segs) {
+    float r2 = checkpoints[(long long)y * segs + s];
+    for (int j = 0; j < SEG; ++j) {
+      const int x = s * SEG + j;
+      float v = 1.0f;
+      if (x < W) {
+        const float r4 = r2 * r2, r6 = r4 * r2;
+        const float gain = 1.0f + k1 * r2 + k2 * r4 + k3 * r6;
+        if (!isfinite(gain) || gain == 0.0f) bad = true;
+        v = 1.0f / gain;
+        r2 += incr[x];
+      }
+      m[warp][lane][j] = v;
+    }
+  }
+  __syncwarp();
+  for (int j = 0; j < 32; ++j) {
+    const int sj = seg0 + j;
+    const int x = sj * SEG + lane;
+    if (sj < segs && x < W) mult[(long long)y * W + x] = m[warp][j][lane];
+  }
+  if (bad) atomicOr(error, 4u);
+}
+
+Status run_vignette_plane(Context& ctx, const rd_optics_desc& optics, float* mult) {
+  const int W = (int)optics.width, H = (int)optics.height;
+  VignetteTables vt;
+  RD_TRY(prepare_vignetting(ctx, optics, W, H, vt));
+  dim3 grid((vt.segs + 8 * 32 - 1) / (8 * 32), H);
+  RD_LAUNCH(ctx, K_VIGNETTE, vignette_plane_kernel<<<grid, 256, 0, ctx.stream>>>(vt.incr, vt.checkpoints, W, H, vt.segs, optics.vignetting_k[0],
+                                                      optics.vignetting_k[1], optics.vignetting_k[2], mult,
+                                                      ctx.d_error));
+  const cudaError_t launch = cudaGetLastError();
+  device_free(ctx, vt.incr, vt.bytes);
+  if (launch != cudaSuccess) return Status{RD_SYNCHRONIZATION, cudaGetErrorString(launch)};
+  return Status{};
+}
+
+// Capture sharpening (and, when given, vignetting) on planar RGB in place.
+Status run_capture(Context& ctx, float* rgb, int W, int H, const rd_detail_desc& detail,
+                   const rd_optics_desc* vignetting) {
+  const bool capture = detail.enabled && detail.amount > 0.0f;
+  const bool vig = vignetting && vignetting->vignetting == 1;
+  if (!capture && !vig) return Status{};
+  const long long plane = (long long)W * H;
+  float* planes = nullptr;
+  size_t plane_bytes = 0;
+  int r = 0;
+  if (capture) {
+    if (!(detail.radius >= 0.3f && detail.radius <= 1.2f) || !(detail.amount <= 1.0f) ||
+        !(detail.noise_protection >= 0.0f && detail.noise_protection <= 1.0f))
+      return Status{RD_INVALID_INPUT, "capture sharpening settings are outside their ranges"};
+    for (int c = 0; c < 3; ++c)
+      if (!std::isfinite(detail.ceilings[c]) || !(detail.ceilings[c] > 0.0f))
+        return Status{RD_INVALID_INPUT, "capture ceilings must be finite and positive"};
+    float w[MAX_TAPS];
+    const int taps = gaussian_kernel(detail.radius, w, MAX_TAPS);
+    if (taps < 0) return Status{RD_INVALID_INPUT, "capture radius too large"};
+    r = taps / 2;
+    RD_CUDA_TRY(cudaMemcpyToSymbolAsync(c_kernel, w, sizeof(float) * taps, 0, cudaMemcpyHostToDevice, ctx.stream));
+    plane_bytes = sizeof(float) * (size_t)plane * 5;
+    void* p = nullptr;
+    RD_TRY(device_alloc(ctx, plane_bytes, &p));
+    planes = static_cast<float*>(p);
+  }
+  float* guide = planes;
+  float* mask = planes ? planes + plane : nullptr;
+  float* mask2 = planes ? planes + 2 * plane : nullptr;
+  float* est = planes ? planes + 3 * plane : nullptr;
+  float* est2 = planes ? planes + 4 * plane : nullptr;
+  Status st;
+  if (capture) {
+    RD_LAUNCH(ctx, K_RL_INIT, rl_init_kernel<<<(unsigned)((plane + 255) / 256), 256, 0, ctx.stream>>>(
+        rgb, plane, detail.ceilings[0], detail.ceilings[1], detail.ceilings[2], guide, mask, est, ctx.d_error));
+    dim3 grid((W + TX - 1) / TX, (H + TY - 1) / TY);
+    const size_t mask_smem = sizeof(RlMaskSmem);
+    cudaFuncSetAttribute(rl_mask_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mask_smem);
+    RD_LAUNCH(ctx, K_RL_MASK, rl_mask_kernel<<<grid, 256, mask_smem, ctx.stream>>>(mask, guide, mask2, W, H, r, detail.noise_protection));
+    std::swap(mask, mask2);
+    const size_t iter_smem = sizeof(RlIterSmem);
+    cudaFuncSetAttribute(rl_iter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)iter_smem);
+    for (int it = 0; it < detail.iterations; ++it) {
+      RD_LAUNCH(ctx, K_RL_ITER, rl_iter_kernel<<<grid, 256, iter_smem, ctx.stream>>>(est, guide, est2, W, H, r));
+      std::swap(est, est2);
+    }
+    if (cudaGetLastError() != cudaSuccess) st = Status{RD_SYNCHRONIZATION, "capture kernels failed to launch"};
+  }
+  VignetteTables vt;
+  if (st.ok() && vig) st = prepare_vignetting(ctx, *vignetting, W, H, vt);
+  if (st.ok()) {
+    ApplyParams ap{};
+    ap.rgb = rgb;
+    ap.plane = plane;
+    ap.W = W;
+    ap.H = H;
+    ap.capture = capture ? 1 : 0;
+    ap.amount = detail.amount;
+    ap.mask = mask;
+    ap.est = est;
+    ap.guide = guide;
+    ap.vignetting = vig ? 1 : 0;
+    ap.incr = vt.incr;
+    ap.checkpoints = vt.checkpoints;
+    ap.segs = vig ? vt.segs : (W + SEG - 1) / SEG;
+    if (vig) {
+      ap.k1 = vignetting->vignetting_k[0];
+      ap.k2 = vignetting->vignetting_k[1];
+      ap.k3 = vignetting->vignetting_k[2];
+    }
+    ap.error = ctx.d_error;
+    const int segs = (W + SEG - 1) / SEG;
+    dim3 grid((segs + 8 * 32 - 1) / (8 * 32), H);
+    RD_LAUNCH(ctx, K_RL_APPLY, rl_apply_kernel<<<grid, 256, 0, ctx.stream>>>(ap));
+    if (cudaGetLastError() != cudaSuccess) st = Status{RD_SYNCHRONIZATION, "capture apply failed to launch"};
+  }
+  if (vt.incr) device_free(ctx, vt.incr, vt.bytes);
+  if (planes) device_free(ctx, planes, plane_bytes);
+  return st;
+}
+
+}  // namespace rd

@@ -1,0 +1,728 @@
+// Opposed highlight reconstruction on sm_103a (crates/highlight/src/
+// {opposed,cells,regions,support,region_correction}.rs).
+//
+// Pipeline (all on the device, no host round trip between kernels):
+//   1. suspected-site count (early exit as opposed.rs:75-81 when zero: every
+//      later kernel reads the count and returns);
+//   2. cell summaries (cells.rs:41-113): per 2x2 cell, channel means of the
+//      clean positive samples and usable / suspected flags;
+//   3. dilated mask (regions.rs:127-182): a cell is inside when any cell of
+//      its 3x3 neighbourhood holds a suspected sample (DILATION_CELLS = 1);
+//   4. 8-connected labelling (regions.rs:188-281) as a lock-free union-find
+//      whose root is always the smallest cell index of the component; a prefix
+//      sum over roots in raster order then gives exactly the reference's
+//      compact labels (numbered by first appearance in raster order);
+//   5. per-region clipped channels and wanted (channel, support) slots
+//      (region_correction.rs:134-178);
+//   6. two-pass trimmed means over each region's clean border ring plus the
+//      image-wide pool, f64 accumulators (region_correction.rs:196-256);
+//   7. per-site estimate (opposed.rs:86-330): local median over clean cells
+//      1..3 cells away, region/pool correction, chromaticity guard, 4x level
+//      bound, raise or neutralise.
+// The f64 accumulation order of step 6 differs from the reference's raster
+// scan; the trimmed means agree to f64 rounding, which is far below f32.
+// Every retry loop carries an iteration limit and reports through the error
+// word instead of spinning.
+#include <cuda_runtime.h>
+
+#include "rd_internal.cuh"
+
+namespace rd {
+namespace {
+
+constexpr float DARK_SUPPORT_FRACTION = 0.2f;
+constexpr float CROSS_CHANNEL_TOLERANCE_EV = 0.75f;
+constexpr int SLOTS = 9, PATTERNS = 3;
+constexpr unsigned MIN_BORDER_CELLS = 3;
+constexpr double TRIM_DEVIATIONS = 2.0;
+constexpr float TRIM_FLOOR = 1e-5f;
+constexpr float BORDER_MIN_FRACTION = 0.5f;
+constexpr int LAST_RADIUS = 3, MAX_CANDIDATES = 48, MIN_CANDIDATES = 3;
+constexpr float MAX_ESTIMATE_MULT = 4.0f;
+constexpr unsigned NONE = 0xFFFFFFFFu;
+constexpr int UNION_LIMIT = 1 << 20;
+constexpr unsigned OPPOSED_ERROR = 16u;
+
+struct Cell {
+  float m[3];
+  unsigned flags;
+};
+
+struct OpposedParams {
+  float* mosaic;
+  int W, H, cw, ch, cfa;
+  float levels[3];
+  int has_ceiling;
+  float ceiling[3];
+  float4* cells;             // xyz = means, w = flags (as bits)
+  unsigned char* dilated;
+  unsigned* parent;
+  unsigned* labels;
+  unsigned* block_sums;
+  unsigned* region_clipped;  // per label
+  unsigned* wanted;          // per label; wanted[0] = union over regions
+  double* acc;               // per (label, slot): count, kept, accum, second (4 doubles)
+  float* trim;               // per (label, slot): mean, tolerance
+  unsigned max_labels;
+  unsigned long long* stats; // 9 counters (reconstructed etc. at [1..5])
+  unsigned* counters;        // [0] suspected count, [1] region count
+  unsigned* error;
+};
+
+__device__ __forceinline__ Cell load_cell(const OpposedParams& p, int x, int y) {
+  const float4 v = p.cells[(long long)y * p.cw + x];
+  Cell c;
+  c.m[0] = v.x;
+  c.m[1] = v.y;
+  c.m[2] = v.z;
+  c.flags = __float_as_uint(v.w);
+  return c;
+}
+__device__ __forceinline__ bool usable(const Cell& c, int ch) { return c.flags & (1u << ch); }
+__device__ __forceinline__ bool clean(const Cell& c, int ch) { return !(c.flags & (1u << (ch + 3))); }
+__device__ __forceinline__ bool bright_clean(const Cell& c, int ch, const float* lv) {
+  return usable(c, ch) && clean(c, ch) && c.m[ch] > DARK_SUPPORT_FRACTION * lv[ch];
+}
+__device__ __forceinline__ unsigned support_mask(const Cell& c, int target, const float* lv) {
+  unsigned m = 0;
+  for (int ch = 0; ch < 3; ++ch)
+    if (ch != target && bright_clean(c, ch, lv)) m |= 1u << ch;
+  return m;
+}
+// support.rs:56-77
+__device__ bool reference_value(const Cell& c, unsigned support, float& out) {
+  if (__popc(support) == 1) {
+    const float v = c.m[__ffs(support) - 1];
+    if (isfinite(v) && v > 0.0f) {
+      out = v;
+      return true;
+    }
+    return false;
+  }
+  float sum = 0.0f;
+  int count = 0;
+  for (int ch = 0; ch < 3; ++ch) {
+    if (!(support & (1u << ch))) continue;
+    const float v = c.m[ch];
+    if (!isfinite(v) || v <= 0.0f) return false;
+    sum += cbrtf(v);
+    count += 1;
+  }
+  if (count == 0) return false;
+  const float root = sum / (float)count;
+  out = root * root * root;
+  return true;
+}
+__device__ bool correction(const Cell& c, int target, unsigned support, const float* lv, float& out) {
+  if (!bright_clean(c, target, lv)) return false;
+  for (int ch = 0; ch < 3; ++ch)
+    if ((support & (1u << ch)) && !bright_clean(c, ch, lv)) return false;
+  float ref;
+  if (!reference_value(c, support, ref)) return false;
+  const float v = c.m[target] - ref;
+  if (!isfinite(v)) return false;
+  out = v;
+  return true;
+}
+__device__ bool log_ratio(const Cell& c, unsigned support, float& out) {
+  if (__popc(support) != 2) return false;
+  const int first = __ffs(support) - 1;
+  const int second = __ffs(support & ~(1u << first)) - 1;
+  const float ratio = c.m[first] / c.m[second];
+  if (!(isfinite(ratio) && ratio > 0.0f)) return false;
+  out = log2f(ratio);
+  return true;
+}
+__device__ __forceinline__ bool chroma_agrees(unsigned support, bool ht, float t, bool he, float e) {
+  if (__popc(support) < 2) return true;
+  if (ht && he) return fabsf(t - e) <= CROSS_CHANNEL_TOLERANCE_EV;
+  return false;
+}
+__device__ __forceinline__ void support_patterns(int ch, unsigned out[3]) {
+  const int o0 = ch == 0 ? 1 : 0;
+  const int o1 = ch == 2 ? 1 : 2;
+  out[0] = 1u << o0;
+  out[1] = 1u << o1;
+  out[2] = (1u << o0) | (1u << o1);
+}
+__device__ __forceinline__ int pattern_position(int ch, unsigned support) {
+  unsigned p[3];
+  support_patterns(ch, p);
+  for (int k = 0; k < 3; ++k)
+    if (p[k] == support) return k;
+  return -1;
+}
+
+// 1. suspected sites
+__global__ void count_kernel(const OpposedParams p) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned hit = 0, ch = 0;
+  if (i < (long long)p.W * p.H) {
+    const int x = (int)(i % p.W), y = (int)(i / p.W);
+    ch = color_at(p.cfa, x, y);
+    hit = p.mosaic[i] >= p.levels[ch];
+  }
+  const unsigned ballot = __ballot_sync(0xffffffffu, hit);
+  if ((threadIdx.x & 31) == 0 && ballot) atomicAdd(&p.counters[0], __popc(ballot));
+  for (int c = 0; c < 3; ++c) {
+    const unsigned b = __ballot_sync(0xffffffffu, hit && ch == (unsigned)c);
+    if ((threadIdx.x & 31) == 0 && b) atomicAdd(&p.stats[6 + c], (unsigned long long)__popc(b));
+  }
+}
+
+// 2. cell summaries
+__global__ void cells_kernel(const OpposedParams p) {
+  if (p.counters[0] == 0) return;
+  const int cx = blockIdx.x * blockDim.x + threadIdx.x, cy = blockIdx.y;
+  if (cx >= p.cw) return;
+  float sums[3] = {0.0f, 0.0f, 0.0f};
+  unsigned counts[3] = {0, 0, 0};
+  unsigned flags = 0;
+  for (int y = 2 * cy; y < min(2 * cy + 2, p.H); ++y)
+    for (int x = 2 * cx; x < min(2 * cx + 2, p.W); ++x) {
+      const int ch = color_at(p.cfa, x, y);
+      const float s = p.mosaic[(long long)y * p.W + x];
+      if (s >= p.levels[ch]) {
+        flags |= 1u << (ch + 3);
+      } else if (s > 0.0f) {
+        sums[ch] += s;
+        counts[ch] += 1;
+      }
+    }
+  float m[3] = {0.0f, 0.0f, 0.0f};
+  for (int ch = 0; ch < 3; ++ch)
+    if (counts[ch] != 0) {
+      m[ch] = sums[ch] / (float)counts[ch];
+      flags |= 1u << ch;
+    }
+  p.cells[(long long)cy * p.cw + cx] = make_float4(m[0], m[1], m[2], __uint_as_float(flags));
+}
+
+// 3. dilation + union-find initialisation
+__global__ void dilate_kernel(const OpposedParams p) {
+  if (p.counters[0] == 0) return;
+  const int cx = blockIdx.x * blockDim.x + threadIdx.x, cy = blockIdx.y;
+  if (cx >= p.cw) return;
+  bool inside = false;
+  for (int y = max(cy - 1, 0); y <= min(cy + 1, p.ch - 1) && !inside; ++y)
+    for (int x = max(cx - 1, 0); x <= min(cx + 1, p.cw - 1); ++x)
+      if (__float_as_uint(p.cells[(long long)y * p.cw + x].w) >> 3) {
+        inside = true;
+        break;
+      }
+  const long long i = (long long)cy * p.cw + cx;
+  p.dilated[i] = inside;
+  p.parent[i] = inside ? (unsigned)i : NONE;
+}
+
+// Root of i. Links only ever point to smaller indices, so shortening a path
+// with atomicMin (never raising a link) keeps every component intact.
+__device__ unsigned find_root(unsigned* parent, unsigned i, unsigned* error) {
+  for (int k = 0; k < UNION_LIMIT; ++k) {
+    const unsigned q = parent[i];
+    if (q == i) return i;
+    const unsigned g = parent[q];
+    if (g < q) atomicMin(&parent[i], g);
+    i = q;
+  }
+  atomicOr(error, OPPOSED_ERROR);
+  return i;
+}
+
+// Link the roots of a and b, the larger root pointing at the smaller.
+__device__ void unite(unsigned* parent, unsigned a, unsigned b, unsigned* error) {
+  for (int k = 0; k < UNION_LIMIT; ++k) {
+    a = find_root(parent, a, error);
+    b = find_root(parent, b, error);
+    if (a == b) return;
+    if (a > b) {
+      const unsigned t = a;
+      a = b;
+      b = t;
+    }
+    const unsigned old = atomicMin(&parent[b], a);
+    if (old == b) return;
+    b = old;
+  }
+  atomicOr(error, OPPOSED_ERROR);
+}
+
+__global__ void union_kernel(const OpposedParams p) {
+  if (p.counters[0] == 0) return;
+  const int cx = blockIdx.x * blockDim.x + threadIdx.x, cy = blockIdx.y;
+  if (cx >= p.cw) return;
+  const unsigned i = (unsigned)((long long)cy * p.cw + cx);
+  if (!p.dilated[i]) return;
+  if (cx > 0 && p.dilated[i - 1]) unite(p.parent, i, i - 1, p.error);
+  if (cy > 0) {
+    const unsigned up = i - p.cw;
+    if (cx > 0 && p.dilated[up - 1]) unite(p.parent, i, up - 1, p.error);
+    if (p.dilated[up]) unite(p.parent, i, up, p.error);
+    if (cx + 1 < p.cw && p.dilated[up + 1]) unite(p.parent, i, up + 1, p.error);
+  }
+}
+
+// Flatten and count roots per block (raster order of the flat cell index).
+constexpr int SCAN_BLOCK = 1024;
+__global__ void flatten_kernel(const OpposedParams p) {
+  if (p.counters[0] == 0) return;
+  __shared__ unsigned warp_sums[SCAN_BLOCK / 32];
+  const long long n = (long long)p.cw * p.ch;
+  const long long i = (long long)blockIdx.x * SCAN_BLOCK + threadIdx.x;
+  unsigned root = 0;
+  if (i < n && p.dilated[i]) {
+    const unsigned r = find_root(p.parent, (unsigned)i, p.error);
+    p.labels[i] = r;  // provisional: the component's smallest cell index
+    root = (r == (unsigned)i);
+  }
+  const unsigned ballot = __ballot_sync(0xffffffffu, root);
+  if ((threadIdx.x & 31) == 0) warp_sums[threadIdx.x >> 5] = __popc(ballot);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned s = 0;
+    for (int k = 0; k < SCAN_BLOCK / 32; ++k) s += warp_sums[k];
+    p.block_sums[blockIdx.x] = s;
+  }
+}
+
+// Exclusive scan of the per-block root counts (one block).
+__global__ void scan_blocks_kernel(const OpposedParams p, int blocks) {
+  if (p.counters[0] == 0) return;
+  __shared__ unsigned carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < blocks; base += blockDim.x) {
+    const int k = base + threadIdx.x;
+    const unsigned v = k < blocks ? p.block_sums[k] : 0;
+    // Inclusive warp scan, then across warps through shared memory.
+    unsigned x = v;
+    for (int off = 1; off < 32; off <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, x, off);
+      if ((threadIdx.x & 31) >= off) x += y;
+    }
+    __shared__ unsigned wsum[32];
+    if ((threadIdx.x & 31) == 31) wsum[threadIdx.x >> 5] = x;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      unsigned w = threadIdx.x < blockDim.x / 32 ? wsum[threadIdx.x] : 0;
+      for (int off = 1; off < 32; off <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, w, off);
+        if (threadIdx.x >= off) w += y;
+      }
+      wsum[threadIdx.x] = w;
+    }
+    __syncthreads();
+    const unsigned before = (threadIdx.x >= 32 ? wsum[(threadIdx.x >> 5) - 1] : 0) + x - v;
+    if (k < blocks) p.block_sums[k] = carry + before;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry += before + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) p.counters[1] = carry;
+}
+
+// Compact ids for roots: block offset + rank of the root inside its block.
+__global__ void root_ids_kernel(const OpposedParams p) {
+  if (p.counters[0] == 0) return;
+  __shared__ unsigned warp_sums[SCAN_BLOCK / 32];
+  const long long n = (long long)p.cw * p.ch;
+  const long long i = (long long)blockIdx.x * SCAN_BLOCK + threadIdx.x;
+  const bool root = i < n && p.dilated[i] && p.labels[i] == (unsigned)i;
+  const unsigned ballot = __ballot_sync(0xffffffffu, root);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) warp_sums[warp] = __popc(ballot);
+  __syncthreads();
+  unsigned before = p.block_sums[blockIdx.x];
+  for (int k = 0; k < warp; ++k) before += warp_sums[k];
+  before += __popc(ballot & ((1u << lane) - 1u));
+  // Roots keep their compact id (1-based) in `parent`, which is no longer needed.
+  if (root) p.parent[i] = before + 1;
+}
+
+__global__ void relabel_kernel(const OpposedParams p) {
+  if (p.counters[0] == 0) return;
+  const int cx = blockIdx.x * blockDim.x + threadIdx.x, cy = blockIdx.y;
+  if (cx >= p.cw) return;
+  const long long i = (long long)cy * p.cw + cx;
+  unsigned label = 0;
+  if (p.dilated[i]) label = p.parent[p.labels[i]];
+  if (label >= p.max_labels) {  // cannot happen for 8-connected regions of a 3x3 dilation
+    atomicOr(p.error, OPPOSED_ERROR);
+    label = 0;
+  }
+  p.labels[i] = label;
+  const unsigned clipped = __float_as_uint(p.cells[i].w) >> 3;
+  if (label && clipped) atomicOr(&p.region_clipped[label], clipped);
+}
+
+// 5. wanted (channel, support) slots per region (region_correction.rs:134-178)
+__global__ void wanted_kernel(const OpposedParams p) {
+  if (p.counters[0] == 0) return;
+  const int cx = blockIdx.x * blockDim.x + threadIdx.x, cy = blockIdx.y;
+  if (cx >= p.cw) return;
+  const long long i = (long long)cy * p.cw + cx;
+  const unsigned label = p.labels[i];
+  const Cell c = load_cell(p, cx, cy);
+  const unsigned clipped = c.flags >> 3;
+  if (label == 0 || clipped == 0) return;
+  unsigned bits = 0;
+  for (int ch = 0; ch < 3; ++ch) {
+    if (!(clipped & (1u << ch))) continue;
+    bool has_clean = false;
+    for (int o = 0; o < 3; ++o)
+      if (o != ch && usable(c, o) && clean(c, o)) has_clean = true;
+    if (!has_clean) continue;
+    const int pos = pattern_position(ch, support_mask(c, ch, p.levels));
+    if (pos >= 0) bits |= 1u << (ch * PATTERNS + pos);
+  }
+  if (bits) {
+    atomicOr(&p.wanted[label], bits);
+    atomicOr(&p.wanted[0], bits);
+  }
+}
+
+// 6. region border statistics; pass 0 = moments, pass 1 = trimmed sums.
+__global__ void border_kernel(const OpposedParams p, int pass) {
+  if (p.counters[0] == 0) return;
+  __shared__ double pool[SLOTS][3];
+  __shared__ unsigned pool_n[SLOTS];
+  if (threadIdx.x < SLOTS) {
+    pool[threadIdx.x][0] = pool[threadIdx.x][1] = pool[threadIdx.x][2] = 0.0;
+    pool_n[threadIdx.x] = 0;
+  }
+  __syncthreads();
+  const int cx = blockIdx.x * blockDim.x + threadIdx.x, cy = blockIdx.y;
+  if (cx < p.cw) {
+    const long long i = (long long)cy * p.cw + cx;
+    const unsigned label = p.labels[i];
+    const Cell c = load_cell(p, cx, cy);
+    if (label != 0 && (c.flags >> 3) == 0) {
+      const unsigned rclip = p.region_clipped[label];
+      const unsigned want_r = p.wanted[label], want_any = p.wanted[0];
+      for (int ch = 0; ch < 3; ++ch) {
+        if (!(rclip & (1u << ch))) continue;
+        if (c.m[ch] < BORDER_MIN_FRACTION * p.levels[ch]) continue;
+        unsigned pats[3];
+        support_patterns(ch, pats);
+        for (int k = 0; k < 3; ++k) {
+          const int off = ch * PATTERNS + k;
+          const bool for_region = want_r & (1u << off);
+          const bool for_pool = want_any & (1u << off);
+          if (!for_region && !for_pool) continue;
+          float value;
+          if (!correction(c, ch, pats[k], p.levels, value)) continue;
+          float ratio = 0.0f;
+          const bool has_ratio = log_ratio(c, pats[k], ratio);
+          const double wide = (double)value;
+          auto add = [&](long long slot, bool shared_pool) {
+            double* a = p.acc + slot * 4;
+            if (pass == 0) {
+              if (shared_pool) {
+                atomicAdd(&pool_n[off], 1u);
+                atomicAdd(&pool[off][0], wide);
+                atomicAdd(&pool[off][1], wide * wide);
+              } else {
+                atomicAdd(&a[0], 1.0);
+                atomicAdd(&a[2], wide);
+                atomicAdd(&a[3], wide * wide);
+              }
+            } else {
+              const float* t = p.trim + slot * 2;
+              if (fabsf(value - t[0]) <= t[1]) {
+                const double r = (double)(has_ratio ? ratio : 0.0f);
+                if (shared_pool) {
+                  atomicAdd(&pool_n[off], 1u);
+                  atomicAdd(&pool[off][0], wide);
+                  atomicAdd(&pool[off][2], r);
+                } else {
+                  atomicAdd(&a[1], 1.0);
+                  atomicAdd(&a[2], wide);
+                  atomicAdd(&a[3], r);
+                }
+              }
+            }
+          };
+          if (for_region) add((long long)label * SLOTS + off, false);
+          if (for_pool) add(off, true);
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < SLOTS && pool_n[threadIdx.x]) {
+    double* a = p.acc + threadIdx.x * 4;
+    if (pass == 0) {
+      atomicAdd(&a[0], (double)pool_n[threadIdx.x]);
+      atomicAdd(&a[2], pool[threadIdx.x][0]);
+      atomicAdd(&a[3], pool[threadIdx.x][1]);
+    } else {
+      atomicAdd(&a[1], (double)pool_n[threadIdx.x]);
+      atomicAdd(&a[2], pool[threadIdx.x][0]);
+      atomicAdd(&a[3], pool[threadIdx.x][2]);
+    }
+  }
+}
+
+// Slot::finish_moments (region_correction.rs:73-86): trimming window, then
+// the accumulators restart for the trimmed pass.
+__global__ void finish_moments_kernel(const OpposedParams p) {
+  if (p.counters[0] == 0) return;
+  const unsigned slots = (p.counters[1] + 1) * SLOTS;
+  for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < slots; s += gridDim.x * blockDim.x) {
+    double* a = p.acc + (long long)s * 4;
+    const double count = a[0];
+    if (count != 0.0) {
+      const double mean = a[2] / count;
+      double variance = a[3] / count - mean * mean;
+      if (variance < 0.0) variance = 0.0;
+      p.trim[(long long)s * 2] = (float)mean;
+      p.trim[(long long)s * 2 + 1] = (float)(TRIM_DEVIATIONS * sqrt(variance)) + TRIM_FLOOR;
+    }
+    a[2] = 0.0;
+    a[3] = 0.0;
+  }
+}
+
+// Slot::value (region_correction.rs:90-103)
+__device__ bool slot_value(const OpposedParams& p, long long slot, bool has_ratio, float& offset, bool& hr,
+                           float& ratio) {
+  const double* a = p.acc + slot * 4;
+  if (a[0] < (double)MIN_BORDER_CELLS || a[1] == 0.0) return false;
+  offset = (float)(a[2] / a[1]);
+  hr = has_ratio;
+  if (has_ratio) ratio = (float)(a[3] / a[1]);
+  return true;
+}
+
+__device__ __forceinline__ bool total_less(float a, float b) {
+  if (a == b) return signbit(a) && !signbit(b);
+  return a < b;
+}
+
+// 7. per-site estimate (opposed.rs:86-180, 236-330)
+__global__ void estimate_kernel(const OpposedParams p) {
+  if (p.counters[0] == 0) return;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+  unsigned long long n_rec = 0, n_changed = 0, n_fallback = 0, n_unsup = 0, n_neutral = 0;
+  if (x < p.W) {
+    float& s = p.mosaic[(long long)y * p.W + x];
+    const int ch = color_at(p.cfa, x, y);
+    const float level = p.levels[ch];
+    if (s >= level) {
+      const int tx = x / 2, ty = y / 2;
+      const Cell target = load_cell(p, tx, ty);
+      int support_count = 0;
+      for (int o = 0; o < 3; ++o)
+        if (o != ch && usable(target, o) && clean(target, o)) support_count++;
+      bool ok = false;
+      float estimate = 0.0f;
+      if (support_count != 0) {
+        const unsigned support = support_mask(target, ch, p.levels);
+        float ref;
+        if (reference_value(target, support, ref)) {
+          float tratio = 0.0f;
+          const bool has_tratio = log_ratio(target, support, tratio);
+          float corr[MAX_CANDIDATES];
+          int count = 0;
+          bool has_local = false;
+          float local = 0.0f;
+          int local_radius = 0;
+          for (int radius = 1; radius <= LAST_RADIUS && !has_local; ++radius) {
+            for (int cy = max(ty - radius, 0); cy <= min(ty + radius, p.ch - 1); ++cy)
+              for (int cx = max(tx - radius, 0); cx <= min(tx + radius, p.cw - 1); ++cx) {
+                if (max(abs(tx - cx), abs(ty - cy)) != radius) continue;
+                const Cell cand = load_cell(p, cx, cy);
+                if (!(usable(cand, ch) && clean(cand, ch))) continue;
+                float value;
+                if (!correction(cand, ch, support, p.levels, value)) continue;
+                float cratio = 0.0f;
+                const bool has_cratio = log_ratio(cand, support, cratio);
+                if (!chroma_agrees(support, has_tratio, tratio, has_cratio, cratio)) continue;
+                if (count < MAX_CANDIDATES) corr[count++] = value;
+              }
+            if (count >= MIN_CANDIDATES) {
+              for (int a = 1; a < count; ++a) {  // insertion sort, total order
+                const float v = corr[a];
+                int b = a - 1;
+                while (b >= 0 && total_less(v, corr[b])) {
+                  corr[b + 1] = corr[b];
+                  --b;
+                }
+                corr[b + 1] = v;
+              }
+              const int mid = count / 2;
+              local = count % 2 == 0 ? (corr[mid - 1] + corr[mid]) * 0.5f : corr[mid];
+              local_radius = radius;
+              has_local = true;
+            }
+          }
+          const unsigned label = p.labels[(long long)ty * p.cw + tx];
+          bool has_region = false;
+          float region = 0.0f;
+          const int pos = pattern_position(ch, support);
+          if (pos >= 0) {
+            const int off = ch * PATTERNS + pos;
+            const bool want_ratio = __popc(support) == 2;
+            float bratio = 0.0f;
+            bool has_bratio = false;
+            if (slot_value(p, (long long)label * SLOTS + off, want_ratio, region, has_bratio, bratio) ||
+                slot_value(p, off, want_ratio, region, has_bratio, bratio))
+              has_region = chroma_agrees(support, has_tratio, tratio, has_bratio, bratio);
+          }
+          float correction_value = 0.0f;
+          bool have = true;
+          if (has_local && has_region) {
+            const float weight = (float)(LAST_RADIUS + 1 - local_radius) / (float)LAST_RADIUS;
+            correction_value = weight * local + (1.0f - weight) * region;
+          } else if (has_local) {
+            correction_value = local;
+          } else if (has_region) {
+            correction_value = region;
+          } else {
+            have = false;
+          }
+          if (have) {
+            estimate = ref + correction_value;
+            ok = isfinite(estimate) && estimate > 0.0f;
+          }
+        }
+      }
+      bool neutralise = false;
+      if (!ok) {
+        n_fallback++;
+        if (support_count == 0) n_unsup++;
+        neutralise = true;
+      } else {
+        n_rec++;
+        float bounded = MAX_ESTIMATE_MULT * level;
+        if (estimate < bounded) bounded = estimate;  // f32::min of finite values
+        if (bounded > s) {
+          s = bounded;
+          n_changed++;
+        } else {
+          neutralise = true;
+        }
+      }
+      if (neutralise && p.has_ceiling && s > p.ceiling[ch]) {
+        s = p.ceiling[ch];
+        n_neutral++;
+      }
+    }
+  }
+  unsigned long long v[5] = {n_rec, n_changed, n_fallback, n_unsup, n_neutral};
+  for (int k = 0; k < 5; ++k) {
+    unsigned long long t = v[k];
+    for (int off = 16; off > 0; off >>= 1) t += __shfl_down_sync(0xffffffffu, t, off);
+    if ((threadIdx.x & 31) == 0 && t) atomicAdd(&p.stats[1 + k], t);
+  }
+}
+
+__global__ void copy_suspected_kernel(const OpposedParams p) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) p.stats[0] = p.counters[0];
+}
+
+}  // namespace
+
+// reconstruct_opposed_cancellable on a crop-sized normalized mosaic, in place.
+// d_stats (9 counters) follows OpposedStats; labels_out (optional, device,
+// ceil(w/2)*ceil(h/2)) receives the compact region labels.
+Status run_opposed_labels(Context& ctx, float* mosaic, int W, int H, int cfa, const float levels[3],
+                          const float* ceiling, unsigned long long* d_stats, uint32_t* labels_out,
+                          uint32_t* region_count_out) {
+  const int cw = W / 2 + W % 2, chh = H / 2 + H % 2;
+  const long long cells = (long long)cw * chh;
+  // max_regions (regions.rs:117-124): raw-mask cells of separate regions are >= 4 cells apart.
+  const unsigned max_labels = (unsigned)(((cw + 3) / 4) * ((chh + 3) / 4) + 1);
+  const int scan_blocks = (int)((cells + SCAN_BLOCK - 1) / SCAN_BLOCK);
+  size_t bytes = 0;
+  auto take = [&](size_t n) {
+    const size_t at = bytes;
+    bytes += (n + 255) & ~(size_t)255;
+    return at;
+  };
+  const size_t o_cells = take(sizeof(float4) * cells);
+  const size_t o_dil = take(cells);
+  const size_t o_parent = take(sizeof(unsigned) * cells);
+  const size_t o_labels = take(sizeof(unsigned) * cells);
+  const size_t o_bsum = take(sizeof(unsigned) * scan_blocks);
+  const size_t o_rclip = take(sizeof(unsigned) * max_labels);
+  const size_t o_wanted = take(sizeof(unsigned) * max_labels);
+  const size_t o_acc = take(sizeof(double) * 4 * SLOTS * (size_t)max_labels);
+  const size_t o_trim = take(sizeof(float) * 2 * SLOTS * (size_t)max_labels);
+  const size_t o_cnt = take(sizeof(unsigned) * 4);
+  void* base = nullptr;
+  RD_TRY(device_alloc(ctx, bytes, &base));
+  char* b = static_cast<char*>(base);
+  OpposedParams p{};
+  p.mosaic = mosaic;
+  p.W = W;
+  p.H = H;
+  p.cw = cw;
+  p.ch = chh;
+  p.cfa = cfa;
+  for (int c = 0; c < 3; ++c) {
+    p.levels[c] = levels[c];
+    p.ceiling[c] = ceiling ? ceiling[c] : 0.0f;
+  }
+  p.has_ceiling = ceiling ? 1 : 0;
+  p.cells = reinterpret_cast<float4*>(b + o_cells);
+  p.dilated = reinterpret_cast<unsigned char*>(b + o_dil);
+  p.parent = reinterpret_cast<unsigned*>(b + o_parent);
+  p.labels = reinterpret_cast<unsigned*>(b + o_labels);
+  p.block_sums = reinterpret_cast<unsigned*>(b + o_bsum);
+  p.region_clipped = reinterpret_cast<unsigned*>(b + o_rclip);
+  p.wanted = reinterpret_cast<unsigned*>(b + o_wanted);
+  p.acc = reinterpret_cast<double*>(b + o_acc);
+  p.trim = reinterpret_cast<float*>(b + o_trim);
+  p.max_labels = max_labels;
+  p.stats = d_stats;
+  p.counters = reinterpret_cast<unsigned*>(b + o_cnt);
+  p.error = ctx.d_error;
+  // Zero the per-label tables and counters (labels, dilation and cells are fully written).
+  RD_CUDA_TRY(cudaMemsetAsync(b + o_rclip, 0, o_cnt + 256 - o_rclip, ctx.stream));
+  const long long pixels = (long long)W * H;
+  RD_LAUNCH(ctx, K_OPPOSED, count_kernel<<<(unsigned)((pixels + 255) / 256), 256, 0, ctx.stream>>>(p));
+  const dim3 cgrid((cw + 127) / 128, chh);
+  RD_LAUNCH(ctx, K_OPPOSED, cells_kernel<<<cgrid, 128, 0, ctx.stream>>>(p));
+  RD_LAUNCH(ctx, K_OPPOSED, dilate_kernel<<<cgrid, 128, 0, ctx.stream>>>(p));
+  RD_LAUNCH(ctx, K_OPPOSED, union_kernel<<<cgrid, 128, 0, ctx.stream>>>(p));
+  RD_LAUNCH(ctx, K_OPPOSED, flatten_kernel<<<scan_blocks, SCAN_BLOCK, 0, ctx.stream>>>(p));
+  RD_LAUNCH(ctx, K_OPPOSED, scan_blocks_kernel<<<1, 1024, 0, ctx.stream>>>(p, scan_blocks));
+  RD_LAUNCH(ctx, K_OPPOSED, root_ids_kernel<<<scan_blocks, SCAN_BLOCK, 0, ctx.stream>>>(p));
+  RD_LAUNCH(ctx, K_OPPOSED, relabel_kernel<<<cgrid, 128, 0, ctx.stream>>>(p));
+  RD_LAUNCH(ctx, K_OPPOSED, wanted_kernel<<<cgrid, 128, 0, ctx.stream>>>(p));
+  RD_LAUNCH(ctx, K_OPPOSED, border_kernel<<<cgrid, 128, 0, ctx.stream>>>(p, 0));
+  RD_LAUNCH(ctx, K_OPPOSED, finish_moments_kernel<<<256, 256, 0, ctx.stream>>>(p));
+  RD_LAUNCH(ctx, K_OPPOSED, border_kernel<<<cgrid, 128, 0, ctx.stream>>>(p, 1));
+  RD_LAUNCH(ctx, K_OPPOSED, estimate_kernel<<<dim3((W + 127) / 128, H), 128, 0, ctx.stream>>>(p));
+  RD_LAUNCH(ctx, K_OPPOSED, copy_suspected_kernel<<<1, 32, 0, ctx.stream>>>(p));
+  cudaError_t launch = cudaGetLastError();
+  if (launch == cudaSuccess && labels_out) {
+    // With no suspected site the labelling kernels returned early: report empty labels.
+    launch = cudaMemsetAsync(labels_out, 0, sizeof(uint32_t) * cells, ctx.stream);
+    if (launch == cudaSuccess) {
+      unsigned suspected = 0;
+      launch = cudaMemcpyAsync(&suspected, p.counters, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx.stream);
+      if (launch == cudaSuccess) launch = cudaStreamSynchronize(ctx.stream);
+      if (launch == cudaSuccess && suspected)
+        launch = cudaMemcpyAsync(labels_out, p.labels, sizeof(uint32_t) * cells, cudaMemcpyDeviceToDevice,
+                                 ctx.stream);
+    }
+  }
+  if (launch == cudaSuccess && region_count_out) {
+    unsigned counters[2] = {0, 0};
+    launch = cudaMemcpyAsync(counters, p.counters, sizeof(counters), cudaMemcpyDeviceToHost, ctx.stream);
+    if (launch == cudaSuccess) launch = cudaStreamSynchronize(ctx.stream);
+    *region_count_out = counters[0] ? counters[1] : 0;
+  }
+  device_free(ctx, base, bytes);
+  if (launch != cudaSuccess) return Status{RD_SYNCHRONIZATION, cudaGetErrorString(launch)};
+  return Status{};
+}
+
+Status run_opposed(Context& ctx, float* mosaic, int W, int H, int cfa, const float levels[3], const float* ceiling,
+                   unsigned long long* d_stats, uint32_t* region_count) {
+  return run_opposed_labels(ctx, mosaic, W, H, cfa, levels, ceiling, d_stats, nullptr, region_count);
+}
+
+}  // namespace rd

@@ -1,0 +1,321 @@
+// Lens distortion / TCA gather (crates/optics/src/{plan,resample}.rs) and
+// exact separable area reduction (crates/core/src/resample.rs) on sm_103a.
+//
+// Optics: the per-column and per-row halves of the pre-transform
+// (plan.rs:448-455 and correction.rs input_coordinate_x/y) are resolved on the
+// host in f64 and uploaded as f32 tables, so a pixel starts from two loads.
+// The inverse distortion runs the lensfun Newton iteration in f64 from the f32
+// coordinates (radius sqrt(f64(x*x + y*y)), <= 7 steps, |F| < 1e-5, input kept
+// on non-convergence; Poly3 returns NaN), TCA is applied in f32 and the
+// post-transform back to pixels is f64 narrowed once, as in
+// plan.rs:466-483. Each channel is a 4x4 Catmull-Rom gather with the
+// reference's tap order (resample.rs:21-33); a footprint outside [1, W-2]
+// sets the error word, which the host turns into RD_INVALID_INPUT.
+//
+// Area reduction: the host builds the overlap tables exactly as
+// AreaReductionAxis::new (f64 overlaps narrowed to f32); the horizontal and
+// vertical passes accumulate taps in table order from 0, as the reference.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "rd_internal.cuh"
+
+namespace rd {
+namespace {
+
+constexpr double NEWTON_EPS = 0.00001;
+
+struct OpticsParams {
+  const float* in;   // planar RGB
+  const float* mult; // vignetting multipliers, or null
+  float* out;
+  int W, H;
+  const float* ix;   // per-column input x (f32, lens units)
+  const float* iy;   // per-row input y
+  double cx, cy, unscale;
+  int dist_model;
+  float d0, d1, d2;
+  int tca_model;
+  float tr[3], tb[3];
+  unsigned* error;
+};
+
+__device__ __forceinline__ void undistort(const OpticsParams& p, float x, float y, float& ox, float& oy) {
+  ox = x;
+  oy = y;
+  if (p.dist_model == 0) return;
+  const double rd = sqrt((double)(x * x + y * y));
+  if (rd == 0.0) return;
+  const double a = p.d0, b = p.d1, c = p.d2;
+  double ru = rd;
+  bool converged = false;
+  if (p.dist_model == RD_DISTORTION_POLY3) {
+    const double inv_k1 = (double)(1.0f / p.d0);
+    const double rd_div_k1 = (double)(float)(rd * inv_k1);
+    for (int s = 0; s < 7; ++s) {
+      const double f = ru * ru * ru + ru * inv_k1 - rd_div_k1;
+      if (fabs(f) < NEWTON_EPS) { converged = true; break; }
+      ru -= f / (3.0 * ru * ru + inv_k1);
+    }
+    if (!converged || ru < 0.0) { ox = nanf(""); oy = nanf(""); return; }
+  } else if (p.dist_model == RD_DISTORTION_POLY5) {
+    for (int s = 0; s < 7; ++s) {
+      const double ru2 = ru * ru;
+      const double f = ru * (1.0 + a * ru2 + b * ru2 * ru2) - rd;
+      if (fabs(f) < NEWTON_EPS) { converged = true; break; }
+      ru -= f / (1.0 + 3.0 * a * ru2 + 5.0 * b * ru2 * ru2);
+    }
+    if (!converged || ru < 0.0) return;
+  } else {
+    for (int s = 0; s < 7; ++s) {
+      const double f = ru * (a * ru * ru * ru + b * ru * ru + c * ru + 1.0) - rd;
+      if (fabs(f) < NEWTON_EPS) { converged = true; break; }
+      ru -= f / (4.0 * a * ru * ru * ru + 3.0 * b * ru * ru + 2.0 * c * ru + 1.0);
+    }
+    if (!converged || ru < 0.0) return;
+  }
+  const double ratio = ru / rd;
+  ox = (float)((double)x * ratio);
+  oy = (float)((double)y * ratio);
+}
+
+__device__ __forceinline__ void tca_poly3(const float* ch, float x, float y, float& ox, float& oy) {
+  ox = x;
+  oy = y;
+  const double rd = sqrt((double)(x * x + y * y));
+  if (rd == 0.0) return;
+  const double v = ch[0], c = ch[1], b = ch[2];
+  double ru = rd;
+  bool converged = false;
+  for (int s = 0; s < 7; ++s) {
+    const double ru2 = ru * ru;
+    const double f = b * ru2 * ru + c * ru2 + v * ru - rd;
+    if (fabs(f) < NEWTON_EPS) { converged = true; break; }
+    ru -= f / (3.0 * b * ru2 + 2.0 * c * ru + v);
+  }
+  if (!converged || ru <= 0.0) return;
+  const double ratio = ru / rd;
+  ox = (float)((double)x * ratio);
+  oy = (float)((double)y * ratio);
+}
+
+__device__ __forceinline__ float cubic_weight(float d) {
+  const float a = fabsf(d);
+  if (a <= 1.0f) return 1.5f * a * a * a - 2.5f * a * a + 1.0f;
+  if (a < 2.0f) return -0.5f * a * a * a + 2.5f * a * a - 4.0f * a + 2.0f;
+  return 0.0f;
+}
+
+// resample.rs:3-41. Returns false for a non-finite coordinate or a footprint
+// that leaves the image.
+__device__ __forceinline__ bool cubic_sample(const float* __restrict__ plane, const float* __restrict__ mult, int W,
+                                             int H, float x, float y, float& out) {
+  if (!isfinite(x) || !isfinite(y)) return false;
+  const int fx = (int)floorf(x), fy = (int)floorf(y);
+  if (fx - 1 < 0 || fy - 1 < 0 || fx + 2 >= W || fy + 2 >= H) return false;
+  float value = 0.0f;
+#pragma unroll
+  for (int oy = -1; oy <= 2; ++oy) {
+    const float wy = cubic_weight(y - (float)(fy + oy));
+    const float* row = plane + (long long)(fy + oy) * W;
+    const float* mrow = mult ? mult + (long long)(fy + oy) * W : nullptr;
+#pragma unroll
+    for (int ox = -1; ox <= 2; ++ox) {
+      const float weight = wy * cubic_weight(x - (float)(fx + ox));
+      float sample = __ldg(row + fx + ox);
+      if (mrow) sample = sample * __ldg(mrow + fx + ox);  // the vignetted source value
+      value += sample * weight;
+    }
+  }
+  if (!isfinite(value)) return false;
+  out = value;
+  return true;
+}
+
+__global__ void __launch_bounds__(256) optics_kernel(const OpticsParams p) {
+  const int x = blockIdx.x * 32 + (threadIdx.x & 31);
+  const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
+  if (x >= p.W || y >= p.H) return;
+  float gx, gy;
+  undistort(p, p.ix[x], p.iy[y], gx, gy);
+  bool bad = !isfinite(gx) || !isfinite(gy);
+  float n[6] = {gx, gy, gx, gy, gx, gy};
+  if (p.tca_model == RD_TCA_LINEAR) {
+    n[0] = gx * p.tr[0];
+    n[1] = gy * p.tr[0];
+    n[4] = gx * p.tb[0];
+    n[5] = gy * p.tb[0];
+  } else if (p.tca_model == RD_TCA_POLY3) {
+    tca_poly3(p.tr, gx, gy, n[0], n[1]);
+    tca_poly3(p.tb, gx, gy, n[4], n[5]);
+  }
+  const long long plane = (long long)p.W * p.H;
+  const long long o = (long long)y * p.W + x;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float sx = (float)(((double)n[2 * c] + p.cx) * p.unscale);
+    const float sy = (float)(((double)n[2 * c + 1] + p.cy) * p.unscale);
+    float v = 0.0f;
+    if (!bad && !cubic_sample(p.in + c * plane, p.mult, p.W, p.H, sx, sy, v)) bad = true;
+    p.out[c * plane + o] = v;
+  }
+  if (bad) atomicOr(p.error, 8u);
+}
+
+// Horizontal area pass: one thread per (row, target column, channel-plane).
+__global__ void area_h_kernel(const float* __restrict__ in, const float* __restrict__ mult, int W, int H, int tw,
+                              const int* __restrict__ first,
+                              const int* __restrict__ offset, const int* __restrict__ count,
+                              const float* __restrict__ weights, float* __restrict__ mid) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  const int c = blockIdx.z;
+  if (t >= tw) return;
+  const float* row = in + (long long)c * W * H + (long long)y * W + first[t];
+  const float* mrow = mult ? mult + (long long)y * W + first[t] : nullptr;
+  const float* wt = weights + offset[t];
+  float acc = 0.0f;
+  for (int k = 0; k < count[t]; ++k) {
+    float sample = row[k];
+    if (mrow) sample = sample * mrow[k];
+    acc += sample * wt[k];
+  }
+  mid[(long long)c * tw * H + (long long)y * tw + t] = acc;
+}
+
+__global__ void area_v_kernel(const float* __restrict__ mid, int H, int tw, int th, const int* __restrict__ first,
+                              const int* __restrict__ offset, const int* __restrict__ count,
+                              const float* __restrict__ weights, float* __restrict__ out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = blockIdx.y;
+  const int c = blockIdx.z;
+  if (x >= tw) return;
+  const float* col = mid + (long long)c * tw * H + (long long)first[t] * tw + x;
+  const float* wt = weights + offset[t];
+  float acc = 0.0f;
+  for (int k = 0; k < count[t]; ++k) acc += col[(long long)k * tw] * wt[k];
+  out[(long long)c * tw * th + (long long)t * tw + x] = acc;
+}
+
+struct AxisTable {
+  std::vector<int> first, offset, count;
+  std::vector<float> weights;
+};
+
+// AreaReductionAxis::new (resample.rs:45-113).
+AxisTable build_axis(int source, int target) {
+  AxisTable a;
+  const double scale = (double)source / (double)target;
+  for (int t = 0; t < target; ++t) {
+    const double left = (double)t * scale, right = (double)(t + 1) * scale;
+    const int first = (int)std::floor(left);
+    const int end = std::min((int)std::ceil(right), source);
+    a.first.push_back(first);
+    a.offset.push_back((int)a.weights.size());
+    a.count.push_back(end - first);
+    for (int s = first; s < end; ++s) {
+      const double overlap = std::min(right, (double)(s + 1)) - std::max(left, (double)s);
+      a.weights.push_back((float)(overlap / scale));
+    }
+  }
+  return a;
+}
+
+}  // namespace
+
+Status run_optics_gather(Context& ctx, const rd_optics_desc& o, const float* rgb_in, const float* mult,
+                         float* rgb_out) {
+  const int W = (int)o.width, H = (int)o.height;
+  // Per-axis pre-transform, plan.rs:448-455 / correction.rs input_coordinate_x,y.
+  std::vector<float> tab((size_t)W + H);
+  const double cpx = o.center_x * o.norm_unscale, cpy = o.center_y * o.norm_unscale;
+  for (int x = 0; x < W; ++x) {
+    const double mapped = cpx + ((double)x - cpx) / (double)o.scale;
+    tab[x] = (float)(mapped * o.norm_scale - o.center_x);
+  }
+  for (int y = 0; y < H; ++y) {
+    const double mapped = cpy + ((double)y - cpy) / (double)o.scale;
+    tab[W + y] = (float)(mapped * o.norm_scale - o.center_y);
+  }
+  void* d = nullptr;
+  RD_TRY(device_alloc(ctx, sizeof(float) * tab.size(), &d));
+  float* dtab = static_cast<float*>(d);
+  RD_CUDA_TRY(cudaMemcpyAsync(dtab, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice, ctx.stream));
+  OpticsParams p{};
+  p.in = rgb_in;
+  p.mult = mult;
+  p.out = rgb_out;
+  p.W = W;
+  p.H = H;
+  p.ix = dtab;
+  p.iy = dtab + W;
+  p.cx = o.center_x;
+  p.cy = o.center_y;
+  p.unscale = o.norm_unscale;
+  p.dist_model = o.distortion_model;
+  p.d0 = o.distortion[0];
+  p.d1 = o.distortion[1];
+  p.d2 = o.distortion[2];
+  p.tca_model = o.tca_model;
+  for (int c = 0; c < 3; ++c) {
+    p.tr[c] = o.tca_red[c];
+    p.tb[c] = o.tca_blue[c];
+  }
+  p.error = ctx.d_error;
+  dim3 grid((W + 31) / 32, (H + 7) / 8);
+  RD_LAUNCH(ctx, K_OPTICS, optics_kernel<<<grid, 256, 0, ctx.stream>>>(p));
+  const cudaError_t launch = cudaGetLastError();
+  device_free(ctx, dtab, sizeof(float) * tab.size());
+  if (launch != cudaSuccess) return Status{RD_SYNCHRONIZATION, cudaGetErrorString(launch)};
+  return Status{};
+}
+
+size_t area_reduce_scratch_floats(int W, int H, int tw, int th) {
+  (void)W;
+  (void)th;
+  return (size_t)3 * tw * H;
+}
+
+Status run_area_reduce(Context& ctx, const float* rgb, const float* mult, int W, int H, int tw, int th, float* out,
+                       float* mid) {
+  const AxisTable ha = build_axis(W, tw), va = build_axis(H, th);
+  const size_t ints = ha.first.size() * 3 + va.first.size() * 3;
+  const size_t bytes = ints * sizeof(int) + (ha.weights.size() + va.weights.size()) * sizeof(float);
+  std::vector<unsigned char> host(bytes);
+  unsigned char* q = host.data();
+  auto put = [&](const void* src, size_t n) {
+    std::memcpy(q, src, n);
+    q += n;
+  };
+  put(ha.first.data(), tw * sizeof(int));
+  put(ha.offset.data(), tw * sizeof(int));
+  put(ha.count.data(), tw * sizeof(int));
+  put(va.first.data(), th * sizeof(int));
+  put(va.offset.data(), th * sizeof(int));
+  put(va.count.data(), th * sizeof(int));
+  put(ha.weights.data(), ha.weights.size() * sizeof(float));
+  put(va.weights.data(), va.weights.size() * sizeof(float));
+  void* d = nullptr;
+  RD_TRY(device_alloc(ctx, bytes, &d));
+  unsigned char* b = static_cast<unsigned char*>(d);
+  RD_CUDA_TRY(cudaMemcpyAsync(b, host.data(), bytes, cudaMemcpyHostToDevice, ctx.stream));
+  const int* hf = reinterpret_cast<const int*>(b);
+  const int* ho = hf + tw;
+  const int* hc = ho + tw;
+  const int* vf = hc + tw;
+  const int* vo = vf + th;
+  const int* vc = vo + th;
+  const float* hw = reinterpret_cast<const float*>(vc + th);
+  const float* vw = hw + ha.weights.size();
+  RD_LAUNCH(ctx, K_AREA_H, area_h_kernel<<<dim3((tw + 127) / 128, H, 3), 128, 0, ctx.stream>>>(rgb, mult, W, H, tw, hf, ho, hc, hw, mid));
+  RD_LAUNCH(ctx, K_AREA_V, area_v_kernel<<<dim3((tw + 127) / 128, th, 3), 128, 0, ctx.stream>>>(mid, H, tw, th, vf, vo, vc, vw, out));
+  const cudaError_t launch = cudaGetLastError();
+  device_free(ctx, b, bytes);
+  if (launch != cudaSuccess) return Status{RD_SYNCHRONIZATION, cudaGetErrorString(launch)};
+  return Status{};
+}
+
+}  // namespace rd

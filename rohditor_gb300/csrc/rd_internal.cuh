@@ -1,0 +1,209 @@
+// Internal declarations shared by the library's translation units.
+//
+// Device layout conventions:
+//  * mosaics: row-major, pitch = width (f32) or row_stride (u16 input);
+//  * camera / Rec.2020 RGB: three planar f32 planes R, G, B, each [h][w],
+//    allocated as one buffer of 3*w*h floats so a plane is `base + c*w*h`;
+//  * sRGB8 output: interleaved u8 [h][3w], the host format.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/rd_gpu.h"
+
+namespace rd {
+
+// ------------------------------------------------------------------ errors
+struct Status {
+  rd_status code = RD_OK;
+  std::string message;
+  bool ok() const { return code == RD_OK; }
+};
+
+#define RD_CUDA_TRY(expr)                                                                        \
+  do {                                                                                           \
+    cudaError_t rd_err_ = (expr);                                                                \
+    if (rd_err_ != cudaSuccess)                                                                  \
+      return ::rd::Status{RD_SYNCHRONIZATION, std::string(#expr) + ": " + cudaGetErrorString(rd_err_)}; \
+  } while (0)
+
+#define RD_TRY(expr)                 \
+  do {                               \
+    ::rd::Status rd_st_ = (expr);    \
+    if (!rd_st_.ok()) return rd_st_; \
+  } while (0)
+
+// ------------------------------------------------------------------ context
+// Kernel families timed by the optional per-launch event bracketing.
+enum KernelFamily {
+  K_NORMALIZE, K_OPPOSED, K_MHC, K_RCD, K_AMAZE, K_RL_INIT, K_RL_MASK, K_RL_ITER, K_RL_APPLY, K_VIGNETTE,
+  K_OPTICS, K_AREA_H, K_AREA_V, K_WB_MATRIX, K_COLOR, K_SYNTH, K_FAMILY_COUNT
+};
+static_assert(K_FAMILY_COUNT == RD_KERNEL_FAMILIES, "family table size");
+const char* kernel_family_name(int family);
+
+struct Context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  uint64_t budget = 0;     // 0 = unlimited
+  uint64_t reserved = 0;   // bytes currently held by this context
+  uint64_t launches = 0;   // kernels launched by this library on this context
+  std::string last_error;
+  // Error word written by kernels (bounds/footprint/non-finite), read after a stage.
+  uint32_t* d_error = nullptr;
+  // AMaZE per-CTA scratch slots (kept across calls).
+  float* amaze_scratch = nullptr;
+  size_t amaze_slots = 0;
+  int sm_count = 0;
+  cudaEvent_t ev[8] = {};
+  // Sizes of the allocations handed out through rd_device_alloc.
+  std::unordered_map<void*, size_t> user_allocs;
+  // Measurement: user event slots, an L2 flush buffer and per-family kernel timing.
+  cudaEvent_t user_ev[64] = {};
+  void* flush_buf = nullptr;
+  size_t flush_bytes = 0;
+  bool timing = false;
+  std::vector<cudaEvent_t> event_pool;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+  double family_ms[K_FAMILY_COUNT] = {};
+  uint64_t family_launches[K_FAMILY_COUNT] = {};
+};
+
+// Brackets one kernel launch with events when kernel timing is enabled, and
+// counts the launch either way.
+struct LaunchScope {
+  Context& ctx;
+  int family;
+  cudaEvent_t a = nullptr, b = nullptr;
+  LaunchScope(Context& c, int f);
+  ~LaunchScope();
+};
+// Resolves the pending launch events into per-family totals (after a sync).
+void resolve_kernel_timing(Context& ctx);
+
+#define RD_LAUNCH(ctx, family, ...)              \
+  do {                                           \
+    ::rd::LaunchScope rd_scope_((ctx), (family)); \
+    __VA_ARGS__;                                 \
+  } while (0)
+
+Status reserve(Context& ctx, size_t bytes);
+void release(Context& ctx, size_t bytes);
+Status device_alloc(Context& ctx, size_t bytes, void** out);
+void device_free(Context& ctx, void* ptr, size_t bytes);
+Status check_kernel_error(Context& ctx, const char* stage);
+
+// ------------------------------------------------------------------ mosaic source
+// Per-sample view of the (cropped, normalized, highlight-processed) mosaic,
+// optionally scaled by the demosaic channel balance. Either reads the raw u16
+// sensor data and applies normalization + Clip on the fly (fused path), or
+// reads an already reconstructed f32 mosaic (after Opposed).
+struct MosaicSource {
+  const uint16_t* raw;    // sensor samples, or null
+  const float* f32;       // crop-sized normalized mosaic (pitch = width), or null
+  long long row_stride;   // raw row stride in samples
+  int crop_x, crop_y;
+  int sensor_cfa;         // CFA at sensor (0,0)
+  int width, height;      // crop size
+  int cfa;                // CFA at crop (0,0)
+  int black_w, black_h;
+  int white_count;
+  int clip;               // 1: apply Clip ceilings after normalization
+  float clip_levels[3];
+  float fwd[3];           // balance multipliers (1,1,1 when not balanced)
+  float black[RD_MAX_LEVEL_PATTERN];
+  float white[RD_MAX_LEVEL_PATTERN];
+};
+
+__host__ __device__ inline int color_at(int pattern, int x, int y) {
+  // BayerPattern::color_at: RGGB, BGGR, GRBG, GBRG packed 2 bits per site.
+  const unsigned table = pattern == 0 ? 0x94u : pattern == 1 ? 0x16u : pattern == 2 ? 0x61u : 0x49u;
+  return (table >> (2 * (((y & 1) << 1) | (x & 1)))) & 3;
+}
+
+__host__ __device__ inline int shifted_cfa(int pattern, int x, int y) {
+  const int px = x & 1, py = y & 1;
+  if (!px && !py) return pattern;
+  // A column shift maps RGGB<->GRBG and BGGR<->GBRG (p ^ 2); a row shift maps
+  // RGGB<->GBRG and BGGR<->GRBG (3 - p).
+  int p = pattern;
+  if (px) p ^= 2;
+  if (py) p = 3 - p;
+  return p;
+}
+
+// Normalized sample at crop coordinates (x, y) before any highlight step:
+// NormalizationContract::normalize with levels at sensor coordinates.
+__device__ __forceinline__ float source_normalized(const MosaicSource& s, int x, int y) {
+  if (s.f32) return s.f32[(long long)y * s.width + x];
+  const int sx = s.crop_x + x, sy = s.crop_y + y;
+  const float sample = (float)s.raw[(long long)sy * s.row_stride + sx];
+  const int bi = (sy % s.black_h) * s.black_w + (sx % s.black_w);
+  const float black = s.black[bi];
+  float white;
+  if (s.white_count == 1) white = s.white[0];
+  else if (s.white_count == 3) white = s.white[color_at(s.sensor_cfa, sx, sy)];
+  else white = s.white[bi];
+  return __fdiv_rn(__fsub_rn(sample, black), __fsub_rn(white, black));
+}
+
+// Normalized, highlight-processed sample (Clip applied when selected), before balance.
+__device__ __forceinline__ float source_linear(const MosaicSource& s, int x, int y) {
+  float v = source_normalized(s, x, y);
+  if (s.clip) {
+    const float limit = s.clip_levels[color_at(s.cfa, x, y)];
+    if (v > limit) v = limit;
+  }
+  return v;
+}
+
+__device__ __forceinline__ float source_balanced(const MosaicSource& s, int x, int y) {
+  const float v = source_linear(s, x, y);
+  return __fmul_rn(v, s.fwd[color_at(s.cfa, x, y)]);
+}
+
+// mirror_coordinate (whole-sample reflection, parity preserving).
+__device__ __forceinline__ int mirror_index(int index, int length) {
+  if (length <= 1) return 0;
+  const int period = 2 * (length - 1);
+  int w = index % period;
+  if (w < 0) w += period;
+  return w < period - w ? w : period - w;
+}
+
+// ------------------------------------------------------------------ stage launchers
+// Each returns after enqueueing on ctx.stream. Planar RGB outputs.
+Status launch_normalize(Context& ctx, const MosaicSource& src, float* out, unsigned long long* clip_stats);
+Status run_opposed(Context& ctx, float* mosaic, int width, int height, int cfa, const float levels[3],
+                   const float* ceiling, unsigned long long* d_stats, uint32_t* region_count);
+Status run_opposed_labels(Context& ctx, float* mosaic, int width, int height, int cfa, const float levels[3],
+                          const float* ceiling, unsigned long long* d_stats, uint32_t* labels_out,
+                          uint32_t* region_count);
+Status run_demosaic(Context& ctx, const MosaicSource& src, int algorithm, float* rgb, unsigned long long* clip_stats);
+Status run_capture(Context& ctx, float* rgb, int width, int height, const rd_detail_desc& detail,
+                   const rd_optics_desc* vignetting);
+// Vignetting multiplier plane (width*height f32) of an optics execution.
+Status run_vignette_plane(Context& ctx, const rd_optics_desc& optics, float* mult);
+// Distortion / TCA gather; `mult` (optional) is the vignetting plane applied to
+// each source sample as it is read.
+Status run_optics_gather(Context& ctx, const rd_optics_desc& optics, const float* rgb_in, const float* mult,
+                         float* rgb_out);
+Status run_area_reduce(Context& ctx, const float* rgb, const float* mult, int width, int height, int tw, int th,
+                       float* out, float* scratch);
+size_t area_reduce_scratch_floats(int width, int height, int tw, int th);
+Status run_wb_matrix(Context& ctx, float* rgb, size_t pixels, const float gains[3], const float matrix[9]);
+Status run_color_output(Context& ctx, const float* rgb, int width, int height, const rd_color_desc& color,
+                        bool camera_native, uint8_t* srgb, unsigned long long* d_hist);
+Status run_synth(Context& ctx, const rd_synth_desc& desc, uint16_t* out);
+
+// Host contract helpers.
+int gaussian_kernel(float sigma, float* weights, int max_taps);
+Status optics_plan(rd_optics_desc& optics, float crop, float real_focal, float cx, float cy);
+void standard_base_lut(float* lut);
+
+}  // namespace rd

@@ -1,0 +1,487 @@
+"""Host-side mirror of the reference's `rohditor-gpu` processor interface.
+
+The classes keep the reference's names, argument meaning and error behaviour
+so an engine written against crates/gpu reads the same here:
+
+  GpuPreviewError        crates/gpu/src/lib.rs:55-111 (variants, is_routing)
+  GpuSensorProcessor     crates/gpu/src/sensor/normalize.rs:75-157 (new, set_budget)
+                         crates/gpu/src/sensor/develop.rs:54-141 (supports, develop)
+  GpuDevelopedSource     crates/gpu/src/sensor/develop.rs:28-47
+  GpuSpatialProcessor    crates/gpu/src/spatial/reduction.rs:15 (reduce_preview)
+  GpuPreviewProcessor    crates/gpu/src/preview/processor.rs:1011-1060,1518 (render, histogram)
+
+Everything runs in librd_gpu.so through the C ABI; numpy arrays are the host
+buffers and nothing here computes pixels.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import weakref
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _ffi
+
+
+class GpuPreviewError(RuntimeError):
+    """A failed call; `variant` is the GpuPreviewError variant name."""
+
+    def __init__(self, code: int, message: str):
+        self.code = code
+        self.variant = _ffi.STATUS_NAMES[code] if 0 <= code < len(_ffi.STATUS_NAMES) else "Unknown"
+        super().__init__(f"{self.variant}: {message}")
+
+    def is_routing(self) -> bool:
+        """UnsupportedEdits and OverBudget keep the device; callers route to another path."""
+        return bool(_ffi.load().rd_status_is_routing(self.code))
+
+
+def _f32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _ptr(a: np.ndarray, ctype):
+    return a.ctypes.data_as(ctypes.POINTER(ctype))
+
+
+# ---------------------------------------------------------------- contracts
+@dataclass
+class SensorDescription:
+    """NormalizationContract + SensorDevelopmentDescription (sensor.rs:56-67, 280-298)."""
+
+    sensor_width: int
+    sensor_height: int
+    cfa: str = "RGGB"
+    crop: tuple[int, int, int, int] | None = None  # x, y, w, h
+    black: tuple[float, ...] = (0.0,)
+    black_repeat: tuple[int, int] = (1, 1)
+    white: tuple[float, ...] = (1.0,)
+    highlight: str = "off"
+    clip_levels: tuple[float, float, float] = (1.0, 1.0, 1.0)
+    detection_levels: tuple[float, float, float] = (1.0, 1.0, 1.0)
+    neutral_ceiling: tuple[float, float, float] | None = None
+    demosaic: str = "amaze"
+    demosaic_balance: tuple[float, float, float] = (1.0, 1.0, 1.0)
+
+    def to_c(self) -> _ffi.SensorDesc:
+        d = _ffi.SensorDesc()
+        d.sensor_width, d.sensor_height = self.sensor_width, self.sensor_height
+        cx, cy, cw, ch = self.crop or (0, 0, self.sensor_width, self.sensor_height)
+        d.crop_x, d.crop_y, d.crop_width, d.crop_height = cx, cy, cw, ch
+        d.cfa = _ffi.CFA[self.cfa.upper()]
+        d.black_repeat_w, d.black_repeat_h = self.black_repeat
+        for i, v in enumerate(self.black):
+            d.black[i] = v
+        d.white_count = len(self.white)
+        for i, v in enumerate(self.white):
+            d.white[i] = v
+        d.highlight = _ffi.HIGHLIGHT[self.highlight]
+        for c in range(3):
+            d.clip_levels[c] = self.clip_levels[c]
+            d.detection_levels[c] = self.detection_levels[c]
+            d.demosaic_balance[c] = self.demosaic_balance[c]
+        if self.neutral_ceiling is not None:
+            d.has_neutral_ceiling = 1
+            for c in range(3):
+                d.neutral_ceiling[c] = self.neutral_ceiling[c]
+        d.demosaic = _ffi.DEMOSAIC[self.demosaic]
+        return d
+
+    @property
+    def crop_size(self) -> tuple[int, int]:
+        if self.crop:
+            return self.crop[2], self.crop[3]
+        return self.sensor_width, self.sensor_height
+
+
+DETECTION_SAFETY_MARGIN = np.float32(0.987)  # crates/highlight/src/lib.rs:27
+
+
+def clip_levels(threshold: float, gains) -> tuple[float, float, float]:
+    """HighlightExecution::Clip ceilings from the user WB gains (sensor.rs:407-420)."""
+    g = [np.float32(x) for x in gains]
+    common = np.float32(np.float32(threshold) * DETECTION_SAFETY_MARGIN) * min(g[0], g[1], g[2])
+    return tuple(float(np.float32(common / x)) for x in g)
+
+
+def opposed_levels(threshold: float, as_shot) -> tuple[tuple[float, ...], tuple[float, ...]]:
+    """Opposed detection levels and neutral ceiling from the as-shot gains (sensor.rs:421-455)."""
+    level = np.float32(np.float32(threshold) * DETECTION_SAFETY_MARGIN)
+    g = [np.float32(x) for x in as_shot]
+    common = np.float32(level * min(g[0], g[1], g[2]))
+    return (float(level),) * 3, tuple(float(np.float32(common / x)) for x in g)
+
+
+@dataclass
+class CaptureContract:
+    """CaptureSharpeningContract (sharpening.rs:17-68) with an explicit iteration count."""
+
+    amount: float = 0.5
+    radius: float = 0.6
+    noise_protection: float = 0.5
+    ceilings: tuple[float, float, float] = (1.0, 1.0, 1.0)
+    iterations: int = 8
+    enabled: bool = True
+
+    def to_c(self) -> _ffi.DetailDesc:
+        d = _ffi.DetailDesc()
+        d.enabled = 1 if self.enabled else 0
+        d.amount, d.radius, d.noise_protection = self.amount, self.radius, self.noise_protection
+        for c in range(3):
+            d.ceilings[c] = self.ceilings[c]
+        d.iterations = self.iterations
+        return d
+
+
+@dataclass
+class OpticsExecution:
+    """OpticsExecution (crates/optics/src/plan.rs:37-50), resolved on the host."""
+
+    width: int
+    height: int
+    distortion: str = "none"
+    distortion_k: tuple[float, float, float] = (0.0, 0.0, 0.0)
+    tca: str = "none"
+    tca_red: tuple[float, float, float] = (1.0, 0.0, 0.0)
+    tca_blue: tuple[float, float, float] = (1.0, 0.0, 0.0)
+    vignetting_k: tuple[float, float, float] | None = None
+    crop_factor: float = 1.0
+    real_focal: float = 35.0
+    lens_center: tuple[float, float] = (0.0, 0.0)
+    _c: _ffi.OpticsDesc | None = field(default=None, repr=False)
+
+    def to_c(self) -> _ffi.OpticsDesc:
+        if self._c is not None:
+            return self._c
+        d = _ffi.OpticsDesc()
+        d.width, d.height = self.width, self.height
+        d.distortion_model = _ffi.DISTORTION[self.distortion]
+        d.tca_model = _ffi.TCA[self.tca]
+        for c in range(3):
+            d.distortion[c] = self.distortion_k[c]
+            d.tca_red[c] = self.tca_red[c]
+            d.tca_blue[c] = self.tca_blue[c]
+        if self.vignetting_k is not None:
+            d.vignetting = 1
+            for c in range(3):
+                d.vignetting_k[c] = self.vignetting_k[c]
+        rc = _ffi.load().rd_optics_plan(ctypes.byref(d), self.crop_factor, self.real_focal, *self.lens_center)
+        if rc != 0:
+            raise GpuPreviewError(rc, "optics plan failed (no safe automatic scale)")
+        self._c = d
+        return d
+
+
+@dataclass
+class ColorContract:
+    """White balance, camera matrix and the global adjustment chain with resolved LUTs."""
+
+    wb_gains: tuple[float, float, float] = (1.0, 1.0, 1.0)
+    camera_to_rec2020: tuple[float, ...] = (1, 0, 0, 0, 1, 0, 0, 0, 1)
+    exposure_ev: float = 0.0
+    base_lut: np.ndarray | None = None
+    tone_lut: np.ndarray | None = None
+    saturation: float = 1.0
+    vibrance: float = 0.0
+    hsl: np.ndarray | None = None       # 8 x 3
+    grading: np.ndarray | None = None   # 3 x 3
+
+    def to_c(self) -> _ffi.ColorDesc:
+        d = _ffi.ColorDesc()
+        for c in range(3):
+            d.wb_gains[c] = self.wb_gains[c]
+        for k in range(9):
+            d.camera_to_rec2020[k] = self.camera_to_rec2020[k]
+        d.exposure_ev = self.exposure_ev
+        if self.base_lut is not None:
+            d.has_base_lut = 1
+            ctypes.memmove(d.base_lut, _f32(self.base_lut).ctypes.data, 4096 * 4)
+        if self.tone_lut is not None:
+            d.has_tone_lut = 1
+            ctypes.memmove(d.tone_lut, _f32(self.tone_lut).ctypes.data, 4096 * 4)
+        d.saturation, d.vibrance = self.saturation, self.vibrance
+        if self.hsl is not None:
+            d.has_hsl = 1
+            ctypes.memmove(d.hsl, _f32(self.hsl).ctypes.data, 24 * 4)
+        if self.grading is not None:
+            d.has_grading = 1
+            ctypes.memmove(d.grading, _f32(self.grading).ctypes.data, 9 * 4)
+        return d
+
+
+def standard_base_lut() -> np.ndarray:
+    """BaseRenderingLut::standard_v1 values (crates/core/src/rendering.rs:36-50)."""
+    out = np.zeros(4096, dtype=np.float32)
+    _ffi.load().rd_standard_base_lut(_ptr(out, ctypes.c_float))
+    return out
+
+
+# ---------------------------------------------------------------- processors
+class Device:
+    """One CUDA context (stream + budgeted memory pool) on one GPU."""
+
+    def __init__(self, device: int = 0, budget_bytes: int = 0):
+        self.lib = _ffi.load()
+        h = ctypes.c_void_p()
+        rc = self.lib.rd_ctx_create(device, budget_bytes, ctypes.byref(h))
+        if rc != 0:
+            raise GpuPreviewError(rc, f"could not create a context on device {device}")
+        self.handle = h
+        # Resident objects must be released before the context that owns their memory.
+        self._children = weakref.WeakSet()
+
+    def check(self, rc: int):
+        if rc != 0:
+            raise GpuPreviewError(rc, self.lib.rd_ctx_last_error(self.handle).decode())
+
+    def set_budget(self, budget_bytes: int):
+        self.check(self.lib.rd_ctx_set_budget(self.handle, budget_bytes))
+
+    def synchronize(self):
+        self.check(self.lib.rd_ctx_synchronize(self.handle))
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(self.lib.rd_ctx_kernel_launches(self.handle))
+
+    def close(self):
+        if self.handle:
+            for child in list(self._children):
+                child.release()
+            self.lib.rd_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class GpuDevelopedSource:
+    """Full-resolution camera RGB resident on the device."""
+
+    def __init__(self, device: Device, handle: ctypes.c_void_p, metrics: _ffi.Metrics):
+        self.device, self.handle, self.metrics = device, handle, metrics
+        device._children.add(self)
+        w, h = ctypes.c_uint32(), ctypes.c_uint32()
+        device.check(device.lib.rd_source_dimensions(handle, ctypes.byref(w), ctypes.byref(h)))
+        self.width, self.height = w.value, h.value
+
+    def download(self) -> np.ndarray:
+        out = np.empty((self.height, 3 * self.width), dtype=np.float32)
+        self.device.check(self.device.lib.rd_source_download(self.device.handle, self.handle, _ptr(out, ctypes.c_float)))
+        return out
+
+    def release(self):
+        if self.handle and self.device.handle:
+            self.device.lib.rd_source_release(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+class GpuBase:
+    """Reduced linear Rec.2020 base resident on the device."""
+
+    def __init__(self, device: Device, handle: ctypes.c_void_p, metrics: _ffi.Metrics):
+        self.device, self.handle, self.metrics = device, handle, metrics
+        device._children.add(self)
+        w, h = ctypes.c_uint32(), ctypes.c_uint32()
+        device.check(device.lib.rd_base_dimensions(handle, ctypes.byref(w), ctypes.byref(h)))
+        self.width, self.height = w.value, h.value
+
+    def download(self) -> np.ndarray:
+        out = np.empty((self.height, 3 * self.width), dtype=np.float32)
+        self.device.check(self.device.lib.rd_base_download(self.device.handle, self.handle, _ptr(out, ctypes.c_float)))
+        return out
+
+    def release(self):
+        if self.handle and self.device.handle:
+            self.device.lib.rd_base_release(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+class GpuSensorProcessor:
+    """normalize -> highlight -> demosaic -> capture sharpening on the device."""
+
+    def __init__(self, device: Device):
+        self.device = device
+
+    def set_budget(self, budget_bytes: int):
+        self.device.set_budget(budget_bytes)
+
+    @staticmethod
+    def supports(description: SensorDescription) -> bool:
+        d = description.to_c()
+        return bool(_ffi.load().rd_supports(ctypes.byref(d)))
+
+    def develop(self, mosaic: np.ndarray, description: SensorDescription, capture: CaptureContract | None = None,
+                cancel: np.ndarray | None = None) -> GpuDevelopedSource:
+        mosaic = np.ascontiguousarray(mosaic, dtype=np.uint16)
+        row_stride = mosaic.shape[1]
+        d = description.to_c()
+        detail = capture.to_c() if capture is not None else None
+        out = ctypes.c_void_p()
+        m = _ffi.Metrics()
+        cancel_ptr = cancel.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)) if cancel is not None else None
+        self.device.check(self.device.lib.rd_develop(
+            self.device.handle, _ptr(mosaic, ctypes.c_uint16), row_stride, ctypes.byref(d),
+            ctypes.byref(detail) if detail is not None else None, cancel_ptr, ctypes.byref(out), ctypes.byref(m)))
+        return GpuDevelopedSource(self.device, out, m)
+
+    def develop_device(self, d_mosaic: int, row_stride: int, description: SensorDescription,
+                       capture: CaptureContract | None = None) -> GpuDevelopedSource:
+        d = description.to_c()
+        detail = capture.to_c() if capture is not None else None
+        out = ctypes.c_void_p()
+        m = _ffi.Metrics()
+        self.device.check(self.device.lib.rd_develop_device(
+            self.device.handle, ctypes.c_void_p(d_mosaic), row_stride, ctypes.byref(d),
+            ctypes.byref(detail) if detail is not None else None, None, ctypes.byref(out), ctypes.byref(m)))
+        return GpuDevelopedSource(self.device, out, m)
+
+
+class GpuSpatialProcessor:
+    """Optics (vignetting, distortion, TCA) + exact area reduction + WB/matrix to Rec.2020."""
+
+    def __init__(self, device: Device):
+        self.device = device
+
+    def reduce_preview(self, source: GpuDevelopedSource, optics: OpticsExecution | None, target: tuple[int, int],
+                       wb_gains, camera_to_rec2020) -> GpuBase:
+        o = optics.to_c() if optics is not None else None
+        g = _f32(wb_gains)
+        m = _f32(camera_to_rec2020).reshape(-1)
+        out = ctypes.c_void_p()
+        met = _ffi.Metrics()
+        self.device.check(self.device.lib.rd_spatial(
+            self.device.handle, source.handle, ctypes.byref(o) if o is not None else None, target[0], target[1],
+            _ptr(g, ctypes.c_float), _ptr(m, ctypes.c_float), ctypes.byref(out), ctypes.byref(met)))
+        return GpuBase(self.device, out, met)
+
+
+@dataclass
+class Histogram:
+    """R, G, B and luma bins plus shadow/highlight clip counts (histogram.rs:13-21)."""
+
+    red: np.ndarray
+    green: np.ndarray
+    blue: np.ndarray
+    luminance: np.ndarray
+    shadow_clipped: np.ndarray
+    highlight_clipped: np.ndarray
+
+
+class GpuPreviewProcessor:
+    """Adjustments + sRGB 8-bit output + histogram of that output."""
+
+    def __init__(self, device: Device):
+        self.device = device
+
+    def render(self, base: GpuBase, color: ColorContract) -> tuple[np.ndarray, Histogram]:
+        c = color.to_c()
+        out = np.empty((base.height, 3 * base.width), dtype=np.uint8)
+        hist = np.zeros(1024, dtype=np.uint64)
+        clipped = np.zeros(6, dtype=np.uint64)
+        self.device.check(self.device.lib.rd_render(
+            self.device.handle, base.handle, ctypes.byref(c), _ptr(out, ctypes.c_uint8), _ptr(hist, ctypes.c_uint64),
+            _ptr(clipped, ctypes.c_uint64), None))
+        return out, Histogram(hist[0:256], hist[256:512], hist[512:768], hist[768:1024], clipped[:3], clipped[3:])
+
+    def render_device(self, base: GpuBase, color_c: _ffi.ColorDesc):
+        self.device.check(self.device.lib.rd_render_device(self.device.handle, base.handle, ctypes.byref(color_c), None))
+
+
+# ---------------------------------------------------------------- stage API
+class Stages:
+    """The crates' stage functions, each run on the device with host buffers."""
+
+    def __init__(self, device: Device):
+        self.device = device
+        self.lib = device.lib
+
+    def highlight(self, mosaic: np.ndarray, description: SensorDescription) -> tuple[np.ndarray, np.ndarray]:
+        mosaic = np.ascontiguousarray(mosaic, dtype=np.uint16)
+        d = description.to_c()
+        w, h = description.crop_size
+        out = np.empty((h, w), dtype=np.float32)
+        stats = np.zeros(9, dtype=np.uint64)
+        self.device.check(self.lib.rd_stage_highlight(self.device.handle, _ptr(mosaic, ctypes.c_uint16), mosaic.shape[1],
+                                                      ctypes.byref(d), _ptr(out, ctypes.c_float),
+                                                      _ptr(stats, ctypes.c_uint64)))
+        return out, stats
+
+    def opposed(self, mosaic: np.ndarray, cfa: str, levels, ceiling=None):
+        """reconstruct_opposed on a normalized mosaic: (mosaic, stats[9], cell labels, region count)."""
+        mosaic = _f32(mosaic)
+        h, w = mosaic.shape
+        lv = _f32(levels)
+        ce = _f32(ceiling) if ceiling is not None else None
+        out = np.empty_like(mosaic)
+        stats = np.zeros(9, dtype=np.uint64)
+        labels = np.zeros(((h + 1) // 2, (w + 1) // 2), dtype=np.uint32)
+        count = ctypes.c_uint32()
+        self.device.check(self.lib.rd_stage_opposed(
+            self.device.handle, _ptr(mosaic, ctypes.c_float), w, h, _ffi.CFA[cfa.upper()], _ptr(lv, ctypes.c_float),
+            _ptr(ce, ctypes.c_float) if ce is not None else None, _ptr(out, ctypes.c_float),
+            _ptr(stats, ctypes.c_uint64), labels.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), ctypes.byref(count)))
+        return out, stats, labels, count.value
+
+    def demosaic(self, mosaic: np.ndarray, cfa: str, algorithm: str, balance=(1.0, 1.0, 1.0)) -> np.ndarray:
+        mosaic = _f32(mosaic)
+        h, w = mosaic.shape
+        bal = _f32(balance)
+        out = np.empty((h, 3 * w), dtype=np.float32)
+        self.device.check(self.lib.rd_stage_demosaic(self.device.handle, _ptr(mosaic, ctypes.c_float), w, h,
+                                                     _ffi.CFA[cfa.upper()], _ffi.DEMOSAIC[algorithm],
+                                                     _ptr(bal, ctypes.c_float), _ptr(out, ctypes.c_float)))
+        return out
+
+    def capture(self, rgb: np.ndarray, capture: CaptureContract) -> np.ndarray:
+        rgb = _f32(rgb).copy()
+        h, w3 = rgb.shape
+        d = capture.to_c()
+        self.device.check(self.lib.rd_stage_capture(self.device.handle, _ptr(rgb, ctypes.c_float), w3 // 3, h,
+                                                    ctypes.byref(d)))
+        return rgb
+
+    def optics(self, rgb: np.ndarray, optics: OpticsExecution) -> np.ndarray:
+        rgb = _f32(rgb)
+        out = np.empty_like(rgb)
+        o = optics.to_c()
+        self.device.check(self.lib.rd_stage_optics(self.device.handle, ctypes.byref(o), _ptr(rgb, ctypes.c_float),
+                                                   _ptr(out, ctypes.c_float)))
+        return out
+
+    def area_reduce(self, rgb: np.ndarray, target: tuple[int, int]) -> np.ndarray:
+        rgb = _f32(rgb)
+        h, w3 = rgb.shape
+        out = np.empty((target[1], 3 * target[0]), dtype=np.float32)
+        self.device.check(self.lib.rd_stage_area_reduce(self.device.handle, _ptr(rgb, ctypes.c_float), w3 // 3, h,
+                                                        target[0], target[1], _ptr(out, ctypes.c_float)))
+        return out
+
+    def color(self, rgb: np.ndarray, color: ColorContract) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        rgb = _f32(rgb)
+        h, w3 = rgb.shape
+        c = color.to_c()
+        out = np.empty((h, w3), dtype=np.uint8)
+        hist = np.zeros(1024, dtype=np.uint64)
+        clipped = np.zeros(6, dtype=np.uint64)
+        self.device.check(self.lib.rd_stage_color(self.device.handle, _ptr(rgb, ctypes.c_float), w3 // 3, h,
+                                                  ctypes.byref(c), _ptr(out, ctypes.c_uint8),
+                                                  _ptr(hist, ctypes.c_uint64), _ptr(clipped, ctypes.c_uint64)))
+        return out, hist, clipped

@@ -1,0 +1,363 @@
+"""Parity of the sm_103a kernels (through the C ABI) with the CPU oracle.
+
+Bars (from the path's contract):
+  * bit-exact: crop, CFA indexing, the Clip mask and its statistics, every
+    demosaic (bilinear, MHC, RCD, AMaZE, incl. the reference's golden hashes),
+    the area reduction, and the histogram of the kernel's own 8-bit output;
+  * linear f32 within 1e-4 max abs after a stage, 5e-4 after 10 RL iterations;
+  * optics within the reference's own GPU gate, 2e-4 + 2e-4 |x|
+    (crates/gpu/src/spatial/tests.rs:174);
+  * sRGB8 within 1 LSB on at most 0.1% of the samples.
+Sizes are small enough for the oracle to finish in seconds; they include odd
+sizes, image edges, several AMaZE/RCD tiles and the size gates.
+"""
+
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+PINS = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_pins.json")))
+PATTERNS = {"RGGB": 0, "BGGR": 1, "GRBG": 2, "GBRG": 3}
+ALGOS = {"bilinear": 0, "mhc": 1, "rcd": 2, "amaze": 3}
+
+
+def textured_mosaic(w, h, seed, clip_frac=0.03):
+    """Signed, textured mosaic with flat areas, hard edges and clipped patches."""
+    rng = np.random.default_rng(seed)
+    yy, xx = np.mgrid[0:h, 0:w].astype(np.float32)
+    v = 0.35 + 0.25 * np.sin(xx * 0.37 + yy * 0.11) * np.cos(yy * 0.29)
+    v += 0.1 * rng.standard_normal((h, w)).astype(np.float32)
+    v[(xx // 17 + yy // 13) % 7 == 0] = 0.05
+    blob = rng.uniform(size=(h, w)) < clip_frac
+    v[blob] = 1.3
+    v[(xx.astype(int) + 2 * yy.astype(int)) % 97 == 0] = -0.02
+    return v.astype(np.float32)
+
+
+@pytest.mark.parametrize("name", sorted(PINS["amaze_hashes"]))
+def test_amaze_golden_hashes_on_gpu(stages, oracle, name):
+    layout, label = name.split()
+    mosaic = oracle.amaze_golden_fixture()
+    balance = (1.0, 1.0, 1.0) if label == "identity" else (2.1, 1.0, 2.6)
+    out = stages.demosaic(mosaic, layout, "amaze", balance)
+    assert f"{oracle.fnv1a(out):016x}" == PINS["amaze_hashes"][name]
+
+
+@pytest.mark.parametrize("algorithm", ["bilinear", "mhc", "rcd", "amaze"])
+@pytest.mark.parametrize("layout", ["RGGB", "BGGR", "GRBG", "GBRG"])
+@pytest.mark.parametrize("size", [(517, 389), (53, 47)])
+def test_demosaic_bit_exact(stages, oracle, algorithm, layout, size):
+    w, h = size
+    mosaic = textured_mosaic(w, h, seed=w * 7 + h)
+    for balance in [(1.0, 1.0, 1.0), (2.0, 1.0, 1.6)]:
+        ours = stages.demosaic(mosaic, layout, algorithm, balance)
+        ref = oracle.demosaic(mosaic, PATTERNS[layout], balance, ALGOS[algorithm])
+        assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32)), (
+            algorithm, layout, size, balance, float(np.max(np.abs(ours - ref))))
+
+
+@pytest.mark.parametrize("size", [(33, 33), (32, 40), (24, 30), (25, 25), (2, 2), (240, 225)])
+def test_demosaic_size_gates_and_edges(stages, oracle, size):
+    w, h = size
+    mosaic = textured_mosaic(w, h, seed=5)
+    for algorithm in ["rcd", "amaze", "mhc"]:
+        ours = stages.demosaic(mosaic, "GBRG", algorithm, (1.9, 1.0, 1.4))
+        ref = oracle.demosaic(mosaic, 3, (1.9, 1.0, 1.4), ALGOS[algorithm])
+        assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32)), (algorithm, size)
+
+
+def raw_mosaic(sw, sh, stride, seed):
+    rng = np.random.default_rng(seed)
+    raw = rng.integers(0, 4096, size=(sh, stride), dtype=np.uint16)
+    raw[rng.uniform(size=raw.shape) < 0.05] = 4095
+    raw[rng.uniform(size=raw.shape) < 0.01] = 0
+    return raw
+
+
+@pytest.mark.parametrize("layout", ["RGGB", "GBRG"])
+@pytest.mark.parametrize("highlight", ["off", "clip"])
+def test_normalize_and_clip_bit_exact(stages, oracle, layout, highlight):
+    from rohditor_gb300 import SensorDescription
+
+    sw, sh, stride = 131, 97, 136
+    raw = raw_mosaic(sw, sh, stride, seed=11)
+    crop = (3, 2, 120, 90)
+    black = (200.0, 210.0, 190.0, 205.0)
+    white = (4000.0, 4095.0, 3900.0)
+    desc = SensorDescription(sw, sh, cfa=layout, crop=crop, black=black, black_repeat=(2, 2), white=white,
+                             highlight=highlight, clip_levels=(0.91, 0.987, 0.8), demosaic="amaze")
+    ours, stats = stages.highlight(raw, desc)
+    odesc = oracle.sensor_desc(sw, sh, stride, crop, PATTERNS[layout], black, (2, 2), white)
+    ref, crop_pattern = oracle.normalize(raw, odesc)
+    if highlight == "clip":
+        ref, ref_stats = oracle.clip(ref, crop_pattern, (0.91, 0.987, 0.8))
+        assert stats[:6].tolist() == ref_stats.tolist()
+    assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32))
+
+
+def test_fused_develop_matches_staged_oracle(device, oracle):
+    """rd_develop fuses normalize + Clip + balance into the AMaZE tile load."""
+    from rohditor_gb300 import GpuSensorProcessor, SensorDescription
+
+    sw, sh, stride = 517, 389, 520
+    raw = raw_mosaic(sw, sh, stride, seed=21)
+    desc = SensorDescription(sw, sh, cfa="GRBG", crop=(0, 0, sw, sh), black=(256.0,), white=(4095.0,),
+                             highlight="clip", clip_levels=(0.6, 0.987, 0.75), demosaic="amaze",
+                             demosaic_balance=(2.0, 1.0, 1.6))
+    src = GpuSensorProcessor(device).develop(raw, desc)
+    ours = src.download()
+    odesc = oracle.sensor_desc(sw, sh, stride, (0, 0, sw, sh), 2, [256.0], (1, 1), [4095.0])
+    m, pattern = oracle.normalize(raw, odesc)
+    m, stats = oracle.clip(m, pattern, (0.6, 0.987, 0.75))
+    ref = oracle.demosaic(m, pattern, (2.0, 1.0, 1.6), 3)
+    assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32))
+    assert list(src.metrics.highlight_stats)[:6] == stats.tolist()
+
+
+@pytest.mark.parametrize("iterations", [8, 10])
+def test_capture_sharpening(stages, oracle, iterations):
+    from rohditor_gb300 import CaptureContract
+
+    mosaic = np.clip(textured_mosaic(301, 203, seed=31, clip_frac=0.01), 0.0, None)
+    rgb = oracle.demosaic(mosaic, 0, (1, 1, 1), 1)
+    cap = CaptureContract(amount=0.5, radius=0.7, noise_protection=0.5, ceilings=(1.0, 1.0, 1.0),
+                          iterations=iterations)
+    ours = stages.capture(rgb, cap)
+    ref = oracle.capture(rgb, 0.5, 0.7, 0.5, (1.0, 1.0, 1.0), iterations)
+    err = float(np.max(np.abs(ours - ref)))
+    assert err <= 5e-4, err
+    # The kernels keep the reference's tap order, so they agree bit for bit.
+    assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32)), err
+
+
+def test_capture_radius_range_and_edges(stages, oracle):
+    from rohditor_gb300 import CaptureContract
+
+    rgb = np.abs(textured_mosaic(3 * 37, 29, seed=7)).reshape(29, 111)
+    for radius in (0.3, 1.2):
+        cap = CaptureContract(amount=1.0, radius=radius, noise_protection=0.0, ceilings=(0.9, 1.0, 0.8),
+                              iterations=3)
+        ours = stages.capture(rgb, cap)
+        ref = oracle.capture(rgb, 1.0, radius, 0.0, (0.9, 1.0, 0.8), 3)
+        assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32)), radius
+
+
+def smooth_rgb(w, h, seed):
+    rng = np.random.default_rng(seed)
+    yy, xx = np.mgrid[0:h, 0:w].astype(np.float32)
+    r = 0.4 + 0.3 * np.sin(xx / 13.0) * np.cos(yy / 17.0)
+    g = 0.5 + 0.2 * np.cos(xx / 7.0 + yy / 11.0)
+    b = 0.3 + 0.25 * np.sin((xx + yy) / 19.0)
+    rgb = np.stack([r, g, b], axis=-1)
+    rgb[(xx.astype(int) // 23 + yy.astype(int) // 19) % 5 == 0] = [0.9, 0.1, 0.05]
+    rgb += 0.01 * rng.standard_normal(rgb.shape)
+    return rgb.reshape(h, 3 * w).astype(np.float32)
+
+
+@pytest.mark.parametrize("size", [(320, 213), (161, 97)])
+def test_optics(stages, oracle, size):
+    from rohditor_gb300 import OpticsExecution
+
+    w, h = size
+    rgb = smooth_rgb(w, h, seed=4)
+    ex = OpticsExecution(w, h, distortion="poly5", distortion_k=(-0.02, 0.005, 0.0), tca="linear",
+                         tca_red=(1.0003, 0, 0), tca_blue=(0.9997, 0, 0), vignetting_k=(-0.3, 0.05, -0.01))
+    ours = stages.optics(rgb, ex)
+    ref = oracle.optics_apply(oracle.optics_desc_from(ex.to_c()), rgb)
+    tol = 2e-4 + 2e-4 * np.abs(ref)
+    assert np.all(np.abs(ours - ref) <= tol), float(np.max(np.abs(ours - ref)))
+    assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32))
+
+
+def test_vignetting_only(stages, oracle):
+    from rohditor_gb300 import OpticsExecution
+
+    rgb = smooth_rgb(203, 131, seed=9)
+    ex = OpticsExecution(203, 131, vignetting_k=(-0.35, 0.06, -0.015))
+    ours = stages.optics(rgb, ex)
+    ref = oracle.optics_apply(oracle.optics_desc_from(ex.to_c()), rgb)
+    assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32))
+
+
+@pytest.mark.parametrize("src,dst", [((611, 409), (256, 171)), ((97, 53), (41, 23)), ((40, 30), (40, 30)),
+                                     ((64, 48), (1, 1))])
+def test_area_reduce_bit_exact(stages, oracle, src, dst):
+    rgb = smooth_rgb(src[0], src[1], seed=2)
+    ours = stages.area_reduce(rgb, dst)
+    ref = oracle.area_reduce(rgb, dst)
+    assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32))
+
+
+def colour_contract(**kw):
+    from rohditor_gb300 import ColorContract, standard_base_lut
+    from rohditor_gb300.workloads import CAMERA_TO_REC2020, hsl_bands, sixteen_knot_curve
+
+    base = dict(wb_gains=(2.0, 1.0, 1.6), camera_to_rec2020=CAMERA_TO_REC2020, exposure_ev=0.5,
+                base_lut=standard_base_lut(), tone_lut=sixteen_knot_curve(), hsl=hsl_bands())
+    base.update(kw)
+    return ColorContract(**base)
+
+
+def oracle_colour(oracle, rgb, c):
+    x = oracle.white_balance(rgb, c.wb_gains)
+    x = oracle.camera_matrix(x, c.camera_to_rec2020)
+    x = oracle.adjust(x, c.exposure_ev, c.base_lut, c.tone_lut, c.saturation, c.vibrance, c.hsl, c.grading)
+    return oracle.display_srgb8(x)
+
+
+@pytest.mark.parametrize("variant", ["config", "grading_saturation", "neutral"])
+def test_colour_output_and_histogram(stages, oracle, variant):
+    rng = np.random.default_rng(17)
+    u = rng.uniform(-0.05, 0.8, size=(173, 3 * 251))
+    rgb = (np.sign(u) * np.abs(u) ** 1.5).astype(np.float32)
+    rgb[:5] = 2.5  # over-range rows clip to white
+    if variant == "config":
+        c = colour_contract()
+    elif variant == "grading_saturation":
+        c = colour_contract(saturation=1.2, vibrance=0.3,
+                            grading=np.array([[0.2, -0.1, 0.05], [0.0, 0.1, -0.2], [-0.1, 0.0, 0.3]], np.float32))
+    else:
+        c = colour_contract(exposure_ev=0.0, base_lut=None, tone_lut=None, hsl=None)
+    ours, hist, clipped = stages.color(rgb, c)
+    ref = oracle_colour(oracle, rgb, c)
+    diff = np.abs(ours.astype(int) - ref.astype(int))
+    assert diff.max() <= 1
+    assert (diff > 0).mean() <= 1e-3
+    # The histogram of the kernel's own 8-bit output is exact.
+    ref_hist, ref_clipped = oracle.histogram(ours)
+    assert np.array_equal(hist, ref_hist) and np.array_equal(clipped, ref_clipped)
+
+
+def test_processor_pipeline_end_to_end(device, oracle):
+    """develop -> spatial -> render through the processor API, stage by stage against the oracle."""
+    from rohditor_gb300 import (CaptureContract, GpuPreviewProcessor, GpuSensorProcessor, GpuSpatialProcessor,
+                                OpticsExecution, SensorDescription, clip_levels)
+    from rohditor_gb300.workloads import CAMERA_TO_REC2020, preview_dimensions
+
+    sw, sh = 700, 467
+    raw = raw_mosaic(sw, sh, sw, seed=41)
+    wb = (2.0, 1.0, 1.6)
+    levels = clip_levels(1.0, wb)
+    desc = SensorDescription(sw, sh, cfa="RGGB", black=(256.0,), white=(4095.0,), highlight="clip",
+                             clip_levels=levels, demosaic="amaze", demosaic_balance=wb)
+    cap = CaptureContract(amount=0.5, radius=0.7, noise_protection=0.5, ceilings=levels, iterations=10)
+    src = GpuSensorProcessor(device).develop(raw, desc, cap)
+    odesc = oracle.sensor_desc(sw, sh, sw, (0, 0, sw, sh), 0, [256.0], (1, 1), [4095.0])
+    m, pattern = oracle.normalize(raw, odesc)
+    m, _ = oracle.clip(m, pattern, levels)
+    ref = oracle.demosaic(m, pattern, wb, 3)
+    ref = oracle.capture(ref, 0.5, 0.7, 0.5, levels, 10)
+    got = src.download()
+    assert float(np.max(np.abs(got - ref))) <= 5e-4
+    ex = OpticsExecution(sw, sh, distortion="poly5", distortion_k=(-0.02, 0.005, 0.0), tca="linear",
+                         tca_red=(1.0003, 0, 0), tca_blue=(0.9997, 0, 0), vignetting_k=(-0.3, 0.05, -0.01))
+    target = preview_dimensions(sw, sh, 256)
+    base = GpuSpatialProcessor(device).reduce_preview(src, ex, target, wb, CAMERA_TO_REC2020)
+    ref_o = oracle.optics_apply(oracle.optics_desc_from(ex.to_c()), ref)
+    ref_r = oracle.area_reduce(ref_o, target)
+    ref_b = oracle.camera_matrix(oracle.white_balance(ref_r, wb), CAMERA_TO_REC2020)
+    got_b = base.download()
+    assert float(np.max(np.abs(got_b - ref_b))) <= 1e-4 + 1e-4 * float(np.max(np.abs(ref_b)))
+    c = colour_contract()
+    out, hist = GpuPreviewProcessor(device).render(base, c)
+    x = oracle.adjust(got_b, c.exposure_ev, c.base_lut, c.tone_lut, c.saturation, c.vibrance, c.hsl, c.grading)
+    ref8 = oracle.display_srgb8(x)
+    diff = np.abs(out.astype(int) - ref8.astype(int))
+    assert diff.max() <= 1 and (diff > 0).mean() <= 1e-3
+    ref_hist, _ = oracle.histogram(out)
+    assert np.array_equal(np.concatenate([hist.red, hist.green, hist.blue, hist.luminance]), ref_hist)
+
+
+def test_cancellation_before_start(device):
+    from rohditor_gb300 import GpuPreviewError, GpuSensorProcessor, SensorDescription
+
+    raw = raw_mosaic(64, 48, 64, seed=1)
+    cancel = np.ones(1, dtype=np.uint32)
+    with pytest.raises(GpuPreviewError) as err:
+        GpuSensorProcessor(device).develop(raw, SensorDescription(64, 48, black=(0.0,), white=(4095.0,)),
+                                           cancel=cancel)
+    assert err.value.variant == "Cancelled" and not err.value.is_routing()
+
+
+def test_budget_is_a_routing_answer(device):
+    from rohditor_gb300 import GpuPreviewError, GpuSensorProcessor, SensorDescription
+
+    raw = raw_mosaic(640, 480, 640, seed=1)
+    device.set_budget(1 << 20)
+    try:
+        with pytest.raises(GpuPreviewError) as err:
+            GpuSensorProcessor(device).develop(raw, SensorDescription(640, 480, black=(0.0,), white=(4095.0,)))
+        assert err.value.variant == "OverBudget" and err.value.is_routing()
+    finally:
+        device.set_budget(0)
+
+
+def test_kernel_launches_are_counted(device, stages):
+    before = device.kernel_launches
+    stages.demosaic(textured_mosaic(64, 64, 1), "RGGB", "mhc")
+    assert device.kernel_launches > before
+
+
+def opposed_scene(w, h, seed, layout="RGGB"):
+    """Bayer samples of a smooth warm scene with blown discs of varying size, some at the borders."""
+    rng = np.random.default_rng(seed)
+    yy, xx = np.mgrid[0:h, 0:w].astype(np.float32)
+    rgb = np.stack([0.55 + 0.1 * np.sin(xx / 9.0), 0.45 + 0.1 * np.cos(yy / 7.0),
+                    0.30 + 0.05 * np.sin((xx + yy) / 11.0)], axis=-1)
+    for _ in range(12):
+        cx, cy, r = rng.uniform(0, w), rng.uniform(0, h), rng.uniform(2, 14)
+        amp = rng.uniform(1.0, 2.5)
+        d2 = ((xx - cx) ** 2 + (yy - cy) ** 2) / (r * r)
+        tint = rng.uniform(0.6, 1.0, size=3)
+        rgb += (amp * np.exp(-d2))[..., None] * tint
+    rgb += 0.004 * rng.standard_normal(rgb.shape)
+    table = {"RGGB": [0, 1, 1, 2], "BGGR": [2, 1, 1, 0], "GRBG": [1, 0, 2, 1], "GBRG": [1, 2, 0, 1]}[layout]
+    ch = np.array(table)[((yy.astype(int) & 1) << 1) | (xx.astype(int) & 1)]
+    return np.take_along_axis(rgb, ch[..., None], axis=-1)[..., 0].astype(np.float32)
+
+
+@pytest.mark.parametrize("layout", ["RGGB", "GBRG"])
+@pytest.mark.parametrize("size", [(120, 94), (333, 257), (41, 37)])
+def test_opposed_matches_oracle(stages, oracle, layout, size):
+    from rohditor_gb300 import opposed_levels
+
+    w, h = size
+    mosaic = opposed_scene(w, h, seed=w + h, layout=layout)
+    det, ceiling = opposed_levels(1.0, (2.0, 1.0, 1.6))
+    ours, stats, labels, count = stages.opposed(mosaic, layout, det, ceiling)
+    ref, ref_stats, ref_labels, ref_count = oracle.opposed(mosaic, PATTERNS[layout], det, ceiling)
+    # Region labelling (compact, raster order) and the clipped mask are exact.
+    assert count == ref_count
+    assert np.array_equal(labels, ref_labels)
+    assert stats.tolist() == ref_stats.tolist()
+    assert float(np.max(np.abs(ours - ref))) <= 1e-4
+
+
+def test_opposed_without_clipping_is_identity(stages, oracle):
+    mosaic = np.full((50, 64), 0.4, dtype=np.float32)
+    ours, stats, labels, count = stages.opposed(mosaic, "RGGB", (0.987,) * 3, None)
+    assert np.array_equal(ours, mosaic) and stats[0] == 0 and count == 0 and not labels.any()
+
+
+def test_develop_with_opposed(device, oracle):
+    from rohditor_gb300 import GpuSensorProcessor, SensorDescription, opposed_levels
+
+    w, h = 301, 203
+    mosaic = opposed_scene(w, h, seed=3)
+    raw = np.clip(np.rint(256 + mosaic * (4095 - 256)), 0, 4095).astype(np.uint16)
+    det, ceiling = opposed_levels(1.0, (2.0, 1.0, 1.6))
+    desc = SensorDescription(w, h, cfa="RGGB", black=(256.0,), white=(4095.0,), highlight="opposed",
+                             detection_levels=det, neutral_ceiling=ceiling, demosaic="amaze",
+                             demosaic_balance=(2.0, 1.0, 1.6))
+    src = GpuSensorProcessor(device).develop(raw, desc)
+    odesc = oracle.sensor_desc(w, h, w, (0, 0, w, h), 0, [256.0], (1, 1), [4095.0])
+    m, pattern = oracle.normalize(raw, odesc)
+    m, stats, _, _ = oracle.opposed(m, pattern, det, ceiling)
+    ref = oracle.demosaic(m, pattern, (2.0, 1.0, 1.6), 3)
+    got = src.download()
+    assert list(src.metrics.highlight_stats) == stats.tolist()
+    assert float(np.max(np.abs(got - ref))) <= 1e-4
