@@ -89,6 +89,10 @@ class ClockSampler:
                  "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            # nvidia-smi takes a moment to start; begin the timed region once it samples.
+            t0 = time.perf_counter()
+            while not self.lines and time.perf_counter() - t0 < 5.0 and self.proc.poll() is None:
+                time.sleep(0.02)
         except FileNotFoundError:
             self.proc = None
         return self
@@ -220,8 +224,8 @@ def run_ours(args, world, rank, local, pg):
     launches0 = dev.kernel_launches
     barrier(pg)
     dev.synchronize()
-    with ClockSampler(local) as clocks:
-        total_ms, per = timed(step_device, args.steps)
+    clocks = ClockSampler(local).__enter__()
+    total_ms, per = timed(step_device, args.steps)
     dev.synchronize()
     launches = dev.kernel_launches - launches0
     lib.rd_ctx_enable_kernel_timing(h, 0)
@@ -240,6 +244,7 @@ def run_ours(args, world, rank, local, pg):
         step_e2e()
     barrier(pg)
     e2e_ms, e2e_per = timed(step_e2e, args.steps)
+    clocks.__exit__(None, None, None)  # sampled across both timed legs
     e2e_ms = max_over_ranks(pg, e2e_ms)
 
     ms_per_step = total_ms / args.steps
@@ -382,7 +387,7 @@ def run_reference(args, world, rank, pg):
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--steps", type=int, default=40)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--highlight", default="opposed", choices=["opposed", "clip"])
