@@ -762,16 +762,17 @@ Status run_amaze(Context& ctx, const MosaicSource& src, const float gains[3], fl
   const int waves = (ntiles + max_ctas - 1) / max_ctas;
   const int grid = (ntiles + waves - 1) / waves;
   if ((size_t)grid > ctx.amaze_slots) {
+    // Slots are kept between calls and only grow, to the grid of the largest image seen.
     if (ctx.amaze_scratch) device_free(ctx, ctx.amaze_scratch, ctx.amaze_slots * SLOT_FLOATS * sizeof(float));
     ctx.amaze_scratch = nullptr;
     ctx.amaze_slots = 0;
     void* p = nullptr;
-    RD_TRY(device_alloc(ctx, (size_t)max_ctas * SLOT_FLOATS * sizeof(float), &p));
+    RD_TRY(device_alloc(ctx, (size_t)grid * SLOT_FLOATS * sizeof(float), &p));
     // vcd/hcd/vcdalt/hcdalt are read outside the region the stages write and
     // must stay zero there (scratch.rs:95-104); nothing ever writes them.
-    RD_CUDA_TRY(cudaMemsetAsync(p, 0, (size_t)max_ctas * SLOT_FLOATS * sizeof(float), ctx.stream));
+    RD_CUDA_TRY(cudaMemsetAsync(p, 0, (size_t)grid * SLOT_FLOATS * sizeof(float), ctx.stream));
     ctx.amaze_scratch = static_cast<float*>(p);
-    ctx.amaze_slots = max_ctas;
+    ctx.amaze_slots = grid;
   }
   AmazeParams prm;
   prm.src = src;

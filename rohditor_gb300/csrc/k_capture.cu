@@ -96,75 +96,186 @@ __device__ __forceinline__ float hblur(const float* row, int qx, int x, int W, i
   return v;
 }
 
-struct RlIterSmem {
-  float e[EH * EW];       // estimate window, origin (x0 - 2r, y0 - 2r)
-  float t1[EH * RWX];     // horizontal blur of e, window columns x0 - r ..
-  float q[RWY * RWX];     // blur(e) then the ratio, origin (x0 - r, y0 - r)
-  float t2[RWY * TX];     // horizontal blur of the ratio, core columns
+// ---- one fused RL iteration per tile --------------------------------------
+// Compile-time radius R (1..4) and tile. Each separable pass runs as "runs":
+// a thread produces RUN consecutive outputs along the blur direction from a
+// register window, so shared memory is read about once per output instead of
+// 2R+1 times. Every output still sums its taps in kernel order from 0 (or
+// -0.0 on horizontal border columns), exactly as the reference.
+template <int R>
+struct IterGeom {
+  static constexpr int T = 2 * R + 1;
+  static constexpr int EW = TX + 4 * R, EH = TY + 4 * R;  // estimate window
+  static constexpr int QW = TX + 2 * R, QH = TY + 2 * R;  // ratio window
+  static constexpr int EP = EW | 1, QP = QW | 1, CP = TX + 1;  // odd pitches: conflict-free columns
 };
 
-__global__ void __launch_bounds__(256) rl_iter_kernel(const float* __restrict__ est_in, const float* __restrict__ guide,
-                                                      float* __restrict__ est_out, int W, int H, int r) {
+template <int R>
+struct IterSmem {
+  using G = IterGeom<R>;
+  float e[G::EH * G::EP];
+  float t1[G::EH * G::QP];
+  float q[G::QH * G::QP];
+  float t2[G::QH * G::CP];
+};
+
+// Horizontal run: `n` (<= RUN) outputs starting at window column `c0` of
+// `row`, written to `out`; `x0img` is the image column of the first output.
+template <int R, int RUN>
+__device__ __forceinline__ void hrun(const float* __restrict__ row, int c0, int n, float* __restrict__ out, int x0img,
+                                     int W, const float (&w)[2 * R + 1]) {
+  constexpr int T = 2 * R + 1;
+  float win[RUN + 2 * R];
+#pragma unroll
+  for (int k = 0; k < RUN + 2 * R; ++k) win[k] = (k < n + 2 * R) ? row[c0 - R + k] : 0.0f;
+#pragma unroll
+  for (int j = 0; j < RUN; ++j) {
+    if (j < n) {
+      const int x = x0img + j;
+      float v = (W <= 2 * R || x < R || x >= W - R) ? -0.0f : 0.0f;
+#pragma unroll
+      for (int k = 0; k < T; ++k) v += win[j + k] * w[k];
+      out[j] = v;
+    }
+  }
+}
+
+template <int R>
+__global__ void __launch_bounds__(256, 2) rl_iter_kernel(const float* __restrict__ est_in,
+                                                         const float* __restrict__ guide,
+                                                         float* __restrict__ est_out, int W, int H) {
+  using G = IterGeom<R>;
+  constexpr int T = G::T;
   extern __shared__ float4 rl_smem_raw[];
-  RlIterSmem& S = *reinterpret_cast<RlIterSmem*>(rl_smem_raw);
-  const int taps = 2 * r + 1;
+  IterSmem<R>& S = *reinterpret_cast<IterSmem<R>*>(rl_smem_raw);
+  float w[T];
+#pragma unroll
+  for (int k = 0; k < T; ++k) w[k] = c_kernel[k];
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
-  const int ew = TX + 4 * r, eh = TY + 4 * r, qw = TX + 2 * r, qh = TY + 2 * r;
-  load_window(S.e, ew, eh, est_in, W, H, x0 - 2 * r, y0 - 2 * r);
-  __syncthreads();
-  // Horizontal pass of blur #1 at window columns x0 - r .. x0 + TX + r (in-image
-  // columns only; the rest are filled from their mirror after the ratio).
-  for (int k = threadIdx.x; k < eh * qw; k += blockDim.x) {
-    const int qy = k / qw, qx = k % qw;
-    const int x = x0 - r + qx;
-    if (x < 0 || x >= W) continue;
-    S.t1[qy * qw + qx] = hblur(S.e + qy * ew, qx + r, x, W, r, taps);
+  const int tid = threadIdx.x;
+  const bool interior = x0 - 2 * R >= 0 && x0 + TX + 2 * R <= W && y0 - 2 * R >= 0 && y0 + TY + 2 * R <= H;
+  const int ex = x0 - 2 * R, ey = y0 - 2 * R;  // estimate window origin
+  // 1. estimate window (mirrored reads only on edge tiles)
+  if (interior) {
+    for (int k = tid; k < G::EH * G::EW; k += 256) {
+      const int r = k / G::EW, c = k - r * G::EW;
+      S.e[r * G::EP + c] = est_in[(long long)(ey + r) * W + ex + c];
+    }
+  } else {
+    for (int k = tid; k < G::EH * G::EW; k += 256) {
+      const int r = k / G::EW, c = k - r * G::EW;
+      S.e[r * G::EP + c] = est_in[(long long)mirror_half(ey + r, H) * W + mirror_half(ex + c, W)];
+    }
   }
   __syncthreads();
-  // Vertical pass of blur #1 and the ratio at in-image positions of the ratio window.
-  for (int k = threadIdx.x; k < qh * qw; k += blockDim.x) {
-    const int qy = k / qw, qx = k % qw;
-    const int x = x0 - r + qx, y = y0 - r + qy;
-    if (x < 0 || x >= W || y < 0 || y >= H) continue;
-    float b = 0.0f;
-    for (int j = 0; j < taps; ++j) b += S.t1[(qy + j) * qw + qx] * c_kernel[j];
-    S.q[k] = guide[(long long)y * W + x] / rmax(b, FLOOR);
+  // 2. horizontal pass of blur #1: window rows x ratio-window columns, runs of 16
+  {
+    constexpr int RUN = 16, RUNS = (G::QW + RUN - 1) / RUN;
+    for (int k = tid; k < G::EH * RUNS; k += 256) {
+      const int r = k / RUNS, s = k - r * RUNS;
+      const int qc0 = s * RUN;
+      const int n = min(RUN, G::QW - qc0);
+      const int x0img = x0 - R + qc0;
+      // Columns outside the image are never read downstream; computing them is harmless.
+      hrun<R, RUN>(S.e + r * G::EP, qc0 + R, n, S.t1 + r * G::QP + qc0, x0img, W, w);
+    }
   }
   __syncthreads();
-  // Out-of-image ratio entries within the blur radius of the image take the
-  // value at their mirror position, which lies inside this window. Entries
-  // further out are never read.
-  for (int k = threadIdx.x; k < qh * qw; k += blockDim.x) {
-    const int qy = k / qw, qx = k % qw;
-    const int x = x0 - r + qx, y = y0 - r + qy;
-    if (x >= 0 && x < W && y >= 0 && y < H) continue;
-    if (x < -r || x >= W + r || y < -r || y >= H + r) continue;
-    const int mx = mirror_half(x, W) - (x0 - r), my = mirror_half(y, H) - (y0 - r);
-    S.q[k] = S.q[my * qw + mx];
+  // 3. vertical pass of blur #1 and the ratio, runs of RUN rows per column
+  {
+    constexpr int RUN = (G::QH + 2) / 3;
+    constexpr int RUNS = (G::QH + RUN - 1) / RUN;
+    for (int k = tid; k < G::QW * RUNS; k += 256) {
+      const int s = k / G::QW, qc = k - s * G::QW;
+      const int qr0 = s * RUN;
+      const int n = min(RUN, G::QH - qr0);
+      const int x = x0 - R + qc;
+      float win[RUN + 2 * R];
+#pragma unroll
+      for (int j = 0; j < RUN + 2 * R; ++j) win[j] = (j < n + 2 * R) ? S.t1[(qr0 + j) * G::QP + qc] : 0.0f;
+#pragma unroll
+      for (int j = 0; j < RUN; ++j) {
+        const int y = y0 - R + qr0 + j;
+        if (j < n && x >= 0 && x < W && y >= 0 && y < H) {
+          float b = 0.0f;
+#pragma unroll
+          for (int t = 0; t < T; ++t) b += win[j + t] * w[t];
+          S.q[(qr0 + j) * G::QP + qc] = __ldg(guide + (long long)y * W + x) / rmax(b, FLOOR);
+        }
+      }
+    }
   }
   __syncthreads();
-  // Horizontal pass of blur #2 on the core columns.
-  for (int k = threadIdx.x; k < qh * TX; k += blockDim.x) {
-    const int qy = k / TX, cx = k % TX;
-    const int x = x0 + cx;
-    if (x >= W) continue;
-    S.t2[k] = hblur(S.q + qy * qw, cx + r, x, W, r, taps);
+  if (!interior) {
+    // Out-of-image ratio entries within R of the image take their mirror's value.
+    for (int k = tid; k < G::QH * G::QW; k += 256) {
+      const int qr = k / G::QW, qc = k - qr * G::QW;
+      const int x = x0 - R + qc, y = y0 - R + qr;
+      if (x >= 0 && x < W && y >= 0 && y < H) continue;
+      if (x < -R || x >= W + R || y < -R || y >= H + R) continue;
+      const int mx = mirror_half(x, W) - (x0 - R), my = mirror_half(y, H) - (y0 - R);
+      S.q[qr * G::QP + qc] = S.q[my * G::QP + mx];
+    }
+    __syncthreads();
+  }
+  // 4. horizontal pass of blur #2 on the core columns, runs of 16
+  {
+    constexpr int RUN = 16, RUNS = TX / RUN;
+    for (int k = tid; k < G::QH * RUNS; k += 256) {
+      const int r = k / RUNS, s = k - r * RUNS;
+      const int c0 = s * RUN;
+      const int n = min(RUN, W - (x0 + c0));
+      if (n <= 0) continue;
+      hrun<R, RUN>(S.q + r * G::QP, c0 + R, n, S.t2 + r * G::CP + c0, x0 + c0, W, w);
+    }
   }
   __syncthreads();
-  // Vertical pass of blur #2 and the bounded update.
-  for (int k = threadIdx.x; k < TY * TX; k += blockDim.x) {
-    const int cy = k / TX, cx = k % TX;
-    const int x = x0 + cx, y = y0 + cy;
-    if (x >= W || y >= H) continue;
-    float b = 0.0f;
-    for (int j = 0; j < taps; ++j) b += S.t2[(cy + j) * TX + cx] * c_kernel[j];
-    const long long o = (long long)y * W + x;
-    const float g = guide[o];
-    float e = S.e[(cy + 2 * r) * ew + cx + 2 * r] * b;
-    const float lo = g * 0.5f, hi = g * 2.0f;
-    if (e < lo) e = lo;
-    if (e > hi) e = hi;
-    est_out[o] = e;
+  // 5. vertical pass of blur #2 and the bounded update, runs of 8 rows
+  {
+    constexpr int RUN = 8, RUNS = TY / RUN;
+    for (int k = tid; k < TX * RUNS; k += 256) {
+      const int s = k / TX, c = k - s * TX;
+      const int x = x0 + c;
+      if (x >= W) continue;
+      const int r0 = s * RUN;
+      float win[RUN + 2 * R];
+#pragma unroll
+      for (int j = 0; j < RUN + 2 * R; ++j) win[j] = S.t2[(r0 + j) * G::CP + c];
+#pragma unroll
+      for (int j = 0; j < RUN; ++j) {
+        const int y = y0 + r0 + j;
+        if (y >= H) break;
+        float b = 0.0f;
+#pragma unroll
+        for (int t = 0; t < T; ++t) b += win[j + t] * w[t];
+        const long long o = (long long)y * W + x;
+        const float g = __ldg(guide + o);
+        float e = S.e[(r0 + j + 2 * R) * G::EP + c + 2 * R] * b;
+        const float lo = g * 0.5f, hi = g * 2.0f;
+        if (e < lo) e = lo;
+        if (e > hi) e = hi;
+        est_out[o] = e;
+      }
+    }
+  }
+}
+
+template <int R>
+Status launch_rl_iter(Context& ctx, const float* est, const float* guide, float* out, int W, int H) {
+  const size_t smem = sizeof(IterSmem<R>);
+  RD_CUDA_TRY(cudaFuncSetAttribute(rl_iter_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid((W + TX - 1) / TX, (H + TY - 1) / TY);
+  RD_LAUNCH(ctx, K_RL_ITER, rl_iter_kernel<R><<<grid, 256, smem, ctx.stream>>>(est, guide, out, W, H));
+  return Status{};
+}
+
+Status rl_iteration(Context& ctx, int r, const float* est, const float* guide, float* out, int W, int H) {
+  switch (r) {
+    case 1: return launch_rl_iter<1>(ctx, est, guide, out, W, H);
+    case 2: return launch_rl_iter<2>(ctx, est, guide, out, W, H);
+    case 3: return launch_rl_iter<3>(ctx, est, guide, out, W, H);
+    case 4: return launch_rl_iter<4>(ctx, est, guide, out, W, H);
+    default: return Status{RD_INVALID_INPUT, "capture radius outside 1..4"};
   }
 }
 
@@ -464,10 +575,8 @@ Status run_capture(Context& ctx, float* rgb, int W, int H, const rd_detail_desc&
     cudaFuncSetAttribute(rl_mask_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mask_smem);
     RD_LAUNCH(ctx, K_RL_MASK, rl_mask_kernel<<<grid, 256, mask_smem, ctx.stream>>>(mask, guide, mask2, W, H, r, detail.noise_protection));
     std::swap(mask, mask2);
-    const size_t iter_smem = sizeof(RlIterSmem);
-    cudaFuncSetAttribute(rl_iter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)iter_smem);
-    for (int it = 0; it < detail.iterations; ++it) {
-      RD_LAUNCH(ctx, K_RL_ITER, rl_iter_kernel<<<grid, 256, iter_smem, ctx.stream>>>(est, guide, est2, W, H, r));
+    for (int it = 0; it < detail.iterations && st.ok(); ++it) {
+      st = rl_iteration(ctx, r, est, guide, est2, W, H);
       std::swap(est, est2);
     }
     if (cudaGetLastError() != cudaSuccess) st = Status{RD_SYNCHRONIZATION, "capture kernels failed to launch"};

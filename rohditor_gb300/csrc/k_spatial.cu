@@ -28,6 +28,10 @@ namespace {
 
 constexpr double NEWTON_EPS = 0.00001;
 
+struct FastOptics {
+  float cxh, cxl, cyh, cyl, uh, ul;  // f64 constants split into FP32 pairs
+};
+
 struct OpticsParams {
   const float* in;   // planar RGB
   const float* mult; // vignetting multipliers, or null
@@ -41,6 +45,7 @@ struct OpticsParams {
   int tca_model;
   float tr[3], tb[3];
   unsigned* error;
+  FastOptics fast;
 };
 
 __device__ __forceinline__ void undistort(const OpticsParams& p, float x, float y, float& ox, float& oy) {
@@ -102,6 +107,123 @@ __device__ __forceinline__ void tca_poly3(const float* ch, float x, float y, flo
   oy = (float)((double)y * ratio);
 }
 
+// ---- exact FP32 fast path -------------------------------------------------
+// GB300 runs FP64 at a small fraction of its FP32 rate, so the per-pixel f64
+// arithmetic of the reference (lensfun's Newton inversion, the f64 pixel
+// transform) is evaluated in double-float FP32 arithmetic (~44-bit accuracy).
+// The f64 result is then rounded to f32 exactly as the reference does; when
+// the double-float value lies so close to an f32 rounding midpoint (or to the
+// Newton break threshold) that the two could disagree, the pixel takes the
+// f64 path instead. The output is therefore the f64 path's, bit for bit.
+struct df {
+  float h, l;
+};
+__device__ __forceinline__ df two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ df fast_two_sum(float a, float b) {
+  const float s = a + b;
+  return {s, b - (s - a)};
+}
+__device__ __forceinline__ df two_prod(float a, float b) {
+  const float p = a * b;
+  return {p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ df df_add(df x, df y) {
+  const df s = two_sum(x.h, y.h);
+  return fast_two_sum(s.h, s.l + x.l + y.l);
+}
+__device__ __forceinline__ df df_mul(df x, df y) {
+  df p = two_prod(x.h, y.h);
+  p.l = p.l + (x.h * y.l + x.l * y.h);
+  return fast_two_sum(p.h, p.l);
+}
+__device__ __forceinline__ df df_mul_f(df x, float b) {
+  df p = two_prod(x.h, b);
+  p.l = p.l + x.l * b;
+  return fast_two_sum(p.h, p.l);
+}
+__device__ __forceinline__ df df_div(df x, df y) {
+  const float q1 = x.h / y.h;
+  const df r = df_add(x, df_mul_f({-y.h, -y.l}, q1));
+  const float q2 = r.h / y.h;
+  return fast_two_sum(q1, q2);
+}
+// Nearest f32 of the double-float value; `amb` is set when the value lies
+// within a relative 2^-40 of a rounding midpoint.
+__device__ __forceinline__ float df_round(df v, bool& amb) {
+  const float r = v.h + v.l;
+  const float d = (v.h - r) + v.l;
+  const float up = (nextafterf(r, INFINITY) - r) * 0.5f;
+  const float dn = (r - nextafterf(r, -INFINITY)) * 0.5f;
+  const float room = d >= 0.0f ? up - d : dn + d;
+  if (!(room > fabsf(r) * 9.094947e-13f)) amb = true;  // 2^-40
+  return r;
+}
+
+// (n + c) * unscale in f64, narrowed to f32 (plan.rs:476-478).
+__device__ __forceinline__ float post_transform(float n, float ch, float cl, const FastOptics& f, double c64,
+                                                double unscale, bool& fell_back) {
+  df t = two_sum(n, ch);
+  t = fast_two_sum(t.h, t.l + cl);
+  bool amb = false;
+  const float r = df_round(df_mul(t, {f.uh, f.ul}), amb);
+  if (!amb) return r;
+  fell_back = true;
+  return (float)(((double)n + c64) * unscale);
+}
+
+// Poly5 inverse from f32 (x, y): the f64 Newton result, computed through the
+// one-step closed form when that is what the iteration does (break at step 0:
+// ratio 1; break at step 1: ratio = 1 - g/d with g = k1 u + k2 u^2 and
+// d = 1 + 3 k1 u + 5 k2 u^2 for u = x^2 + y^2), else through f64.
+__device__ __forceinline__ void undistort_poly5_fast(float x, float y, float a, float b, float& ox, float& oy,
+                                                     bool& need_f64) {
+  ox = x;
+  oy = y;
+  const float s = x * x + y * y;
+  if (s == 0.0f) return;
+  const float g32 = a * s + b * (s * s);
+  const float sq = sqrtf(s);
+  const float f0 = sq * g32;
+  const float thr = 1.0e-5f;
+  if (fabsf(f0) < thr * (1.0f - 1.0e-5f)) return;  // |F(rd)| < 1e-5: frozen at the input
+  if (fabsf(f0) <= thr * (1.0f + 1.0e-5f)) {
+    need_f64 = true;
+    return;
+  }
+  const float d32 = 1.0f + 3.0f * a * s + 5.0f * b * (s * s);
+  const float q32 = f0 / d32;
+  const float f1 = (3.0f * a * sq + 10.0f * b * sq * s) * q32 * q32;  // F(ru1) ~ F''/2 (F/F')^2
+  if (!(fabsf(f1) < 1.0e-6f) || !(d32 > 0.0f)) {
+    need_f64 = true;
+    return;
+  }
+  const df as = two_prod(a, s);
+  const df ss = two_prod(s, s);
+  const df bss = df_mul_f(ss, b);
+  const df g = df_add(as, bss);
+  const df d = df_add(df_add({1.0f, 0.0f}, df_mul_f(as, 3.0f)), df_mul_f(bss, 5.0f));
+  const df q = df_div(g, d);
+  const df ratio = fast_two_sum(1.0f, -q.h);
+  const df rr = {ratio.h, ratio.l - q.l};
+  if (!(rr.h > 0.0f)) {
+    need_f64 = true;
+    return;
+  }
+  bool amb = false;
+  const float rx = df_round(df_mul_f(rr, x), amb);
+  const float ry = df_round(df_mul_f(rr, y), amb);
+  if (amb) {
+    need_f64 = true;
+    return;
+  }
+  ox = rx;
+  oy = ry;
+}
+
 __device__ __forceinline__ float cubic_weight(float d) {
   const float a = fabsf(d);
   if (a <= 1.0f) return 1.5f * a * a * a - 2.5f * a * a + 1.0f;
@@ -117,6 +239,9 @@ __device__ __forceinline__ bool cubic_sample(const float* __restrict__ plane, co
   const int fx = (int)floorf(x), fy = (int)floorf(y);
   if (fx - 1 < 0 || fy - 1 < 0 || fx + 2 >= W || fy + 2 >= H) return false;
   float value = 0.0f;
+  float wx[4];
+#pragma unroll
+  for (int ox = -1; ox <= 2; ++ox) wx[ox + 1] = cubic_weight(x - (float)(fx + ox));  // same for every row
 #pragma unroll
   for (int oy = -1; oy <= 2; ++oy) {
     const float wy = cubic_weight(y - (float)(fy + oy));
@@ -124,7 +249,7 @@ __device__ __forceinline__ bool cubic_sample(const float* __restrict__ plane, co
     const float* mrow = mult ? mult + (long long)(fy + oy) * W : nullptr;
 #pragma unroll
     for (int ox = -1; ox <= 2; ++ox) {
-      const float weight = wy * cubic_weight(x - (float)(fx + ox));
+      const float weight = wy * wx[ox + 1];
       float sample = __ldg(row + fx + ox);
       if (mrow) sample = sample * __ldg(mrow + fx + ox);  // the vignetted source value
       value += sample * weight;
@@ -140,7 +265,14 @@ __global__ void __launch_bounds__(256) optics_kernel(const OpticsParams p) {
   const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
   if (x >= p.W || y >= p.H) return;
   float gx, gy;
-  undistort(p, p.ix[x], p.iy[y], gx, gy);
+  const float ix = p.ix[x], iy = p.iy[y];
+  if (p.dist_model == RD_DISTORTION_POLY5) {
+    bool need_f64 = false;
+    undistort_poly5_fast(ix, iy, p.d0, p.d1, gx, gy, need_f64);
+    if (need_f64) undistort(p, ix, iy, gx, gy);
+  } else {
+    undistort(p, ix, iy, gx, gy);
+  }
   bool bad = !isfinite(gx) || !isfinite(gy);
   float n[6] = {gx, gy, gx, gy, gx, gy};
   if (p.tca_model == RD_TCA_LINEAR) {
@@ -156,8 +288,9 @@ __global__ void __launch_bounds__(256) optics_kernel(const OpticsParams p) {
   const long long o = (long long)y * p.W + x;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    const float sx = (float)(((double)n[2 * c] + p.cx) * p.unscale);
-    const float sy = (float)(((double)n[2 * c + 1] + p.cy) * p.unscale);
+    bool fell_back = false;
+    const float sx = post_transform(n[2 * c], p.fast.cxh, p.fast.cxl, p.fast, p.cx, p.unscale, fell_back);
+    const float sy = post_transform(n[2 * c + 1], p.fast.cyh, p.fast.cyl, p.fast, p.cy, p.unscale, fell_back);
     float v = 0.0f;
     if (!bad && !cubic_sample(p.in + c * plane, p.mult, p.W, p.H, sx, sy, v)) bad = true;
     p.out[c * plane + o] = v;
@@ -265,6 +398,13 @@ Status run_optics_gather(Context& ctx, const rd_optics_desc& o, const float* rgb
     p.tb[c] = o.tca_blue[c];
   }
   p.error = ctx.d_error;
+  auto split = [](double v, float& h, float& l) {
+    h = (float)v;
+    l = (float)(v - (double)h);
+  };
+  split(o.center_x, p.fast.cxh, p.fast.cxl);
+  split(o.center_y, p.fast.cyh, p.fast.cyl);
+  split(o.norm_unscale, p.fast.uh, p.fast.ul);
   dim3 grid((W + 31) / 32, (H + 7) / 8);
   RD_LAUNCH(ctx, K_OPTICS, optics_kernel<<<grid, 256, 0, ctx.stream>>>(p));
   const cudaError_t launch = cudaGetLastError();
