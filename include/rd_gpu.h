@@ -176,6 +176,27 @@ rd_status rd_render(rd_ctx* ctx, const rd_base* base, const rd_color_desc* color
 /* Device-resident render: writes u8 output and histogram into device memory
  * owned by the base; nothing is copied to the host. */
 rd_status rd_render_device(rd_ctx* ctx, rd_base* base, const rd_color_desc* color, rd_metrics* metrics);
+/* Allocation-free render. No counterpart in the reference: it exists for
+ * callers that cannot allocate device memory on the render path (an
+ * interactive loop re-rendering the preview per slider event under a fixed,
+ * pre-reserved device budget). Same arithmetic as rd_render_device.
+ *   d_base      planar Rec.2020 f32 [3][height][width] on the current device
+ *               (the white-balanced, camera-matrixed base)
+ *   d_srgb_out  device [height][3*width] u8
+ *   d_hist      device 4*256 u64 (R, G, B, luma); cleared by this call
+ *   stream      cudaStream_t the work is enqueued on (NULL: legacy default)
+ * Returns after enqueueing; results are ready when `stream` completes. No
+ * context, no device allocation: the two 4096-entry LUTs (32 KB, the only
+ * scratch; LUT length is fixed by rd_color_desc, image size is not limited)
+ * are staged in a static device array of this library. The first call on a
+ * device resolves that array's address and may load the module there; make
+ * it before any stream capture. Calls overlapping in time on one device
+ * (any streams, any threads) share the array and race: serialise them.
+ * RD_INVALID_INPUT for null pointers, zero or > INT32_MAX sizes or device
+ * ordinals >= 64; RD_SYNCHRONIZATION when a CUDA call fails. */
+rd_status rd_render_device_noalloc(const float* d_base, uint32_t width, uint32_t height,
+                                   const rd_color_desc* color, uint8_t* d_srgb_out, uint64_t* d_hist,
+                                   void* stream);
 
 rd_status rd_source_dimensions(const rd_source* source, uint32_t* width, uint32_t* height);
 rd_status rd_source_download(rd_ctx* ctx, const rd_source* source, float* rgb_interleaved);

@@ -125,6 +125,8 @@ SIGNATURES = {
     "rd_render": (ctypes.c_int, [VOIDP, VOIDP, ctypes.POINTER(ColorDesc), U8P, U64P, U64P,
                                  ctypes.POINTER(Metrics)]),
     "rd_render_device": (ctypes.c_int, [VOIDP, VOIDP, ctypes.POINTER(ColorDesc), ctypes.POINTER(Metrics)]),
+    "rd_render_device_noalloc": (ctypes.c_int, [VOIDP, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ColorDesc),
+                                                VOIDP, VOIDP, VOIDP]),
     "rd_source_dimensions": (ctypes.c_int, [VOIDP, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32)]),
     "rd_source_download": (ctypes.c_int, [VOIDP, VOIDP, F32P]),
     "rd_base_dimensions": (ctypes.c_int, [VOIDP, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32)]),

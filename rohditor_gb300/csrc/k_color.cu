@@ -16,7 +16,9 @@
 // image once; the histogram never leaves the SM until its final flush.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
+#include <mutex>
 
 #include "rd_internal.cuh"
 
@@ -385,3 +387,117 @@ Status run_color_output(Context& ctx, const float* rgb, int W, int H, const rd_c
 }
 
 }  // namespace rd
+
+// ---- allocation-free render ------------------------------------------------
+// rd_render_device_noalloc renders a base that the caller already holds in
+// device memory into device buffers the caller owns, and allocates nothing.
+// It is for callers that cannot allocate on the render path: an interactive
+// editor re-renders the preview on every slider event, often from a UI or
+// frame-callback thread, where a device allocation can block on the allocator
+// or on device-wide synchronisation, and where the device working set has
+// been sized and reserved up front under a fixed budget. The only per-call
+// scratch of the render, the two 4096-entry LUTs, is staged in the file-scope
+// array below instead of a stream-ordered buffer.
+namespace rd {
+namespace {
+
+constexpr int NOALLOC_LUT_ENTRIES = 4096;
+constexpr int NOALLOC_MAX_DEVICES = 64;
+// Base rendering LUT at [0, 4096), tone curve LUT at [4096, 8192): 32 KB.
+__device__ __align__(256) float g_noalloc_luts[2 * NOALLOC_LUT_ENTRIES];
+
+struct NoallocDevice {
+  float* luts = nullptr;  // device address of g_noalloc_luts on this device
+  int sm_count = 0;
+};
+std::mutex g_noalloc_mutex;
+NoallocDevice g_noalloc_devices[NOALLOC_MAX_DEVICES];
+
+// Resolves the array's address once per device, with that device current.
+// The first call may load this file's module on the device.
+rd_status noalloc_device(int device, NoallocDevice* out) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  NoallocDevice& d = g_noalloc_devices[device];
+  if (!d.luts) {
+    float* p = nullptr;
+    if (cudaGetSymbolAddress(reinterpret_cast<void**>(&p), g_noalloc_luts) != cudaSuccess || !p) {
+      cudaGetLastError();
+      return RD_SYNCHRONIZATION;
+    }
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+      cudaGetLastError();
+      return RD_SYNCHRONIZATION;
+    }
+    d.luts = p;
+    d.sm_count = sms;
+  }
+  *out = d;
+  return RD_OK;
+}
+
+}  // namespace
+}  // namespace rd
+
+extern "C" rd_status rd_render_device_noalloc(const float* d_base, uint32_t width, uint32_t height,
+                                              const rd_color_desc* color, uint8_t* d_srgb_out,
+                                              uint64_t* d_hist, void* stream) {
+  using namespace rd;
+  if (!d_base || !color || !d_srgb_out || !d_hist) return RD_INVALID_INPUT;
+  if (width == 0 || height == 0 || width > (uint32_t)INT32_MAX || height > (uint32_t)INT32_MAX)
+    return RD_INVALID_INPUT;
+  int device = -1;
+  if (cudaGetDevice(&device) != cudaSuccess) {
+    cudaGetLastError();
+    return RD_SYNCHRONIZATION;
+  }
+  if (device < 0 || device >= NOALLOC_MAX_DEVICES) return RD_INVALID_INPUT;
+  NoallocDevice dev;
+  const rd_status setup = noalloc_device(device, &dev);
+  if (setup != RD_OK) return setup;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const rd_color_desc& c = *color;
+  ColorParams p{};
+  p.in = d_base;
+  p.W = (int)width;
+  p.H = (int)height;
+  p.camera_native = 0;
+  p.has_exposure = c.exposure_ev != 0.0f;
+  p.exposure_gain = std::exp2(c.exposure_ev);
+  p.has_sat = std::fabs(c.saturation - 1.0f) > F32_EPS || c.vibrance != 0.0f;
+  p.saturation = c.saturation;
+  p.vibrance = c.vibrance;
+  p.has_hsl = c.has_hsl;
+  for (int k = 0; k < 8; ++k)
+    for (int j = 0; j < 3; ++j) p.hsl[k][j] = c.hsl[k][j];
+  p.has_grading = c.has_grading;
+  for (int k = 0; k < 3; ++k)
+    for (int j = 0; j < 3; ++j) p.grading[k][j] = c.grading[k][j];
+  rec2020_to_srgb(p.out_m);
+  p.out = d_srgb_out;
+  p.hist = reinterpret_cast<unsigned long long*>(d_hist);
+  // The histogram accumulates with atomics, so it must start at zero; the LUTs
+  // are overwritten whole before the kernel reads them.
+  if (cudaMemsetAsync(d_hist, 0, 1024 * sizeof(uint64_t), s) != cudaSuccess) {
+    cudaGetLastError();
+    return RD_SYNCHRONIZATION;
+  }
+  if (c.has_base_lut &&
+      cudaMemcpyAsync(dev.luts, c.base_lut, sizeof(float) * NOALLOC_LUT_ENTRIES, cudaMemcpyHostToDevice, s) !=
+          cudaSuccess) {
+    cudaGetLastError();
+    return RD_SYNCHRONIZATION;
+  }
+  if (c.has_tone_lut && cudaMemcpyAsync(dev.luts + NOALLOC_LUT_ENTRIES, c.tone_lut,
+                                        sizeof(float) * NOALLOC_LUT_ENTRIES, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+    cudaGetLastError();
+    return RD_SYNCHRONIZATION;
+  }
+  p.base_lut = c.has_base_lut ? dev.luts : nullptr;
+  p.tone_lut = c.has_tone_lut ? dev.luts + NOALLOC_LUT_ENTRIES : nullptr;
+  const long long pixels = (long long)width * height;
+  const int grid = (int)std::min<long long>((pixels + 255) / 256, (long long)dev.sm_count * 8);
+  color_kernel<<<grid, 256, 0, s>>>(p);
+  if (cudaGetLastError() != cudaSuccess) return RD_SYNCHRONIZATION;
+  return RD_OK;
+}
