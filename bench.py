@@ -133,8 +133,8 @@ class ClockSampler:
 # (dram__bytes_read.sum + dram__bytes_write.sum); the traffic grows with the pixel count, so the
 # bench workload's traffic is this figure times its pixels.
 MEASURED_TRAFFIC_BPP = {
-    "amaze": (375.6, "profiles/amaze_kernel_4096x3072.md"),
-    "rl_iteration": (10.1, "profiles/rl_iter_kernel_4096x3072.md"),
+    "amaze": (27.1, "profiles/amaze_kernel_4096x3072.md"),
+    "rl_iteration": (10.0, "profiles/rl_stream_kernel_4096x3072.md"),
     "optics_gather": (24.9, "profiles/optics_kernel_4096x3072.md"),
 }
 

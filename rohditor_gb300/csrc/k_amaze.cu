@@ -1,29 +1,42 @@
-// AMaZE demosaic on sm_103a.
+// AMaZE demosaic on sm_103a: row-streamed tiles in shared memory.
 //
 // The reference reconstructs 256-pixel tiles with a 16-pixel mirrored halo
 // (crates/demosaic/src/amaze_geometry.rs:13-15, amaze/mod.rs:60-214), and its
-// result depends on that tile grid: each tile keeps its own Nyquist bounding
-// box (amaze/nyquist.rs:25-95) and several stages are in-place raster-order
+// result depends on that tile grid: several stages are in-place raster-order
 // recurrences whose start depends on the tile edge. This kernel keeps the grid
-// and the arithmetic bit-identical and maps the work as follows:
+// and the arithmetic bit-identical and maps one tile onto one SM:
 //
-//  * one persistent CTA (512 threads) per tile in flight; each CTA owns a
-//    scratch slot of 12 full + 14 half planes (~5 MB) that stays hot in L2;
-//  * the raw u16 samples are normalized, clipped and channel-balanced while
-//    the tile is loaded (MosaicSource), so no f32 mosaic is written to HBM;
-//  * the recurrences are restated exactly:
-//      - bound_differences (green.rs:187-222): hcd is a recurrence along each
-//        row with stride 2 and vcd along each column with stride 2; every
-//        (row, parity) and (column, parity) chain runs in its own thread;
+//  * one persistent 1024-thread CTA per SM walks tiles; a tile is processed
+//    top to bottom in steps of 8 rows. Every stage runs a fixed number of rows
+//    behind the rows loaded so far (its lag is the sum of the stencil reaches
+//    of the stages feeding it), and each plane lives in a shared-memory ring
+//    that holds just the rows still to be read;
+//  * phase A (gradients .. Nyquist test, green.rs + nyquist.rs:25-95) writes
+//    four small planes per tile (direction weight, bounded vertical and
+//    horizontal colour differences at red/blue sites, Nyquist flag: 416 KB)
+//    to an L2-resident per-CTA slab; phase B (Nyquist area .. output,
+//    nyquist.rs:108-236, diagonal.rs, chroma.rs, mod.rs:196-268) streams them
+//    back with the mosaic;
+//  * the per-tile Nyquist bounding box (nyquist.rs:60-105) only prunes work:
+//    a site outside it has at most three flagged voters and is never refined,
+//    so the streamed stages evaluate every site of [8, 248)^2 and get the same
+//    flags without a tile-wide barrier;
+//  * recurrences, restated exactly:
+//      - bound_differences (green.rs:187-222): each hcd row chain is a
+//        two-state automaton (the bounded value is one of two candidates that
+//        do not depend on the chain); one warp per chain evaluates both
+//        candidates and the state transitions of 124 steps in parallel and
+//        resolves the chain with a warp scan of the transition maps. The vcd
+//        column chains run one per thread with the chain value held in a
+//        register across steps;
 //      - populate_green / combine_diagonals (nyquist.rs:176-222,
 //        diagonal.rs:150-171): the hvwt / pmwt updates read the already
-//        updated row above, so rows are swept in order with a CTA barrier,
-//        and the per-site products that only read the final weight run as a
-//        separate parallel pass;
-//  * everything else is a parallel sweep between CTA barriers;
-//  * the tile core is written straight to the planar RGB output, with the
+//        updated row above, so one warp sweeps each recurrence row by row;
+//  * the raw u16 samples are normalized, clipped and channel-balanced while
+//    rows are loaded (MosaicSource), so no f32 mosaic is written to HBM, and
+//    the tile core is written straight to the planar RGB output with the
 //    measured sample restored, green clamped at zero and the inverse balance
-//    applied (amaze/mod.rs:196-268).
+//    applied.
 // The file is compiled with --fmad=false so no multiply-add is fused, as in
 // the reference.
 #include <cuda_runtime.h>
@@ -34,16 +47,9 @@ namespace rd {
 namespace {
 
 constexpr int TS = 256, TSH = 128, BORDER = 16, VALID = TS - 2 * BORDER;
-constexpr int FULL = TS * TS, HALFN = TS * TSH;
-constexpr int THREADS = 512;
+constexpr int THREADS = 1024;
+constexpr int BH = 8;  // rows per streaming step
 
-enum { P_CFA, P_GREEN, P_DELHV, P_W0, P_W1, P_VCD, P_HCD, P_VCDALT, P_HCDALT, P_CDD, P_DGINTV, P_DGINTH, N_FULL };
-enum { H_HVWT, H_DGRB0, H_DGRB1, H_D2H, H_D2V, H_DELP, H_DELM, H_SQ1M, H_SQ1P, H_NYQT, H_PMWT, H_RBM, H_RBP,
-       H_RBINT, N_HALF };
-// Two u8 flag planes (nyquist, nyquist2) follow, HALFN bytes each.
-constexpr size_t SLOT_FLOATS = (size_t)N_FULL * FULL + (size_t)N_HALF * HALFN + (2 * HALFN) / 4;
-
-constexpr long V1 = TS, V2 = 2 * TS, P1 = -TS + 1, P2 = -2 * TS + 2, M1 = TS + 1, M2 = 2 * TS + 2;
 constexpr float EPS = 1.0e-5f, EPSSQ = 1.0e-10f, ARTHRESH = 0.75f;
 __constant__ float GAUSSODD[4] = {0.14659727707323927f, 0.103592713382435f, 0.0732036125103057f,
                                   0.0365543548389495f};
@@ -117,30 +123,42 @@ __device__ __forceinline__ float green_from_rb(float sample, float centre, float
   return fabsf(1.0f - ratio) < ARTHRESH ? centre * ratio : sample + 0.5f * (centre - other);
 }
 
-struct Planes {
-  float* f[N_FULL];
-  float* h[N_HALF];
-  unsigned char* nyq;
-  unsigned char* nyq2;
+
+// A ring of RS rows (a power of two) of LEN elements; row r lives in slot r mod RS.
+template <int RS, int LEN, typename T = float>
+struct Ring {
+  T* p;
+  __device__ __forceinline__ T* row(int r) const { return p + (r & (RS - 1)) * LEN; }
 };
 
-__device__ __forceinline__ Planes slot_planes(float* base) {
-  Planes p;
-  for (int k = 0; k < N_FULL; ++k) p.f[k] = base + (size_t)k * FULL;
-  float* hb = base + (size_t)N_FULL * FULL;
-  for (int k = 0; k < N_HALF; ++k) p.h[k] = hb + (size_t)k * HALFN;
-  p.nyq = reinterpret_cast<unsigned char*>(hb + (size_t)N_HALF * HALFN);
-  p.nyq2 = p.nyq + HALFN;
-  return p;
-}
+// Shared-memory layout, in floats. Ring depths follow from the stage lags
+// (depth >= consumer lag - producer lag + upward reach + BH).
+// Phase A: nine 16-row full rings, an 8-row hcdalt ring, a 16-row cdd half ring.
+enum { A_CFA, A_W0, A_W1, A_DELHV, A_VCD, A_HCD, A_VALT, A_DGV, A_DGH, A_N16 };
+constexpr int A_HALT_OFF = A_N16 * 16 * TS;
+constexpr int A_CDD_OFF = A_HALT_OFF + 8 * TS;
+constexpr int A_FLOATS = A_CDD_OFF + 16 * TSH;
+// Phase B: 32-row mosaic ring; 32-row half rings for the slab planes; 16-row
+// half rings; u8 Nyquist flags (16 rows) and refined flags (32 rows).
+constexpr int B_CFA_OFF = 0;
+constexpr int B_HV_OFF = B_CFA_OFF + 32 * TS;
+constexpr int B_VRB_OFF = B_HV_OFF + 32 * TSH;
+constexpr int B_HRB_OFF = B_VRB_OFF + 32 * TSH;
+enum { B_DGRB0, B_DGRB1, B_GREEN, B_D2H, B_D2V, B_DELP, B_DELM, B_SQP, B_SQM, B_PMWT, B_RBP, B_RBM, B_RBINT, B_N16 };
+constexpr int B_H16_OFF = B_HRB_OFF + 32 * TSH;
+constexpr int B_U8_OFF = B_H16_OFF + B_N16 * 16 * TSH;
+constexpr int B_FLOATS = B_U8_OFF + (16 * TSH + 32 * TSH) / 4;
+constexpr int SMEM_FLOATS = A_FLOATS > B_FLOATS ? A_FLOATS : B_FLOATS;
+constexpr size_t SMEM_BYTES = sizeof(float) * SMEM_FLOATS;
 
-// Number of red/blue sites in [c0 + gae, c1) with step 2.
-__device__ __forceinline__ int site_count(int c0, int c1) { return (c1 - c0 + 1) / 2; }
+// Per-CTA slab in global memory: hvwt, vcd, hcd at red/blue sites (half
+// planes) and the Nyquist flags (u8 half plane).
+constexpr size_t SLAB_FLOATS = 3 * (size_t)TS * TSH + (size_t)TS * TSH / 4;
 
 struct AmazeParams {
   MosaicSource src;
   float* out;              // planar RGB, 3 * width * height
-  float* scratch;          // SLOT_FLOATS per CTA
+  float* slab;             // SLAB_FLOATS per CTA
   int tiles_x, tiles_y;
   float clip_point;
   float gains[3];          // inverse balance applied to the output
@@ -149,591 +167,746 @@ struct AmazeParams {
   unsigned int* error;
 };
 
-__global__ void __launch_bounds__(THREADS, 2) amaze_kernel(const AmazeParams prm) {
+// Mosaic sample at image coordinates (x, y), mirrored into the image when outside it.
+__device__ __forceinline__ float tile_sample(const MosaicSource& src, int x, int y, int W, int H) {
+  const int sx = (unsigned)x < (unsigned)W ? x : mirror_index(x, W);
+  const int sy = (unsigned)y < (unsigned)H ? y : mirror_index(y, H);
+  return source_balanced(src, sx, sy);
+}
+
+// Two-state transition maps: bit 0 = next state after state A, bit 1 = after
+// state B (0 = A, 1 = B). compose(m, o) applies o first, then m.
+__device__ __forceinline__ unsigned compose(unsigned m, unsigned o) {
+  return ((m >> (o & 1u)) & 1u) | (((m >> ((o >> 1) & 1u)) & 1u) << 1);
+}
+
+__device__ __forceinline__ float bound_sel(bool green_site, float d, float cur, float a, float b, float clip_pt) {
+  return green_site ? bound_at_green(d, cur, a, b, clip_pt) : bound_at_red_blue(d, cur, a, b, clip_pt);
+}
+
+__global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm) {
+  extern __shared__ float4 amaze_smem4[];
+  float* sm = reinterpret_cast<float*>(amaze_smem4);
+  __shared__ unsigned long long s_stats[6];
+  __shared__ int s_bad;
   const MosaicSource& src = prm.src;
-  Planes P = slot_planes(prm.scratch + (size_t)blockIdx.x * SLOT_FLOATS);
-  float* cfa = P.f[P_CFA];
-  float* green = P.f[P_GREEN];
-  float* w0 = P.f[P_W0];
-  float* w1 = P.f[P_W1];
-  float* vcd = P.f[P_VCD];
-  float* hcd = P.f[P_HCD];
-  float* vcdalt = P.f[P_VCDALT];
-  float* hcdalt = P.f[P_HCDALT];
-  float* cdd = P.f[P_CDD];
-  float* delhv = P.f[P_DELHV];
-  float* dgintv = P.f[P_DGINTV];
-  float* dginth = P.f[P_DGINTH];
-  float* hvwt = P.h[H_HVWT];
-  float* dgrb0 = P.h[H_DGRB0];
-  float* dgrb1 = P.h[H_DGRB1];
-  float* d2h = P.h[H_D2H];
-  float* d2v = P.h[H_D2V];
-  float* pmwt = P.h[H_PMWT];
-  const int t = threadIdx.x;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const unsigned FULL = 0xffffffffu;
   const int pattern = src.cfa;
   const float clip_pt = prm.clip_point;
   const float clip_pt8 = 0.8f * clip_pt;
   const int W = src.width, H = src.height;
   const long long plane = (long long)W * H;
-  __shared__ int s_box[4];
-  __shared__ unsigned long long s_stats[6];
-  __shared__ int s_bad;
+  float* slab = prm.slab + (size_t)blockIdx.x * SLAB_FLOATS;
+  float* g_hv = slab;
+  float* g_vrb = slab + TS * TSH;
+  float* g_hrb = slab + 2 * TS * TSH;
+  unsigned char* g_nyq = reinterpret_cast<unsigned char*>(slab + 3 * TS * TSH);
+  // Rows holding blue sites: interpolate_chroma moves their differences to dgrb1 (chroma.rs:23-44).
+  int ey;
+  {
+    const int c00 = color_at(pattern, 0, 0), c10 = color_at(pattern, 1, 0);
+    if (c00 == 1 && c10 == 0) ey = 0;
+    else if (c00 == 1) ey = 1;
+    else if (c00 == 0) ey = 0;
+    else ey = 1;
+  }
+  const int blue_par = (13 - ey) & 1;
 
   const int ntiles = prm.tiles_x * prm.tiles_y;
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int ox = (tile % prm.tiles_x) * VALID, oy = (tile / prm.tiles_x) * VALID;
 
-    // ---- populate (mod.rs:175-194) and per-tile clears (scratch.rs:105-111)
-    for (int k = t; k < FULL; k += THREADS) {
-      const int row = k >> 8, col = k & (TS - 1);
-      const int sx = mirror_index(ox - BORDER + col, W), sy = mirror_index(oy - BORDER + row, H);
-      const float v = source_balanced(src, sx, sy);
-      cfa[k] = v;
-      green[k] = v;
-    }
-    for (int k = t; k < HALFN; k += THREADS) {
-      P.nyq[k] = 0;
-      P.nyq2[k] = 0;
-      d2h[k] = 0.0f;
-      d2v[k] = 0.0f;
-    }
+    // ================= phase A: green.rs:13-292, nyquist.rs:25-95 =================
+    for (int k = t; k < A_FLOATS; k += THREADS) sm[k] = 0.0f;
     if (t < 6) s_stats[t] = 0;
-    if (t == 0) {
-      s_box[0] = TS; s_box[1] = 0; s_box[2] = TS + 1; s_box[3] = 0;
-      s_bad = 0;
-    }
+    if (t == 0) s_bad = 0;
     __syncthreads();
-
-    // ---- gradients (green.rs:13-29)
-    for (int k = t; k < (TS - 4) * (TS - 4); k += THREADS) {
-      const int rr = 2 + k / (TS - 4), cc = 2 + k % (TS - 4);
-      const int i = rr * TS + cc;
-      const float delh = fabsf(cfa[i + 1] - cfa[i - 1]);
-      const float delv = fabsf(cfa[i + TS] - cfa[i - TS]);
-      w0[i] = EPS + fabsf(cfa[i + 2 * TS] - cfa[i]) + fabsf(cfa[i] - cfa[i - 2 * TS]) + delv;
-      w1[i] = EPS + fabsf(cfa[i + 2] - cfa[i]) + fabsf(cfa[i] - cfa[i - 2]) + delh;
-      delhv[i] = sqr(delh) + sqr(delv);
-    }
-    __syncthreads();
-
-    // ---- colour differences (green.rs:46-139)
-    for (int k = t; k < (TS - 8) * (TS - 8); k += THREADS) {
-      const int rr = 4 + k / (TS - 8), cc = 4 + k % (TS - 8);
-      const int i = rr * TS + cc;
-      const bool green_first = (fc(pattern, rr, 4) & 1) == 1;
-      const bool fcswitch = green_first == ((cc & 1) == 0);
-      const float cur = cfa[i];
-      const float up = cfa[i - TS], up2 = cfa[i - 2 * TS], down = cfa[i + TS], down2 = cfa[i + 2 * TS];
-      const float left = cfa[i - 1], left2 = cfa[i - 2], right = cfa[i + 1], right2 = cfa[i + 2];
-      const float cru = up * (w0[i - 2 * TS] + w0[i]) / (w0[i - 2 * TS] * (EPS + cur) + w0[i] * (EPS + up2));
-      const float crd = down * (w0[i + 2 * TS] + w0[i]) / (w0[i + 2 * TS] * (EPS + cur) + w0[i] * (EPS + down2));
-      const float crl = left * (w1[i - 2] + w1[i]) / (w1[i - 2] * (EPS + cur) + w1[i] * (EPS + left2));
-      const float crr = right * (w1[i + 2] + w1[i]) / (w1[i + 2] * (EPS + cur) + w1[i] * (EPS + right2));
-      const float guha = up + 0.5f * (cur - up2);
-      const float gdha = down + 0.5f * (cur - down2);
-      const float glha = left + 0.5f * (cur - left2);
-      const float grha = right + 0.5f * (cur - right2);
-      float guar = adaptive_or(cru, cur, guha);
-      float gdar = adaptive_or(crd, cur, gdha);
-      float glar = adaptive_or(crl, cur, glha);
-      float grar = adaptive_or(crr, cur, grha);
-      const float hwt = w1[i - 1] / (w1[i - 1] + w1[i + 1]);
-      const float vwt = w0[i - TS] / (w0[i + TS] + w0[i - TS]);
-      const float gintvha = vwt * gdha + (1.0f - vwt) * guha;
-      const float ginthha = hwt * grha + (1.0f - hwt) * glha;
-      float v, h, va, ha;
-      if (fcswitch) {
-        v = cur - (vwt * gdar + (1.0f - vwt) * guar);
-        h = cur - (hwt * grar + (1.0f - hwt) * glar);
-        va = cur - gintvha;
-        ha = cur - ginthha;
-      } else {
-        v = (vwt * gdar + (1.0f - vwt) * guar) - cur;
-        h = (hwt * grar + (1.0f - hwt) * glar) - cur;
-        va = gintvha - cur;
-        ha = ginthha - cur;
-      }
-      const bool clipped = (cur > clip_pt8) | (gintvha > clip_pt8) | (ginthha > clip_pt8);
-      if (clipped) {
-        guar = guha; gdar = gdha; glar = glha; grar = grha;
-        v = va; h = ha;
-      }
-      dgintv[i] = fmin_(sqr(guha - gdha), sqr(guar - gdar));
-      dginth[i] = fmin_(sqr(glha - grha), sqr(glar - grar));
-      vcd[i] = v;
-      hcd[i] = h;
-      vcdalt[i] = va;
-      hcdalt[i] = ha;
-    }
-    __syncthreads();
-
-    // ---- bound_differences (green.rs:187-222): exact chain restatement.
-    if (t < 2 * (TS - 8)) {
-      const int line = 4 + (t >> 1), par = t & 1;
-      // Horizontal chain: row `line`, columns 4+par, 6+par, ...
-      const int hr = line;
-      const bool hg4 = (fc(pattern, hr, 4) & 1) == 1;
-      float prev_h = hcd[hr * TS + 2 + par];
-      // Vertical chain: column `line`, rows 4+par, 6+par, ...
-      const int vc = line;
-      float prev_v = vcd[(2 + par) * TS + vc];
-      for (int k = 0; k < (TS - 8) / 2; ++k) {
-        {
-          const int cc = 4 + par + 2 * k;
-          const int i = hr * TS + cc;
-          const float hcdvar = spread(prev_h, hcd[i], hcd[i + 2]);
-          const float hcdaltvar = spread(hcdalt[i - 2], hcdalt[i], hcdalt[i + 2]);
-          const float hsel = hcdaltvar < hcdvar ? hcdalt[i] : hcd[i];
-          const bool g = hg4 != (((cc - 4) & 1) == 1);
-          const float cur = cfa[i];
-          const float b = g ? bound_at_green(hsel, cur, cfa[i - 1], cfa[i + 1], clip_pt)
-                            : bound_at_red_blue(hsel, cur, cfa[i - 1], cfa[i + 1], clip_pt);
-          hcd[i] = b;
-          prev_h = b;
-        }
-        {
-          const int rr = 4 + par + 2 * k;
-          const int i = rr * TS + vc;
-          const float vcdvar = spread(prev_v, vcd[i], vcd[i + 2 * TS]);
-          const float vcdaltvar = spread(vcdalt[i - 2 * TS], vcdalt[i], vcdalt[i + 2 * TS]);
-          const float vsel = vcdaltvar < vcdvar ? vcdalt[i] : vcd[i];
-          const bool g = ((fc(pattern, rr, 4) & 1) == 1) != (((vc - 4) & 1) == 1);
-          const float cur = cfa[i];
-          const float b = g ? bound_at_green(vsel, cur, cfa[i - TS], cfa[i + TS], clip_pt)
-                            : bound_at_red_blue(vsel, cur, cfa[i - TS], cfa[i + TS], clip_pt);
-          vcd[i] = b;
-          prev_v = b;
-        }
-      }
-    }
-    __syncthreads();
-    for (int k = t; k < (TS - 8) * (TS - 8); k += THREADS) {
-      const int rr = 4 + k / (TS - 8), cc = 4 + k % (TS - 8);
-      const bool g = ((fc(pattern, rr, 4) & 1) == 1) != (((cc - 4) & 1) == 1);
-      if (!g) {
-        const int i = rr * TS + cc;
-        cdd[i] = sqr(vcd[i] - hcd[i]);
-      }
-    }
-    __syncthreads();
-
-    // ---- direction_weights (green.rs:225-292)
     {
-      const int per_row = site_count(6, TS - 6);
-      for (int k = t; k < (TS - 12) * per_row; k += THREADS) {
-        const int rr = 6 + k / per_row;
-        const int cc = 6 + gae(pattern, rr) + 2 * (k % per_row);
-        if (cc >= TS - 6) continue;
-        const int i = rr * TS + cc;
-        const float uave = vcd[i] + vcd[i - TS] + vcd[i - 2 * TS] + vcd[i - 3 * TS];
-        const float dave = vcd[i] + vcd[i + TS] + vcd[i + 2 * TS] + vcd[i + 3 * TS];
-        const float lave = hcd[i] + hcd[i - 1] + hcd[i - 2] + hcd[i - 3];
-        const float rave = hcd[i] + hcd[i + 1] + hcd[i + 2] + hcd[i + 3];
-        const float vu = sqr(vcd[i] - uave) + sqr(vcd[i - TS] - uave) + sqr(vcd[i - 2 * TS] - uave) + sqr(vcd[i - 3 * TS] - uave);
-        const float vd = sqr(vcd[i] - dave) + sqr(vcd[i + TS] - dave) + sqr(vcd[i + 2 * TS] - dave) + sqr(vcd[i + 3 * TS] - dave);
-        const float hl = sqr(hcd[i] - lave) + sqr(hcd[i - 1] - lave) + sqr(hcd[i - 2] - lave) + sqr(hcd[i - 3] - lave);
-        const float hrr = sqr(hcd[i] - rave) + sqr(hcd[i + 1] - rave) + sqr(hcd[i + 2] - rave) + sqr(hcd[i + 3] - rave);
-        const float hwt = w1[i - 1] / (w1[i - 1] + w1[i + 1]);
-        const float vwt = w0[i - TS] / (w0[i + TS] + w0[i - TS]);
-        const float vcdvar = EPSSQ + vwt * vd + (1.0f - vwt) * vu;
-        const float hcdvar = EPSSQ + hwt * hrr + (1.0f - hwt) * hl;
-        const float fu = dgintv[i] + dgintv[i - TS] + dgintv[i - 2 * TS];
-        const float fd = dgintv[i] + dgintv[i + TS] + dgintv[i + 2 * TS];
-        const float fl = dginth[i] + dginth[i - 1] + dginth[i - 2];
-        const float fr = dginth[i] + dginth[i + 1] + dginth[i + 2];
-        const float vcdvar1 = EPSSQ + vwt * fd + (1.0f - vwt) * fu;
-        const float hcdvar1 = EPSSQ + hwt * fr + (1.0f - hwt) * fl;
-        const float varwt = hcdvar / (vcdvar + hcdvar);
-        const float diffwt = hcdvar1 / (vcdvar1 + hcdvar1);
-        hvwt[i >> 1] = ((0.5f - varwt) * (0.5f - diffwt) > 0.0f && fabsf(0.5f - diffwt) < fabsf(0.5f - varwt))
-                           ? varwt
-                           : diffwt;
-      }
-    }
-    __syncthreads();
-
-    // ---- Nyquist test (nyquist.rs:25-95)
-    {
-      float* nyqt = P.h[H_NYQT];
-      const float* c = cdd;
-      const float* d = delhv;
-      const int per_row = site_count(6, TS - 6);
-      for (int k = t; k < (TS - 12) * per_row; k += THREADS) {
-        const int rr = 6 + k / per_row;
-        const int cc = 6 + gae(pattern, rr) + 2 * (k % per_row);
-        if (cc >= TS - 6) continue;
-        const int i = rr * TS + cc;
-        const float v =
-            (GAUSSODD[0] * c[i] + GAUSSODD[1] * (c[i - TS - 1] + c[i - TS + 1] + c[i + TS - 1] + c[i + TS + 1]) +
-             GAUSSODD[2] * (c[i - 2 * TS] + c[i - 2] + c[i + 2] + c[i + 2 * TS]) +
-             GAUSSODD[3] * (c[i - 2 * TS - 2] + c[i - 2 * TS + 2] + c[i + 2 * TS - 2] + c[i + 2 * TS + 2])) -
-            (GAUSSGRAD[0] * d[i] + GAUSSGRAD[1] * (d[i - TS] + d[i + 1] + d[i - 1] + d[i + TS]) +
-             GAUSSGRAD[2] * (d[i - TS - 1] + d[i - TS + 1] + d[i + TS - 1] + d[i + TS + 1]) +
-             GAUSSGRAD[3] * (d[i - 2 * TS] + d[i - 2] + d[i + 2] + d[i + 2 * TS]) +
-             GAUSSGRAD[4] * (d[i - 2 * TS - 1] + d[i - 2 * TS + 1] + d[i - TS - 2] + d[i - TS + 2] + d[i + TS - 2] +
-                             d[i + TS + 2] + d[i + 2 * TS - 1] + d[i + 2 * TS + 1]) +
-             GAUSSGRAD[5] * (d[i - 2 * TS - 2] + d[i - 2 * TS + 2] + d[i + 2 * TS - 2] + d[i + 2 * TS + 2]));
-        nyqt[i >> 1] = v;
-        if (v > 0.0f) {
-          P.nyq[i >> 1] = 1;
-          atomicMin(&s_box[0], rr);
-          atomicMax(&s_box[1], rr);
-          atomicMin(&s_box[2], cc);
-          atomicMax(&s_box[3], cc);
-        }
-      }
-    }
-    __syncthreads();
-    int start_row = s_box[0], end_row = s_box[1], start_col = s_box[2], end_col = s_box[3];
-    if (start_row == TS) start_row = 0;  // no flagged site
-    const bool has_area = !(start_row == end_row || start_col == end_col);
-    if (has_area) {
-      end_row += 1;
-      end_col += 1;
-      start_col -= start_col & 1;
-      start_row = max(start_row, 8);
-      end_row = min(end_row, TS - 8);
-      start_col = max(start_col, 8);
-      end_col = min(end_col, TS - 8);
-    }
-    const int area_rows = has_area ? max(end_row - start_row, 0) : 0;
-    const int area_sites = has_area ? (end_col - start_col + 1) / 2 + 1 : 0;
-
-    // ---- area interpolation (nyquist.rs:108-170)
-    if (has_area) {
-      for (int k = t; k < area_rows * area_sites; k += THREADS) {
-        const int rr = start_row + k / area_sites;
-        const long i = (long)rr * TS + start_col + gae(pattern, rr) + 2 * (k % area_sites);
-        if (i >= (long)rr * TS + end_col) continue;
-        const unsigned char* n = P.nyq;
-        const unsigned votes = n[(i - V2) >> 1] + n[(i - M1) >> 1] + n[(i + P1) >> 1] + n[(i - 2) >> 1] +
-                               n[(i + 2) >> 1] + n[(i - P1) >> 1] + n[(i + M1) >> 1] + n[(i + V2) >> 1];
-        P.nyq2[i >> 1] = votes >= 5 ? 1 : (votes == 4 ? n[i >> 1] : 0);
-      }
-      __syncthreads();
-      for (int k = t; k < area_rows * area_sites; k += THREADS) {
-        const int rr = start_row + k / area_sites;
-        const long i = (long)rr * TS + start_col + gae(pattern, rr) + 2 * (k % area_sites);
-        if (i >= (long)rr * TS + end_col) continue;
-        if (P.nyq2[i >> 1] == 0) continue;
-        float sumcfa = 0.0f, sumh = 0.0f, sumv = 0.0f, sumsqh = 0.0f, sumsqv = 0.0f, areawt = 0.0f;
-        for (int di = -6; di < 7; di += 2) {
-          long i1 = i + di * V1 - 6;
-          for (int dj = -6; dj < 7; dj += 2) {
-            if (P.nyq2[i1 >> 1] != 0) {
-              const float c = cfa[i1];
-              sumcfa += c;
-              sumh += cfa[i1 - 1] + cfa[i1 + 1];
-              sumv += cfa[i1 - V1] + cfa[i1 + V1];
-              sumsqh += sqr(c - cfa[i1 - 1]) + sqr(c - cfa[i1 + 1]);
-              sumsqv += sqr(c - cfa[i1 - V1]) + sqr(c - cfa[i1 + V1]);
-              areawt += 1.0f;
-            }
-            i1 += 2;
+      const Ring<16, TS> cfa{sm + A_CFA * 16 * TS}, w0{sm + A_W0 * 16 * TS}, w1{sm + A_W1 * 16 * TS},
+          delhv{sm + A_DELHV * 16 * TS}, vcd{sm + A_VCD * 16 * TS}, hcd{sm + A_HCD * 16 * TS},
+          valt{sm + A_VALT * 16 * TS}, dgv{sm + A_DGV * 16 * TS}, dgh{sm + A_DGH * 16 * TS};
+      const Ring<8, TS> halt{sm + A_HALT_OFF};
+      const Ring<16, TSH> cdd{sm + A_CDD_OFF};
+      float vprev = 0.0f;  // vcd column chain value (threads 512..1007)
+      for (int F = BH; F <= TS + 8; F += BH) {
+        // -- load rows [F-8, F): populate (mod.rs:175-194)
+        {
+          const int lo = F - BH, hi = min(F, TS);
+          for (int k = t; k < (hi - lo) * TS; k += THREADS) {
+            const int rr = lo + (k >> 8), cc = k & (TS - 1);
+            cfa.row(rr)[cc] = tile_sample(src, ox - BORDER + cc, oy - BORDER + rr, W, H);
           }
         }
-        sumh = sumcfa - 0.5f * sumh;
-        sumv = sumcfa - 0.5f * sumv;
-        areawt *= 0.5f;
-        const float hcdvar = EPSSQ + fabsf(areawt * sumsqh - sumh * sumh);
-        const float vcdvar = EPSSQ + fabsf(areawt * sumsqv - sumv * sumv);
-        hvwt[i >> 1] = hcdvar / (vcdvar + hcdvar);
-      }
-    }
-    __syncthreads();
-
-    // ---- populate_green (nyquist.rs:176-222): row-ordered hvwt update ...
-    for (int rr = 8; rr < TS - 8; ++rr) {
-      const int cc = 8 + gae(pattern, rr) + 2 * t;
-      if (t < site_count(8, TS - 8) && cc < TS - 8) {
-        const int i1 = (rr * TS + cc) >> 1;
-        const float alt = (hvwt[((rr - 1) * TS + cc - 1) >> 1] + hvwt[((rr - 1) * TS + cc + 1) >> 1] +
-                           hvwt[((rr + 1) * TS + cc - 1) >> 1] + hvwt[((rr + 1) * TS + cc + 1) >> 1]) /
-                          4.0f;
-        if (fabsf(0.5f - hvwt[i1]) < fabsf(0.5f - alt)) hvwt[i1] = alt;
-      }
-      __syncthreads();
-    }
-    // ... then the per-site products, which read only final weights.
-    {
-      const int per_row = site_count(8, TS - 8);
-      for (int k = t; k < (TS - 16) * per_row; k += THREADS) {
-        const int rr = 8 + k / per_row;
-        const int cc = 8 + gae(pattern, rr) + 2 * (k % per_row);
-        if (cc >= TS - 8) continue;
-        const int i = rr * TS + cc, i1 = i >> 1;
-        const float dg = intp(hvwt[i1], vcd[i], hcd[i]);
-        dgrb0[i1] = dg;
-        const float gv = cfa[i] + dg;
-        green[i] = gv;
-        const bool flagged = P.nyq2[i1] != 0;
-        d2h[i1] = flagged ? sqr(gv - 0.5f * (green[i - 1] + green[i + 1])) : 0.0f;
-        d2v[i1] = flagged ? sqr(gv - 0.5f * (green[i - TS] + green[i + TS])) : 0.0f;
-      }
-    }
-    __syncthreads();
-
-    // ---- refine_green (nyquist.rs:225-236)
-    if (has_area) {
-      for (int k = t; k < area_rows * area_sites; k += THREADS) {
-        const int rr = start_row + k / area_sites;
-        const long i = (long)rr * TS + start_col + gae(pattern, rr) + 2 * (k % area_sites);
-        if (i >= (long)rr * TS + end_col) continue;
-        if (P.nyq2[i >> 1] == 0) continue;
-        const float gvarh = EPSSQ + (GQUINC[0] * d2h[i >> 1] +
-                                     GQUINC[1] * (d2h[(i - M1) >> 1] + d2h[(i + P1) >> 1] + d2h[(i - P1) >> 1] + d2h[(i + M1) >> 1]) +
-                                     GQUINC[2] * (d2h[(i - V2) >> 1] + d2h[(i - 2) >> 1] + d2h[(i + 2) >> 1] + d2h[(i + V2) >> 1]) +
-                                     GQUINC[3] * (d2h[(i - M2) >> 1] + d2h[(i + P2) >> 1] + d2h[(i - P2) >> 1] + d2h[(i + M2) >> 1]));
-        const float gvarv = EPSSQ + (GQUINC[0] * d2v[i >> 1] +
-                                     GQUINC[1] * (d2v[(i - M1) >> 1] + d2v[(i + P1) >> 1] + d2v[(i - P1) >> 1] + d2v[(i + M1) >> 1]) +
-                                     GQUINC[2] * (d2v[(i - V2) >> 1] + d2v[(i - 2) >> 1] + d2v[(i + 2) >> 1] + d2v[(i + V2) >> 1]) +
-                                     GQUINC[3] * (d2v[(i - M2) >> 1] + d2v[(i + P2) >> 1] + d2v[(i - P2) >> 1] + d2v[(i + M2) >> 1]));
-        const float dg = (hcd[i] * gvarv + vcd[i] * gvarh) / (gvarv + gvarh);
-        dgrb0[i >> 1] = dg;
-        green[i] = cfa[i] + dg;
-      }
-    }
-    __syncthreads();
-
-    // ---- diagonal_gradients (diagonal.rs:15-45)
-    {
-      float* delp = P.h[H_DELP];
-      float* delm = P.h[H_DELM];
-      float* sqp = P.h[H_SQ1P];
-      float* sqm = P.h[H_SQ1M];
-      const int per_row = site_count(6, TS - 6) ;
-      for (int k = t; k < (TS - 12) * per_row; k += THREADS) {
-        const int rr = 6 + k / per_row;
-        const int cc = 6 + 2 * (k % per_row);
-        if (cc >= TS - 6) continue;
-        const float* up = cfa + (rr - 1) * TS;
-        const float* mid = cfa + rr * TS;
-        const float* down = cfa + (rr + 1) * TS;
-        const int i1 = rr * TSH + (cc >> 1);
-        if (gae(pattern, rr) == 0) {
-          delp[i1] = fabsf(up[cc + 1] - down[cc - 1]);
-          delm[i1] = fabsf(down[cc + 1] - up[cc - 1]);
-          const float g = mid[cc + 1];
-          sqp[i1] = sqr(g - down[cc]) + sqr(g - up[cc + 2]);
-          sqm[i1] = sqr(g - up[cc]) + sqr(g - down[cc + 2]);
-        } else {
-          const float g = mid[cc];
-          sqp[i1] = sqr(g - down[cc - 1]) + sqr(g - up[cc + 1]);
-          sqm[i1] = sqr(g - up[cc - 1]) + sqr(g - down[cc + 1]);
-          delp[i1] = fabsf(up[cc + 2] - down[cc]);
-          delm[i1] = fabsf(down[cc + 2] - up[cc]);
+        __syncthreads();
+        // -- gradients (green.rs:13-29), lag 2, rows/cols [2, 254)
+        {
+          const int lo = max(F - BH - 2, 2), hi = min(F - 2, TS - 2);
+          for (int k = t; k < (hi - lo) * (TS - 4); k += THREADS) {
+            const int rr = lo + k / (TS - 4), cc = 2 + k % (TS - 4);
+            const float* c0 = cfa.row(rr);
+            const float* cu = cfa.row(rr - 1);
+            const float* cd = cfa.row(rr + 1);
+            const float delh = fabsf(c0[cc + 1] - c0[cc - 1]);
+            const float delv = fabsf(cd[cc] - cu[cc]);
+            w0.row(rr)[cc] = EPS + fabsf(cfa.row(rr + 2)[cc] - c0[cc]) + fabsf(c0[cc] - cfa.row(rr - 2)[cc]) + delv;
+            w1.row(rr)[cc] = EPS + fabsf(c0[cc + 2] - c0[cc]) + fabsf(c0[cc] - c0[cc - 2]) + delh;
+            delhv.row(rr)[cc] = sqr(delh) + sqr(delv);
+          }
         }
+        __syncthreads();
+        // -- colour differences (green.rs:46-139), lag 4, rows/cols [4, 252)
+        {
+          const int lo = max(F - BH - 4, 4), hi = min(F - 4, TS - 4);
+          for (int k = t; k < (hi - lo) * (TS - 8); k += THREADS) {
+            const int rr = lo + k / (TS - 8), cc = 4 + k % (TS - 8);
+            const bool green_first = (fc(pattern, rr, 4) & 1) == 1;
+            const bool fcswitch = green_first == ((cc & 1) == 0);
+            const float* c0 = cfa.row(rr);
+            const float cur = c0[cc];
+            const float up = cfa.row(rr - 1)[cc], up2 = cfa.row(rr - 2)[cc];
+            const float down = cfa.row(rr + 1)[cc], down2 = cfa.row(rr + 2)[cc];
+            const float left = c0[cc - 1], left2 = c0[cc - 2], right = c0[cc + 1], right2 = c0[cc + 2];
+            const float w0c = w0.row(rr)[cc], w0u2 = w0.row(rr - 2)[cc], w0d2 = w0.row(rr + 2)[cc];
+            const float* w1r = w1.row(rr);
+            const float w1c = w1r[cc];
+            const float cru = up * (w0u2 + w0c) / (w0u2 * (EPS + cur) + w0c * (EPS + up2));
+            const float crd = down * (w0d2 + w0c) / (w0d2 * (EPS + cur) + w0c * (EPS + down2));
+            const float crl = left * (w1r[cc - 2] + w1c) / (w1r[cc - 2] * (EPS + cur) + w1c * (EPS + left2));
+            const float crr = right * (w1r[cc + 2] + w1c) / (w1r[cc + 2] * (EPS + cur) + w1c * (EPS + right2));
+            const float guha = up + 0.5f * (cur - up2);
+            const float gdha = down + 0.5f * (cur - down2);
+            const float glha = left + 0.5f * (cur - left2);
+            const float grha = right + 0.5f * (cur - right2);
+            float guar = adaptive_or(cru, cur, guha);
+            float gdar = adaptive_or(crd, cur, gdha);
+            float glar = adaptive_or(crl, cur, glha);
+            float grar = adaptive_or(crr, cur, grha);
+            const float hwt = w1r[cc - 1] / (w1r[cc - 1] + w1r[cc + 1]);
+            const float w0u = w0.row(rr - 1)[cc], w0d = w0.row(rr + 1)[cc];
+            const float vwt = w0u / (w0d + w0u);
+            const float gintvha = vwt * gdha + (1.0f - vwt) * guha;
+            const float ginthha = hwt * grha + (1.0f - hwt) * glha;
+            float v, h, va, ha;
+            if (fcswitch) {
+              v = cur - (vwt * gdar + (1.0f - vwt) * guar);
+              h = cur - (hwt * grar + (1.0f - hwt) * glar);
+              va = cur - gintvha;
+              ha = cur - ginthha;
+            } else {
+              v = (vwt * gdar + (1.0f - vwt) * guar) - cur;
+              h = (hwt * grar + (1.0f - hwt) * glar) - cur;
+              va = gintvha - cur;
+              ha = ginthha - cur;
+            }
+            const bool clipped = (cur > clip_pt8) | (gintvha > clip_pt8) | (ginthha > clip_pt8);
+            if (clipped) {
+              guar = guha; gdar = gdha; glar = glha; grar = grha;
+              v = va; h = ha;
+            }
+            dgv.row(rr)[cc] = fmin_(sqr(guha - gdha), sqr(guar - gdar));
+            dgh.row(rr)[cc] = fmin_(sqr(glha - grha), sqr(glar - grar));
+            vcd.row(rr)[cc] = v;
+            hcd.row(rr)[cc] = h;
+            valt.row(rr)[cc] = va;
+            halt.row(rr)[cc] = ha;
+          }
+        }
+        __syncthreads();
+        // -- bound_differences (green.rs:187-222)
+        if (warp < 16) {
+          // hcd row chain of row F-12+warp/2, parity warp&1, lag 4: one warp per chain, in
+          // four rounds of 32 consecutive steps (one step per lane).
+          const int rr = F - 12 + (warp >> 1), par = warp & 1;
+          if (rr >= 4 && rr < TS - 4) {
+            float* hr = hcd.row(rr);
+            const float* ha = halt.row(rr);
+            const float* c0 = cfa.row(rr);
+            const bool hg4 = (fc(pattern, rr, 4) & 1) == 1;
+            constexpr int STEPS = (TS - 8) / 2;  // 124 sites per chain
+            unsigned s_in = 0;                   // chain state after the previous round
+            float last_a = 0.0f, last_b = 0.0f;  // candidates of the previous round's last step
+#pragma unroll
+            for (int round = 0; round < 4; ++round) {
+              const int k = 32 * round + lane;
+              const int cc = 4 + par + 2 * k;
+              const bool valid = k < STEPS;
+              float ca = 0.0f, cb = 0.0f, hk = 0.0f, hk1 = 0.0f, av = 0.0f;
+              if (valid) {
+                const bool g = hg4 != (((cc - 4) & 1) == 1);
+                const float cur = c0[cc];
+                hk = hr[cc];
+                hk1 = hr[cc + 2];
+                av = spread(ha[cc - 2], ha[cc], ha[cc + 2]);
+                ca = bound_sel(g, ha[cc], cur, c0[cc - 1], c0[cc + 1], clip_pt);
+                cb = bound_sel(g, hk, cur, c0[cc - 1], c0[cc + 1], clip_pt);
+              }
+              float pa = __shfl_up_sync(FULL, ca, 1), pb = __shfl_up_sync(FULL, cb, 1);
+              if (lane == 0) {
+                pa = last_a;
+                pb = last_b;
+              }
+              unsigned m;
+              if (!valid) {
+                m = 2u;  // identity
+              } else if (k == 0) {
+                // The chain starts from hcd at column 2 + par, which is zero.
+                const unsigned s0 = av < spread(0.0f, hk, hk1) ? 0u : 1u;
+                m = s0 | (s0 << 1);
+              } else {
+                const unsigned sa = av < spread(pa, hk, hk1) ? 0u : 1u;
+                const unsigned sb = av < spread(pb, hk, hk1) ? 0u : 1u;
+                m = sa | (sb << 1);
+              }
+#pragma unroll
+              for (int d = 1; d < 32; d <<= 1) {
+                const unsigned o = __shfl_up_sync(FULL, m, d);
+                if (lane >= d) m = compose(m, o);
+              }
+              const unsigned st = (m >> s_in) & 1u;  // state after this lane's step
+              __syncwarp();
+              if (valid) hr[cc] = st ? cb : ca;
+              s_in = __shfl_sync(FULL, st, 31);
+              last_a = __shfl_sync(FULL, ca, 31);
+              last_b = __shfl_sync(FULL, cb, 31);
+            }
+          }
+        } else if (t >= 512 && t < 512 + 2 * (TS - 8)) {
+          // vcd column chains, lag 6: column vc, rows 4+par, 6+par, ... in order.
+          const int u = t - 512, vc = 4 + u % (TS - 8), par = u / (TS - 8);
+          const int lo = max(F - BH - 6, 4), hi = min(F - 6, TS - 4);
+          const bool vg4 = ((vc - 4) & 1) == 1;
+          for (int rr = lo + ((lo ^ par) & 1); rr < hi; rr += 2) {
+            const float vcur = vcd.row(rr)[vc];
+            const float vnext = rr + 2 < TS - 4 ? vcd.row(rr + 2)[vc] : 0.0f;
+            const float aprev = rr - 2 >= 4 ? valt.row(rr - 2)[vc] : 0.0f;
+            const float acur = valt.row(rr)[vc];
+            const float anext = rr + 2 < TS - 4 ? valt.row(rr + 2)[vc] : 0.0f;
+            const float vcdvar = spread(vprev, vcur, vnext);
+            const float vcdaltvar = spread(aprev, acur, anext);
+            const float vsel = vcdaltvar < vcdvar ? acur : vcur;
+            const bool g = ((fc(pattern, rr, 4) & 1) == 1) != vg4;
+            const float b = bound_sel(g, vsel, cfa.row(rr)[vc], cfa.row(rr - 1)[vc], cfa.row(rr + 1)[vc], clip_pt);
+            vcd.row(rr)[vc] = b;
+            vprev = b;
+          }
+        }
+        __syncthreads();
+        // -- cdd at red/blue sites (green.rs:187-222 tail), lag 6
+        {
+          const int lo = max(F - BH - 6, 4), hi = min(F - 6, TS - 4);
+          constexpr int per_row = (TS - 8) / 2;
+          for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
+            const int rr = lo + k / per_row;
+            const int cc = 4 + gae(pattern, rr) + 2 * (k % per_row);
+            cdd.row(rr)[cc >> 1] = sqr(vcd.row(rr)[cc] - hcd.row(rr)[cc]);
+          }
+        }
+        // -- direction_weights (green.rs:225-292), lag 9, red/blue sites of [6, 250)^2
+        {
+          const int lo = max(F - BH - 9, 6), hi = min(F - 9, TS - 6);
+          constexpr int per_row = (TS - 12 + 1) / 2;
+          for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
+            const int rr = lo + k / per_row;
+            const int cc = 6 + gae(pattern, rr) + 2 * (k % per_row);
+            if (cc >= TS - 6) continue;
+            // vcd rows outside [4, 252) were never written: zero.
+            float vv[7];
+#pragma unroll
+            for (int d = -3; d <= 3; ++d) {
+              const int r = rr + d;
+              vv[d + 3] = (r >= 4 && r < TS - 4) ? vcd.row(r)[cc] : 0.0f;
+            }
+            const float* hr = hcd.row(rr);
+            const float uave = vv[3] + vv[2] + vv[1] + vv[0];
+            const float dave = vv[3] + vv[4] + vv[5] + vv[6];
+            const float lave = hr[cc] + hr[cc - 1] + hr[cc - 2] + hr[cc - 3];
+            const float rave = hr[cc] + hr[cc + 1] + hr[cc + 2] + hr[cc + 3];
+            const float vu = sqr(vv[3] - uave) + sqr(vv[2] - uave) + sqr(vv[1] - uave) + sqr(vv[0] - uave);
+            const float vd = sqr(vv[3] - dave) + sqr(vv[4] - dave) + sqr(vv[5] - dave) + sqr(vv[6] - dave);
+            const float hl = sqr(hr[cc] - lave) + sqr(hr[cc - 1] - lave) + sqr(hr[cc - 2] - lave) + sqr(hr[cc - 3] - lave);
+            const float hrr = sqr(hr[cc] - rave) + sqr(hr[cc + 1] - rave) + sqr(hr[cc + 2] - rave) + sqr(hr[cc + 3] - rave);
+            const float* w1r = w1.row(rr);
+            const float hwt = w1r[cc - 1] / (w1r[cc - 1] + w1r[cc + 1]);
+            const float w0u = w0.row(rr - 1)[cc], w0d = w0.row(rr + 1)[cc];
+            const float vwt = w0u / (w0d + w0u);
+            const float vcdvar = EPSSQ + vwt * vd + (1.0f - vwt) * vu;
+            const float hcdvar = EPSSQ + hwt * hrr + (1.0f - hwt) * hl;
+            const float dv0 = dgv.row(rr)[cc];
+            const float fu = dv0 + dgv.row(rr - 1)[cc] + dgv.row(rr - 2)[cc];
+            const float fd = dv0 + dgv.row(rr + 1)[cc] + dgv.row(rr + 2)[cc];
+            const float* dhr = dgh.row(rr);
+            const float fl = dhr[cc] + dhr[cc - 1] + dhr[cc - 2];
+            const float fr = dhr[cc] + dhr[cc + 1] + dhr[cc + 2];
+            const float vcdvar1 = EPSSQ + vwt * fd + (1.0f - vwt) * fu;
+            const float hcdvar1 = EPSSQ + hwt * fr + (1.0f - hwt) * fl;
+            const float varwt = hcdvar / (vcdvar + hcdvar);
+            const float diffwt = hcdvar1 / (vcdvar1 + hcdvar1);
+            const int o = rr * TSH + (cc >> 1);
+            g_hv[o] = ((0.5f - varwt) * (0.5f - diffwt) > 0.0f && fabsf(0.5f - diffwt) < fabsf(0.5f - varwt))
+                          ? varwt
+                          : diffwt;
+            g_vrb[o] = vv[3];
+            g_hrb[o] = hr[cc];
+          }
+        }
+        __syncthreads();
+        // -- Nyquist test (nyquist.rs:25-95), lag 8, red/blue sites of [6, 250)^2
+        {
+          const int lo = max(F - BH - 8, 6), hi = min(F - 8, TS - 6);
+          constexpr int per_row = (TS - 12 + 1) / 2;
+          for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
+            const int rr = lo + k / per_row;
+            const int cc = 6 + gae(pattern, rr) + 2 * (k % per_row);
+            if (cc >= TS - 6) continue;
+            const float* cm2 = cdd.row(rr - 2);
+            const float* cm1 = cdd.row(rr - 1);
+            const float* c0 = cdd.row(rr);
+            const float* cp1 = cdd.row(rr + 1);
+            const float* cp2 = cdd.row(rr + 2);
+            const int j = cc >> 1, jm = (cc - 1) >> 1, jp = (cc + 1) >> 1;
+            const float* dm2 = delhv.row(rr - 2);
+            const float* dm1 = delhv.row(rr - 1);
+            const float* d0 = delhv.row(rr);
+            const float* dp1 = delhv.row(rr + 1);
+            const float* dp2 = delhv.row(rr + 2);
+            const float v =
+                (GAUSSODD[0] * c0[j] + GAUSSODD[1] * (cm1[jm] + cm1[jp] + cp1[jm] + cp1[jp]) +
+                 GAUSSODD[2] * (cm2[j] + c0[j - 1] + c0[j + 1] + cp2[j]) +
+                 GAUSSODD[3] * (cm2[j - 1] + cm2[j + 1] + cp2[j - 1] + cp2[j + 1])) -
+                (GAUSSGRAD[0] * d0[cc] + GAUSSGRAD[1] * (dm1[cc] + d0[cc + 1] + d0[cc - 1] + dp1[cc]) +
+                 GAUSSGRAD[2] * (dm1[cc - 1] + dm1[cc + 1] + dp1[cc - 1] + dp1[cc + 1]) +
+                 GAUSSGRAD[3] * (dm2[cc] + d0[cc - 2] + d0[cc + 2] + dp2[cc]) +
+                 GAUSSGRAD[4] * (dm2[cc - 1] + dm2[cc + 1] + dm1[cc - 2] + dm1[cc + 2] + dp1[cc - 2] +
+                                 dp1[cc + 2] + dp2[cc - 1] + dp2[cc + 1]) +
+                 GAUSSGRAD[5] * (dm2[cc - 2] + dm2[cc + 2] + dp2[cc - 2] + dp2[cc + 2]));
+            g_nyq[rr * TSH + j] = v > 0.0f ? 1 : 0;
+          }
+        }
+        __syncthreads();
       }
     }
-    __syncthreads();
 
-    // ---- diagonal_estimates (diagonal.rs:99-145)
-    {
-      const float* delp = P.h[H_DELP];
-      const float* delm = P.h[H_DELM];
-      const float* sqp = P.h[H_SQ1P];
-      const float* sqm = P.h[H_SQ1M];
-      float* rbp = P.h[H_RBP];
-      float* rbm = P.h[H_RBM];
-      const int per_row = site_count(8, TS - 8);
-      for (int k = t; k < (TS - 16) * per_row; k += THREADS) {
-        const int rr = 8 + k / per_row;
-        const int cc = 8 + gae(pattern, rr) + 2 * (k % per_row);
-        if (cc >= TS - 8) continue;
-        const int i = rr * TS + cc, i1 = cc >> 1;
-        const float centre = cfa[i];
-        const float se1 = cfa[i + TS + 1], se2 = cfa[i + 2 * TS + 2];
-        const float nw1 = cfa[i - TS - 1], nw2 = cfa[i - 2 * TS - 2];
-        const float ne1 = cfa[i - TS + 1], ne2 = cfa[i - 2 * TS + 2];
-        const float sw1 = cfa[i + TS - 1], sw2 = cfa[i + 2 * TS - 2];
-        const float rbse = diagonal_estimate(centre, se1, se2);
-        const float rbnw = diagonal_estimate(centre, nw1, nw2);
-        const float rbne = diagonal_estimate(centre, ne1, ne2);
-        const float rbsw = diagonal_estimate(centre, sw1, sw2);
-        const int r0 = (rr - 2) * TSH, r1 = (rr - 1) * TSH, r2 = rr * TSH, r3 = (rr + 1) * TSH, r4 = (rr + 2) * TSH;
-        const float wtse = EPS + delm[r2 + i1] + delm[r3 + ((cc + 1) >> 1)] + delm[r4 + ((cc + 2) >> 1)];
-        const float wtnw = EPS + delm[r2 + i1] + delm[r1 + ((cc - 1) >> 1)] + delm[r0 + ((cc - 2) >> 1)];
-        const float wtne = EPS + delp[r2 + i1] + delp[r1 + ((cc + 1) >> 1)] + delp[r0 + ((cc + 2) >> 1)];
-        const float wtsw = EPS + delp[r2 + i1] + delp[r3 + ((cc - 1) >> 1)] + delp[r4 + ((cc - 2) >> 1)];
-        const float rbm_est = (wtse * rbnw + wtnw * rbse) / (wtse + wtnw);
-        const float rbp_est = (wtne * rbsw + wtsw * rbne) / (wtne + wtsw);
-        const float em = GAUSSEVEN[0] * (sqm[r1 + (cc >> 1)] + sqm[r2 + ((cc - 1) >> 1)] + sqm[r2 + ((cc + 1) >> 1)] + sqm[r3 + (cc >> 1)]) +
-                         GAUSSEVEN[1] * (sqm[r0 + ((cc - 1) >> 1)] + sqm[r0 + ((cc + 1) >> 1)] + sqm[r1 + ((cc - 2) >> 1)] +
-                                         sqm[r1 + ((cc + 2) >> 1)] + sqm[r3 + ((cc - 2) >> 1)] + sqm[r3 + ((cc + 2) >> 1)] +
-                                         sqm[r4 + ((cc - 1) >> 1)] + sqm[r4 + ((cc + 1) >> 1)]);
-        const float ep = GAUSSEVEN[0] * (sqp[r1 + (cc >> 1)] + sqp[r2 + ((cc - 1) >> 1)] + sqp[r2 + ((cc + 1) >> 1)] + sqp[r3 + (cc >> 1)]) +
-                         GAUSSEVEN[1] * (sqp[r0 + ((cc - 1) >> 1)] + sqp[r0 + ((cc + 1) >> 1)] + sqp[r1 + ((cc - 2) >> 1)] +
-                                         sqp[r1 + ((cc + 2) >> 1)] + sqp[r3 + ((cc - 2) >> 1)] + sqp[r3 + ((cc + 2) >> 1)] +
-                                         sqp[r4 + ((cc - 1) >> 1)] + sqp[r4 + ((cc + 1) >> 1)]);
-        const float rbvarm = EPSSQ + em;
-        pmwt[r2 + i1] = rbvarm / ((EPSSQ + ep) + rbvarm);
-        rbp[r2 + i1] = bound_diagonal(rbp_est, centre, sw1, ne1, clip_pt);
-        rbm[r2 + i1] = bound_diagonal(rbm_est, centre, nw1, se1, clip_pt);
-      }
-    }
-    __syncthreads();
-
-    // ---- combine_diagonals (diagonal.rs:150-171): row-ordered pmwt update ...
-    for (int rr = 10; rr < TS - 10; ++rr) {
-      const int cc = 10 + gae(pattern, rr) + 2 * t;
-      if (t < site_count(10, TS - 10) && cc < TS - 10) {
-        const float alt = (pmwt[(rr - 1) * TSH + ((cc - 1) >> 1)] + pmwt[(rr - 1) * TSH + ((cc + 1) >> 1)] +
-                           pmwt[(rr + 1) * TSH + ((cc - 1) >> 1)] + pmwt[(rr + 1) * TSH + ((cc + 1) >> 1)]) /
-                          4.0f;
-        float* p = &pmwt[rr * TSH + (cc >> 1)];
-        if (fabsf(0.5f - *p) < fabsf(0.5f - alt)) *p = alt;
-      }
-      __syncthreads();
-    }
-    // ... then R+B from the final weights.
-    {
-      const float* rbp = P.h[H_RBP];
-      const float* rbm = P.h[H_RBM];
-      float* rbint = P.h[H_RBINT];
-      const int per_row = site_count(10, TS - 10);
-      for (int k = t; k < (TS - 20) * per_row; k += THREADS) {
-        const int rr = 10 + k / per_row;
-        const int cc = 10 + gae(pattern, rr) + 2 * (k % per_row);
-        if (cc >= TS - 10) continue;
-        const int j = rr * TSH + (cc >> 1);
-        const float p = pmwt[j];
-        rbint[j] = 0.5f * (cfa[rr * TS + cc] + rbm[j] * (1.0f - p) + rbp[j] * p);
-      }
-    }
-    __syncthreads();
-
-    // ---- refine_green_with_rb (diagonal.rs:205-247)
-    {
-      const float* rbint = P.h[H_RBINT];
-      const int per_row = site_count(12, TS - 12);
-      for (int k = t; k < (TS - 24) * per_row; k += THREADS) {
-        const int rr = 12 + k / per_row;
-        const int cc = 12 + gae(pattern, rr) + 2 * (k % per_row);
-        if (cc >= TS - 12) continue;
-        const int i = rr * TS + cc, i1 = cc >> 1;
-        const float pm = pmwt[rr * TSH + i1];
-        const float hv = hvwt[rr * TSH + i1];
-        if (fabsf(0.5f - pm) < fabsf(0.5f - hv)) continue;
-        const float* rb_up = rbint + (rr - 2) * TSH;
-        const float* rb = rbint + rr * TSH;
-        const float* rb_down = rbint + (rr + 2) * TSH;
-        const float centre = rb[i1];
-        const float gu = green_from_rb(cfa[i - TS], centre, rb_up[i1]);
-        const float gd = green_from_rb(cfa[i + TS], centre, rb_down[i1]);
-        const float gl = green_from_rb(cfa[i - 1], centre, rb[i1 - 1]);
-        const float gr = green_from_rb(cfa[i + 1], centre, rb[i1 + 1]);
-        float gintv = (w0[i - TS] * gd + w0[i + TS] * gu) / (w0[i + TS] + w0[i - TS]);
-        float ginth = (w1[i - 1] * gr + w1[i + 1] * gl) / (w1[i - 1] + w1[i + 1]);
-        gintv = bound_diagonal(gintv, centre, cfa[i - TS], cfa[i + TS], clip_pt);
-        ginth = bound_diagonal(ginth, centre, cfa[i - 1], cfa[i + 1], clip_pt);
-        const float gv = ginth * (1.0f - hv) + gintv * hv;
-        green[i] = gv;
-        dgrb0[rr * TSH + i1] = gv - cfa[i];
-      }
-    }
-    __syncthreads();
-
-    // ---- interpolate_chroma (chroma.rs:23-91). Reads and writes of each plane
-    // fall on different Bayer cosets, so the sweep is order-free.
-    {
-      const int c00 = color_at(pattern, 0, 0), c10 = color_at(pattern, 1, 0);
-      int ey, ex;
-      if (c00 == 1 && c10 == 0) { ey = 0; ex = 1; }
-      else if (c00 == 1) { ey = 1; ex = 0; }
-      else if (c00 == 0) { ey = 0; ex = 0; }
-      else { ey = 1; ex = 1; }
-      const int first_row = 13 - ey;
-      const int rows = (TS - 12 - first_row + 1) / 2;
-      const int lo = (13 - ex) >> 1, hi = (TS - 12) >> 1;  // half-index range within the row
-      for (int k = t; k < rows * (hi - lo); k += THREADS) {
-        const int rr = first_row + 2 * (k / (hi - lo));
-        const int i1 = rr * TSH + lo + k % (hi - lo);
-        dgrb1[i1] = dgrb0[i1];
-        dgrb0[i1] = 0.0f;
-      }
-    }
+    // ================= phase B: nyquist.rs:108-236, diagonal.rs, chroma.rs, mod.rs:196-268 =================
+    for (int k = t; k < B_FLOATS; k += THREADS) sm[k] = 0.0f;
     __syncthreads();
     {
-      const int per_row = site_count(14, TS - 14);
-      for (int k = t; k < (TS - 28) * per_row; k += THREADS) {
-        const int rr = 14 + k / per_row;
-        const int start = 14 + gae(pattern, rr);
-        const int cc = start + 2 * (k % per_row);
-        if (cc >= TS - 14) continue;
-        float* p = (1 - fc(pattern, rr, start) / 2) == 0 ? dgrb0 : dgrb1;
-        auto d = [&](int dr, int dc) { return p[(rr + dr) * TSH + ((cc + dc) >> 1)]; };
-        const float wtnw = 1.0f / (EPS + fabsf(d(-1, -1) - d(1, 1)) + fabsf(d(-1, -1) - d(-3, -3)) + fabsf(d(1, 1) - d(-3, -3)));
-        const float wtne = 1.0f / (EPS + fabsf(d(-1, 1) - d(1, -1)) + fabsf(d(-1, 1) - d(-3, 3)) + fabsf(d(1, -1) - d(-3, 3)));
-        const float wtsw = 1.0f / (EPS + fabsf(d(1, -1) - d(-1, 1)) + fabsf(d(1, -1) - d(3, 3)) + fabsf(d(-1, 1) - d(3, -3)));
-        const float wtse = 1.0f / (EPS + fabsf(d(1, 1) - d(-1, -1)) + fabsf(d(1, 1) - d(3, -3)) + fabsf(d(-1, -1) - d(3, 3)));
-        p[rr * TSH + (cc >> 1)] =
-            (wtnw * (1.325f * d(-1, -1) - 0.175f * d(-3, -3) - 0.075f * d(-1, -3) - 0.075f * d(-3, -1)) +
-             wtne * (1.325f * d(-1, 1) - 0.175f * d(-3, 3) - 0.075f * d(-1, 3) - 0.075f * d(1, 1)) +
-             wtsw * (1.325f * d(1, -1) - 0.175f * d(3, -3) - 0.075f * d(1, -3) - 0.075f * d(-1, -1)) +
-             wtse * (1.325f * d(1, 1) - 0.175f * d(3, 3) - 0.075f * d(1, 3) - 0.075f * d(3, 1))) /
-            (wtnw + wtne + wtsw + wtse);
-      }
-    }
-    __syncthreads();
-
-    // ---- finish_planes (chroma.rs:98-147) + write_tile (mod.rs:196-268)
-    {
-      unsigned long long affected = 0, changed = 0, over = 0, ac[3] = {0, 0, 0};
+      const Ring<32, TS> cfa{sm + B_CFA_OFF};
+      const Ring<32, TSH> hv{sm + B_HV_OFF}, vrb{sm + B_VRB_OFF}, hrb{sm + B_HRB_OFF};
+      float* h16 = sm + B_H16_OFF;
+      const Ring<16, TSH> dgrb0{h16 + B_DGRB0 * 16 * TSH}, dgrb1{h16 + B_DGRB1 * 16 * TSH},
+          green{h16 + B_GREEN * 16 * TSH}, d2h{h16 + B_D2H * 16 * TSH}, d2v{h16 + B_D2V * 16 * TSH},
+          delp{h16 + B_DELP * 16 * TSH}, delm{h16 + B_DELM * 16 * TSH}, sqp{h16 + B_SQP * 16 * TSH},
+          sqm{h16 + B_SQM * 16 * TSH}, pmwt{h16 + B_PMWT * 16 * TSH}, rbp{h16 + B_RBP * 16 * TSH},
+          rbm{h16 + B_RBM * 16 * TSH}, rbint{h16 + B_RBINT * 16 * TSH};
+      unsigned char* u8 = reinterpret_cast<unsigned char*>(sm + B_U8_OFF);
+      const Ring<16, TSH, unsigned char> nyq{u8};
+      const Ring<32, TSH, unsigned char> nyq2{u8 + 16 * TSH};
+      unsigned long long affected = 0, changed = 0, over = 0, ac0 = 0, ac1 = 0, ac2 = 0;
       int bad = 0;
-      for (int k = t; k < VALID * VALID; k += THREADS) {
-        const int ly = k / VALID, lx = k % VALID;
-        const int gx = ox + lx, gy = oy + ly;
-        if (gx >= W || gy >= H) continue;
-        const int rr = ly + BORDER, cc = lx + BORDER;
-        const int i = rr * TS + cc;
-        float r, b;
-        const float gv = green[i];
-        if (fc(pattern, rr, cc) == 1) {
-          const float up = hvwt[(rr - 1) * TSH + (cc >> 1)], down = hvwt[(rr + 1) * TSH + (cc >> 1)];
-          const float left = hvwt[rr * TSH + ((cc - 1) >> 1)], right = hvwt[rr * TSH + ((cc + 1) >> 1)];
-          const float temp = 1.0f / (up + 2.0f - right - left + down);
-          const float br = (up * dgrb0[(rr - 1) * TSH + (cc >> 1)] + (1.0f - right) * dgrb0[rr * TSH + ((cc + 1) >> 1)] +
-                            (1.0f - left) * dgrb0[rr * TSH + ((cc - 1) >> 1)] + down * dgrb0[(rr + 1) * TSH + (cc >> 1)]) *
-                           temp;
-          const float bb = (up * dgrb1[(rr - 1) * TSH + (cc >> 1)] + (1.0f - right) * dgrb1[rr * TSH + ((cc + 1) >> 1)] +
-                            (1.0f - left) * dgrb1[rr * TSH + ((cc - 1) >> 1)] + down * dgrb1[(rr + 1) * TSH + (cc >> 1)]) *
-                           temp;
-          r = gv - br;
-          b = gv - bb;
-        } else {
-          r = gv - dgrb0[rr * TSH + (cc >> 1)];
-          b = gv - dgrb1[rr * TSH + (cc >> 1)];
+      for (int F = BH; F <= TS; F += BH) {
+        // -- load rows [F-8, F): mosaic, and the slab rows of [6, 250)
+        {
+          const int lo = F - BH;
+          for (int k = t; k < BH * TS; k += THREADS) {
+            const int rr = lo + (k >> 8), cc = k & (TS - 1);
+            cfa.row(rr)[cc] = tile_sample(src, ox - BORDER + cc, oy - BORDER + rr, W, H);
+          }
+          for (int k = t; k < BH * TSH; k += THREADS) {
+            const int rr = lo + (k >> 7), j = k & (TSH - 1);
+            if (rr < 6 || rr >= TS - 6) continue;
+            const int o = rr * TSH + j;
+            hv.row(rr)[j] = g_hv[o];
+            vrb.row(rr)[j] = g_vrb[o];
+            hrb.row(rr)[j] = g_hrb[o];
+            nyq.row(rr)[j] = g_nyq[o];
+          }
         }
-        r = fmax_(r, 0.0f);
-        b = fmax_(b, 0.0f);
-        const float sample = source_balanced(src, gx, gy);
-        const int ch = color_at(pattern, gx, gy);
-        float rgb0 = ch == 0 ? sample : r;
-        float rgb1 = ch == 1 ? sample : fmax_(gv, 0.0f);
-        float rgb2 = ch == 2 ? sample : b;
-        rgb0 = rgb0 * prm.gains[0];
-        rgb1 = rgb1 * prm.gains[1];
-        rgb2 = rgb2 * prm.gains[2];
-        if (!isfinite(rgb0) || !isfinite(rgb1) || !isfinite(rgb2)) bad = 1;
-        const long long o = (long long)gy * W + gx;
-        prm.out[o] = rgb0;
-        prm.out[plane + o] = rgb1;
-        prm.out[2 * plane + o] = rgb2;
-        if (prm.count_clip) {
-          const float v = source_normalized(src, gx, gy);
-          const float limit = src.clip_levels[ch];
-          if (v >= limit) { affected++; ac[ch]++; }
-          if (v > 1.0f) over++;
-          if (v > limit) changed++;
+        __syncthreads();
+        // -- Nyquist flag refinement (nyquist.rs:108-130), lag 2, red/blue sites of [8, 248)^2;
+        //    diagonal_gradients (diagonal.rs:15-45), lag 6, rows [6, 250)
+        {
+          const int lo = max(F - BH - 2, 8), hi = min(F - 2, TS - 8);
+          constexpr int per_row = (TS - 16) / 2;
+          for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
+            const int rr = lo + k / per_row;
+            const int cc = 8 + gae(pattern, rr) + 2 * (k % per_row);
+            const int j = cc >> 1, jm = (cc - 1) >> 1, jp = (cc + 1) >> 1;
+            const unsigned char* nm2 = nyq.row(rr - 2);
+            const unsigned char* nm1 = nyq.row(rr - 1);
+            const unsigned char* n0 = nyq.row(rr);
+            const unsigned char* np1 = nyq.row(rr + 1);
+            const unsigned char* np2 = nyq.row(rr + 2);
+            const unsigned votes = nm2[j] + nm1[jm] + nm1[jp] + n0[j - 1] + n0[j + 1] + np1[jm] + np1[jp] + np2[j];
+            nyq2.row(rr)[j] = votes >= 5 ? 1 : (votes == 4 ? n0[j] : 0);
+          }
         }
+        {
+          const int lo = max(F - BH - 6, 6), hi = min(F - 6, TS - 6);
+          constexpr int per_row = (TS - 12 + 1) / 2;
+          for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
+            const int rr = lo + k / per_row;
+            const int cc = 6 + 2 * (k % per_row);
+            if (cc >= TS - 6) continue;
+            const float* up = cfa.row(rr - 1);
+            const float* mid = cfa.row(rr);
+            const float* down = cfa.row(rr + 1);
+            const int j = cc >> 1;
+            if (gae(pattern, rr) == 0) {
+              delp.row(rr)[j] = fabsf(up[cc + 1] - down[cc - 1]);
+              delm.row(rr)[j] = fabsf(down[cc + 1] - up[cc - 1]);
+              const float g = mid[cc + 1];
+              sqp.row(rr)[j] = sqr(g - down[cc]) + sqr(g - up[cc + 2]);
+              sqm.row(rr)[j] = sqr(g - up[cc]) + sqr(g - down[cc + 2]);
+            } else {
+              const float g = mid[cc];
+              sqp.row(rr)[j] = sqr(g - down[cc - 1]) + sqr(g - up[cc + 1]);
+              sqm.row(rr)[j] = sqr(g - up[cc - 1]) + sqr(g - down[cc + 1]);
+              delp.row(rr)[j] = fabsf(up[cc + 2] - down[cc]);
+              delm.row(rr)[j] = fabsf(down[cc + 2] - up[cc]);
+            }
+          }
+        }
+        __syncthreads();
+        // -- area interpolation at refined Nyquist sites (nyquist.rs:132-170), lag 8
+        {
+          const int lo = max(F - BH - 8, 8), hi = min(F - 8, TS - 8);
+          constexpr int per_row = (TS - 16) / 2;
+          for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
+            const int rr = lo + k / per_row;
+            const int cc = 8 + gae(pattern, rr) + 2 * (k % per_row);
+            if (nyq2.row(rr)[cc >> 1] == 0) continue;
+            float sumcfa = 0.0f, sumh = 0.0f, sumv = 0.0f, sumsqh = 0.0f, sumsqv = 0.0f, areawt = 0.0f;
+            for (int di = -6; di < 7; di += 2) {
+              const int r1 = rr + di;
+              // Refined flags outside [8, 248) were never set: zero.
+              if (r1 < 8 || r1 >= TS - 8) continue;
+              const unsigned char* f = nyq2.row(r1);
+              const float* c0 = cfa.row(r1);
+              const float* cu = cfa.row(r1 - 1);
+              const float* cd = cfa.row(r1 + 1);
+              for (int c1 = cc - 6; c1 < cc + 7; c1 += 2) {
+                if (f[c1 >> 1] != 0) {
+                  const float c = c0[c1];
+                  sumcfa += c;
+                  sumh += c0[c1 - 1] + c0[c1 + 1];
+                  sumv += cu[c1] + cd[c1];
+                  sumsqh += sqr(c - c0[c1 - 1]) + sqr(c - c0[c1 + 1]);
+                  sumsqv += sqr(c - cu[c1]) + sqr(c - cd[c1]);
+                  areawt += 1.0f;
+                }
+              }
+            }
+            sumh = sumcfa - 0.5f * sumh;
+            sumv = sumcfa - 0.5f * sumv;
+            areawt *= 0.5f;
+            const float hcdvar = EPSSQ + fabsf(areawt * sumsqh - sumh * sumh);
+            const float vcdvar = EPSSQ + fabsf(areawt * sumsqv - sumv * sumv);
+            hv.row(rr)[cc >> 1] = hcdvar / (vcdvar + hcdvar);
+          }
+        }
+        // -- diagonal_estimates (diagonal.rs:99-145), lag 8, red/blue sites of [8, 248)^2
+        {
+          const int lo = max(F - BH - 8, 8), hi = min(F - 8, TS - 8);
+          constexpr int per_row = (TS - 16) / 2;
+          for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
+            const int rr = lo + k / per_row;
+            const int cc = 8 + gae(pattern, rr) + 2 * (k % per_row);
+            const int j = cc >> 1;
+            const float* cm2 = cfa.row(rr - 2);
+            const float* cm1 = cfa.row(rr - 1);
+            const float* c0 = cfa.row(rr);
+            const float* cp1 = cfa.row(rr + 1);
+            const float* cp2 = cfa.row(rr + 2);
+            const float centre = c0[cc];
+            const float se1 = cp1[cc + 1], se2 = cp2[cc + 2];
+            const float nw1 = cm1[cc - 1], nw2 = cm2[cc - 2];
+            const float ne1 = cm1[cc + 1], ne2 = cm2[cc + 2];
+            const float sw1 = cp1[cc - 1], sw2 = cp2[cc - 2];
+            const float rbse = diagonal_estimate(centre, se1, se2);
+            const float rbnw = diagonal_estimate(centre, nw1, nw2);
+            const float rbne = diagonal_estimate(centre, ne1, ne2);
+            const float rbsw = diagonal_estimate(centre, sw1, sw2);
+            const float wtse = EPS + delm.row(rr)[j] + delm.row(rr + 1)[(cc + 1) >> 1] + delm.row(rr + 2)[(cc + 2) >> 1];
+            const float wtnw = EPS + delm.row(rr)[j] + delm.row(rr - 1)[(cc - 1) >> 1] + delm.row(rr - 2)[(cc - 2) >> 1];
+            const float wtne = EPS + delp.row(rr)[j] + delp.row(rr - 1)[(cc + 1) >> 1] + delp.row(rr - 2)[(cc + 2) >> 1];
+            const float wtsw = EPS + delp.row(rr)[j] + delp.row(rr + 1)[(cc - 1) >> 1] + delp.row(rr + 2)[(cc - 2) >> 1];
+            const float rbm_est = (wtse * rbnw + wtnw * rbse) / (wtse + wtnw);
+            const float rbp_est = (wtne * rbsw + wtsw * rbne) / (wtne + wtsw);
+            const float* qm0 = sqm.row(rr - 2);
+            const float* qm1 = sqm.row(rr - 1);
+            const float* qm2 = sqm.row(rr);
+            const float* qm3 = sqm.row(rr + 1);
+            const float* qm4 = sqm.row(rr + 2);
+            const float em = GAUSSEVEN[0] * (qm1[cc >> 1] + qm2[(cc - 1) >> 1] + qm2[(cc + 1) >> 1] + qm3[cc >> 1]) +
+                             GAUSSEVEN[1] * (qm0[(cc - 1) >> 1] + qm0[(cc + 1) >> 1] + qm1[(cc - 2) >> 1] +
+                                             qm1[(cc + 2) >> 1] + qm3[(cc - 2) >> 1] + qm3[(cc + 2) >> 1] +
+                                             qm4[(cc - 1) >> 1] + qm4[(cc + 1) >> 1]);
+            const float* qp0 = sqp.row(rr - 2);
+            const float* qp1 = sqp.row(rr - 1);
+            const float* qp2 = sqp.row(rr);
+            const float* qp3 = sqp.row(rr + 1);
+            const float* qp4 = sqp.row(rr + 2);
+            const float ep = GAUSSEVEN[0] * (qp1[cc >> 1] + qp2[(cc - 1) >> 1] + qp2[(cc + 1) >> 1] + qp3[cc >> 1]) +
+                             GAUSSEVEN[1] * (qp0[(cc - 1) >> 1] + qp0[(cc + 1) >> 1] + qp1[(cc - 2) >> 1] +
+                                             qp1[(cc + 2) >> 1] + qp3[(cc - 2) >> 1] + qp3[(cc + 2) >> 1] +
+                                             qp4[(cc - 1) >> 1] + qp4[(cc + 1) >> 1]);
+            const float rbvarm = EPSSQ + em;
+            pmwt.row(rr)[j] = rbvarm / ((EPSSQ + ep) + rbvarm);
+            rbp.row(rr)[j] = bound_diagonal(rbp_est, centre, sw1, ne1, clip_pt);
+            rbm.row(rr)[j] = bound_diagonal(rbm_est, centre, nw1, se1, clip_pt);
+          }
+        }
+        __syncthreads();
+        // -- row recurrences, lag 9: populate_green's hvwt update (nyquist.rs:176-222) on
+        //    warp 0, combine_diagonals' pmwt update (diagonal.rs:150-171) on warp 1.
+        if (warp == 0) {
+          const int lo = max(F - BH - 9, 8), hi = min(F - 9, TS - 8);
+          constexpr int sites = (TS - 16) / 2;
+          for (int rr = lo; rr < hi; ++rr) {
+            const int g = gae(pattern, rr);
+            const float* up = hv.row(rr - 1);
+            const float* down = hv.row(rr + 1);
+            float* cur = hv.row(rr);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              const int k = lane + 32 * q;
+              if (k < sites) {
+                const int cc = 8 + g + 2 * k;
+                const float alt = (up[(cc - 1) >> 1] + up[(cc + 1) >> 1] + down[(cc - 1) >> 1] + down[(cc + 1) >> 1]) / 4.0f;
+                float* p = &cur[cc >> 1];
+                if (fabsf(0.5f - *p) < fabsf(0.5f - alt)) *p = alt;
+              }
+            }
+            __syncwarp();
+          }
+        } else if (warp == 1) {
+          const int lo = max(F - BH - 9, 10), hi = min(F - 9, TS - 10);
+          constexpr int sites = (TS - 20) / 2;
+          for (int rr = lo; rr < hi; ++rr) {
+            const int g = gae(pattern, rr);
+            const float* up = pmwt.row(rr - 1);
+            const float* down = pmwt.row(rr + 1);
+            float* cur = pmwt.row(rr);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              const int k = lane + 32 * q;
+              if (k < sites) {
+                const int cc = 10 + g + 2 * k;
+                const float alt = (up[(cc - 1) >> 1] + up[(cc + 1) >> 1] + down[(cc - 1) >> 1] + down[(cc + 1) >> 1]) / 4.0f;
+                float* p = &cur[cc >> 1];
+                if (fabsf(0.5f - *p) < fabsf(0.5f - alt)) *p = alt;
+              }
+            }
+            __syncwarp();
+          }
+        }
+        __syncthreads();
+        // -- per-site products of populate_green (lag 9, [8, 248)^2) and the R+B
+        //    interpolation of combine_diagonals (lag 9, [10, 246)^2)
+        {
+          const int lo = max(F - BH - 9, 8), hi = min(F - 9, TS - 8);
+          constexpr int per_row = (TS - 16) / 2;
+          for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
+            const int rr = lo + k / per_row;
+            const int cc = 8 + gae(pattern, rr) + 2 * (k % per_row);
+            const int j = cc >> 1;
+            const float* c0 = cfa.row(rr);
+            const float dg = intp(hv.row(rr)[j], vrb.row(rr)[j], hrb.row(rr)[j]);
+            dgrb0.row(rr)[j] = dg;
+            const float gv = c0[cc] + dg;
+            green.row(rr)[j] = gv;
+            const bool flagged = nyq2.row(rr)[j] != 0;
+            d2h.row(rr)[j] = flagged ? sqr(gv - 0.5f * (c0[cc - 1] + c0[cc + 1])) : 0.0f;
+            d2v.row(rr)[j] = flagged ? sqr(gv - 0.5f * (cfa.row(rr - 1)[cc] + cfa.row(rr + 1)[cc])) : 0.0f;
+          }
+        }
+        {
+          const int lo = max(F - BH - 9, 10), hi = min(F - 9, TS - 10);
+          constexpr int per_row = (TS - 20) / 2;
+          for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
+            const int rr = lo + k / per_row;
+            const int cc = 10 + gae(pattern, rr) + 2 * (k % per_row);
+            const int j = cc >> 1;
+            const float p = pmwt.row(rr)[j];
+            rbint.row(rr)[j] = 0.5f * (cfa.row(rr)[cc] + rbm.row(rr)[j] * (1.0f - p) + rbp.row(rr)[j] * p);
+          }
+        }
+        __syncthreads();
+        // -- refine_green (nyquist.rs:225-236), lag 11, refined Nyquist sites
+        {
+          const int lo = max(F - BH - 11, 8), hi = min(F - 11, TS - 8);
+          constexpr int per_row = (TS - 16) / 2;
+          for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
+            const int rr = lo + k / per_row;
+            const int cc = 8 + gae(pattern, rr) + 2 * (k % per_row);
+            const int j = cc >> 1;
+            if (nyq2.row(rr)[j] == 0) continue;
+            // d2h / d2v rows outside [8, 248) were never written: zero.
+            const float* hm2 = rr - 2 >= 8 ? d2h.row(rr - 2) : nullptr;
+            const float* hp2 = rr + 2 < TS - 8 ? d2h.row(rr + 2) : nullptr;
+            const float* hm1 = rr - 1 >= 8 ? d2h.row(rr - 1) : nullptr;
+            const float* hp1 = rr + 1 < TS - 8 ? d2h.row(rr + 1) : nullptr;
+            const float* vm2 = rr - 2 >= 8 ? d2v.row(rr - 2) : nullptr;
+            const float* vp2 = rr + 2 < TS - 8 ? d2v.row(rr + 2) : nullptr;
+            const float* vm1 = rr - 1 >= 8 ? d2v.row(rr - 1) : nullptr;
+            const float* vp1 = rr + 1 < TS - 8 ? d2v.row(rr + 1) : nullptr;
+            const float* h0 = d2h.row(rr);
+            const float* v0 = d2v.row(rr);
+            const int jm = (cc - 1) >> 1, jp = (cc + 1) >> 1;
+            auto at = [](const float* r, int x) { return r ? r[x] : 0.0f; };
+            const float gvarh = EPSSQ + (GQUINC[0] * h0[j] +
+                                         GQUINC[1] * (at(hm1, jm) + at(hm1, jp) + at(hp1, jm) + at(hp1, jp)) +
+                                         GQUINC[2] * (at(hm2, j) + h0[j - 1] + h0[j + 1] + at(hp2, j)) +
+                                         GQUINC[3] * (at(hm2, j - 1) + at(hm2, j + 1) + at(hp2, j - 1) + at(hp2, j + 1)));
+            const float gvarv = EPSSQ + (GQUINC[0] * v0[j] +
+                                         GQUINC[1] * (at(vm1, jm) + at(vm1, jp) + at(vp1, jm) + at(vp1, jp)) +
+                                         GQUINC[2] * (at(vm2, j) + v0[j - 1] + v0[j + 1] + at(vp2, j)) +
+                                         GQUINC[3] * (at(vm2, j - 1) + at(vm2, j + 1) + at(vp2, j - 1) + at(vp2, j + 1)));
+            const float dg = (hrb.row(rr)[j] * gvarv + vrb.row(rr)[j] * gvarh) / (gvarv + gvarh);
+            dgrb0.row(rr)[j] = dg;
+            green.row(rr)[j] = cfa.row(rr)[cc] + dg;
+          }
+        }
+        __syncthreads();
+        // -- refine_green_with_rb (diagonal.rs:205-247) and the move of blue-row
+        //    differences to dgrb1 (chroma.rs:23-44), lag 11, [12, 244)^2
+        {
+          const int lo = max(F - BH - 11, 12), hi = min(F - 11, TS - 12);
+          constexpr int per_row = (TS - 24) / 2;
+          for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
+            const int rr = lo + k / per_row;
+            const int cc = 12 + gae(pattern, rr) + 2 * (k % per_row);
+            const int j = cc >> 1;
+            const float pm = pmwt.row(rr)[j];
+            const float hvv = hv.row(rr)[j];
+            if (!(fabsf(0.5f - pm) < fabsf(0.5f - hvv))) {
+              const float* rb_up = rbint.row(rr - 2);
+              const float* rb = rbint.row(rr);
+              const float* rb_down = rbint.row(rr + 2);
+              const float* c0 = cfa.row(rr);
+              const float* cu = cfa.row(rr - 1);
+              const float* cd = cfa.row(rr + 1);
+              const float* cu2 = cfa.row(rr - 2);
+              const float* cd2 = cfa.row(rr + 2);
+              const float* cu3 = cfa.row(rr - 3);
+              const float* cd3 = cfa.row(rr + 3);
+              const float centre = rb[j];
+              const float gu = green_from_rb(cu[cc], centre, rb_up[j]);
+              const float gd = green_from_rb(cd[cc], centre, rb_down[j]);
+              const float gl = green_from_rb(c0[cc - 1], centre, rb[j - 1]);
+              const float gr = green_from_rb(c0[cc + 1], centre, rb[j + 1]);
+              // Directional gradient weights (green.rs:13-29) at the four neighbours.
+              const float w0u = EPS + fabsf(cd[cc] - cu[cc]) + fabsf(cu[cc] - cu3[cc]) + fabsf(c0[cc] - cu2[cc]);
+              const float w0d = EPS + fabsf(cd3[cc] - cd[cc]) + fabsf(cd[cc] - cu[cc]) + fabsf(cd2[cc] - c0[cc]);
+              const float w1l = EPS + fabsf(c0[cc + 1] - c0[cc - 1]) + fabsf(c0[cc - 1] - c0[cc - 3]) + fabsf(c0[cc] - c0[cc - 2]);
+              const float w1r = EPS + fabsf(c0[cc + 3] - c0[cc + 1]) + fabsf(c0[cc + 1] - c0[cc - 1]) + fabsf(c0[cc + 2] - c0[cc]);
+              float gintv = (w0u * gd + w0d * gu) / (w0d + w0u);
+              float ginth = (w1l * gr + w1r * gl) / (w1l + w1r);
+              gintv = bound_diagonal(gintv, centre, cu[cc], cd[cc], clip_pt);
+              ginth = bound_diagonal(ginth, centre, c0[cc - 1], c0[cc + 1], clip_pt);
+              const float gv = ginth * (1.0f - hvv) + gintv * hvv;
+              green.row(rr)[j] = gv;
+              dgrb0.row(rr)[j] = gv - c0[cc];
+            }
+            if ((rr & 1) == blue_par) {
+              dgrb1.row(rr)[j] = dgrb0.row(rr)[j];
+              dgrb0.row(rr)[j] = 0.0f;
+            }
+          }
+        }
+        __syncthreads();
+        // -- interpolate_chroma (chroma.rs:46-91), lag 14, [14, 242)^2: reads and
+        //    writes of each plane fall on different rows
+        {
+          const int lo = max(F - BH - 14, 14), hi = min(F - 14, TS - 14);
+          constexpr int per_row = (TS - 28) / 2;
+          for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
+            const int rr = lo + k / per_row;
+            const int start = 14 + gae(pattern, rr);
+            const int cc = start + 2 * (k % per_row);
+            const Ring<16, TSH>& p = (1 - fc(pattern, rr, start) / 2) == 0 ? dgrb0 : dgrb1;
+            auto d = [&](int dr, int dc) { return p.row(rr + dr)[(cc + dc) >> 1]; };
+            const float wtnw = 1.0f / (EPS + fabsf(d(-1, -1) - d(1, 1)) + fabsf(d(-1, -1) - d(-3, -3)) + fabsf(d(1, 1) - d(-3, -3)));
+            const float wtne = 1.0f / (EPS + fabsf(d(-1, 1) - d(1, -1)) + fabsf(d(-1, 1) - d(-3, 3)) + fabsf(d(1, -1) - d(-3, 3)));
+            const float wtsw = 1.0f / (EPS + fabsf(d(1, -1) - d(-1, 1)) + fabsf(d(1, -1) - d(3, 3)) + fabsf(d(-1, 1) - d(3, -3)));
+            const float wtse = 1.0f / (EPS + fabsf(d(1, 1) - d(-1, -1)) + fabsf(d(1, 1) - d(3, -3)) + fabsf(d(-1, -1) - d(3, 3)));
+            p.row(rr)[cc >> 1] =
+                (wtnw * (1.325f * d(-1, -1) - 0.175f * d(-3, -3) - 0.075f * d(-1, -3) - 0.075f * d(-3, -1)) +
+                 wtne * (1.325f * d(-1, 1) - 0.175f * d(-3, 3) - 0.075f * d(-1, 3) - 0.075f * d(1, 1)) +
+                 wtsw * (1.325f * d(1, -1) - 0.175f * d(3, -3) - 0.075f * d(1, -3) - 0.075f * d(-1, -1)) +
+                 wtse * (1.325f * d(1, 1) - 0.175f * d(3, 3) - 0.075f * d(1, 3) - 0.075f * d(3, 1))) /
+                (wtnw + wtne + wtsw + wtse);
+          }
+        }
+        __syncthreads();
+        // -- finish_planes (chroma.rs:98-147) + write_tile (mod.rs:196-268), lag 15, core rows
+        {
+          const int lo = max(F - BH - 15, BORDER), hi = min(F - 15, TS - BORDER);
+          for (int k = t; k < (hi - lo) * VALID; k += THREADS) {
+            const int ly = lo - BORDER + k / VALID, lx = k % VALID;
+            const int gx = ox + lx, gy = oy + ly;
+            if (gx >= W || gy >= H) continue;
+            const int rr = ly + BORDER, cc = lx + BORDER;
+            const float sample = cfa.row(rr)[cc];  // in-image core sample, not mirrored
+            const int ch = color_at(pattern, gx, gy);
+            float r, b, gv;
+            if (fc(pattern, rr, cc) == 1) {
+              gv = sample;
+              const float* hvr = hv.row(rr);
+              const float up = hv.row(rr - 1)[cc >> 1], down = hv.row(rr + 1)[cc >> 1];
+              const float left = hvr[(cc - 1) >> 1], right = hvr[(cc + 1) >> 1];
+              const float temp = 1.0f / (up + 2.0f - right - left + down);
+              const float* a0 = dgrb0.row(rr);
+              const float* b0 = dgrb1.row(rr);
+              const float br = (up * dgrb0.row(rr - 1)[cc >> 1] + (1.0f - right) * a0[(cc + 1) >> 1] +
+                                (1.0f - left) * a0[(cc - 1) >> 1] + down * dgrb0.row(rr + 1)[cc >> 1]) *
+                               temp;
+              const float bb = (up * dgrb1.row(rr - 1)[cc >> 1] + (1.0f - right) * b0[(cc + 1) >> 1] +
+                                (1.0f - left) * b0[(cc - 1) >> 1] + down * dgrb1.row(rr + 1)[cc >> 1]) *
+                               temp;
+              r = gv - br;
+              b = gv - bb;
+            } else {
+              gv = green.row(rr)[cc >> 1];
+              r = gv - dgrb0.row(rr)[cc >> 1];
+              b = gv - dgrb1.row(rr)[cc >> 1];
+            }
+            r = fmax_(r, 0.0f);
+            b = fmax_(b, 0.0f);
+            float rgb0 = ch == 0 ? sample : r;
+            float rgb1 = ch == 1 ? sample : fmax_(gv, 0.0f);
+            float rgb2 = ch == 2 ? sample : b;
+            rgb0 = rgb0 * prm.gains[0];
+            rgb1 = rgb1 * prm.gains[1];
+            rgb2 = rgb2 * prm.gains[2];
+            if (!isfinite(rgb0) || !isfinite(rgb1) || !isfinite(rgb2)) bad = 1;
+            const long long o = (long long)gy * W + gx;
+            prm.out[o] = rgb0;
+            prm.out[plane + o] = rgb1;
+            prm.out[2 * plane + o] = rgb2;
+            if (prm.count_clip) {
+              const float v = source_normalized(src, gx, gy);
+              const float limit = src.clip_levels[ch];
+              if (v >= limit) {
+                affected++;
+                if (ch == 0) ac0++;
+                else if (ch == 1) ac1++;
+                else ac2++;
+              }
+              if (v > 1.0f) over++;
+              if (v > limit) changed++;
+            }
+          }
+        }
+        __syncthreads();
       }
       if (prm.count_clip) {
-        unsigned long long vals[6] = {affected, changed, over, ac[0], ac[1], ac[2]};
+        unsigned long long vals[6] = {affected, changed, over, ac0, ac1, ac2};
         for (int c = 0; c < 6; ++c) {
           unsigned long long v = vals[c];
-          for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-          if ((t & 31) == 0 && v) atomicAdd(&s_stats[c], v);
+          for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(FULL, v, off);
+          if (lane == 0 && v) atomicAdd(&s_stats[c], v);
         }
       }
       if (bad) atomicOr(&s_bad, 1);
@@ -751,33 +924,30 @@ __global__ void __launch_bounds__(THREADS, 2) amaze_kernel(const AmazeParams prm
 
 }  // namespace
 
-size_t amaze_slot_floats() { return SLOT_FLOATS; }
-
 Status run_amaze(Context& ctx, const MosaicSource& src, const float gains[3], float clip_point, float* rgb,
                  int count_clip, unsigned long long* clip_stats) {
   const int tiles_x = (src.width + VALID - 1) / VALID, tiles_y = (src.height + VALID - 1) / VALID;
   const int ntiles = tiles_x * tiles_y;
-  // Two resident CTAs per SM; balance the waves so the last one is full.
-  const int max_ctas = 2 * (ctx.sm_count > 0 ? ctx.sm_count : 152);
-  const int waves = (ntiles + max_ctas - 1) / max_ctas;
+  // One resident CTA per SM; balance the tiles so every CTA gets the same count or one fewer.
+  const int sms = ctx.sm_count > 0 ? ctx.sm_count : 152;
+  const int waves = (ntiles + sms - 1) / sms;
   const int grid = (ntiles + waves - 1) / waves;
   if ((size_t)grid > ctx.amaze_slots) {
-    // Slots are kept between calls and only grow, to the grid of the largest image seen.
-    if (ctx.amaze_scratch) device_free(ctx, ctx.amaze_scratch, ctx.amaze_slots * SLOT_FLOATS * sizeof(float));
+    // Slabs are kept between calls and only grow, to the grid of the largest image seen.
+    if (ctx.amaze_scratch) device_free(ctx, ctx.amaze_scratch, ctx.amaze_slots * SLAB_FLOATS * sizeof(float));
     ctx.amaze_scratch = nullptr;
     ctx.amaze_slots = 0;
     void* p = nullptr;
-    RD_TRY(device_alloc(ctx, (size_t)grid * SLOT_FLOATS * sizeof(float), &p));
-    // vcd/hcd/vcdalt/hcdalt are read outside the region the stages write and
-    // must stay zero there (scratch.rs:95-104); nothing ever writes them.
-    RD_CUDA_TRY(cudaMemsetAsync(p, 0, (size_t)grid * SLOT_FLOATS * sizeof(float), ctx.stream));
+    RD_TRY(device_alloc(ctx, (size_t)grid * SLAB_FLOATS * sizeof(float), &p));
+    RD_CUDA_TRY(cudaMemsetAsync(p, 0, (size_t)grid * SLAB_FLOATS * sizeof(float), ctx.stream));
     ctx.amaze_scratch = static_cast<float*>(p);
     ctx.amaze_slots = grid;
   }
+  RD_CUDA_TRY(cudaFuncSetAttribute(amaze_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
   AmazeParams prm;
   prm.src = src;
   prm.out = rgb;
-  prm.scratch = ctx.amaze_scratch;
+  prm.slab = ctx.amaze_scratch;
   prm.tiles_x = tiles_x;
   prm.tiles_y = tiles_y;
   prm.clip_point = clip_point;
@@ -785,7 +955,7 @@ Status run_amaze(Context& ctx, const MosaicSource& src, const float gains[3], fl
   prm.count_clip = count_clip;
   prm.clip_stats = clip_stats;
   prm.error = ctx.d_error;
-  RD_LAUNCH(ctx, K_AMAZE, amaze_kernel<<<grid, THREADS, 0, ctx.stream>>>(prm));
+  RD_LAUNCH(ctx, K_AMAZE, amaze_kernel<<<grid, THREADS, SMEM_BYTES, ctx.stream>>>(prm));
   RD_CUDA_TRY(cudaGetLastError());
   return Status{};
 }

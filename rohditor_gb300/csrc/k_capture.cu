@@ -6,7 +6,7 @@
 // and a ping-pong pair for the estimate). Kernels:
 //   rl_init      guide = max(sum max(c,0)/3, 1e-6), mask = 1 - smoothstep(peak)
 //   rl_mask      blur(mask) and blur(guide) on one tile, refines the mask
-//   rl_iter      one whole RL iteration per tile in shared memory:
+//   rl_stream    one whole RL iteration streamed down column strips:
 //                blur(estimate) -> ratio = guide / max(b, 1e-6) -> blur(ratio)
 //                -> estimate = clamp(estimate * b, guide/2, 2 guide)
 //                so an iteration reads the estimate and guide once and writes
@@ -18,6 +18,8 @@
 // values outside the image are filled from their mirror position, so every
 // stencil read equals the reference's mirrored read bit for bit.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 #include "rd_internal.cuh"
 
@@ -96,28 +98,52 @@ __device__ __forceinline__ float hblur(const float* row, int qx, int x, int W, i
   return v;
 }
 
-// ---- one fused RL iteration per tile --------------------------------------
-// Compile-time radius R (1..4) and tile. Each separable pass runs as "runs":
-// a thread produces RUN consecutive outputs along the blur direction from a
-// register window, so shared memory is read about once per output instead of
-// 2R+1 times. Every output still sums its taps in kernel order from 0 (or
-// -0.0 on horizontal border columns), exactly as the reference.
+// ---- one RL iteration, streamed down column strips --------------------------
+// A CTA owns a strip of SW = 128 - 2R output columns and a segment of rows and
+// walks the segment top to bottom in steps of BH rows:
+//   * estimate and guide rows arrive by cp.async one step ahead into 32-row
+//     rings;
+//   * the horizontal pass of blur #1 runs on every arriving row; the vertical
+//     pass and the ratio run R rows behind, the horizontal pass of blur #2 on
+//     the same rows, and the vertical pass of blur #2 with the bounded update
+//     2R rows behind, each from a 16-row ring;
+//   * rows above or below the image are never computed: a vertical pass reads
+//     the mirrored row instead, which holds the same values (a horizontal pass
+//     commutes with a row reflection, and the ratio of a mirrored position is
+//     its mirror's ratio), so only the 2R columns at each strip edge are
+//     recomputed.
+// Runs of RUN outputs per thread come from a register window, so shared
+// memory is read about once per output; every output still sums its taps in
+// kernel order from 0 (or -0.0 on horizontal border columns).
 template <int R>
-struct IterGeom {
+struct StreamGeom {
   static constexpr int T = 2 * R + 1;
-  static constexpr int EW = TX + 4 * R, EH = TY + 4 * R;  // estimate window
-  static constexpr int QW = TX + 2 * R, QH = TY + 2 * R;  // ratio window
-  static constexpr int EP = EW | 1, QP = QW | 1, CP = TX + 1;  // odd pitches: conflict-free columns
+  static constexpr int QW = 128;         // columns [x0 - R, x0 + SW + R): one per thread
+  static constexpr int SW = QW - 2 * R;  // output columns of a strip
+  static constexpr int EW = QW + 2 * R;  // estimate columns [x0 - 2R, x0 + SW + 2R)
+  static constexpr int BH = 8, RIN = 32, RS = 16;
+  static constexpr int H1_RUNS = 15, H1_RUN = (QW + H1_RUNS - 1) / H1_RUNS;
+  static constexpr int H2_RUN = 8, H2_RUNS = (SW + H2_RUN - 1) / H2_RUN;
 };
 
 template <int R>
-struct IterSmem {
-  using G = IterGeom<R>;
-  float e[G::EH * G::EP];
-  float t1[G::EH * G::QP];
-  float q[G::QH * G::QP];
-  float t2[G::QH * G::CP];
+struct StreamSmem {
+  using G = StreamGeom<R>;
+  float e[G::RIN][G::EW];   // estimate rows
+  float g[G::RIN][G::QW];   // guide rows (in-image columns)
+  float t1[G::RS][G::QW];   // horizontal pass of blur #1
+  float q[G::BH][G::QW];    // ratio rows of the current step
+  float t2[G::RS][G::QW];   // horizontal pass of blur #2 (first SW columns)
 };
+
+__device__ __forceinline__ void cp_async4(float* smem, const float* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+__device__ __forceinline__ int mirror_row(int y, int H) { return (unsigned)y < (unsigned)H ? y : mirror_half(y, H); }
 
 // Horizontal run: `n` (<= RUN) outputs starting at window column `c0` of
 // `row`, written to `out`; `x0img` is the image column of the first output.
@@ -141,131 +167,153 @@ __device__ __forceinline__ void hrun(const float* __restrict__ row, int c0, int 
 }
 
 template <int R>
-__global__ void __launch_bounds__(256, 2) rl_iter_kernel(const float* __restrict__ est_in,
-                                                         const float* __restrict__ guide,
-                                                         float* __restrict__ est_out, int W, int H) {
-  using G = IterGeom<R>;
-  constexpr int T = G::T;
+__global__ void __launch_bounds__(128) rl_stream_kernel(const float* __restrict__ est_in,
+                                                        const float* __restrict__ guide,
+                                                        float* __restrict__ est_out, int W, int H, int strips,
+                                                        int seg_h, int items) {
+  using G = StreamGeom<R>;
+  constexpr int T = G::T, SW = G::SW, QW = G::QW, EW = G::EW, BH = G::BH;
   extern __shared__ float4 rl_smem_raw[];
-  IterSmem<R>& S = *reinterpret_cast<IterSmem<R>*>(rl_smem_raw);
+  StreamSmem<R>& S = *reinterpret_cast<StreamSmem<R>*>(rl_smem_raw);
   float w[T];
 #pragma unroll
   for (int k = 0; k < T; ++k) w[k] = c_kernel[k];
-  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
   const int tid = threadIdx.x;
-  const bool interior = x0 - 2 * R >= 0 && x0 + TX + 2 * R <= W && y0 - 2 * R >= 0 && y0 + TY + 2 * R <= H;
-  const int ex = x0 - 2 * R, ey = y0 - 2 * R;  // estimate window origin
-  // 1. estimate window (mirrored reads only on edge tiles)
-  if (interior) {
-    for (int k = tid; k < G::EH * G::EW; k += 256) {
-      const int r = k / G::EW, c = k - r * G::EW;
-      S.e[r * G::EP + c] = est_in[(long long)(ey + r) * W + ex + c];
-    }
-  } else {
-    for (int k = tid; k < G::EH * G::EW; k += 256) {
-      const int r = k / G::EW, c = k - r * G::EW;
-      S.e[r * G::EP + c] = est_in[(long long)mirror_half(ey + r, H) * W + mirror_half(ex + c, W)];
-    }
-  }
-  __syncthreads();
-  // 2. horizontal pass of blur #1: window rows x ratio-window columns, runs of 16
-  {
-    constexpr int RUN = 16, RUNS = (G::QW + RUN - 1) / RUN;
-    for (int k = tid; k < G::EH * RUNS; k += 256) {
-      const int r = k / RUNS, s = k - r * RUNS;
-      const int qc0 = s * RUN;
-      const int n = min(RUN, G::QW - qc0);
-      const int x0img = x0 - R + qc0;
-      // Columns outside the image are never read downstream; computing them is harmless.
-      hrun<R, RUN>(S.e + r * G::EP, qc0 + R, n, S.t1 + r * G::QP + qc0, x0img, W, w);
-    }
-  }
-  __syncthreads();
-  // 3. vertical pass of blur #1 and the ratio, runs of RUN rows per column
-  {
-    constexpr int RUN = (G::QH + 2) / 3;
-    constexpr int RUNS = (G::QH + RUN - 1) / RUN;
-    for (int k = tid; k < G::QW * RUNS; k += 256) {
-      const int s = k / G::QW, qc = k - s * G::QW;
-      const int qr0 = s * RUN;
-      const int n = min(RUN, G::QH - qr0);
-      const int x = x0 - R + qc;
-      float win[RUN + 2 * R];
+  for (int item = blockIdx.x; item < items; item += gridDim.x) {
+    const int x0 = (item % strips) * SW, y0 = (item / strips) * seg_h;
+    const int y1 = min(y0 + seg_h, H);
+    const int e_end = min(y1 + 2 * R, H), q_end = min(y1 + R, H);
+    int e_next = max(y0 - 2 * R, 0), q_next = max(y0 - R, 0), o_next = y0;
+    const bool edge = x0 - 2 * R < 0 || x0 + SW + 2 * R > W;
+    // Estimate and guide rows [r0, r1) into the input rings.
+    auto issue = [&](int r0, int r1) {
+      for (int k = tid; k < (r1 - r0) * EW; k += 128) {
+        const int r = r0 + k / EW, c = k - (k / EW) * EW;
+        const int x = x0 - 2 * R + c;
+        const int sx = (unsigned)x < (unsigned)W ? x : mirror_half(x, W);
+        cp_async4(&S.e[r & (G::RIN - 1)][c], est_in + (long long)r * W + sx);
+      }
+      for (int k = tid; k < (r1 - r0) * QW; k += 128) {
+        const int r = r0 + (k >> 7), c = k & (QW - 1);
+        const int x = x0 - R + c;
+        if ((unsigned)x < (unsigned)W) cp_async4(&S.g[r & (G::RIN - 1)][c], guide + (long long)r * W + x);
+      }
+    };
+    issue(e_next, min(e_next + BH, e_end));
+    cp_async_commit();
+    while (o_next < y1) {
+      const int e_hi = min(e_next + BH, e_end);
+      issue(e_hi, min(e_hi + BH, e_end));
+      cp_async_commit();
+      cp_async_wait1();
+      __syncthreads();
+      // 1. horizontal pass of blur #1 on rows [e_next, e_hi)
+      for (int k = tid; k < (e_hi - e_next) * G::H1_RUNS; k += 128) {
+        const int r = e_next + k / G::H1_RUNS, s = k % G::H1_RUNS;
+        const int qc0 = s * G::H1_RUN;
+        const int n = min(G::H1_RUN, QW - qc0);
+        if (n > 0) hrun<R, G::H1_RUN>(S.e[r & (G::RIN - 1)], qc0 + R, n, S.t1[r & (G::RS - 1)] + qc0, x0 - R + qc0, W, w);
+      }
+      const int q_avail = e_hi >= H ? q_end : e_hi - R;
+      const int q_hi = max(q_next, min(min(q_next + BH, q_end), q_avail));
+      __syncthreads();
+      // 2. vertical pass of blur #1 and the ratio on rows [q_next, q_hi), column tid
+      {
+        const int x = x0 - R + tid, n = q_hi - q_next;
+        if (n > 0 && (unsigned)x < (unsigned)W) {
+          float win[BH + 2 * R];
 #pragma unroll
-      for (int j = 0; j < RUN + 2 * R; ++j) win[j] = (j < n + 2 * R) ? S.t1[(qr0 + j) * G::QP + qc] : 0.0f;
+          for (int j = 0; j < BH + 2 * R; ++j)
+            win[j] = j < n + 2 * R ? S.t1[mirror_row(q_next - R + j, H) & (G::RS - 1)][tid] : 0.0f;
 #pragma unroll
-      for (int j = 0; j < RUN; ++j) {
-        const int y = y0 - R + qr0 + j;
-        if (j < n && x >= 0 && x < W && y >= 0 && y < H) {
-          float b = 0.0f;
+          for (int j = 0; j < BH; ++j) {
+            if (j < n) {
+              float b = 0.0f;
 #pragma unroll
-          for (int t = 0; t < T; ++t) b += win[j + t] * w[t];
-          S.q[(qr0 + j) * G::QP + qc] = __ldg(guide + (long long)y * W + x) / rmax(b, FLOOR);
+              for (int t = 0; t < T; ++t) b += win[j + t] * w[t];
+              const int y = q_next + j;
+              S.q[y & (BH - 1)][tid] = S.g[y & (G::RIN - 1)][tid] / rmax(b, FLOOR);
+            }
+          }
         }
       }
-    }
-  }
-  __syncthreads();
-  if (!interior) {
-    // Out-of-image ratio entries within R of the image take their mirror's value.
-    for (int k = tid; k < G::QH * G::QW; k += 256) {
-      const int qr = k / G::QW, qc = k - qr * G::QW;
-      const int x = x0 - R + qc, y = y0 - R + qr;
-      if (x >= 0 && x < W && y >= 0 && y < H) continue;
-      if (x < -R || x >= W + R || y < -R || y >= H + R) continue;
-      const int mx = mirror_half(x, W) - (x0 - R), my = mirror_half(y, H) - (y0 - R);
-      S.q[qr * G::QP + qc] = S.q[my * G::QP + mx];
-    }
-    __syncthreads();
-  }
-  // 4. horizontal pass of blur #2 on the core columns, runs of 16
-  {
-    constexpr int RUN = 16, RUNS = TX / RUN;
-    for (int k = tid; k < G::QH * RUNS; k += 256) {
-      const int r = k / RUNS, s = k - r * RUNS;
-      const int c0 = s * RUN;
-      const int n = min(RUN, W - (x0 + c0));
-      if (n <= 0) continue;
-      hrun<R, RUN>(S.q + r * G::QP, c0 + R, n, S.t2 + r * G::CP + c0, x0 + c0, W, w);
-    }
-  }
-  __syncthreads();
-  // 5. vertical pass of blur #2 and the bounded update, runs of 8 rows
-  {
-    constexpr int RUN = 8, RUNS = TY / RUN;
-    for (int k = tid; k < TX * RUNS; k += 256) {
-      const int s = k / TX, c = k - s * TX;
-      const int x = x0 + c;
-      if (x >= W) continue;
-      const int r0 = s * RUN;
-      float win[RUN + 2 * R];
-#pragma unroll
-      for (int j = 0; j < RUN + 2 * R; ++j) win[j] = S.t2[(r0 + j) * G::CP + c];
-#pragma unroll
-      for (int j = 0; j < RUN; ++j) {
-        const int y = y0 + r0 + j;
-        if (y >= H) break;
-        float b = 0.0f;
-#pragma unroll
-        for (int t = 0; t < T; ++t) b += win[j + t] * w[t];
-        const long long o = (long long)y * W + x;
-        const float g = __ldg(guide + o);
-        float e = S.e[(r0 + j + 2 * R) * G::EP + c + 2 * R] * b;
-        const float lo = g * 0.5f, hi = g * 2.0f;
-        if (e < lo) e = lo;
-        if (e > hi) e = hi;
-        est_out[o] = e;
+      __syncthreads();
+      if (edge) {
+        // Ratio entries outside the image within R of it take their mirror's value.
+        const int x = x0 - R + tid;
+        if ((unsigned)x >= (unsigned)W && x >= -R && x < W + R) {
+          const int src = mirror_half(x, W) - (x0 - R);
+          for (int y = q_next; y < q_hi; ++y) S.q[y & (BH - 1)][tid] = S.q[y & (BH - 1)][src];
+        }
+        __syncthreads();
       }
+      // 3. horizontal pass of blur #2 on rows [q_next, q_hi), output columns
+      for (int k = tid; k < (q_hi - q_next) * G::H2_RUNS; k += 128) {
+        const int r = q_next + k / G::H2_RUNS, s = k % G::H2_RUNS;
+        const int c0 = s * G::H2_RUN;
+        const int n = min(min(G::H2_RUN, SW - c0), W - (x0 + c0));
+        if (n > 0) hrun<R, G::H2_RUN>(S.q[r & (BH - 1)], c0 + R, n, S.t2[r & (G::RS - 1)] + c0, x0 + c0, W, w);
+      }
+      const int o_avail = q_hi >= H ? y1 : q_hi - R;
+      const int o_hi = max(o_next, min(min(o_next + BH, y1), o_avail));
+      __syncthreads();
+      // 4. vertical pass of blur #2 and the bounded update on rows [o_next, o_hi)
+      {
+        const int x = x0 + tid, n = o_hi - o_next;
+        if (tid < SW && x < W && n > 0) {
+          float win[BH + 2 * R];
+#pragma unroll
+          for (int j = 0; j < BH + 2 * R; ++j)
+            win[j] = j < n + 2 * R ? S.t2[mirror_row(o_next - R + j, H) & (G::RS - 1)][tid] : 0.0f;
+#pragma unroll
+          for (int j = 0; j < BH; ++j) {
+            if (j < n) {
+              float b = 0.0f;
+#pragma unroll
+              for (int t = 0; t < T; ++t) b += win[j + t] * w[t];
+              const int y = o_next + j;
+              const float g = S.g[y & (G::RIN - 1)][tid + R];
+              float e = S.e[y & (G::RIN - 1)][tid + 2 * R] * b;
+              const float lo = g * 0.5f, hi = g * 2.0f;
+              if (e < lo) e = lo;
+              if (e > hi) e = hi;
+              est_out[(long long)y * W + x] = e;
+            }
+          }
+        }
+      }
+      e_next = e_hi;
+      q_next = q_hi;
+      o_next = o_hi;
+      __syncthreads();
     }
+    // Drain the (empty) trailing copy group before the rings are reused.
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    __syncthreads();
   }
 }
 
 template <int R>
 Status launch_rl_iter(Context& ctx, const float* est, const float* guide, float* out, int W, int H) {
-  const size_t smem = sizeof(IterSmem<R>);
-  RD_CUDA_TRY(cudaFuncSetAttribute(rl_iter_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  dim3 grid((W + TX - 1) / TX, (H + TY - 1) / TY);
-  RD_LAUNCH(ctx, K_RL_ITER, rl_iter_kernel<R><<<grid, 256, smem, ctx.stream>>>(est, guide, out, W, H));
+  using G = StreamGeom<R>;
+  const size_t smem = sizeof(StreamSmem<R>);
+  RD_CUDA_TRY(cudaFuncSetAttribute(rl_stream_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int occ = 0;
+  RD_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, rl_stream_kernel<R>, 128, smem));
+  const int sms = ctx.sm_count > 0 ? ctx.sm_count : 152;
+  const int slots = std::max(1, occ) * sms;
+  const int strips = (W + G::SW - 1) / G::SW;
+  // Segments: one round of (strip, segment) items over all resident CTAs, each
+  // segment at least 32 rows (vertical halos) and at most 512 (more rounds).
+  const int per_round = std::max(1, slots / strips);
+  int segs = std::min(per_round, std::max(1, H / 32));
+  while ((H + segs - 1) / segs > 512) segs += per_round;
+  const int seg_h = (H + segs - 1) / segs;
+  const int nseg = (H + seg_h - 1) / seg_h;
+  const int items = strips * nseg;
+  const int grid = std::min(items, slots);
+  RD_LAUNCH(ctx, K_RL_ITER, rl_stream_kernel<R><<<grid, 128, smem, ctx.stream>>>(est, guide, out, W, H, strips,
+                                                                               seg_h, items));
   return Status{};
 }
 

@@ -143,7 +143,10 @@ __device__ __forceinline__ float source_normalized(const MosaicSource& s, int x,
   if (s.f32) return s.f32[(long long)y * s.width + x];
   const int sx = s.crop_x + x, sy = s.crop_y + y;
   const float sample = (float)s.raw[(long long)sy * s.row_stride + sx];
-  const int bi = (sy % s.black_h) * s.black_w + (sx % s.black_w);
+  // Level patterns repeat every 1, 2 or 4 samples in practice: mask instead of divide.
+  const int by = (s.black_h & (s.black_h - 1)) == 0 ? (sy & (s.black_h - 1)) : sy % s.black_h;
+  const int bx = (s.black_w & (s.black_w - 1)) == 0 ? (sx & (s.black_w - 1)) : sx % s.black_w;
+  const int bi = by * s.black_w + bx;
   const float black = s.black[bi];
   float white;
   if (s.white_count == 1) white = s.white[0];
