@@ -138,14 +138,17 @@ enum { A_CFA, A_W0, A_W1, A_DELHV, A_VCD, A_HCD, A_VALT, A_DGV, A_DGH, A_N16 };
 constexpr int A_HALT_OFF = A_N16 * 16 * TS;
 constexpr int A_CDD_OFF = A_HALT_OFF + 8 * TS;
 constexpr int A_FLOATS = A_CDD_OFF + 16 * TSH;
-// Phase B: 32-row mosaic ring; 32-row half rings for the slab planes; 16-row
-// half rings; u8 Nyquist flags (16 rows) and refined flags (32 rows).
+// Phase B: 32-row mosaic ring; 32-row half rings for the slab planes and for
+// the diagonal weights / estimates (read two steps after they are made);
+// 16-row half rings; u8 Nyquist flags (16 rows) and refined flags (32 rows).
 constexpr int B_CFA_OFF = 0;
 constexpr int B_HV_OFF = B_CFA_OFF + 32 * TS;
 constexpr int B_VRB_OFF = B_HV_OFF + 32 * TSH;
 constexpr int B_HRB_OFF = B_VRB_OFF + 32 * TSH;
-enum { B_DGRB0, B_DGRB1, B_GREEN, B_D2H, B_D2V, B_DELP, B_DELM, B_SQP, B_SQM, B_PMWT, B_RBP, B_RBM, B_RBINT, B_N16 };
-constexpr int B_H16_OFF = B_HRB_OFF + 32 * TSH;
+enum { B_DGRB0, B_DGRB1, B_GREEN, B_D2H, B_D2V, B_DELP, B_DELM, B_SQP, B_SQM, B_RBINT, B_N16 };
+enum { B_PMWT, B_RBP, B_RBM, B_N32 };
+constexpr int B_H32_OFF = B_HRB_OFF + 32 * TSH;
+constexpr int B_H16_OFF = B_H32_OFF + B_N32 * 32 * TSH;
 constexpr int B_U8_OFF = B_H16_OFF + B_N16 * 16 * TSH;
 constexpr int B_FLOATS = B_U8_OFF + (16 * TSH + 32 * TSH) / 4;
 constexpr int SMEM_FLOATS = A_FLOATS > B_FLOATS ? A_FLOATS : B_FLOATS;
@@ -172,6 +175,62 @@ __device__ __forceinline__ float tile_sample(const MosaicSource& src, int x, int
   const int sx = (unsigned)x < (unsigned)W ? x : mirror_index(x, W);
   const int sy = (unsigned)y < (unsigned)H ? y : mirror_index(y, H);
   return source_balanced(src, sx, sy);
+}
+
+// One warp sweeps rows [lo, hi) of a weight recurrence (populate_green's hvwt
+// update with START = 8, combine_diagonals' pmwt update with START = 10): at
+// each red/blue site cc = START + gae + 2k of [START, 256 - START), the weight
+// w takes alt = (w'(r-1, cc-1) + w'(r-1, cc+1) + w(r+1, cc-1) + w(r+1, cc+1)) / 4
+// when alt is further from 0.5, where w' is the already updated row above.
+// Lane l owns half-indices 4l + START/2 .. +3 (site k = half-index - START/2);
+// the updated row above stays in registers (`up`), so a row costs two
+// shuffles and no barrier. The row below and the row itself are read from
+// shared memory, the updated row is written back there.
+template <int START, class RingT>
+__device__ __forceinline__ void recurrence_rows(const RingT& ring, int lo, int hi, int g0, int lane,
+                                                float (&up)[4]) {
+  constexpr int J0 = START / 2;                // half-index of site k = 0
+  constexpr int SITES = (TS - 2 * START) / 2;  // sites per row
+  const unsigned FULL = 0xffffffffu;
+  const int jb = J0 + 4 * lane;
+  for (int rr = lo; rr < hi; ++rr) {
+    if (rr == START) {
+      // The row above the first updated row keeps its values.
+      const float* a = ring.row(rr - 1);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) up[q] = jb + q < TSH ? a[jb + q] : 0.0f;
+    }
+    const int g = g0 ^ (rr & 1);
+    const float* down = ring.row(rr + 1);
+    float* cur = ring.row(rr);
+    // Updated row above at half-indices jb - 1 and jb + 4 (neighbouring lanes;
+    // jb - 1 of lane 0 lies left of every site and was never updated).
+    float left_in = __shfl_up_sync(FULL, up[3], 1);
+    const float right_in = __shfl_down_sync(FULL, up[0], 1);
+    if (lane == 0) left_in = ring.row(rr - 1)[J0 - 1];
+    float nu[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int j = jb + q, k = 4 * lane + q;
+      nu[q] = 0.0f;
+      if (j < TSH) {
+        const float w = cur[j];
+        nu[q] = w;
+        if (k < SITES) {
+          const float ua = g == 0 ? (q == 0 ? left_in : up[q - 1]) : up[q];
+          const float ub = g == 0 ? up[q] : (q == 3 ? right_in : up[q + 1]);
+          // x * 0.25 and x / 4 are the same correctly rounded value for every x.
+          const float alt = (ua + ub + down[j - 1 + g] + down[j + g]) * 0.25f;
+          if (fabsf(0.5f - w) < fabsf(0.5f - alt)) {
+            nu[q] = alt;
+            cur[j] = alt;
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) up[q] = nu[q];
+  }
 }
 
 // Two-state transition maps: bit 0 = next state after state A, bit 1 = after
@@ -212,6 +271,10 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
     else ey = 1;
   }
   const int blue_par = (13 - ey) & 1;
+  // Red/blue sites of row r sit at columns of parity g0 ^ (r & 1) (gae of the
+  // reference); ctab is the packed 2x2 colour table of the pattern (color_at).
+  const int g0 = gae(pattern, 0);
+  const unsigned ctab = pattern == 0 ? 0x94u : pattern == 1 ? 0x16u : pattern == 2 ? 0x61u : 0x49u;
 
   const int ntiles = prm.tiles_x * prm.tiles_y;
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -229,21 +292,24 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
       const Ring<8, TS> halt{sm + A_HALT_OFF};
       const Ring<16, TSH> cdd{sm + A_CDD_OFF};
       float vprev = 0.0f;  // vcd column chain value (threads 512..1007)
-      for (int F = BH; F <= TS + 8; F += BH) {
-        // -- load rows [F-8, F): populate (mod.rs:175-194)
-        {
-          const int lo = F - BH, hi = min(F, TS);
-          for (int k = t; k < (hi - lo) * TS; k += THREADS) {
-            const int rr = lo + (k >> 8), cc = k & (TS - 1);
-            cfa.row(rr)[cc] = tile_sample(src, ox - BORDER + cc, oy - BORDER + rr, W, H);
-          }
+      // populate (mod.rs:175-194): rows [F, F+8) are loaded at the end of the
+      // step before, while the last stage computes.
+      auto load_rows = [&](int lo) {
+        const int hi = min(lo + BH, TS);
+        for (int k = t; k < (hi - lo) * TS; k += THREADS) {
+          const int rr = lo + (k >> 8), cc = k & (TS - 1);
+          cfa.row(rr)[cc] = tile_sample(src, ox - BORDER + cc, oy - BORDER + rr, W, H);
         }
-        __syncthreads();
+      };
+      load_rows(0);
+      __syncthreads();
+      for (int F = BH; F <= TS + 8; F += BH) {
         // -- gradients (green.rs:13-29), lag 2, rows/cols [2, 254)
         {
           const int lo = max(F - BH - 2, 2), hi = min(F - 2, TS - 2);
-          for (int k = t; k < (hi - lo) * (TS - 4); k += THREADS) {
-            const int rr = lo + k / (TS - 4), cc = 2 + k % (TS - 4);
+          for (int k = t; k < (hi - lo) * TS; k += THREADS) {
+            const int rr = lo + (k >> 8), cc = 2 + (k & (TS - 1));
+            if (cc >= TS - 2) continue;
             const float* c0 = cfa.row(rr);
             const float* cu = cfa.row(rr - 1);
             const float* cd = cfa.row(rr + 1);
@@ -258,9 +324,10 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
         // -- colour differences (green.rs:46-139), lag 4, rows/cols [4, 252)
         {
           const int lo = max(F - BH - 4, 4), hi = min(F - 4, TS - 4);
-          for (int k = t; k < (hi - lo) * (TS - 8); k += THREADS) {
-            const int rr = lo + k / (TS - 8), cc = 4 + k % (TS - 8);
-            const bool green_first = (fc(pattern, rr, 4) & 1) == 1;
+          for (int k = t; k < (hi - lo) * TS; k += THREADS) {
+            const int rr = lo + (k >> 8), cc = 4 + (k & (TS - 1));
+            if (cc >= TS - 4) continue;
+            const bool green_first = (g0 ^ (rr & 1)) == 1;
             const bool fcswitch = green_first == ((cc & 1) == 0);
             const float* c0 = cfa.row(rr);
             const float cur = c0[cc];
@@ -322,7 +389,7 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
             float* hr = hcd.row(rr);
             const float* ha = halt.row(rr);
             const float* c0 = cfa.row(rr);
-            const bool hg4 = (fc(pattern, rr, 4) & 1) == 1;
+            const bool hg4 = (g0 ^ (rr & 1)) == 1;
             constexpr int STEPS = (TS - 8) / 2;  // 124 sites per chain
             unsigned s_in = 0;                   // chain state after the previous round
             float last_a = 0.0f, last_b = 0.0f;  // candidates of the previous round's last step
@@ -385,7 +452,7 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
             const float vcdvar = spread(vprev, vcur, vnext);
             const float vcdaltvar = spread(aprev, acur, anext);
             const float vsel = vcdaltvar < vcdvar ? acur : vcur;
-            const bool g = ((fc(pattern, rr, 4) & 1) == 1) != vg4;
+            const bool g = ((g0 ^ (rr & 1)) == 1) != vg4;
             const float b = bound_sel(g, vsel, cfa.row(rr)[vc], cfa.row(rr - 1)[vc], cfa.row(rr + 1)[vc], clip_pt);
             vcd.row(rr)[vc] = b;
             vprev = b;
@@ -395,20 +462,21 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
         // -- cdd at red/blue sites (green.rs:187-222 tail), lag 6
         {
           const int lo = max(F - BH - 6, 4), hi = min(F - 6, TS - 4);
-          constexpr int per_row = (TS - 8) / 2;
+          constexpr int per_row = 128;  // site slots per row: one pass of 1024 threads over 8 rows
           for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
-            const int rr = lo + k / per_row;
-            const int cc = 4 + gae(pattern, rr) + 2 * (k % per_row);
+            const int rr = lo + (k >> 7);
+            const int cc = 4 + (g0 ^ (rr & 1)) + 2 * (k & 127);
+            if (cc >= TS - 4) continue;
             cdd.row(rr)[cc >> 1] = sqr(vcd.row(rr)[cc] - hcd.row(rr)[cc]);
           }
         }
         // -- direction_weights (green.rs:225-292), lag 9, red/blue sites of [6, 250)^2
         {
           const int lo = max(F - BH - 9, 6), hi = min(F - 9, TS - 6);
-          constexpr int per_row = (TS - 12 + 1) / 2;
+          constexpr int per_row = 128;  // site slots per row: one pass of 1024 threads over 8 rows
           for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
-            const int rr = lo + k / per_row;
-            const int cc = 6 + gae(pattern, rr) + 2 * (k % per_row);
+            const int rr = lo + (k >> 7);
+            const int cc = 6 + (g0 ^ (rr & 1)) + 2 * (k & 127);
             if (cc >= TS - 6) continue;
             // vcd rows outside [4, 252) were never written: zero.
             float vv[7];
@@ -454,10 +522,10 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
         // -- Nyquist test (nyquist.rs:25-95), lag 8, red/blue sites of [6, 250)^2
         {
           const int lo = max(F - BH - 8, 6), hi = min(F - 8, TS - 6);
-          constexpr int per_row = (TS - 12 + 1) / 2;
+          constexpr int per_row = 128;  // site slots per row: one pass of 1024 threads over 8 rows
           for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
-            const int rr = lo + k / per_row;
-            const int cc = 6 + gae(pattern, rr) + 2 * (k % per_row);
+            const int rr = lo + (k >> 7);
+            const int cc = 6 + (g0 ^ (rr & 1)) + 2 * (k & 127);
             if (cc >= TS - 6) continue;
             const float* cm2 = cdd.row(rr - 2);
             const float* cm1 = cdd.row(rr - 1);
@@ -483,6 +551,8 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
             g_nyq[rr * TSH + j] = v > 0.0f ? 1 : 0;
           }
         }
+        // -- rows of the next step (their ring slots held rows no stage reads any more)
+        if (F < TS) load_rows(F);
         __syncthreads();
       }
     }
@@ -497,40 +567,44 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
       const Ring<16, TSH> dgrb0{h16 + B_DGRB0 * 16 * TSH}, dgrb1{h16 + B_DGRB1 * 16 * TSH},
           green{h16 + B_GREEN * 16 * TSH}, d2h{h16 + B_D2H * 16 * TSH}, d2v{h16 + B_D2V * 16 * TSH},
           delp{h16 + B_DELP * 16 * TSH}, delm{h16 + B_DELM * 16 * TSH}, sqp{h16 + B_SQP * 16 * TSH},
-          sqm{h16 + B_SQM * 16 * TSH}, pmwt{h16 + B_PMWT * 16 * TSH}, rbp{h16 + B_RBP * 16 * TSH},
-          rbm{h16 + B_RBM * 16 * TSH}, rbint{h16 + B_RBINT * 16 * TSH};
+          sqm{h16 + B_SQM * 16 * TSH}, rbint{h16 + B_RBINT * 16 * TSH};
+      float* h32 = sm + B_H32_OFF;
+      const Ring<32, TSH> pmwt{h32 + B_PMWT * 32 * TSH}, rbp{h32 + B_RBP * 32 * TSH}, rbm{h32 + B_RBM * 32 * TSH};
       unsigned char* u8 = reinterpret_cast<unsigned char*>(sm + B_U8_OFF);
       const Ring<16, TSH, unsigned char> nyq{u8};
       const Ring<32, TSH, unsigned char> nyq2{u8 + 16 * TSH};
       unsigned long long affected = 0, changed = 0, over = 0, ac0 = 0, ac1 = 0, ac2 = 0;
       int bad = 0;
-      for (int F = BH; F <= TS; F += BH) {
-        // -- load rows [F-8, F): mosaic, and the slab rows of [6, 250)
-        {
-          const int lo = F - BH;
-          for (int k = t; k < BH * TS; k += THREADS) {
-            const int rr = lo + (k >> 8), cc = k & (TS - 1);
-            cfa.row(rr)[cc] = tile_sample(src, ox - BORDER + cc, oy - BORDER + rr, W, H);
-          }
-          for (int k = t; k < BH * TSH; k += THREADS) {
-            const int rr = lo + (k >> 7), j = k & (TSH - 1);
-            if (rr < 6 || rr >= TS - 6) continue;
-            const int o = rr * TSH + j;
-            hv.row(rr)[j] = g_hv[o];
-            vrb.row(rr)[j] = g_vrb[o];
-            hrb.row(rr)[j] = g_hrb[o];
-            nyq.row(rr)[j] = g_nyq[o];
-          }
+      // Updated weights of the row above, four half-indices per lane (warps 0 and 1).
+      float hv_up[4] = {0.0f, 0.0f, 0.0f, 0.0f}, pm_up[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+      // Rows [lo, lo+8) of the mosaic and of the slab ([6, 250) only).
+      auto load_rows = [&](int lo) {
+        for (int k = t; k < BH * TS; k += THREADS) {
+          const int rr = lo + (k >> 8), cc = k & (TS - 1);
+          cfa.row(rr)[cc] = tile_sample(src, ox - BORDER + cc, oy - BORDER + rr, W, H);
         }
+        for (int k = t; k < BH * TSH; k += THREADS) {
+          const int rr = lo + (k >> 7), j = k & (TSH - 1);
+          if (rr < 6 || rr >= TS - 6) continue;
+          const int o = rr * TSH + j;
+          hv.row(rr)[j] = g_hv[o];
+          vrb.row(rr)[j] = g_vrb[o];
+          hrb.row(rr)[j] = g_hrb[o];
+          nyq.row(rr)[j] = g_nyq[o];
+        }
+      };
+      for (int F = BH; F <= TS + BH; F += BH) {
+        if (F - BH < TS) load_rows(F - BH);
         __syncthreads();
         // -- Nyquist flag refinement (nyquist.rs:108-130), lag 2, red/blue sites of [8, 248)^2;
         //    diagonal_gradients (diagonal.rs:15-45), lag 6, rows [6, 250)
         {
           const int lo = max(F - BH - 2, 8), hi = min(F - 2, TS - 8);
-          constexpr int per_row = (TS - 16) / 2;
+          constexpr int per_row = 128;  // site slots per row: one pass of 1024 threads over 8 rows
           for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
-            const int rr = lo + k / per_row;
-            const int cc = 8 + gae(pattern, rr) + 2 * (k % per_row);
+            const int rr = lo + (k >> 7);
+            const int cc = 8 + (g0 ^ (rr & 1)) + 2 * (k & 127);
+            if (cc >= TS - 8) continue;
             const int j = cc >> 1, jm = (cc - 1) >> 1, jp = (cc + 1) >> 1;
             const unsigned char* nm2 = nyq.row(rr - 2);
             const unsigned char* nm1 = nyq.row(rr - 1);
@@ -543,16 +617,16 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
         }
         {
           const int lo = max(F - BH - 6, 6), hi = min(F - 6, TS - 6);
-          constexpr int per_row = (TS - 12 + 1) / 2;
+          constexpr int per_row = 128;  // site slots per row: one pass of 1024 threads over 8 rows
           for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
-            const int rr = lo + k / per_row;
-            const int cc = 6 + 2 * (k % per_row);
+            const int rr = lo + (k >> 7);
+            const int cc = 6 + 2 * (k & 127);
             if (cc >= TS - 6) continue;
             const float* up = cfa.row(rr - 1);
             const float* mid = cfa.row(rr);
             const float* down = cfa.row(rr + 1);
             const int j = cc >> 1;
-            if (gae(pattern, rr) == 0) {
+            if ((g0 ^ (rr & 1)) == 0) {
               delp.row(rr)[j] = fabsf(up[cc + 1] - down[cc - 1]);
               delm.row(rr)[j] = fabsf(down[cc + 1] - up[cc - 1]);
               const float g = mid[cc + 1];
@@ -568,15 +642,20 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
           }
         }
         __syncthreads();
+        // -- warps 2-31: area interpolation and diagonal estimates (lag 8); warps 0-1:
+        //    the row recurrences of populate_green's hvwt (nyquist.rs:176-222) and
+        //    combine_diagonals' pmwt (diagonal.rs:150-171) one step behind (lag 17),
+        //    so they read rows finished in the step before and overlap the others.
+        if (warp >= 2) {
         // -- area interpolation at refined Nyquist sites (nyquist.rs:132-170), lag 8
-        {
-          const int lo = max(F - BH - 8, 8), hi = min(F - 8, TS - 8);
-          constexpr int per_row = (TS - 16) / 2;
-          for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
-            const int rr = lo + k / per_row;
-            const int cc = 8 + gae(pattern, rr) + 2 * (k % per_row);
-            if (nyq2.row(rr)[cc >> 1] == 0) continue;
-            float sumcfa = 0.0f, sumh = 0.0f, sumv = 0.0f, sumsqh = 0.0f, sumsqv = 0.0f, areawt = 0.0f;
+          {
+            const int lo = max(F - BH - 8, 8), hi = min(F - 8, TS - 8);
+            constexpr int per_row = (TS - 16) / 2;
+            for (int k = t - 64; k < (hi - lo) * per_row; k += THREADS - 64) {
+              const int rr = lo + k / per_row;
+              const int cc = 8 + (g0 ^ (rr & 1)) + 2 * (k % per_row);
+              if (nyq2.row(rr)[cc >> 1] == 0) continue;
+              float sumcfa = 0.0f, sumh = 0.0f, sumv = 0.0f, sumsqh = 0.0f, sumsqv = 0.0f, areawt = 0.0f;
             for (int di = -6; di < 7; di += 2) {
               const int r1 = rr + di;
               // Refined flags outside [8, 248) were never set: zero.
@@ -598,118 +677,80 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
               }
             }
             sumh = sumcfa - 0.5f * sumh;
-            sumv = sumcfa - 0.5f * sumv;
-            areawt *= 0.5f;
-            const float hcdvar = EPSSQ + fabsf(areawt * sumsqh - sumh * sumh);
-            const float vcdvar = EPSSQ + fabsf(areawt * sumsqv - sumv * sumv);
-            hv.row(rr)[cc >> 1] = hcdvar / (vcdvar + hcdvar);
+              sumv = sumcfa - 0.5f * sumv;
+              areawt *= 0.5f;
+              const float hcdvar = EPSSQ + fabsf(areawt * sumsqh - sumh * sumh);
+              const float vcdvar = EPSSQ + fabsf(areawt * sumsqv - sumv * sumv);
+              hv.row(rr)[cc >> 1] = hcdvar / (vcdvar + hcdvar);
+            }
           }
-        }
-        // -- diagonal_estimates (diagonal.rs:99-145), lag 8, red/blue sites of [8, 248)^2
-        {
-          const int lo = max(F - BH - 8, 8), hi = min(F - 8, TS - 8);
-          constexpr int per_row = (TS - 16) / 2;
-          for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
-            const int rr = lo + k / per_row;
-            const int cc = 8 + gae(pattern, rr) + 2 * (k % per_row);
-            const int j = cc >> 1;
-            const float* cm2 = cfa.row(rr - 2);
-            const float* cm1 = cfa.row(rr - 1);
-            const float* c0 = cfa.row(rr);
-            const float* cp1 = cfa.row(rr + 1);
-            const float* cp2 = cfa.row(rr + 2);
-            const float centre = c0[cc];
-            const float se1 = cp1[cc + 1], se2 = cp2[cc + 2];
-            const float nw1 = cm1[cc - 1], nw2 = cm2[cc - 2];
-            const float ne1 = cm1[cc + 1], ne2 = cm2[cc + 2];
-            const float sw1 = cp1[cc - 1], sw2 = cp2[cc - 2];
-            const float rbse = diagonal_estimate(centre, se1, se2);
-            const float rbnw = diagonal_estimate(centre, nw1, nw2);
-            const float rbne = diagonal_estimate(centre, ne1, ne2);
-            const float rbsw = diagonal_estimate(centre, sw1, sw2);
-            const float wtse = EPS + delm.row(rr)[j] + delm.row(rr + 1)[(cc + 1) >> 1] + delm.row(rr + 2)[(cc + 2) >> 1];
-            const float wtnw = EPS + delm.row(rr)[j] + delm.row(rr - 1)[(cc - 1) >> 1] + delm.row(rr - 2)[(cc - 2) >> 1];
-            const float wtne = EPS + delp.row(rr)[j] + delp.row(rr - 1)[(cc + 1) >> 1] + delp.row(rr - 2)[(cc + 2) >> 1];
-            const float wtsw = EPS + delp.row(rr)[j] + delp.row(rr + 1)[(cc - 1) >> 1] + delp.row(rr + 2)[(cc - 2) >> 1];
-            const float rbm_est = (wtse * rbnw + wtnw * rbse) / (wtse + wtnw);
-            const float rbp_est = (wtne * rbsw + wtsw * rbne) / (wtne + wtsw);
-            const float* qm0 = sqm.row(rr - 2);
-            const float* qm1 = sqm.row(rr - 1);
-            const float* qm2 = sqm.row(rr);
-            const float* qm3 = sqm.row(rr + 1);
-            const float* qm4 = sqm.row(rr + 2);
-            const float em = GAUSSEVEN[0] * (qm1[cc >> 1] + qm2[(cc - 1) >> 1] + qm2[(cc + 1) >> 1] + qm3[cc >> 1]) +
-                             GAUSSEVEN[1] * (qm0[(cc - 1) >> 1] + qm0[(cc + 1) >> 1] + qm1[(cc - 2) >> 1] +
-                                             qm1[(cc + 2) >> 1] + qm3[(cc - 2) >> 1] + qm3[(cc + 2) >> 1] +
-                                             qm4[(cc - 1) >> 1] + qm4[(cc + 1) >> 1]);
-            const float* qp0 = sqp.row(rr - 2);
-            const float* qp1 = sqp.row(rr - 1);
-            const float* qp2 = sqp.row(rr);
-            const float* qp3 = sqp.row(rr + 1);
-            const float* qp4 = sqp.row(rr + 2);
-            const float ep = GAUSSEVEN[0] * (qp1[cc >> 1] + qp2[(cc - 1) >> 1] + qp2[(cc + 1) >> 1] + qp3[cc >> 1]) +
-                             GAUSSEVEN[1] * (qp0[(cc - 1) >> 1] + qp0[(cc + 1) >> 1] + qp1[(cc - 2) >> 1] +
-                                             qp1[(cc + 2) >> 1] + qp3[(cc - 2) >> 1] + qp3[(cc + 2) >> 1] +
-                                             qp4[(cc - 1) >> 1] + qp4[(cc + 1) >> 1]);
-            const float rbvarm = EPSSQ + em;
-            pmwt.row(rr)[j] = rbvarm / ((EPSSQ + ep) + rbvarm);
-            rbp.row(rr)[j] = bound_diagonal(rbp_est, centre, sw1, ne1, clip_pt);
-            rbm.row(rr)[j] = bound_diagonal(rbm_est, centre, nw1, se1, clip_pt);
+          // -- diagonal_estimates (diagonal.rs:99-145), lag 8, red/blue sites of [8, 248)^2
+          {
+            const int lo = max(F - BH - 8, 8), hi = min(F - 8, TS - 8);
+            constexpr int per_row = (TS - 16) / 2;
+            for (int k = t - 64; k < (hi - lo) * per_row; k += THREADS - 64) {
+              const int rr = lo + k / per_row;
+              const int cc = 8 + (g0 ^ (rr & 1)) + 2 * (k % per_row);
+              const int j = cc >> 1;
+              const float* cm2 = cfa.row(rr - 2);
+              const float* cm1 = cfa.row(rr - 1);
+              const float* c0 = cfa.row(rr);
+              const float* cp1 = cfa.row(rr + 1);
+              const float* cp2 = cfa.row(rr + 2);
+              const float centre = c0[cc];
+              const float se1 = cp1[cc + 1], se2 = cp2[cc + 2];
+              const float nw1 = cm1[cc - 1], nw2 = cm2[cc - 2];
+              const float ne1 = cm1[cc + 1], ne2 = cm2[cc + 2];
+              const float sw1 = cp1[cc - 1], sw2 = cp2[cc - 2];
+              const float rbse = diagonal_estimate(centre, se1, se2);
+              const float rbnw = diagonal_estimate(centre, nw1, nw2);
+              const float rbne = diagonal_estimate(centre, ne1, ne2);
+              const float rbsw = diagonal_estimate(centre, sw1, sw2);
+              const float wtse = EPS + delm.row(rr)[j] + delm.row(rr + 1)[(cc + 1) >> 1] + delm.row(rr + 2)[(cc + 2) >> 1];
+              const float wtnw = EPS + delm.row(rr)[j] + delm.row(rr - 1)[(cc - 1) >> 1] + delm.row(rr - 2)[(cc - 2) >> 1];
+              const float wtne = EPS + delp.row(rr)[j] + delp.row(rr - 1)[(cc + 1) >> 1] + delp.row(rr - 2)[(cc + 2) >> 1];
+              const float wtsw = EPS + delp.row(rr)[j] + delp.row(rr + 1)[(cc - 1) >> 1] + delp.row(rr + 2)[(cc - 2) >> 1];
+              const float rbm_est = (wtse * rbnw + wtnw * rbse) / (wtse + wtnw);
+              const float rbp_est = (wtne * rbsw + wtsw * rbne) / (wtne + wtsw);
+              const float* qm0 = sqm.row(rr - 2);
+              const float* qm1 = sqm.row(rr - 1);
+              const float* qm2 = sqm.row(rr);
+              const float* qm3 = sqm.row(rr + 1);
+              const float* qm4 = sqm.row(rr + 2);
+              const float em = GAUSSEVEN[0] * (qm1[cc >> 1] + qm2[(cc - 1) >> 1] + qm2[(cc + 1) >> 1] + qm3[cc >> 1]) +
+                               GAUSSEVEN[1] * (qm0[(cc - 1) >> 1] + qm0[(cc + 1) >> 1] + qm1[(cc - 2) >> 1] +
+                                               qm1[(cc + 2) >> 1] + qm3[(cc - 2) >> 1] + qm3[(cc + 2) >> 1] +
+                                               qm4[(cc - 1) >> 1] + qm4[(cc + 1) >> 1]);
+              const float* qp0 = sqp.row(rr - 2);
+              const float* qp1 = sqp.row(rr - 1);
+              const float* qp2 = sqp.row(rr);
+              const float* qp3 = sqp.row(rr + 1);
+              const float* qp4 = sqp.row(rr + 2);
+              const float ep = GAUSSEVEN[0] * (qp1[cc >> 1] + qp2[(cc - 1) >> 1] + qp2[(cc + 1) >> 1] + qp3[cc >> 1]) +
+                               GAUSSEVEN[1] * (qp0[(cc - 1) >> 1] + qp0[(cc + 1) >> 1] + qp1[(cc - 2) >> 1] +
+                                               qp1[(cc + 2) >> 1] + qp3[(cc - 2) >> 1] + qp3[(cc + 2) >> 1] +
+                                               qp4[(cc - 1) >> 1] + qp4[(cc + 1) >> 1]);
+              const float rbvarm = EPSSQ + em;
+              pmwt.row(rr)[j] = rbvarm / ((EPSSQ + ep) + rbvarm);
+              rbp.row(rr)[j] = bound_diagonal(rbp_est, centre, sw1, ne1, clip_pt);
+              rbm.row(rr)[j] = bound_diagonal(rbm_est, centre, nw1, se1, clip_pt);
+            }
           }
+        } else if (warp == 0) {
+          recurrence_rows<8>(hv, max(F - BH - 17, 8), min(F - 17, TS - 8), g0, lane, hv_up);
+        } else {
+          recurrence_rows<10>(pmwt, max(F - BH - 17, 10), min(F - 17, TS - 10), g0, lane, pm_up);
         }
         __syncthreads();
-        // -- row recurrences, lag 9: populate_green's hvwt update (nyquist.rs:176-222) on
-        //    warp 0, combine_diagonals' pmwt update (diagonal.rs:150-171) on warp 1.
-        if (warp == 0) {
-          const int lo = max(F - BH - 9, 8), hi = min(F - 9, TS - 8);
-          constexpr int sites = (TS - 16) / 2;
-          for (int rr = lo; rr < hi; ++rr) {
-            const int g = gae(pattern, rr);
-            const float* up = hv.row(rr - 1);
-            const float* down = hv.row(rr + 1);
-            float* cur = hv.row(rr);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              const int k = lane + 32 * q;
-              if (k < sites) {
-                const int cc = 8 + g + 2 * k;
-                const float alt = (up[(cc - 1) >> 1] + up[(cc + 1) >> 1] + down[(cc - 1) >> 1] + down[(cc + 1) >> 1]) / 4.0f;
-                float* p = &cur[cc >> 1];
-                if (fabsf(0.5f - *p) < fabsf(0.5f - alt)) *p = alt;
-              }
-            }
-            __syncwarp();
-          }
-        } else if (warp == 1) {
-          const int lo = max(F - BH - 9, 10), hi = min(F - 9, TS - 10);
-          constexpr int sites = (TS - 20) / 2;
-          for (int rr = lo; rr < hi; ++rr) {
-            const int g = gae(pattern, rr);
-            const float* up = pmwt.row(rr - 1);
-            const float* down = pmwt.row(rr + 1);
-            float* cur = pmwt.row(rr);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              const int k = lane + 32 * q;
-              if (k < sites) {
-                const int cc = 10 + g + 2 * k;
-                const float alt = (up[(cc - 1) >> 1] + up[(cc + 1) >> 1] + down[(cc - 1) >> 1] + down[(cc + 1) >> 1]) / 4.0f;
-                float* p = &cur[cc >> 1];
-                if (fabsf(0.5f - *p) < fabsf(0.5f - alt)) *p = alt;
-              }
-            }
-            __syncwarp();
-          }
-        }
-        __syncthreads();
-        // -- per-site products of populate_green (lag 9, [8, 248)^2) and the R+B
-        //    interpolation of combine_diagonals (lag 9, [10, 246)^2)
+        // -- per-site products of populate_green (lag 17, [8, 248)^2) and the R+B
+        //    interpolation of combine_diagonals (lag 17, [10, 246)^2)
         {
-          const int lo = max(F - BH - 9, 8), hi = min(F - 9, TS - 8);
-          constexpr int per_row = (TS - 16) / 2;
+          const int lo = max(F - BH - 17, 8), hi = min(F - 17, TS - 8);
+          constexpr int per_row = 128;  // site slots per row: one pass of 1024 threads over 8 rows
           for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
-            const int rr = lo + k / per_row;
-            const int cc = 8 + gae(pattern, rr) + 2 * (k % per_row);
+            const int rr = lo + (k >> 7);
+            const int cc = 8 + (g0 ^ (rr & 1)) + 2 * (k & 127);
+            if (cc >= TS - 8) continue;
             const int j = cc >> 1;
             const float* c0 = cfa.row(rr);
             const float dg = intp(hv.row(rr)[j], vrb.row(rr)[j], hrb.row(rr)[j]);
@@ -722,24 +763,26 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
           }
         }
         {
-          const int lo = max(F - BH - 9, 10), hi = min(F - 9, TS - 10);
-          constexpr int per_row = (TS - 20) / 2;
+          const int lo = max(F - BH - 17, 10), hi = min(F - 17, TS - 10);
+          constexpr int per_row = 128;  // site slots per row: one pass of 1024 threads over 8 rows
           for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
-            const int rr = lo + k / per_row;
-            const int cc = 10 + gae(pattern, rr) + 2 * (k % per_row);
+            const int rr = lo + (k >> 7);
+            const int cc = 10 + (g0 ^ (rr & 1)) + 2 * (k & 127);
+            if (cc >= TS - 10) continue;
             const int j = cc >> 1;
             const float p = pmwt.row(rr)[j];
             rbint.row(rr)[j] = 0.5f * (cfa.row(rr)[cc] + rbm.row(rr)[j] * (1.0f - p) + rbp.row(rr)[j] * p);
           }
         }
         __syncthreads();
-        // -- refine_green (nyquist.rs:225-236), lag 11, refined Nyquist sites
+        // -- refine_green (nyquist.rs:225-236), lag 19, refined Nyquist sites
         {
-          const int lo = max(F - BH - 11, 8), hi = min(F - 11, TS - 8);
-          constexpr int per_row = (TS - 16) / 2;
+          const int lo = max(F - BH - 19, 8), hi = min(F - 19, TS - 8);
+          constexpr int per_row = 128;  // site slots per row: one pass of 1024 threads over 8 rows
           for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
-            const int rr = lo + k / per_row;
-            const int cc = 8 + gae(pattern, rr) + 2 * (k % per_row);
+            const int rr = lo + (k >> 7);
+            const int cc = 8 + (g0 ^ (rr & 1)) + 2 * (k & 127);
+            if (cc >= TS - 8) continue;
             const int j = cc >> 1;
             if (nyq2.row(rr)[j] == 0) continue;
             // d2h / d2v rows outside [8, 248) were never written: zero.
@@ -770,13 +813,14 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
         }
         __syncthreads();
         // -- refine_green_with_rb (diagonal.rs:205-247) and the move of blue-row
-        //    differences to dgrb1 (chroma.rs:23-44), lag 11, [12, 244)^2
+        //    differences to dgrb1 (chroma.rs:23-44), lag 19, [12, 244)^2
         {
-          const int lo = max(F - BH - 11, 12), hi = min(F - 11, TS - 12);
-          constexpr int per_row = (TS - 24) / 2;
+          const int lo = max(F - BH - 19, 12), hi = min(F - 19, TS - 12);
+          constexpr int per_row = 128;  // site slots per row: one pass of 1024 threads over 8 rows
           for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
-            const int rr = lo + k / per_row;
-            const int cc = 12 + gae(pattern, rr) + 2 * (k % per_row);
+            const int rr = lo + (k >> 7);
+            const int cc = 12 + (g0 ^ (rr & 1)) + 2 * (k & 127);
+            if (cc >= TS - 12) continue;
             const int j = cc >> 1;
             const float pm = pmwt.row(rr)[j];
             const float hvv = hv.row(rr)[j];
@@ -816,16 +860,18 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
           }
         }
         __syncthreads();
-        // -- interpolate_chroma (chroma.rs:46-91), lag 14, [14, 242)^2: reads and
+        // -- interpolate_chroma (chroma.rs:46-91), lag 22, [14, 242)^2: reads and
         //    writes of each plane fall on different rows
         {
-          const int lo = max(F - BH - 14, 14), hi = min(F - 14, TS - 14);
-          constexpr int per_row = (TS - 28) / 2;
+          const int lo = max(F - BH - 22, 14), hi = min(F - 22, TS - 14);
+          constexpr int per_row = 128;  // site slots per row: one pass of 1024 threads over 8 rows
           for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
-            const int rr = lo + k / per_row;
-            const int start = 14 + gae(pattern, rr);
-            const int cc = start + 2 * (k % per_row);
-            const Ring<16, TSH>& p = (1 - fc(pattern, rr, start) / 2) == 0 ? dgrb0 : dgrb1;
+            const int rr = lo + (k >> 7);
+            const int start = 14 + (g0 ^ (rr & 1));
+            const int cc = start + 2 * (k & 127);
+            if (cc >= TS - 14) continue;
+            // A blue site interpolates the red difference (dgrb0), a red site the blue one.
+            const Ring<16, TSH>& p = (rr & 1) == blue_par ? dgrb0 : dgrb1;
             auto d = [&](int dr, int dc) { return p.row(rr + dr)[(cc + dc) >> 1]; };
             const float wtnw = 1.0f / (EPS + fabsf(d(-1, -1) - d(1, 1)) + fabsf(d(-1, -1) - d(-3, -3)) + fabsf(d(1, 1) - d(-3, -3)));
             const float wtne = 1.0f / (EPS + fabsf(d(-1, 1) - d(1, -1)) + fabsf(d(-1, 1) - d(-3, 3)) + fabsf(d(1, -1) - d(-3, 3)));
@@ -840,18 +886,19 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
           }
         }
         __syncthreads();
-        // -- finish_planes (chroma.rs:98-147) + write_tile (mod.rs:196-268), lag 15, core rows
+        // -- finish_planes (chroma.rs:98-147) + write_tile (mod.rs:196-268), lag 23, core rows
         {
-          const int lo = max(F - BH - 15, BORDER), hi = min(F - 15, TS - BORDER);
-          for (int k = t; k < (hi - lo) * VALID; k += THREADS) {
-            const int ly = lo - BORDER + k / VALID, lx = k % VALID;
+          const int lo = max(F - BH - 23, BORDER), hi = min(F - 23, TS - BORDER);
+          for (int k = t; k < (hi - lo) * TS; k += THREADS) {
+            const int ly = lo - BORDER + (k >> 8), lx = k & (TS - 1);
+            if (lx >= VALID) continue;
             const int gx = ox + lx, gy = oy + ly;
             if (gx >= W || gy >= H) continue;
             const int rr = ly + BORDER, cc = lx + BORDER;
             const float sample = cfa.row(rr)[cc];  // in-image core sample, not mirrored
-            const int ch = color_at(pattern, gx, gy);
+            const int ch = (ctab >> (2 * (((gy & 1) << 1) | (gx & 1)))) & 3;
             float r, b, gv;
-            if (fc(pattern, rr, cc) == 1) {
+            if ((cc & 1) != (g0 ^ (rr & 1))) {  // green site
               gv = sample;
               const float* hvr = hv.row(rr);
               const float up = hv.row(rr - 1)[cc >> 1], down = hv.row(rr + 1)[cc >> 1];

@@ -101,8 +101,8 @@ __device__ __forceinline__ float hblur(const float* row, int qx, int x, int W, i
 // ---- one RL iteration, streamed down column strips --------------------------
 // A CTA owns a strip of SW = 128 - 2R output columns and a segment of rows and
 // walks the segment top to bottom in steps of BH rows:
-//   * estimate and guide rows arrive by cp.async one step ahead into 32-row
-//     rings;
+//   * estimate rows arrive by cp.async one step ahead into a 24-row ring
+//     (the guide is read from L2 where it is used);
 //   * the horizontal pass of blur #1 runs on every arriving row; the vertical
 //     pass and the ratio run R rows behind, the horizontal pass of blur #2 on
 //     the same rows, and the vertical pass of blur #2 with the bounded update
@@ -121,7 +121,7 @@ struct StreamGeom {
   static constexpr int QW = 128;         // columns [x0 - R, x0 + SW + R): one per thread
   static constexpr int SW = QW - 2 * R;  // output columns of a strip
   static constexpr int EW = QW + 2 * R;  // estimate columns [x0 - 2R, x0 + SW + 2R)
-  static constexpr int BH = 8, RIN = 32, RS = 16;
+  static constexpr int BH = 8, RIN = 24, RS = 16;  // RIN >= 2 BH + 2R: rows in use plus rows in flight
   static constexpr int H1_RUNS = 15, H1_RUN = (QW + H1_RUNS - 1) / H1_RUNS;
   static constexpr int H2_RUN = 8, H2_RUNS = (SW + H2_RUN - 1) / H2_RUN;
 };
@@ -130,7 +130,6 @@ template <int R>
 struct StreamSmem {
   using G = StreamGeom<R>;
   float e[G::RIN][G::EW];   // estimate rows
-  float g[G::RIN][G::QW];   // guide rows (in-image columns)
   float t1[G::RS][G::QW];   // horizontal pass of blur #1
   float q[G::BH][G::QW];    // ratio rows of the current step
   float t2[G::RS][G::QW];   // horizontal pass of blur #2 (first SW columns)
@@ -151,6 +150,20 @@ template <int R, int RUN>
 __device__ __forceinline__ void hrun(const float* __restrict__ row, int c0, int n, float* __restrict__ out, int x0img,
                                      int W, const float (&w)[2 * R + 1]) {
   constexpr int T = 2 * R + 1;
+  if (n == RUN && x0img >= R && x0img + RUN <= W - R) {
+    // Whole run of interior columns: every sum starts at +0.0.
+    float win[RUN + 2 * R];
+#pragma unroll
+    for (int k = 0; k < RUN + 2 * R; ++k) win[k] = row[c0 - R + k];
+#pragma unroll
+    for (int j = 0; j < RUN; ++j) {
+      float v = 0.0f;
+#pragma unroll
+      for (int k = 0; k < T; ++k) v += win[j + k] * w[k];
+      out[j] = v;
+    }
+    return;
+  }
   float win[RUN + 2 * R];
 #pragma unroll
   for (int k = 0; k < RUN + 2 * R; ++k) win[k] = (k < n + 2 * R) ? row[c0 - R + k] : 0.0f;
@@ -185,18 +198,21 @@ __global__ void __launch_bounds__(128) rl_stream_kernel(const float* __restrict_
     const int e_end = min(y1 + 2 * R, H), q_end = min(y1 + R, H);
     int e_next = max(y0 - 2 * R, 0), q_next = max(y0 - R, 0), o_next = y0;
     const bool edge = x0 - 2 * R < 0 || x0 + SW + 2 * R > W;
-    // Estimate and guide rows [r0, r1) into the input rings.
+    // Estimate rows [r0, r1) into the input ring: this thread copies window
+    // columns tid and tid + 128 (mirrored into the image).
+    const int xa = x0 - 2 * R + tid, xb = xa + 128;
+    const int sxa = (unsigned)xa < (unsigned)W ? xa : mirror_half(xa, W);
+    const bool has_b = tid + 128 < EW;
+    const int sxb = has_b ? ((unsigned)xb < (unsigned)W ? xb : mirror_half(xb, W)) : 0;
     auto issue = [&](int r0, int r1) {
-      for (int k = tid; k < (r1 - r0) * EW; k += 128) {
-        const int r = r0 + k / EW, c = k - (k / EW) * EW;
-        const int x = x0 - 2 * R + c;
-        const int sx = (unsigned)x < (unsigned)W ? x : mirror_half(x, W);
-        cp_async4(&S.e[r & (G::RIN - 1)][c], est_in + (long long)r * W + sx);
-      }
-      for (int k = tid; k < (r1 - r0) * QW; k += 128) {
-        const int r = r0 + (k >> 7), c = k & (QW - 1);
-        const int x = x0 - R + c;
-        if ((unsigned)x < (unsigned)W) cp_async4(&S.g[r & (G::RIN - 1)][c], guide + (long long)r * W + x);
+      int slot = r0 % G::RIN;
+      const float* src = est_in + (long long)r0 * W;
+      for (int r = r0; r < r1; ++r) {
+        float* dst = S.e[slot];
+        cp_async4(dst + tid, src + sxa);
+        if (has_b) cp_async4(dst + tid + 128, src + sxb);
+        src += W;
+        slot = slot + 1 == G::RIN ? 0 : slot + 1;
       }
     };
     issue(e_next, min(e_next + BH, e_end));
@@ -212,7 +228,7 @@ __global__ void __launch_bounds__(128) rl_stream_kernel(const float* __restrict_
         const int r = e_next + k / G::H1_RUNS, s = k % G::H1_RUNS;
         const int qc0 = s * G::H1_RUN;
         const int n = min(G::H1_RUN, QW - qc0);
-        if (n > 0) hrun<R, G::H1_RUN>(S.e[r & (G::RIN - 1)], qc0 + R, n, S.t1[r & (G::RS - 1)] + qc0, x0 - R + qc0, W, w);
+        if (n > 0) hrun<R, G::H1_RUN>(S.e[r % G::RIN], qc0 + R, n, S.t1[r & (G::RS - 1)] + qc0, x0 - R + qc0, W, w);
       }
       const int q_avail = e_hi >= H ? q_end : e_hi - R;
       const int q_hi = max(q_next, min(min(q_next + BH, q_end), q_avail));
@@ -222,17 +238,19 @@ __global__ void __launch_bounds__(128) rl_stream_kernel(const float* __restrict_
         const int x = x0 - R + tid, n = q_hi - q_next;
         if (n > 0 && (unsigned)x < (unsigned)W) {
           float win[BH + 2 * R];
+          const bool inside = n == BH && q_next - R >= 0 && q_next + BH + R <= H;  // no mirrored rows
 #pragma unroll
           for (int j = 0; j < BH + 2 * R; ++j)
-            win[j] = j < n + 2 * R ? S.t1[mirror_row(q_next - R + j, H) & (G::RS - 1)][tid] : 0.0f;
+            win[j] = inside ? S.t1[(q_next - R + j) & (G::RS - 1)][tid]
+                            : (j < n + 2 * R ? S.t1[mirror_row(q_next - R + j, H) & (G::RS - 1)][tid] : 0.0f);
+          const float* gp = guide + (long long)q_next * W + x;
 #pragma unroll
           for (int j = 0; j < BH; ++j) {
             if (j < n) {
               float b = 0.0f;
 #pragma unroll
               for (int t = 0; t < T; ++t) b += win[j + t] * w[t];
-              const int y = q_next + j;
-              S.q[y & (BH - 1)][tid] = S.g[y & (G::RIN - 1)][tid] / rmax(b, FLOOR);
+              S.q[(q_next + j) & (BH - 1)][tid] = __ldg(gp + (long long)j * W) / rmax(b, FLOOR);
             }
           }
         }
@@ -262,22 +280,27 @@ __global__ void __launch_bounds__(128) rl_stream_kernel(const float* __restrict_
         const int x = x0 + tid, n = o_hi - o_next;
         if (tid < SW && x < W && n > 0) {
           float win[BH + 2 * R];
+          const bool inside = n == BH && o_next - R >= 0 && o_next + BH + R <= H;  // no mirrored rows
 #pragma unroll
           for (int j = 0; j < BH + 2 * R; ++j)
-            win[j] = j < n + 2 * R ? S.t2[mirror_row(o_next - R + j, H) & (G::RS - 1)][tid] : 0.0f;
+            win[j] = inside ? S.t2[(o_next - R + j) & (G::RS - 1)][tid]
+                            : (j < n + 2 * R ? S.t2[mirror_row(o_next - R + j, H) & (G::RS - 1)][tid] : 0.0f);
+          const long long o0 = (long long)o_next * W + x;
+          const int es = o_next % G::RIN;
 #pragma unroll
           for (int j = 0; j < BH; ++j) {
             if (j < n) {
               float b = 0.0f;
 #pragma unroll
               for (int t = 0; t < T; ++t) b += win[j + t] * w[t];
-              const int y = o_next + j;
-              const float g = S.g[y & (G::RIN - 1)][tid + R];
-              float e = S.e[y & (G::RIN - 1)][tid + 2 * R] * b;
+              const long long o = o0 + (long long)j * W;
+              const float g = __ldg(guide + o);
+              const int slot = es + j < G::RIN ? es + j : es + j - G::RIN;
+              float e = S.e[slot][tid + 2 * R] * b;
               const float lo = g * 0.5f, hi = g * 2.0f;
               if (e < lo) e = lo;
               if (e > hi) e = hi;
-              est_out[(long long)y * W + x] = e;
+              est_out[o] = e;
             }
           }
         }

@@ -151,15 +151,21 @@ __device__ __forceinline__ df df_div(df x, df y) {
   const float q2 = r.h / y.h;
   return fast_two_sum(q1, q2);
 }
-// Nearest f32 of the double-float value; `amb` is set when the value lies
-// within a relative 2^-40 of a rounding midpoint.
+// Nearest f32 of a normalised double-float value (|l| <= ulp(h)/2). The
+// rounding midpoints next to h sit at h +- ulp(h)/2, so `amb` is set when |l|
+// lies within a relative 2^-40 of ulp(h)/2, and also whenever the gaps around
+// h are uneven or tiny (h a power of two, zero, subnormal-adjacent or not
+// finite); the caller then takes the f64 path.
 __device__ __forceinline__ float df_round(df v, bool& amb) {
   const float r = v.h + v.l;
-  const float d = (v.h - r) + v.l;
-  const float up = (nextafterf(r, INFINITY) - r) * 0.5f;
-  const float dn = (r - nextafterf(r, -INFINITY)) * 0.5f;
-  const float room = d >= 0.0f ? up - d : dn + d;
-  if (!(room > fabsf(r) * 9.094947e-13f)) amb = true;  // 2^-40
+  const unsigned bits = __float_as_uint(v.h) & 0x7fffffffu;
+  const unsigned expo = bits >> 23;
+  if (expo <= 25u || expo == 255u || (bits & 0x7fffffu) == 0u) {
+    amb = true;
+    return r;
+  }
+  const float half_ulp = __uint_as_float((expo - 24u) << 23);
+  if (!(fabsf(fabsf(v.l) - half_ulp) > fabsf(v.h) * 9.094947e-13f)) amb = true;  // 2^-40
   return r;
 }
 
