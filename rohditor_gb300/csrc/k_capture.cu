@@ -219,6 +219,25 @@ __global__ void __launch_bounds__(128) rl_stream_kernel(const float* __restrict_
     cp_async_commit();
     while (o_next < y1) {
       const int e_hi = min(e_next + BH, e_end);
+      // Rows each later stage of this step will produce (availability of their inputs).
+      const int q_avail = e_hi >= H ? q_end : e_hi - R;
+      const int q_hi = max(q_next, min(min(q_next + BH, q_end), q_avail));
+      const int o_avail = q_hi >= H ? y1 : q_hi - R;
+      const int o_hi = max(o_next, min(min(o_next + BH, y1), o_avail));
+      // Guide values of those rows, loaded now so their latency overlaps the copy wait
+      // and the horizontal pass.
+      float gq[BH], go[BH];
+      {
+        const int xq = x0 - R + tid, xo = x0 + tid;
+        const bool okq = (unsigned)xq < (unsigned)W, oko = tid < SW && xo < W;
+        const float* pq = guide + (long long)q_next * W + xq;
+        const float* po = guide + (long long)o_next * W + xo;
+#pragma unroll
+        for (int j = 0; j < BH; ++j) {
+          gq[j] = okq && j < q_hi - q_next ? __ldg(pq + (long long)j * W) : 0.0f;
+          go[j] = oko && j < o_hi - o_next ? __ldg(po + (long long)j * W) : 0.0f;
+        }
+      }
       issue(e_hi, min(e_hi + BH, e_end));
       cp_async_commit();
       cp_async_wait1();
@@ -230,8 +249,6 @@ __global__ void __launch_bounds__(128) rl_stream_kernel(const float* __restrict_
         const int n = min(G::H1_RUN, QW - qc0);
         if (n > 0) hrun<R, G::H1_RUN>(S.e[r % G::RIN], qc0 + R, n, S.t1[r & (G::RS - 1)] + qc0, x0 - R + qc0, W, w);
       }
-      const int q_avail = e_hi >= H ? q_end : e_hi - R;
-      const int q_hi = max(q_next, min(min(q_next + BH, q_end), q_avail));
       __syncthreads();
       // 2. vertical pass of blur #1 and the ratio on rows [q_next, q_hi), column tid
       {
@@ -243,14 +260,13 @@ __global__ void __launch_bounds__(128) rl_stream_kernel(const float* __restrict_
           for (int j = 0; j < BH + 2 * R; ++j)
             win[j] = inside ? S.t1[(q_next - R + j) & (G::RS - 1)][tid]
                             : (j < n + 2 * R ? S.t1[mirror_row(q_next - R + j, H) & (G::RS - 1)][tid] : 0.0f);
-          const float* gp = guide + (long long)q_next * W + x;
 #pragma unroll
           for (int j = 0; j < BH; ++j) {
             if (j < n) {
               float b = 0.0f;
 #pragma unroll
               for (int t = 0; t < T; ++t) b += win[j + t] * w[t];
-              S.q[(q_next + j) & (BH - 1)][tid] = __ldg(gp + (long long)j * W) / rmax(b, FLOOR);
+              S.q[(q_next + j) & (BH - 1)][tid] = gq[j] / rmax(b, FLOOR);
             }
           }
         }
@@ -272,8 +288,6 @@ __global__ void __launch_bounds__(128) rl_stream_kernel(const float* __restrict_
         const int n = min(min(G::H2_RUN, SW - c0), W - (x0 + c0));
         if (n > 0) hrun<R, G::H2_RUN>(S.q[r & (BH - 1)], c0 + R, n, S.t2[r & (G::RS - 1)] + c0, x0 + c0, W, w);
       }
-      const int o_avail = q_hi >= H ? y1 : q_hi - R;
-      const int o_hi = max(o_next, min(min(o_next + BH, y1), o_avail));
       __syncthreads();
       // 4. vertical pass of blur #2 and the bounded update on rows [o_next, o_hi)
       {
@@ -294,7 +308,7 @@ __global__ void __launch_bounds__(128) rl_stream_kernel(const float* __restrict_
 #pragma unroll
               for (int t = 0; t < T; ++t) b += win[j + t] * w[t];
               const long long o = o0 + (long long)j * W;
-              const float g = __ldg(guide + o);
+              const float g = go[j];
               const int slot = es + j < G::RIN ? es + j : es + j - G::RIN;
               float e = S.e[slot][tid + 2 * R] * b;
               const float lo = g * 0.5f, hi = g * 2.0f;

@@ -354,12 +354,26 @@ __global__ void __launch_bounds__(256) rcd_kernel(const MosaicSource src, float 
 
 // Normalize (+ Clip) into an f32 mosaic: the input of Opposed and of the
 // stage entry point. Each sample is visited once, so Clip statistics are exact.
-__global__ void normalize_kernel(const MosaicSource src, float* out, int count_clip, unsigned long long* clip_stats) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+// Four consecutive samples of a row per thread (one 16-byte store when aligned).
+constexpr int NPX = 4;
+
+__global__ void __launch_bounds__(256) normalize_kernel(const MosaicSource src, float* out, int count_clip,
+                                                        unsigned long long* clip_stats) {
+  const int x0 = (blockIdx.x * blockDim.x + threadIdx.x) * NPX, y = blockIdx.y;
   ClipTally tally;
-  if (x < src.width) {
-    out[(long long)y * src.width + x] = source_linear(src, x, y);
-    if (count_clip) tally.add(src, x, y);
+  if (x0 < src.width) {
+    const int n = min(NPX, src.width - x0);
+    float v[NPX];
+#pragma unroll
+    for (int j = 0; j < NPX; ++j) v[j] = j < n ? source_linear(src, x0 + j, y) : 0.0f;
+    float* o = out + (long long)y * src.width + x0;
+    if (n == NPX && (reinterpret_cast<uintptr_t>(o) & 15) == 0) {
+      *reinterpret_cast<float4*>(o) = make_float4(v[0], v[1], v[2], v[3]);
+    } else {
+      for (int j = 0; j < n; ++j) o[j] = v[j];
+    }
+    if (count_clip)
+      for (int j = 0; j < n; ++j) tally.add(src, x0 + j, y);
   }
   if (count_clip) tally.flush(clip_stats);
 }
@@ -367,7 +381,7 @@ __global__ void normalize_kernel(const MosaicSource src, float* out, int count_c
 }  // namespace
 
 Status launch_normalize(Context& ctx, const MosaicSource& src, float* out, unsigned long long* clip_stats) {
-  dim3 grid((src.width + 255) / 256, src.height);
+  dim3 grid((src.width + 256 * NPX - 1) / (256 * NPX), src.height);
   RD_LAUNCH(ctx, K_NORMALIZE, normalize_kernel<<<grid, 256, 0, ctx.stream>>>(src, out, src.clip, clip_stats));
   RD_CUDA_TRY(cudaGetLastError());
   return Status{};
