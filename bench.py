@@ -320,7 +320,128 @@ def run_ours(args, world, rank, local, pg):
     lib.rd_host_free(h_out)
     dev.check(lib.rd_device_free(h, ctypes.c_void_p(d_mosaic)))
     dev.close()
+    if rank == 0 and not args.no_edit_latency:
+        line["edit_latency"] = edit_latency(args)
     return line
+
+
+def edit_latency(args, images: int = 16, seconds: float = 2.0, rate: float = 200.0, develop_share: float = 0.1,
+                 seed: int = 4) -> dict:
+    """Preview edit latency, served vs plain, on one seeded Poisson trace.
+
+    `images` 24 MP images are open; requests arrive at `rate` per second for
+    `seconds`; a share are full re-develops (jittered capture amount), the rest
+    preview edits of a resident base (jittered exposure, tone curve and HSL),
+    with per-image increasing revisions. Served: the trace is submitted to the
+    served loop (rd_server_*), latency = submit -> result with the sRGB8 image
+    and histogram on the host. Plain: the same trace run in arrival order, one
+    request at a time, through rd_develop/rd_spatial/rd_render on one context
+    (each edit a synchronous render of its image's current base).
+    """
+    from rohditor_gb300 import (CaptureContract, Device, GpuPreviewProcessor, GpuSensorProcessor,
+                                GpuSpatialProcessor)
+    from rohditor_gb300.served import EDIT, PreviewServer
+    from rohditor_gb300.workloads import full_24mp, hsl_bands, sixteen_knot_curve
+
+    wl = full_24mp(demosaic=args.demosaic, iterations=args.iterations, highlight=args.highlight,
+                   width=args.width, height=args.height)
+    dev = Device(0)
+    lib = dev.lib
+    mosaics = []
+    for i in range(images):
+        w = full_24mp(demosaic=args.demosaic, iterations=args.iterations, highlight=args.highlight, seed=100 + i,
+                      width=args.width, height=args.height)
+        host = np.empty((w.height, w.width), dtype=np.uint16)
+        d = w.synth_desc()
+        dev.check(lib.rd_synth_mosaic(dev.handle, ctypes.byref(d),
+                                      host.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16))))
+        mosaics.append(host)
+    rng = np.random.default_rng(seed)
+    trace = []
+    t = 0.0
+    revision = [0] * images
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= seconds:
+            break
+        img = int(rng.integers(images))
+        revision[img] += 1
+        if rng.random() < develop_share:
+            cap = CaptureContract(amount=float(rng.uniform(0.3, 0.7)), radius=wl.capture.radius,
+                                  noise_protection=wl.capture.noise_protection, ceilings=wl.capture.ceilings,
+                                  iterations=wl.capture.iterations)
+            trace.append((t, 1, img, revision[img], cap))
+        else:
+            c = wl.color
+            color = type(c)(wb_gains=c.wb_gains, camera_to_rec2020=c.camera_to_rec2020,
+                            exposure_ev=float(0.5 + rng.uniform(-0.3, 0.3)), base_lut=c.base_lut,
+                            tone_lut=sixteen_knot_curve(seed=int(rng.integers(1 << 30))),
+                            hsl=hsl_bands(seed=int(rng.integers(1 << 30))))
+            trace.append((t, 0, img, revision[img], color))
+
+    def pct(v):
+        v = np.asarray(v, dtype=np.float64)
+        if v.size == 0:
+            return {"p50_ms": None, "p99_ms": None, "n": 0}
+        return {"p50_ms": round(float(np.percentile(v, 50)), 3), "p99_ms": round(float(np.percentile(v, 99)), 3),
+                "mean_ms": round(float(v.mean()), 3), "n": int(v.size)}
+
+    # Served.
+    server = PreviewServer(0)
+    for i in range(images):
+        server.open(i, mosaics[i], wl.sensor, wl.capture, wl.optics, wl.target, wl.color.wb_gains,
+                    wl.color.camera_to_rec2020)
+    server.drain(120000)
+    server.poll(4096)
+    colors = [item[4].to_c() if item[1] == 0 else None for item in trace]
+    t0 = time.perf_counter()
+    for k, (ts, kind, img, rev, payload) in enumerate(trace):
+        while time.perf_counter() - t0 < ts:
+            time.sleep(0.0002)
+        if kind == 0:
+            server.submit_edit(img, rev, colors[k])
+        else:
+            server.submit_develop(img, rev, payload, wl.optics)
+    server.drain(120000)
+    res = server.poll(1 << 16)
+    stats = server.stats()
+    server.close()
+    served_edits = [r["latency_ms"] for r in res if r["kind"] == EDIT and r["status"] == 0]
+    served_dev = [r["latency_ms"] for r in res if r["kind"] != EDIT and r["status"] == 0]
+
+    # Plain: one request at a time in arrival order.
+    sensor_p, spatial_p, preview_p = GpuSensorProcessor(dev), GpuSpatialProcessor(dev), GpuPreviewProcessor(dev)
+    bases = []
+    for i in range(images):
+        src = sensor_p.develop(mosaics[i], wl.sensor, wl.capture)
+        bases.append(spatial_p.reduce_preview(src, wl.optics, wl.target, wl.color.wb_gains,
+                                              wl.color.camera_to_rec2020))
+        src.release()
+    plain_edits, plain_dev = [], []
+    t0 = time.perf_counter()
+    for ts, kind, img, rev, payload in trace:
+        while time.perf_counter() - t0 < ts:
+            time.sleep(0.0002)
+        if kind == 0:
+            preview_p.render(bases[img], payload)
+            plain_edits.append(1e3 * (time.perf_counter() - t0 - ts))
+        else:
+            src = sensor_p.develop(mosaics[img], wl.sensor, payload)
+            base = spatial_p.reduce_preview(src, wl.optics, wl.target, wl.color.wb_gains, wl.color.camera_to_rec2020)
+            src.release()
+            bases[img].release()
+            bases[img] = base
+            plain_dev.append(1e3 * (time.perf_counter() - t0 - ts))
+    for b in bases:
+        b.release()
+    dev.close()
+    return {
+        "trace": {"images": images, "image": f"{wl.width}x{wl.height}", "seconds": seconds, "rate_per_s": rate,
+                  "develop_share": develop_share, "requests": len(trace), "seed": seed},
+        "served": {"edit": pct(served_edits), "develop": pct(served_dev), "coalesced": stats["coalesced"],
+                   "batches": stats["batches"], "batched_edits": stats["batched_edits"]},
+        "plain": {"edit": pct(plain_edits), "develop": pct(plain_dev)},
+    }
 
 
 def cpu_develop_band(rows: int, args) -> tuple[float, float]:
@@ -411,6 +532,7 @@ def main():
     p.add_argument("--width", type=int, default=6048, help="mosaic width (smaller cases for profiling)")
     p.add_argument("--height", type=int, default=4024)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-edit-latency", action="store_true", help="skip the served-vs-plain edit latency trace")
     p.add_argument("--cpu-baseline-rows", type=int, default=2048,
                    help="band height of the CPU baseline sample (2048 rows = half a 24 MP develop)")
     args = p.parse_args()

@@ -236,6 +236,54 @@ rd_status rd_optics_plan(rd_optics_desc* optics, float crop_factor, float real_f
 /* BaseRenderingLut::standard_v1 (crates/core/src/rendering.rs:36-50). */
 void rd_standard_base_lut(float* lut4096);
 
+/* ---- served preview loop ----
+ * Replaces the engine's preview worker and caches
+ * (crates/engine/src/coordinator/scheduler.rs:44-180 newest-wins mailbox,
+ * coordinator/worker.rs:1597-1703 develop_preview, preview_cache/spatial.rs:475-600,
+ * crates/gpu/src/memory.rs:44-60 reservations) for many open images on one GPU:
+ * images stay resident (decoded mosaic, 2560-px Rec.2020 base, render outputs),
+ * requests are newest-wins per image by (revision, submission order), pending
+ * edits of all images render in one batched launch ahead of develops, and the
+ * least recently used images lose their layers when the budget is reached.
+ * A worker thread serves requests; results are polled. Device < 0 creates a
+ * dry server that models service times without a GPU (policy tests). */
+typedef struct rd_server rd_server;
+typedef struct rd_server_result {
+  uint64_t request_id;
+  uint32_t image_id;
+  int32_t kind;      /* 0 edit (render), 1 develop */
+  int32_t status;    /* rd_status; RD_CANCELLED: replaced by a newer request or closed */
+  uint32_t batch_size;
+  uint64_t revision;
+  double queue_ms, service_ms, latency_ms;  /* submit->start, start->done, submit->done */
+} rd_server_result;
+typedef struct rd_server_stats {
+  uint64_t requested, completed, coalesced, failed, redeveloped, evictions, batches, batched_edits;
+  uint64_t resident_bytes, peak_resident_bytes, budget_bytes;
+} rd_server_stats;
+rd_status rd_server_create(int device, uint64_t budget_bytes, rd_server** out);
+/* Dry servers only: modelled develop and render times. */
+rd_status rd_server_set_dry_timing(rd_server* server, uint32_t develop_us, uint32_t render_us);
+void rd_server_destroy(rd_server* server);
+/* Copies the mosaic and the contracts; queues the first develop (revision 0). */
+rd_status rd_server_open(rd_server* server, uint32_t image_id, const uint16_t* mosaic, size_t row_stride,
+                         const rd_sensor_desc* sensor, const rd_detail_desc* detail, const rd_optics_desc* optics,
+                         uint32_t target_width, uint32_t target_height, const float wb_gains[3],
+                         const float camera_to_rec2020[9], uint64_t* request_id);
+rd_status rd_server_close_image(rd_server* server, uint32_t image_id);
+rd_status rd_server_submit_edit(rd_server* server, uint32_t image_id, uint64_t revision, const rd_color_desc* color,
+                                uint64_t* request_id);
+rd_status rd_server_submit_develop(rd_server* server, uint32_t image_id, uint64_t revision,
+                                   const rd_detail_desc* detail, const rd_optics_desc* optics, uint64_t* request_id);
+/* Up to max_results completed requests (waiting up to wait_ms for the first); returns the count. */
+int32_t rd_server_poll(rd_server* server, rd_server_result* out, int32_t max_results, int32_t wait_ms);
+/* The latest rendered output of an image: sRGB8 [h][3w], 1024 histogram bins, its revision. */
+rd_status rd_server_read_output(rd_server* server, uint32_t image_id, uint8_t* srgb, uint64_t* hist,
+                                uint64_t* revision);
+rd_status rd_server_get_stats(rd_server* server, rd_server_stats* out);
+/* Waits up to wait_ms until no request is pending or running. */
+rd_status rd_server_drain(rd_server* server, int32_t wait_ms);
+
 /* ---- synthetic scene generator (seeded, counter-based; identical on CPU and GPU) ---- */
 typedef struct rd_synth_desc {
   uint32_t width, height;

@@ -103,6 +103,20 @@ class SynthDesc(ctypes.Structure):
     ]
 
 
+class ServerResult(ctypes.Structure):
+    _fields_ = [
+        ("request_id", ctypes.c_uint64), ("image_id", ctypes.c_uint32), ("kind", ctypes.c_int32),
+        ("status", ctypes.c_int32), ("batch_size", ctypes.c_uint32), ("revision", ctypes.c_uint64),
+        ("queue_ms", ctypes.c_double), ("service_ms", ctypes.c_double), ("latency_ms", ctypes.c_double),
+    ]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_uint64) for name in (
+        "requested", "completed", "coalesced", "failed", "redeveloped", "evictions", "batches", "batched_edits",
+        "resident_bytes", "peak_resident_bytes", "budget_bytes")]
+
+
 # Every exported symbol of include/rd_gpu.h with its ctypes signature.
 SIGNATURES = {
     "rd_status_is_routing": (ctypes.c_int, [ctypes.c_int]),
@@ -148,6 +162,20 @@ SIGNATURES = {
                                       ctypes.c_float]),
     "rd_standard_base_lut": (None, [F32P]),
     "rd_synth_mosaic_device": (ctypes.c_int, [VOIDP, ctypes.POINTER(SynthDesc), VOIDP]),
+    "rd_server_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(VOIDP)]),
+    "rd_server_set_dry_timing": (ctypes.c_int, [VOIDP, ctypes.c_uint32, ctypes.c_uint32]),
+    "rd_server_destroy": (None, [VOIDP]),
+    "rd_server_open": (ctypes.c_int, [VOIDP, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint16), ctypes.c_size_t,
+                                      ctypes.POINTER(SensorDesc), ctypes.POINTER(DetailDesc),
+                                      ctypes.POINTER(OpticsDesc), ctypes.c_uint32, ctypes.c_uint32, F32P, F32P, U64P]),
+    "rd_server_close_image": (ctypes.c_int, [VOIDP, ctypes.c_uint32]),
+    "rd_server_submit_edit": (ctypes.c_int, [VOIDP, ctypes.c_uint32, ctypes.c_uint64, ctypes.POINTER(ColorDesc), U64P]),
+    "rd_server_submit_develop": (ctypes.c_int, [VOIDP, ctypes.c_uint32, ctypes.c_uint64, ctypes.POINTER(DetailDesc),
+                                                ctypes.POINTER(OpticsDesc), U64P]),
+    "rd_server_poll": (ctypes.c_int32, [VOIDP, ctypes.POINTER(ServerResult), ctypes.c_int32, ctypes.c_int32]),
+    "rd_server_read_output": (ctypes.c_int, [VOIDP, ctypes.c_uint32, U8P, U64P, U64P]),
+    "rd_server_get_stats": (ctypes.c_int, [VOIDP, ctypes.POINTER(ServerStats)]),
+    "rd_server_drain": (ctypes.c_int, [VOIDP, ctypes.c_int32]),
     "rd_synth_mosaic": (ctypes.c_int, [VOIDP, ctypes.POINTER(SynthDesc), U16P]),
     "rd_ctx_event_record": (ctypes.c_int, [VOIDP, ctypes.c_int]),
     "rd_ctx_event_elapsed": (ctypes.c_int, [VOIDP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),

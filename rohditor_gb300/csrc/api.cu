@@ -14,24 +14,7 @@
 
 #include "rd_internal.cuh"
 
-struct rd_ctx {
-  rd::Context c;
-};
-struct rd_source {
-  rd_ctx* ctx;
-  float* rgb;  // planar camera-native RGB
-  int W, H;
-  size_t bytes;
-};
-struct rd_base {
-  rd_ctx* ctx;
-  float* rgb;  // planar linear Rec.2020 RGB
-  int W, H;
-  size_t bytes;
-  uint8_t* d_srgb;             // device output of rd_render_device
-  unsigned long long* d_hist;  // 1024 bins
-  size_t out_bytes;
-};
+#include "rd_handles.cuh"
 
 namespace rd {
 
@@ -110,6 +93,20 @@ void resolve_kernel_timing(Context& ctx) {
 }
 
 // Reads and clears the kernels' error word; one synchronization point per call.
+// Recreates the context's stream at the device's highest (or lowest) priority;
+// the stream must be idle.
+Status set_stream_priority(Context& c, bool high) {
+  int least = 0, greatest = 0;
+  RD_CUDA_TRY(cudaSetDevice(c.device));
+  RD_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+  RD_CUDA_TRY(cudaStreamSynchronize(c.stream));
+  cudaStream_t s = nullptr;
+  RD_CUDA_TRY(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, high ? greatest : least));
+  cudaStreamDestroy(c.stream);
+  c.stream = s;
+  return Status{};
+}
+
 Status check_kernel_error(Context& ctx, const char* stage) {
   uint32_t word = 0;
   RD_CUDA_TRY(cudaMemcpyAsync(&word, ctx.d_error, sizeof(word), cudaMemcpyDeviceToHost, ctx.stream));
@@ -520,6 +517,7 @@ rd_status rd_ctx_create(int device, uint64_t budget_bytes, rd_ctx** out) {
   *out = h;
   return RD_OK;
 }
+
 
 void rd_ctx_destroy(rd_ctx* h) {
   if (!h) return;

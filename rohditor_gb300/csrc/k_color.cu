@@ -18,6 +18,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <mutex>
 
 #include "rd_internal.cuh"
@@ -236,72 +237,103 @@ struct ColorParams {
   unsigned long long* hist;  // 1024 bins
 };
 
+// The adjustment chain, output transform, sRGB8 quantisation and histogram
+// bins of one base pixel (index i of a plane of `plane` pixels).
+__device__ __forceinline__ void color_pixel(const ColorParams& p, long long i, long long plane, unsigned int* bins) {
+  float v[3] = {p.in[i], p.in[plane + i], p.in[2 * plane + i]};
+  if (p.camera_native) {
+    v[0] *= p.wb[0];
+    v[1] *= p.wb[1];
+    v[2] *= p.wb[2];
+    const float a = v[0], b = v[1], c = v[2];
+    v[0] = p.m[0] * a + p.m[1] * b + p.m[2] * c;
+    v[1] = p.m[3] * a + p.m[4] * b + p.m[5] * c;
+    v[2] = p.m[6] * a + p.m[7] * b + p.m[8] * c;
+  }
+  if (p.has_exposure) {
+    v[0] *= p.exposure_gain;
+    v[1] *= p.exposure_gain;
+    v[2] *= p.exposure_gain;
+  }
+  if (p.base_lut) {
+    const float cur = luminance(v);
+    const float tgt = base_sample(p.base_lut, cur);
+    if (isfinite(tgt) && fabsf(tgt - cur) > F32_EPS) luminance_delta(v, cur, tgt);
+  }
+  if (p.tone_lut) {
+    const float cur = luminance(v);
+    const float tgt = lut_sample(p.tone_lut, cur);
+    if (isfinite(tgt) && fabsf(tgt - cur) > F32_EPS) luminance_delta(v, cur, tgt);
+  }
+  if (p.has_sat) {
+    const float lum = luminance(v);
+    float chroma = 0.0f;
+    for (int c = 0; c < 3; ++c) chroma = rmax(chroma, fabsf(v[c] - lum));
+    const float cs = rclamp(chroma / rmax(fabsf(lum), 1.0e-6f), 0.0f, 1.0f);
+    const float sat = p.saturation * (1.0f + p.vibrance * (1.0f - cs));
+    if (fabsf(sat - 1.0f) > F32_EPS)
+      for (int c = 0; c < 3; ++c) v[c] = lum + sat * (v[c] - lum);
+  }
+  if (p.has_hsl) apply_hsl(v, p.hsl);
+  if (p.has_grading) apply_grading(v, p.grading);
+  unsigned char q[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    float lin = p.out_m[3 * r] * v[0] + p.out_m[3 * r + 1] * v[1] + p.out_m[3 * r + 2] * v[2];
+    if (isnan(lin) || lin == -INFINITY) lin = 0.0f;
+    else if (lin == INFINITY) lin = 1.0f;
+    else lin = rclamp(lin, 0.0f, 1.0f);
+    const float enc = lin <= 0.0031308f ? 12.92f * lin : 1.055f * powf(lin, 1.0f / 2.4f) - 0.055f;
+    // (encoded * 255 + dither).round().clamp(0, 255) with DitherMode::None.
+    q[r] = (unsigned char)rclamp(roundf(enc * 255.0f + 0.0f), 0.0f, 255.0f);
+  }
+  const long long y = i / p.W, x = i % p.W;
+  unsigned char* o = p.out + y * 3 * p.W + 3 * x;
+  o[0] = q[0];
+  o[1] = q[1];
+  o[2] = q[2];
+  atomicAdd(&bins[q[0]], 1u);
+  atomicAdd(&bins[256 + q[1]], 1u);
+  atomicAdd(&bins[512 + q[2]], 1u);
+  atomicAdd(&bins[768 + (2126u * q[0] + 7152u * q[1] + 722u * q[2] + 5000u) / 10000u], 1u);
+}
+
 __global__ void __launch_bounds__(256) color_kernel(const ColorParams p) {
   __shared__ unsigned int bins[1024];
   for (int k = threadIdx.x; k < 1024; k += blockDim.x) bins[k] = 0;
   __syncthreads();
   const long long plane = (long long)p.W * p.H;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < plane; i += (long long)gridDim.x * blockDim.x) {
-    float v[3] = {p.in[i], p.in[plane + i], p.in[2 * plane + i]};
-    if (p.camera_native) {
-      v[0] *= p.wb[0];
-      v[1] *= p.wb[1];
-      v[2] *= p.wb[2];
-      const float a = v[0], b = v[1], c = v[2];
-      v[0] = p.m[0] * a + p.m[1] * b + p.m[2] * c;
-      v[1] = p.m[3] * a + p.m[4] * b + p.m[5] * c;
-      v[2] = p.m[6] * a + p.m[7] * b + p.m[8] * c;
-    }
-    if (p.has_exposure) {
-      v[0] *= p.exposure_gain;
-      v[1] *= p.exposure_gain;
-      v[2] *= p.exposure_gain;
-    }
-    if (p.base_lut) {
-      const float cur = luminance(v);
-      const float tgt = base_sample(p.base_lut, cur);
-      if (isfinite(tgt) && fabsf(tgt - cur) > F32_EPS) luminance_delta(v, cur, tgt);
-    }
-    if (p.tone_lut) {
-      const float cur = luminance(v);
-      const float tgt = lut_sample(p.tone_lut, cur);
-      if (isfinite(tgt) && fabsf(tgt - cur) > F32_EPS) luminance_delta(v, cur, tgt);
-    }
-    if (p.has_sat) {
-      const float lum = luminance(v);
-      float chroma = 0.0f;
-      for (int c = 0; c < 3; ++c) chroma = rmax(chroma, fabsf(v[c] - lum));
-      const float cs = rclamp(chroma / rmax(fabsf(lum), 1.0e-6f), 0.0f, 1.0f);
-      const float sat = p.saturation * (1.0f + p.vibrance * (1.0f - cs));
-      if (fabsf(sat - 1.0f) > F32_EPS)
-        for (int c = 0; c < 3; ++c) v[c] = lum + sat * (v[c] - lum);
-    }
-    if (p.has_hsl) apply_hsl(v, p.hsl);
-    if (p.has_grading) apply_grading(v, p.grading);
-    unsigned char q[3];
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-      float lin = p.out_m[3 * r] * v[0] + p.out_m[3 * r + 1] * v[1] + p.out_m[3 * r + 2] * v[2];
-      if (isnan(lin) || lin == -INFINITY) lin = 0.0f;
-      else if (lin == INFINITY) lin = 1.0f;
-      else lin = rclamp(lin, 0.0f, 1.0f);
-      const float enc = lin <= 0.0031308f ? 12.92f * lin : 1.055f * powf(lin, 1.0f / 2.4f) - 0.055f;
-      // (encoded * 255 + dither).round().clamp(0, 255) with DitherMode::None.
-      q[r] = (unsigned char)rclamp(roundf(enc * 255.0f + 0.0f), 0.0f, 255.0f);
-    }
-    const long long y = i / p.W, x = i % p.W;
-    unsigned char* o = p.out + y * 3 * p.W + 3 * x;
-    o[0] = q[0];
-    o[1] = q[1];
-    o[2] = q[2];
-    atomicAdd(&bins[q[0]], 1u);
-    atomicAdd(&bins[256 + q[1]], 1u);
-    atomicAdd(&bins[512 + q[2]], 1u);
-    atomicAdd(&bins[768 + (2126u * q[0] + 7152u * q[1] + 722u * q[2] + 5000u) / 10000u], 1u);
-  }
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < plane; i += (long long)gridDim.x * blockDim.x)
+    color_pixel(p, i, plane, bins);
   __syncthreads();
   for (int k = threadIdx.x; k < 1024; k += blockDim.x)
     if (bins[k]) atomicAdd(&p.hist[k], (unsigned long long)bins[k]);
+}
+
+// Several bases in one launch: blocks [block_start[k], block_start[k+1]) render
+// image k with params[k]; each block stages its image's parameters in shared
+// memory and flushes its histogram to that image's bins.
+__global__ void __launch_bounds__(256) color_batch_kernel(const ColorParams* __restrict__ params,
+                                                          const int* __restrict__ block_start, int n) {
+  __shared__ unsigned int bins[1024];
+  __shared__ ColorParams sp;
+  const int b = blockIdx.x;
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (block_start[mid] <= b) lo = mid;
+    else hi = mid;
+  }
+  if (threadIdx.x == 0) sp = params[lo];
+  for (int k = threadIdx.x; k < 1024; k += blockDim.x) bins[k] = 0;
+  __syncthreads();
+  const long long plane = (long long)sp.W * sp.H;
+  const int first = block_start[lo], nb = block_start[lo + 1] - first;
+  for (long long i = (long long)(b - first) * blockDim.x + threadIdx.x; i < plane; i += (long long)nb * blockDim.x)
+    color_pixel(sp, i, plane, bins);
+  __syncthreads();
+  for (int k = threadIdx.x; k < 1024; k += blockDim.x)
+    if (bins[k]) atomicAdd(&sp.hist[k], (unsigned long long)bins[k]);
 }
 
 __global__ void wb_matrix_kernel(float* rgb, long long plane, float g0, float g1, float g2, float m0, float m1, float m2,
@@ -383,6 +415,81 @@ Status run_color_output(Context& ctx, const float* rgb, int W, int H, const rd_c
   const cudaError_t launch = cudaGetLastError();
   if (luts) device_free(ctx, luts, lut_bytes);
   if (launch != cudaSuccess) return Status{RD_SYNCHRONIZATION, cudaGetErrorString(launch)};
+  return Status{};
+}
+
+}  // namespace rd
+
+// ---- several bases in one launch ---------------------------------------------
+namespace rd {
+namespace {
+
+// Adjustment parameters of a non-camera-native render (the base already holds
+// white-balanced Rec.2020); buffers and LUT pointers are filled by the caller.
+ColorParams base_color_params(const rd_color_desc& c) {
+  ColorParams p{};
+  p.camera_native = 0;
+  p.has_exposure = c.exposure_ev != 0.0f;
+  p.exposure_gain = std::exp2(c.exposure_ev);
+  p.has_sat = std::fabs(c.saturation - 1.0f) > F32_EPS || c.vibrance != 0.0f;
+  p.saturation = c.saturation;
+  p.vibrance = c.vibrance;
+  p.has_hsl = c.has_hsl;
+  for (int k = 0; k < 8; ++k)
+    for (int j = 0; j < 3; ++j) p.hsl[k][j] = c.hsl[k][j];
+  p.has_grading = c.has_grading;
+  for (int k = 0; k < 3; ++k)
+    for (int j = 0; j < 3; ++j) p.grading[k][j] = c.grading[k][j];
+  rec2020_to_srgb(p.out_m);
+  return p;
+}
+
+constexpr int BATCH_PIXELS_PER_THREAD = 16;
+
+size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+}  // namespace
+
+size_t color_batch_staging_bytes(int n) {
+  return align256(sizeof(ColorParams) * n) + align256(sizeof(int) * (n + 1)) + sizeof(float) * 8192 * (size_t)n;
+}
+
+Status run_color_batch(Context& ctx, const ColorBatchItem* items, int n, void* d_staging, void* h_staging) {
+  if (n <= 0) return Status{};
+  unsigned char* hb = static_cast<unsigned char*>(h_staging);
+  unsigned char* db = static_cast<unsigned char*>(d_staging);
+  ColorParams* hp = reinterpret_cast<ColorParams*>(hb);
+  const size_t off_starts = align256(sizeof(ColorParams) * n);
+  const size_t off_luts = off_starts + align256(sizeof(int) * (n + 1));
+  int* hs = reinterpret_cast<int*>(hb + off_starts);
+  float* hl = reinterpret_cast<float*>(hb + off_luts);
+  float* dl = reinterpret_cast<float*>(db + off_luts);
+  int blocks = 0;
+  for (int k = 0; k < n; ++k) {
+    const ColorBatchItem& it = items[k];
+    ColorParams p = base_color_params(*it.color);
+    p.in = it.rgb;
+    p.W = it.width;
+    p.H = it.height;
+    p.out = it.srgb;
+    p.hist = it.hist;
+    float* lut = hl + (size_t)8192 * k;
+    if (it.color->has_base_lut) std::memcpy(lut, it.color->base_lut, sizeof(float) * 4096);
+    if (it.color->has_tone_lut) std::memcpy(lut + 4096, it.color->tone_lut, sizeof(float) * 4096);
+    p.base_lut = it.color->has_base_lut ? dl + (size_t)8192 * k : nullptr;
+    p.tone_lut = it.color->has_tone_lut ? dl + (size_t)8192 * k + 4096 : nullptr;
+    hp[k] = p;
+    hs[k] = blocks;
+    const long long pixels = (long long)it.width * it.height;
+    blocks += (int)((pixels + 256LL * BATCH_PIXELS_PER_THREAD - 1) / (256LL * BATCH_PIXELS_PER_THREAD));
+  }
+  hs[n] = blocks;
+  RD_CUDA_TRY(cudaMemcpyAsync(d_staging, h_staging, color_batch_staging_bytes(n), cudaMemcpyHostToDevice, ctx.stream));
+  for (int k = 0; k < n; ++k)
+    RD_CUDA_TRY(cudaMemsetAsync(items[k].hist, 0, 1024 * sizeof(unsigned long long), ctx.stream));
+  RD_LAUNCH(ctx, K_COLOR, color_batch_kernel<<<blocks, 256, 0, ctx.stream>>>(
+                              reinterpret_cast<const ColorParams*>(db), reinterpret_cast<const int*>(db + off_starts), n));
+  RD_CUDA_TRY(cudaGetLastError());
   return Status{};
 }
 

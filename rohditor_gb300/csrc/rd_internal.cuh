@@ -97,6 +97,7 @@ void release(Context& ctx, size_t bytes);
 Status device_alloc(Context& ctx, size_t bytes, void** out);
 void device_free(Context& ctx, void* ptr, size_t bytes);
 Status check_kernel_error(Context& ctx, const char* stage);
+Status set_stream_priority(Context& ctx, bool high);
 
 // ------------------------------------------------------------------ mosaic source
 // Per-sample view of the (cropped, normalized, highlight-processed) mosaic,
@@ -203,6 +204,18 @@ Status run_wb_matrix(Context& ctx, float* rgb, size_t pixels, const float gains[
 Status run_color_output(Context& ctx, const float* rgb, int width, int height, const rd_color_desc& color,
                         bool camera_native, uint8_t* srgb, unsigned long long* d_hist);
 Status run_synth(Context& ctx, const rd_synth_desc& desc, uint16_t* out);
+// One launch rendering several bases (render path of the served loop). The
+// staging buffers (host pinned and device, color_batch_staging_bytes(n) each)
+// carry the per-image parameters and LUTs.
+struct ColorBatchItem {
+  const float* rgb;  // planar Rec.2020 base
+  int width, height;
+  const rd_color_desc* color;
+  uint8_t* srgb;              // device [height][3 width]
+  unsigned long long* hist;   // device 1024 bins, cleared by the call
+};
+size_t color_batch_staging_bytes(int n);
+Status run_color_batch(Context& ctx, const ColorBatchItem* items, int n, void* d_staging, void* h_staging);
 
 // Host contract helpers.
 int gaussian_kernel(float sigma, float* weights, int max_taps);

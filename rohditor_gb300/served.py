@@ -1,0 +1,107 @@
+"""Served preview loop (the engine's preview worker and caches on the GPU).
+
+`PreviewServer` wraps the C ABI's `rd_server_*` entry points
+(include/rd_gpu.h), which replace crates/engine/src/coordinator/scheduler.rs
+(newest-wins mailbox), coordinator/worker.rs (develop_preview) and the preview
+caches for many open images: images stay resident, edits are newest-wins per
+image and render in cross-image batches ahead of develops, and the least
+recently used images lose their device layers when the budget is reached.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _ffi
+from .processor import (CaptureContract, ColorContract, GpuPreviewError, OpticsExecution, SensorDescription, _f32,
+                        _ptr)
+
+EDIT, DEVELOP = 0, 1
+
+
+class PreviewServer:
+    """A served loop on GPU `device`, or a dry server (device < 0) that models
+    develop and render times on the host, for tests of the policy."""
+
+    def __init__(self, device: int = 0, budget_bytes: int = 0):
+        self.lib = _ffi.load()
+        h = ctypes.c_void_p()
+        rc = self.lib.rd_server_create(device, budget_bytes, ctypes.byref(h))
+        if rc != 0:
+            raise GpuPreviewError(rc, f"could not create a preview server on device {device}")
+        self.handle = h
+        self._sizes: dict[int, tuple[int, int]] = {}
+
+    @classmethod
+    def dry(cls, budget_bytes: int = 0, develop_us: int = 2000, render_us: int = 200) -> "PreviewServer":
+        s = cls(-1, budget_bytes)
+        s._check(s.lib.rd_server_set_dry_timing(s.handle, develop_us, render_us))
+        return s
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise GpuPreviewError(rc, self.lib.rd_status_name(rc).decode())
+
+    def open(self, image_id: int, mosaic: np.ndarray, sensor: SensorDescription, capture: CaptureContract,
+             optics: OpticsExecution, target: tuple[int, int], wb_gains, camera_to_rec2020) -> int:
+        mosaic = np.ascontiguousarray(mosaic, dtype=np.uint16)
+        wb = _f32(wb_gains)
+        cam = _f32(camera_to_rec2020)
+        rid = ctypes.c_uint64()
+        s, d, o = sensor.to_c(), capture.to_c(), optics.to_c()
+        self._check(self.lib.rd_server_open(self.handle, image_id, _ptr(mosaic, ctypes.c_uint16), mosaic.shape[1],
+                                            ctypes.byref(s), ctypes.byref(d), ctypes.byref(o), target[0], target[1],
+                                            _ptr(wb, ctypes.c_float), _ptr(cam, ctypes.c_float), ctypes.byref(rid)))
+        self._sizes[image_id] = target
+        return int(rid.value)
+
+    def close_image(self, image_id: int):
+        self._check(self.lib.rd_server_close_image(self.handle, image_id))
+
+    def submit_edit(self, image_id: int, revision: int, color: ColorContract | _ffi.ColorDesc) -> int:
+        c = color if isinstance(color, _ffi.ColorDesc) else color.to_c()
+        rid = ctypes.c_uint64()
+        self._check(self.lib.rd_server_submit_edit(self.handle, image_id, revision, ctypes.byref(c), ctypes.byref(rid)))
+        return int(rid.value)
+
+    def submit_develop(self, image_id: int, revision: int, capture: CaptureContract, optics: OpticsExecution) -> int:
+        d, o = capture.to_c(), optics.to_c()
+        rid = ctypes.c_uint64()
+        self._check(self.lib.rd_server_submit_develop(self.handle, image_id, revision, ctypes.byref(d),
+                                                      ctypes.byref(o), ctypes.byref(rid)))
+        return int(rid.value)
+
+    def poll(self, max_results: int = 256, wait_ms: int = 0) -> list[dict]:
+        buf = (_ffi.ServerResult * max_results)()
+        n = self.lib.rd_server_poll(self.handle, buf, max_results, wait_ms)
+        return [{f: getattr(buf[i], f) for f, _ in _ffi.ServerResult._fields_} for i in range(n)]
+
+    def read_output(self, image_id: int) -> tuple[np.ndarray, np.ndarray, int]:
+        w, h = self._sizes[image_id]
+        out = np.empty((h, 3 * w), dtype=np.uint8)
+        hist = np.zeros(1024, dtype=np.uint64)
+        rev = ctypes.c_uint64()
+        self._check(self.lib.rd_server_read_output(self.handle, image_id, _ptr(out, ctypes.c_uint8),
+                                                   _ptr(hist, ctypes.c_uint64), ctypes.byref(rev)))
+        return out, hist, int(rev.value)
+
+    def stats(self) -> dict:
+        st = _ffi.ServerStats()
+        self._check(self.lib.rd_server_get_stats(self.handle, ctypes.byref(st)))
+        return {f: int(getattr(st, f)) for f, _ in _ffi.ServerStats._fields_}
+
+    def drain(self, wait_ms: int = 60000):
+        self._check(self.lib.rd_server_drain(self.handle, wait_ms))
+
+    def close(self):
+        if self.handle:
+            self.lib.rd_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
