@@ -133,8 +133,9 @@ class ClockSampler:
 # (dram__bytes_read.sum + dram__bytes_write.sum); the traffic grows with the pixel count, so the
 # bench workload's traffic is this figure times its pixels.
 MEASURED_TRAFFIC_BPP = {
-    "amaze": (27.1, "profiles/amaze_kernel_4096x3072.md"),
-    "rl_iteration": (10.0, "profiles/rl_stream_kernel_4096x3072.md"),
+    "amaze": (26.8, "profiles/amaze_kernel_4096x3072.md"),
+    "rl_iteration": (4.5, "profiles/rl_stream_kernel_4096x3072.md"),
+    "rl_mask": (17.6, "profiles/rl_prep_kernel_4096x3072.md"),
     "optics_gather": (24.9, "profiles/optics_kernel_4096x3072.md"),
 }
 
@@ -144,8 +145,7 @@ def family_bytes(name: str, N: int, n: int, H: int, tw: int) -> float | None:
     table = {
         "amaze": 14.0 * N,          # u16 mosaic in, planar f32 RGB out
         "rl_iteration": 12.0 * N,   # estimate in, guide in, estimate out
-        "rl_mask": 12.0 * N,
-        "rl_init": 24.0 * N,
+        "rl_mask": 20.0 * N,        # guide + mask preparation: RGB in, guide + refined mask out
         "rl_apply": 36.0 * N,
         "vignetting": 4.0 * N,
         "optics_gather": 28.0 * N,  # RGB + multiplier in, RGB out

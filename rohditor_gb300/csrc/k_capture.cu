@@ -3,9 +3,11 @@
 // sm_103a.
 //
 // Data layout: planar RGB plus four full-resolution f32 planes (guide, mask,
-// and a ping-pong pair for the estimate). Kernels:
-//   rl_init      guide = max(sum max(c,0)/3, 1e-6), mask = 1 - smoothstep(peak)
-//   rl_mask      blur(mask) and blur(guide) on one tile, refines the mask
+// and a ping-pong pair for the estimate; the guide is the first estimate).
+// Kernels:
+//   rl_prep      guide = max(sum max(c,0)/3, 1e-6), mask = 1 - smoothstep(peak),
+//                then blur(mask) and blur(guide) refine the mask, streamed
+//                down column strips;
 //   rl_stream    one whole RL iteration streamed down column strips:
 //                blur(estimate) -> ratio = guide / max(b, 1e-6) -> blur(ratio)
 //                -> estimate = clamp(estimate * b, guide/2, 2 guide)
@@ -53,50 +55,7 @@ __device__ __forceinline__ int mirror_half(int index, int length) {
   return f < length ? f : 2 * length - 1 - f;
 }
 
-__global__ void rl_init_kernel(const float* __restrict__ rgb, long long plane, float c0, float c1, float c2,
-                               float* __restrict__ guide, float* __restrict__ mask, float* __restrict__ est,
-                               unsigned* error) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= plane) return;
-  const float r = rgb[i], g = rgb[plane + i], b = rgb[2 * plane + i];
-  if (!isfinite(r) || !isfinite(g) || !isfinite(b)) atomicOr(error, 2u);
-  float s = -0.0f;
-  s += rmax(r, 0.0f) / 3.0f;
-  s += rmax(g, 0.0f) / 3.0f;
-  s += rmax(b, 0.0f) / 3.0f;
-  const float gd = rmax(s, FLOOR);
-  float peak = 0.0f;
-  peak = rmax(peak, r / c0);
-  peak = rmax(peak, g / c1);
-  peak = rmax(peak, b / c2);
-  guide[i] = gd;
-  est[i] = gd;
-  mask[i] = 1.0f - smoothstep(0.85f, 0.98f, peak);
-}
 
-// Tile geometry of the fused kernels: a TX x TY core with radius-r halos.
-constexpr int TX = 64, TY = 32, RMAX = 4;
-constexpr int EW = TX + 4 * RMAX, EH = TY + 4 * RMAX;  // estimate window (two blurs)
-constexpr int RWX = TX + 2 * RMAX, RWY = TY + 2 * RMAX; // ratio window (one blur)
-
-// Load a real field into a window whose origin is (ox, oy): every entry holds
-// the field at the mirrored (in-image) position.
-__device__ __forceinline__ void load_window(float* dst, int ww, int wh, const float* __restrict__ src, int W, int H,
-                                            int ox, int oy) {
-  for (int k = threadIdx.x; k < ww * wh; k += blockDim.x) {
-    const int qy = k / ww, qx = k % ww;
-    dst[k] = src[(long long)mirror_half(oy + qy, H) * W + mirror_half(ox + qx, W)];
-  }
-}
-
-// Horizontal taps at image column x (in-image) of window row `row` whose
-// window column of x is qx: the reference's interior/border split.
-__device__ __forceinline__ float hblur(const float* row, int qx, int x, int W, int r, int taps) {
-  const bool border = W <= 2 * r || x < r || x >= W - r;
-  float v = border ? -0.0f : 0.0f;
-  for (int k = 0; k < taps; ++k) v += row[qx - r + k] * c_kernel[k];
-  return v;
-}
 
 // ---- one RL iteration, streamed down column strips --------------------------
 // A CTA owns a strip of SW = 128 - 2R output columns and a segment of rows and
@@ -354,6 +313,158 @@ Status launch_rl_iter(Context& ctx, const float* est, const float* guide, float*
   return Status{};
 }
 
+// ---- guide and mask, streamed down column strips ---------------------------
+// sharpening.rs:180-230 before the iterations: guide = max(sum max(c,0)/3,
+// 1e-6) and mask = 1 - smoothstep(0.85, 0.98, max c/ceil_c) for every pixel,
+// then mask = min(mask, blur(mask)^4) * smoothstep(thr, 3 thr, |g - blur(g)|)
+// * smoothstep(0.001, 0.01, g). One CTA walks a strip of SW = 128 - 2R output
+// columns down a row segment: each arriving row is turned into guide and mask
+// values for the strip plus R mirrored columns on each side, blurred
+// horizontally, and R rows later blurred vertically and combined. The guide
+// doubles as the first estimate of the iterations.
+template <int R>
+struct PrepSmem {
+  static constexpr int QW = 128, SW = QW - 2 * R, RS = 16;
+  float g[RS][QW];   // guide
+  float m[RS][QW];   // initial mask
+  float tg[RS][QW];  // horizontal blur of the guide (first SW columns)
+  float tm[RS][QW];  // horizontal blur of the mask
+};
+
+template <int R>
+__global__ void __launch_bounds__(128) rl_prep_kernel(const float* __restrict__ rgb, long long plane, float c0,
+                                                      float c1, float c2, float noise, float* __restrict__ guide,
+                                                      float* __restrict__ mask, int W, int H, int strips, int seg_h,
+                                                      int items, unsigned* error) {
+  using S_ = PrepSmem<R>;
+  constexpr int T = 2 * R + 1, SW = S_::SW, RS = S_::RS, BH = 8;
+  extern __shared__ float4 rl_smem_raw[];
+  S_& S = *reinterpret_cast<S_*>(rl_smem_raw);
+  float w[T];
+#pragma unroll
+  for (int k = 0; k < T; ++k) w[k] = c_kernel[k];
+  const int tid = threadIdx.x;
+  bool bad = false;
+  for (int item = blockIdx.x; item < items; item += gridDim.x) {
+    const int x0 = (item % strips) * SW, y0 = (item / strips) * seg_h;
+    const int y1 = min(y0 + seg_h, H);
+    const int e_end = min(y1 + R, H);
+    int e_next = max(y0 - R, 0), o_next = y0;
+    const int xq = x0 - R + tid;  // this thread's column of the guide / mask rows
+    const int sx = (unsigned)xq < (unsigned)W ? xq : mirror_half(xq, W);
+    while (o_next < y1) {
+      const int e_hi = min(e_next + BH, e_end);
+      const int o_avail = e_hi >= H ? y1 : e_hi - R;
+      const int o_hi = max(o_next, min(min(o_next + BH, y1), o_avail));
+      // 1. guide and initial mask of rows [e_next, e_hi) (rl_init, sharpening.rs:187-203)
+      for (int y = e_next; y < e_hi; ++y) {
+        const long long i = (long long)y * W + sx;
+        const float r = rgb[i], g = rgb[plane + i], b = rgb[2 * plane + i];
+        if (!isfinite(r) || !isfinite(g) || !isfinite(b)) bad = true;
+        float s = -0.0f;
+        s += rmax(r, 0.0f) / 3.0f;
+        s += rmax(g, 0.0f) / 3.0f;
+        s += rmax(b, 0.0f) / 3.0f;
+        float peak = 0.0f;
+        peak = rmax(peak, r / c0);
+        peak = rmax(peak, g / c1);
+        peak = rmax(peak, b / c2);
+        S.g[y & (RS - 1)][tid] = rmax(s, FLOOR);
+        S.m[y & (RS - 1)][tid] = 1.0f - smoothstep(0.85f, 0.98f, peak);
+      }
+      __syncthreads();
+      // 2. horizontal blurs of rows [e_next, e_hi), output columns, runs of 8
+      {
+        constexpr int RUN = 8, RUNS = (SW + RUN - 1) / RUN;
+        for (int k = tid; k < (e_hi - e_next) * RUNS * 2; k += 128) {
+          const int field = k & 1, rest = k >> 1;
+          const int y = e_next + rest / RUNS, c0 = (rest % RUNS) * RUN;
+          const int n = min(min(RUN, SW - c0), W - (x0 + c0));
+          if (n <= 0) continue;
+          const float* src = field ? S.m[y & (RS - 1)] : S.g[y & (RS - 1)];
+          float* dst = field ? S.tm[y & (RS - 1)] : S.tg[y & (RS - 1)];
+          hrun<R, RUN>(src, c0 + R, n, dst + c0, x0 + c0, W, w);
+        }
+      }
+      __syncthreads();
+      // 3. vertical blurs and the mask refinement of rows [o_next, o_hi) (sharpening.rs:205-230)
+      {
+        const int x = x0 + tid, n = o_hi - o_next;
+        if (tid < SW && x < W && n > 0) {
+          float wg[BH + 2 * R], wm[BH + 2 * R];
+#pragma unroll
+          for (int j = 0; j < BH + 2 * R; ++j) {
+            const int row = j < n + 2 * R ? mirror_row(o_next - R + j, H) & (RS - 1) : 0;
+            wg[j] = S.tg[row][tid];
+            wm[j] = S.tm[row][tid];
+          }
+#pragma unroll
+          for (int j = 0; j < BH; ++j) {
+            if (j < n) {
+              float bm = 0.0f, bg = 0.0f;
+#pragma unroll
+              for (int t = 0; t < T; ++t) {
+                bm += wm[j + t] * w[t];
+                bg += wg[j + t] * w[t];
+              }
+              const int y = o_next + j;
+              const float m0 = S.m[y & (RS - 1)][tid + R];
+              const float g = S.g[y & (RS - 1)][tid + R];
+              const float b2 = bm * bm;
+              float m = rmin(m0, b2 * b2);
+              const float threshold = 0.0005f + noise * 0.008f + bg * noise * 0.02f;
+              const float detail = fabsf(g - bg);
+              m *= smoothstep(threshold, threshold * 3.0f, detail) * smoothstep(0.001f, 0.01f, g);
+              const long long o = (long long)y * W + x;
+              mask[o] = m;
+              guide[o] = g;
+            }
+          }
+        }
+      }
+      e_next = e_hi;
+      o_next = o_hi;
+      __syncthreads();
+    }
+  }
+  if (bad) atomicOr(error, 2u);
+}
+
+template <int R>
+Status launch_rl_prep(Context& ctx, const float* rgb, long long plane, const float ceil[3], float noise, float* guide,
+                      float* mask, int W, int H) {
+  using S_ = PrepSmem<R>;
+  const size_t smem = sizeof(S_);
+  RD_CUDA_TRY(cudaFuncSetAttribute(rl_prep_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int occ = 0;
+  RD_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, rl_prep_kernel<R>, 128, smem));
+  const int sms = ctx.sm_count > 0 ? ctx.sm_count : 152;
+  const int slots = std::max(1, occ) * sms;
+  const int strips = (W + S_::SW - 1) / S_::SW;
+  const int per_round = std::max(1, slots / strips);
+  int segs = std::min(per_round, std::max(1, H / 32));
+  while ((H + segs - 1) / segs > 512) segs += per_round;
+  const int seg_h = (H + segs - 1) / segs;
+  const int nseg = (H + seg_h - 1) / seg_h;
+  const int items = strips * nseg;
+  const int grid = std::min(items, slots);
+  RD_LAUNCH(ctx, K_RL_MASK, rl_prep_kernel<R><<<grid, 128, smem, ctx.stream>>>(
+                                rgb, plane, ceil[0], ceil[1], ceil[2], noise, guide, mask, W, H, strips, seg_h, items,
+                                ctx.d_error));
+  return Status{};
+}
+
+Status rl_prep(Context& ctx, int r, const float* rgb, long long plane, const float ceil[3], float noise, float* guide,
+               float* mask, int W, int H) {
+  switch (r) {
+    case 1: return launch_rl_prep<1>(ctx, rgb, plane, ceil, noise, guide, mask, W, H);
+    case 2: return launch_rl_prep<2>(ctx, rgb, plane, ceil, noise, guide, mask, W, H);
+    case 3: return launch_rl_prep<3>(ctx, rgb, plane, ceil, noise, guide, mask, W, H);
+    case 4: return launch_rl_prep<4>(ctx, rgb, plane, ceil, noise, guide, mask, W, H);
+    default: return Status{RD_INVALID_INPUT, "capture radius outside 1..4"};
+  }
+}
+
 Status rl_iteration(Context& ctx, int r, const float* est, const float* guide, float* out, int W, int H) {
   switch (r) {
     case 1: return launch_rl_iter<1>(ctx, est, guide, out, W, H);
@@ -364,52 +475,6 @@ Status rl_iteration(Context& ctx, int r, const float* est, const float* guide, f
   }
 }
 
-// Mask refinement: blur(mask) and blur(guide) of one tile, then
-//   mask = min(mask, blur(mask)^4) * smoothstep(thr, 3 thr, |g - blur(g)|) * smoothstep(0.001, 0.01, g).
-struct RlMaskSmem {
-  float m[RWY * RWX];
-  float g[RWY * RWX];
-  float tm[RWY * TX];
-  float tg[RWY * TX];
-};
-
-__global__ void __launch_bounds__(256) rl_mask_kernel(const float* __restrict__ mask_in, const float* __restrict__ guide,
-                                                      float* __restrict__ mask_out, int W, int H, int r, float noise) {
-  extern __shared__ float4 rl_smem_raw[];
-  RlMaskSmem& S = *reinterpret_cast<RlMaskSmem*>(rl_smem_raw);
-  const int taps = 2 * r + 1;
-  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
-  const int qw = TX + 2 * r, qh = TY + 2 * r;
-  load_window(S.m, qw, qh, mask_in, W, H, x0 - r, y0 - r);
-  load_window(S.g, qw, qh, guide, W, H, x0 - r, y0 - r);
-  __syncthreads();
-  for (int k = threadIdx.x; k < qh * TX; k += blockDim.x) {
-    const int qy = k / TX, cx = k % TX;
-    const int x = x0 + cx;
-    if (x >= W) continue;
-    S.tm[k] = hblur(S.m + qy * qw, cx + r, x, W, r, taps);
-    S.tg[k] = hblur(S.g + qy * qw, cx + r, x, W, r, taps);
-  }
-  __syncthreads();
-  for (int k = threadIdx.x; k < TY * TX; k += blockDim.x) {
-    const int cy = k / TX, cx = k % TX;
-    const int x = x0 + cx, y = y0 + cy;
-    if (x >= W || y >= H) continue;
-    float bm = 0.0f, bg = 0.0f;
-    for (int j = 0; j < taps; ++j) {
-      bm += S.tm[(cy + j) * TX + cx] * c_kernel[j];
-      bg += S.tg[(cy + j) * TX + cx] * c_kernel[j];
-    }
-    const float m0 = S.m[(cy + r) * qw + cx + r];
-    const float g = S.g[(cy + r) * qw + cx + r];
-    const float b2 = bm * bm;
-    float m = rmin(m0, b2 * b2);
-    const float threshold = 0.0005f + noise * 0.008f + bg * noise * 0.02f;
-    const float detail = fabsf(g - bg);
-    m *= smoothstep(threshold, threshold * 3.0f, detail) * smoothstep(0.001f, 0.01f, g);
-    mask_out[(long long)y * W + x] = m;
-  }
-}
 
 // Vignetting radius scan (correction.rs:239-262): r2 advances along each row
 // by the row-independent increment d[k] = 2 ns x_k + ns^2 with f32 rounding at
@@ -641,30 +706,25 @@ Status run_capture(Context& ctx, float* rgb, int W, int H, const rd_detail_desc&
     if (taps < 0) return Status{RD_INVALID_INPUT, "capture radius too large"};
     r = taps / 2;
     RD_CUDA_TRY(cudaMemcpyToSymbolAsync(c_kernel, w, sizeof(float) * taps, 0, cudaMemcpyHostToDevice, ctx.stream));
-    plane_bytes = sizeof(float) * (size_t)plane * 5;
+    plane_bytes = sizeof(float) * (size_t)plane * 4;
     void* p = nullptr;
     RD_TRY(device_alloc(ctx, plane_bytes, &p));
     planes = static_cast<float*>(p);
   }
   float* guide = planes;
   float* mask = planes ? planes + plane : nullptr;
-  float* mask2 = planes ? planes + 2 * plane : nullptr;
-  float* est = planes ? planes + 3 * plane : nullptr;
-  float* est2 = planes ? planes + 4 * plane : nullptr;
+  float* est_buf[2] = {planes ? planes + 2 * plane : nullptr, planes ? planes + 3 * plane : nullptr};
+  // The estimate starts as the guide (sharpening.rs:203), so the first
+  // iteration reads the guide plane itself.
+  const float* est = guide;
   Status st;
   if (capture) {
-    RD_LAUNCH(ctx, K_RL_INIT, rl_init_kernel<<<(unsigned)((plane + 255) / 256), 256, 0, ctx.stream>>>(
-        rgb, plane, detail.ceilings[0], detail.ceilings[1], detail.ceilings[2], guide, mask, est, ctx.d_error));
-    dim3 grid((W + TX - 1) / TX, (H + TY - 1) / TY);
-    const size_t mask_smem = sizeof(RlMaskSmem);
-    cudaFuncSetAttribute(rl_mask_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mask_smem);
-    RD_LAUNCH(ctx, K_RL_MASK, rl_mask_kernel<<<grid, 256, mask_smem, ctx.stream>>>(mask, guide, mask2, W, H, r, detail.noise_protection));
-    std::swap(mask, mask2);
+    st = rl_prep(ctx, r, rgb, plane, detail.ceilings, detail.noise_protection, guide, mask, W, H);
     for (int it = 0; it < detail.iterations && st.ok(); ++it) {
-      st = rl_iteration(ctx, r, est, guide, est2, W, H);
-      std::swap(est, est2);
+      st = rl_iteration(ctx, r, est, guide, est_buf[it & 1], W, H);
+      est = est_buf[it & 1];
     }
-    if (cudaGetLastError() != cudaSuccess) st = Status{RD_SYNCHRONIZATION, "capture kernels failed to launch"};
+    if (st.ok() && cudaGetLastError() != cudaSuccess) st = Status{RD_SYNCHRONIZATION, "capture kernels failed to launch"};
   }
   VignetteTables vt;
   if (st.ok() && vig) st = prepare_vignetting(ctx, *vignetting, W, H, vt);
