@@ -322,6 +322,8 @@ def run_ours(args, world, rank, local, pg):
     dev.close()
     if rank == 0 and not args.no_edit_latency:
         line["edit_latency"] = edit_latency(args)
+    if rank == 0 and not args.no_batched:
+        line["batched"] = batched_throughput(args)
     return line
 
 
@@ -444,6 +446,31 @@ def edit_latency(args, images: int = 16, seconds: float = 2.0, rate: float = 200
     }
 
 
+def batched_throughput(args, count: int = 24, lanes: int = 3) -> dict:
+    """The uneven batch (rohditor_gb300.workloads.batched_uneven: 12-60 MP,
+    random CFA phase, black, WB and matrices; Opposed + AMaZE + RL K=5 +
+    optics + 2560-px preview, sRGB8 + histogram to the host) through
+    rd_develop_batch with `lanes` concurrent lanes, and the same images one at
+    a time (one lane). Host mosaics in, host outputs out, timed end to end."""
+    from rohditor_gb300 import Device
+    from rohditor_gb300.batch import BatchImage, develop_batch
+    from rohditor_gb300.workloads import batched_uneven
+
+    dev = Device(0)
+    wls = batched_uneven(count)
+    images = [BatchImage(w.mosaic(dev), w.sensor, w.capture, w.optics, w.target, w.color.wb_gains,
+                         w.color.camera_to_rec2020, w.color) for w in wls]
+    dev.close()
+    pixels = sum(w.width * w.height for w in wls)
+    develop_batch(images[:lanes], lanes=lanes)  # warm-up
+    _, _, wall = develop_batch(images, lanes=lanes)
+    _, _, wall1 = develop_batch(images, lanes=1)
+    return {"images": count, "megapixels": round(pixels / 1e6, 1), "lanes": lanes, "wall_ms": round(wall, 1),
+            "develops_per_s": round(count / (wall / 1e3), 2), "mp_per_s": round(pixels / 1e6 / (wall / 1e3), 1),
+            "one_lane_wall_ms": round(wall1, 1), "speedup_vs_one_lane": round(wall1 / wall, 3),
+            "workload": "uneven batch: 12/24/45/60 MP, random CFA phase, Opposed + AMaZE + RL5 + optics + preview"}
+
+
 def cpu_develop_band(rows: int, args) -> tuple[float, float]:
     """Run the oracle pipeline on a `rows`-high band of the 24 MP workload; returns (seconds, fraction)."""
     from oracle import oracle as o
@@ -533,6 +560,7 @@ def main():
     p.add_argument("--height", type=int, default=4024)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-edit-latency", action="store_true", help="skip the served-vs-plain edit latency trace")
+    p.add_argument("--no-batched", action="store_true", help="skip the uneven batched-develop measurement")
     p.add_argument("--cpu-baseline-rows", type=int, default=2048,
                    help="band height of the CPU baseline sample (2048 rows = half a 24 MP develop)")
     args = p.parse_args()

@@ -236,6 +236,32 @@ rd_status rd_optics_plan(rd_optics_desc* optics, float crop_factor, float real_f
 /* BaseRenderingLut::standard_v1 (crates/core/src/rendering.rs:36-50). */
 void rd_standard_base_lut(float* lut4096);
 
+/* ---- batched develop ----
+ * Many mosaics of uneven sizes, CFA phases and settings through the whole path
+ * (rd_develop -> rd_spatial -> rd_render, host buffers in and out) on one GPU:
+ * `lanes` host threads with their own contexts and streams take images from a
+ * shared queue, so their kernels overlap on the device. The reference runs one
+ * image per call (SpatialCache::prepare_sensor,
+ * crates/engine/src/preview_cache/spatial.rs:475-600). Each item reports its
+ * status and time; the return value is the first failing status (RD_OK when
+ * all succeed); wall_ms (optional) is the elapsed time of the whole batch. */
+typedef struct rd_batch_item {
+  const uint16_t* mosaic;  /* host, sensor_height rows of row_stride samples */
+  size_t row_stride;
+  rd_sensor_desc sensor;
+  rd_detail_desc detail;
+  rd_optics_desc optics;
+  uint32_t target_width, target_height;
+  float wb_gains[3];
+  float camera_to_rec2020[9];
+  rd_color_desc color;
+  uint8_t* srgb_out;       /* host [target_height][3*target_width] */
+  uint64_t* hist;          /* host 1024 bins, or NULL */
+  int32_t status;          /* out */
+  double ms;               /* out: this item's time in its lane */
+} rd_batch_item;
+rd_status rd_develop_batch(int device, rd_batch_item* items, int32_t count, int32_t lanes, double* wall_ms);
+
 /* ---- served preview loop ----
  * Replaces the engine's preview worker and caches
  * (crates/engine/src/coordinator/scheduler.rs:44-180 newest-wins mailbox,

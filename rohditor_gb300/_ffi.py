@@ -103,6 +103,16 @@ class SynthDesc(ctypes.Structure):
     ]
 
 
+class BatchItem(ctypes.Structure):
+    _fields_ = [
+        ("mosaic", ctypes.POINTER(ctypes.c_uint16)), ("row_stride", ctypes.c_size_t), ("sensor", SensorDesc),
+        ("detail", DetailDesc), ("optics", OpticsDesc), ("target_width", ctypes.c_uint32),
+        ("target_height", ctypes.c_uint32), ("wb_gains", ctypes.c_float * 3), ("camera_to_rec2020", ctypes.c_float * 9),
+        ("color", ColorDesc), ("srgb_out", ctypes.POINTER(ctypes.c_uint8)), ("hist", ctypes.POINTER(ctypes.c_uint64)),
+        ("status", ctypes.c_int32), ("ms", ctypes.c_double),
+    ]
+
+
 class ServerResult(ctypes.Structure):
     _fields_ = [
         ("request_id", ctypes.c_uint64), ("image_id", ctypes.c_uint32), ("kind", ctypes.c_int32),
@@ -162,6 +172,8 @@ SIGNATURES = {
                                       ctypes.c_float]),
     "rd_standard_base_lut": (None, [F32P]),
     "rd_synth_mosaic_device": (ctypes.c_int, [VOIDP, ctypes.POINTER(SynthDesc), VOIDP]),
+    "rd_develop_batch": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(BatchItem), ctypes.c_int32, ctypes.c_int32,
+                                        ctypes.POINTER(ctypes.c_double)]),
     "rd_server_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(VOIDP)]),
     "rd_server_set_dry_timing": (ctypes.c_int, [VOIDP, ctypes.c_uint32, ctypes.c_uint32]),
     "rd_server_destroy": (None, [VOIDP]),

@@ -167,3 +167,38 @@ def full_24mp(demosaic: str = "amaze", iterations: int = 10, seed: int = 2, high
                           base_lut=standard_base_lut(), tone_lut=sixteen_knot_curve(), hsl=hsl_bands())
     return Workload("full_24mp", width, height, "RGGB", 14, 512.0, 16383.0, 0.05, True, wb, sensor, capture, optics,
                     target, color, seed)
+
+
+# Sizes and bit depths of the uneven batch (12-, 24-, 45- and 60-megapixel sensors).
+BATCH_SENSORS = ((4000, 3000, 12), (6048, 4024, 14), (8256, 5504, 14), (9504, 6336, 14))
+
+
+def batched_uneven(count: int = 48, seed: int = 3, iterations: int = 5) -> list[Workload]:
+    """The uneven batch: sizes drawn from BATCH_SENSORS, random CFA phase,
+    black U(256, 1024), per-image as-shot WB and camera matrix from seeded
+    ranges; Opposed + AMaZE + RL (K iterations) + optics + 2560-px preview."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        width, height, bits = BATCH_SENSORS[int(rng.integers(len(BATCH_SENSORS)))]
+        cfa = ("RGGB", "BGGR", "GRBG", "GBRG")[int(rng.integers(4))]
+        white = float((1 << bits) - 1)
+        black = float(rng.uniform(256.0, 1024.0)) if bits == 14 else float(rng.uniform(64.0, 256.0))
+        wb = (float(rng.uniform(1.6, 2.4)), 1.0, float(rng.uniform(1.3, 2.0)))
+        cam = tuple(float(v) for v in (np.asarray(CAMERA_TO_REC2020) * rng.uniform(0.95, 1.05, 9)))
+        det, ceiling = opposed_levels(1.0, wb)
+        sensor = SensorDescription(sensor_width=width, sensor_height=height, cfa=cfa, black=(black,), white=(white,),
+                                   highlight="opposed", detection_levels=det, neutral_ceiling=ceiling,
+                                   demosaic="amaze", demosaic_balance=wb)
+        capture = CaptureContract(amount=0.5, radius=0.7, noise_protection=0.5, ceilings=(1.0, 1.0, 1.0),
+                                  iterations=iterations)
+        vig = tuple(float(v) for v in (-rng.uniform(0.2, 0.4), rng.uniform(0.02, 0.08), -rng.uniform(0.0, 0.02)))
+        optics = OpticsExecution(width=width, height=height, distortion="poly5", distortion_k=(-0.02, 0.005, 0.0),
+                                 tca="linear", tca_red=(1.0003, 0.0, 0.0), tca_blue=(0.9997, 0.0, 0.0),
+                                 vignetting_k=vig, crop_factor=1.0, real_focal=35.0)
+        color = ColorContract(wb_gains=wb, camera_to_rec2020=cam, exposure_ev=float(rng.uniform(-0.5, 0.8)),
+                              base_lut=standard_base_lut(), tone_lut=sixteen_knot_curve(seed=int(rng.integers(1 << 30))),
+                              hsl=hsl_bands(seed=int(rng.integers(1 << 30))))
+        out.append(Workload(f"batch_{k}", width, height, cfa, bits, black, white, 0.05, True, wb, sensor, capture,
+                            optics, preview_dimensions(width, height, 2560), color, seed * 1000 + k))
+    return out

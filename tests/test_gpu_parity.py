@@ -361,3 +361,46 @@ def test_develop_with_opposed(device, oracle):
     got = src.download()
     assert list(src.metrics.highlight_stats) == stats.tolist()
     assert float(np.max(np.abs(got - ref))) <= 1e-4
+
+
+def test_batched_develop_matches_one_at_a_time(device):
+    """rd_develop_batch over uneven sizes and CFA phases equals the per-image path, bit for bit."""
+    from rohditor_gb300 import (CaptureContract, ColorContract, GpuPreviewProcessor, GpuSensorProcessor,
+                                GpuSpatialProcessor, OpticsExecution, SensorDescription, clip_levels, opposed_levels)
+    from rohditor_gb300.batch import BatchImage, develop_batch
+    from rohditor_gb300.workloads import CAMERA_TO_REC2020, hsl_bands, preview_dimensions, sixteen_knot_curve
+
+    shapes = [(700, 467, "RGGB", "clip"), (1024, 768, "GBRG", "opposed"), (512, 384, "BGGR", "clip"),
+              (640, 480, "GRBG", "opposed")]
+    images = []
+    for k, (w, h, cfa, hl) in enumerate(shapes):
+        raw = raw_mosaic(w, h, w, seed=70 + k)
+        wb = (2.0 - 0.1 * k, 1.0, 1.6 + 0.1 * k)
+        if hl == "clip":
+            sensor = SensorDescription(w, h, cfa=cfa, black=(256.0,), white=(4095.0,), highlight="clip",
+                                       clip_levels=clip_levels(1.0, wb), demosaic="amaze", demosaic_balance=wb)
+            ceil = clip_levels(1.0, wb)
+        else:
+            det, neutral = opposed_levels(1.0, wb)
+            sensor = SensorDescription(w, h, cfa=cfa, black=(256.0,), white=(4095.0,), highlight="opposed",
+                                       detection_levels=det, neutral_ceiling=neutral, demosaic="amaze",
+                                       demosaic_balance=wb)
+            ceil = (1.0, 1.0, 1.0)
+        cap = CaptureContract(amount=0.5, radius=0.7, noise_protection=0.5, ceilings=ceil, iterations=5)
+        optics = OpticsExecution(w, h, distortion="poly5", distortion_k=(-0.02, 0.005, 0.0), tca="linear",
+                                 tca_red=(1.0003, 0, 0), tca_blue=(0.9997, 0, 0), vignetting_k=(-0.3, 0.05, -0.01))
+        color = ColorContract(wb_gains=wb, camera_to_rec2020=CAMERA_TO_REC2020, exposure_ev=0.1 * k,
+                              tone_lut=sixteen_knot_curve(seed=k), hsl=hsl_bands(seed=k))
+        images.append(BatchImage(raw, sensor, cap, optics, preview_dimensions(w, h, 256), wb, CAMERA_TO_REC2020,
+                                 color))
+    outs, ms, wall = develop_batch(images, lanes=3)
+    assert wall > 0 and all(m > 0 for m in ms)
+    for im, (srgb, hist) in zip(images, outs):
+        src = GpuSensorProcessor(device).develop(im.mosaic, im.sensor, im.capture)
+        base = GpuSpatialProcessor(device).reduce_preview(src, im.optics, im.target, im.wb_gains,
+                                                          im.camera_to_rec2020)
+        ref, ref_hist = GpuPreviewProcessor(device).render(base, im.color)
+        base.release()
+        src.release()
+        assert np.array_equal(srgb, ref)
+        assert np.array_equal(hist[:256], ref_hist.red) and np.array_equal(hist[768:], ref_hist.luminance)
