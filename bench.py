@@ -147,7 +147,7 @@ def family_bytes(name: str, N: int, n: int, H: int, tw: int) -> float | None:
         "rl_iteration": 12.0 * N,   # estimate in, guide in, estimate out
         "rl_mask": 20.0 * N,        # guide + mask preparation: RGB in, guide + refined mask out
         "rl_apply": 36.0 * N,
-        "vignetting": 4.0 * N,
+        "vignetting": 4.0 * N,      # multiplier plane out
         "optics_gather": 28.0 * N,  # RGB + multiplier in, RGB out
         "area_horizontal": 12.0 * N + 12.0 * tw * H,
         "area_vertical": 12.0 * tw * H + 12.0 * n,

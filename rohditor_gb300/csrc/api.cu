@@ -608,6 +608,9 @@ rd_status rd_spatial(rd_ctx* h, const rd_source* source, const rd_optics_desc* o
   void* p = nullptr;
   float* mult = nullptr;
   float* warped = nullptr;
+  // Vignetting multiplies the source in place before the warp
+  // (correction.rs:70-211); the source stays reusable here, so the gather and
+  // the area reduction apply the multiplier plane to each sample they read.
   if (vig) {
     st = rd::device_alloc(ctx, sizeof(float) * plane, &p);
     if (st.ok()) {

@@ -23,6 +23,8 @@
 // scan; the trimmed means agree to f64 rounding, which is far below f32.
 // Every retry loop carries an iteration limit and reports through the error
 // word instead of spinning.
+#include <cooperative_groups.h>
+#include <cooperative_groups/reduce.h>
 #include <cuda_runtime.h>
 
 #include "rd_internal.cuh"
@@ -339,6 +341,16 @@ __global__ void root_ids_kernel(const OpposedParams p) {
   if (root) p.parent[i] = before + 1;
 }
 
+// OR `bits` into word[key] once per distinct key of the warp (neighbouring
+// cells nearly always share their region).
+__device__ __forceinline__ void warp_or(unsigned* word, unsigned key, unsigned bits) {
+  namespace cg = cooperative_groups;
+  const cg::coalesced_group active = cg::coalesced_threads();
+  const cg::coalesced_group peers = cg::labeled_partition(active, key);
+  const unsigned v = cg::reduce(peers, bits, cg::bit_or<unsigned>());
+  if (peers.thread_rank() == 0 && v) atomicOr(&word[key], v);
+}
+
 __global__ void relabel_kernel(const OpposedParams p) {
   if (p.counters[0] == 0) return;
   const int cx = blockIdx.x * blockDim.x + threadIdx.x, cy = blockIdx.y;
@@ -352,7 +364,7 @@ __global__ void relabel_kernel(const OpposedParams p) {
   }
   p.labels[i] = label;
   const unsigned clipped = __float_as_uint(p.cells[i].w) >> 3;
-  if (label && clipped) atomicOr(&p.region_clipped[label], clipped);
+  warp_or(p.region_clipped, label && clipped ? label : 0u, label ? clipped : 0u);
 }
 
 // 5. wanted (channel, support) slots per region (region_correction.rs:134-178)
@@ -376,8 +388,8 @@ __global__ void wanted_kernel(const OpposedParams p) {
     if (pos >= 0) bits |= 1u << (ch * PATTERNS + pos);
   }
   if (bits) {
-    atomicOr(&p.wanted[label], bits);
-    atomicOr(&p.wanted[0], bits);
+    warp_or(p.wanted, label, bits);
+    warp_or(p.wanted, 0u, bits);
   }
 }
 
