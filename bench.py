@@ -40,6 +40,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "24MP develops/s"
 UNIT = "develops/s"
+KERNEL_FAMILIES = 17  # RD_KERNEL_FAMILIES of include/rd_gpu.h
 
 
 def dist_setup(gpus: int):
@@ -242,7 +243,7 @@ def run_ours(args, world, rank, local, pg):
     barrier(pg)
     total_ms = max_over_ranks(pg, total_ms)
     families = {}
-    for f in range(16):
+    for f in range(KERNEL_FAMILIES):
         name = ctypes.c_char_p()
         ms = ctypes.c_double()
         cnt = ctypes.c_uint64()
@@ -324,6 +325,8 @@ def run_ours(args, world, rank, local, pg):
         line["edit_latency"] = edit_latency(args)
     if rank == 0 and not args.no_batched:
         line["batched"] = batched_throughput(args)
+    if rank == 0 and not args.no_export:
+        line["export"] = export_output(args)
     return line
 
 
@@ -471,6 +474,77 @@ def batched_throughput(args, count: int = 24, lanes: int = 3) -> dict:
             "workload": "uneven batch: 12/24/45/60 MP, random CFA phase, Opposed + AMaZE + RL5 + optics + preview"}
 
 
+def export_output(args, reps: int = 5) -> dict:
+    """Full-resolution outputs of the 24 MP develop: one base at the mosaic's
+    size (no area reduction), then rd_render_output_device into device buffers
+    for each export format. Device time per launch of the output kernel, L2
+    flushed before each; algorithmic bytes = 12 B/px planar f32 read + the
+    format's bytes written."""
+    from rohditor_gb300 import Device, OutputSpec
+    from rohditor_gb300.workloads import full_24mp
+
+    dev = Device(0)
+    lib, h = dev.lib, dev.handle
+    wl = full_24mp(demosaic=args.demosaic, iterations=args.iterations, highlight=args.highlight,
+                   width=args.width, height=args.height)
+    W, H = wl.width, wl.height
+    sensor, detail, optics, color = wl.sensor.to_c(), wl.capture.to_c(), wl.optics.to_c(), wl.color.to_c()
+    wb = np.ascontiguousarray(wl.color.wb_gains, dtype=np.float32)
+    cam = np.ascontiguousarray(wl.color.camera_to_rec2020, dtype=np.float32)
+    d_mosaic = wl.mosaic_device(dev)
+    src, base = ctypes.c_void_p(), ctypes.c_void_p()
+    dev.check(lib.rd_develop_device(h, ctypes.c_void_p(d_mosaic), W, ctypes.byref(sensor), ctypes.byref(detail),
+                                    None, ctypes.byref(src), None))
+    dev.check(lib.rd_spatial(h, src, ctypes.byref(optics), W, H, wb.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                             cam.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), ctypes.byref(base), None))
+    lib.rd_source_release(src)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    specs = {
+        "extended_f16_p3_compress_h4": OutputSpec(format="extended_f16", primaries="display_p3",
+                                                  policy="chroma_compress", headroom=4.0),
+        "srgb8_clip": OutputSpec(format="srgb8"),
+        "srgb16_compress_dither": OutputSpec(format="srgb16", policy="chroma_compress", dither="ordered8x8"),
+        "extended_f32_srgb_clip_rotate90": OutputSpec(format="extended_f32", orientation="rotate90", headroom=2.0),
+    }
+    out = {}
+    d_out, d_gamut = ctypes.c_void_p(), ctypes.c_void_p()
+    dev.check(lib.rd_device_alloc(h, 12 * W * H, ctypes.byref(d_out)))
+    dev.check(lib.rd_device_alloc(h, 64, ctypes.byref(d_gamut)))
+    for name, spec in specs.items():
+        oc = spec.to_c()
+        bpp = {"srgb8": 3, "srgb16": 6, "extended_f32": 12, "extended_f16": 6}[spec.format]
+        dev.check(lib.rd_render_output_device(h, base, ctypes.byref(color), ctypes.byref(oc), d_out, None, d_gamut,
+                                              None))
+        dev.synchronize()
+        lib.rd_ctx_reset_kernel_timing(h)
+        lib.rd_ctx_enable_kernel_timing(h, 1)
+        for _ in range(reps):
+            dev.check(lib.rd_ctx_flush_l2(h))
+            dev.check(lib.rd_render_output_device(h, base, ctypes.byref(color), ctypes.byref(oc), d_out, None,
+                                                  d_gamut, None))
+        dev.synchronize()
+        lib.rd_ctx_enable_kernel_timing(h, 0)
+        nm, ms, cnt = ctypes.c_char_p(), ctypes.c_double(), ctypes.c_uint64()
+        lib.rd_ctx_kernel_timing(h, 16, ctypes.byref(nm), ctypes.byref(ms), ctypes.byref(cnt))
+        per = ms.value / max(int(cnt.value), 1)
+        gbs = (12 + bpp) * W * H / (per / 1e3) / 1e9
+        gamut = np.zeros(5, dtype=np.uint64)
+        dev.check(lib.rd_copy_to_host(h, gamut.ctypes.data_as(ctypes.c_void_p), d_gamut, 40))
+        out[name] = {"ms": round(per, 4), "algorithmic_gbs": round(gbs, 1), "hbm_frac": round(gbs / hbm_peak, 3),
+                     "out_bytes_per_px": bpp, "gamut": [int(v) for v in gamut]}
+    dev.check(lib.rd_device_free(h, d_out))
+    dev.check(lib.rd_device_free(h, d_gamut))
+    lib.rd_base_release(base)
+    dev.check(lib.rd_device_free(h, ctypes.c_void_p(d_mosaic)))
+    dev.close()
+    return {"image": f"{W}x{H}", "peak_gbs": hbm_peak, "outputs": out}
+
+
 def cpu_develop_band(rows: int, args) -> tuple[float, float]:
     """Run the oracle pipeline on a `rows`-high band of the 24 MP workload; returns (seconds, fraction)."""
     from oracle import oracle as o
@@ -561,6 +635,7 @@ def main():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-edit-latency", action="store_true", help="skip the served-vs-plain edit latency trace")
     p.add_argument("--no-batched", action="store_true", help="skip the uneven batched-develop measurement")
+    p.add_argument("--no-export", action="store_true", help="skip the full-resolution output measurement")
     p.add_argument("--cpu-baseline-rows", type=int, default=2048,
                    help="band height of the CPU baseline sample (2048 rows = half a 24 MP develop)")
     args = p.parse_args()

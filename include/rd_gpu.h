@@ -17,6 +17,10 @@
  *   rd_spatial               GpuSpatialProcessor::reduce_preview crates/gpu/src/spatial/reduction.rs:15
  *   rd_render                GpuPreviewProcessor::render + begin_histogram
  *                                                       crates/gpu/src/preview/processor.rs:1011,1518
+ *   rd_render_output         GpuExportProcessor::render's output conversion
+ *                            crates/gpu/src/export/mod.rs:218, matching the CPU renders render_display8_cancellable,
+ *                            render_display_srgb16_with_geometry, render_extended_linear_with_geometry
+ *                            crates/core/src/cpu/stages.rs:1028-1195, crates/core/src/cpu/extended.rs:27
  *   stage entry points       the crates' stage APIs the CPU pipeline calls:
  *     rd_stage_normalize     NormalizationContract::normalize crates/core/src/pipeline/sensor.rs:221
  *     rd_stage_highlight     HighlightExecution::apply_cancellable crates/highlight/src/lib.rs:172
@@ -28,6 +32,7 @@
  *                            apply_adjustments_with_local + render_display8 + Histogram
  *                            crates/core/src/cpu/stages.rs:250-308,380-528,1028-1094;
  *                            crates/core/src/analysis/histogram.rs:92-128
+ *     rd_stage_output        apply_adjustments_with_local + the output conversions above
  */
 #ifndef RD_GPU_H
 #define RD_GPU_H
@@ -198,6 +203,70 @@ rd_status rd_render_device_noalloc(const float* d_base, uint32_t width, uint32_t
                                    const rd_color_desc* color, uint8_t* d_srgb_out, uint64_t* d_hist,
                                    void* stream);
 
+/* ---- display and extended-range output ----
+ * The output conversions of the reference's renders: the adjustment chain of
+ * rd_color_desc, then orientation + crop (OutputGeometry), gamut mapping into
+ * the target primaries and the output encoding:
+ *   RD_OUTPUT_SRGB8         render_display8_cancellable   crates/core/src/cpu/stages.rs:1028-1094
+ *   RD_OUTPUT_SRGB16        render_display_srgb16_with_geometry_and_diagnostics  stages.rs:1124-1195
+ *   RD_OUTPUT_EXTENDED_F32  render_extended_linear_with_geometry  crates/core/src/cpu/extended.rs:27-106
+ *   RD_OUTPUT_EXTENDED_F16  the same, each channel rounded to binary16 (round to nearest even)
+ * All outputs are interleaved [out_h][3*out_w]: u8, u16, f32, or binary16 bits
+ * in u16. 8- and 16-bit values are sRGB-transfer encoded; extended values are
+ * linear in 0..headroom with diffuse white at 1. The cube root of OkLab and the
+ * transfer power are correctly rounded (the reference takes both from the
+ * platform libm). */
+typedef enum rd_output_format {
+  RD_OUTPUT_SRGB8 = 0,
+  RD_OUTPUT_SRGB16 = 1,
+  RD_OUTPUT_EXTENDED_F32 = 2,
+  RD_OUTPUT_EXTENDED_F16 = 3
+} rd_output_format;
+/* RgbPrimaries (crates/image), OutputPolicy (crates/core/src/pipeline/orchestration.rs:53),
+ * DitherMode (crates/core/src/export/types.rs:99), Orientation (crates/image/src/orientation.rs). */
+enum { RD_PRIMARIES_SRGB = 0, RD_PRIMARIES_DISPLAY_P3 = 1 };
+enum { RD_POLICY_CLIP = 0, RD_POLICY_CHROMA_COMPRESS = 1 };
+enum { RD_DITHER_NONE = 0, RD_DITHER_ORDERED_8X8 = 1 };
+enum {
+  RD_ORIENTATION_NORMAL = 0, RD_ORIENTATION_HORIZONTAL_FLIP = 1, RD_ORIENTATION_ROTATE180 = 2,
+  RD_ORIENTATION_VERTICAL_FLIP = 3, RD_ORIENTATION_TRANSPOSE = 4, RD_ORIENTATION_ROTATE90 = 5,
+  RD_ORIENTATION_TRANSVERSE = 6, RD_ORIENTATION_ROTATE270 = 7, RD_ORIENTATION_UNKNOWN = 8
+};
+typedef struct rd_output_desc {
+  int32_t format;       /* rd_output_format */
+  int32_t primaries;    /* RD_PRIMARIES_* */
+  int32_t policy;       /* RD_POLICY_*: clip_linear_rgb or compress_chroma */
+  int32_t dither;       /* RD_DITHER_*: 8- and 16-bit outputs only */
+  int32_t orientation;  /* RD_ORIENTATION_* */
+  int32_t has_crop;
+  double crop[4];       /* NormalizedCropRect left, top, right, bottom on the oriented canvas */
+  float headroom;       /* extended outputs: the ceiling, finite and >= 1 */
+} rd_output_desc;
+/* Output size of a width x height base (OutputGeometry::output_dimensions,
+ * crates/core/src/geometry.rs:111-114); RD_INVALID_INPUT for an invalid
+ * description (unknown enum, crop outside 0..1, unordered or below one pixel,
+ * extended headroom not finite or < 1). bytes_per_pixel may be NULL. */
+rd_status rd_output_dimensions(uint32_t width, uint32_t height, const rd_output_desc* output, uint32_t* out_width,
+                               uint32_t* out_height, uint32_t* bytes_per_pixel);
+/* out: host buffer of at least out_capacity = out_w*out_h*bytes_per_pixel bytes.
+ * hist: 4*256 u64 of the 8-bit output (R, G, B, luma), or NULL (must be NULL
+ * for the other formats). gamut: 5 u64 GamutMappingDiagnostics (in_gamut,
+ * compressed, limited, clipped_fallback, invalid), or NULL. */
+rd_status rd_render_output(rd_ctx* ctx, const rd_base* base, const rd_color_desc* color, const rd_output_desc* output,
+                           void* out, size_t out_capacity, uint64_t* hist, uint64_t* gamut, rd_metrics* metrics);
+/* Same into device buffers (d_out of out_w*out_h*bytes_per_pixel bytes; d_hist
+ * 1024 u64 or NULL; d_gamut 5 u64 or NULL), ordered on the context's stream. */
+rd_status rd_render_output_device(rd_ctx* ctx, const rd_base* base, const rd_color_desc* color,
+                                  const rd_output_desc* output, void* d_out, uint64_t* d_hist, uint64_t* d_gamut,
+                                  rd_metrics* metrics);
+/* Self-check of the correctly rounded arithmetic on the device, for test
+ * suites (no reference counterpart). which = 0: the number of positive finite
+ * f32 whose cube root is not correctly rounded (or not odd-symmetric), exact
+ * integer comparison, expected 0. which = 1: the largest distance in ulps of
+ * powf(x, 1/2.4) from the correctly rounded power over (0.0031308, 1], which
+ * must not exceed the bound the 8- and 16-bit quantisation relies on (2). */
+rd_status rd_check_math(rd_ctx* ctx, int32_t which, uint64_t* result);
+
 rd_status rd_source_dimensions(const rd_source* source, uint32_t* width, uint32_t* height);
 rd_status rd_source_download(rd_ctx* ctx, const rd_source* source, float* rgb_interleaved);
 rd_status rd_base_dimensions(const rd_base* base, uint32_t* width, uint32_t* height);
@@ -227,6 +296,11 @@ rd_status rd_stage_area_reduce(rd_ctx* ctx, const float* rgb_in, uint32_t width,
 /* Camera-native RGB -> WB -> matrix -> adjustments -> sRGB8 + histogram. */
 rd_status rd_stage_color(rd_ctx* ctx, const float* rgb_in, uint32_t width, uint32_t height,
                          const rd_color_desc* color, uint8_t* srgb_out, uint64_t* hist, uint64_t* clipped);
+/* Linear Rec.2020 (interleaved [h][3w]) -> adjustments -> display / extended
+ * output, as rd_render_output. */
+rd_status rd_stage_output(rd_ctx* ctx, const float* rgb_in, uint32_t width, uint32_t height,
+                          const rd_color_desc* color, const rd_output_desc* output, void* out, size_t out_capacity,
+                          uint64_t* hist, uint64_t* gamut);
 
 /* ---- host-side contract helpers ---- */
 /* build_plan geometry + automatic scale (crates/optics/src/plan.rs:173-231,521-559)
@@ -338,7 +412,7 @@ rd_status rd_ctx_flush_l2(rd_ctx* ctx);
  * bracketed by CUDA events; totals are resolved at each call's final sync. */
 rd_status rd_ctx_enable_kernel_timing(rd_ctx* ctx, int enable);
 /* family: index 0..RD_KERNEL_FAMILIES-1; returns its name, total ms and launch count. */
-#define RD_KERNEL_FAMILIES 16
+#define RD_KERNEL_FAMILIES 17
 rd_status rd_ctx_kernel_timing(const rd_ctx* ctx, int family, const char** name, double* total_ms,
                                uint64_t* launches);
 rd_status rd_ctx_reset_kernel_timing(rd_ctx* ctx);

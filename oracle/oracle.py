@@ -72,6 +72,14 @@ class AdjustDesc(ctypes.Structure):
     ]
 
 
+class OutputDesc(ctypes.Structure):
+    _fields_ = [
+        ("format", ctypes.c_int), ("primaries", ctypes.c_int), ("policy", ctypes.c_int), ("dither", ctypes.c_int),
+        ("orientation", ctypes.c_int), ("has_crop", ctypes.c_int), ("crop", ctypes.c_double * 4),
+        ("headroom", ctypes.c_float),
+    ]
+
+
 def load():
     global _lib
     with _lock:
@@ -108,6 +116,18 @@ def load():
             "ro_standard_base_lut": (None, [F32P]),
             "ro_display_srgb8": (None, [F32P, ctypes.c_size_t, U8P]),
             "ro_histogram": (None, [U8P, ctypes.c_size_t, U64P, U64P]),
+            "ro_set_exact_math": (None, [ctypes.c_int]),
+            "ro_cbrt": (ctypes.c_float, [ctypes.c_float]),
+            "ro_cbrt_correctly_rounded": (ctypes.c_float, [ctypes.c_float]),
+            "ro_output_geometry": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(OutputDesc),
+                                                  ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                                  ctypes.POINTER(ctypes.c_int)]),
+            "ro_source_coordinate": (None, [ctypes.c_int] * 5 + [ctypes.POINTER(ctypes.c_int)] * 2),
+            "ro_gamut_map": (ctypes.c_int, [F32P, ctypes.c_int, ctypes.c_int, ctypes.c_float, F32P]),
+            "ro_oklab": (None, [ctypes.c_int, F32P, F32P]),
+            "ro_oklab_inverse": (None, [ctypes.c_int, F32P, F32P]),
+            "ro_render_output": (ctypes.c_int, [F32P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(OutputDesc),
+                                                ctypes.c_void_p, U64P]),
         }
         for name, (res, args) in list(sig.items()) + list(optional.items()):
             if not hasattr(lib, name):
@@ -346,3 +366,76 @@ def histogram(rgb8: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
     load().ro_histogram(ptr(rgb8, ctypes.c_uint8), rgb8.size // 3, ptr(hist, ctypes.c_uint64),
                         ptr(clipped, ctypes.c_uint64))
     return hist, clipped
+
+
+# ---- display / extended output (output.cpp) ----
+FORMATS = {"srgb8": 0, "srgb16": 1, "extended_f32": 2}
+ORIENTATIONS = ("normal", "horizontal_flip", "rotate180", "vertical_flip", "transpose", "rotate90", "transverse",
+                "rotate270", "unknown")
+
+
+def output_desc(fmt="srgb8", primaries="srgb", policy="clip", dither="none", orientation="normal", crop=None,
+                headroom=1.0) -> OutputDesc:
+    d = OutputDesc()
+    d.format = FORMATS[fmt]
+    d.primaries = {"srgb": 0, "display_p3": 1}[primaries]
+    d.policy = {"clip": 0, "chroma_compress": 1}[policy]
+    d.dither = {"none": 0, "ordered8x8": 1}[dither]
+    d.orientation = ORIENTATIONS.index(orientation)
+    if crop is not None:
+        d.has_crop = 1
+        for k in range(4):
+            d.crop[k] = crop[k]
+    d.headroom = headroom
+    return d
+
+
+def set_exact_math(on: bool) -> None:
+    """True: correctly rounded cube root and transfer power; False: the platform libm."""
+    load().ro_set_exact_math(1 if on else 0)
+
+
+def output_geometry(width: int, height: int, desc: OutputDesc):
+    """(out_width, out_height, (left, top, right, bottom)) or None for an invalid geometry."""
+    ow, oh = ctypes.c_int(), ctypes.c_int()
+    crop = (ctypes.c_int * 4)()
+    if load().ro_output_geometry(width, height, ctypes.byref(desc), ctypes.byref(ow), ctypes.byref(oh), crop) != 0:
+        return None
+    return ow.value, oh.value, tuple(crop)
+
+
+def render_output(rgb: np.ndarray, desc: OutputDesc):
+    """Adjusted linear Rec.2020 [h][3w] -> (image, gamut counts[5]); None for invalid geometry/headroom."""
+    rgb = f32(rgb)
+    h, w3 = rgb.shape
+    geo = output_geometry(w3 // 3, h, desc)
+    if geo is None:
+        return None
+    ow, oh, _ = geo
+    dtype = {0: np.uint8, 1: np.uint16, 2: np.float32}[desc.format]
+    out = np.zeros((oh, 3 * ow), dtype=dtype)
+    gamut = np.zeros(5, dtype=np.uint64)
+    if load().ro_render_output(ptr(rgb), w3 // 3, h, ctypes.byref(desc), out.ctypes.data_as(ctypes.c_void_p),
+                               ptr(gamut, ctypes.c_uint64)) != 0:
+        return None
+    return out, gamut
+
+
+GAMUT_STATUS = ("in_gamut", "compressed", "limited", "clipped_fallback", "invalid")
+
+
+def gamut_map(rgb, primaries="srgb", policy="chroma_compress", ceiling=1.0):
+    """(mapped linear rgb, status name) of one pixel in the target primaries."""
+    v = np.asarray(rgb, dtype=np.float32).copy()
+    out = np.zeros(3, dtype=np.float32)
+    st = load().ro_gamut_map(ptr(v), 1 if primaries == "display_p3" else 0, 1 if policy == "chroma_compress" else 0,
+                             ceiling, ptr(out))
+    return out, GAMUT_STATUS[st]
+
+
+def oklab(rgb, primaries="srgb", inverse=False) -> np.ndarray:
+    v = np.asarray(rgb, dtype=np.float32).copy()
+    out = np.zeros(3, dtype=np.float32)
+    fn = load().ro_oklab_inverse if inverse else load().ro_oklab
+    fn(1 if primaries == "display_p3" else 0, ptr(v), ptr(out))
+    return out

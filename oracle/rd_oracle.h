@@ -98,6 +98,32 @@ void ro_standard_base_lut(float* lut4096);
 void ro_display_srgb8(const float* rgb, size_t pixels, uint8_t* out);
 void ro_histogram(const uint8_t* rgb8, size_t pixels, uint64_t hist[4 * 256], uint64_t clipped[6]);
 
+/* ---- display / extended output (output.cpp) ---- */
+typedef struct ro_output {
+  int format;       /* 0 display u8, 1 sRGB u16, 2 extended linear f32 */
+  int primaries;    /* 0 sRGB, 1 Display P3 */
+  int policy;       /* 0 clip, 1 chroma compress */
+  int dither;       /* 0 none, 1 ordered 8x8 */
+  int orientation;  /* 0 Normal, 1 HorizontalFlip, 2 Rotate180, 3 VerticalFlip, 4 Transpose,
+                       5 Rotate90, 6 Transverse, 7 Rotate270, 8 Unknown */
+  int has_crop;
+  double crop[4];   /* normalized left, top, right, bottom on the oriented canvas */
+  float headroom;   /* extended output ceiling, finite and >= 1 */
+} ro_output;
+/* 1: correctly rounded cube root and transfer power; 0 (default): platform libm. */
+void ro_set_exact_math(int on);
+float ro_cbrt(float x);
+float ro_cbrt_correctly_rounded(float x);
+/* gamut.rs mappers on linear RGB in the target primaries; returns the status index. */
+int ro_gamut_map(const float rgb[3], int p3, int policy, float ceiling, float out[3]);
+void ro_oklab(int p3, const float rgb[3], float lab[3]);
+void ro_oklab_inverse(int p3, const float lab[3], float rgb[3]);
+int ro_output_geometry(int w, int h, const ro_output* o, int* out_w, int* out_h, int crop[4]);
+void ro_source_coordinate(int w, int h, int orientation, int x, int y, int* sx, int* sy);
+/* rgb: adjusted linear Rec.2020, interleaved. gamut = {in_gamut, compressed, limited,
+ * clipped_fallback, invalid}. Returns 0, or -1 for an invalid geometry or headroom. */
+int ro_render_output(const float* rgb, int w, int h, const ro_output* o, void* out, uint64_t gamut[5]);
+
 #ifdef __cplusplus
 }
 #endif

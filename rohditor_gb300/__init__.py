@@ -2,12 +2,13 @@
 built from csrc/ into _lib/librd_gpu.so, with a host-side mirror of the
 reference's `rohditor-gpu` processor interface."""
 
-from .processor import (CaptureContract, ColorContract, Device, GpuBase, GpuDevelopedSource, GpuPreviewError,
-                        GpuPreviewProcessor, GpuSensorProcessor, GpuSpatialProcessor, Histogram, OpticsExecution,
-                        SensorDescription, Stages, clip_levels, opposed_levels, standard_base_lut)
+from .processor import (CaptureContract, ColorContract, Device, GamutDiagnostics, GpuBase, GpuDevelopedSource,
+                        GpuPreviewError, GpuPreviewProcessor, GpuSensorProcessor, GpuSpatialProcessor, Histogram,
+                        OpticsExecution, OutputSpec, SensorDescription, Stages, clip_levels, opposed_levels,
+                        standard_base_lut)
 
 __all__ = [
-    "CaptureContract", "ColorContract", "Device", "GpuBase", "GpuDevelopedSource", "GpuPreviewError",
+    "CaptureContract", "ColorContract", "Device", "GamutDiagnostics", "GpuBase", "GpuDevelopedSource", "GpuPreviewError",
     "GpuPreviewProcessor", "GpuSensorProcessor", "GpuSpatialProcessor", "Histogram", "OpticsExecution",
-    "SensorDescription", "Stages", "clip_levels", "opposed_levels", "standard_base_lut",
+    "OutputSpec", "SensorDescription", "Stages", "clip_levels", "opposed_levels", "standard_base_lut",
 ]

@@ -128,6 +128,22 @@ class ServerStats(ctypes.Structure):
 
 
 # Every exported symbol of include/rd_gpu.h with its ctypes signature.
+class OutputDesc(ctypes.Structure):
+    _fields_ = [
+        ("format", ctypes.c_int32), ("primaries", ctypes.c_int32), ("policy", ctypes.c_int32),
+        ("dither", ctypes.c_int32), ("orientation", ctypes.c_int32), ("has_crop", ctypes.c_int32),
+        ("crop", ctypes.c_double * 4), ("headroom", ctypes.c_float),
+    ]
+
+
+OUTPUT_FORMAT = {"srgb8": 0, "srgb16": 1, "extended_f32": 2, "extended_f16": 3}
+PRIMARIES = {"srgb": 0, "display_p3": 1}
+OUTPUT_POLICY = {"clip": 0, "chroma_compress": 1}
+DITHER = {"none": 0, "ordered8x8": 1}
+ORIENTATION = {"normal": 0, "horizontal_flip": 1, "rotate180": 2, "vertical_flip": 3, "transpose": 4,
+               "rotate90": 5, "transverse": 6, "rotate270": 7, "unknown": 8}
+GAMUT_STATUS = ("in_gamut", "compressed", "limited", "clipped_fallback", "invalid")
+
 SIGNATURES = {
     "rd_status_is_routing": (ctypes.c_int, [ctypes.c_int]),
     "rd_status_name": (ctypes.c_char_p, [ctypes.c_int]),
@@ -151,6 +167,16 @@ SIGNATURES = {
     "rd_render_device": (ctypes.c_int, [VOIDP, VOIDP, ctypes.POINTER(ColorDesc), ctypes.POINTER(Metrics)]),
     "rd_render_device_noalloc": (ctypes.c_int, [VOIDP, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ColorDesc),
                                                 VOIDP, VOIDP, VOIDP]),
+    "rd_output_dimensions": (ctypes.c_int, [ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(OutputDesc),
+                                            ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32),
+                                            ctypes.POINTER(ctypes.c_uint32)]),
+    "rd_render_output": (ctypes.c_int, [VOIDP, VOIDP, ctypes.POINTER(ColorDesc), ctypes.POINTER(OutputDesc), VOIDP,
+                                        ctypes.c_size_t, U64P, U64P, ctypes.POINTER(Metrics)]),
+    "rd_render_output_device": (ctypes.c_int, [VOIDP, VOIDP, ctypes.POINTER(ColorDesc), ctypes.POINTER(OutputDesc),
+                                               VOIDP, VOIDP, VOIDP, ctypes.POINTER(Metrics)]),
+    "rd_check_math": (ctypes.c_int, [VOIDP, ctypes.c_int32, U64P]),
+    "rd_stage_output": (ctypes.c_int, [VOIDP, F32P, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ColorDesc),
+                                       ctypes.POINTER(OutputDesc), VOIDP, ctypes.c_size_t, U64P, U64P]),
     "rd_source_dimensions": (ctypes.c_int, [VOIDP, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32)]),
     "rd_source_download": (ctypes.c_int, [VOIDP, VOIDP, F32P]),
     "rd_base_dimensions": (ctypes.c_int, [VOIDP, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32)]),

@@ -52,7 +52,7 @@ const char* kernel_family_name(int family) {
   static const char* names[K_FAMILY_COUNT] = {
       "normalize", "opposed", "mhc_bilinear", "rcd", "amaze", "rl_init", "rl_mask", "rl_iteration",
       "rl_apply", "vignetting", "optics_gather", "area_horizontal", "area_vertical", "wb_matrix",
-      "color_output", "synth"};
+      "color_output", "synth", "display_output"};
   return family >= 0 && family < K_FAMILY_COUNT ? names[family] : "unknown";
 }
 
@@ -738,6 +738,110 @@ rd_status rd_render(rd_ctx* h, const rd_base* cbase, const rd_color_desc* color,
   return finish(h, st);
 }
 
+rd_status rd_output_dimensions(uint32_t width, uint32_t height, const rd_output_desc* output, uint32_t* out_width,
+                               uint32_t* out_height, uint32_t* bytes_per_pixel) {
+  if (!output || !out_width || !out_height) return RD_INVALID_INPUT;
+  if (width == 0 || height == 0 || width > (uint32_t)INT32_MAX || height > (uint32_t)INT32_MAX)
+    return RD_INVALID_DIMENSIONS;
+  rd::OutputGeometry g;
+  const Status st = rd::resolve_output_geometry((int)width, (int)height, *output, &g);
+  if (!st.ok()) return st.code;
+  *out_width = (uint32_t)g.width;
+  *out_height = (uint32_t)g.height;
+  if (bytes_per_pixel) *bytes_per_pixel = (uint32_t)rd::output_bytes_per_pixel(output->format);
+  return RD_OK;
+}
+
+rd_status rd_render_output_device(rd_ctx* h, const rd_base* base, const rd_color_desc* color,
+                                  const rd_output_desc* output, void* d_out, uint64_t* d_hist, uint64_t* d_gamut,
+                                  rd_metrics* metrics) {
+  if (!h || !base || !color || !output || !d_out) return finish(h, Status{RD_INVALID_INPUT, "null argument"});
+  if (base->ctx != h) return finish(h, Status{RD_BASE_MISMATCH, "base belongs to another context"});
+  rd::Context& ctx = h->c;
+  cudaSetDevice(ctx.device);
+  rd::OutputGeometry g;
+  Status st = rd::resolve_output_geometry(base->W, base->H, *output, &g);
+  if (st.ok() && d_hist && output->format != RD_OUTPUT_SRGB8)
+    st = Status{RD_INVALID_INPUT, "the histogram is counted on the 8-bit output only"};
+  if (!st.ok()) return finish(h, st);
+  Timer tm(ctx);
+  tm.mark();
+  st = rd::run_display_output(ctx, base->rgb, *color, *output, g, d_out,
+                              reinterpret_cast<unsigned long long*>(d_hist),
+                              reinterpret_cast<unsigned long long*>(d_gamut));
+  tm.mark();
+  if (st.ok()) st = rd::check_kernel_error(ctx, "output");
+  if (st.ok() && metrics) {
+    metrics->color_ms = tm.span(0, 1);
+    metrics->total_ms = metrics->color_ms;
+    metrics->kernel_launches = ctx.launches;
+  }
+  return finish(h, st);
+}
+
+// Device output + readback into host buffers. The device output, histogram and
+// counters share one allocation of the context.
+static Status render_output_host(rd_ctx* h, const float* d_rgb, int W, int H, const rd_color_desc& color,
+                                 const rd_output_desc& output, void* out, size_t out_capacity, uint64_t* hist,
+                                 uint64_t* gamut, float* color_ms) {
+  rd::Context& ctx = h->c;
+  rd::OutputGeometry g;
+  RD_TRY(rd::resolve_output_geometry(W, H, output, &g));
+  if (hist && output.format != RD_OUTPUT_SRGB8)
+    return Status{RD_INVALID_INPUT, "the histogram is counted on the 8-bit output only"};
+  const size_t out_bytes = (size_t)g.width * g.height * rd::output_bytes_per_pixel(output.format);
+  if (out_capacity < out_bytes) return Status{RD_INVALID_DIMENSIONS, "output buffer is smaller than the output"};
+  const size_t counters = 1024 + 8;  // histogram, gamut counters (padded)
+  const size_t total = counters * sizeof(unsigned long long) + out_bytes;
+  void* p = nullptr;
+  RD_TRY(rd::device_alloc(ctx, total, &p));
+  unsigned long long* d_hist = static_cast<unsigned long long*>(p);
+  unsigned long long* d_gamut = d_hist + 1024;
+  void* d_out = d_hist + counters;
+  Timer tm(ctx);
+  tm.mark();
+  Status st = rd::run_display_output(ctx, d_rgb, color, output, g, d_out, hist ? d_hist : nullptr, d_gamut);
+  tm.mark();
+  uint64_t bins[1024];
+  uint64_t diag[5];
+  if (st.ok() && (cudaMemcpyAsync(out, d_out, out_bytes, cudaMemcpyDeviceToHost, ctx.stream) != cudaSuccess ||
+                  cudaMemcpyAsync(diag, d_gamut, sizeof(diag), cudaMemcpyDeviceToHost, ctx.stream) != cudaSuccess ||
+                  (hist && cudaMemcpyAsync(bins, d_hist, sizeof(bins), cudaMemcpyDeviceToHost, ctx.stream) !=
+                               cudaSuccess)))
+    st = Status{RD_READBACK, "output readback failed"};
+  if (st.ok() && cudaStreamSynchronize(ctx.stream) != cudaSuccess) st = Status{RD_READBACK, "readback failed"};
+  if (st.ok()) st = rd::check_kernel_error(ctx, "output");
+  if (st.ok()) {
+    if (hist) std::memcpy(hist, bins, sizeof(bins));
+    if (gamut) std::memcpy(gamut, diag, sizeof(diag));
+    if (color_ms) *color_ms = tm.span(0, 1);
+  }
+  rd::device_free(ctx, p, total);
+  return st;
+}
+
+rd_status rd_render_output(rd_ctx* h, const rd_base* base, const rd_color_desc* color, const rd_output_desc* output,
+                           void* out, size_t out_capacity, uint64_t* hist, uint64_t* gamut, rd_metrics* metrics) {
+  if (!h || !base || !color || !output || !out) return finish(h, Status{RD_INVALID_INPUT, "null argument"});
+  if (base->ctx != h) return finish(h, Status{RD_BASE_MISMATCH, "base belongs to another context"});
+  cudaSetDevice(h->c.device);
+  float ms = 0.0f;
+  const Status st = render_output_host(h, base->rgb, base->W, base->H, *color, *output, out, out_capacity, hist,
+                                       gamut, &ms);
+  if (st.ok() && metrics) {
+    metrics->color_ms = ms;
+    metrics->total_ms = ms;
+    metrics->kernel_launches = h->c.launches;
+  }
+  return finish(h, st);
+}
+
+rd_status rd_check_math(rd_ctx* h, int32_t which, uint64_t* result) {
+  if (!h || !result || (which != 0 && which != 1)) return finish(h, Status{RD_INVALID_INPUT, "bad argument"});
+  cudaSetDevice(h->c.device);
+  return finish(h, rd::run_math_check(h->c, which, result));
+}
+
 rd_status rd_source_dimensions(const rd_source* s, uint32_t* w, uint32_t* hgt) {
   if (!s || !w || !hgt) return RD_INVALID_INPUT;
   *w = (uint32_t)s->W;
@@ -1054,6 +1158,23 @@ rd_status rd_stage_color(rd_ctx* h, const float* rgb_in, uint32_t W, uint32_t H,
   }
   if (d) rd::device_free(ctx, d, bytes);
   if (p) rd::device_free(ctx, p, out_bytes);
+  cudaStreamSynchronize(ctx.stream);
+  return finish(h, st);
+}
+
+rd_status rd_stage_output(rd_ctx* h, const float* rgb_in, uint32_t W, uint32_t H, const rd_color_desc* color,
+                          const rd_output_desc* output, void* out, size_t out_capacity, uint64_t* hist,
+                          uint64_t* gamut) {
+  if (!h || !rgb_in || !color || !output || !out) return finish(h, Status{RD_INVALID_INPUT, "null argument"});
+  if (W == 0 || H == 0 || W > (uint32_t)INT32_MAX || H > (uint32_t)INT32_MAX)
+    return finish(h, Status{RD_INVALID_DIMENSIONS, "empty image"});
+  rd::Context& ctx = h->c;
+  cudaSetDevice(ctx.device);
+  float* d = nullptr;
+  size_t bytes = 0;
+  Status st = upload_planar(ctx, rgb_in, (int)W, (int)H, &d, &bytes);
+  if (st.ok()) st = render_output_host(h, d, (int)W, (int)H, *color, *output, out, out_capacity, hist, gamut, nullptr);
+  if (d) rd::device_free(ctx, d, bytes);
   cudaStreamSynchronize(ctx.stream);
   return finish(h, st);
 }

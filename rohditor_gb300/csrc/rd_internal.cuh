@@ -42,7 +42,7 @@ struct Status {
 // Kernel families timed by the optional per-launch event bracketing.
 enum KernelFamily {
   K_NORMALIZE, K_OPPOSED, K_MHC, K_RCD, K_AMAZE, K_RL_INIT, K_RL_MASK, K_RL_ITER, K_RL_APPLY, K_VIGNETTE,
-  K_OPTICS, K_AREA_H, K_AREA_V, K_WB_MATRIX, K_COLOR, K_SYNTH, K_FAMILY_COUNT
+  K_OPTICS, K_AREA_H, K_AREA_V, K_WB_MATRIX, K_COLOR, K_SYNTH, K_OUTPUT, K_FAMILY_COUNT
 };
 static_assert(K_FAMILY_COUNT == RD_KERNEL_FAMILIES, "family table size");
 const char* kernel_family_name(int family);
@@ -216,6 +216,24 @@ struct ColorBatchItem {
 };
 size_t color_batch_staging_bytes(int n);
 Status run_color_batch(Context& ctx, const ColorBatchItem* items, int n, void* d_staging, void* h_staging);
+
+// Display / extended output (k_output.cu). The geometry is OutputGeometry of
+// the reference resolved on the host: the axis swap and mirrors of the
+// orientation, and the crop rectangle on the oriented canvas.
+struct OutputGeometry {
+  int swap, flip_h, flip_v;
+  int src_w, src_h;
+  int left, top, width, height;  // crop origin and output size
+};
+size_t output_bytes_per_pixel(int format);  // 0 for an unknown format
+Status resolve_output_geometry(int width, int height, const rd_output_desc& output, OutputGeometry* g);
+// rgb: planar linear Rec.2020 of g.src_w x g.src_h. d_hist (1024 bins, 8-bit
+// output only) and d_gamut (5 counters) may be null; both are cleared first.
+Status run_display_output(Context& ctx, const float* rgb, const rd_color_desc& color, const rd_output_desc& output,
+                          const OutputGeometry& g, void* d_out, unsigned long long* d_hist,
+                          unsigned long long* d_gamut);
+// Exhaustive device checks of the correctly rounded arithmetic (rd_check_math).
+Status run_math_check(Context& ctx, int which, uint64_t* result);
 
 // Host contract helpers.
 int gaussian_kernel(float sigma, float* weights, int max_taps);

@@ -211,6 +211,63 @@ class ColorContract:
         return d
 
 
+@dataclass
+class OutputSpec:
+    """Output conversion of a render: format, target primaries, gamut policy,
+    dither and OutputGeometry (orientation + normalized crop on the oriented
+    canvas). Formats: "srgb8", "srgb16", "extended_f32", "extended_f16"."""
+
+    format: str = "srgb8"
+    primaries: str = "srgb"
+    policy: str = "clip"
+    dither: str = "none"
+    orientation: str = "normal"
+    crop: tuple[float, float, float, float] | None = None
+    headroom: float = 1.0
+
+    def to_c(self) -> _ffi.OutputDesc:
+        d = _ffi.OutputDesc()
+        d.format = _ffi.OUTPUT_FORMAT[self.format]
+        d.primaries = _ffi.PRIMARIES[self.primaries]
+        d.policy = _ffi.OUTPUT_POLICY[self.policy]
+        d.dither = _ffi.DITHER[self.dither]
+        d.orientation = _ffi.ORIENTATION[self.orientation]
+        if self.crop is not None:
+            d.has_crop = 1
+            for k in range(4):
+                d.crop[k] = self.crop[k]
+        d.headroom = self.headroom
+        return d
+
+    @property
+    def dtype(self):
+        return {"srgb8": np.uint8, "srgb16": np.uint16, "extended_f32": np.float32,
+                "extended_f16": np.float16}[self.format]
+
+    def dimensions(self, width: int, height: int) -> tuple[int, int]:
+        ow, oh, bpp = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+        rc = _ffi.load().rd_output_dimensions(width, height, ctypes.byref(self.to_c()), ctypes.byref(ow),
+                                              ctypes.byref(oh), ctypes.byref(bpp))
+        if rc != 0:
+            raise GpuPreviewError(rc, "invalid output description")
+        return ow.value, oh.value
+
+
+@dataclass
+class GamutDiagnostics:
+    """GamutMappingDiagnostics (crates/color/src/gamut.rs:60-98)."""
+
+    in_gamut: int
+    compressed: int
+    limited: int
+    clipped_fallback: int
+    invalid: int
+
+    @property
+    def total(self) -> int:
+        return self.in_gamut + self.compressed + self.limited + self.clipped_fallback + self.invalid
+
+
 def standard_base_lut() -> np.ndarray:
     """BaseRenderingLut::standard_v1 values (crates/core/src/rendering.rs:36-50)."""
     out = np.zeros(4096, dtype=np.float32)
@@ -401,6 +458,24 @@ class GpuPreviewProcessor:
             _ptr(clipped, ctypes.c_uint64), None))
         return out, Histogram(hist[0:256], hist[256:512], hist[512:768], hist[768:1024], clipped[:3], clipped[3:])
 
+    def render_output(self, base: GpuBase, color: ColorContract, output: OutputSpec,
+                      histogram: bool = False) -> tuple[np.ndarray, Histogram | None, GamutDiagnostics]:
+        """Display / extended output of the base: [out_h][3*out_w] of output.dtype."""
+        ow, oh = output.dimensions(base.width, base.height)
+        out = np.empty((oh, 3 * ow), dtype=output.dtype)
+        hist = np.zeros(1024, dtype=np.uint64) if histogram else None
+        gamut = np.zeros(5, dtype=np.uint64)
+        self.device.check(self.device.lib.rd_render_output(
+            self.device.handle, base.handle, ctypes.byref(color.to_c()), ctypes.byref(output.to_c()),
+            out.ctypes.data_as(ctypes.c_void_p), out.nbytes, _ptr(hist, ctypes.c_uint64) if hist is not None else None,
+            _ptr(gamut, ctypes.c_uint64), None))
+        h = None
+        if hist is not None:
+            clipped = np.array([hist[256 * c] for c in range(3)] + [hist[256 * c + 255] for c in range(3)],
+                               dtype=np.uint64)
+            h = Histogram(hist[0:256], hist[256:512], hist[512:768], hist[768:1024], clipped[:3], clipped[3:])
+        return out, h, GamutDiagnostics(*(int(v) for v in gamut))
+
     def render_device(self, base: GpuBase, color_c: _ffi.ColorDesc):
         self.device.check(self.device.lib.rd_render_device(self.device.handle, base.handle, ctypes.byref(color_c), None))
 
@@ -473,6 +548,27 @@ class Stages:
         self.device.check(self.lib.rd_stage_area_reduce(self.device.handle, _ptr(rgb, ctypes.c_float), w3 // 3, h,
                                                         target[0], target[1], _ptr(out, ctypes.c_float)))
         return out
+
+    def output(self, rgb: np.ndarray, color: ColorContract, output: OutputSpec,
+               histogram: bool = False) -> tuple[np.ndarray, np.ndarray | None, np.ndarray]:
+        """Linear Rec.2020 [h][3w] -> adjustments -> output: (image, 1024 bins or None, gamut counts[5])."""
+        rgb = _f32(rgb)
+        h, w3 = rgb.shape
+        ow, oh = output.dimensions(w3 // 3, h)
+        out = np.empty((oh, 3 * ow), dtype=output.dtype)
+        hist = np.zeros(1024, dtype=np.uint64) if histogram else None
+        gamut = np.zeros(5, dtype=np.uint64)
+        self.device.check(self.lib.rd_stage_output(
+            self.device.handle, _ptr(rgb, ctypes.c_float), w3 // 3, h, ctypes.byref(color.to_c()),
+            ctypes.byref(output.to_c()), out.ctypes.data_as(ctypes.c_void_p), out.nbytes,
+            _ptr(hist, ctypes.c_uint64) if hist is not None else None, _ptr(gamut, ctypes.c_uint64)))
+        return out, hist, gamut
+
+    def check_math(self, which: int) -> int:
+        """rd_check_math: 0 -> cube roots not correctly rounded; 1 -> largest powf distance in ulps."""
+        v = ctypes.c_uint64()
+        self.device.check(self.lib.rd_check_math(self.device.handle, which, ctypes.byref(v)))
+        return v.value
 
     def color(self, rgb: np.ndarray, color: ColorContract) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
         rgb = _f32(rgb)
