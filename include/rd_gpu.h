@@ -264,7 +264,9 @@ rd_status rd_render_output_device(rd_ctx* ctx, const rd_base* base, const rd_col
  * f32 whose cube root is not correctly rounded (or not odd-symmetric), exact
  * integer comparison, expected 0. which = 1: the largest distance in ulps of
  * powf(x, 1/2.4) from the correctly rounded power over (0.0031308, 1], which
- * must not exceed the bound the 8- and 16-bit quantisation relies on (2). */
+ * must not exceed the bound the 8- and 16-bit quantisation relies on (1).
+ * which = 2: the number of f32 in (0.0031308, 1] whose transfer power (as the
+ * quantisation computes it) differs from the correctly rounded one, expected 0. */
 rd_status rd_check_math(rd_ctx* ctx, int32_t which, uint64_t* result);
 
 rd_status rd_source_dimensions(const rd_source* source, uint32_t* width, uint32_t* height);

@@ -30,8 +30,10 @@ __device__ __forceinline__ float sstep(float e0, float e1, float v) {
   n = n < 0.0f ? 0.0f : (n > 1.0f ? 1.0f : n);
   return n * n * (3.0f - 2.0f * n);
 }
+// f32::rem_euclid. fmod(x, m) is x itself when |x| < |m| (the common case
+// for hues), so fmodf runs only outside that range.
 __device__ __forceinline__ float rem_euclid(float x, float m) {
-  const float r = fmodf(x, m);
+  const float r = fabsf(x) < fabsf(m) ? x : fmodf(x, m);
   return r < 0.0f ? r + fabsf(m) : r;
 }
 __device__ __forceinline__ float rmax(float a, float b) {
@@ -122,7 +124,11 @@ __device__ void hsl_to_rgb(float h, float s, float l, float* out) {
   if (s <= F32_EPS) { out[0] = out[1] = out[2] = l; return; }
   const float chroma = (1.0f - fabsf(2.0f * l - 1.0f)) * s;
   const float hp = h * 6.0f;
-  const float sec = chroma * (1.0f - fabsf(rem_euclid(hp, 2.0f) - 1.0f));
+  // rem_euclid(hp, 2): for hp in [0, 6) the remainder hp - 2k is exact
+  // (Sterbenz), as fmodf's is.
+  const float rem = (hp >= 0.0f && hp < 6.0f) ? (hp < 2.0f ? hp : (hp < 4.0f ? hp - 2.0f : hp - 4.0f))
+                                              : rem_euclid(hp, 2.0f);
+  const float sec = chroma * (1.0f - fabsf(rem - 1.0f));
   float r, g, b;
   if (hp < 1.0f) { r = chroma; g = sec; b = 0.0f; }
   else if (hp < 2.0f) { r = sec; g = chroma; b = 0.0f; }
@@ -151,23 +157,27 @@ __device__ void apply_hsl(float* p, const float (*hsl)[3]) {
   float hue = hv[0], sat = hv[1], light = hv[2];
   const float cw = sstep(0.0f, 0.05f, sat);
   if (cw <= F32_EPS) return;
-  float w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  // The two bands around the hue get weights 1 - f and f, every other band 0
+  // (selected per band, so the weights stay in registers).
+  int left = -1, right = -1;
+  float fraction = 0.0f;
   if (isfinite(hue)) {
     const float hh = rem_euclid(hue, 1.0f);
-    int left = 7, right = 0;
+    left = 7;
+    right = 0;
     float start = HSL_CENTERS[7], end = 1.0f;
     for (int k = 0; k < 7; ++k)
       if (hh >= HSL_CENTERS[k] && hh < HSL_CENTERS[k + 1]) {
         left = k; right = k + 1; start = HSL_CENTERS[k]; end = HSL_CENTERS[k + 1];
         break;
       }
-    const float fraction = rclamp((hh - start) / (end - start), 0.0f, 1.0f);
-    w[left] = 1.0f - fraction;
-    w[right] = fraction;
+    fraction = rclamp((hh - start) / (end - start), 0.0f, 1.0f);
   }
   float hs = 0.0f, ss = 0.0f, ls = 0.0f;
+#pragma unroll
   for (int k = 0; k < 8; ++k) {
-    const float wt = w[k] * cw;
+    const float wk = k == left ? 1.0f - fraction : (k == right ? fraction : 0.0f);
+    const float wt = wk * cw;
     hs += hsl[k][0] * 0.125f * wt;
     ss += hsl[k][1] * 0.5f * wt;
     ls += hsl[k][2] * 0.25f * wt;
@@ -252,10 +262,74 @@ __device__ __forceinline__ void apply_adjustments(const AdjustParams& a, float* 
   if (a.has_grading) apply_grading(v, a.grading);
 }
 
+// ---- float-float arithmetic (error-free transformations) -------------------
+// A pair (hi, lo) stands for hi + lo with |lo| <= ulp(hi) / 2. two_prod is
+// exact (Dekker / FMA); the products below lose at most a few units of 2^-48
+// relative. The library is compiled without FMA contraction, so every fmaf
+// here is explicit and every other product is rounded on its own.
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ FF two_prod(float a, float b) {
+  const float p = a * b;
+  return FF{p, fmaf(a, b, -p)};
+}
+__device__ __forceinline__ FF fast_two_sum(float a, float b) {
+  const float s = a + b;
+  return FF{s, b - (s - a)};
+}
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+  const FF p = two_prod(a.hi, b.hi);
+  return fast_two_sum(p.hi, p.lo + (a.hi * b.lo + a.lo * b.hi));
+}
+__device__ __forceinline__ FF ff_mul_f(FF a, float b) {
+  const FF p = two_prod(a.hi, b);
+  return fast_two_sum(p.hi, p.lo + a.lo * b);
+}
+__device__ __forceinline__ float next_up(float r) { return __int_as_float(__float_as_int(r) + 1); }
+__device__ __forceinline__ float next_down(float r) { return __int_as_float(__float_as_int(r) - 1); }
+
+// ---- correctly rounded sRGB transfer power -----------------------------------
 // Largest distance, in ulps, of powf(x, 1/2.4) from the correctly rounded
-// power over the sRGB transfer's domain (0.0031308, 1]; the exhaustive device
-// check of the library (rd_check_math) asserts it.
-constexpr int TRANSFER_POW_ULPS = 2;
+// power over the transfer's domain (0.0031308, 1]; the exhaustive device check
+// of the library (rd_check_math) asserts it.
+constexpr int TRANSFER_POW_ULPS = 1;
+
+// Which side of m = r + h does x^e lie on, e = 1/2.4 rounded to f32?
+// e = 5/12 - 2^-23/12 exactly, so x^e > m  <=>  x^5 > m^12 * x^(2^-23), and
+// x^(2^-23) = 1 + w + w^2/2 + O(w^3) with w = 2^-23 ln x, |w| < 7e-7. Both
+// sides are formed in float-float; their relative error stays below 2^-41, so
+// a difference above 2^-38 decides. Returns +1 (above), -1 (below) or 0 (too
+// close to call: the true power is within about 2^-41 of the midpoint).
+__device__ __forceinline__ int transfer_side(float x, float r, float h) {
+  const FF x2 = two_prod(x, x);
+  const FF q = ff_mul_f(ff_mul(x2, x2), x);
+  const FF m{r, h};
+  const FF m2 = ff_mul(m, m);
+  const FF m4 = ff_mul(m2, m2);
+  const FF m12 = ff_mul(ff_mul(m4, m4), m4);
+  const float w = logf(x) * 1.1920928955078125e-7f;  // exact scaling by 2^-23
+  const float c = w + 0.5f * w * w;
+  const FF p = fast_two_sum(m12.hi, m12.lo + m12.hi * c);
+  const float d = (q.hi - p.hi) + (q.lo - p.lo);  // q.hi - p.hi is exact (Sterbenz)
+  const float eps = q.hi * 3.637978807091713e-12f;  // 2^-38
+  return d > eps ? 1 : (d < -eps ? -1 : 0);
+}
+
+// x^e for x in (0.0031308, 1] correctly rounded to f32: powf, moved by one ulp
+// where the exact midpoint test says so, in double where it cannot tell.
+__device__ __forceinline__ float transfer_pow_rn(float x) {
+  const float e = 1.0f / 2.4f;
+  const float r = powf(x, e);
+  const float up = next_up(r), down = next_down(r);
+  const int above = transfer_side(x, r, (up - r) * 0.5f);
+  if (above > 0) return up;
+  if (above == 0) return (float)pow((double)x, (double)e);
+  const int below = transfer_side(x, r, (down - r) * 0.5f);
+  if (below < 0) return down;
+  if (below == 0) return (float)pow((double)x, (double)e);
+  return r;
+}
 
 __device__ __forceinline__ float transfer_code(float r, float scale, float dither) {
   return roundf((1.055f * r - 0.055f) * scale + dither);
@@ -263,30 +337,54 @@ __device__ __forceinline__ float transfer_code(float r, float scale, float dithe
 
 // linear_srgb_to_srgb (crates/color/src/transfer.rs:5-11) followed by the
 // quantisation (encoded * scale + dither).round().clamp(0, scale) of
-// stages.rs:1085-1087 and :1181-1183, for `lin` already in [0, 1].
+// stages.rs:1085-1087 and :1181-1183, for the three channels of a pixel
+// already in [0, 1], with the power correctly rounded.
 //
-// The code is a monotone function of the power r = lin^(1/2.4). powf is within
-// TRANSFER_POW_ULPS of the correctly rounded power, so when the codes of the
-// two ends of that interval agree, so does the code of the correctly rounded
-// power; otherwise the power is recomputed in double and rounded once to f32,
-// which gives the correctly rounded value. The result is then the code of the
-// correctly rounded transfer, whatever powf's own rounding.
-__device__ __forceinline__ float quantize_srgb(float lin, float scale, float dither) {
-  float code;
-  if (lin <= 0.0031308f) {
-    code = roundf(12.92f * lin * scale + dither);
-  } else {
-    const float e = 1.0f / 2.4f;
-    float r = powf(lin, e);
-    code = transfer_code(r, scale, dither);
-    const float lo = __int_as_float(__float_as_int(r) - TRANSFER_POW_ULPS);
-    const float hi = __int_as_float(__float_as_int(r) + TRANSFER_POW_ULPS);
-    if (transfer_code(lo, scale, dither) != transfer_code(hi, scale, dither)) {
-      r = (float)pow((double)lin, (double)e);
-      code = transfer_code(r, scale, dither);
+// The code is a monotone function of the power r, and powf is within one ulp
+// of the correctly rounded power. When the codes of powf's result one ulp
+// down and one ulp up agree, that is the code. Otherwise one boundary lies
+// between them, and the side of the midpoint on that boundary's side decides
+// between two codes (transfer_side, double only when it cannot tell). The
+// pixel's undecided channels are resolved in one loop, so a warp pays the
+// decision once per pixel, not once per channel.
+__device__ __forceinline__ void quantize_srgb3(const float* lin, float scale, float dither, float* code) {
+  const float e = 1.0f / 2.4f;
+  float r[3];
+  unsigned undecided = 0, upward = 0;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    if (lin[c] <= 0.0031308f) {
+      code[c] = roundf(12.92f * lin[c] * scale + dither);
+      r[c] = 0.0f;
+    } else {
+      r[c] = powf(lin[c], e);
+      code[c] = transfer_code(r[c], scale, dither);
+      const float lo = transfer_code(next_down(r[c]), scale, dither);
+      const float hi = transfer_code(next_up(r[c]), scale, dither);
+      if (lo != hi) {
+        undecided |= 1u << c;
+        if (code[c] == lo) upward |= 1u << c;  // the boundary is above r
+      }
     }
   }
-  return rclamp(code, 0.0f, scale);
+  while (undecided) {
+    const int c = __ffs(undecided) - 1;
+    undecided &= undecided - 1;
+    const float x = c == 0 ? lin[0] : (c == 1 ? lin[1] : lin[2]);
+    const float rc = c == 0 ? r[0] : (c == 1 ? r[1] : r[2]);
+    const bool up = (upward >> c) & 1u;
+    const float nb = up ? next_up(rc) : next_down(rc);
+    const int side = transfer_side(x, rc, (nb - rc) * 0.5f);
+    float rr = rc;
+    if (side == 0) rr = (float)pow((double)x, (double)e);
+    else if (up ? side > 0 : side < 0) rr = nb;
+    const float q = transfer_code(rr, scale, dither);
+    if (c == 0) code[0] = q;
+    else if (c == 1) code[1] = q;
+    else code[2] = q;
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) code[c] = rclamp(code[c], 0.0f, scale);
 }
 
 // Scalar adjustment parameters of a colour description; the caller stages the

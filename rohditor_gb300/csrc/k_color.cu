@@ -53,16 +53,19 @@ __device__ __forceinline__ void color_pixel(const ColorParams& p, long long i, l
     v[2] = p.m[6] * a + p.m[7] * b + p.m[8] * c;
   }
   apply_adjustments(p.adj, v);
-  unsigned char q[3];
+  float lin[3];
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
-    float lin = p.out_m[3 * r] * v[0] + p.out_m[3 * r + 1] * v[1] + p.out_m[3 * r + 2] * v[2];
-    if (isnan(lin) || lin == -INFINITY) lin = 0.0f;
-    else if (lin == INFINITY) lin = 1.0f;
-    else lin = rclamp(lin, 0.0f, 1.0f);
-    // (encoded * 255 + dither).round().clamp(0, 255) with DitherMode::None.
-    q[r] = (unsigned char)quantize_srgb(lin, 255.0f, 0.0f);
+    float l = p.out_m[3 * r] * v[0] + p.out_m[3 * r + 1] * v[1] + p.out_m[3 * r + 2] * v[2];
+    if (isnan(l) || l == -INFINITY) l = 0.0f;
+    else if (l == INFINITY) l = 1.0f;
+    else l = rclamp(l, 0.0f, 1.0f);
+    lin[r] = l;
   }
+  // (encoded * 255 + dither).round().clamp(0, 255) with DitherMode::None.
+  float code[3];
+  quantize_srgb3(lin, 255.0f, 0.0f, code);
+  const unsigned char q[3] = {(unsigned char)code[0], (unsigned char)code[1], (unsigned char)code[2]};
   const long long y = i / p.W, x = i % p.W;
   unsigned char* o = p.out + y * 3 * p.W + 3 * x;
   o[0] = q[0];

@@ -24,7 +24,7 @@
 // which is not correctly rounded (glibc 2.39's cbrtf misses on about one f32
 // in ten). This file computes both correctly rounded: the cube root by one
 // Newton step in double from cbrtf followed by an exact midpoint test, the
-// transfer through quantize_srgb (color_chain.cuh).
+// transfer through quantize_srgb3 (color_chain.cuh).
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -44,17 +44,22 @@ enum : int { FMT_U8 = RD_OUTPUT_SRGB8, FMT_U16 = RD_OUTPUT_SRGB16, FMT_F32 = RD_
 enum : int { ST_IN_GAMUT = 0, ST_COMPRESSED = 1, ST_LIMITED = 2, ST_CLIPPED_FALLBACK = 3, ST_INVALID = 4 };
 
 // ------------------------------------------------------------ cube root
-// Correctly rounded cube root of an f32. cbrtf gives an estimate y0 within a
-// few ulps; one Newton step for y^3 = x, with the residual x - y0^3 formed in
-// double (y0*y0 is exact there), leaves an error far below half an f32 ulp.
-// Rounding that to f32 can only miss on the side of the midpoint between the
-// result and its neighbour towards the double value, and the sign of
-// m^3 - x at that midpoint m is computed exactly: m*m is exact in double, the
-// product with m is split into hi + lo by an FMA (Dekker's TwoProduct), and
-// hi - x is exact because hi and x agree to within a factor of two.
-__device__ __forceinline__ float cbrt_rn(float x) {
-  if (x == 0.0f || !isfinite(x)) return x;
-  const float ax = fabsf(x);
+// Correctly rounded cube root of an f32.
+//
+// cbrtf's estimate r is within an ulp. The side of the midpoint m = r +- ulp/2
+// that the true root lies on is the sign of x - m^3, with m^3 formed in
+// float-float (relative error below 2^-44): a difference above 2^-40 x
+// decides, and r moves to its neighbour when the root lies beyond the
+// midpoint. Inputs outside [2^-60, 2^60] are scaled by 2^-+90 first (exact,
+// and the root scales by 2^-+30) so that no low part of the float-float
+// arithmetic underflows. Only when the root is within about 2^-42 of a
+// midpoint (about one input in 10^5) does the double method below decide.
+
+// Double method: one Newton step for y^3 = x from cbrtf, then the exact sign
+// of m^3 - x at the midpoint towards the double value (m*m is exact in double,
+// the product with m splits into hi + lo by an FMA, and hi - x is exact
+// because hi and x agree to within a factor of two). For positive finite x.
+__device__ __noinline__ float cbrt_rn_double(float ax) {
   const double d = (double)ax;
   const float y0 = cbrtf(ax);
   const double y0d = (double)y0;
@@ -64,7 +69,7 @@ __device__ __forceinline__ float cbrt_rn(float x) {
   float r = (float)yd;
   if (yd != (double)r) {
     const bool up = yd > (double)r;
-    const float nb = __int_as_float(__float_as_int(r) + (up ? 1 : -1));
+    const float nb = up ? next_up(r) : next_down(r);
     const double m = ((double)r + (double)nb) * 0.5;
     const double m2 = m * m;
     const double hi = m2 * m;
@@ -72,7 +77,50 @@ __device__ __forceinline__ float cbrt_rn(float x) {
     const double diff = (hi - d) + lo;  // sign of m^3 - x
     if (up ? diff < 0.0 : diff > 0.0) r = nb;
   }
-  return signbit(x) ? -r : r;
+  return r;
+}
+
+// +1 when cbrt(x) > r + h, -1 when below, 0 when too close to call.
+__device__ __forceinline__ int cube_side(float x, float r, float h) {
+  const FF m{r, h};
+  const FF m3 = ff_mul(ff_mul(m, m), m);
+  const float d = (x - m3.hi) - m3.lo;             // x - m3.hi is exact (Sterbenz)
+  const float eps = x * 9.094947017729282e-13f;  // 2^-40
+  return d > eps ? 1 : (d < -eps ? -1 : 0);
+}
+
+__device__ __forceinline__ float cbrt_rn(float x) {
+  if (x == 0.0f || !isfinite(x)) return x;
+  float ax = fabsf(x), post = 1.0f;
+  if (ax < 0x1p-60f) {
+    ax *= 0x1p90f;
+    post = 0x1p-30f;
+  } else if (ax > 0x1p60f) {
+    ax *= 0x1p-90f;
+    post = 0x1p30f;
+  }
+  float r = cbrtf(ax);
+  for (int k = 0; k < 3; ++k) {
+    const float up = next_up(r);
+    const int above = cube_side(ax, r, (up - r) * 0.5f);
+    if (above > 0) {
+      r = up;
+      continue;
+    }
+    if (above == 0) {
+      r = cbrt_rn_double(ax);
+      break;
+    }
+    const float down = next_down(r);
+    const int below = cube_side(ax, r, (down - r) * 0.5f);
+    if (below < 0) {
+      r = down;
+      continue;
+    }
+    if (below == 0) r = cbrt_rn_double(ax);
+    break;
+  }
+  return copysignf(r * post, x);
 }
 
 // ------------------------------------------------------------ OkLab
@@ -144,8 +192,10 @@ __device__ __forceinline__ int clip_rgb(const float* rgb, float ceiling, float* 
 }
 // compress_chroma (gamut.rs:124-182): in-gamut pixels pass bit-exactly; the
 // rest keep their OkLab hue and (limited) lightness and lose chroma, found by
-// 16 bisection steps on the scale of the a/b pair.
-__device__ int compress_chroma(const float* rgb, int p3, float ceiling, float lightness_ceiling, float* out) {
+// 16 bisection steps on the scale of the a/b pair. The front returns -1 for a
+// pixel that needs the bisection (finite and out of gamut), which
+// compress_out_of_gamut then maps.
+__device__ __forceinline__ int compress_front(const float* rgb, float ceiling, float* out) {
   if (!fin3(rgb)) {
     sanitize3(rgb, ceiling, out);
     return ST_INVALID;
@@ -156,6 +206,9 @@ __device__ int compress_chroma(const float* rgb, int p3, float ceiling, float li
     out[2] = rgb[2];
     return ST_IN_GAMUT;
   }
+  return -1;
+}
+__device__ int compress_out_of_gamut(const float* rgb, int p3, float ceiling, float lightness_ceiling, float* out) {
   float lab[3];
   to_oklab(p3, rgb, lab);
   if (!fin3(lab)) {
@@ -164,11 +217,17 @@ __device__ int compress_chroma(const float* rgb, int p3, float ceiling, float li
   }
   const float limited = rclamp(lab[0], 0.0f, lightness_ceiling);
   const int status = limited != lab[0] ? ST_LIMITED : ST_COMPRESSED;
-  // hypot, correctly rounded: both squares are exact in double.
-  const double a2 = (double)lab[1] * (double)lab[1] + (double)lab[2] * (double)lab[2];
-  const float chroma = (float)sqrt(a2);
+  // chroma = hypot(a, b) <= 1e-6 with the hypot correctly rounded, i.e.
+  // a^2 + b^2 below (1e-6 + half an ulp)^2 = 1.0000001e-12. The f32 sum of
+  // squares is within 2^-22 of the exact one, so it decides outside a 1e-5
+  // band around the bound; inside it the squares are exact in double.
+  const float a2f = lab[1] * lab[1] + lab[2] * lab[2];
+  bool neutral;
+  if (a2f < 0.99999e-12f) neutral = true;
+  else if (a2f > 1.00001e-12f) neutral = false;
+  else neutral = (float)sqrt((double)lab[1] * (double)lab[1] + (double)lab[2] * (double)lab[2]) <= 1.0e-6f;
   float c[3];
-  if (chroma <= 1.0e-6f) {
+  if (neutral) {
     from_oklab(p3, limited, 0.0f, 0.0f, c);
     sanitize3(c, ceiling, out);
     return status;
@@ -177,7 +236,8 @@ __device__ int compress_chroma(const float* rgb, int p3, float ceiling, float li
   for (int k = 0; k < 16; ++k) {
     const float scale = (lower + upper) * 0.5f;
     from_oklab(p3, limited, lab[1] * scale, lab[2] * scale, c);
-    if (fin3(c) && in_gamut(c, ceiling)) lower = scale;
+    // in_gamut is false for NaN and infinities, so it covers the finite test.
+    if (in_gamut(c, ceiling)) lower = scale;
     else upper = scale;
   }
   from_oklab(p3, limited, lab[1] * lower, lab[2] * lower, c);
@@ -234,9 +294,9 @@ __device__ __forceinline__ void encode_pixel(const OutputParams& p, int ox, int 
   } else {
     const float scale = FMT == FMT_U16 ? 65535.0f : 255.0f;
     const float dz = p.dither ? ((float)BAYER8[oy & 7][ox & 7] + 0.5f) / 64.0f - 0.5f : 0.0f;
-    const float q0 = quantize_srgb(mapped[0], scale, dz);
-    const float q1 = quantize_srgb(mapped[1], scale, dz);
-    const float q2 = quantize_srgb(mapped[2], scale, dz);
+    float code[3];
+    quantize_srgb3(mapped, scale, dz, code);
+    const float q0 = code[0], q1 = code[1], q2 = code[2];
     if (FMT == FMT_U16) {
       unsigned short* d = static_cast<unsigned short*>(p.out) + o;
       d[0] = (unsigned short)q0;
@@ -258,27 +318,47 @@ __device__ __forceinline__ void encode_pixel(const OutputParams& p, int ox, int 
   }
 }
 
-template <int FMT, bool SWAP>
+// One CTA walks 32x32 output tiles. With chroma compression, a tile's
+// out-of-gamut pixels (which need the 16-step bisection, the bulk of the work)
+// are queued in shared memory by warp-aggregated appends and mapped in a
+// second pass over the queue, so every warp of that pass is full instead of
+// carrying the in-gamut lanes of a divergent branch.
+struct Deferred {
+  float r, g, b;
+  int xy;  // local tile coordinate: y * TILE + x
+};
+
+template <int FMT, bool SWAP, bool COMPRESS>
 __global__ void __launch_bounds__(TILE * ROWS) output_kernel(const OutputParams p) {
   __shared__ unsigned int bins[FMT == FMT_U8 ? 1024 : 1];
   __shared__ unsigned int diag[5];
   __shared__ float stage[SWAP ? 3 : 1][TILE][TILE + 1];
+  __shared__ Deferred queue[COMPRESS ? TILE * TILE : 1];
+  __shared__ int queued;
   const int tid = threadIdx.x, lane = tid & 31, row = tid >> 5;
   if (FMT == FMT_U8)
     for (int k = tid; k < 1024; k += TILE * ROWS) bins[k] = 0;
   if (tid < 5) diag[tid] = 0;
-  __syncthreads();
   unsigned int n_in = 0, n_comp = 0, n_lim = 0, n_clip = 0, n_inv = 0;
+  auto count = [&](int st) {
+    n_in += st == ST_IN_GAMUT;
+    n_comp += st == ST_COMPRESSED;
+    n_lim += st == ST_LIMITED;
+    n_clip += st == ST_CLIPPED_FALLBACK;
+    n_inv += st == ST_INVALID;
+  };
   const int tiles_x = (p.OW + TILE - 1) / TILE;
   const long long ntiles = (long long)tiles_x * ((p.OH + TILE - 1) / TILE);
   const long long plane = (long long)p.SW * p.SH;
   for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int ox0 = (int)(t % tiles_x) * TILE, oy0 = (int)(t / tiles_x) * TILE;
+    // The previous tile's staged samples and queue are consumed.
+    __syncthreads();
+    if (COMPRESS && tid == 0) queued = 0;
     if (SWAP) {
       // Output (ox, oy) reads source column top+oy of source row left+ox (both
       // mirrored as the orientation says): stage[c][ox - ox0][oy - oy0], loaded
       // with oy fastest so a warp reads along one source row.
-      __syncthreads();
       for (int k = row; k < TILE; k += ROWS) {
         const int ox = ox0 + k, oy = oy0 + lane;
         if (ox < p.OW && oy < p.OH) {
@@ -291,43 +371,66 @@ __global__ void __launch_bounds__(TILE * ROWS) output_kernel(const OutputParams 
           stage[2][k][lane] = __ldg(p.in + 2 * plane + i);
         }
       }
-      __syncthreads();
     }
+    if (SWAP || COMPRESS) __syncthreads();
     for (int k = row; k < TILE; k += ROWS) {
       const int ox = ox0 + lane, oy = oy0 + k;
-      if (ox >= p.OW || oy >= p.OH) continue;
-      float v[3];
-      if (SWAP) {
-        v[0] = stage[0][lane][k];
-        v[1] = stage[1][lane][k];
-        v[2] = stage[2][lane][k];
-      } else {
-        const int X = p.left + ox, Y = p.top + oy;
-        const int sx = p.flip_h ? p.SW - 1 - X : X;
-        const int sy = p.flip_v ? p.SH - 1 - Y : Y;
-        const long long i = (long long)sy * p.SW + sx;
-        v[0] = __ldg(p.in + i);
-        v[1] = __ldg(p.in + plane + i);
-        v[2] = __ldg(p.in + 2 * plane + i);
-      }
-      apply_adjustments(p.adj, v);
-      float lin[3];
+      const bool valid = ox < p.OW && oy < p.OH;
+      float lin[3] = {0.0f, 0.0f, 0.0f}, mapped[3];
+      int st = ST_IN_GAMUT;
+      if (valid) {
+        float v[3];
+        if (SWAP) {
+          v[0] = stage[0][lane][k];
+          v[1] = stage[1][lane][k];
+          v[2] = stage[2][lane][k];
+        } else {
+          const int X = p.left + ox, Y = p.top + oy;
+          const int sx = p.flip_h ? p.SW - 1 - X : X;
+          const int sy = p.flip_v ? p.SH - 1 - Y : Y;
+          const long long i = (long long)sy * p.SW + sx;
+          v[0] = __ldg(p.in + i);
+          v[1] = __ldg(p.in + plane + i);
+          v[2] = __ldg(p.in + 2 * plane + i);
+        }
+        apply_adjustments(p.adj, v);
 #pragma unroll
-      for (int r = 0; r < 3; ++r) lin[r] = p.m[3 * r] * v[0] + p.m[3 * r + 1] * v[1] + p.m[3 * r + 2] * v[2];
-      float mapped[3];
-      const int st = p.compress ? compress_chroma(lin, p.p3, p.ceiling, p.lightness_ceiling, mapped)
-                                : clip_rgb(lin, p.ceiling, mapped);
-      n_in += st == ST_IN_GAMUT;
-      n_comp += st == ST_COMPRESSED;
-      n_lim += st == ST_LIMITED;
-      n_clip += st == ST_CLIPPED_FALLBACK;
-      n_inv += st == ST_INVALID;
-      encode_pixel<FMT>(p, ox, oy, mapped, bins);
+        for (int r = 0; r < 3; ++r) lin[r] = p.m[3 * r] * v[0] + p.m[3 * r + 1] * v[1] + p.m[3 * r + 2] * v[2];
+        st = COMPRESS ? compress_front(lin, p.ceiling, mapped) : clip_rgb(lin, p.ceiling, mapped);
+      }
+      const bool defer = COMPRESS && valid && st < 0;
+      if (COMPRESS) {
+        const unsigned int ballot = __ballot_sync(0xffffffffu, defer);
+        if (ballot) {
+          int base = 0;
+          if (lane == 0) base = atomicAdd(&queued, __popc(ballot));
+          base = __shfl_sync(0xffffffffu, base, 0);
+          if (defer)
+            queue[base + __popc(ballot & ((1u << lane) - 1u))] = Deferred{lin[0], lin[1], lin[2], k * TILE + lane};
+        }
+      }
+      if (valid && !defer) {
+        count(st);
+        encode_pixel<FMT>(p, ox, oy, mapped, bins);
+      }
+    }
+    if (COMPRESS) {
+      __syncthreads();
+      const int n = queued;
+      for (int j = tid; j < n; j += TILE * ROWS) {
+        const Deferred d = queue[j];
+        const float lin[3] = {d.r, d.g, d.b};
+        float mapped[3];
+        const int st = compress_out_of_gamut(lin, p.p3, p.ceiling, p.lightness_ceiling, mapped);
+        count(st);
+        encode_pixel<FMT>(p, ox0 + d.xy % TILE, oy0 + d.xy / TILE, mapped, bins);
+      }
     }
   }
   const unsigned int counts[5] = {__reduce_add_sync(0xffffffffu, n_in), __reduce_add_sync(0xffffffffu, n_comp),
                                   __reduce_add_sync(0xffffffffu, n_lim), __reduce_add_sync(0xffffffffu, n_clip),
                                   __reduce_add_sync(0xffffffffu, n_inv)};
+  __syncthreads();
   if (lane == 0)
     for (int s = 0; s < 5; ++s)
       if (counts[s]) atomicAdd(&diag[s], counts[s]);
@@ -397,6 +500,20 @@ __global__ void transfer_pow_check_kernel(unsigned int first, unsigned int last,
   }
   worst = __reduce_max_sync(0xffffffffu, worst);
   if ((threadIdx.x & 31) == 0) atomicMax(max_ulps, worst);
+}
+
+// Every f32 of (0.0031308, 1]: transfer_pow_rn against the power computed in
+// double and rounded once. Counts the differences.
+__global__ void transfer_rn_check_kernel(unsigned int first, unsigned int last, unsigned long long* failures) {
+  unsigned int bad = 0;
+  const unsigned int stride = gridDim.x * blockDim.x;
+  const float e = 1.0f / 2.4f;
+  for (unsigned int u = first + blockIdx.x * blockDim.x + threadIdx.x; u <= last; u += stride) {
+    const float x = __uint_as_float(u);
+    bad += transfer_pow_rn(x) != (float)pow((double)x, (double)e);
+  }
+  bad = __reduce_add_sync(0xffffffffu, bad);
+  if ((threadIdx.x & 31) == 0 && bad) atomicAdd(failures, (unsigned long long)bad);
 }
 
 // Host copy of cbrt_rn's method (std::cbrt in double as the estimate).
@@ -526,9 +643,11 @@ Status run_display_output(Context& ctx, const float* rgb, const rd_color_desc& c
   const long long tiles = (long long)((g.width + TILE - 1) / TILE) * ((g.height + TILE - 1) / TILE);
   const int grid = (int)std::min<long long>(tiles, (long long)(ctx.sm_count > 0 ? ctx.sm_count : 152) * 8);
   const dim3 block(TILE * ROWS);
-#define RD_OUTPUT_LAUNCH(F)                                                                            \
-  if (g.swap) RD_LAUNCH(ctx, K_OUTPUT, (output_kernel<F, true><<<grid, block, 0, ctx.stream>>>(p)));  \
-  else RD_LAUNCH(ctx, K_OUTPUT, (output_kernel<F, false><<<grid, block, 0, ctx.stream>>>(p)))
+#define RD_OUTPUT_LAUNCH(F)                                                                                   \
+  if (g.swap && p.compress) RD_LAUNCH(ctx, K_OUTPUT, (output_kernel<F, true, true><<<grid, block, 0, ctx.stream>>>(p)));  \
+  else if (g.swap) RD_LAUNCH(ctx, K_OUTPUT, (output_kernel<F, true, false><<<grid, block, 0, ctx.stream>>>(p)));    \
+  else if (p.compress) RD_LAUNCH(ctx, K_OUTPUT, (output_kernel<F, false, true><<<grid, block, 0, ctx.stream>>>(p))); \
+  else RD_LAUNCH(ctx, K_OUTPUT, (output_kernel<F, false, false><<<grid, block, 0, ctx.stream>>>(p)))
   switch (o.format) {
     case RD_OUTPUT_SRGB8: RD_OUTPUT_LAUNCH(FMT_U8); break;
     case RD_OUTPUT_SRGB16: RD_OUTPUT_LAUNCH(FMT_U16); break;
@@ -547,16 +666,18 @@ Status run_math_check(Context& ctx, int which, uint64_t* result) {
   RD_TRY(device_alloc(ctx, 16, &p));
   RD_CUDA_TRY(cudaMemsetAsync(p, 0, 16, ctx.stream));
   const int grid = (ctx.sm_count > 0 ? ctx.sm_count : 152) * 8;
+  const float lo = 0.0031308f, one = 1.0f;
+  unsigned int first = 0, last = 0;
+  std::memcpy(&first, &lo, 4);
+  std::memcpy(&last, &one, 4);
   if (which == 0) {
     RD_LAUNCH(ctx, K_OUTPUT, (cbrt_check_kernel<<<grid, 256, 0, ctx.stream>>>(static_cast<unsigned long long*>(p))));
-  } else {
-    const float lo = 0.0031308f;
-    unsigned int first = 0, last = 0;
-    std::memcpy(&first, &lo, 4);
-    const float one = 1.0f;
-    std::memcpy(&last, &one, 4);
+  } else if (which == 1) {
     RD_LAUNCH(ctx, K_OUTPUT,
               (transfer_pow_check_kernel<<<grid, 256, 0, ctx.stream>>>(first + 1, last, static_cast<unsigned int*>(p))));
+  } else {
+    RD_LAUNCH(ctx, K_OUTPUT, (transfer_rn_check_kernel<<<grid, 256, 0, ctx.stream>>>(
+                                 first + 1, last, static_cast<unsigned long long*>(p))));
   }
   Status st;
   uint64_t v = 0;
@@ -564,7 +685,7 @@ Status run_math_check(Context& ctx, int which, uint64_t* result) {
       cudaStreamSynchronize(ctx.stream) != cudaSuccess)
     st = Status{RD_SYNCHRONIZATION, "math check failed"};
   device_free(ctx, p, 16);
-  if (st.ok()) *result = which == 0 ? v : (v & 0xffffffffull);
+  if (st.ok()) *result = which == 1 ? (v & 0xffffffffull) : v;
   return st;
 }
 

@@ -73,7 +73,11 @@ def test_cube_root_is_correctly_rounded_for_every_f32(stages):
 
 
 def test_transfer_power_is_within_the_quantisation_bound(stages):
-    assert stages.check_math(1) <= 2
+    assert stages.check_math(1) <= 1
+
+
+def test_transfer_power_is_correctly_rounded_for_every_f32(stages):
+    assert stages.check_math(2) == 0
 
 
 @pytest.mark.parametrize("fmt", FORMATS)

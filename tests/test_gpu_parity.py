@@ -224,9 +224,9 @@ def test_colour_output_and_histogram(stages, oracle, variant):
         c = colour_contract(exposure_ev=0.0, base_lut=None, tone_lut=None, hsl=None)
     ours, hist, clipped = stages.color(rgb, c)
     ref = oracle_colour(oracle, rgb, c)
-    diff = np.abs(ours.astype(int) - ref.astype(int))
-    assert diff.max() <= 1
-    assert (diff > 0).mean() <= 1e-3
+    # The 8-bit code of the correctly rounded transfer equals glibc powf's on
+    # every f32 of the transfer's domain, so the output is bit-exact.
+    assert np.array_equal(ours, ref)
     # The histogram of the kernel's own 8-bit output is exact.
     ref_hist, ref_clipped = oracle.histogram(ours)
     assert np.array_equal(hist, ref_hist) and np.array_equal(clipped, ref_clipped)
