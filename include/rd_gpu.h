@@ -266,7 +266,10 @@ rd_status rd_render_output_device(rd_ctx* ctx, const rd_base* base, const rd_col
  * powf(x, 1/2.4) from the correctly rounded power over (0.0031308, 1], which
  * must not exceed the bound the 8- and 16-bit quantisation relies on (1).
  * which = 2: the number of f32 in (0.0031308, 1] whose transfer power (as the
- * quantisation computes it) differs from the correctly rounded one, expected 0. */
+ * quantisation computes it) differs from the correctly rounded one, expected 0.
+ * which = 3: the number of (f32 in that domain, 8- or 16-bit, three dither
+ * offsets) whose quantised code differs from the code of the correctly
+ * rounded power, expected 0. */
 rd_status rd_check_math(rd_ctx* ctx, int32_t which, uint64_t* result);
 
 rd_status rd_source_dimensions(const rd_source* source, uint32_t* width, uint32_t* height);

@@ -358,12 +358,18 @@ __device__ __forceinline__ void quantize_srgb3(const float* lin, float scale, fl
       r[c] = 0.0f;
     } else {
       r[c] = powf(lin[c], e);
-      code[c] = transfer_code(r[c], scale, dither);
-      const float lo = transfer_code(next_down(r[c]), scale, dither);
-      const float hi = transfer_code(next_up(r[c]), scale, dither);
-      if (lo != hi) {
-        undecided |= 1u << c;
-        if (code[c] == lo) upward |= 1u << c;  // the boundary is above r
+      const float q = (1.055f * r[c] - 0.055f) * scale + dither;
+      code[c] = roundf(q);
+      // One ulp of r moves q by at most 1.055 * scale * 2^-23 plus the
+      // rounding of the three operations, under scale * 4e-7 together; only a
+      // q within twice that of a rounding boundary can change code.
+      if (fabsf((q - floorf(q)) - 0.5f) < scale * 7.5e-7f) {
+        const float lo = transfer_code(next_down(r[c]), scale, dither);
+        const float hi = transfer_code(next_up(r[c]), scale, dither);
+        if (lo != hi) {
+          undecided |= 1u << c;
+          if (code[c] == lo) upward |= 1u << c;  // the boundary is above r
+        }
       }
     }
   }

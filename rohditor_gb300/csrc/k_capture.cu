@@ -214,11 +214,15 @@ __global__ void __launch_bounds__(128) rl_stream_kernel(const float* __restrict_
         const int x = x0 - R + tid, n = q_hi - q_next;
         if (n > 0 && (unsigned)x < (unsigned)W) {
           float win[BH + 2 * R];
-          const bool inside = n == BH && q_next - R >= 0 && q_next + BH + R <= H;  // no mirrored rows
+          if (n == BH && q_next - R >= 0 && q_next + BH + R <= H) {  // no mirrored rows
+            const int r0 = q_next - R;
 #pragma unroll
-          for (int j = 0; j < BH + 2 * R; ++j)
-            win[j] = inside ? S.t1[(q_next - R + j) & (G::RS - 1)][tid]
-                            : (j < n + 2 * R ? S.t1[mirror_row(q_next - R + j, H) & (G::RS - 1)][tid] : 0.0f);
+            for (int j = 0; j < BH + 2 * R; ++j) win[j] = S.t1[(r0 + j) & (G::RS - 1)][tid];
+          } else {
+#pragma unroll
+            for (int j = 0; j < BH + 2 * R; ++j)
+              win[j] = j < n + 2 * R ? S.t1[mirror_row(q_next - R + j, H) & (G::RS - 1)][tid] : 0.0f;
+          }
 #pragma unroll
           for (int j = 0; j < BH; ++j) {
             if (j < n) {
@@ -253,11 +257,15 @@ __global__ void __launch_bounds__(128) rl_stream_kernel(const float* __restrict_
         const int x = x0 + tid, n = o_hi - o_next;
         if (tid < SW && x < W && n > 0) {
           float win[BH + 2 * R];
-          const bool inside = n == BH && o_next - R >= 0 && o_next + BH + R <= H;  // no mirrored rows
+          if (n == BH && o_next - R >= 0 && o_next + BH + R <= H) {  // no mirrored rows
+            const int r0 = o_next - R;
 #pragma unroll
-          for (int j = 0; j < BH + 2 * R; ++j)
-            win[j] = inside ? S.t2[(o_next - R + j) & (G::RS - 1)][tid]
-                            : (j < n + 2 * R ? S.t2[mirror_row(o_next - R + j, H) & (G::RS - 1)][tid] : 0.0f);
+            for (int j = 0; j < BH + 2 * R; ++j) win[j] = S.t2[(r0 + j) & (G::RS - 1)][tid];
+          } else {
+#pragma unroll
+            for (int j = 0; j < BH + 2 * R; ++j)
+              win[j] = j < n + 2 * R ? S.t2[mirror_row(o_next - R + j, H) & (G::RS - 1)][tid] : 0.0f;
+          }
           const long long o0 = (long long)o_next * W + x;
           const int es = o_next % G::RIN;
 #pragma unroll
@@ -392,11 +400,20 @@ __global__ void __launch_bounds__(128) rl_prep_kernel(const float* __restrict__ 
         const int x = x0 + tid, n = o_hi - o_next;
         if (tid < SW && x < W && n > 0) {
           float wg[BH + 2 * R], wm[BH + 2 * R];
+          if (n == BH && o_next - R >= 0 && o_next + BH + R <= H) {  // no mirrored rows
+            const int r0 = o_next - R;
 #pragma unroll
-          for (int j = 0; j < BH + 2 * R; ++j) {
-            const int row = j < n + 2 * R ? mirror_row(o_next - R + j, H) & (RS - 1) : 0;
-            wg[j] = S.tg[row][tid];
-            wm[j] = S.tm[row][tid];
+            for (int j = 0; j < BH + 2 * R; ++j) {
+              wg[j] = S.tg[(r0 + j) & (RS - 1)][tid];
+              wm[j] = S.tm[(r0 + j) & (RS - 1)][tid];
+            }
+          } else {
+#pragma unroll
+            for (int j = 0; j < BH + 2 * R; ++j) {
+              const int row = j < n + 2 * R ? mirror_row(o_next - R + j, H) & (RS - 1) : 0;
+              wg[j] = S.tg[row][tid];
+              wm[j] = S.tm[row][tid];
+            }
           }
 #pragma unroll
           for (int j = 0; j < BH; ++j) {

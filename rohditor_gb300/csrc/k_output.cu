@@ -516,6 +516,31 @@ __global__ void transfer_rn_check_kernel(unsigned int first, unsigned int last, 
   if ((threadIdx.x & 31) == 0 && bad) atomicAdd(failures, (unsigned long long)bad);
 }
 
+// Every f32 of (0.0031308, 1], 8- and 16-bit, with and without dither:
+// quantize_srgb3's code against the code of the correctly rounded power.
+__global__ void quantize_check_kernel(unsigned int first, unsigned int last, unsigned long long* failures) {
+  unsigned int bad = 0;
+  const unsigned int stride = gridDim.x * blockDim.x;
+  const float dithers[3] = {0.0f, (0.0f + 0.5f) / 64.0f - 0.5f, (63.0f + 0.5f) / 64.0f - 0.5f};
+  for (unsigned int u = first + blockIdx.x * blockDim.x + threadIdx.x; u <= last; u += stride) {
+    const float x = __uint_as_float(u);
+    const float r = transfer_pow_rn(x);
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const float scale = s ? 65535.0f : 255.0f;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const float lin[3] = {x, 0.5f, 0.0f};
+        float code[3];
+        quantize_srgb3(lin, scale, dithers[d], code);
+        bad += code[0] != rclamp(transfer_code(r, scale, dithers[d]), 0.0f, scale);
+      }
+    }
+  }
+  bad = __reduce_add_sync(0xffffffffu, bad);
+  if ((threadIdx.x & 31) == 0 && bad) atomicAdd(failures, (unsigned long long)bad);
+}
+
 // Host copy of cbrt_rn's method (std::cbrt in double as the estimate).
 float cbrt_rn_host(float x) {
   if (x == 0.0f || !std::isfinite(x)) return x;
@@ -675,8 +700,11 @@ Status run_math_check(Context& ctx, int which, uint64_t* result) {
   } else if (which == 1) {
     RD_LAUNCH(ctx, K_OUTPUT,
               (transfer_pow_check_kernel<<<grid, 256, 0, ctx.stream>>>(first + 1, last, static_cast<unsigned int*>(p))));
-  } else {
+  } else if (which == 2) {
     RD_LAUNCH(ctx, K_OUTPUT, (transfer_rn_check_kernel<<<grid, 256, 0, ctx.stream>>>(
+                                 first + 1, last, static_cast<unsigned long long*>(p))));
+  } else {
+    RD_LAUNCH(ctx, K_OUTPUT, (quantize_check_kernel<<<grid, 256, 0, ctx.stream>>>(
                                  first + 1, last, static_cast<unsigned long long*>(p))));
   }
   Status st;

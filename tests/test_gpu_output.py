@@ -80,6 +80,10 @@ def test_transfer_power_is_correctly_rounded_for_every_f32(stages):
     assert stages.check_math(2) == 0
 
 
+def test_quantised_codes_follow_the_correctly_rounded_power_for_every_f32(stages):
+    assert stages.check_math(3) == 0
+
+
 @pytest.mark.parametrize("fmt", FORMATS)
 @pytest.mark.parametrize("policy", ["clip", "chroma_compress"])
 @pytest.mark.parametrize("primaries", ["srgb", "display_p3"])
