@@ -157,12 +157,11 @@ __device__ __forceinline__ int pattern_position(int ch, unsigned support) {
 
 // 1. suspected sites
 __global__ void count_kernel(const OpposedParams p) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
   unsigned hit = 0, ch = 0;
-  if (i < (long long)p.W * p.H) {
-    const int x = (int)(i % p.W), y = (int)(i / p.W);
+  if (x < p.W) {
     ch = color_at(p.cfa, x, y);
-    hit = p.mosaic[i] >= p.levels[ch];
+    hit = p.mosaic[(long long)y * p.W + x] >= p.levels[ch];
   }
   const unsigned ballot = __ballot_sync(0xffffffffu, hit);
   if ((threadIdx.x & 31) == 0 && ballot) atomicAdd(&p.counters[0], __popc(ballot));
@@ -364,7 +363,7 @@ __global__ void relabel_kernel(const OpposedParams p) {
   }
   p.labels[i] = label;
   const unsigned clipped = __float_as_uint(p.cells[i].w) >> 3;
-  warp_or(p.region_clipped, label && clipped ? label : 0u, label ? clipped : 0u);
+  if (label && clipped) warp_or(p.region_clipped, label, clipped);
 }
 
 // 5. wanted (channel, support) slots per region (region_correction.rs:134-178)
@@ -621,12 +620,16 @@ __global__ void estimate_kernel(const OpposedParams p) {
       }
     }
   }
-  unsigned long long v[5] = {n_rec, n_changed, n_fallback, n_unsup, n_neutral};
-  for (int k = 0; k < 5; ++k) {
-    unsigned long long t = v[k];
-    for (int off = 16; off > 0; off >>= 1) t += __shfl_down_sync(0xffffffffu, t, off);
-    if ((threadIdx.x & 31) == 0 && t) atomicAdd(&p.stats[1 + k], t);
-  }
+  // Each counter is 0 or 1 per thread, so a warp's five sums fit 6-bit fields
+  // of one word and reduce in one step.
+  const unsigned packed = (unsigned)n_rec | (unsigned)n_changed << 6 | (unsigned)n_fallback << 12 |
+                          (unsigned)n_unsup << 18 | (unsigned)n_neutral << 24;
+  const unsigned sum = __reduce_add_sync(0xffffffffu, packed);
+  if ((threadIdx.x & 31) == 0 && sum)
+    for (int k = 0; k < 5; ++k) {
+      const unsigned long long t = (sum >> (6 * k)) & 63u;
+      if (t) atomicAdd(&p.stats[1 + k], t);
+    }
 }
 
 __global__ void copy_suspected_kernel(const OpposedParams p) {
@@ -692,8 +695,7 @@ Status run_opposed_labels(Context& ctx, float* mosaic, int W, int H, int cfa, co
   p.error = ctx.d_error;
   // Zero the per-label tables and counters (labels, dilation and cells are fully written).
   RD_CUDA_TRY(cudaMemsetAsync(b + o_rclip, 0, o_cnt + 256 - o_rclip, ctx.stream));
-  const long long pixels = (long long)W * H;
-  RD_LAUNCH(ctx, K_OPPOSED, count_kernel<<<(unsigned)((pixels + 255) / 256), 256, 0, ctx.stream>>>(p));
+  RD_LAUNCH(ctx, K_OPPOSED, count_kernel<<<dim3((W + 255) / 256, H), 256, 0, ctx.stream>>>(p));
   const dim3 cgrid((cw + 127) / 128, chh);
   RD_LAUNCH(ctx, K_OPPOSED, cells_kernel<<<cgrid, 128, 0, ctx.stream>>>(p));
   RD_LAUNCH(ctx, K_OPPOSED, dilate_kernel<<<cgrid, 128, 0, ctx.stream>>>(p));
