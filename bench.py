@@ -141,6 +141,13 @@ MEASURED_TRAFFIC_BPP = {
 }
 
 
+# Algorithmic FP32 operations per output pixel of AMaZE, from the oracle census
+# (profiles/amaze_fp32_census.md), and the non-FMA FP32 issue rate of the GPU
+# at its maximum SM clock (152 SMs x 128 lanes x 2.07 GHz).
+AMAZE_FP32_OPS_PER_PX = 478.18
+FP32_PEAK_TOPS = 152 * 128 * 2.07e9 / 1e12
+
+
 # Algorithmic bytes per launch of each kernel family, per pixel of the image it covers.
 def family_bytes(name: str, N: int, n: int, H: int, tw: int) -> float | None:
     table = {
@@ -297,6 +304,16 @@ def run_ours(args, world, rank, local, pg):
                     "algorithmic_bytes": round(family_bytes(dominant, N, n, H, tw)),
                     "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
                     else "fallback 6.8 TB/s"}
+    fp32_roofline = None
+    if "amaze" in families:
+        rec = families["amaze"]
+        per_launch_s = rec["ms"] / rec["launches"] / 1e3
+        tops = AMAZE_FP32_OPS_PER_PX * N / per_launch_s / 1e12
+        fp32_roofline = {"bound": "fp32", "kernel": "amaze", "achieved": round(tops, 2), "peak": round(FP32_PEAK_TOPS, 1),
+                         "unit": "Top/s", "frac": round(tops / FP32_PEAK_TOPS, 3),
+                         "ops_per_px": AMAZE_FP32_OPS_PER_PX,
+                         "ops_source": "oracle census, profiles/amaze_fp32_census.md",
+                         "peak_source": "nominal non-FMA FP32 rate at 2070 MHz (the kernel runs without FMA)"}
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3), "higher_is_better": True,
@@ -310,6 +327,7 @@ def run_ours(args, world, rank, local, pg):
                 "d2h_bytes_per_step": 3 * n + 1024 * 8 + 6 * 8, "ms_per_step": round(e2e_ms / args.steps, 3)},
         "gpu_launches": int(launches),
         "roofline": roofline,
+        "fp32_roofline": fp32_roofline,
         "kernels": kernels,
         "dominant_kernel": dominant,
         "kernel_ms_per_step": round(step_kernel_ms, 3),
@@ -327,6 +345,8 @@ def run_ours(args, world, rank, local, pg):
         line["batched"] = batched_throughput(args)
     if rank == 0 and not args.no_export:
         line["export"] = export_output(args)
+    if rank == 0 and args.export_stream:
+        line["export_stream"] = export_stream(args, count=args.export_stream)
     return line
 
 
@@ -545,6 +565,95 @@ def export_output(args, reps: int = 5) -> dict:
     return {"image": f"{W}x{H}", "peak_gbs": hbm_peak, "outputs": out}
 
 
+def export_stream(args, count: int = 24, window: int = 3, cap_gb: float = 60.0) -> dict:
+    """The large-sensor export stream through the served loop: `count` 101.8 MP
+    16-bit mosaics with hot pixels and specular blobs (workloads.large_export:
+    Opposed + AMaZE + RL K = 20 + full optics) are opened in one rd_server with
+    a `cap_gb` budget (each open develops and keeps the image's layers), then
+    each is exported at full resolution as extended f16 (Display P3, chroma
+    compression, headroom 4) plus sRGB8, into pinned host buffers reused by
+    `window` exports in flight. Times are wall clock around the submissions
+    and the polled results."""
+    from rohditor_gb300 import Device, OutputSpec
+    from rohditor_gb300 import _ffi
+    from rohditor_gb300.workloads import CAMERA_TO_REC2020, hot_pixels, large_export
+
+    wls = large_export(count)
+    dev = Device(0)
+    lib = dev.lib
+    server = ctypes.c_void_p()
+    dev.check(lib.rd_server_create(0, int(cap_gb * (1 << 30)), ctypes.byref(server)))
+    W, H = wls[0].width, wls[0].height
+    t0 = time.perf_counter()
+    for k, wl in enumerate(wls):
+        raw = hot_pixels(wl.mosaic(dev), seed=k)
+        s, d, o = wl.sensor.to_c(), wl.capture.to_c(), wl.optics.to_c()
+        wb = np.ascontiguousarray(wl.color.wb_gains, dtype=np.float32)
+        cam = np.ascontiguousarray(CAMERA_TO_REC2020, dtype=np.float32)
+        dev.check(lib.rd_server_open(server, k, raw.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16)), W,
+                                     ctypes.byref(s), ctypes.byref(d), ctypes.byref(o), wl.target[0], wl.target[1],
+                                     wb.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                     cam.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), None))
+    dev.check(lib.rd_server_drain(server, 600000))
+    buf = (_ffi.ServerResult * 256)()
+    opened = [buf[i].status for i in range(lib.rd_server_poll(server, buf, 256, 0))]
+    t1 = time.perf_counter()
+    specs = [OutputSpec(format="extended_f16", primaries="display_p3", policy="chroma_compress", headroom=4.0),
+             OutputSpec(format="srgb8")]
+    sizes = [W * H * 6, W * H * 3]
+    descs = (_ffi.OutputDesc * 2)(*[sp.to_c() for sp in specs])
+    pool = []
+    for _ in range(window):
+        ptrs = []
+        for n in sizes:
+            p = ctypes.c_void_p()
+            dev.check(lib.rd_host_alloc(n, ctypes.byref(p)))
+            ptrs.append(p.value)
+        pool.append(ptrs)
+    in_flight, statuses, latencies = {}, [], []
+    t2 = time.perf_counter()
+    for k, wl in enumerate(wls):
+        while not pool:
+            n = lib.rd_server_poll(server, buf, 256, 1000)
+            for i in range(n):
+                if buf[i].kind == 2:
+                    pool.append(in_flight.pop(buf[i].request_id))
+                    statuses.append(buf[i].status)
+                    latencies.append(buf[i].latency_ms)
+        ptrs = pool.pop()
+        dst = (ctypes.c_void_p * 2)(*ptrs)
+        caps = (ctypes.c_size_t * 2)(*sizes)
+        rid = ctypes.c_uint64()
+        c = wl.color.to_c()
+        dev.check(lib.rd_server_submit_export(server, k, 1, ctypes.byref(c), descs, 2, dst, caps, ctypes.byref(rid)))
+        in_flight[rid.value] = ptrs
+    while in_flight:
+        n = lib.rd_server_poll(server, buf, 256, 1000)
+        for i in range(n):
+            if buf[i].kind == 2:
+                pool.append(in_flight.pop(buf[i].request_id))
+                statuses.append(buf[i].status)
+                latencies.append(buf[i].latency_ms)
+    t3 = time.perf_counter()
+    st = _ffi.ServerStats()
+    dev.check(lib.rd_server_get_stats(server, ctypes.byref(st)))
+    lib.rd_server_destroy(server)
+    for ptrs in pool:
+        for p in ptrs:
+            lib.rd_host_free(ctypes.c_void_p(p))
+    dev.close()
+    mp = W * H / 1e6
+    return {"images": count, "image": f"{W}x{H} RGGB 16-bit, 0.5% hot pixels, specular blobs",
+            "pipeline": "Opposed + AMaZE + RL20 + optics; export: extended f16 Display P3 chroma-compressed "
+                        "headroom 4 + sRGB8, full resolution",
+            "open_develop_s": round(t1 - t0, 2), "opens_ok": sum(1 for v in opened if v == 0),
+            "export_s": round(t3 - t2, 3), "exports_ok": sum(1 for v in statuses if v == 0),
+            "exports_per_s": round(count / (t3 - t2), 2), "export_mp_per_s": round(count * mp / (t3 - t2), 1),
+            "export_latency_p50_ms": round(float(np.percentile(latencies, 50)), 1) if latencies else None,
+            "peak_resident_gb": round(st.peak_resident_bytes / (1 << 30), 2), "cap_gb": cap_gb,
+            "evictions": int(st.evictions)}
+
+
 def cpu_develop_band(rows: int, args) -> tuple[float, float]:
     """Run the oracle pipeline on a `rows`-high band of the 24 MP workload; returns (seconds, fraction)."""
     from oracle import oracle as o
@@ -636,6 +745,8 @@ def main():
     p.add_argument("--no-edit-latency", action="store_true", help="skip the served-vs-plain edit latency trace")
     p.add_argument("--no-batched", action="store_true", help="skip the uneven batched-develop measurement")
     p.add_argument("--no-export", action="store_true", help="skip the full-resolution output measurement")
+    p.add_argument("--export-stream", type=int, default=0, metavar="N",
+                   help="also run the large-sensor export stream through the served loop with N images")
     p.add_argument("--cpu-baseline-rows", type=int, default=2048,
                    help="band height of the CPU baseline sample (2048 rows = half a 24 MP develop)")
     args = p.parse_args()

@@ -356,7 +356,7 @@ typedef struct rd_server rd_server;
 typedef struct rd_server_result {
   uint64_t request_id;
   uint32_t image_id;
-  int32_t kind;      /* 0 edit (render), 1 develop */
+  int32_t kind;      /* 0 edit (render), 1 develop, 2 export */
   int32_t status;    /* rd_status; RD_CANCELLED: replaced by a newer request or closed */
   uint32_t batch_size;
   uint64_t revision;
@@ -365,6 +365,7 @@ typedef struct rd_server_result {
 typedef struct rd_server_stats {
   uint64_t requested, completed, coalesced, failed, redeveloped, evictions, batches, batched_edits;
   uint64_t resident_bytes, peak_resident_bytes, budget_bytes;
+  uint64_t exports;  /* exports served (completed or failed) */
 } rd_server_stats;
 rd_status rd_server_create(int device, uint64_t budget_bytes, rd_server** out);
 /* Dry servers only: modelled develop and render times. */
@@ -382,6 +383,17 @@ rd_status rd_server_submit_develop(rd_server* server, uint32_t image_id, uint64_
                                    const rd_detail_desc* detail, const rd_optics_desc* optics, uint64_t* request_id);
 /* Up to max_results completed requests (waiting up to wait_ms for the first); returns the count. */
 int32_t rd_server_poll(rd_server* server, rd_server_result* out, int32_t max_results, int32_t wait_ms);
+/* Export of an open image at full resolution (GpuExportProcessor::render,
+ * crates/gpu/src/export/mod.rs:218): a develop from the resident mosaic with
+ * the image's current settings, the spatial pass at the crop size, then each
+ * of the n_outputs descriptions rendered into the client's host buffer dst[k]
+ * (capacity[k] bytes, at least rd_output_dimensions' size). Runs on the
+ * develop lane, its working set charged against the budget; completes with a
+ * result of kind 2. The buffers must stay valid until that result is polled.
+ * A later revision replaces a pending export of the same image (RD_CANCELLED). */
+rd_status rd_server_submit_export(rd_server* server, uint32_t image_id, uint64_t revision, const rd_color_desc* color,
+                                  const rd_output_desc* outputs, int32_t n_outputs, void* const* dst,
+                                  const size_t* capacities, uint64_t* request_id);
 /* The latest rendered output of an image: sRGB8 [h][3w], 1024 histogram bins, its revision. */
 rd_status rd_server_read_output(rd_server* server, uint32_t image_id, uint8_t* srgb, uint64_t* hist,
                                 uint64_t* revision);

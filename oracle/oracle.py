@@ -141,6 +141,62 @@ def load():
         return lib
 
 
+_flops_lib = None
+FLOP_CLASSES = ("add_sub", "mul", "div", "compare", "abs", "min_max")
+
+
+def load_flops():
+    """The operation-counting AMaZE build (oracle/flops/amaze_flops.cpp)."""
+    global _flops_lib
+    with _lock:
+        if _flops_lib is None:
+            path = os.path.join(_HERE, "_build", "librd_oracle_flops.so")
+            if _stale() or not os.path.exists(path):
+                build()
+            lib = ctypes.CDLL(path)
+            lib.ro_amaze_reconstruct.restype = ctypes.c_int
+            lib.ro_amaze_reconstruct.argtypes = [F32P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, F32P,
+                                                 ctypes.c_float, F32P, ctypes.c_int]
+            lib.ro_flops_reset.restype = None
+            lib.ro_flops_read.argtypes = [U64P]
+            lib.ro_flops_read.restype = None
+            _flops_lib = lib
+        return _flops_lib
+
+
+def amaze_counted(mosaic: np.ndarray, pattern: int, balance) -> tuple[np.ndarray, dict]:
+    """AMaZE as ro_demosaic runs it (channel balance first), with its operation counts."""
+    lib = load_flops()
+    mosaic = f32(mosaic)
+    h, w = mosaic.shape
+    bal = np.asarray(balance, dtype=np.float32)
+    fwd = bal / bal.max()
+    gains = np.ones(3, dtype=np.float32)
+    clip_point = np.float32(1.0)
+    src = mosaic
+    if not np.all(fwd == 1.0):
+        ch = np.zeros((h, w), dtype=np.int64)
+        for y in range(2):
+            for x in range(2):
+                ch[y::2, x::2] = _CFA_TABLE[pattern][(y << 1) | x]
+        src = (mosaic * fwd[ch]).astype(np.float32)
+        gains = (np.float32(1.0) / fwd).astype(np.float32)
+        clip_point = np.float32(fwd.min())
+    src = np.ascontiguousarray(src)
+    out = np.zeros((h, 3 * w), dtype=np.float32)
+    lib.ro_flops_reset()
+    rc = lib.ro_amaze_reconstruct(ptr(src), w, h, w, pattern, ptr(gains), float(clip_point), ptr(out), 3 * w)
+    if rc != 0:
+        raise RuntimeError(f"counted AMaZE failed: {rc}")
+    ops = np.zeros(6, dtype=np.uint64)
+    lib.ro_flops_read(ptr(ops, ctypes.c_uint64))
+    return out, dict(zip(FLOP_CLASSES, (int(v) for v in ops)))
+
+
+# color_at (crates/image/src/lib.rs:88-116): channel of (x & 1, y & 1) per CFA code.
+_CFA_TABLE = ((0, 1, 1, 2), (2, 1, 1, 0), (1, 0, 2, 1), (1, 2, 0, 1))
+
+
 def ptr(array: np.ndarray, ctype=ctypes.c_float):
     assert array.flags["C_CONTIGUOUS"]
     return array.ctypes.data_as(ctypes.POINTER(ctype))

@@ -124,10 +124,9 @@ class ServerResult(ctypes.Structure):
 class ServerStats(ctypes.Structure):
     _fields_ = [(name, ctypes.c_uint64) for name in (
         "requested", "completed", "coalesced", "failed", "redeveloped", "evictions", "batches", "batched_edits",
-        "resident_bytes", "peak_resident_bytes", "budget_bytes")]
+        "resident_bytes", "peak_resident_bytes", "budget_bytes", "exports")]
 
 
-# Every exported symbol of include/rd_gpu.h with its ctypes signature.
 class OutputDesc(ctypes.Structure):
     _fields_ = [
         ("format", ctypes.c_int32), ("primaries", ctypes.c_int32), ("policy", ctypes.c_int32),
@@ -144,6 +143,7 @@ ORIENTATION = {"normal": 0, "horizontal_flip": 1, "rotate180": 2, "vertical_flip
                "rotate90": 5, "transverse": 6, "rotate270": 7, "unknown": 8}
 GAMUT_STATUS = ("in_gamut", "compressed", "limited", "clipped_fallback", "invalid")
 
+# Every exported symbol of include/rd_gpu.h with its ctypes signature.
 SIGNATURES = {
     "rd_status_is_routing": (ctypes.c_int, [ctypes.c_int]),
     "rd_status_name": (ctypes.c_char_p, [ctypes.c_int]),
@@ -210,6 +210,9 @@ SIGNATURES = {
     "rd_server_submit_edit": (ctypes.c_int, [VOIDP, ctypes.c_uint32, ctypes.c_uint64, ctypes.POINTER(ColorDesc), U64P]),
     "rd_server_submit_develop": (ctypes.c_int, [VOIDP, ctypes.c_uint32, ctypes.c_uint64, ctypes.POINTER(DetailDesc),
                                                 ctypes.POINTER(OpticsDesc), U64P]),
+    "rd_server_submit_export": (ctypes.c_int, [VOIDP, ctypes.c_uint32, ctypes.c_uint64, ctypes.POINTER(ColorDesc),
+                                               ctypes.POINTER(OutputDesc), ctypes.c_int32, ctypes.POINTER(VOIDP),
+                                               ctypes.POINTER(ctypes.c_size_t), U64P]),
     "rd_server_poll": (ctypes.c_int32, [VOIDP, ctypes.POINTER(ServerResult), ctypes.c_int32, ctypes.c_int32]),
     "rd_server_read_output": (ctypes.c_int, [VOIDP, ctypes.c_uint32, U8P, U64P, U64P]),
     "rd_server_get_stats": (ctypes.c_int, [VOIDP, ctypes.POINTER(ServerStats)]),

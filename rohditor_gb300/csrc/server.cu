@@ -2,8 +2,9 @@
 // worker (crates/engine/src/coordinator/{scheduler,worker}.rs, preview_cache/).
 //
 // Images are opened once: the server keeps a host copy of the decoded mosaic
-// and, as device-resident cache layers, the mosaic itself, the 2560-px
-// Rec.2020 preview base and the render outputs. Requests are newest-wins per
+// and, as device-resident cache layers, the mosaic itself, the
+// full-resolution demosaiced source, the 2560-px Rec.2020 preview base and the
+// render outputs. Requests are newest-wins per
 // image, with the reference's ticket order (scheduler.rs:176-180: a later
 // revision, or the same revision and a later sequence, replaces a pending
 // request; an older one is dropped). Two lanes serve them:
@@ -26,6 +27,11 @@
 // transient working set are charged against the byte budget before they are
 // taken; when a develop does not fit, the least recently used images not in
 // use lose their layers (render outputs, base, mosaic).
+//
+// Exports (full-resolution develop + output conversions into client buffers,
+// the reference's GpuExportProcessor::render, crates/gpu/src/export/mod.rs:218)
+// run on the develop lane, oldest first among develops and exports, with their
+// transient working set charged against the same budget.
 //
 // The executor behind the policy is either the CUDA pipeline or, for host-only
 // tests of the policy, a dry executor that models service times.
@@ -80,6 +86,20 @@ struct DevelopRequest {
   Clock::time_point submitted;
 };
 
+// A full-resolution export: develop from the resident mosaic with the image's
+// current settings, the spatial pass at the crop size, then each output
+// conversion into a host buffer the client keeps until the result is polled.
+struct ExportRequest {
+  uint64_t id = 0;
+  Ticket ticket;
+  rd_color_desc color;
+  std::vector<rd_output_desc> outputs;
+  std::vector<void*> dst;
+  std::vector<size_t> capacity;
+  size_t largest_output = 0;  // bytes of the largest output
+  Clock::time_point submitted;
+};
+
 struct ServedImage {
   uint32_t id = 0;
   std::vector<uint16_t> mosaic;  // host copy, sensor_height rows of row_stride samples
@@ -91,6 +111,7 @@ struct ServedImage {
   float wb[3] = {1, 1, 1}, cam[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
   // resident layers (allocated and released by the develop lane)
   uint16_t* d_mosaic = nullptr;
+  rd_source* source = nullptr;  // full-resolution demosaiced, sharpened camera RGB
   rd_base* base = nullptr;
   std::vector<rd_base*> retired;  // replaced bases still read by a render in flight
   uint8_t* d_out = nullptr;
@@ -103,19 +124,27 @@ struct ServedImage {
   rd_color_desc last_color{};  // colour settings of the latest served edit
   bool has_color = false;
   // pending requests
-  bool has_edit = false, has_develop = false;
+  bool has_edit = false, has_develop = false, has_export = false;
   EditRequest edit;
   DevelopRequest develop;
+  ExportRequest exp;
   bool render_busy = false, develop_busy = false, closing = false;
   uint64_t last_used = 0;
 
   size_t mosaic_bytes() const { return sizeof(uint16_t) * mosaic.size(); }
+  size_t source_bytes() const { return 12 * (size_t)sensor.crop_width * sensor.crop_height; }
   size_t base_bytes() const { return sizeof(float) * 3 * (size_t)tw * th; }
   size_t out_bytes() const { return 3 * (size_t)tw * th + 1024 * sizeof(unsigned long long); }
   size_t develop_bytes() const {
-    // Transient working set of one develop + spatial pass: mosaic plane, RGB
-    // source, RL planes, vignetting plane, optics output and tile slabs.
-    return 44 * (size_t)sensor.crop_width * sensor.crop_height + ((size_t)64 << 20);
+    // Transient working set of one develop + spatial pass besides the source
+    // (a layer of its own): f32 mosaic, RL planes, vignetting plane, optics
+    // output, tile slabs.
+    return 32 * (size_t)sensor.crop_width * sensor.crop_height + ((size_t)64 << 20);
+  }
+  // An export's transient: the full-resolution spatial pass (vignetting plane,
+  // optics output, base) and the device copy of its largest output.
+  size_t export_bytes(size_t largest_output) const {
+    return 32 * (size_t)sensor.crop_width * sensor.crop_height + largest_output + ((size_t)64 << 20);
   }
   bool busy() const { return render_busy || develop_busy; }
 };
@@ -128,9 +157,11 @@ class Executor {
   virtual void drop_mosaic(ServedImage& im) = 0;
   virtual Status develop_source(ServedImage& im, const DevelopRequest& rq, rd_source** src) = 0;
   virtual Status develop_base(ServedImage& im, const DevelopRequest& rq, rd_source* src, rd_base** base) = 0;
+  virtual void drop_source(rd_source* src) = 0;
   virtual void drop_base(rd_base* base) = 0;
   virtual Status ensure_outputs(ServedImage& im) = 0;
   virtual void drop_outputs(ServedImage& im) = 0;
+  virtual Status export_outputs(ServedImage& im, const ExportRequest& rq) = 0;
   // Render lane.
   // `bases[k]` is the base of ims[k] taken when the batch was formed.
   virtual Status render(const std::vector<ServedImage*>& ims, const std::vector<rd_base*>& bases,
@@ -178,9 +209,11 @@ class CudaExecutor : public Executor {
                      "develop failed");
   }
   Status develop_base(ServedImage& im, const DevelopRequest& rq, rd_source* src, rd_base** base) override {
-    const rd_status st = rd_spatial(dev, src, &rq.optics, im.tw, im.th, im.wb, im.cam, base, nullptr);
-    rd_source_release(src);
-    return from_code(st, "spatial pass failed");
+    return from_code(rd_spatial(dev, src, &rq.optics, im.tw, im.th, im.wb, im.cam, base, nullptr),
+                     "spatial pass failed");
+  }
+  void drop_source(rd_source* src) override {
+    if (src) rd_source_release(src);
   }
   void drop_base(rd_base* base) override {
     if (base) rd_base_release(base);
@@ -207,6 +240,18 @@ class CudaExecutor : public Executor {
     im.d_out = nullptr;
     im.h_front = im.h_back = nullptr;
     im.has_output = false;
+  }
+  Status export_outputs(ServedImage& im, const ExportRequest& rq) override {
+    rd_base* base = nullptr;
+    RD_TRY(from_code(rd_spatial(dev, im.source, &im.optics, im.sensor.crop_width, im.sensor.crop_height, im.wb,
+                                im.cam, &base, nullptr),
+                     "export spatial pass failed"));
+    rd_status st = RD_OK;
+    for (size_t k = 0; k < rq.outputs.size() && st == RD_OK; ++k)
+      st = rd_render_output(dev, base, &rq.color, &rq.outputs[k], rq.dst[k], rq.capacity[k], nullptr, nullptr,
+                            nullptr);
+    rd_base_release(base);
+    return from_code(st, "export output failed");
   }
   Status render(const std::vector<ServedImage*>& ims, const std::vector<rd_base*>& bases,
                 const std::vector<const rd_color_desc*>& colors) override {
@@ -256,7 +301,7 @@ class DryExecutor : public Executor {
   void drop_mosaic(ServedImage& im) override { im.d_mosaic = nullptr; }
   Status develop_source(ServedImage&, const DevelopRequest&, rd_source** src) override {
     std::this_thread::sleep_for(std::chrono::microseconds(develop_us / 2));
-    *src = nullptr;
+    *src = new rd_source{};  // marks the layer resident
     return Status{};
   }
   Status develop_base(ServedImage&, const DevelopRequest&, rd_source*, rd_base** base) override {
@@ -264,6 +309,7 @@ class DryExecutor : public Executor {
     *base = new rd_base{};
     return Status{};
   }
+  void drop_source(rd_source* src) override { delete src; }
   void drop_base(rd_base* base) override { delete base; }
   Status ensure_outputs(ServedImage& im) override {
     if (im.h_front) return Status{};
@@ -278,6 +324,12 @@ class DryExecutor : public Executor {
     delete[] im.h_back;
     im.h_front = im.h_back = im.d_out = nullptr;
     im.has_output = false;
+  }
+  Status export_outputs(ServedImage&, const ExportRequest& rq) override {
+    std::this_thread::sleep_for(std::chrono::microseconds(develop_us));
+    const uint8_t v = (uint8_t)(rq.color.exposure_ev * 10.0f);
+    for (size_t k = 0; k < rq.dst.size(); ++k) std::memset(rq.dst[k], v, rq.capacity[k]);
+    return Status{};
   }
   Status render(const std::vector<ServedImage*>& ims, const std::vector<rd_base*>&,
                 const std::vector<const rd_color_desc*>& colors) override {
@@ -309,7 +361,8 @@ struct rd_server {
 
   // -------------------------------------------------------------- accounting
   size_t layers(const rd::ServedImage& im) const {
-    return (im.d_mosaic ? im.mosaic_bytes() : 0) + (im.base ? im.base_bytes() : 0) + (im.d_out ? im.out_bytes() : 0);
+    return (im.d_mosaic ? im.mosaic_bytes() : 0) + (im.source ? im.source_bytes() : 0) +
+           (im.base ? im.base_bytes() : 0) + (im.d_out ? im.out_bytes() : 0);
   }
   void charge(int64_t delta) {
     resident = (uint64_t)((int64_t)resident + delta);
@@ -324,6 +377,8 @@ struct rd_server {
     im.base = nullptr;
     for (rd_base* b : im.retired) exec->drop_base(b);
     im.retired.clear();
+    exec->drop_source(im.source);
+    im.source = nullptr;
     exec->drop_mosaic(im);
     charge(-(int64_t)before);
   }
@@ -440,7 +495,7 @@ struct rd_server {
     for (auto& kv : images) {
       const rd::ServedImage& im = *kv.second;
       if (im.busy()) continue;
-      if (im.closing || im.has_develop || !im.retired.empty()) return true;
+      if (im.closing || im.has_develop || im.has_export || !im.retired.empty()) return true;
       if (im.has_edit && (!im.base || !im.d_out)) return true;  // needs a (re-)develop first
     }
     return false;
@@ -472,22 +527,36 @@ struct rd_server {
       ++it;
     }
   }
-  // The oldest pending develop.
+  // The oldest pending develop or export.
   void serve_develop(std::unique_lock<std::mutex>& lk) {
     rd::ServedImage* target = nullptr;
+    bool is_export = false;
+    rd::Clock::time_point oldest{};
     for (auto& kv : images) {
       rd::ServedImage& im = *kv.second;
-      if (!im.has_develop || im.closing || im.busy()) continue;
-      if (!target || im.develop.submitted < target->develop.submitted) target = &im;
+      if (im.closing || im.busy()) continue;
+      if (im.has_develop && (!target || im.develop.submitted < oldest)) {
+        target = &im;
+        is_export = false;
+        oldest = im.develop.submitted;
+      }
+      if (im.has_export && !im.has_develop && (!target || im.exp.submitted < oldest)) {
+        // A pending develop of the same image goes first: the export uses its settings.
+        target = &im;
+        is_export = true;
+        oldest = im.exp.submitted;
+      }
     }
     if (!target) return;
+    if (is_export) return serve_export(lk, *target);
     rd::ServedImage& im = *target;
     const rd::DevelopRequest rq = im.develop;
     im.has_develop = false;
     im.develop_busy = true;
     im.last_used = ++lru_clock;
     const auto started = rd::Clock::now();
-    uint64_t need = im.develop_bytes() + im.base_bytes();  // the new base coexists with the old one
+    // The new source and base coexist with the old ones until they are published.
+    uint64_t need = im.develop_bytes() + im.source_bytes() + im.base_bytes();
     if (!im.d_mosaic) need += im.mosaic_bytes();
     if (!im.d_out) need += im.out_bytes();
     rd::Status st;
@@ -501,14 +570,22 @@ struct rd_server {
       if (st.ok()) charge((int64_t)im.out_bytes());
     }
     rd_base* base = nullptr;
+    rd_source* src = nullptr;
     if (st.ok()) {
       lk.unlock();
-      rd_source* src = nullptr;
       st = exec->develop_source(im, rq, &src);
       if (st.ok()) st = exec->develop_base(im, rq, src, &base);
       lk.lock();
     }
+    if (!st.ok() && src) {
+      exec->drop_source(src);
+      src = nullptr;
+    }
     if (st.ok()) {
+      // The demosaiced source of the current settings stays resident.
+      if (im.source) exec->drop_source(im.source);
+      else charge((int64_t)im.source_bytes());
+      im.source = src;
       // Publish the new base; the old one goes when no render reads it.
       if (im.base) {
         if (im.render_busy) im.retired.push_back(im.base);
@@ -533,6 +610,50 @@ struct rd_server {
                 rd::Clock::now(), 1);
     if (!st.ok() && rq.id == 0 && im.has_edit) fail_edit(im, st.code);  // its edit waited on it
     render_cv.notify_all();
+  }
+  void serve_export(std::unique_lock<std::mutex>& lk, rd::ServedImage& im) {
+    const rd::ExportRequest rq = im.exp;
+    im.has_export = false;
+    im.develop_busy = true;
+    im.last_used = ++lru_clock;
+    const auto started = rd::Clock::now();
+    const uint64_t transient = im.export_bytes(rq.largest_output);
+    uint64_t need = transient;
+    if (!im.d_mosaic) need += im.mosaic_bytes();
+    if (!im.source) need += im.develop_bytes() + im.source_bytes();
+    rd::Status st;
+    if (!admit(need, &im)) st = rd::Status{RD_OVER_BUDGET, "export does not fit the budget"};
+    if (st.ok() && !im.d_mosaic) {
+      st = exec->upload(im);
+      if (st.ok()) charge((int64_t)im.mosaic_bytes());
+    }
+    if (st.ok() && !im.source) {
+      // Evicted or never kept: develop the source with the current settings.
+      rd::DevelopRequest dq;
+      dq.detail = im.detail;
+      dq.optics = im.optics;
+      rd_source* src = nullptr;
+      lk.unlock();
+      st = exec->develop_source(im, dq, &src);
+      lk.lock();
+      if (st.ok()) {
+        im.source = src;
+        charge((int64_t)im.source_bytes());
+      }
+    }
+    if (st.ok()) {
+      // The transient is charged while the export runs, so concurrent
+      // admissions see it.
+      charge((int64_t)transient);
+      lk.unlock();
+      st = exec->export_outputs(im, rq);
+      lk.lock();
+      charge(-(int64_t)transient);
+    }
+    im.develop_busy = false;
+    stats.exports++;
+    push_result(rq.id, im.id, 2, st.ok() ? RD_OK : st.code, rq.ticket.revision, rq.submitted, started,
+                rd::Clock::now(), 1);
   }
   void develop_loop() {
     std::unique_lock<std::mutex> lk(mu);
@@ -560,7 +681,7 @@ struct rd_server {
   bool idle() const { return !rendering && !developing && !render_work() && !develop_work() && !pending(); }
   bool pending() const {
     for (auto& kv : images)
-      if (kv.second->has_edit || kv.second->has_develop || kv.second->busy()) return true;
+      if (kv.second->has_edit || kv.second->has_develop || kv.second->has_export || kv.second->busy()) return true;
     return false;
   }
 };
@@ -662,7 +783,9 @@ rd_status rd_server_close_image(rd_server* s, uint32_t image_id) {
   if (im.has_edit) s->push_result(im.edit.id, im.id, 0, RD_CANCELLED, im.edit.ticket.revision, im.edit.submitted, now, now, 0);
   if (im.has_develop)
     s->push_result(im.develop.id, im.id, 1, RD_CANCELLED, im.develop.ticket.revision, im.develop.submitted, now, now, 0);
-  im.has_edit = im.has_develop = false;
+  if (im.has_export)
+    s->push_result(im.exp.id, im.id, 2, RD_CANCELLED, im.exp.ticket.revision, im.exp.submitted, now, now, 0);
+  im.has_edit = im.has_develop = im.has_export = false;
   im.closing = true;
   s->wake();
   return RD_OK;
@@ -722,6 +845,46 @@ rd_status rd_server_submit_develop(rd_server* s, uint32_t image_id, uint64_t rev
   }
   im.develop = rq;
   im.has_develop = true;
+  s->wake();
+  return RD_OK;
+}
+
+rd_status rd_server_submit_export(rd_server* s, uint32_t image_id, uint64_t revision, const rd_color_desc* color,
+                                  const rd_output_desc* outputs, int32_t n_outputs, void* const* dst,
+                                  const size_t* capacities, uint64_t* request_id) {
+  if (!s || !color || !outputs || !dst || !capacities || n_outputs <= 0) return RD_INVALID_INPUT;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->images.find(image_id);
+  if (it == s->images.end() || it->second->closing) return RD_INVALID_INPUT;
+  rd::ServedImage& im = *it->second;
+  rd::ExportRequest rq;
+  for (int32_t k = 0; k < n_outputs; ++k) {
+    uint32_t ow = 0, oh = 0, bpp = 0;
+    const rd_status st = rd_output_dimensions(im.sensor.crop_width, im.sensor.crop_height, &outputs[k], &ow, &oh, &bpp);
+    if (st != RD_OK) return st;
+    const size_t bytes = (size_t)ow * oh * bpp;
+    if (!dst[k] || capacities[k] < bytes) return RD_INVALID_DIMENSIONS;
+    rq.outputs.push_back(outputs[k]);
+    rq.dst.push_back(dst[k]);
+    rq.capacity.push_back(capacities[k]);
+    rq.largest_output = std::max(rq.largest_output, bytes);
+  }
+  rq.id = s->next_request++;
+  rq.ticket = {revision, ++s->sequence};
+  rq.color = *color;
+  rq.submitted = rd::Clock::now();
+  if (request_id) *request_id = rq.id;
+  s->stats.requested++;
+  if (im.has_export) {
+    if (!rd::replaces(im.exp.ticket, rq.ticket)) {
+      s->push_result(rq.id, im.id, 2, RD_CANCELLED, revision, rq.submitted, rq.submitted, rq.submitted, 0);
+      return RD_OK;
+    }
+    s->push_result(im.exp.id, im.id, 2, RD_CANCELLED, im.exp.ticket.revision, im.exp.submitted, rq.submitted,
+                   rq.submitted, 0);
+  }
+  im.exp = std::move(rq);
+  im.has_export = true;
   s->wake();
   return RD_OK;
 }

@@ -15,10 +15,10 @@ import ctypes
 import numpy as np
 
 from . import _ffi
-from .processor import (CaptureContract, ColorContract, GpuPreviewError, OpticsExecution, SensorDescription, _f32,
-                        _ptr)
+from .processor import (CaptureContract, ColorContract, GpuPreviewError, OpticsExecution, OutputSpec,
+                        SensorDescription, _f32, _ptr)
 
-EDIT, DEVELOP = 0, 1
+EDIT, DEVELOP, EXPORT = 0, 1, 2
 
 
 class PreviewServer:
@@ -33,6 +33,8 @@ class PreviewServer:
             raise GpuPreviewError(rc, f"could not create a preview server on device {device}")
         self.handle = h
         self._sizes: dict[int, tuple[int, int]] = {}
+        self._crops: dict[int, tuple[int, int]] = {}
+        self._export_buffers: dict[int, list] = {}
 
     @classmethod
     def dry(cls, budget_bytes: int = 0, develop_us: int = 2000, render_us: int = 200) -> "PreviewServer":
@@ -55,6 +57,7 @@ class PreviewServer:
                                             ctypes.byref(s), ctypes.byref(d), ctypes.byref(o), target[0], target[1],
                                             _ptr(wb, ctypes.c_float), _ptr(cam, ctypes.c_float), ctypes.byref(rid)))
         self._sizes[image_id] = target
+        self._crops[image_id] = sensor.crop_size
         return int(rid.value)
 
     def close_image(self, image_id: int):
@@ -73,10 +76,33 @@ class PreviewServer:
                                                       ctypes.byref(o), ctypes.byref(rid)))
         return int(rid.value)
 
+    def submit_export(self, image_id: int, revision: int, color: ColorContract,
+                      outputs: list[OutputSpec]) -> tuple[int, list[np.ndarray]]:
+        """Full-resolution export of an open image; returns the request id and the
+        output arrays, which the server fills before the export's result is polled."""
+        cw, ch = self._crops[image_id]
+        arrays = []
+        for spec in outputs:
+            ow, oh = spec.dimensions(cw, ch)
+            arrays.append(np.empty((oh, 3 * ow), dtype=spec.dtype))
+        descs = (_ffi.OutputDesc * len(outputs))(*[spec.to_c() for spec in outputs])
+        dst = (ctypes.c_void_p * len(outputs))(*[a.ctypes.data for a in arrays])
+        caps = (ctypes.c_size_t * len(outputs))(*[a.nbytes for a in arrays])
+        c = color.to_c()
+        rid = ctypes.c_uint64()
+        self._check(self.lib.rd_server_submit_export(self.handle, image_id, revision, ctypes.byref(c), descs,
+                                                     len(outputs), dst, caps, ctypes.byref(rid)))
+        self._export_buffers[int(rid.value)] = arrays  # alive until the result is polled
+        return int(rid.value), arrays
+
     def poll(self, max_results: int = 256, wait_ms: int = 0) -> list[dict]:
         buf = (_ffi.ServerResult * max_results)()
         n = self.lib.rd_server_poll(self.handle, buf, max_results, wait_ms)
-        return [{f: getattr(buf[i], f) for f, _ in _ffi.ServerResult._fields_} for i in range(n)]
+        out = [{f: getattr(buf[i], f) for f, _ in _ffi.ServerResult._fields_} for i in range(n)]
+        for r in out:
+            if r["kind"] == EXPORT:
+                self._export_buffers.pop(r["request_id"], None)
+        return out
 
     def read_output(self, image_id: int) -> tuple[np.ndarray, np.ndarray, int]:
         w, h = self._sizes[image_id]

@@ -202,3 +202,40 @@ def batched_uneven(count: int = 48, seed: int = 3, iterations: int = 5) -> list[
         out.append(Workload(f"batch_{k}", width, height, cfa, bits, black, white, 0.05, True, wb, sensor, capture,
                             optics, preview_dimensions(width, height, 2560), color, seed * 1000 + k))
     return out
+
+
+def large_export(count: int = 24, seed: int = 5, iterations: int = 20) -> list[Workload]:
+    """The large-sensor export stream: 11648x8736 (101.8 MP) RGGB 16-bit
+    mosaics (white 65535) with saturated specular blobs; Opposed + AMaZE + RL
+    (K iterations) + full optics; a 2560-px preview while open. Hot pixels
+    (0.5% of samples at white) are added to the host mosaic by `hot_pixels`."""
+    out = []
+    width, height, bits = 11648, 8736, 16
+    for k in range(count):
+        rng = np.random.default_rng(seed * 1000 + k)
+        wb = (float(rng.uniform(1.7, 2.3)), 1.0, float(rng.uniform(1.4, 1.9)))
+        det, ceiling = opposed_levels(1.0, wb)
+        sensor = SensorDescription(sensor_width=width, sensor_height=height, cfa="RGGB", black=(1024.0,),
+                                   white=(65535.0,), highlight="opposed", detection_levels=det,
+                                   neutral_ceiling=ceiling, demosaic="amaze", demosaic_balance=wb)
+        capture = CaptureContract(amount=0.5, radius=0.7, noise_protection=0.5, ceilings=(1.0, 1.0, 1.0),
+                                  iterations=iterations)
+        vig = tuple(float(v) for v in (-rng.uniform(0.2, 0.4), rng.uniform(0.02, 0.08), -rng.uniform(0.0, 0.02)))
+        optics = OpticsExecution(width=width, height=height, distortion="poly5", distortion_k=(-0.02, 0.005, 0.0),
+                                 tca="linear", tca_red=(1.0003, 0.0, 0.0), tca_blue=(0.9997, 0.0, 0.0),
+                                 vignetting_k=vig, crop_factor=1.0, real_focal=35.0)
+        color = ColorContract(wb_gains=wb, camera_to_rec2020=CAMERA_TO_REC2020, exposure_ev=0.3,
+                              base_lut=standard_base_lut(), tone_lut=sixteen_knot_curve(seed=k),
+                              hsl=hsl_bands(seed=k))
+        out.append(Workload(f"export_{k}", width, height, "RGGB", bits, 1024.0, 65535.0, 0.05, True, wb, sensor,
+                            capture, optics, preview_dimensions(width, height, 2560), color, seed * 1000 + k))
+    return out
+
+
+def hot_pixels(mosaic: np.ndarray, fraction: float = 0.005, seed: int = 0, white: int = 65535) -> np.ndarray:
+    """Stuck-at-white samples at a seeded `fraction` of positions (in place)."""
+    rng = np.random.default_rng(seed)
+    n = int(mosaic.size * fraction)
+    flat = mosaic.reshape(-1)
+    flat[rng.choice(mosaic.size, size=n, replace=False)] = white
+    return mosaic

@@ -193,3 +193,15 @@ def test_opposed_raises_clipped_sites_from_opposing_channels(oracle):
     out, stats, labels, count = oracle.opposed(m, 0, (0.987,) * 3, ceiling=(0.4935, 0.987, 0.616875))
     assert stats[0] == int((red & disc).sum()) and count >= 1
     assert stats[1] + stats[3] == stats[0]
+
+
+def test_counted_amaze_build_is_bit_exact_and_counts(oracle):
+    """The FLOP-census build of AMaZE (counting floats) reconstructs the same
+    bits as the oracle, so its operation counts describe the real algorithm."""
+    m = oracle.amaze_golden_fixture()
+    for balance in ((1.0, 1.0, 1.0), (2.0, 1.0, 1.6)):
+        ref = oracle.demosaic(m, 0, balance, 3)
+        out, ops = oracle.amaze_counted(m, 0, balance)
+        assert np.array_equal(ref.view(np.uint32), out.view(np.uint32))
+        per_px = {k: v / m.size for k, v in ops.items()}
+        assert 300 < per_px["add_sub"] < 600 and 100 < per_px["mul"] < 400 and per_px["div"] > 10

@@ -13,7 +13,8 @@ import numpy as np
 import pytest
 
 from rohditor_gb300 import CaptureContract, ColorContract, OpticsExecution, SensorDescription, clip_levels
-from rohditor_gb300.served import DEVELOP, EDIT, PreviewServer
+from rohditor_gb300 import OutputSpec
+from rohditor_gb300.served import DEVELOP, EDIT, EXPORT, PreviewServer
 
 RD_OK, RD_CANCELLED, RD_OVER_BUDGET = 0, 1, 3
 MB = 1 << 20
@@ -32,8 +33,8 @@ def _image(w=1024, h=1024, seed=0):
 
 def _footprint(w, h, tw, th):
     """Resident bytes of one image and the develop's transient, as the server charges them."""
-    layers = 2 * w * h + 12 * tw * th + (3 * tw * th + 8192)
-    develop = 44 * w * h + 64 * MB
+    layers = 2 * w * h + 12 * w * h + 12 * tw * th + (3 * tw * th + 8192)
+    develop = 32 * w * h + 64 * MB
     return layers, develop
 
 
@@ -175,6 +176,95 @@ def test_dry_close_cancels_pending_requests():
     assert res[edit]["status"] == RD_CANCELLED
     assert s.stats()["resident_bytes"] > 0  # image 0 stays
     s.close()
+
+
+EXPORTS = [OutputSpec(format="srgb8"), OutputSpec(format="extended_f16", primaries="display_p3",
+                                                  policy="chroma_compress", headroom=4.0)]
+
+
+def test_dry_export_fills_the_client_buffers():
+    s = PreviewServer.dry(develop_us=1000, render_us=100)
+    _open(s, 3)
+    _results(s)
+    rid, outs = s.submit_export(3, 1, _edit(0.7), EXPORTS)
+    res = {r["request_id"]: r for r in _results(s)}
+    assert res[rid]["kind"] == EXPORT and res[rid]["status"] == RD_OK
+    assert outs[0].shape == (1024, 3 * 1024) and outs[1].dtype == np.float16
+    assert np.all(outs[0] == 7)
+    assert s.stats()["exports"] == 1
+    s.close()
+
+
+def test_dry_newer_export_replaces_a_pending_one():
+    s = PreviewServer.dry(develop_us=200_000, render_us=100)
+    _open(s, 0)  # the first develop holds the develop lane
+    first, _ = s.submit_export(0, 1, _edit(0.1), EXPORTS[:1])
+    second, outs = s.submit_export(0, 2, _edit(0.2), EXPORTS[:1])
+    res = {r["request_id"]: r for r in _results(s, 5000)}
+    assert res[first]["status"] == RD_CANCELLED and res[second]["status"] == RD_OK
+    assert np.all(outs[0] == 2)
+    s.close()
+
+
+def test_dry_export_is_admitted_against_the_budget():
+    layers, develop = _footprint(1024, 1024, 512, 512)
+    export = 32 * 1024 * 1024 + 6 * 1024 * 1024 + 64 * MB
+    s = PreviewServer.dry(budget_bytes=layers + develop + MB, develop_us=1000, render_us=100)
+    _open(s, 0)
+    _results(s)
+    assert export > develop + MB
+    rid, _ = s.submit_export(0, 1, _edit(0.1), EXPORTS[1:])
+    res = {r["request_id"]: r for r in _results(s)}
+    assert res[rid]["status"] == RD_OVER_BUDGET  # the export's transient does not fit
+    s.close()
+    s = PreviewServer.dry(budget_bytes=layers + export + MB, develop_us=1000, render_us=100)
+    _open(s, 0)
+    _results(s)
+    rid, _ = s.submit_export(0, 1, _edit(0.1), EXPORTS[1:])
+    res = {r["request_id"]: r for r in _results(s)}
+    assert res[rid]["status"] == RD_OK and s.stats()["peak_resident_bytes"] <= layers + export + MB
+    s.close()
+
+
+def test_dry_close_cancels_a_pending_export():
+    s = PreviewServer.dry(develop_us=200_000, render_us=100)
+    _open(s, 0)
+    _open(s, 1)
+    rid, _ = s.submit_export(1, 1, _edit(0.1), EXPORTS[:1])
+    s.close_image(1)
+    res = {r["request_id"]: r for r in _results(s, 5000)}
+    assert res[rid]["status"] == RD_CANCELLED
+    s.close()
+
+
+@pytest.mark.gpu
+def test_served_export_matches_the_direct_path(device):
+    """A served full-resolution export equals develop + spatial pass at the crop
+    size + rd_render_output of the same settings, bit for bit."""
+    from rohditor_gb300 import GpuPreviewProcessor, GpuSensorProcessor, GpuSpatialProcessor
+    from rohditor_gb300.workloads import CAMERA_TO_REC2020, hsl_bands, sixteen_knot_curve
+
+    server = PreviewServer(0, budget_bytes=2 << 30)
+    raw, desc, cap, optics, wb = _image(w=768, h=512, seed=21)
+    server.open(5, raw, desc, cap, optics, (384, 256), wb, CAMERA_TO_REC2020)
+    color = ColorContract(wb_gains=wb, camera_to_rec2020=CAMERA_TO_REC2020, exposure_ev=0.3,
+                          tone_lut=sixteen_knot_curve(seed=4), hsl=hsl_bands(seed=4))
+    specs = EXPORTS + [OutputSpec(format="srgb16", dither="ordered8x8", orientation="rotate90")]
+    rid, outs = server.submit_export(5, 1, color, specs)
+    server.drain()
+    res = {r["request_id"]: r for r in server.poll(64)}
+    assert res[rid]["kind"] == EXPORT and res[rid]["status"] == RD_OK
+    src = GpuSensorProcessor(device).develop(raw, desc, cap)
+    base = GpuSpatialProcessor(device).reduce_preview(src, optics, (768, 512), wb, CAMERA_TO_REC2020)
+    preview = GpuPreviewProcessor(device)
+    for spec, out in zip(specs, outs):
+        ref, _, _ = preview.render_output(base, color, spec)
+        assert np.array_equal(out.view(np.uint8), ref.view(np.uint8)), spec.format
+    base.release()
+    src.release()
+    st = server.stats()
+    assert st["exports"] == 1 and st["peak_resident_bytes"] <= 2 << 30
+    server.close()
 
 
 @pytest.mark.gpu
