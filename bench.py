@@ -476,7 +476,7 @@ def batched_throughput(args, count: int = 24, lanes: int = 3) -> dict:
     rd_develop_batch with `lanes` concurrent lanes, and the same images one at
     a time (one lane). Host mosaics in, host outputs out, timed end to end."""
     from rohditor_gb300 import Device
-    from rohditor_gb300.batch import BatchImage, develop_batch
+    from rohditor_gb300.batch import BatchImage, PinnedBatch, develop_batch
     from rohditor_gb300.workloads import batched_uneven
 
     dev = Device(0)
@@ -488,9 +488,28 @@ def batched_throughput(args, count: int = 24, lanes: int = 3) -> dict:
     develop_batch(images[:lanes], lanes=lanes)  # warm-up
     _, _, wall = develop_batch(images, lanes=lanes)
     _, _, wall1 = develop_batch(images, lanes=1)
+    # With the mosaics and outputs in pinned host memory (a decoder writing
+    # into pinned buffers): one lane, concurrent lanes, and the batch as one
+    # captured CUDA graph (rd_develop_batch_graph) with `chains` branches,
+    # capture + instantiation timed apart.
+    pinned = PinnedBatch(images)
+    pinned.run(lanes=lanes)  # warm-up
+    p1 = pinned.run(lanes=1)["wall_ms"]
+    pl = pinned.run(lanes=lanes)["wall_ms"]
+    graph = {}
+    for chains in (lanes, 2 * lanes):
+        g = pinned.run(lanes=chains, graph=True)
+        graph[str(chains)] = {"launch_ms": round(g["launch_ms"], 1), "capture_ms": round(g["capture_ms"], 1),
+                              "develops_per_s": round(count / (g["launch_ms"] / 1e3), 2),
+                              "mp_per_s": round(pixels / 1e6 / (g["launch_ms"] / 1e3), 1),
+                              "speedup_vs_one_lane": round(p1 / g["launch_ms"], 3)}
+    pinned.close()
+    pinned_runs = {"one_lane_wall_ms": round(p1, 1), "lanes_wall_ms": round(pl, 1),
+                   "lanes_mp_per_s": round(pixels / 1e6 / (pl / 1e3), 1), "graph_chains": graph}
     return {"images": count, "megapixels": round(pixels / 1e6, 1), "lanes": lanes, "wall_ms": round(wall, 1),
             "develops_per_s": round(count / (wall / 1e3), 2), "mp_per_s": round(pixels / 1e6 / (wall / 1e3), 1),
             "one_lane_wall_ms": round(wall1, 1), "speedup_vs_one_lane": round(wall1 / wall, 3),
+            "pinned_host": pinned_runs,
             "workload": "uneven batch: 12/24/45/60 MP, random CFA phase, Opposed + AMaZE + RL5 + optics + preview"}
 
 

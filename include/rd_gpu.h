@@ -340,6 +340,17 @@ typedef struct rd_batch_item {
   double ms;               /* out: this item's time in its lane */
 } rd_batch_item;
 rd_status rd_develop_batch(int device, rd_batch_item* items, int32_t count, int32_t lanes, double* wall_ms);
+/* The same batch captured into one CUDA graph (uneven develops in one
+ * captured launch graph). `chains` parallel branches each run their share of
+ * the images (k % chains) through develop -> spatial -> render, with every
+ * device buffer allocated and freed inside the graph; the batch is one graph
+ * launch. With host_pinned != 0 the items' mosaic, srgb_out and hist are
+ * pinned host memory (rd_host_alloc) and the graph reads and writes them in
+ * place; otherwise they are staged through pinned copies. Optional timings:
+ * capture_ms (capture + instantiation), launch_ms (launch to completion),
+ * wall_ms (launch plus staging copies). Per-item `ms` is 0. */
+rd_status rd_develop_batch_graph(int device, rd_batch_item* items, int32_t count, int32_t chains,
+                                 int32_t host_pinned, double* wall_ms, double* capture_ms, double* launch_ms);
 
 /* ---- served preview loop ----
  * Replaces the engine's preview worker and caches

@@ -107,7 +107,21 @@ Status set_stream_priority(Context& c, bool high) {
   return Status{};
 }
 
+Status upload(Context& ctx, void* dst, const void* src, size_t bytes) {
+  if (!ctx.capturing) {
+    RD_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx.stream));
+    return Status{};
+  }
+  void* pinned = nullptr;
+  RD_CUDA_TRY(cudaHostAlloc(&pinned, bytes, cudaHostAllocDefault));
+  ctx.pinned_uploads.push_back(pinned);
+  std::memcpy(pinned, src, bytes);
+  RD_CUDA_TRY(cudaMemcpyAsync(dst, pinned, bytes, cudaMemcpyHostToDevice, ctx.stream));
+  return Status{};
+}
+
 Status check_kernel_error(Context& ctx, const char* stage) {
+  if (ctx.capturing) return Status{};  // read after the graph has run
   uint32_t word = 0;
   RD_CUDA_TRY(cudaMemcpyAsync(&word, ctx.d_error, sizeof(word), cudaMemcpyDeviceToHost, ctx.stream));
   RD_CUDA_TRY(cudaStreamSynchronize(ctx.stream));
@@ -365,7 +379,7 @@ struct Timer {
   int n = 0;
   explicit Timer(rd::Context& ctx) : c(ctx) {}
   void mark() {
-    if (n < 8) cudaEventRecord(c.ev[n++], c.stream);
+    if (n < 8 && !c.capturing) cudaEventRecord(c.ev[n++], c.stream);
   }
   float span(int a, int b) const {
     float ms = 0.0f;
@@ -429,7 +443,7 @@ Status develop_impl(rd_ctx* h, const uint16_t* d_raw, size_t row_stride, const r
   tm.mark();
   if (d_mosaic) rd::device_free(ctx, d_mosaic, mosaic_bytes);
   uint64_t host_stats[16] = {};
-  if (st.ok()) {
+  if (st.ok() && !ctx.capturing) {
     const cudaError_t e = cudaMemcpyAsync(host_stats, d_stats, sizeof(host_stats), cudaMemcpyDeviceToHost, ctx.stream);
     if (e != cudaSuccess) st = Status{RD_READBACK, cudaGetErrorString(e)};
   }
@@ -526,6 +540,7 @@ void rd_ctx_destroy(rd_ctx* h) {
   if (c.amaze_scratch) rd::device_free(c, c.amaze_scratch, 0);
   if (c.flush_buf) rd::device_free(c, c.flush_buf, c.flush_bytes);
   cudaStreamSynchronize(c.stream);
+  for (void* p : c.pinned_uploads) cudaFreeHost(p);
   rd::resolve_kernel_timing(c);
   for (auto e : c.event_pool) cudaEventDestroy(e);
   for (auto& e : c.user_ev)
@@ -717,6 +732,19 @@ rd_status rd_render(rd_ctx* h, const rd_base* cbase, const rd_color_desc* color,
   rd_status s = rd_render_device(h, base, color, metrics);
   if (s != RD_OK) return s;
   rd::Context& ctx = h->c;
+  if (ctx.capturing) {
+    // Graph capture: copies straight into the caller's (pinned) buffers, which
+    // must live until the graph has run; clip counts come from the histogram.
+    if (clipped) return finish(h, Status{RD_INVALID_INPUT, "clip counts are not read back under graph capture"});
+    Status cs;
+    if (srgb_out && cudaMemcpyAsync(srgb_out, base->d_srgb, (size_t)3 * base->W * base->H, cudaMemcpyDeviceToHost,
+                                    ctx.stream) != cudaSuccess)
+      cs = Status{RD_READBACK, "output readback failed"};
+    if (cs.ok() && hist &&
+        cudaMemcpyAsync(hist, base->d_hist, 1024 * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx.stream) != cudaSuccess)
+      cs = Status{RD_READBACK, "histogram readback failed"};
+    return finish(h, cs);
+  }
   uint64_t bins[1024];
   Status st;
   if (srgb_out &&

@@ -971,6 +971,22 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
 
 }  // namespace
 
+// Allocates the per-CTA slabs for the largest grid (one CTA per SM) up front,
+// so that later launches never allocate (a graph capture needs that).
+Status reserve_amaze_scratch(Context& ctx) {
+  const size_t sms = ctx.sm_count > 0 ? (size_t)ctx.sm_count : 152;
+  if (ctx.amaze_slots >= sms) return Status{};
+  if (ctx.amaze_scratch) device_free(ctx, ctx.amaze_scratch, ctx.amaze_slots * SLAB_FLOATS * sizeof(float));
+  ctx.amaze_scratch = nullptr;
+  ctx.amaze_slots = 0;
+  void* p = nullptr;
+  RD_TRY(device_alloc(ctx, sms * SLAB_FLOATS * sizeof(float), &p));
+  RD_CUDA_TRY(cudaMemsetAsync(p, 0, sms * SLAB_FLOATS * sizeof(float), ctx.stream));
+  ctx.amaze_scratch = static_cast<float*>(p);
+  ctx.amaze_slots = sms;
+  return Status{};
+}
+
 Status run_amaze(Context& ctx, const MosaicSource& src, const float gains[3], float clip_point, float* rgb,
                  int count_clip, unsigned long long* clip_stats) {
   const int tiles_x = (src.width + VALID - 1) / VALID, tiles_y = (src.height + VALID - 1) / VALID;

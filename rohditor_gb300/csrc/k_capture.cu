@@ -30,7 +30,11 @@ namespace {
 
 constexpr float FLOOR = 1.0e-6f;
 constexpr int MAX_TAPS = 9;  // radius <= 4 for sigma <= 1.2 (CAPTURE_RADIUS_RANGE)
-__constant__ float c_kernel[MAX_TAPS];
+// The Gaussian taps travel with each launch (by value), so concurrent develops
+// with different radii never share them.
+struct Taps {
+  float w[MAX_TAPS];
+};
 
 __device__ __forceinline__ float smoothstep(float low, float high, float value) {
   float t = (value - low) / (high - low);
@@ -142,14 +146,14 @@ template <int R>
 __global__ void __launch_bounds__(128) rl_stream_kernel(const float* __restrict__ est_in,
                                                         const float* __restrict__ guide,
                                                         float* __restrict__ est_out, int W, int H, int strips,
-                                                        int seg_h, int items) {
+                                                        int seg_h, int items, const Taps taps) {
   using G = StreamGeom<R>;
   constexpr int T = G::T, SW = G::SW, QW = G::QW, EW = G::EW, BH = G::BH;
   extern __shared__ float4 rl_smem_raw[];
   StreamSmem<R>& S = *reinterpret_cast<StreamSmem<R>*>(rl_smem_raw);
   float w[T];
 #pragma unroll
-  for (int k = 0; k < T; ++k) w[k] = c_kernel[k];
+  for (int k = 0; k < T; ++k) w[k] = taps.w[k];
   const int tid = threadIdx.x;
   for (int item = blockIdx.x; item < items; item += gridDim.x) {
     const int x0 = (item % strips) * SW, y0 = (item / strips) * seg_h;
@@ -298,7 +302,7 @@ __global__ void __launch_bounds__(128) rl_stream_kernel(const float* __restrict_
 }
 
 template <int R>
-Status launch_rl_iter(Context& ctx, const float* est, const float* guide, float* out, int W, int H) {
+Status launch_rl_iter(Context& ctx, const float* est, const float* guide, float* out, int W, int H, const Taps& taps) {
   using G = StreamGeom<R>;
   const size_t smem = sizeof(StreamSmem<R>);
   RD_CUDA_TRY(cudaFuncSetAttribute(rl_stream_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -317,7 +321,7 @@ Status launch_rl_iter(Context& ctx, const float* est, const float* guide, float*
   const int items = strips * nseg;
   const int grid = std::min(items, slots);
   RD_LAUNCH(ctx, K_RL_ITER, rl_stream_kernel<R><<<grid, 128, smem, ctx.stream>>>(est, guide, out, W, H, strips,
-                                                                               seg_h, items));
+                                                                               seg_h, items, taps));
   return Status{};
 }
 
@@ -343,14 +347,14 @@ template <int R>
 __global__ void __launch_bounds__(128) rl_prep_kernel(const float* __restrict__ rgb, long long plane, float c0,
                                                       float c1, float c2, float noise, float* __restrict__ guide,
                                                       float* __restrict__ mask, int W, int H, int strips, int seg_h,
-                                                      int items, unsigned* error) {
+                                                      int items, unsigned* error, const Taps taps) {
   using S_ = PrepSmem<R>;
   constexpr int T = 2 * R + 1, SW = S_::SW, RS = S_::RS, BH = 8;
   extern __shared__ float4 rl_smem_raw[];
   S_& S = *reinterpret_cast<S_*>(rl_smem_raw);
   float w[T];
 #pragma unroll
-  for (int k = 0; k < T; ++k) w[k] = c_kernel[k];
+  for (int k = 0; k < T; ++k) w[k] = taps.w[k];
   const int tid = threadIdx.x;
   bool bad = false;
   for (int item = blockIdx.x; item < items; item += gridDim.x) {
@@ -448,7 +452,7 @@ __global__ void __launch_bounds__(128) rl_prep_kernel(const float* __restrict__ 
 }
 
 template <int R>
-Status launch_rl_prep(Context& ctx, const float* rgb, long long plane, const float ceil[3], float noise, float* guide,
+Status launch_rl_prep(Context& ctx, const Taps& taps, const float* rgb, long long plane, const float ceil[3], float noise, float* guide,
                       float* mask, int W, int H) {
   using S_ = PrepSmem<R>;
   const size_t smem = sizeof(S_);
@@ -467,27 +471,28 @@ Status launch_rl_prep(Context& ctx, const float* rgb, long long plane, const flo
   const int grid = std::min(items, slots);
   RD_LAUNCH(ctx, K_RL_MASK, rl_prep_kernel<R><<<grid, 128, smem, ctx.stream>>>(
                                 rgb, plane, ceil[0], ceil[1], ceil[2], noise, guide, mask, W, H, strips, seg_h, items,
-                                ctx.d_error));
+                                ctx.d_error, taps));
   return Status{};
 }
 
-Status rl_prep(Context& ctx, int r, const float* rgb, long long plane, const float ceil[3], float noise, float* guide,
+Status rl_prep(Context& ctx, int r, const Taps& taps, const float* rgb, long long plane, const float ceil[3], float noise, float* guide,
                float* mask, int W, int H) {
   switch (r) {
-    case 1: return launch_rl_prep<1>(ctx, rgb, plane, ceil, noise, guide, mask, W, H);
-    case 2: return launch_rl_prep<2>(ctx, rgb, plane, ceil, noise, guide, mask, W, H);
-    case 3: return launch_rl_prep<3>(ctx, rgb, plane, ceil, noise, guide, mask, W, H);
-    case 4: return launch_rl_prep<4>(ctx, rgb, plane, ceil, noise, guide, mask, W, H);
+    case 1: return launch_rl_prep<1>(ctx, taps, rgb, plane, ceil, noise, guide, mask, W, H);
+    case 2: return launch_rl_prep<2>(ctx, taps, rgb, plane, ceil, noise, guide, mask, W, H);
+    case 3: return launch_rl_prep<3>(ctx, taps, rgb, plane, ceil, noise, guide, mask, W, H);
+    case 4: return launch_rl_prep<4>(ctx, taps, rgb, plane, ceil, noise, guide, mask, W, H);
     default: return Status{RD_INVALID_INPUT, "capture radius outside 1..4"};
   }
 }
 
-Status rl_iteration(Context& ctx, int r, const float* est, const float* guide, float* out, int W, int H) {
+Status rl_iteration(Context& ctx, int r, const Taps& taps, const float* est, const float* guide, float* out, int W,
+                    int H) {
   switch (r) {
-    case 1: return launch_rl_iter<1>(ctx, est, guide, out, W, H);
-    case 2: return launch_rl_iter<2>(ctx, est, guide, out, W, H);
-    case 3: return launch_rl_iter<3>(ctx, est, guide, out, W, H);
-    case 4: return launch_rl_iter<4>(ctx, est, guide, out, W, H);
+    case 1: return launch_rl_iter<1>(ctx, est, guide, out, W, H, taps);
+    case 2: return launch_rl_iter<2>(ctx, est, guide, out, W, H, taps);
+    case 3: return launch_rl_iter<3>(ctx, est, guide, out, W, H, taps);
+    case 4: return launch_rl_iter<4>(ctx, est, guide, out, W, H, taps);
     default: return Status{RD_INVALID_INPUT, "capture radius outside 1..4"};
   }
 }
@@ -655,8 +660,8 @@ Status prepare_vignetting(Context& ctx, const rd_optics_desc& o, int W, int H, V
   t.incr = static_cast<float*>(p);
   t.r2_start = t.incr + W;
   t.checkpoints = t.r2_start + H;
-  RD_CUDA_TRY(cudaMemcpyAsync(t.incr, incr.data(), sizeof(float) * W, cudaMemcpyHostToDevice, ctx.stream));
-  RD_CUDA_TRY(cudaMemcpyAsync(t.r2_start, r2s.data(), sizeof(float) * H, cudaMemcpyHostToDevice, ctx.stream));
+  RD_TRY(upload(ctx, t.incr, incr.data(), sizeof(float) * W));
+  RD_TRY(upload(ctx, t.r2_start, r2s.data(), sizeof(float) * H));
   RD_LAUNCH(ctx, K_VIGNETTE, vignette_scan_kernel<<<(H + 127) / 128, 128, 0, ctx.stream>>>(t.incr, t.r2_start, W, H, t.checkpoints, t.segs));
   RD_CUDA_TRY(cudaGetLastError());
   return Status{};
@@ -726,6 +731,7 @@ Status run_capture(Context& ctx, float* rgb, int W, int H, const rd_detail_desc&
   float* planes = nullptr;
   size_t plane_bytes = 0;
   int r = 0;
+  Taps taps{};
   if (capture) {
     if (!(detail.radius >= 0.3f && detail.radius <= 1.2f) || !(detail.amount <= 1.0f) ||
         !(detail.noise_protection >= 0.0f && detail.noise_protection <= 1.0f))
@@ -733,11 +739,9 @@ Status run_capture(Context& ctx, float* rgb, int W, int H, const rd_detail_desc&
     for (int c = 0; c < 3; ++c)
       if (!std::isfinite(detail.ceilings[c]) || !(detail.ceilings[c] > 0.0f))
         return Status{RD_INVALID_INPUT, "capture ceilings must be finite and positive"};
-    float w[MAX_TAPS];
-    const int taps = gaussian_kernel(detail.radius, w, MAX_TAPS);
-    if (taps < 0) return Status{RD_INVALID_INPUT, "capture radius too large"};
-    r = taps / 2;
-    RD_CUDA_TRY(cudaMemcpyToSymbolAsync(c_kernel, w, sizeof(float) * taps, 0, cudaMemcpyHostToDevice, ctx.stream));
+    const int ntaps = gaussian_kernel(detail.radius, taps.w, MAX_TAPS);
+    if (ntaps < 0) return Status{RD_INVALID_INPUT, "capture radius too large"};
+    r = ntaps / 2;
     plane_bytes = sizeof(float) * (size_t)plane * 4;
     void* p = nullptr;
     RD_TRY(device_alloc(ctx, plane_bytes, &p));
@@ -751,9 +755,9 @@ Status run_capture(Context& ctx, float* rgb, int W, int H, const rd_detail_desc&
   const float* est = guide;
   Status st;
   if (capture) {
-    st = rl_prep(ctx, r, rgb, plane, detail.ceilings, detail.noise_protection, guide, mask, W, H);
+    st = rl_prep(ctx, r, taps, rgb, plane, detail.ceilings, detail.noise_protection, guide, mask, W, H);
     for (int it = 0; it < detail.iterations && st.ok(); ++it) {
-      st = rl_iteration(ctx, r, est, guide, est_buf[it & 1], W, H);
+      st = rl_iteration(ctx, r, taps, est, guide, est_buf[it & 1], W, H);
       est = est_buf[it & 1];
     }
     if (st.ok() && cudaGetLastError() != cudaSuccess) st = Status{RD_SYNCHRONIZATION, "capture kernels failed to launch"};

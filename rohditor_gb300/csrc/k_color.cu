@@ -155,9 +155,9 @@ Status run_color_output(Context& ctx, const float* rgb, int W, int H, const rd_c
     RD_TRY(device_alloc(ctx, lut_bytes, &d));
     luts = static_cast<float*>(d);
     if (c.has_base_lut)
-      RD_CUDA_TRY(cudaMemcpyAsync(luts, c.base_lut, sizeof(float) * 4096, cudaMemcpyHostToDevice, ctx.stream));
+      RD_TRY(upload(ctx, luts, c.base_lut, sizeof(float) * 4096));
     if (c.has_tone_lut)
-      RD_CUDA_TRY(cudaMemcpyAsync(luts + 4096, c.tone_lut, sizeof(float) * 4096, cudaMemcpyHostToDevice, ctx.stream));
+      RD_TRY(upload(ctx, luts + 4096, c.tone_lut, sizeof(float) * 4096));
   }
   p.adj.base_lut = c.has_base_lut ? luts : nullptr;
   p.adj.tone_lut = c.has_tone_lut ? luts + 4096 : nullptr;

@@ -382,7 +382,7 @@ Status run_optics_gather(Context& ctx, const rd_optics_desc& o, const float* rgb
   void* d = nullptr;
   RD_TRY(device_alloc(ctx, sizeof(float) * tab.size(), &d));
   float* dtab = static_cast<float*>(d);
-  RD_CUDA_TRY(cudaMemcpyAsync(dtab, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice, ctx.stream));
+  RD_TRY(upload(ctx, dtab, tab.data(), sizeof(float) * tab.size()));
   OpticsParams p{};
   p.in = rgb_in;
   p.mult = mult;
@@ -447,7 +447,7 @@ Status run_area_reduce(Context& ctx, const float* rgb, const float* mult, int W,
   void* d = nullptr;
   RD_TRY(device_alloc(ctx, bytes, &d));
   unsigned char* b = static_cast<unsigned char*>(d);
-  RD_CUDA_TRY(cudaMemcpyAsync(b, host.data(), bytes, cudaMemcpyHostToDevice, ctx.stream));
+  RD_TRY(upload(ctx, b, host.data(), bytes));
   const int* hf = reinterpret_cast<const int*>(b);
   const int* ho = hf + tw;
   const int* hc = ho + tw;

@@ -72,6 +72,12 @@ struct Context {
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
   double family_ms[K_FAMILY_COUNT] = {};
   uint64_t family_launches[K_FAMILY_COUNT] = {};
+  // While the stream is being captured into a CUDA graph: no host
+  // synchronisation or readback (errors are read after the graph runs), and
+  // host tables reach the device from pinned copies kept until the context
+  // is destroyed.
+  bool capturing = false;
+  std::vector<void*> pinned_uploads;
 };
 
 // Brackets one kernel launch with events when kernel timing is enabled, and
@@ -91,6 +97,11 @@ void resolve_kernel_timing(Context& ctx);
     ::rd::LaunchScope rd_scope_((ctx), (family)); \
     __VA_ARGS__;                                 \
   } while (0)
+
+// Host -> device copy of a host table on the context's stream. The source may
+// be released as soon as the call returns (under capture it is copied into a
+// pinned buffer that the graph reads).
+Status upload(Context& ctx, void* dst, const void* src, size_t bytes);
 
 Status reserve(Context& ctx, size_t bytes);
 void release(Context& ctx, size_t bytes);
@@ -234,6 +245,8 @@ Status run_display_output(Context& ctx, const float* rgb, const rd_color_desc& c
                           unsigned long long* d_gamut);
 // Exhaustive device checks of the correctly rounded arithmetic (rd_check_math).
 Status run_math_check(Context& ctx, int which, uint64_t* result);
+
+Status reserve_amaze_scratch(Context& ctx);
 
 // Host contract helpers.
 int gaussian_kernel(float sigma, float* weights, int max_taps);

@@ -363,8 +363,11 @@ def test_develop_with_opposed(device, oracle):
     assert float(np.max(np.abs(got - ref))) <= 1e-4
 
 
-def test_batched_develop_matches_one_at_a_time(device):
-    """rd_develop_batch over uneven sizes and CFA phases equals the per-image path, bit for bit."""
+@pytest.mark.parametrize("graph", [False, True])
+def test_batched_develop_matches_one_at_a_time(device, graph):
+    """rd_develop_batch (concurrent lanes) and rd_develop_batch_graph (one
+    captured CUDA graph) over uneven sizes, CFA phases and capture radii equal
+    the per-image path, bit for bit."""
     from rohditor_gb300 import (CaptureContract, ColorContract, GpuPreviewProcessor, GpuSensorProcessor,
                                 GpuSpatialProcessor, OpticsExecution, SensorDescription, clip_levels, opposed_levels)
     from rohditor_gb300.batch import BatchImage, develop_batch
@@ -386,15 +389,25 @@ def test_batched_develop_matches_one_at_a_time(device):
                                        detection_levels=det, neutral_ceiling=neutral, demosaic="amaze",
                                        demosaic_balance=wb)
             ceil = (1.0, 1.0, 1.0)
-        cap = CaptureContract(amount=0.5, radius=0.7, noise_protection=0.5, ceilings=ceil, iterations=5)
+        cap = CaptureContract(amount=0.5, radius=0.7 if k % 2 == 0 else 1.1, noise_protection=0.5, ceilings=ceil,
+                              iterations=5)
         optics = OpticsExecution(w, h, distortion="poly5", distortion_k=(-0.02, 0.005, 0.0), tca="linear",
                                  tca_red=(1.0003, 0, 0), tca_blue=(0.9997, 0, 0), vignetting_k=(-0.3, 0.05, -0.01))
         color = ColorContract(wb_gains=wb, camera_to_rec2020=CAMERA_TO_REC2020, exposure_ev=0.1 * k,
                               tone_lut=sixteen_knot_curve(seed=k), hsl=hsl_bands(seed=k))
         images.append(BatchImage(raw, sensor, cap, optics, preview_dimensions(w, h, 256), wb, CAMERA_TO_REC2020,
                                  color))
-    outs, ms, wall = develop_batch(images, lanes=3)
-    assert wall > 0 and all(m > 0 for m in ms)
+    res = develop_batch(images, lanes=3, graph=graph)
+    outs, ms, wall = res[:3]
+    assert wall > 0 and (graph or all(m > 0 for m in ms))
+    if graph:
+        # Pinned buffers used in place by the graph give the same outputs.
+        from rohditor_gb300.batch import PinnedBatch
+        pinned = PinnedBatch(images)
+        pinned.run(lanes=2, graph=True)
+        for (a, ha), (b, hb) in zip(outs, pinned.outputs()):
+            assert np.array_equal(a, b) and np.array_equal(ha, hb)
+        pinned.close()
     for im, (srgb, hist) in zip(images, outs):
         src = GpuSensorProcessor(device).develop(im.mosaic, im.sensor, im.capture)
         base = GpuSpatialProcessor(device).reduce_preview(src, im.optics, im.target, im.wb_gains,
