@@ -134,6 +134,7 @@ Status check_kernel_error(Context& ctx, const char* stage) {
     if (word & 4u) what += " invalid vignetting gain;";
     if (word & 8u) what += " optics footprint outside the image or non-finite coordinate;";
     if (word & 16u) what += " highlight reconstruction failed;";
+    if (word & 32u) what += " capture-sharpening tensor copy timed out;";
     return Status{RD_INVALID_INPUT, std::string(stage) + ":" + what};
   }
   return Status{};

@@ -19,9 +19,11 @@
 // Iterator::sum does) and its half-sample mirror at the image edges. Field
 // values outside the image are filled from their mirror position, so every
 // stencil read equals the reference's mirrored read bit for bit.
+#include <cuda.h>  // CUtensorMap and its enums; the encoder is reached through the runtime
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "rd_internal.cuh"
 
@@ -64,8 +66,13 @@ __device__ __forceinline__ int mirror_half(int index, int length) {
 // ---- one RL iteration, streamed down column strips --------------------------
 // A CTA owns a strip of SW = 128 - 2R output columns and a segment of rows and
 // walks the segment top to bottom in steps of BH rows:
-//   * estimate rows arrive by cp.async one step ahead into a 24-row ring
-//     (the guide is read from L2 where it is used);
+//   * estimate rows arrive one step ahead into a 24-row ring (the guide is
+//     read from L2 where it is used): on interior strips one thread loads each
+//     8-row block with a TMA tensor copy (cp.async.bulk.tensor, completion on
+//     an mbarrier, the block's x start rounded down to 16 bytes and the
+//     remainder applied when reading); strips at the image edge, whose
+//     columns are mirrored, and images whose rows are not a multiple of 16
+//     bytes copy 4-byte elements with cp.async;
 //   * the horizontal pass of blur #1 runs on every arriving row; the vertical
 //     pass and the ratio run R rows behind, the horizontal pass of blur #2 on
 //     the same rows, and the vertical pass of blur #2 with the bounded update
@@ -85,18 +92,59 @@ struct StreamGeom {
   static constexpr int SW = QW - 2 * R;  // output columns of a strip
   static constexpr int EW = QW + 2 * R;  // estimate columns [x0 - 2R, x0 + SW + 2R)
   static constexpr int BH = 8, RIN = 24, RS = 16;  // RIN >= 2 BH + 2R: rows in use plus rows in flight
+  // Estimate row stride in smem: EW columns plus up to 3 of TMA alignment
+  // remainder, a multiple of 16 bytes; an 8-row block is 35 x 128 bytes.
+  static constexpr int EWP = 140;
+  static_assert(EW + 3 <= EWP && (EWP * 4) % 16 == 0 && (BH * EWP * 4) % 128 == 0, "estimate ring layout");
   static constexpr int H1_RUNS = 15, H1_RUN = (QW + H1_RUNS - 1) / H1_RUNS;
   static constexpr int H2_RUN = 8, H2_RUNS = (SW + H2_RUN - 1) / H2_RUN;
 };
 
 template <int R>
-struct StreamSmem {
+struct __align__(128) StreamSmem {
   using G = StreamGeom<R>;
-  float e[G::RIN][G::EW];   // estimate rows
+  float e[G::RIN][G::EWP];  // estimate rows (first: 128-byte aligned TMA blocks)
   float t1[G::RS][G::QW];   // horizontal pass of blur #1
   float q[G::BH][G::QW];    // ratio rows of the current step
   float t2[G::RS][G::QW];   // horizontal pass of blur #2 (first SW columns)
+  unsigned long long bar[3];  // one mbarrier per 8-row block of the estimate ring
 };
+
+// ---- TMA and mbarrier (inline PTX) -------------------------------------------
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// 2D tensor copy of the box at (x, y) into shared memory, completing on `bar`.
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::"r"(
+          smem_addr(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(smem_addr(bar))
+      : "memory");
+}
+// Bounded wait for a block's copy: sets `failed` (and the error word) instead
+// of spinning forever.
+constexpr unsigned RL_TMA_TIMEOUT = 32u;
+__device__ __forceinline__ void tma_wait(unsigned long long* bar, unsigned parity, bool& failed, unsigned* error) {
+  if (failed) return;
+  for (int i = 0; i < (1 << 20); ++i)
+    if (mbar_try_wait(bar, parity)) return;
+  failed = true;
+  atomicOr(error, RL_TMA_TIMEOUT);
+}
 
 __device__ __forceinline__ void cp_async4(float* smem, const float* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
@@ -146,29 +194,58 @@ template <int R>
 __global__ void __launch_bounds__(128) rl_stream_kernel(const float* __restrict__ est_in,
                                                         const float* __restrict__ guide,
                                                         float* __restrict__ est_out, int W, int H, int strips,
-                                                        int seg_h, int items, const Taps taps) {
+                                                        int seg_h, int items, const Taps taps,
+                                                        const __grid_constant__ CUtensorMap est_map, int use_tma,
+                                                        unsigned* error) {
   using G = StreamGeom<R>;
   constexpr int T = G::T, SW = G::SW, QW = G::QW, EW = G::EW, BH = G::BH;
-  extern __shared__ float4 rl_smem_raw[];
+  extern __shared__ __align__(128) float4 rl_smem_raw[];
   StreamSmem<R>& S = *reinterpret_cast<StreamSmem<R>*>(rl_smem_raw);
   float w[T];
 #pragma unroll
   for (int k = 0; k < T; ++k) w[k] = taps.w[k];
   const int tid = threadIdx.x;
+  if (use_tma) {
+    if (tid == 0) {
+      for (int b = 0; b < 3; ++b) mbar_init(&S.bar[b]);
+      asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+  }
+  unsigned phases = 0;  // parity of the next completion of each block's barrier
+  bool tma_failed = false;
   for (int item = blockIdx.x; item < items; item += gridDim.x) {
     const int x0 = (item % strips) * SW, y0 = (item / strips) * seg_h;
     const int y1 = min(y0 + seg_h, H);
     const int e_end = min(y1 + 2 * R, H), q_end = min(y1 + R, H);
     int e_next = max(y0 - 2 * R, 0), q_next = max(y0 - R, 0), o_next = y0;
     const bool edge = x0 - 2 * R < 0 || x0 + SW + 2 * R > W;
-    // Estimate rows [r0, r1) into the input ring: this thread copies window
-    // columns tid and tid + 128 (mirrored into the image).
+    const bool tma = use_tma && !edge;
+    // Row r of the segment lives in ring slot (r - ebase) % RIN, so each step's
+    // 8 rows fill one contiguous block of the ring.
+    const int ebase = e_next;
+    // Column c of the window [x0 - 2R, x0 + SW + 2R) sits at c + rem of its row.
+    const int xal = (x0 - 2 * R) & ~3;
+    const int rem = tma ? (x0 - 2 * R) - xal : 0;
+    // Estimate rows [r0, r1) into the input ring: with TMA one block by thread
+    // 0; else this thread copies window columns tid and tid + 128 (mirrored
+    // into the image).
     const int xa = x0 - 2 * R + tid, xb = xa + 128;
     const int sxa = (unsigned)xa < (unsigned)W ? xa : mirror_half(xa, W);
     const bool has_b = tid + 128 < EW;
     const int sxb = has_b ? ((unsigned)xb < (unsigned)W ? xb : mirror_half(xb, W)) : 0;
     auto issue = [&](int r0, int r1) {
-      int slot = r0 % G::RIN;
+      if (r0 >= r1) return;
+      if (tma) {
+        if (tid == 0) {
+          const int b = ((r0 - ebase) / BH) % 3;
+          asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+          mbar_expect_tx(&S.bar[b], BH * G::EWP * sizeof(float));
+          tma_load_2d(S.e[b * BH], &est_map, xal, r0, &S.bar[b]);
+        }
+        return;
+      }
+      int slot = (r0 - ebase) % G::RIN;
       const float* src = est_in + (long long)r0 * W;
       for (int r = r0; r < r1; ++r) {
         float* dst = S.e[slot];
@@ -204,13 +281,21 @@ __global__ void __launch_bounds__(128) rl_stream_kernel(const float* __restrict_
       issue(e_hi, min(e_hi + BH, e_end));
       cp_async_commit();
       cp_async_wait1();
+      if (tma && e_hi > e_next) {
+        const int b = ((e_next - ebase) / BH) % 3;
+        tma_wait(&S.bar[b], (phases >> b) & 1u, tma_failed, error);
+        phases ^= 1u << b;
+      }
       __syncthreads();
       // 1. horizontal pass of blur #1 on rows [e_next, e_hi)
+      const int eslot = (e_next - ebase) % G::RIN;  // first slot of this step's block
       for (int k = tid; k < (e_hi - e_next) * G::H1_RUNS; k += 128) {
-        const int r = e_next + k / G::H1_RUNS, s = k % G::H1_RUNS;
+        const int rr = k / G::H1_RUNS, s = k % G::H1_RUNS;
+        const int r = e_next + rr;
         const int qc0 = s * G::H1_RUN;
         const int n = min(G::H1_RUN, QW - qc0);
-        if (n > 0) hrun<R, G::H1_RUN>(S.e[r % G::RIN], qc0 + R, n, S.t1[r & (G::RS - 1)] + qc0, x0 - R + qc0, W, w);
+        if (n > 0)
+          hrun<R, G::H1_RUN>(S.e[eslot + rr] + rem, qc0 + R, n, S.t1[r & (G::RS - 1)] + qc0, x0 - R + qc0, W, w);
       }
       __syncthreads();
       // 2. vertical pass of blur #1 and the ratio on rows [q_next, q_hi), column tid
@@ -271,7 +356,7 @@ __global__ void __launch_bounds__(128) rl_stream_kernel(const float* __restrict_
               win[j] = j < n + 2 * R ? S.t2[mirror_row(o_next - R + j, H) & (G::RS - 1)][tid] : 0.0f;
           }
           const long long o0 = (long long)o_next * W + x;
-          const int es = o_next % G::RIN;
+          const int es = (o_next - ebase) % G::RIN;
 #pragma unroll
           for (int j = 0; j < BH; ++j) {
             if (j < n) {
@@ -281,7 +366,7 @@ __global__ void __launch_bounds__(128) rl_stream_kernel(const float* __restrict_
               const long long o = o0 + (long long)j * W;
               const float g = go[j];
               const int slot = es + j < G::RIN ? es + j : es + j - G::RIN;
-              float e = S.e[slot][tid + 2 * R] * b;
+              float e = S.e[slot][tid + 2 * R + rem] * b;
               const float lo = g * 0.5f, hi = g * 2.0f;
               if (e < lo) e = lo;
               if (e > hi) e = hi;
@@ -302,7 +387,8 @@ __global__ void __launch_bounds__(128) rl_stream_kernel(const float* __restrict_
 }
 
 template <int R>
-Status launch_rl_iter(Context& ctx, const float* est, const float* guide, float* out, int W, int H, const Taps& taps) {
+Status launch_rl_iter(Context& ctx, const float* est, const float* guide, float* out, int W, int H, const Taps& taps,
+                      const CUtensorMap* est_map) {
   using G = StreamGeom<R>;
   const size_t smem = sizeof(StreamSmem<R>);
   RD_CUDA_TRY(cudaFuncSetAttribute(rl_stream_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -320,8 +406,10 @@ Status launch_rl_iter(Context& ctx, const float* est, const float* guide, float*
   const int nseg = (H + seg_h - 1) / seg_h;
   const int items = strips * nseg;
   const int grid = std::min(items, slots);
-  RD_LAUNCH(ctx, K_RL_ITER, rl_stream_kernel<R><<<grid, 128, smem, ctx.stream>>>(est, guide, out, W, H, strips,
-                                                                               seg_h, items, taps));
+  CUtensorMap none{};
+  RD_LAUNCH(ctx, K_RL_ITER, rl_stream_kernel<R><<<grid, 128, smem, ctx.stream>>>(
+                                est, guide, out, W, H, strips, seg_h, items, taps, est_map ? *est_map : none,
+                                est_map ? 1 : 0, ctx.d_error));
   return Status{};
 }
 
@@ -486,13 +574,48 @@ Status rl_prep(Context& ctx, int r, const Taps& taps, const float* rgb, long lon
   }
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry-point query (no
+// link against the driver library); null when unavailable.
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiled tensor_map_encoder() {
+  static EncodeTiled fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiled>(p);
+    else
+      cudaGetLastError();
+  });
+  return fn;
+}
+
+// Tensor map of one f32 plane for the estimate ring's 140x8 boxes; false when
+// TMA cannot address it (row stride not a multiple of 16 bytes, or no encoder).
+bool make_plane_map(CUtensorMap* map, const float* plane, int W, int H) {
+  if (W % 4 != 0 || reinterpret_cast<uintptr_t>(plane) % 16 != 0) return false;
+  const EncodeTiled enc = tensor_map_encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)W, (cuuint64_t)H};
+  const cuuint64_t strides[1] = {(cuuint64_t)W * sizeof(float)};
+  const cuuint32_t box[2] = {(cuuint32_t)StreamGeom<1>::EWP, (cuuint32_t)StreamGeom<1>::BH};
+  const cuuint32_t elem[2] = {1, 1};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(plane), dims, strides, box, elem,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 Status rl_iteration(Context& ctx, int r, const Taps& taps, const float* est, const float* guide, float* out, int W,
-                    int H) {
+                    int H, const CUtensorMap* est_map) {
   switch (r) {
-    case 1: return launch_rl_iter<1>(ctx, est, guide, out, W, H, taps);
-    case 2: return launch_rl_iter<2>(ctx, est, guide, out, W, H, taps);
-    case 3: return launch_rl_iter<3>(ctx, est, guide, out, W, H, taps);
-    case 4: return launch_rl_iter<4>(ctx, est, guide, out, W, H, taps);
+    case 1: return launch_rl_iter<1>(ctx, est, guide, out, W, H, taps, est_map);
+    case 2: return launch_rl_iter<2>(ctx, est, guide, out, W, H, taps, est_map);
+    case 3: return launch_rl_iter<3>(ctx, est, guide, out, W, H, taps, est_map);
+    case 4: return launch_rl_iter<4>(ctx, est, guide, out, W, H, taps, est_map);
     default: return Status{RD_INVALID_INPUT, "capture radius outside 1..4"};
   }
 }
@@ -756,9 +879,16 @@ Status run_capture(Context& ctx, float* rgb, int W, int H, const rd_detail_desc&
   Status st;
   if (capture) {
     st = rl_prep(ctx, r, taps, rgb, plane, detail.ceilings, detail.noise_protection, guide, mask, W, H);
+    // Tensor maps of the three planes an iteration can read (guide, then the
+    // ping-pong estimates), for the TMA-fed estimate ring.
+    CUtensorMap maps[3];
+    const bool tma = make_plane_map(&maps[0], guide, W, H) && make_plane_map(&maps[1], est_buf[0], W, H) &&
+                     make_plane_map(&maps[2], est_buf[1], W, H);
+    const CUtensorMap* in_map = tma ? &maps[0] : nullptr;
     for (int it = 0; it < detail.iterations && st.ok(); ++it) {
-      st = rl_iteration(ctx, r, taps, est, guide, est_buf[it & 1], W, H);
+      st = rl_iteration(ctx, r, taps, est, guide, est_buf[it & 1], W, H, in_map);
       est = est_buf[it & 1];
+      in_map = tma ? &maps[1 + (it & 1)] : nullptr;
     }
     if (st.ok() && cudaGetLastError() != cudaSuccess) st = Status{RD_SYNCHRONIZATION, "capture kernels failed to launch"};
   }
