@@ -168,6 +168,18 @@ def family_bytes(name: str, N: int, n: int, H: int, tw: int) -> float | None:
     return table.get(name)
 
 
+def rl_shape_record(W: int, H: int, radius: float) -> dict | None:
+    """Row segments per strip of the RL iteration that the first (warm-up)
+    develop of this shape picked by timing, beside the occupancy heuristic's."""
+    from rohditor_gb300 import rl_launch_shape
+
+    s = rl_launch_shape(W, H, radius)
+    if s is None:
+        return None
+    return {"segments": s.segments, "default_segments": s.default_segments,
+            "tuned_iteration_ms": round(s.best_ms, 4), "default_iteration_ms": round(s.default_ms, 4)}
+
+
 def run_ours(args, world, rank, local, pg):
     from rohditor_gb300 import Device
     from rohditor_gb300 import _ffi
@@ -331,6 +343,7 @@ def run_ours(args, world, rank, local, pg):
         "kernels": kernels,
         "dominant_kernel": dominant,
         "kernel_ms_per_step": round(step_kernel_ms, 3),
+        "rl_launch_shape": rl_shape_record(W, H, wl.capture.radius),
         "clocks": clocks.summary(),
     }
     if rank == 0 and not args.no_cpu_baseline:

@@ -271,6 +271,16 @@ rd_status rd_render_output_device(rd_ctx* ctx, const rd_base* base, const rd_col
  * offsets) whose quantised code differs from the code of the correctly
  * rounded power, expected 0. */
 rd_status rd_check_math(rd_ctx* ctx, int32_t which, uint64_t* result);
+/* Launch shape of the capture-sharpening iteration chosen for one image shape
+ * (no reference counterpart). The first develop of a (width, height, kernel
+ * radius) shape times its iterations under a few row-segment counts around the
+ * occupancy heuristic's; the fastest is kept process-wide and used by later
+ * develops of that shape. The results are the same under every count.
+ * segments: the chosen count; default_segments: the heuristic's; best_ms and
+ * default_ms: their fastest timed iteration (0 when not timed). Any output may
+ * be NULL except segments. RD_UNSUPPORTED when the shape has not been tuned. */
+rd_status rd_rl_launch_shape(uint32_t width, uint32_t height, float radius, int32_t* segments,
+                             int32_t* default_segments, float* best_ms, float* default_ms);
 
 rd_status rd_source_dimensions(const rd_source* source, uint32_t* width, uint32_t* height);
 rd_status rd_source_download(rd_ctx* ctx, const rd_source* source, float* rgb_interleaved);

@@ -4,11 +4,12 @@ reference's `rohditor-gpu` processor interface."""
 
 from .processor import (CaptureContract, ColorContract, Device, GamutDiagnostics, GpuBase, GpuDevelopedSource,
                         GpuPreviewError, GpuPreviewProcessor, GpuSensorProcessor, GpuSpatialProcessor, Histogram,
-                        OpticsExecution, OutputSpec, SensorDescription, Stages, clip_levels, opposed_levels,
-                        standard_base_lut)
+                        OpticsExecution, OutputSpec, RlLaunchShape, SensorDescription, Stages, clip_levels,
+                        opposed_levels, rl_launch_shape, standard_base_lut)
 
 __all__ = [
     "CaptureContract", "ColorContract", "Device", "GamutDiagnostics", "GpuBase", "GpuDevelopedSource", "GpuPreviewError",
     "GpuPreviewProcessor", "GpuSensorProcessor", "GpuSpatialProcessor", "Histogram", "OpticsExecution",
-    "OutputSpec", "SensorDescription", "Stages", "clip_levels", "opposed_levels", "standard_base_lut",
+    "OutputSpec", "RlLaunchShape", "SensorDescription", "Stages", "clip_levels", "opposed_levels", "rl_launch_shape",
+    "standard_base_lut",
 ]

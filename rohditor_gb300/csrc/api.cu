@@ -126,6 +126,7 @@ Status check_kernel_error(Context& ctx, const char* stage) {
   RD_CUDA_TRY(cudaMemcpyAsync(&word, ctx.d_error, sizeof(word), cudaMemcpyDeviceToHost, ctx.stream));
   RD_CUDA_TRY(cudaStreamSynchronize(ctx.stream));
   if (!ctx.pending.empty()) resolve_kernel_timing(ctx);
+  if (!ctx.tune_runs.empty()) resolve_rl_tuning(ctx);
   if (word) {
     RD_CUDA_TRY(cudaMemsetAsync(ctx.d_error, 0, sizeof(uint32_t), ctx.stream));
     std::string what;
@@ -543,6 +544,10 @@ void rd_ctx_destroy(rd_ctx* h) {
   cudaStreamSynchronize(c.stream);
   for (void* p : c.pinned_uploads) cudaFreeHost(p);
   rd::resolve_kernel_timing(c);
+  for (auto& r : c.tune_runs) {
+    cudaEventDestroy(r.second.first);
+    cudaEventDestroy(r.second.second);
+  }
   for (auto e : c.event_pool) cudaEventDestroy(e);
   for (auto& e : c.user_ev)
     if (e) cudaEventDestroy(e);

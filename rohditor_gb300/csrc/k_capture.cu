@@ -23,7 +23,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <map>
 #include <mutex>
+#include <vector>
 
 #include "rd_internal.cuh"
 
@@ -388,7 +390,7 @@ __global__ void __launch_bounds__(128) rl_stream_kernel(const float* __restrict_
 
 template <int R>
 Status launch_rl_iter(Context& ctx, const float* est, const float* guide, float* out, int W, int H, const Taps& taps,
-                      const CUtensorMap* est_map) {
+                      const CUtensorMap* est_map, int segs) {
   using G = StreamGeom<R>;
   const size_t smem = sizeof(StreamSmem<R>);
   RD_CUDA_TRY(cudaFuncSetAttribute(rl_stream_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -397,11 +399,6 @@ Status launch_rl_iter(Context& ctx, const float* est, const float* guide, float*
   const int sms = ctx.sm_count > 0 ? ctx.sm_count : 152;
   const int slots = std::max(1, occ) * sms;
   const int strips = (W + G::SW - 1) / G::SW;
-  // Segments: one round of (strip, segment) items over all resident CTAs, each
-  // segment at least 32 rows (vertical halos) and at most 512 (more rounds).
-  const int per_round = std::max(1, slots / strips);
-  int segs = std::min(per_round, std::max(1, H / 32));
-  while ((H + segs - 1) / segs > 512) segs += per_round;
   const int seg_h = (H + segs - 1) / segs;
   const int nseg = (H + seg_h - 1) / seg_h;
   const int items = strips * nseg;
@@ -574,6 +571,90 @@ Status rl_prep(Context& ctx, int r, const Taps& taps, const float* rgb, long lon
   }
 }
 
+// ---- launch-shape tuning of the RL iteration -----------------------------------
+// How many row segments each strip is cut into is a pure scheduling choice:
+// every output of an iteration is computed the same way whatever the
+// segmentation. The first develop of an image shape (width, height, radius)
+// therefore runs iterations 1..K-1 under the candidate segment counts in turn
+// (iteration 0, which may pay for loading the kernel, under the heuristic's
+// count and untimed), each timed with events; after the develop's
+// synchronisation the candidate with the fastest iteration is kept for that
+// shape in a process-wide table, and later develops of the shape use it.
+struct RlShape {
+  int W, H, R;
+  bool operator<(const RlShape& o) const {
+    return W != o.W ? W < o.W : (H != o.H ? H < o.H : R < o.R);
+  }
+};
+struct RlChoice {
+  int segs = 0, default_segs = 0;
+  float best_ms = 0.0f, default_ms = 0.0f;
+};
+std::mutex g_rl_tune_mutex;
+std::map<RlShape, RlChoice> g_rl_tuned;
+
+// The occupancy heuristic: one round of (strip, segment) items over all
+// resident CTAs, each segment at least 32 rows (vertical halos) and at most
+// 512 (more rounds).
+int rl_default_segments(int W, int H, int R, int sms) {
+  int occ = 0;
+  size_t smem = 0;
+  switch (R) {
+    case 1: smem = sizeof(StreamSmem<1>); cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, rl_stream_kernel<1>, 128, smem); break;
+    case 2: smem = sizeof(StreamSmem<2>); cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, rl_stream_kernel<2>, 128, smem); break;
+    case 3: smem = sizeof(StreamSmem<3>); cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, rl_stream_kernel<3>, 128, smem); break;
+    default: smem = sizeof(StreamSmem<4>); cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, rl_stream_kernel<4>, 128, smem); break;
+  }
+  cudaGetLastError();
+  const int slots = std::max(1, occ) * std::max(1, sms);
+  const int strips = (W + (128 - 2 * R) - 1) / (128 - 2 * R);
+  const int per_round = std::max(1, slots / strips);
+  int segs = std::min(per_round, std::max(1, H / 32));
+  while ((H + segs - 1) / segs > 512) segs += per_round;
+  return segs;
+}
+
+// Candidate segment counts around the heuristic's (each segment >= 32 rows).
+std::vector<int> rl_candidates(int H, int d) {
+  std::vector<int> c{d};
+  for (int v : {2 * d, std::max(1, d / 2), 3 * d, std::max(1, (3 * d) / 2)})
+    if (H / v >= 32 && std::find(c.begin(), c.end(), v) == c.end()) c.push_back(v);
+  return c;
+}
+
+}  // namespace
+
+void resolve_rl_tuning(Context& ctx) {
+  std::map<int, float> best;  // candidate -> fastest timed iteration
+  for (auto& r : ctx.tune_runs) {
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, r.second.first, r.second.second) == cudaSuccess) {
+      auto it = best.find(r.first);
+      if (it == best.end() || ms < it->second) best[r.first] = ms;
+    }
+    ctx.event_pool.push_back(r.second.first);
+    ctx.event_pool.push_back(r.second.second);
+  }
+  ctx.tune_runs.clear();
+  cudaGetLastError();
+  const RlShape key{ctx.tune_shape[0], ctx.tune_shape[1], ctx.tune_shape[2]};
+  const int d = rl_default_segments(key.W, key.H, key.R, ctx.sm_count > 0 ? ctx.sm_count : 152);
+  RlChoice c;
+  c.default_segs = d;
+  for (auto& kv : best) {
+    if (kv.first == d) c.default_ms = kv.second;
+    if (c.segs == 0 || kv.second < c.best_ms) {
+      c.segs = kv.first;
+      c.best_ms = kv.second;
+    }
+  }
+  if (c.segs == 0) return;
+  std::lock_guard<std::mutex> lk(g_rl_tune_mutex);
+  g_rl_tuned[key] = c;
+}
+
+namespace {
+
 // cuTensorMapEncodeTiled through the runtime's driver entry-point query (no
 // link against the driver library); null when unavailable.
 using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -610,12 +691,12 @@ bool make_plane_map(CUtensorMap* map, const float* plane, int W, int H) {
 }
 
 Status rl_iteration(Context& ctx, int r, const Taps& taps, const float* est, const float* guide, float* out, int W,
-                    int H, const CUtensorMap* est_map) {
+                    int H, const CUtensorMap* est_map, int segs) {
   switch (r) {
-    case 1: return launch_rl_iter<1>(ctx, est, guide, out, W, H, taps, est_map);
-    case 2: return launch_rl_iter<2>(ctx, est, guide, out, W, H, taps, est_map);
-    case 3: return launch_rl_iter<3>(ctx, est, guide, out, W, H, taps, est_map);
-    case 4: return launch_rl_iter<4>(ctx, est, guide, out, W, H, taps, est_map);
+    case 1: return launch_rl_iter<1>(ctx, est, guide, out, W, H, taps, est_map, segs);
+    case 2: return launch_rl_iter<2>(ctx, est, guide, out, W, H, taps, est_map, segs);
+    case 3: return launch_rl_iter<3>(ctx, est, guide, out, W, H, taps, est_map, segs);
+    case 4: return launch_rl_iter<4>(ctx, est, guide, out, W, H, taps, est_map, segs);
     default: return Status{RD_INVALID_INPUT, "capture radius outside 1..4"};
   }
 }
@@ -885,8 +966,45 @@ Status run_capture(Context& ctx, float* rgb, int W, int H, const rd_detail_desc&
     const bool tma = make_plane_map(&maps[0], guide, W, H) && make_plane_map(&maps[1], est_buf[0], W, H) &&
                      make_plane_map(&maps[2], est_buf[1], W, H);
     const CUtensorMap* in_map = tma ? &maps[0] : nullptr;
+    // Launch shape: the tuned segment count of this image shape, or a tuning
+    // run over the candidates (not while the stream is being captured).
+    const RlShape shape{W, H, r};
+    int segs = 0;
+    {
+      std::lock_guard<std::mutex> lk(g_rl_tune_mutex);
+      auto it = g_rl_tuned.find(shape);
+      if (it != g_rl_tuned.end()) segs = it->second.segs;
+    }
+    std::vector<int> cands;
+    if (segs == 0) {
+      segs = rl_default_segments(W, H, r, ctx.sm_count > 0 ? ctx.sm_count : 152);
+      if (!ctx.capturing && ctx.tune_runs.empty() && detail.iterations >= 2) cands = rl_candidates(H, segs);
+    }
+    if (!cands.empty()) {
+      ctx.tune_shape[0] = W;
+      ctx.tune_shape[1] = H;
+      ctx.tune_shape[2] = r;
+    }
     for (int it = 0; it < detail.iterations && st.ok(); ++it) {
-      st = rl_iteration(ctx, r, taps, est, guide, est_buf[it & 1], W, H, in_map);
+      const bool timed = !cands.empty() && it > 0;
+      const int s_it = timed ? cands[(it - 1) % cands.size()] : segs;
+      cudaEvent_t a = nullptr, b = nullptr;
+      if (timed) {
+        for (cudaEvent_t* e : {&a, &b}) {
+          if (!ctx.event_pool.empty()) {
+            *e = ctx.event_pool.back();
+            ctx.event_pool.pop_back();
+          } else {
+            cudaEventCreate(e);
+          }
+        }
+        cudaEventRecord(a, ctx.stream);
+      }
+      st = rl_iteration(ctx, r, taps, est, guide, est_buf[it & 1], W, H, in_map, s_it);
+      if (timed) {
+        cudaEventRecord(b, ctx.stream);
+        ctx.tune_runs.push_back({s_it, {a, b}});
+      }
       est = est_buf[it & 1];
       in_map = tma ? &maps[1 + (it & 1)] : nullptr;
     }
@@ -926,3 +1044,19 @@ Status run_capture(Context& ctx, float* rgb, int W, int H, const rd_detail_desc&
 }
 
 }  // namespace rd
+
+extern "C" rd_status rd_rl_launch_shape(uint32_t width, uint32_t height, float radius, int32_t* segments,
+                                        int32_t* default_segments, float* best_ms, float* default_ms) {
+  float w[rd::MAX_TAPS];
+  const int taps = rd::gaussian_kernel(radius, w, rd::MAX_TAPS);
+  if (taps < 0 || !segments) return RD_INVALID_INPUT;
+  const rd::RlShape key{(int)width, (int)height, taps / 2};
+  std::lock_guard<std::mutex> lk(rd::g_rl_tune_mutex);
+  auto it = rd::g_rl_tuned.find(key);
+  if (it == rd::g_rl_tuned.end()) return RD_UNSUPPORTED;
+  *segments = it->second.segs;
+  if (default_segments) *default_segments = it->second.default_segs;
+  if (best_ms) *best_ms = it->second.best_ms;
+  if (default_ms) *default_ms = it->second.default_ms;
+  return RD_OK;
+}

@@ -78,6 +78,10 @@ struct Context {
   // is destroyed.
   bool capturing = false;
   std::vector<void*> pinned_uploads;
+  // Timed RL iterations of a launch-shape tuning run, resolved after the
+  // stage's synchronisation: (candidate segment count, start, end).
+  int tune_shape[3] = {0, 0, 0};
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> tune_runs;
 };
 
 // Brackets one kernel launch with events when kernel timing is enabled, and
@@ -247,6 +251,9 @@ Status run_display_output(Context& ctx, const float* rgb, const rd_color_desc& c
 Status run_math_check(Context& ctx, int which, uint64_t* result);
 
 Status reserve_amaze_scratch(Context& ctx);
+// Folds the timed RL iterations of a tuning run into the process-wide table of
+// launch shapes (k_capture.cu); called after a synchronisation.
+void resolve_rl_tuning(Context& ctx);
 
 // Host contract helpers.
 int gaussian_kernel(float sigma, float* weights, int max_taps);

@@ -268,6 +268,30 @@ class GamutDiagnostics:
         return self.in_gamut + self.compressed + self.limited + self.clipped_fallback + self.invalid
 
 
+@dataclass
+class RlLaunchShape:
+    """The capture-sharpening launch shape chosen for one image shape."""
+
+    segments: int
+    default_segments: int
+    best_ms: float
+    default_ms: float
+
+
+def rl_launch_shape(width: int, height: int, radius: float) -> RlLaunchShape | None:
+    """rd_rl_launch_shape: the row-segment count the first develop of this
+    (width, height, radius) picked by timing, or None before any develop of it."""
+    segs, dflt = ctypes.c_int32(), ctypes.c_int32()
+    best, dms = ctypes.c_float(), ctypes.c_float()
+    code = _ffi.load().rd_rl_launch_shape(width, height, radius, ctypes.byref(segs), ctypes.byref(dflt),
+                                         ctypes.byref(best), ctypes.byref(dms))
+    if code == _ffi.STATUS_NAMES.index("Unsupported"):
+        return None
+    if code != 0:
+        raise GpuPreviewError(code, "rd_rl_launch_shape")
+    return RlLaunchShape(segs.value, dflt.value, best.value, dms.value)
+
+
 def standard_base_lut() -> np.ndarray:
     """BaseRenderingLut::standard_v1 values (crates/core/src/rendering.rs:36-50)."""
     out = np.zeros(4096, dtype=np.float32)

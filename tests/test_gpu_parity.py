@@ -146,6 +146,28 @@ def test_capture_radius_range_and_edges(stages, oracle):
         assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32)), radius
 
 
+def test_capture_launch_shape_tuning_keeps_results(stages, oracle):
+    """The first sharpening of an image shape times its iterations under several
+    row-segment counts; the second uses the fastest. Both equal the oracle bit
+    for bit, so the segmentation is a pure scheduling choice."""
+    from rohditor_gb300 import CaptureContract, rl_launch_shape
+
+    w, h = 1204, 1130  # 4-column multiple: estimate rows go through the TMA ring
+    rgb = np.abs(textured_mosaic(3 * w, h, seed=41)).reshape(h, 3 * w)
+    cap = CaptureContract(amount=0.6, radius=0.9, noise_protection=0.3, ceilings=(1.0, 1.0, 1.0), iterations=8)
+    assert rl_launch_shape(w, h, 0.9) is None
+    first = stages.capture(rgb, cap)
+    shape = rl_launch_shape(w, h, 0.9)
+    assert shape is not None and shape.segments >= 1 and shape.default_segments >= 1
+    assert shape.best_ms > 0.0 and shape.best_ms <= shape.default_ms
+    assert h // shape.segments >= 32 or shape.segments == shape.default_segments
+    second = stages.capture(rgb, cap)
+    assert rl_launch_shape(w, h, 0.9) == shape
+    ref = oracle.capture(rgb, 0.6, 0.9, 0.3, (1.0, 1.0, 1.0), 8)
+    assert np.array_equal(first.view(np.uint32), ref.view(np.uint32))
+    assert np.array_equal(second.view(np.uint32), ref.view(np.uint32))
+
+
 def smooth_rgb(w, h, seed):
     rng = np.random.default_rng(seed)
     yy, xx = np.mgrid[0:h, 0:w].astype(np.float32)
