@@ -410,6 +410,328 @@ Status launch_rl_iter(Context& ctx, const float* est, const float* guide, float*
   return Status{};
 }
 
+// ---- RL iteration, constant-lag streaming ------------------------------------
+// The same iteration as rl_stream_kernel for images of at least 256 x 64, with
+// less bookkeeping per row. Each step loads one 8-row estimate block E..E+7 and
+// always advances every stage by 8 rows at fixed lags: blur #1 and the ratio
+// produce rows E-R..E-R+7, blur #2 and the update rows E-2R..E-2R+7. The 2R
+// rows each vertical pass needs from earlier steps (and the estimate values of
+// the update rows) are carried in registers, so every shared-memory access in
+// a step is a per-step base plus a compile-time offset. Rows a segment does not
+// own are computed and dropped instead of being skipped.
+//  * Rows outside the image are mirrored on load (half-sample symmetric, as
+//    the reference samples). The first blur is row-wise, so its mirrored rows
+//    equal the rows they mirror bit for bit; the ratio is not (its vertical
+//    sum would run in reverse order), so the second blur's mirrored rows are
+//    copied from the rows they mirror inside the register window: at the
+//    image top in step R/2 of the first segment, at the bottom in the last
+//    step of the last segment, whose start is aligned so that this step ends
+//    exactly at the last image row. Columns outside the image are handled as
+//    in rl_stream_kernel (mirrored estimate columns, copied ratio columns).
+//  * With tensor maps (rows of a multiple of 16 bytes) the guide rows of a
+//    step (E-2R .. E-R+7) arrive as one tensor copy beside the estimate block,
+//    two steps ahead, and are read from shared memory; rows and columns
+//    outside the image read the fill value 0 and only feed dropped outputs or
+//    ratio columns that are overwritten by their mirrors.
+//  * Horizontal passes run 9-column windows from registers over rows padded
+//    so that every run of a step takes the same path (15 runs cover the 128
+//    blur #1 columns, 14 the strip's output columns; the extra outputs land
+//    in the padding and are never read).
+//  * A sum starts from its first product instead of from zero: every value of
+//    the iteration is positive (estimate >= guide / 2 > 0, ratio >= 0, taps >
+//    0), and 0 + p = p for every such p, so the sums are unchanged.
+template <int R>
+struct StepGeom {
+  static constexpr int T = 2 * R + 1;
+  static constexpr int QW = 128;         // blur #1 / ratio columns [x0 - R, x0 - R + 128)
+  static constexpr int SW = QW - 2 * R;  // output columns of a strip
+  static constexpr int EW = QW + 2 * R;  // estimate columns [x0 - 2R, x0 - 2R + EW)
+  static constexpr int BH = 8;
+  static constexpr int GH = BH + R;      // guide rows of a step: E-2R .. E-R+7
+  static constexpr int RUN = 9, H1_RUNS = 15, H2_RUNS = 14;
+  static constexpr int PW = 144;                    // row stride of the blur and ratio rows
+  static constexpr int EWP = R <= 3 ? 144 : 176;    // estimate / guide row stride = tensor-copy box width
+  static constexpr int GSLOT = (GH * EWP + 31) & ~31;  // guide slot, a multiple of 128 bytes
+  static_assert(RUN * H1_RUNS >= QW && RUN * H2_RUNS >= SW, "runs cover the rows");
+  static_assert(3 + RUN * H1_RUNS - 1 + 2 * R < EWP, "blur #1 windows stay inside an estimate row");
+  static_assert(RUN * H2_RUNS - 1 + 2 * R < PW && RUN * H1_RUNS <= PW, "blur #2 windows stay inside a ratio row");
+  static_assert(EW + 3 <= EWP && (EWP * 4) % 16 == 0 && (BH * EWP * 4) % 128 == 0, "estimate ring layout");
+  static_assert(H1_RUNS * BH <= 128 && H2_RUNS * BH <= 128, "one run per thread");
+};
+
+template <int R, bool TMA>
+struct __align__(128) StepSmem {
+  using G = StepGeom<R>;
+  float e[3 * G::BH][G::EWP];       // three 8-row estimate blocks (tensor-copy targets)
+  float g[TMA ? 3 : 1][G::GSLOT];   // three guide slots (tensor-copy targets)
+  float t[G::BH][G::PW];            // blur #1 rows E..E+7, then blur #2 rows E-R..E-R+7
+  float q[G::BH][G::PW];            // ratio rows E-R..E-R+7
+  unsigned long long bar[3];
+};
+
+template <int R, int RUN>
+__device__ __forceinline__ void hrun_full(const float* __restrict__ src, float* __restrict__ dst,
+                                          const float (&w)[2 * R + 1]) {
+  constexpr int T = 2 * R + 1;
+  float win[RUN + 2 * R];
+#pragma unroll
+  for (int k = 0; k < RUN + 2 * R; ++k) win[k] = src[k];
+#pragma unroll
+  for (int j = 0; j < RUN; ++j) {
+    float v = win[j] * w[0];
+#pragma unroll
+    for (int t = 1; t < T; ++t) v += win[j + t] * w[t];
+    dst[j] = v;
+  }
+}
+
+// Row segments: 8-row units spread evenly; every boundary lies at
+// H + 4R (mod 8) so that the last segment's final step ends at row H - 1.
+// Segment s covers [seg_row(s), seg_row(s + 1)).
+struct StepSegments {
+  int q, rem, r8, segs;
+};
+__host__ __device__ __forceinline__ int seg_row(const StepSegments& sg, int s, int H) {
+  if (s <= 0) return 0;
+  if (s >= sg.segs) return H;
+  return sg.r8 + 8 * (s * sg.q + min(s, sg.rem));
+}
+StepSegments step_segments(int H, int R, int want) {
+  const int m = (4 * R) % 8;
+  const int n8 = (H - m) / 8;
+  const int segs = std::max(2, std::min(want, n8));
+  return {n8 / segs, n8 % segs, (H - m) % 8, segs};
+}
+
+template <int R, bool TMA>
+__global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict__ est_in,
+                                                          const float* __restrict__ guide,
+                                                          float* __restrict__ est_out, int W, int H, int strips,
+                                                          const StepSegments sg, int items, const Taps taps,
+                                                          const __grid_constant__ CUtensorMap est_map,
+                                                          const __grid_constant__ CUtensorMap guide_map,
+                                                          unsigned* error) {
+  using G = StepGeom<R>;
+  constexpr int T = G::T, SW = G::SW, BH = G::BH, N2 = 2 * R;
+  extern __shared__ __align__(128) float4 rl_step_raw[];
+  StepSmem<R, TMA>& S = *reinterpret_cast<StepSmem<R, TMA>*>(rl_step_raw);
+  float w[T];
+#pragma unroll
+  for (int k = 0; k < T; ++k) w[k] = taps.w[k];
+  const int tid = threadIdx.x;
+  if (TMA && tid == 0) {
+    for (int b = 0; b < 3; ++b) mbar_init(&S.bar[b]);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncthreads();
+  unsigned phases = 0;
+  bool tma_failed = false;
+  // The run each thread computes in the horizontal passes (row, first column).
+  const bool h1_on = tid < G::H1_RUNS * BH, h2_on = tid < G::H2_RUNS * BH;
+  const int h1_row = tid / G::H1_RUNS, h1_col = (tid % G::H1_RUNS) * G::RUN;
+  const int h2_row = tid / G::H2_RUNS, h2_col = (tid % G::H2_RUNS) * G::RUN;
+  for (int item = blockIdx.x; item < items; item += gridDim.x) {
+    const int strip = item % strips, seg = item / strips;
+    const int x0 = strip * SW;
+    const int y0 = seg_row(sg, seg, H), y1 = seg_row(sg, seg + 1, H);
+    const int E0 = y0 - N2;
+    const int nsteps = (y1 - y0 + 2 * N2 - BH + 7) / BH + 1;
+    const bool inside = x0 - N2 >= 0 && x0 - N2 + G::EW <= W;
+    const bool tma_strip = TMA && inside;
+    const bool edge_q = x0 < R || x0 + SW + R > W;
+    const int xal = (x0 - N2) & ~3;  // rounds down, also below 0
+    const int rem = TMA ? (x0 - N2) - xal : 0;
+    const int xa = x0 - N2 + tid, xb = xa + 128;
+    const int sxa = (unsigned)xa < (unsigned)W ? xa : mirror_half(xa, W);
+    const bool has_b = tid + 128 < G::EW;
+    const int sxb = has_b ? ((unsigned)xb < (unsigned)W ? xb : mirror_half(xb, W)) : 0;
+    // Step k's estimate block (rows [E0 + 8k, +8)) goes to ring block k % 3, by
+    // one tensor copy when the rows and the window lie inside the image, else
+    // by per-thread copies with rows and columns mirrored into the image; its
+    // guide rows go to guide slot k % 3 by one tensor copy.
+    auto e_by_tma = [&](int k) {
+      const int r0 = E0 + BH * k;
+      return tma_strip && r0 >= 0 && r0 + BH <= H;
+    };
+    auto issue = [&](int k) {
+      if (k >= nsteps) return;
+      const int r0 = E0 + BH * k, b = k % 3;
+      const bool et = e_by_tma(k);
+      if (TMA && tid == 0) {
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        mbar_expect_tx(&S.bar[b], (et ? BH * G::EWP * sizeof(float) : 0) + G::GH * G::EWP * sizeof(float));
+        if (et) tma_load_2d(S.e[b * BH], &est_map, xal, r0, &S.bar[b]);
+        tma_load_2d(S.g[b], &guide_map, xal, r0 - N2, &S.bar[b]);
+      }
+      if (et) return;
+#pragma unroll
+      for (int j = 0; j < BH; ++j) {
+        const float* src = est_in + (long long)mirror_row(r0 + j, H) * W;
+        float* dst = S.e[b * BH + j] + rem;
+        cp_async4(dst + tid, src + sxa);
+        if (has_b) cp_async4(dst + tid + 128, src + sxb);
+      }
+    };
+    issue(0);
+    cp_async_commit();
+    issue(1);
+    cp_async_commit();
+    // Carried rows: blur #1 rows [E-2R, E), blur #2 rows [E-3R, E-R), estimate
+    // rows [E-2R, E) of this thread's output column.
+    float c1[N2], c2[N2], ed[N2];
+#pragma unroll
+    for (int i = 0; i < N2; ++i) c1[i] = c2[i] = ed[i] = 1.0f;
+    const int xq = x0 - R + tid, xo = x0 + tid;
+    const bool okq = (unsigned)xq < (unsigned)W;
+    const bool oko = tid < SW && xo < W;
+    for (int k = 0; k < nsteps; ++k) {
+      const int E = E0 + BH * k;
+      // Without tensor maps: guide values of the ratio rows and of the update rows.
+      float gq[BH], go[BH];
+      if (!TMA) {
+#pragma unroll
+        for (int j = 0; j < BH; ++j) {
+          const int rq = E - R + j, ro = E - N2 + j;
+          gq[j] = okq && (unsigned)rq < (unsigned)H ? __ldg(guide + (long long)rq * W + xq) : 0.0f;
+          go[j] = oko && ro >= y0 && ro < y1 ? __ldg(guide + (long long)ro * W + xo) : 0.0f;
+        }
+      }
+      issue(k + 2);
+      cp_async_commit();
+      asm volatile("cp.async.wait_group 2;\n" ::: "memory");
+      if (TMA) {
+        const int b = k % 3;
+        tma_wait(&S.bar[b], (phases >> b) & 1u, tma_failed, error);
+        phases ^= 1u << b;
+      }
+      __syncthreads();
+      const float* eb = S.e[(k % 3) * BH] + rem;
+      const float* gb = S.g[TMA ? k % 3 : 0] + rem;
+      // 1. blur #1, horizontal: rows E..E+7, columns x0-R .. x0-R+134
+      if (h1_on) hrun_full<R, G::RUN>(eb + h1_row * G::EWP + h1_col, S.t[h1_row] + h1_col, w);
+      float ec[BH];
+#pragma unroll
+      for (int j = 0; j < BH; ++j) ec[j] = eb[j * G::EWP + tid + N2];
+      __syncthreads();
+      // 2. blur #1, vertical, and the ratio: rows E-R .. E-R+7, column x0-R+tid
+      {
+        float win[BH + N2];
+#pragma unroll
+        for (int i = 0; i < N2; ++i) win[i] = c1[i];
+#pragma unroll
+        for (int j = 0; j < BH; ++j) win[N2 + j] = S.t[j][tid];
+#pragma unroll
+        for (int j = 0; j < BH; ++j) {
+          float b = win[j] * w[0];
+#pragma unroll
+          for (int t = 1; t < T; ++t) b += win[j + t] * w[t];
+          const float g = TMA ? gb[(R + j) * G::EWP + R + tid] : gq[j];
+          S.q[j][tid] = g / rmax(b, FLOOR);
+        }
+#pragma unroll
+        for (int i = 0; i < N2; ++i) c1[i] = win[BH + i];
+      }
+      __syncthreads();
+      if (edge_q) {
+        // Ratio columns outside the image within R of it take their mirror's value.
+        if ((unsigned)xq >= (unsigned)W && xq >= -R && xq < W + R) {
+          const int src = mirror_half(xq, W) - (x0 - R);
+#pragma unroll
+          for (int j = 0; j < BH; ++j) S.q[j][tid] = S.q[j][src];
+        }
+        __syncthreads();
+      }
+      // 3. blur #2, horizontal: rows E-R .. E-R+7, output columns (over blur #1,
+      //    whose rows every thread has read before the barrier above)
+      if (h2_on) hrun_full<R, G::RUN>(S.q[h2_row] + h2_col, S.t[h2_row] + h2_col, w);
+      __syncthreads();
+      // 4. blur #2, vertical, and the bounded update: rows E-2R .. E-2R+7
+      {
+        float win[BH + N2];
+#pragma unroll
+        for (int i = 0; i < N2; ++i) win[i] = c2[i];
+#pragma unroll
+        for (int j = 0; j < BH; ++j) win[N2 + j] = S.t[j][tid];
+#pragma unroll
+        for (int i = 0; i < N2; ++i) c2[i] = win[BH + i];
+        if (y0 == 0 && k == R / 2) {
+          // Window position p holds row E - 3R + p; rows -1 .. -R take rows 0 .. R-1.
+          constexpr int P0 = 5 * R - 8 * (R / 2);
+#pragma unroll
+          for (int i = 1; i <= R; ++i) win[P0 - i] = win[P0 + i - 1];
+        }
+        if (y1 == H && k == nsteps - 1) {
+          // This step ends at row H - 1: rows H .. H+R-1 take rows H-1 .. H-R.
+#pragma unroll
+          for (int i = 0; i < R; ++i) win[BH + R + i] = win[BH + R - 1 - i];
+        }
+        if (oko && E - N2 + BH > y0) {
+          float* po = est_out + (long long)(E - N2) * W + xo;
+#pragma unroll
+          for (int j = 0; j < BH; ++j) {
+            const int o = E - N2 + j;
+            float b = win[j] * w[0];
+#pragma unroll
+            for (int t = 1; t < T; ++t) b += win[j + t] * w[t];
+            float e = (j < N2 ? ed[j] : ec[j - N2]) * b;
+            const float g = TMA ? gb[j * G::EWP + N2 + tid] : go[j];
+            const float lo = g * 0.5f, hi = g * 2.0f;
+            if (e < lo) e = lo;
+            if (e > hi) e = hi;
+            if (o >= y0 && o < y1) po[(long long)j * W] = e;
+          }
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < N2; ++i) ed[i] = ec[BH - N2 + i];
+    }
+  }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
+// The constant-lag kernel serves images of at least 256 x 64; smaller ones
+// keep the per-step bookkeeping of rl_stream_kernel.
+bool rl_uses_step_kernel(int W, int H, int R) { return W >= 256 && H >= 64 && R >= 1 && R <= 4; }
+
+template <int R, bool TMA>
+int step_occupancy() {
+  int occ = 0;
+  const size_t smem = sizeof(StepSmem<R, TMA>);
+  cudaFuncSetAttribute(rl_step_kernel<R, TMA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, rl_step_kernel<R, TMA>, 128, smem);
+  cudaGetLastError();
+  return std::max(1, occ);
+}
+
+template <int R, bool TMA>
+Status launch_rl_step_t(Context& ctx, const float* est, const float* guide, float* out, int W, int H,
+                        const Taps& taps, const CUtensorMap* est_map, const CUtensorMap* guide_map, int segs) {
+  using G = StepGeom<R>;
+  const size_t smem = sizeof(StepSmem<R, TMA>);
+  RD_CUDA_TRY(cudaFuncSetAttribute(rl_step_kernel<R, TMA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int occ = 0;
+  RD_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, rl_step_kernel<R, TMA>, 128, smem));
+  const int sms = ctx.sm_count > 0 ? ctx.sm_count : 152;
+  const int slots = std::max(1, occ) * sms;
+  const int strips = (W + G::SW - 1) / G::SW;
+  const StepSegments sg = step_segments(H, R, segs);
+  const int items = strips * sg.segs;
+  const int grid = std::min(items, slots);
+  CUtensorMap none{};
+  RD_LAUNCH(ctx, K_RL_ITER, rl_step_kernel<R, TMA><<<grid, 128, smem, ctx.stream>>>(
+                                est, guide, out, W, H, strips, sg, items, taps, est_map ? *est_map : none,
+                                guide_map ? *guide_map : none, ctx.d_error));
+  return Status{};
+}
+
+template <int R>
+Status launch_rl_step(Context& ctx, const float* est, const float* guide, float* out, int W, int H, const Taps& taps,
+                      const CUtensorMap* est_map, const CUtensorMap* guide_map, int segs) {
+  if (est_map && guide_map)
+    return launch_rl_step_t<R, true>(ctx, est, guide, out, W, H, taps, est_map, guide_map, segs);
+  return launch_rl_step_t<R, false>(ctx, est, guide, out, W, H, taps, nullptr, nullptr, segs);
+}
+
 // ---- guide and mask, streamed down column strips ---------------------------
 // sharpening.rs:180-230 before the iterations: guide = max(sum max(c,0)/3,
 // 1e-6) and mask = 1 - smoothstep(0.85, 0.98, max c/ceil_c) for every pixel,
@@ -599,13 +921,19 @@ std::map<RlShape, RlChoice> g_rl_tuned;
 int rl_default_segments(int W, int H, int R, int sms) {
   int occ = 0;
   size_t smem = 0;
+  if (rl_uses_step_kernel(W, H, R)) R += 4;  // cases 5..8: the constant-lag kernel (tensor-copy form)
   switch (R) {
+    case 5: occ = step_occupancy<1, true>(); break;
+    case 6: occ = step_occupancy<2, true>(); break;
+    case 7: occ = step_occupancy<3, true>(); break;
+    case 8: occ = step_occupancy<4, true>(); break;
     case 1: smem = sizeof(StreamSmem<1>); cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, rl_stream_kernel<1>, 128, smem); break;
     case 2: smem = sizeof(StreamSmem<2>); cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, rl_stream_kernel<2>, 128, smem); break;
     case 3: smem = sizeof(StreamSmem<3>); cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, rl_stream_kernel<3>, 128, smem); break;
     default: smem = sizeof(StreamSmem<4>); cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, rl_stream_kernel<4>, 128, smem); break;
   }
   cudaGetLastError();
+  if (R > 4) R -= 4;
   const int slots = std::max(1, occ) * std::max(1, sms);
   const int strips = (W + (128 - 2 * R) - 1) / (128 - 2 * R);
   const int per_round = std::max(1, slots / strips);
@@ -614,10 +942,11 @@ int rl_default_segments(int W, int H, int R, int sms) {
   return segs;
 }
 
-// Candidate segment counts around the heuristic's (each segment >= 32 rows).
+// Candidate segment counts around the heuristic's (each segment >= 32 rows):
+// fewer, equal and several times more work items than resident CTAs.
 std::vector<int> rl_candidates(int H, int d) {
   std::vector<int> c{d};
-  for (int v : {2 * d, std::max(1, d / 2), 3 * d, std::max(1, (3 * d) / 2)})
+  for (int v : {2 * d, 3 * d, 4 * d, 6 * d, std::max(1, d / 2)})
     if (H / v >= 32 && std::find(c.begin(), c.end(), v) == c.end()) c.push_back(v);
   return c;
 }
@@ -675,15 +1004,22 @@ EncodeTiled tensor_map_encoder() {
   return fn;
 }
 
-// Tensor map of one f32 plane for the estimate ring's 140x8 boxes; false when
-// TMA cannot address it (row stride not a multiple of 16 bytes, or no encoder).
-bool make_plane_map(CUtensorMap* map, const float* plane, int W, int H) {
+// Estimate-ring box width (floats) of the kernel that runs an iteration.
+int rl_box_width(int W, int H, int R) {
+  if (!rl_uses_step_kernel(W, H, R)) return StreamGeom<1>::EWP;
+  return R <= 3 ? StepGeom<1>::EWP : StepGeom<4>::EWP;
+}
+
+// Tensor map of one f32 plane for the estimate ring's box_w x 8 boxes; false
+// when TMA cannot address it (row stride not a multiple of 16 bytes, or no
+// encoder).
+bool make_plane_map(CUtensorMap* map, const float* plane, int W, int H, int box_w, int box_h = 8) {
   if (W % 4 != 0 || reinterpret_cast<uintptr_t>(plane) % 16 != 0) return false;
   const EncodeTiled enc = tensor_map_encoder();
   if (!enc) return false;
   const cuuint64_t dims[2] = {(cuuint64_t)W, (cuuint64_t)H};
   const cuuint64_t strides[1] = {(cuuint64_t)W * sizeof(float)};
-  const cuuint32_t box[2] = {(cuuint32_t)StreamGeom<1>::EWP, (cuuint32_t)StreamGeom<1>::BH};
+  const cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)box_h};
   const cuuint32_t elem[2] = {1, 1};
   return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(plane), dims, strides, box, elem,
              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -691,7 +1027,16 @@ bool make_plane_map(CUtensorMap* map, const float* plane, int W, int H) {
 }
 
 Status rl_iteration(Context& ctx, int r, const Taps& taps, const float* est, const float* guide, float* out, int W,
-                    int H, const CUtensorMap* est_map, int segs) {
+                    int H, const CUtensorMap* est_map, const CUtensorMap* guide_map, int segs) {
+  if (rl_uses_step_kernel(W, H, r)) {
+    switch (r) {
+      case 1: return launch_rl_step<1>(ctx, est, guide, out, W, H, taps, est_map, guide_map, segs);
+      case 2: return launch_rl_step<2>(ctx, est, guide, out, W, H, taps, est_map, guide_map, segs);
+      case 3: return launch_rl_step<3>(ctx, est, guide, out, W, H, taps, est_map, guide_map, segs);
+      case 4: return launch_rl_step<4>(ctx, est, guide, out, W, H, taps, est_map, guide_map, segs);
+      default: break;
+    }
+  }
   switch (r) {
     case 1: return launch_rl_iter<1>(ctx, est, guide, out, W, H, taps, est_map, segs);
     case 2: return launch_rl_iter<2>(ctx, est, guide, out, W, H, taps, est_map, segs);
@@ -963,9 +1308,13 @@ Status run_capture(Context& ctx, float* rgb, int W, int H, const rd_detail_desc&
     // Tensor maps of the three planes an iteration can read (guide, then the
     // ping-pong estimates), for the TMA-fed estimate ring.
     CUtensorMap maps[3];
-    const bool tma = make_plane_map(&maps[0], guide, W, H) && make_plane_map(&maps[1], est_buf[0], W, H) &&
-                     make_plane_map(&maps[2], est_buf[1], W, H);
+    const int box_w = rl_box_width(W, H, r);
+    const bool tma = make_plane_map(&maps[0], guide, W, H, box_w) && make_plane_map(&maps[1], est_buf[0], W, H, box_w) &&
+                     make_plane_map(&maps[2], est_buf[1], W, H, box_w);
     const CUtensorMap* in_map = tma ? &maps[0] : nullptr;
+    // The constant-lag kernel also reads each step's guide rows (8 + R) by tensor copy.
+    CUtensorMap guide_map;
+    const bool guide_tma = tma && rl_uses_step_kernel(W, H, r) && make_plane_map(&guide_map, guide, W, H, box_w, 8 + r);
     // Launch shape: the tuned segment count of this image shape, or a tuning
     // run over the candidates (not while the stream is being captured).
     const RlShape shape{W, H, r};
@@ -1000,7 +1349,8 @@ Status run_capture(Context& ctx, float* rgb, int W, int H, const rd_detail_desc&
         }
         cudaEventRecord(a, ctx.stream);
       }
-      st = rl_iteration(ctx, r, taps, est, guide, est_buf[it & 1], W, H, in_map, s_it);
+      st = rl_iteration(ctx, r, taps, est, guide, est_buf[it & 1], W, H, in_map, guide_tma ? &guide_map : nullptr,
+                        s_it);
       if (timed) {
         cudaEventRecord(b, ctx.stream);
         ctx.tune_runs.push_back({s_it, {a, b}});

@@ -146,6 +146,22 @@ def test_capture_radius_range_and_edges(stages, oracle):
         assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32)), radius
 
 
+@pytest.mark.parametrize("radius", [0.3, 0.6, 0.9, 1.2])
+@pytest.mark.parametrize("size", [(260, 67), (517, 389), (1032, 300)])
+def test_capture_constant_lag_kernel(stages, oracle, radius, size):
+    """Images of at least 256 x 64 take the constant-lag RL kernel: mirrored
+    top and bottom rows, ragged right strips, widths with (1032) and without
+    (260, 517) 16-byte rows for the tensor-copy ring, kernel radii 1..4."""
+    from rohditor_gb300 import CaptureContract
+
+    w, h = size
+    rgb = np.abs(textured_mosaic(3 * w, h, seed=int(radius * 10) + w)).reshape(h, 3 * w)
+    cap = CaptureContract(amount=0.7, radius=radius, noise_protection=0.4, ceilings=(1.0, 0.9, 1.1), iterations=5)
+    ours = stages.capture(rgb, cap)
+    ref = oracle.capture(rgb, 0.7, radius, 0.4, (1.0, 0.9, 1.1), 5)
+    assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32))
+
+
 def test_capture_launch_shape_tuning_keeps_results(stages, oracle):
     """The first sharpening of an image shape times its iterations under several
     row-segment counts; the second uses the fastest. Both equal the oracle bit
