@@ -572,6 +572,8 @@ __global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict
         if (has_b) cp_async4(dst + tid + 128, src + sxb);
       }
     };
+    // The previous item's last step may still read guide slots 0 and 1.
+    __syncthreads();
     issue(0);
     cp_async_commit();
     issue(1);
@@ -596,15 +598,18 @@ __global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict
           go[j] = oko && ro >= y0 && ro < y1 ? __ldg(guide + (long long)ro * W + xo) : 0.0f;
         }
       }
-      issue(k + 2);
-      cp_async_commit();
-      asm volatile("cp.async.wait_group 2;\n" ::: "memory");
+      asm volatile("cp.async.wait_group 1;\n" ::: "memory");
       if (TMA) {
         const int b = k % 3;
         tma_wait(&S.bar[b], (phases >> b) & 1u, tma_failed, error);
         phases ^= 1u << b;
       }
       __syncthreads();
+      // Block k + 2 reuses the slots of block k - 1, whose estimate rows were
+      // last read before the second barrier of step k - 1 and whose guide rows
+      // before the barrier above.
+      issue(k + 2);
+      cp_async_commit();
       const float* eb = S.e[(k % 3) * BH] + rem;
       const float* gb = S.g[TMA ? k % 3 : 0] + rem;
       // 1. blur #1, horizontal: rows E..E+7, columns x0-R .. x0-R+134
