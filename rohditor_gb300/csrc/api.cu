@@ -441,7 +441,7 @@ Status develop_impl(rd_ctx* h, const uint16_t* d_raw, size_t row_stride, const r
   if (st.ok()) st = rd::run_demosaic(ctx, src, s.demosaic, result->rgb, d_stats);
   tm.mark();
   if (st.ok() && cancel && *cancel) st = Status{RD_CANCELLED, "cancelled"};
-  if (st.ok() && detail) st = rd::run_capture(ctx, result->rgb, W, H, *detail, nullptr);
+  if (st.ok() && detail) st = rd::run_capture(ctx, result->rgb, W, H, *detail);
   tm.mark();
   if (d_mosaic) rd::device_free(ctx, d_mosaic, mosaic_bytes);
   uint64_t host_stats[16] = {};
@@ -1076,7 +1076,7 @@ rd_status rd_stage_capture(rd_ctx* h, float* rgb, uint32_t W, uint32_t H, const 
   float* d = nullptr;
   size_t bytes = 0;
   Status st = upload_planar(ctx, rgb, (int)W, (int)H, &d, &bytes);
-  if (st.ok()) st = rd::run_capture(ctx, d, (int)W, (int)H, *detail, nullptr);
+  if (st.ok()) st = rd::run_capture(ctx, d, (int)W, (int)H, *detail);
   if (st.ok()) st = rd::check_kernel_error(ctx, "capture");
   if (st.ok() && download_planar(h, d, (int)W, (int)H, rgb) != RD_OK) st = Status{RD_READBACK, "readback failed"};
   if (d) rd::device_free(ctx, d, bytes);

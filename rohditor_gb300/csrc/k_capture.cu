@@ -13,7 +13,11 @@
 //                -> estimate = clamp(estimate * b, guide/2, 2 guide)
 //                so an iteration reads the estimate and guide once and writes
 //                the estimate once (12 bytes per pixel of compulsory traffic);
-//   rl_apply     the bounded common RGB gain, fused with vignetting.
+//   rl_step      the same iteration with constant row lags for images of at
+//                least 256 x 64 (fewer instructions per row, see below);
+//   rl_apply     the bounded common RGB gain;
+//   vignette_scan / vignette_plane  the exact incremental radius scan and the
+//                vignetting multiplier plane the optics gather reads.
 // Every blur keeps the reference's tap order (horizontal pass, then vertical,
 // each tap added in kernel order from 0; border columns start from -0.0 as
 // Iterator::sum does) and its half-sample mirror at the image edges. Field
@@ -1058,111 +1062,61 @@ Status rl_iteration(Context& ctx, int r, const Taps& taps, const float* est, con
 // thread per row walks the row and records r2 at every SEG-th column; the
 // apply kernel resumes each SEG-column segment from its checkpoint exactly.
 constexpr int SEG = 32;
+constexpr int VIGNETTE_MAX_WIDTH = 24576;  // the staged increments fit in shared memory
 
-__global__ void vignette_scan_kernel(const float* __restrict__ incr, const float* __restrict__ r2_start, int W, int H,
-                                     float* __restrict__ checkpoints, int segs) {
+// One thread per row. The increments are the same for every row, so a block
+// stages them in shared memory and every read is a broadcast; what remains on
+// a row is its chain of dependent additions. Checkpoints are stored segment
+// major (checkpoints[s * H + y]) so that a warp's stores are contiguous.
+__global__ void __launch_bounds__(64) vignette_scan_kernel(const float* __restrict__ incr,
+                                                           const float* __restrict__ r2_start, int W, int H,
+                                                           float* __restrict__ checkpoints, int segs) {
+  extern __shared__ __align__(16) float s_incr[];
+  for (int i = threadIdx.x; i < W; i += blockDim.x) s_incr[i] = incr[i];
+  __syncthreads();
   const int y = blockIdx.x * blockDim.x + threadIdx.x;
   if (y >= H) return;
   float r2 = r2_start[y];
-  float* cp = checkpoints + (long long)y * segs;
-  for (int s = 0; s < segs; ++s) {
-    cp[s] = r2;
-    const int x0 = s * SEG;
-    if (x0 + SEG <= W) {
-      // A whole segment: its 32 increments arrive in eight 16-byte loads issued
-      // together, then are added in column order.
-      float4 v[SEG / 4];
+  const int full = W / SEG;
+  for (int s = 0; s < full; ++s) {
+    checkpoints[(long long)s * H + y] = r2;
+    const float4* v = reinterpret_cast<const float4*>(s_incr + s * SEG);
 #pragma unroll
-      for (int q = 0; q < SEG / 4; ++q) v[q] = __ldg(reinterpret_cast<const float4*>(incr + x0) + q);
-#pragma unroll
-      for (int q = 0; q < SEG / 4; ++q) {
-        r2 += v[q].x;
-        r2 += v[q].y;
-        r2 += v[q].z;
-        r2 += v[q].w;
-      }
-    } else {
-      for (int x = x0; x < W; ++x) r2 += incr[x];
+    for (int q = 0; q < SEG / 4; ++q) {
+      const float4 t = v[q];
+      r2 += t.x;
+      r2 += t.y;
+      r2 += t.z;
+      r2 += t.w;
     }
   }
+  // A last partial segment needs only its start.
+  if (full < segs) checkpoints[(long long)full * H + y] = r2;
 }
 
 struct ApplyParams {
   float* rgb;
   long long plane;
   int W, H;
-  // capture gain
-  int capture;
   float amount;
   const float* mask;
   const float* est;
   const float* guide;
-  // vignetting
-  int vignetting;
-  const float* incr;
-  const float* checkpoints;
-  int segs;
-  float k1, k2, k3;
-  unsigned* error;
 };
 
-// One warp per (row, 32 segments): each lane resumes the radius scan of one
-// SEG-column segment from its checkpoint, multipliers go through shared
-// memory, and the warp then sweeps the 1024 pixels with coalesced accesses.
+// sharpening.rs:110-118: the bounded common gain 1 + amount * mask * (est /
+// guide - 1) on all three channels, skipped when it is 1 or would make a
+// channel non-finite. One thread per pixel, coalesced planes.
 __global__ void __launch_bounds__(256) rl_apply_kernel(const ApplyParams p) {
-  __shared__ float mult[8][32][SEG + 1];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int y = blockIdx.y;
-  const int seg0 = (blockIdx.x * 8 + warp) * 32;  // first segment of this warp
-  if (seg0 * SEG >= p.W) return;
-  bool bad = false;
-  if (p.vignetting) {
-    const int s = seg0 + lane;
-    if (s < p.segs) {
-      float r2 = p.checkpoints[(long long)y * p.segs + s];
-      const int xs = s * SEG;
-      for (int j = 0; j < SEG; ++j) {
-        const int x = xs + j;
-        float m = 1.0f;
-        if (x < p.W) {
-          const float r4 = r2 * r2, r6 = r4 * r2;
-          const float gain = 1.0f + p.k1 * r2 + p.k2 * r4 + p.k3 * r6;
-          if (!isfinite(gain) || gain == 0.0f) bad = true;
-          m = 1.0f / gain;
-          r2 += p.incr[x];
-        }
-        mult[warp][lane][j] = m;
-      }
-    }
-    __syncwarp();
+  const long long o = (long long)blockIdx.x * 256 + threadIdx.x;
+  if (o >= p.plane) return;
+  float v0 = p.rgb[o], v1 = p.rgb[p.plane + o], v2 = p.rgb[2 * p.plane + o];
+  const float gain = 1.0f + p.amount * p.mask[o] * (p.est[o] / p.guide[o] - 1.0f);
+  if (gain != 1.0f && isfinite(v0 * gain) && isfinite(v1 * gain) && isfinite(v2 * gain)) {
+    p.rgb[o] = v0 * gain;
+    p.rgb[p.plane + o] = v1 * gain;
+    p.rgb[2 * p.plane + o] = v2 * gain;
   }
-  for (int j = 0; j < 32; ++j) {
-    const int s = seg0 + j;
-    const int x = s * SEG + lane;
-    if (s >= p.segs || x >= p.W) continue;
-    const long long o = (long long)y * p.W + x;
-    float v0 = p.rgb[o], v1 = p.rgb[p.plane + o], v2 = p.rgb[2 * p.plane + o];
-    if (p.capture) {
-      // sharpening.rs:110-118
-      const float gain = 1.0f + p.amount * p.mask[o] * (p.est[o] / p.guide[o] - 1.0f);
-      if (gain != 1.0f && isfinite(v0 * gain) && isfinite(v1 * gain) && isfinite(v2 * gain)) {
-        v0 *= gain;
-        v1 *= gain;
-        v2 *= gain;
-      }
-    }
-    if (p.vignetting) {
-      const float m = mult[warp][j][lane];
-      v0 *= m;
-      v1 *= m;
-      v2 *= m;
-      if (!isfinite(v0) || !isfinite(v1) || !isfinite(v2)) bad = true;
-    }
-    p.rgb[o] = v0;
-    p.rgb[p.plane + o] = v1;
-    p.rgb[2 * p.plane + o] = v2;
-  }
-  if (bad) atomicOr(p.error, 4u);
 }
 
 }  // namespace
@@ -1194,6 +1148,7 @@ struct VignetteTables {
 // Host side of the vignetting scan: the column increments and the row starts
 // follow correction.rs:226-243 operation by operation in f32.
 Status prepare_vignetting(Context& ctx, const rd_optics_desc& o, int W, int H, VignetteTables& t) {
+  if (W > VIGNETTE_MAX_WIDTH) return Status{RD_INVALID_DIMENSIONS, "vignetting supports widths up to 24576"};
   const float ns = (float)o.norm_scale;
   const float step = 2.0f * ns, step_sq = ns * ns;
   const float start_x = (float)(-o.center_x), start_y = (float)(-o.center_y);
@@ -1216,7 +1171,10 @@ Status prepare_vignetting(Context& ctx, const rd_optics_desc& o, int W, int H, V
   t.checkpoints = t.r2_start + H;
   RD_TRY(upload(ctx, t.incr, incr.data(), sizeof(float) * W));
   RD_TRY(upload(ctx, t.r2_start, r2s.data(), sizeof(float) * H));
-  RD_LAUNCH(ctx, K_VIGNETTE, vignette_scan_kernel<<<(H + 127) / 128, 128, 0, ctx.stream>>>(t.incr, t.r2_start, W, H, t.checkpoints, t.segs));
+  const int smem = (int)(sizeof(float) * W);
+  RD_CUDA_TRY(cudaFuncSetAttribute(vignette_scan_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  RD_LAUNCH(ctx, K_VIGNETTE, vignette_scan_kernel<<<(H + 63) / 64, 64, smem, ctx.stream>>>(t.incr, t.r2_start, W, H,
+                                                                                         t.checkpoints, t.segs));
   RD_CUDA_TRY(cudaGetLastError());
   return Status{};
 }
@@ -1225,38 +1183,54 @@ Status prepare_vignetting(Context& ctx, const rd_optics_desc& o, int W, int H, V
 // Vignetting multiplier plane: mult[y][x] = 1 / (1 + k1 r2 + k2 r2^2 + k3 r2^3)
 // with r2 from the exact incremental scan. The optics gather and the area
 // reduction multiply each source sample by it on load, so the resident source
-// itself is never modified.
-__global__ void __launch_bounds__(256) vignette_plane_kernel(const float* __restrict__ incr,
-                                                             const float* __restrict__ checkpoints, int W, int H,
-                                                             int segs, float k1, float k2, float k3,
-                                                             float* __restrict__ mult, unsigned* error) {
-  __shared__ float m[8][32][SEG + 1];
+// itself is never modified. One warp per row: in a pass, lane l resumes the
+// scan of segment 32g + l from its checkpoint and computes the segment's 32
+// multipliers from increments staged in shared memory with one pad word per
+// 32 (lane stride 33 words, no bank conflicts); the warp then writes the
+// pass's 1024 values with coalesced stores through a transposition buffer.
+constexpr int VP_WARPS = 16;
+size_t vignette_plane_smem(int W) { return sizeof(float) * ((size_t)W + W / 32 + 1 + VP_WARPS * 32 * 33); }
+
+__global__ void __launch_bounds__(VP_WARPS * 32) vignette_plane_kernel(const float* __restrict__ incr,
+                                                                      const float* __restrict__ checkpoints, int W,
+                                                                      int H, int segs, float k1, float k2, float k3,
+                                                                      float* __restrict__ mult, unsigned* error) {
+  extern __shared__ float vsm[];
+  float* s_incr = vsm;
+  float* tbuf = vsm + W + W / 32 + 1;
+  for (int i = threadIdx.x; i < W; i += blockDim.x) s_incr[i + (i >> 5)] = incr[i];
+  __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int y = blockIdx.y;
-  const int seg0 = (blockIdx.x * 8 + warp) * 32;
-  if (seg0 >= segs) return;
+  const int y = blockIdx.x * VP_WARPS + warp;
+  if (y >= H) return;
+  float* t = tbuf + warp * 32 * 33;
   bool bad = false;
-  const int s = seg0 + lane;
-  if (s < segs) {
-    float r2 = checkpoints[(long long)y * segs + s];
-    for (int j = 0; j < SEG; ++j) {
-      const int x = s * SEG + j;
-      float v = 1.0f;
-      if (x < W) {
-        const float r4 = r2 * r2, r6 = r4 * r2;
-        const float gain = 1.0f + k1 * r2 + k2 * r4 + k3 * r6;
-        if (!isfinite(gain) || gain == 0.0f) bad = true;
-        v = 1.0f / gain;
-        r2 += incr[x];
+  for (int g = 0; g * 32 < segs; ++g) {
+    const int s = g * 32 + lane;
+    if (s < segs) {
+      float r2 = checkpoints[(long long)s * H + y];
+      const int xs = s * SEG;
+      const float* inc = s_incr + s * (SEG + 1);
+#pragma unroll 8
+      for (int j = 0; j < SEG; ++j) {
+        float m = 1.0f;
+        if (xs + j < W) {
+          const float r4 = r2 * r2, r6 = r4 * r2;
+          const float gain = 1.0f + k1 * r2 + k2 * r4 + k3 * r6;
+          if (!isfinite(gain) || gain == 0.0f) bad = true;
+          m = 1.0f / gain;
+          r2 += inc[j];
+        }
+        t[lane * 33 + j] = m;
       }
-      m[warp][lane][j] = v;
     }
-  }
-  __syncwarp();
-  for (int j = 0; j < 32; ++j) {
-    const int sj = seg0 + j;
-    const int x = sj * SEG + lane;
-    if (sj < segs && x < W) mult[(long long)y * W + x] = m[warp][j][lane];
+    __syncwarp();
+    for (int j = 0; j < 32; ++j) {
+      const int sj = g * 32 + j;
+      const int x = sj * SEG + lane;
+      if (sj < segs && x < W) mult[(long long)y * W + x] = t[j * 33 + lane];
+    }
+    __syncwarp();
   }
   if (bad) atomicOr(error, 4u);
 }
@@ -1265,22 +1239,24 @@ Status run_vignette_plane(Context& ctx, const rd_optics_desc& optics, float* mul
   const int W = (int)optics.width, H = (int)optics.height;
   VignetteTables vt;
   RD_TRY(prepare_vignetting(ctx, optics, W, H, vt));
-  dim3 grid((vt.segs + 8 * 32 - 1) / (8 * 32), H);
-  RD_LAUNCH(ctx, K_VIGNETTE, vignette_plane_kernel<<<grid, 256, 0, ctx.stream>>>(
-                                 vt.incr, vt.checkpoints, W, H, vt.segs, optics.vignetting_k[0],
-                                 optics.vignetting_k[1], optics.vignetting_k[2], mult, ctx.d_error));
-  const cudaError_t launch = cudaGetLastError();
+  const size_t smem = vignette_plane_smem(W);
+  cudaError_t launch =
+      cudaFuncSetAttribute(vignette_plane_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (launch == cudaSuccess) {
+    RD_LAUNCH(ctx, K_VIGNETTE, vignette_plane_kernel<<<(H + VP_WARPS - 1) / VP_WARPS, VP_WARPS * 32, smem, ctx.stream>>>(
+                                   vt.incr, vt.checkpoints, W, H, vt.segs, optics.vignetting_k[0],
+                                   optics.vignetting_k[1], optics.vignetting_k[2], mult, ctx.d_error));
+    launch = cudaGetLastError();
+  }
   device_free(ctx, vt.incr, vt.bytes);
   if (launch != cudaSuccess) return Status{RD_SYNCHRONIZATION, cudaGetErrorString(launch)};
   return Status{};
 }
 
 // Capture sharpening (and, when given, vignetting) on planar RGB in place.
-Status run_capture(Context& ctx, float* rgb, int W, int H, const rd_detail_desc& detail,
-                   const rd_optics_desc* vignetting) {
+Status run_capture(Context& ctx, float* rgb, int W, int H, const rd_detail_desc& detail) {
   const bool capture = detail.enabled && detail.amount > 0.0f;
-  const bool vig = vignetting && vignetting->vignetting == 1;
-  if (!capture && !vig) return Status{};
+  if (!capture) return Status{};
   const long long plane = (long long)W * H;
   float* planes = nullptr;
   size_t plane_bytes = 0;
@@ -1365,35 +1341,19 @@ Status run_capture(Context& ctx, float* rgb, int W, int H, const rd_detail_desc&
     }
     if (st.ok() && cudaGetLastError() != cudaSuccess) st = Status{RD_SYNCHRONIZATION, "capture kernels failed to launch"};
   }
-  VignetteTables vt;
-  if (st.ok() && vig) st = prepare_vignetting(ctx, *vignetting, W, H, vt);
   if (st.ok()) {
     ApplyParams ap{};
     ap.rgb = rgb;
     ap.plane = plane;
     ap.W = W;
     ap.H = H;
-    ap.capture = capture ? 1 : 0;
     ap.amount = detail.amount;
     ap.mask = mask;
     ap.est = est;
     ap.guide = guide;
-    ap.vignetting = vig ? 1 : 0;
-    ap.incr = vt.incr;
-    ap.checkpoints = vt.checkpoints;
-    ap.segs = vig ? vt.segs : (W + SEG - 1) / SEG;
-    if (vig) {
-      ap.k1 = vignetting->vignetting_k[0];
-      ap.k2 = vignetting->vignetting_k[1];
-      ap.k3 = vignetting->vignetting_k[2];
-    }
-    ap.error = ctx.d_error;
-    const int segs = (W + SEG - 1) / SEG;
-    dim3 grid((segs + 8 * 32 - 1) / (8 * 32), H);
-    RD_LAUNCH(ctx, K_RL_APPLY, rl_apply_kernel<<<grid, 256, 0, ctx.stream>>>(ap));
+    RD_LAUNCH(ctx, K_RL_APPLY, rl_apply_kernel<<<(unsigned)((plane + 255) / 256), 256, 0, ctx.stream>>>(ap));
     if (cudaGetLastError() != cudaSuccess) st = Status{RD_SYNCHRONIZATION, "capture apply failed to launch"};
   }
-  if (vt.incr) device_free(ctx, vt.incr, vt.bytes);
   if (planes) device_free(ctx, planes, plane_bytes);
   return st;
 }

@@ -204,8 +204,7 @@ Status run_opposed_labels(Context& ctx, float* mosaic, int width, int height, in
                           const float* ceiling, unsigned long long* d_stats, uint32_t* labels_out,
                           uint32_t* region_count);
 Status run_demosaic(Context& ctx, const MosaicSource& src, int algorithm, float* rgb, unsigned long long* clip_stats);
-Status run_capture(Context& ctx, float* rgb, int width, int height, const rd_detail_desc& detail,
-                   const rd_optics_desc* vignetting);
+Status run_capture(Context& ctx, float* rgb, int width, int height, const rd_detail_desc& detail);
 // Vignetting multiplier plane (width*height f32) of an optics execution.
 Status run_vignette_plane(Context& ctx, const rd_optics_desc& optics, float* mult);
 // Distortion / TCA gather; `mult` (optional) is the vignetting plane applied to
