@@ -867,6 +867,236 @@ __global__ void __launch_bounds__(128) rl_prep_kernel(const float* __restrict__ 
   if (bad) atomicOr(error, 2u);
 }
 
+// Constant-lag form of rl_prep_kernel for images of at least 256 x 64. Step k
+// turns RGB rows E..E+7 (E = E0 + 8k) into guide and initial-mask rows, blurs
+// them horizontally and emits the refined rows E-R..E-R+7. Every thread owns
+// one column of the 128-column window [x0 - R, x0 - R + 128) in every phase,
+// so the guide and mask values the refinement needs R rows later, and the 2R
+// blurred rows the vertical pass needs from the previous step, stay in its
+// registers. Rows and columns outside the image are loaded from their mirror
+// positions; the guide and mask are pointwise and the horizontal blur is
+// row-wise, so every mirrored value equals the one it mirrors bit for bit and
+// no segment needs special treatment. RGB blocks arrive by tensor copy (one
+// per plane, two steps ahead) when the window lies inside the image, else by
+// per-thread copies. Sums start from their first product: guide > 0 and
+// mask >= 0 (never -0.0), so 0 + p = p.
+template <int R>
+struct PrepGeom {
+  static constexpr int T = 2 * R + 1, QW = 128, SW = QW - 2 * R, BH = 8;
+  static constexpr int RUN = 9, H_RUNS = 14;  // 14 runs of 9 cover the output columns
+  static constexpr int PW = 144;              // guide / mask row stride
+  static constexpr int CWP = 132;             // RGB row stride = tensor-copy box width
+  static_assert(RUN * H_RUNS >= SW && RUN * H_RUNS - 1 + 2 * R < PW && R + RUN * H_RUNS <= PW, "runs fit the rows");
+  static_assert(QW + 3 <= CWP && (CWP * 4) % 16 == 0 && (BH * CWP * 4) % 128 == 0, "RGB block layout");
+};
+
+template <int R>
+struct __align__(128) PrepStepSmem {
+  using G = PrepGeom<R>;
+  float rgb[2][3 * G::BH][G::CWP];  // two slots of three 8-row plane blocks
+  float g[G::BH][G::PW], m[G::BH][G::PW];
+  float tg[G::BH][G::PW], tm[G::BH][G::PW];
+  unsigned long long bar[2];
+};
+
+template <int R, bool TMA>
+__global__ void __launch_bounds__(128, 4) rl_prep_step_kernel(const float* __restrict__ rgb, long long plane, float c0,
+                                                               float c1, float c2, float noise,
+                                                               float* __restrict__ guide, float* __restrict__ mask,
+                                                               int W, int H, int strips, int segs, int items,
+                                                               const Taps taps, const __grid_constant__ CUtensorMap rgb_map,
+                                                               unsigned* error) {
+  using G = PrepGeom<R>;
+  constexpr int T = G::T, SW = G::SW, BH = G::BH, N2 = 2 * R;
+  extern __shared__ __align__(128) float4 rl_prep_raw[];
+  PrepStepSmem<R>& S = *reinterpret_cast<PrepStepSmem<R>*>(rl_prep_raw);
+  float w[T];
+#pragma unroll
+  for (int k = 0; k < T; ++k) w[k] = taps.w[k];
+  const int tid = threadIdx.x;
+  if (TMA && tid == 0) {
+    for (int b = 0; b < 2; ++b) mbar_init(&S.bar[b]);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncthreads();
+  unsigned phases = 0;
+  bool tma_failed = false, bad = false;
+  const bool h_on = tid < G::H_RUNS * BH;
+  const int h_row = tid / G::H_RUNS, h_col = (tid % G::H_RUNS) * G::RUN;
+  for (int item = blockIdx.x; item < items; item += gridDim.x) {
+    const int strip = item % strips, seg = item / strips;
+    const int x0 = strip * SW;
+    const int y0 = (int)((long long)seg * H / segs), y1 = (int)((long long)(seg + 1) * H / segs);
+    const int E0 = y0 - R;
+    const int nsteps = (y1 - y0 + N2 - BH + 7) / BH + 1;
+    const bool inside = x0 - R >= 0 && x0 - R + G::QW <= W;
+    const bool tma_strip = TMA && inside;
+    const int xal = (x0 - R) & ~3;
+    const int rem = tma_strip ? (x0 - R) - xal : 0;
+    const int xc = x0 - R + tid;
+    const int sxc = (unsigned)xc < (unsigned)W ? xc : mirror_half(xc, W);
+    auto by_tma = [&](int k) {
+      const int r0 = E0 + BH * k;
+      return tma_strip && r0 >= 0 && r0 + BH <= H;
+    };
+    // Block k: RGB rows [E0 + 8k, +8) of the window into slot k & 1.
+    auto issue = [&](int k) {
+      if (k >= nsteps) return;
+      const int r0 = E0 + BH * k, b = k & 1;
+      if (by_tma(k)) {
+        if (tid == 0) {
+          asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+          mbar_expect_tx(&S.bar[b], 3 * BH * G::CWP * sizeof(float));
+#pragma unroll
+          for (int c = 0; c < 3; ++c) tma_load_2d(S.rgb[b][c * BH], &rgb_map, xal, c * H + r0, &S.bar[b]);
+        }
+        return;
+      }
+#pragma unroll
+      for (int j = 0; j < BH; ++j) {
+        const float* src = rgb + (long long)mirror_row(r0 + j, H) * W + sxc;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) cp_async4(&S.rgb[b][c * BH + j][rem + tid], src + c * plane);
+      }
+    };
+    auto arrive = [&](int k) {  // this thread's view of block k is complete
+      if (by_tma(k)) {
+        tma_wait(&S.bar[k & 1], (phases >> (k & 1)) & 1u, tma_failed, error);
+        phases ^= 1u << (k & 1);
+      }
+    };
+    __syncthreads();  // the previous item's last step has left both slots
+    issue(0);
+    cp_async_commit();
+    issue(1);
+    cp_async_commit();
+    asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    arrive(0);
+    __syncthreads();
+    // Carried rows: blurred guide / mask rows [E-2R, E); guide and initial
+    // mask rows [E-R, E) of this thread's column.
+    float ctg[N2], ctm[N2], cg[R], cm[R];
+#pragma unroll
+    for (int i = 0; i < N2; ++i) ctg[i] = ctm[i] = 1.0f;
+#pragma unroll
+    for (int i = 0; i < R; ++i) cg[i] = cm[i] = 1.0f;
+    const int xo = xc;  // output column of this thread, when it is one
+    const bool store_col = tid >= R && tid < R + SW && xo < W;
+    for (int k = 0; k < nsteps; ++k) {
+      const int E = E0 + BH * k;
+      // 1. guide and initial mask of rows E..E+7 (sharpening.rs:187-203)
+      float gcur[BH], mcur[BH];
+      {
+        const float* pr = &S.rgb[k & 1][0][rem + tid];
+#pragma unroll
+        for (int j = 0; j < BH; ++j) {
+          const float r = pr[j * G::CWP], g = pr[(BH + j) * G::CWP], b = pr[(2 * BH + j) * G::CWP];
+          if (!isfinite(r) || !isfinite(g) || !isfinite(b)) bad = true;
+          float s = -0.0f;
+          s += rmax(r, 0.0f) / 3.0f;
+          s += rmax(g, 0.0f) / 3.0f;
+          s += rmax(b, 0.0f) / 3.0f;
+          float peak = 0.0f;
+          peak = rmax(peak, r / c0);
+          peak = rmax(peak, g / c1);
+          peak = rmax(peak, b / c2);
+          gcur[j] = rmax(s, FLOOR);
+          mcur[j] = 1.0f - smoothstep(0.85f, 0.98f, peak);
+          S.g[j][tid] = gcur[j];
+          S.m[j][tid] = mcur[j];
+        }
+      }
+      __syncthreads();
+      // Slot k & 1 has been read: refill it with block k + 2.
+      issue(k + 2);
+      cp_async_commit();
+      // 2. horizontal blurs of rows E..E+7, output columns of the window
+      if (h_on) {
+        hrun_full<R, G::RUN>(S.g[h_row] + h_col, S.tg[h_row] + R + h_col, w);
+        hrun_full<R, G::RUN>(S.m[h_row] + h_col, S.tm[h_row] + R + h_col, w);
+      }
+      asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+      if (k + 1 < nsteps) arrive(k + 1);
+      __syncthreads();
+      // 3. vertical blurs and the mask refinement of rows E-R..E-R+7 (sharpening.rs:205-230)
+      {
+        float wg[BH + N2], wm[BH + N2];
+#pragma unroll
+        for (int i = 0; i < N2; ++i) {
+          wg[i] = ctg[i];
+          wm[i] = ctm[i];
+        }
+#pragma unroll
+        for (int j = 0; j < BH; ++j) {
+          wg[N2 + j] = S.tg[j][tid];
+          wm[N2 + j] = S.tm[j][tid];
+        }
+        if (store_col && E - R + BH > y0) {
+          float* pm = mask + (long long)(E - R) * W + xo;
+          float* pg = guide + (long long)(E - R) * W + xo;
+#pragma unroll
+          for (int j = 0; j < BH; ++j) {
+            const int y = E - R + j;
+            float bm = wm[j] * w[0], bg = wg[j] * w[0];
+#pragma unroll
+            for (int t = 1; t < T; ++t) {
+              bm += wm[j + t] * w[t];
+              bg += wg[j + t] * w[t];
+            }
+            const float m0 = j < R ? cm[j] : mcur[j - R];
+            const float g = j < R ? cg[j] : gcur[j - R];
+            const float b2 = bm * bm;
+            float m = rmin(m0, b2 * b2);
+            const float threshold = 0.0005f + noise * 0.008f + bg * noise * 0.02f;
+            const float detail = fabsf(g - bg);
+            m *= smoothstep(threshold, threshold * 3.0f, detail) * smoothstep(0.001f, 0.01f, g);
+            if (y >= y0 && y < y1) {
+              pm[(long long)j * W] = m;
+              pg[(long long)j * W] = g;
+            }
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < N2; ++i) {
+          ctg[i] = wg[BH + i];
+          ctm[i] = wm[BH + i];
+        }
+#pragma unroll
+        for (int i = 0; i < R; ++i) {
+          cg[i] = gcur[BH - R + i];
+          cm[i] = mcur[BH - R + i];
+        }
+      }
+    }
+  }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+  if (bad) atomicOr(error, 2u);
+}
+
+bool rl_prep_uses_step_kernel(int W, int H, int R) { return W >= 256 && H >= 64 && R >= 1 && R <= 4; }
+
+template <int R, bool TMA>
+Status launch_rl_prep_step(Context& ctx, const Taps& taps, const float* rgb, long long plane, const float ceil[3],
+                           float noise, float* guide, float* mask, int W, int H, const CUtensorMap* rgb_map) {
+  using G = PrepGeom<R>;
+  const size_t smem = sizeof(PrepStepSmem<R>);
+  RD_CUDA_TRY(cudaFuncSetAttribute(rl_prep_step_kernel<R, TMA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int occ = 0;
+  RD_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, rl_prep_step_kernel<R, TMA>, 128, smem));
+  const int sms = ctx.sm_count > 0 ? ctx.sm_count : 152;
+  const int slots = std::max(1, occ) * sms;
+  const int strips = (W + G::SW - 1) / G::SW;
+  // About three work items per resident CTA, each at least 32 rows.
+  const int segs = std::max(1, std::min(3 * std::max(1, slots / strips), H / 32));
+  const int items = strips * segs;
+  const int grid = std::min(items, slots);
+  CUtensorMap none{};
+  RD_LAUNCH(ctx, K_RL_MASK, rl_prep_step_kernel<R, TMA><<<grid, 128, smem, ctx.stream>>>(
+                                rgb, plane, ceil[0], ceil[1], ceil[2], noise, guide, mask, W, H, strips, segs, items,
+                                taps, rgb_map ? *rgb_map : none, ctx.d_error));
+  return Status{};
+}
+
 template <int R>
 Status launch_rl_prep(Context& ctx, const Taps& taps, const float* rgb, long long plane, const float ceil[3], float noise, float* guide,
                       float* mask, int W, int H) {
@@ -892,7 +1122,21 @@ Status launch_rl_prep(Context& ctx, const Taps& taps, const float* rgb, long lon
 }
 
 Status rl_prep(Context& ctx, int r, const Taps& taps, const float* rgb, long long plane, const float ceil[3], float noise, float* guide,
-               float* mask, int W, int H) {
+               float* mask, int W, int H, const CUtensorMap* rgb_map) {
+  if (rl_prep_uses_step_kernel(W, H, r)) {
+    switch (r) {
+#define RD_PREP_CASE(RR)                                                                                   \
+  case RR:                                                                                                 \
+    return rgb_map ? launch_rl_prep_step<RR, true>(ctx, taps, rgb, plane, ceil, noise, guide, mask, W, H, rgb_map) \
+                   : launch_rl_prep_step<RR, false>(ctx, taps, rgb, plane, ceil, noise, guide, mask, W, H, nullptr);
+      RD_PREP_CASE(1)
+      RD_PREP_CASE(2)
+      RD_PREP_CASE(3)
+      RD_PREP_CASE(4)
+#undef RD_PREP_CASE
+      default: break;
+    }
+  }
   switch (r) {
     case 1: return launch_rl_prep<1>(ctx, taps, rgb, plane, ceil, noise, guide, mask, W, H);
     case 2: return launch_rl_prep<2>(ctx, taps, rgb, plane, ceil, noise, guide, mask, W, H);
@@ -1285,7 +1529,12 @@ Status run_capture(Context& ctx, float* rgb, int W, int H, const rd_detail_desc&
   const float* est = guide;
   Status st;
   if (capture) {
-    st = rl_prep(ctx, r, taps, rgb, plane, detail.ceilings, detail.noise_protection, guide, mask, W, H);
+    // The RGB planes as one (W, 3H) tensor for the prep kernel's tensor copies.
+    CUtensorMap rgb_map;
+    const bool rgb_tma =
+        rl_prep_uses_step_kernel(W, H, r) && make_plane_map(&rgb_map, rgb, W, 3 * H, PrepGeom<1>::CWP, 8);
+    st = rl_prep(ctx, r, taps, rgb, plane, detail.ceilings, detail.noise_protection, guide, mask, W, H,
+                 rgb_tma ? &rgb_map : nullptr);
     // Tensor maps of the three planes an iteration can read (guide, then the
     // ping-pong estimates), for the TMA-fed estimate ring.
     CUtensorMap maps[3];
