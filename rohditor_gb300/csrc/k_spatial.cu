@@ -230,34 +230,45 @@ __device__ __forceinline__ void undistort_poly5_fast(float x, float y, float a, 
   oy = ry;
 }
 
-__device__ __forceinline__ float cubic_weight(float d) {
-  const float a = fabsf(d);
-  if (a <= 1.0f) return 1.5f * a * a * a - 2.5f * a * a + 1.0f;
-  if (a < 2.0f) return -0.5f * a * a * a + 2.5f * a * a - 4.0f * a + 2.0f;
-  return 0.0f;
+// cubic_weight (resample.rs) at the four distances x - (fx - 1) .. x - (fx + 2)
+// of a footprint with fx = floor(x) >= 1. Those differences are exact and lie
+// in [1, 2), [0, 1), [-1, 0) and [-2, -1), so each weight takes one fixed
+// branch: |d| <= 1 for the middle two, 1 < |d| < 2 for the outer two. The
+// outer distances reach 1 or 2 only when x is an integer, where the
+// reference's branch and this one both give +0.0.
+__device__ __forceinline__ void cubic_weights(float x, int fx, float (&w)[4]) {
+  const float a0 = fabsf(x - (float)(fx - 1));
+  const float a1 = fabsf(x - (float)fx);
+  const float a2 = fabsf(x - (float)(fx + 1));
+  const float a3 = fabsf(x - (float)(fx + 2));
+  w[0] = -0.5f * a0 * a0 * a0 + 2.5f * a0 * a0 - 4.0f * a0 + 2.0f;
+  w[1] = 1.5f * a1 * a1 * a1 - 2.5f * a1 * a1 + 1.0f;
+  w[2] = 1.5f * a2 * a2 * a2 - 2.5f * a2 * a2 + 1.0f;
+  w[3] = -0.5f * a3 * a3 * a3 + 2.5f * a3 * a3 - 4.0f * a3 + 2.0f;
 }
 
 // resample.rs:3-41. Returns false for a non-finite coordinate or a footprint
 // that leaves the image.
+template <bool VIG>
 __device__ __forceinline__ bool cubic_sample(const float* __restrict__ plane, const float* __restrict__ mult, int W,
                                              int H, float x, float y, float& out) {
   if (!isfinite(x) || !isfinite(y)) return false;
   const int fx = (int)floorf(x), fy = (int)floorf(y);
   if (fx - 1 < 0 || fy - 1 < 0 || fx + 2 >= W || fy + 2 >= H) return false;
   float value = 0.0f;
-  float wx[4];
-#pragma unroll
-  for (int ox = -1; ox <= 2; ++ox) wx[ox + 1] = cubic_weight(x - (float)(fx + ox));  // same for every row
+  float wx[4], wys[4];
+  cubic_weights(x, fx, wx);  // same for every row
+  cubic_weights(y, fy, wys);
 #pragma unroll
   for (int oy = -1; oy <= 2; ++oy) {
-    const float wy = cubic_weight(y - (float)(fy + oy));
+    const float wy = wys[oy + 1];
     const float* row = plane + (long long)(fy + oy) * W;
-    const float* mrow = mult ? mult + (long long)(fy + oy) * W : nullptr;
+    const float* mrow = VIG ? mult + (long long)(fy + oy) * W : nullptr;
 #pragma unroll
     for (int ox = -1; ox <= 2; ++ox) {
       const float weight = wy * wx[ox + 1];
       float sample = __ldg(row + fx + ox);
-      if (mrow) sample = sample * __ldg(mrow + fx + ox);  // the vignetted source value
+      if (VIG) sample = sample * __ldg(mrow + fx + ox);  // the vignetted source value
       value += sample * weight;
     }
   }
@@ -266,6 +277,7 @@ __device__ __forceinline__ bool cubic_sample(const float* __restrict__ plane, co
   return true;
 }
 
+template <bool VIG>
 __global__ void __launch_bounds__(256) optics_kernel(const OpticsParams p) {
   const int x = blockIdx.x * 32 + (threadIdx.x & 31);
   const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
@@ -298,7 +310,7 @@ __global__ void __launch_bounds__(256) optics_kernel(const OpticsParams p) {
     const float sx = post_transform(n[2 * c], p.fast.cxh, p.fast.cxl, p.fast, p.cx, p.unscale, fell_back);
     const float sy = post_transform(n[2 * c + 1], p.fast.cyh, p.fast.cyl, p.fast, p.cy, p.unscale, fell_back);
     float v = 0.0f;
-    if (!bad && !cubic_sample(p.in + c * plane, p.mult, p.W, p.H, sx, sy, v)) bad = true;
+    if (!bad && !cubic_sample<VIG>(p.in + c * plane, p.mult, p.W, p.H, sx, sy, v)) bad = true;
     p.out[c * plane + o] = v;
   }
   if (bad) atomicOr(p.error, 8u);
@@ -412,7 +424,11 @@ Status run_optics_gather(Context& ctx, const rd_optics_desc& o, const float* rgb
   split(o.center_y, p.fast.cyh, p.fast.cyl);
   split(o.norm_unscale, p.fast.uh, p.fast.ul);
   dim3 grid((W + 31) / 32, (H + 7) / 8);
-  RD_LAUNCH(ctx, K_OPTICS, optics_kernel<<<grid, 256, 0, ctx.stream>>>(p));
+  if (p.mult) {
+    RD_LAUNCH(ctx, K_OPTICS, optics_kernel<true><<<grid, 256, 0, ctx.stream>>>(p));
+  } else {
+    RD_LAUNCH(ctx, K_OPTICS, optics_kernel<false><<<grid, 256, 0, ctx.stream>>>(p));
+  }
   const cudaError_t launch = cudaGetLastError();
   device_free(ctx, dtab, sizeof(float) * tab.size());
   if (launch != cudaSuccess) return Status{RD_SYNCHRONIZATION, cudaGetErrorString(launch)};
