@@ -517,12 +517,13 @@ rd_status rd_ctx_create(int device, uint64_t budget_bytes, rd_ctx** out) {
     return RD_SYNCHRONIZATION;
   }
   for (auto& e : c.ev) cudaEventCreate(&e);
-  if (cudaMalloc(&c.d_error, sizeof(uint32_t)) != cudaSuccess ||
-      cudaMemsetAsync(c.d_error, 0, sizeof(uint32_t), c.stream) != cudaSuccess) {
+  if (cudaMalloc(&c.d_error, 4 * sizeof(uint32_t)) != cudaSuccess ||
+      cudaMemsetAsync(c.d_error, 0, 4 * sizeof(uint32_t), c.stream) != cudaSuccess) {
     cudaStreamDestroy(c.stream);
     delete h;
     return RD_SYNCHRONIZATION;
   }
+  c.d_work = c.d_error + 1;
   // Keep freed pool memory cached between calls instead of returning it to the driver.
   cudaMemPool_t pool;
   if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {

@@ -444,6 +444,32 @@ Status launch_rl_iter(Context& ctx, const float* est, const float* guide, float*
 //  * A sum starts from its first product instead of from zero: every value of
 //    the iteration is positive (estimate >= guide / 2 > 0, ratio >= 0, taps >
 //    0), and 0 + p = p for every such p, so the sums are unchanged.
+// Work item idx -> (strip, segment) for the dynamically scheduled strip
+// kernels: the items of the two edge strips (per-thread copies with mirrored
+// columns, the slowest) are handed out first, then the interior strips', so
+// that the longest items start early and the shorter ones fill in behind them.
+__device__ __forceinline__ void strip_item(int idx, int strips, int segs, int& strip, int& seg) {
+  const int ne = strips >= 2 ? 2 : 1;
+  if (idx < ne * segs) {
+    strip = (idx % ne) ? strips - 1 : 0;
+    seg = idx / ne;
+    return;
+  }
+  const int j = idx - ne * segs, ni = strips - ne;
+  strip = 1 + j % ni;
+  seg = j / ni;
+}
+
+// Next work item of the CTA from the launch's counter (zeroed before the
+// launch), broadcast through shared memory; the barrier in front also ends
+// every read of the previous item's shared buffers.
+__device__ __forceinline__ int next_item(unsigned* work, int& s_item) {
+  __syncthreads();
+  if (threadIdx.x == 0) s_item = (int)atomicAdd(work, 1u);
+  __syncthreads();
+  return s_item;
+}
+
 template <int R>
 struct StepGeom {
   static constexpr int T = 2 * R + 1;
@@ -514,7 +540,7 @@ __global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict
                                                           const StepSegments sg, int items, const Taps taps,
                                                           const __grid_constant__ CUtensorMap est_map,
                                                           const __grid_constant__ CUtensorMap guide_map,
-                                                          unsigned* error) {
+                                                          unsigned* work, unsigned* error) {
   using G = StepGeom<R>;
   constexpr int T = G::T, SW = G::SW, BH = G::BH, N2 = 2 * R;
   extern __shared__ __align__(128) float4 rl_step_raw[];
@@ -534,8 +560,10 @@ __global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict
   const bool h1_on = tid < G::H1_RUNS * BH, h2_on = tid < G::H2_RUNS * BH;
   const int h1_row = tid / G::H1_RUNS, h1_col = (tid % G::H1_RUNS) * G::RUN;
   const int h2_row = tid / G::H2_RUNS, h2_col = (tid % G::H2_RUNS) * G::RUN;
-  for (int item = blockIdx.x; item < items; item += gridDim.x) {
-    const int strip = item % strips, seg = item / strips;
+  __shared__ int s_item;
+  for (int item = next_item(work, s_item); item < items; item = next_item(work, s_item)) {
+    int strip, seg;
+    strip_item(item, strips, sg.segs, strip, seg);
     const int x0 = strip * SW;
     const int y0 = seg_row(sg, seg, H), y1 = seg_row(sg, seg + 1, H);
     const int E0 = y0 - N2;
@@ -545,6 +573,11 @@ __global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict
     const bool edge_q = x0 < R || x0 + SW + R > W;
     const int xal = (x0 - N2) & ~3;  // rounds down, also below 0
     const int rem = TMA ? (x0 - N2) - xal : 0;
+    // Guide boxes stay inside the image columns (a box crossing the image edge
+    // takes the tensor unit much longer); reads shift by xal - gx. Columns the
+    // shifted box misses lie outside the image and only feed ratio columns
+    // that are overwritten by their mirrors and outputs that are not stored.
+    const int gx = TMA ? min(max(xal, 0), W - G::EWP) : 0;
     const int xa = x0 - N2 + tid, xb = xa + 128;
     const int sxa = (unsigned)xa < (unsigned)W ? xa : mirror_half(xa, W);
     const bool has_b = tid + 128 < G::EW;
@@ -565,7 +598,7 @@ __global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         mbar_expect_tx(&S.bar[b], (et ? BH * G::EWP * sizeof(float) : 0) + G::GH * G::EWP * sizeof(float));
         if (et) tma_load_2d(S.e[b * BH], &est_map, xal, r0, &S.bar[b]);
-        tma_load_2d(S.g[b], &guide_map, xal, r0 - N2, &S.bar[b]);
+        tma_load_2d(S.g[b], &guide_map, gx, r0 - N2, &S.bar[b]);
       }
       if (et) return;
 #pragma unroll
@@ -576,8 +609,6 @@ __global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict
         if (has_b) cp_async4(dst + tid + 128, src + sxb);
       }
     };
-    // The previous item's last step may still read guide slots 0 and 1.
-    __syncthreads();
     issue(0);
     cp_async_commit();
     issue(1);
@@ -615,7 +646,7 @@ __global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict
       issue(k + 2);
       cp_async_commit();
       const float* eb = S.e[(k % 3) * BH] + rem;
-      const float* gb = S.g[TMA ? k % 3 : 0] + rem;
+      const float* gb = S.g[TMA ? k % 3 : 0] + rem + (xal - gx);
       // 1. blur #1, horizontal: rows E..E+7, columns x0-R .. x0-R+134
       if (h1_on) hrun_full<R, G::RUN>(eb + h1_row * G::EWP + h1_col, S.t[h1_row] + h1_col, w);
       float ec[BH];
@@ -727,9 +758,10 @@ Status launch_rl_step_t(Context& ctx, const float* est, const float* guide, floa
   const int items = strips * sg.segs;
   const int grid = std::min(items, slots);
   CUtensorMap none{};
+  RD_CUDA_TRY(cudaMemsetAsync(ctx.d_work, 0, sizeof(uint32_t), ctx.stream));
   RD_LAUNCH(ctx, K_RL_ITER, rl_step_kernel<R, TMA><<<grid, 128, smem, ctx.stream>>>(
                                 est, guide, out, W, H, strips, sg, items, taps, est_map ? *est_map : none,
-                                guide_map ? *guide_map : none, ctx.d_error));
+                                guide_map ? *guide_map : none, ctx.d_work, ctx.d_error));
   return Status{};
 }
 
@@ -905,7 +937,7 @@ __global__ void __launch_bounds__(128, 4) rl_prep_step_kernel(const float* __res
                                                                float* __restrict__ guide, float* __restrict__ mask,
                                                                int W, int H, int strips, int segs, int items,
                                                                const Taps taps, const __grid_constant__ CUtensorMap rgb_map,
-                                                               unsigned* error) {
+                                                               unsigned* work, unsigned* error) {
   using G = PrepGeom<R>;
   constexpr int T = G::T, SW = G::SW, BH = G::BH, N2 = 2 * R;
   extern __shared__ __align__(128) float4 rl_prep_raw[];
@@ -923,8 +955,10 @@ __global__ void __launch_bounds__(128, 4) rl_prep_step_kernel(const float* __res
   bool tma_failed = false, bad = false;
   const bool h_on = tid < G::H_RUNS * BH;
   const int h_row = tid / G::H_RUNS, h_col = (tid % G::H_RUNS) * G::RUN;
-  for (int item = blockIdx.x; item < items; item += gridDim.x) {
-    const int strip = item % strips, seg = item / strips;
+  __shared__ int s_item;
+  for (int item = next_item(work, s_item); item < items; item = next_item(work, s_item)) {
+    int strip, seg;
+    strip_item(item, strips, segs, strip, seg);
     const int x0 = strip * SW;
     const int y0 = (int)((long long)seg * H / segs), y1 = (int)((long long)(seg + 1) * H / segs);
     const int E0 = y0 - R;
@@ -965,7 +999,6 @@ __global__ void __launch_bounds__(128, 4) rl_prep_step_kernel(const float* __res
         phases ^= 1u << (k & 1);
       }
     };
-    __syncthreads();  // the previous item's last step has left both slots
     issue(0);
     cp_async_commit();
     issue(1);
@@ -1091,9 +1124,10 @@ Status launch_rl_prep_step(Context& ctx, const Taps& taps, const float* rgb, lon
   const int items = strips * segs;
   const int grid = std::min(items, slots);
   CUtensorMap none{};
+  RD_CUDA_TRY(cudaMemsetAsync(ctx.d_work, 0, sizeof(uint32_t), ctx.stream));
   RD_LAUNCH(ctx, K_RL_MASK, rl_prep_step_kernel<R, TMA><<<grid, 128, smem, ctx.stream>>>(
                                 rgb, plane, ceil[0], ceil[1], ceil[2], noise, guide, mask, W, H, strips, segs, items,
-                                taps, rgb_map ? *rgb_map : none, ctx.d_error));
+                                taps, rgb_map ? *rgb_map : none, ctx.d_work, ctx.d_error));
   return Status{};
 }
 

@@ -56,6 +56,7 @@ struct Context {
   std::string last_error;
   // Error word written by kernels (bounds/footprint/non-finite), read after a stage.
   uint32_t* d_error = nullptr;
+  uint32_t* d_work = nullptr;  // work-item counter of the dynamically scheduled kernels (beside d_error)
   // AMaZE per-CTA scratch slots (kept across calls).
   float* amaze_scratch = nullptr;
   size_t amaze_slots = 0;
