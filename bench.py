@@ -40,7 +40,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "24MP develops/s"
 UNIT = "develops/s"
-KERNEL_FAMILIES = 17  # RD_KERNEL_FAMILIES of include/rd_gpu.h
+KERNEL_FAMILIES = 16  # RD_KERNEL_FAMILIES of include/rd_gpu.h
 
 
 def dist_setup(gpus: int):
@@ -157,8 +157,7 @@ def family_bytes(name: str, N: int, n: int, H: int, tw: int) -> float | None:
         "rl_apply": 36.0 * N,
         "vignetting": 4.0 * N,      # multiplier plane out
         "optics_gather": 28.0 * N,  # RGB + multiplier in, RGB out
-        "area_horizontal": 12.0 * N + 12.0 * tw * H,
-        "area_vertical": 12.0 * tw * H + 12.0 * n,
+        "area_reduce": 12.0 * N + 12.0 * n,  # RGB in, reduced RGB out (one pass)
         "wb_matrix": 24.0 * n,
         "color_output": 15.0 * n,
         "opposed": 6.0 * N,

@@ -51,7 +51,7 @@ void device_free(Context& ctx, void* ptr, size_t bytes) {
 const char* kernel_family_name(int family) {
   static const char* names[K_FAMILY_COUNT] = {
       "normalize", "opposed", "mhc_bilinear", "rcd", "amaze", "rl_init", "rl_mask", "rl_iteration",
-      "rl_apply", "vignetting", "optics_gather", "area_horizontal", "area_vertical", "wb_matrix",
+      "rl_apply", "vignetting", "optics_gather", "area_reduce", "wb_matrix",
       "color_output", "synth", "display_output"};
   return family >= 0 && family < K_FAMILY_COUNT ? names[family] : "unknown";
 }
@@ -666,12 +666,7 @@ rd_status rd_spatial(rd_ctx* h, const rd_source* source, const rd_optics_desc* o
       if (cudaMemcpyAsync(base->rgb, reduce_in, base->bytes, cudaMemcpyDeviceToDevice, ctx.stream) != cudaSuccess)
         st = Status{RD_SYNCHRONIZATION, "copy failed"};
     } else {
-      const size_t mid_bytes = sizeof(float) * rd::area_reduce_scratch_floats(W, H, (int)tw, (int)th);
-      st = rd::device_alloc(ctx, mid_bytes, &p);
-      if (st.ok()) {
-        st = rd::run_area_reduce(ctx, reduce_in, reduce_mult, W, H, (int)tw, (int)th, base->rgb, static_cast<float*>(p));
-        rd::device_free(ctx, p, mid_bytes);
-      }
+      st = rd::run_area_reduce(ctx, reduce_in, reduce_mult, W, H, (int)tw, (int)th, base->rgb);
     }
   }
   tm.mark();
@@ -1115,12 +1110,7 @@ rd_status rd_stage_optics(rd_ctx* h, const rd_optics_desc* o, const float* rgb_i
       st = rd::run_optics_gather(ctx, *o, d, mult, warped);
     } else {
       // Vignetting only: the reduction kernel at 1:1 applies the multiplier exactly.
-      const size_t mid_bytes = sizeof(float) * rd::area_reduce_scratch_floats(W, H, W, H);
-      st = rd::device_alloc(ctx, mid_bytes, &p);
-      if (st.ok()) {
-        st = rd::run_area_reduce(ctx, d, mult, W, H, W, H, warped, static_cast<float*>(p));
-        rd::device_free(ctx, p, mid_bytes);
-      }
+      st = rd::run_area_reduce(ctx, d, mult, W, H, W, H, warped);
     }
   }
   if (st.ok()) st = rd::check_kernel_error(ctx, "optics");
@@ -1142,21 +1132,16 @@ rd_status rd_stage_area_reduce(rd_ctx* h, const float* rgb_in, uint32_t W, uint3
   float* d = nullptr;
   size_t bytes = 0;
   void* p = nullptr;
-  void* pm = nullptr;
   const size_t out_bytes = sizeof(float) * 3 * (size_t)tw * th;
-  const size_t mid_bytes = sizeof(float) * rd::area_reduce_scratch_floats((int)W, (int)H, (int)tw, (int)th);
   Status st = upload_planar(ctx, rgb_in, (int)W, (int)H, &d, &bytes);
   if (st.ok()) st = rd::device_alloc(ctx, out_bytes, &p);
-  if (st.ok()) st = rd::device_alloc(ctx, mid_bytes, &pm);
   if (st.ok())
-    st = rd::run_area_reduce(ctx, d, nullptr, (int)W, (int)H, (int)tw, (int)th, static_cast<float*>(p),
-                             static_cast<float*>(pm));
+    st = rd::run_area_reduce(ctx, d, nullptr, (int)W, (int)H, (int)tw, (int)th, static_cast<float*>(p));
   if (st.ok()) st = rd::check_kernel_error(ctx, "area reduce");
   if (st.ok() && download_planar(h, static_cast<float*>(p), (int)tw, (int)th, rgb_out) != RD_OK)
     st = Status{RD_READBACK, "readback failed"};
   if (d) rd::device_free(ctx, d, bytes);
   if (p) rd::device_free(ctx, p, out_bytes);
-  if (pm) rd::device_free(ctx, pm, mid_bytes);
   cudaStreamSynchronize(ctx.stream);
   return finish(h, st);
 }

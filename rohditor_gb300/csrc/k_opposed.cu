@@ -3,7 +3,7 @@
 //
 // Pipeline (all on the device, no host round trip between kernels):
 //   1. suspected-site count (early exit as opposed.rs:75-81 when zero: every
-//      later kernel reads the count and returns);
+//      later kernel reads the count and returns), in the same pass as
 //   2. cell summaries (cells.rs:41-113): per 2x2 cell, channel means of the
 //      clean positive samples and usable / suspected flags;
 //   3. dilated mask (regions.rs:127-182): a cell is inside when any cell of
@@ -58,6 +58,7 @@ struct OpposedParams {
   float ceiling[3];
   float4* cells;             // xyz = means, w = flags (as bits)
   unsigned char* dilated;
+  unsigned char* suspected;  // per cell: suspected-channel bits
   unsigned* parent;
   unsigned* labels;
   unsigned* block_sums;
@@ -155,48 +156,54 @@ __device__ __forceinline__ int pattern_position(int ch, unsigned support) {
   return -1;
 }
 
-// 1. suspected sites
-__global__ void count_kernel(const OpposedParams p) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
-  unsigned hit = 0, ch = 0;
-  if (x < p.W) {
-    ch = color_at(p.cfa, x, y);
-    hit = p.mosaic[(long long)y * p.W + x] >= p.levels[ch];
-  }
-  const unsigned ballot = __ballot_sync(0xffffffffu, hit);
-  if ((threadIdx.x & 31) == 0 && ballot) atomicAdd(&p.counters[0], __popc(ballot));
-  for (int c = 0; c < 3; ++c) {
-    const unsigned b = __ballot_sync(0xffffffffu, hit && ch == (unsigned)c);
-    if ((threadIdx.x & 31) == 0 && b) atomicAdd(&p.stats[6 + c], (unsigned long long)__popc(b));
-  }
-}
-
-// 2. cell summaries
-__global__ void cells_kernel(const OpposedParams p) {
-  if (p.counters[0] == 0) return;
+// 1 + 2. suspected sites and cell summaries (cells.rs:41-113) in one pass over
+// the mosaic: per 2x2 cell the channel means of the clean positive samples
+// (summed in raster order), the usable / suspected flags, a byte of suspected
+// bits for the dilation, and the suspected-site counts per channel, reduced
+// per block before they reach the global counters.
+__global__ void __launch_bounds__(128) cells_kernel(const OpposedParams p) {
+  __shared__ unsigned block_counts[4];
+  if (threadIdx.x < 4) block_counts[threadIdx.x] = 0;
+  __syncthreads();
   const int cx = blockIdx.x * blockDim.x + threadIdx.x, cy = blockIdx.y;
-  if (cx >= p.cw) return;
-  float sums[3] = {0.0f, 0.0f, 0.0f};
-  unsigned counts[3] = {0, 0, 0};
-  unsigned flags = 0;
-  for (int y = 2 * cy; y < min(2 * cy + 2, p.H); ++y)
-    for (int x = 2 * cx; x < min(2 * cx + 2, p.W); ++x) {
-      const int ch = color_at(p.cfa, x, y);
-      const float s = p.mosaic[(long long)y * p.W + x];
-      if (s >= p.levels[ch]) {
-        flags |= 1u << (ch + 3);
-      } else if (s > 0.0f) {
-        sums[ch] += s;
-        counts[ch] += 1;
+  unsigned n_ch[3] = {0, 0, 0};
+  if (cx < p.cw) {
+    float sums[3] = {0.0f, 0.0f, 0.0f};
+    unsigned counts[3] = {0, 0, 0};
+    unsigned flags = 0;
+    for (int y = 2 * cy; y < min(2 * cy + 2, p.H); ++y)
+      for (int x = 2 * cx; x < min(2 * cx + 2, p.W); ++x) {
+        const int ch = color_at(p.cfa, x, y);
+        const float s = p.mosaic[(long long)y * p.W + x];
+        if (s >= p.levels[ch]) {
+          flags |= 1u << (ch + 3);
+          n_ch[ch] += 1;
+        } else if (s > 0.0f) {
+          sums[ch] += s;
+          counts[ch] += 1;
+        }
       }
-    }
-  float m[3] = {0.0f, 0.0f, 0.0f};
-  for (int ch = 0; ch < 3; ++ch)
-    if (counts[ch] != 0) {
-      m[ch] = sums[ch] / (float)counts[ch];
-      flags |= 1u << ch;
-    }
-  p.cells[(long long)cy * p.cw + cx] = make_float4(m[0], m[1], m[2], __uint_as_float(flags));
+    float m[3] = {0.0f, 0.0f, 0.0f};
+    for (int ch = 0; ch < 3; ++ch)
+      if (counts[ch] != 0) {
+        m[ch] = sums[ch] / (float)counts[ch];
+        flags |= 1u << ch;
+      }
+    const long long i = (long long)cy * p.cw + cx;
+    p.cells[i] = make_float4(m[0], m[1], m[2], __uint_as_float(flags));
+    p.suspected[i] = (unsigned char)(flags >> 3);
+  }
+  // A cell holds at most four sites, so the per-channel counts of a warp fit
+  // 8-bit fields of one word.
+  const unsigned packed = n_ch[0] | n_ch[1] << 8 | n_ch[2] << 16;
+  const unsigned sum = __reduce_add_sync(0xffffffffu, packed);
+  if ((threadIdx.x & 31) == 0 && sum)
+    for (int c = 0; c < 3; ++c) atomicAdd(&block_counts[c], (sum >> (8 * c)) & 255u);
+  __syncthreads();
+  if (threadIdx.x < 3 && block_counts[threadIdx.x]) {
+    atomicAdd(&p.counters[0], block_counts[threadIdx.x]);
+    atomicAdd(&p.stats[6 + threadIdx.x], (unsigned long long)block_counts[threadIdx.x]);
+  }
 }
 
 // 3. dilation + union-find initialisation
@@ -205,12 +212,9 @@ __global__ void dilate_kernel(const OpposedParams p) {
   const int cx = blockIdx.x * blockDim.x + threadIdx.x, cy = blockIdx.y;
   if (cx >= p.cw) return;
   bool inside = false;
-  for (int y = max(cy - 1, 0); y <= min(cy + 1, p.ch - 1) && !inside; ++y)
+  for (int y = max(cy - 1, 0); y <= min(cy + 1, p.ch - 1); ++y)
     for (int x = max(cx - 1, 0); x <= min(cx + 1, p.cw - 1); ++x)
-      if (__float_as_uint(p.cells[(long long)y * p.cw + x].w) >> 3) {
-        inside = true;
-        break;
-      }
+      inside |= p.suspected[(long long)y * p.cw + x] != 0;
   const long long i = (long long)cy * p.cw + cx;
   p.dilated[i] = inside;
   p.parent[i] = inside ? (unsigned)i : NONE;
@@ -657,6 +661,7 @@ Status run_opposed_labels(Context& ctx, float* mosaic, int W, int H, int cfa, co
   };
   const size_t o_cells = take(sizeof(float4) * cells);
   const size_t o_dil = take(cells);
+  const size_t o_susp = take(cells);
   const size_t o_parent = take(sizeof(unsigned) * cells);
   const size_t o_labels = take(sizeof(unsigned) * cells);
   const size_t o_bsum = take(sizeof(unsigned) * scan_blocks);
@@ -682,6 +687,7 @@ Status run_opposed_labels(Context& ctx, float* mosaic, int W, int H, int cfa, co
   p.has_ceiling = ceiling ? 1 : 0;
   p.cells = reinterpret_cast<float4*>(b + o_cells);
   p.dilated = reinterpret_cast<unsigned char*>(b + o_dil);
+  p.suspected = reinterpret_cast<unsigned char*>(b + o_susp);
   p.parent = reinterpret_cast<unsigned*>(b + o_parent);
   p.labels = reinterpret_cast<unsigned*>(b + o_labels);
   p.block_sums = reinterpret_cast<unsigned*>(b + o_bsum);
@@ -695,7 +701,6 @@ Status run_opposed_labels(Context& ctx, float* mosaic, int W, int H, int cfa, co
   p.error = ctx.d_error;
   // Zero the per-label tables and counters (labels, dilation and cells are fully written).
   RD_CUDA_TRY(cudaMemsetAsync(b + o_rclip, 0, o_cnt + 256 - o_rclip, ctx.stream));
-  RD_LAUNCH(ctx, K_OPPOSED, count_kernel<<<dim3((W + 255) / 256, H), 256, 0, ctx.stream>>>(p));
   const dim3 cgrid((cw + 127) / 128, chh);
   RD_LAUNCH(ctx, K_OPPOSED, cells_kernel<<<cgrid, 128, 0, ctx.stream>>>(p));
   RD_LAUNCH(ctx, K_OPPOSED, dilate_kernel<<<cgrid, 128, 0, ctx.stream>>>(p));

@@ -317,38 +317,60 @@ __global__ void __launch_bounds__(256) optics_kernel(const OpticsParams p) {
 }
 
 // Horizontal area pass: one thread per (row, target column, channel-plane).
-__global__ void area_h_kernel(const float* __restrict__ in, const float* __restrict__ mult, int W, int H, int tw,
-                              const int* __restrict__ first,
-                              const int* __restrict__ offset, const int* __restrict__ count,
-                              const float* __restrict__ weights, float* __restrict__ mid) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y;
-  const int c = blockIdx.z;
-  if (t >= tw) return;
-  const float* row = in + (long long)c * W * H + (long long)y * W + first[t];
-  const float* mrow = mult ? mult + (long long)y * W + first[t] : nullptr;
-  const float* wt = weights + offset[t];
-  float acc = 0.0f;
-  for (int k = 0; k < count[t]; ++k) {
-    float sample = row[k];
-    if (mrow) sample = sample * mrow[k];
-    acc += sample * wt[k];
-  }
-  mid[(long long)c * tw * H + (long long)y * tw + t] = acc;
-}
+// Exact separable area reduction in one pass: a thread owns one output
+// column and channel of a tile of AREA_ROWS output rows and walks the tile's
+// input rows in order. Each input row's horizontal sum is computed once (a row
+// shared by two consecutive output rows is kept from the row before) and added
+// to the vertical sum of the output row it belongs to, so neither pass stores
+// the intermediate rows. Both sums accumulate their taps in table order from
+// 0, as the two-pass form (and resample.rs) does, so the outputs are the same
+// bit for bit.
+constexpr int AREA_ROWS = 16;
 
-__global__ void area_v_kernel(const float* __restrict__ mid, int H, int tw, int th, const int* __restrict__ first,
-                              const int* __restrict__ offset, const int* __restrict__ count,
-                              const float* __restrict__ weights, float* __restrict__ out) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int t = blockIdx.y;
+template <bool VIG>
+__global__ void __launch_bounds__(128) area_kernel(const float* __restrict__ in, const float* __restrict__ mult,
+                                                   int W, int H, int tw, int th, const int* __restrict__ hfirst,
+                                                   const int* __restrict__ hoffset, const int* __restrict__ hcount,
+                                                   const float* __restrict__ hweights,
+                                                   const int* __restrict__ vfirst, const int* __restrict__ voffset,
+                                                   const int* __restrict__ vcount, const float* __restrict__ vweights,
+                                                   float* __restrict__ out) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
   const int c = blockIdx.z;
-  if (x >= tw) return;
-  const float* col = mid + (long long)c * tw * H + (long long)first[t] * tw + x;
-  const float* wt = weights + offset[t];
-  float acc = 0.0f;
-  for (int k = 0; k < count[t]; ++k) acc += col[(long long)k * tw] * wt[k];
-  out[(long long)c * tw * th + (long long)t * tw + x] = acc;
+  if (s >= tw) return;
+  const int t0 = blockIdx.y * AREA_ROWS, t1 = min(t0 + AREA_ROWS, th);
+  const float* plane = in + (long long)c * W * H + hfirst[s];
+  const float* mplane = VIG ? mult + hfirst[s] : nullptr;
+  const float* hw = hweights + hoffset[s];
+  const int hn = hcount[s];
+  float* o = out + (long long)c * tw * th + s;
+  int last_r = -1;
+  float last_mid = 0.0f;
+  for (int t = t0; t < t1; ++t) {
+    const int r0 = vfirst[t], vn = vcount[t];
+    const float* vw = vweights + voffset[t];
+    float acc = 0.0f;
+    for (int k = 0; k < vn; ++k) {
+      const int r = r0 + k;
+      float mid;
+      if (r == last_r) {
+        mid = last_mid;
+      } else {
+        const float* row = plane + (long long)r * W;
+        const float* mrow = VIG ? mplane + (long long)r * W : nullptr;
+        mid = 0.0f;
+        for (int j = 0; j < hn; ++j) {
+          float sample = __ldg(row + j);
+          if (VIG) sample = sample * __ldg(mrow + j);
+          mid += sample * __ldg(hw + j);
+        }
+        last_r = r;
+        last_mid = mid;
+      }
+      acc += mid * __ldg(vw + k);
+    }
+    o[(long long)t * tw] = acc;
+  }
 }
 
 struct AxisTable {
@@ -435,14 +457,8 @@ Status run_optics_gather(Context& ctx, const rd_optics_desc& o, const float* rgb
   return Status{};
 }
 
-size_t area_reduce_scratch_floats(int W, int H, int tw, int th) {
-  (void)W;
-  (void)th;
-  return (size_t)3 * tw * H;
-}
 
-Status run_area_reduce(Context& ctx, const float* rgb, const float* mult, int W, int H, int tw, int th, float* out,
-                       float* mid) {
+Status run_area_reduce(Context& ctx, const float* rgb, const float* mult, int W, int H, int tw, int th, float* out) {
   const AxisTable ha = build_axis(W, tw), va = build_axis(H, th);
   const size_t ints = ha.first.size() * 3 + va.first.size() * 3;
   const size_t bytes = ints * sizeof(int) + (ha.weights.size() + va.weights.size()) * sizeof(float);
@@ -472,8 +488,14 @@ Status run_area_reduce(Context& ctx, const float* rgb, const float* mult, int W,
   const int* vc = vo + th;
   const float* hw = reinterpret_cast<const float*>(vc + th);
   const float* vw = hw + ha.weights.size();
-  RD_LAUNCH(ctx, K_AREA_H, area_h_kernel<<<dim3((tw + 127) / 128, H, 3), 128, 0, ctx.stream>>>(rgb, mult, W, H, tw, hf, ho, hc, hw, mid));
-  RD_LAUNCH(ctx, K_AREA_V, area_v_kernel<<<dim3((tw + 127) / 128, th, 3), 128, 0, ctx.stream>>>(mid, H, tw, th, vf, vo, vc, vw, out));
+  const dim3 grid((tw + 127) / 128, (th + AREA_ROWS - 1) / AREA_ROWS, 3);
+  if (mult) {
+    RD_LAUNCH(ctx, K_AREA, area_kernel<true><<<grid, 128, 0, ctx.stream>>>(rgb, mult, W, H, tw, th, hf, ho, hc, hw,
+                                                                               vf, vo, vc, vw, out));
+  } else {
+    RD_LAUNCH(ctx, K_AREA, area_kernel<false><<<grid, 128, 0, ctx.stream>>>(rgb, mult, W, H, tw, th, hf, ho, hc,
+                                                                                hw, vf, vo, vc, vw, out));
+  }
   const cudaError_t launch = cudaGetLastError();
   device_free(ctx, b, bytes);
   if (launch != cudaSuccess) return Status{RD_SYNCHRONIZATION, cudaGetErrorString(launch)};

@@ -42,7 +42,7 @@ struct Status {
 // Kernel families timed by the optional per-launch event bracketing.
 enum KernelFamily {
   K_NORMALIZE, K_OPPOSED, K_MHC, K_RCD, K_AMAZE, K_RL_INIT, K_RL_MASK, K_RL_ITER, K_RL_APPLY, K_VIGNETTE,
-  K_OPTICS, K_AREA_H, K_AREA_V, K_WB_MATRIX, K_COLOR, K_SYNTH, K_OUTPUT, K_FAMILY_COUNT
+  K_OPTICS, K_AREA, K_WB_MATRIX, K_COLOR, K_SYNTH, K_OUTPUT, K_FAMILY_COUNT
 };
 static_assert(K_FAMILY_COUNT == RD_KERNEL_FAMILIES, "family table size");
 const char* kernel_family_name(int family);
@@ -212,9 +212,10 @@ Status run_vignette_plane(Context& ctx, const rd_optics_desc& optics, float* mul
 // each source sample as it is read.
 Status run_optics_gather(Context& ctx, const rd_optics_desc& optics, const float* rgb_in, const float* mult,
                          float* rgb_out);
+// Exact area reduction of planar RGB to tw x th (one pass, no intermediate
+// plane); `mult` (optional) is applied to each source sample as it is read.
 Status run_area_reduce(Context& ctx, const float* rgb, const float* mult, int width, int height, int tw, int th,
-                       float* out, float* scratch);
-size_t area_reduce_scratch_floats(int width, int height, int tw, int th);
+                       float* out);
 Status run_wb_matrix(Context& ctx, float* rgb, size_t pixels, const float gains[3], const float matrix[9]);
 Status run_color_output(Context& ctx, const float* rgb, int width, int height, const rd_color_desc& color,
                         bool camera_native, uint8_t* srgb, unsigned long long* d_hist);
