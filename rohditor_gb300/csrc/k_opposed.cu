@@ -514,6 +514,17 @@ __device__ __forceinline__ bool total_less(float a, float b) {
   return a < b;
 }
 
+// Cell offsets (dx, dy) of the rings at Chebyshev distance 1, 2 and 3 (8, 16
+// and 24 cells), ring after ring, each in raster order.
+__constant__ char2 c_ring[48] = {
+    {-1, -1}, {0, -1}, {1, -1}, {-1, 0}, {1, 0}, {-1, 1}, {0, 1}, {1, 1},
+    {-2, -2}, {-1, -2}, {0, -2}, {1, -2}, {2, -2}, {-2, -1}, {2, -1}, {-2, 0},
+    {2, 0}, {-2, 1}, {2, 1}, {-2, 2}, {-1, 2}, {0, 2}, {1, 2}, {2, 2},
+    {-3, -3}, {-2, -3}, {-1, -3}, {0, -3}, {1, -3}, {2, -3}, {3, -3}, {-3, -2},
+    {3, -2}, {-3, -1}, {3, -1}, {-3, 0}, {3, 0}, {-3, 1}, {3, 1}, {-3, 2},
+    {3, 2}, {-3, 3}, {-2, 3}, {-1, 3}, {0, 3}, {1, 3}, {2, 3}, {3, 3},
+};
+
 // 7. per-site estimate (opposed.rs:86-180, 236-330)
 __global__ void estimate_kernel(const OpposedParams p) {
   if (p.counters[0] == 0) return;
@@ -543,18 +554,22 @@ __global__ void estimate_kernel(const OpposedParams p) {
           float local = 0.0f;
           int local_radius = 0;
           for (int radius = 1; radius <= LAST_RADIUS && !has_local; ++radius) {
-            for (int cy = max(ty - radius, 0); cy <= min(ty + radius, p.ch - 1); ++cy)
-              for (int cx = max(tx - radius, 0); cx <= min(tx + radius, p.cw - 1); ++cx) {
-                if (max(abs(tx - cx), abs(ty - cy)) != radius) continue;
-                const Cell cand = load_cell(p, cx, cy);
-                if (!(usable(cand, ch) && clean(cand, ch))) continue;
-                float value;
-                if (!correction(cand, ch, support, p.levels, value)) continue;
-                float cratio = 0.0f;
-                const bool has_cratio = log_ratio(cand, support, cratio);
-                if (!chroma_agrees(support, has_tratio, tratio, has_cratio, cratio)) continue;
-                if (count < MAX_CANDIDATES) corr[count++] = value;
-              }
+            // The ring's cells from the offset table (no pass over the square's
+            // interior); the candidates are sorted below, so the visiting order
+            // does not matter, and the three rings hold 48 = MAX_CANDIDATES cells.
+            const int ring0 = 4 * radius * (radius - 1), ring_n = 8 * radius;
+            for (int q = 0; q < ring_n; ++q) {
+              const int cx = tx + c_ring[ring0 + q].x, cy = ty + c_ring[ring0 + q].y;
+              if ((unsigned)cx >= (unsigned)p.cw || (unsigned)cy >= (unsigned)p.ch) continue;
+              const Cell cand = load_cell(p, cx, cy);
+              if (!(usable(cand, ch) && clean(cand, ch))) continue;
+              float value;
+              if (!correction(cand, ch, support, p.levels, value)) continue;
+              float cratio = 0.0f;
+              const bool has_cratio = log_ratio(cand, support, cratio);
+              if (!chroma_agrees(support, has_tratio, tratio, has_cratio, cratio)) continue;
+              if (count < MAX_CANDIDATES) corr[count++] = value;
+            }
             if (count >= MIN_CANDIDATES) {
               for (int a = 1; a < count; ++a) {  // insertion sort, total order
                 const float v = corr[a];
