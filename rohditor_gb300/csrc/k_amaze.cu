@@ -248,6 +248,9 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
   float* sm = reinterpret_cast<float*>(amaze_smem4);
   __shared__ unsigned long long s_stats[6];
   __shared__ int s_bad;
+  // Refined Nyquist sites of a step (phase B), by step parity.
+  __shared__ unsigned short s_nyq_queue[BH * (TS - 16) / 2];
+  __shared__ int s_nyq_n[2];
   const MosaicSource& src = prm.src;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const unsigned FULL = 0xffffffffu;
@@ -559,6 +562,7 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
 
     // ================= phase B: nyquist.rs:108-236, diagonal.rs, chroma.rs, mod.rs:196-268 =================
     for (int k = t; k < B_FLOATS; k += THREADS) sm[k] = 0.0f;
+    if (t < 2) s_nyq_n[t] = 0;
     __syncthreads();
     {
       const Ring<32, TS> cfa{sm + B_CFA_OFF};
@@ -647,42 +651,68 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
         //    combine_diagonals' pmwt (diagonal.rs:150-171) one step behind (lag 17),
         //    so they read rows finished in the step before and overlap the others.
         if (warp >= 2) {
-        // -- area interpolation at refined Nyquist sites (nyquist.rs:132-170), lag 8
+        // -- area interpolation at refined Nyquist sites (nyquist.rs:132-170), lag 8.
+        //    The flagged sites of the step are queued in shared memory (warp-
+        //    aggregated appends) and then taken by full warps; a neighbour's
+        //    terms are added as +0.0 when it is not flagged, which leaves every
+        //    sum unchanged (each starts at +0.0 and so can never be -0.0), so
+        //    the 7x7 loop runs without divergence.
           {
             const int lo = max(F - BH - 8, 8), hi = min(F - 8, TS - 8);
             constexpr int per_row = (TS - 16) / 2;
-            for (int k = t - 64; k < (hi - lo) * per_row; k += THREADS - 64) {
-              const int rr = lo + k / per_row;
-              const int cc = 8 + (g0 ^ (rr & 1)) + 2 * (k % per_row);
-              if (nyq2.row(rr)[cc >> 1] == 0) continue;
-              float sumcfa = 0.0f, sumh = 0.0f, sumv = 0.0f, sumsqh = 0.0f, sumsqv = 0.0f, areawt = 0.0f;
-            for (int di = -6; di < 7; di += 2) {
-              const int r1 = rr + di;
-              // Refined flags outside [8, 248) were never set: zero.
-              if (r1 < 8 || r1 >= TS - 8) continue;
-              const unsigned char* f = nyq2.row(r1);
-              const float* c0 = cfa.row(r1);
-              const float* cu = cfa.row(r1 - 1);
-              const float* cd = cfa.row(r1 + 1);
-              for (int c1 = cc - 6; c1 < cc + 7; c1 += 2) {
-                if (f[c1 >> 1] != 0) {
-                  const float c = c0[c1];
-                  sumcfa += c;
-                  sumh += c0[c1 - 1] + c0[c1 + 1];
-                  sumv += cu[c1] + cd[c1];
-                  sumsqh += sqr(c - c0[c1 - 1]) + sqr(c - c0[c1 + 1]);
-                  sumsqv += sqr(c - cu[c1]) + sqr(c - cd[c1]);
-                  areawt += 1.0f;
-                }
+            const int u = t - 64, par = (F / BH) & 1;
+            {
+              const int k = u;
+              bool flagged = false;
+              if (k < (hi - lo) * per_row) {
+                const int rr = lo + k / per_row;
+                const int cc = 8 + (g0 ^ (rr & 1)) + 2 * (k % per_row);
+                flagged = nyq2.row(rr)[cc >> 1] != 0;
+              }
+              const unsigned ballot = __ballot_sync(FULL, flagged);
+              if (ballot) {
+                int base = 0;
+                if (lane == 0) base = atomicAdd(&s_nyq_n[par], __popc(ballot));
+                base = __shfl_sync(FULL, base, 0);
+                if (flagged) s_nyq_queue[base + __popc(ballot & ((1u << lane) - 1u))] = (unsigned short)k;
               }
             }
-            sumh = sumcfa - 0.5f * sumh;
+            asm volatile("bar.sync 1, 960;" ::: "memory");
+            const int queued = s_nyq_n[par];
+            for (int q = u; q < queued; q += THREADS - 64) {
+              const int k = s_nyq_queue[q];
+              const int rr = lo + k / per_row;
+              const int cc = 8 + (g0 ^ (rr & 1)) + 2 * (k % per_row);
+              float sumcfa = 0.0f, sumh = 0.0f, sumv = 0.0f, sumsqh = 0.0f, sumsqv = 0.0f, areawt = 0.0f;
+              for (int di = -6; di < 7; di += 2) {
+                const int r1 = rr + di;
+                // Refined flags outside [8, 248) were never set: zero.
+                if (r1 < 8 || r1 >= TS - 8) continue;
+                const unsigned char* f = nyq2.row(r1);
+                const float* c0 = cfa.row(r1);
+                const float* cu = cfa.row(r1 - 1);
+                const float* cd = cfa.row(r1 + 1);
+#pragma unroll
+                for (int c1 = cc - 6; c1 < cc + 7; c1 += 2) {
+                  const bool on = f[c1 >> 1] != 0;
+                  const float c = c0[c1], l = c0[c1 - 1], r = c0[c1 + 1], up = cu[c1], dn = cd[c1];
+                  sumcfa += on ? c : 0.0f;
+                  sumh += on ? l + r : 0.0f;
+                  sumv += on ? up + dn : 0.0f;
+                  sumsqh += on ? sqr(c - l) + sqr(c - r) : 0.0f;
+                  sumsqv += on ? sqr(c - up) + sqr(c - dn) : 0.0f;
+                  areawt += on ? 1.0f : 0.0f;
+                }
+              }
+              sumh = sumcfa - 0.5f * sumh;
               sumv = sumcfa - 0.5f * sumv;
               areawt *= 0.5f;
               const float hcdvar = EPSSQ + fabsf(areawt * sumsqh - sumh * sumh);
               const float vcdvar = EPSSQ + fabsf(areawt * sumsqv - sumv * sumv);
               hv.row(rr)[cc >> 1] = hcdvar / (vcdvar + hcdvar);
             }
+            // The other parity's counter was last read in the step before.
+            if (u == 0) s_nyq_n[par ^ 1] = 0;
           }
           // -- diagonal_estimates (diagonal.rs:99-145), lag 8, red/blue sites of [8, 248)^2
           {
