@@ -59,6 +59,7 @@ struct OpposedParams {
   float4* cells;             // xyz = means, w = flags (as bits)
   unsigned char* dilated;
   unsigned char* suspected;  // per cell: suspected-channel bits
+  unsigned* sites;           // linear indices of the suspected sites (counters[2] of them)
   unsigned* parent;
   unsigned* labels;
   unsigned* block_sums;
@@ -167,6 +168,7 @@ __global__ void __launch_bounds__(128) cells_kernel(const OpposedParams p) {
   __syncthreads();
   const int cx = blockIdx.x * blockDim.x + threadIdx.x, cy = blockIdx.y;
   unsigned n_ch[3] = {0, 0, 0};
+  unsigned smask = 0;  // suspected positions of the cell, bit 2 dy + dx
   if (cx < p.cw) {
     float sums[3] = {0.0f, 0.0f, 0.0f};
     unsigned counts[3] = {0, 0, 0};
@@ -177,6 +179,7 @@ __global__ void __launch_bounds__(128) cells_kernel(const OpposedParams p) {
         const float s = p.mosaic[(long long)y * p.W + x];
         if (s >= p.levels[ch]) {
           flags |= 1u << (ch + 3);
+          smask |= 1u << (2 * (y - 2 * cy) + (x - 2 * cx));
           n_ch[ch] += 1;
         } else if (s > 0.0f) {
           sums[ch] += s;
@@ -192,6 +195,22 @@ __global__ void __launch_bounds__(128) cells_kernel(const OpposedParams p) {
     const long long i = (long long)cy * p.cw + cx;
     p.cells[i] = make_float4(m[0], m[1], m[2], __uint_as_float(flags));
     p.suspected[i] = (unsigned char)(flags >> 3);
+  }
+  // Append the cell's suspected sites to the list: one atomic per warp.
+  {
+    const unsigned FULL = 0xffffffffu, lane = threadIdx.x & 31;
+    const unsigned n_sites = __popc(smask);
+    unsigned incl = n_sites;
+    for (int off = 1; off < 32; off <<= 1) {
+      const unsigned v = __shfl_up_sync(FULL, incl, off);
+      if (lane >= (unsigned)off) incl += v;
+    }
+    const unsigned total = __shfl_sync(FULL, incl, 31);
+    unsigned base = 0;
+    if (lane == 31 && total) base = atomicAdd(&p.counters[2], total);
+    base = __shfl_sync(FULL, base, 31) + incl - n_sites;
+    for (unsigned k = 0; k < 4; ++k)
+      if (smask & (1u << k)) p.sites[base++] = (unsigned)((long long)(2 * cy + (k >> 1)) * p.W + 2 * cx + (k & 1));
   }
   // A cell holds at most four sites, so the per-channel counts of a warp fit
   // 8-bit fields of one word.
@@ -526,15 +545,19 @@ __constant__ char2 c_ring[48] = {
 };
 
 // 7. per-site estimate (opposed.rs:86-180, 236-330)
-__global__ void estimate_kernel(const OpposedParams p) {
-  if (p.counters[0] == 0) return;
-  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
-  unsigned long long n_rec = 0, n_changed = 0, n_fallback = 0, n_unsup = 0, n_neutral = 0;
-  if (x < p.W) {
+// The estimate of one suspected site (x, y); counts[5]: reconstructed,
+// changed, fallback, unsupported, neutralised.
+__device__ void estimate_site(const OpposedParams& p, int x, int y, unsigned (&counts)[5]) {
+  unsigned& n_rec = counts[0];
+  unsigned& n_changed = counts[1];
+  unsigned& n_fallback = counts[2];
+  unsigned& n_unsup = counts[3];
+  unsigned& n_neutral = counts[4];
+  {
     float& s = p.mosaic[(long long)y * p.W + x];
     const int ch = color_at(p.cfa, x, y);
     const float level = p.levels[ch];
-    if (s >= level) {
+    {
       const int tx = x / 2, ty = y / 2;
       const Cell target = load_cell(p, tx, ty);
       int support_count = 0;
@@ -639,16 +662,21 @@ __global__ void estimate_kernel(const OpposedParams p) {
       }
     }
   }
-  // Each counter is 0 or 1 per thread, so a warp's five sums fit 6-bit fields
-  // of one word and reduce in one step.
-  const unsigned packed = (unsigned)n_rec | (unsigned)n_changed << 6 | (unsigned)n_fallback << 12 |
-                          (unsigned)n_unsup << 18 | (unsigned)n_neutral << 24;
-  const unsigned sum = __reduce_add_sync(0xffffffffu, packed);
-  if ((threadIdx.x & 31) == 0 && sum)
-    for (int k = 0; k < 5; ++k) {
-      const unsigned long long t = (sum >> (6 * k)) & 63u;
-      if (t) atomicAdd(&p.stats[1 + k], t);
-    }
+}
+
+// 7. per-site estimate over the suspected sites listed by the cell pass, a
+// grid-stride loop whose warps are made of suspected sites only.
+__global__ void __launch_bounds__(256) estimate_kernel(const OpposedParams p) {
+  const unsigned n = p.counters[2];
+  unsigned counts[5] = {0, 0, 0, 0, 0};
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const unsigned idx = p.sites[i];
+    estimate_site(p, (int)(idx % (unsigned)p.W), (int)(idx / (unsigned)p.W), counts);
+  }
+  for (int k = 0; k < 5; ++k) {
+    const unsigned sum = __reduce_add_sync(0xffffffffu, counts[k]);
+    if ((threadIdx.x & 31) == 0 && sum) atomicAdd(&p.stats[1 + k], (unsigned long long)sum);
+  }
 }
 
 __global__ void copy_suspected_kernel(const OpposedParams p) {
@@ -679,6 +707,7 @@ Status run_opposed_labels(Context& ctx, float* mosaic, int W, int H, int cfa, co
   const size_t o_susp = take(cells);
   const size_t o_parent = take(sizeof(unsigned) * cells);
   const size_t o_labels = take(sizeof(unsigned) * cells);
+  const size_t o_sites = take(sizeof(unsigned) * (size_t)W * H);
   const size_t o_bsum = take(sizeof(unsigned) * scan_blocks);
   const size_t o_rclip = take(sizeof(unsigned) * max_labels);
   const size_t o_wanted = take(sizeof(unsigned) * max_labels);
@@ -703,6 +732,7 @@ Status run_opposed_labels(Context& ctx, float* mosaic, int W, int H, int cfa, co
   p.cells = reinterpret_cast<float4*>(b + o_cells);
   p.dilated = reinterpret_cast<unsigned char*>(b + o_dil);
   p.suspected = reinterpret_cast<unsigned char*>(b + o_susp);
+  p.sites = reinterpret_cast<unsigned*>(b + o_sites);
   p.parent = reinterpret_cast<unsigned*>(b + o_parent);
   p.labels = reinterpret_cast<unsigned*>(b + o_labels);
   p.block_sums = reinterpret_cast<unsigned*>(b + o_bsum);
@@ -728,7 +758,7 @@ Status run_opposed_labels(Context& ctx, float* mosaic, int W, int H, int cfa, co
   RD_LAUNCH(ctx, K_OPPOSED, border_kernel<<<cgrid, 128, 0, ctx.stream>>>(p, 0));
   RD_LAUNCH(ctx, K_OPPOSED, finish_moments_kernel<<<256, 256, 0, ctx.stream>>>(p));
   RD_LAUNCH(ctx, K_OPPOSED, border_kernel<<<cgrid, 128, 0, ctx.stream>>>(p, 1));
-  RD_LAUNCH(ctx, K_OPPOSED, estimate_kernel<<<dim3((W + 127) / 128, H), 128, 0, ctx.stream>>>(p));
+  RD_LAUNCH(ctx, K_OPPOSED, estimate_kernel<<<(ctx.sm_count > 0 ? ctx.sm_count : 152) * 8, 256, 0, ctx.stream>>>(p));
   RD_LAUNCH(ctx, K_OPPOSED, copy_suspected_kernel<<<1, 32, 0, ctx.stream>>>(p));
   cudaError_t launch = cudaGetLastError();
   if (launch == cudaSuccess && labels_out) {

@@ -162,6 +162,22 @@ def test_capture_constant_lag_kernel(stages, oracle, radius, size):
     assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32))
 
 
+@pytest.mark.parametrize("radius", [0.3, 1.2])
+@pytest.mark.parametrize("size", [(256, 64), (263, 71), (384, 129), (300, 65)])
+def test_capture_constant_lag_kernel_at_its_size_limits(stages, oracle, radius, size):
+    """The smallest images the constant-lag kernels take (256 x 64) and ragged
+    heights: segments of one 8-row unit, the last segment's alignment to the
+    bottom row and the first segment's mirrored top in the same few steps."""
+    from rohditor_gb300 import CaptureContract
+
+    w, h = size
+    rgb = np.abs(textured_mosaic(3 * w, h, seed=int(radius * 10) + h)).reshape(h, 3 * w)
+    cap = CaptureContract(amount=0.8, radius=radius, noise_protection=0.2, ceilings=(1.0, 1.0, 1.0), iterations=4)
+    ours = stages.capture(rgb, cap)
+    ref = oracle.capture(rgb, 0.8, radius, 0.2, (1.0, 1.0, 1.0), 4)
+    assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32))
+
+
 def test_capture_launch_shape_tuning_keeps_results(stages, oracle):
     """The first sharpening of an image shape times its iterations under several
     row-segment counts; the second uses the fastest. Both equal the oracle bit
