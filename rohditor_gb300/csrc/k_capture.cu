@@ -666,7 +666,9 @@ __global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict
 #pragma unroll
           for (int t = 1; t < T; ++t) b += win[j + t] * w[t];
           const float g = TMA ? gb[(R + j) * G::EWP + R + tid] : gq[j];
-          S.q[j][tid] = g / rmax(b, FLOOR);
+          // fmaxf(b, FLOOR) equals rmax(b, FLOOR): the floor is not NaN, and
+          // a NaN b gives the floor either way.
+          S.q[j][tid] = g / fmaxf(b, FLOOR);
         }
 #pragma unroll
         for (int i = 0; i < N2; ++i) c1[i] = win[BH + i];
@@ -707,9 +709,9 @@ __global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict
         }
         if (oko && E - N2 + BH > y0) {
           float* po = est_out + (long long)(E - N2) * W + xo;
+          float eo[BH];
 #pragma unroll
           for (int j = 0; j < BH; ++j) {
-            const int o = E - N2 + j;
             float b = win[j] * w[0];
 #pragma unroll
             for (int t = 1; t < T; ++t) b += win[j + t] * w[t];
@@ -718,7 +720,21 @@ __global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict
             const float lo = g * 0.5f, hi = g * 2.0f;
             if (e < lo) e = lo;
             if (e > hi) e = hi;
-            if (o >= y0 && o < y1) po[(long long)j * W] = e;
+            eo[j] = e;
+          }
+          if (E - N2 >= y0 && E - N2 + BH <= y1) {
+#pragma unroll
+            for (int j = 0; j < BH; ++j) {
+              *po = eo[j];
+              po += W;
+            }
+          } else {
+#pragma unroll
+            for (int j = 0; j < BH; ++j) {
+              const int o = E - N2 + j;
+              if (o >= y0 && o < y1) *po = eo[j];
+              po += W;
+            }
           }
         }
       }

@@ -173,20 +173,31 @@ __global__ void __launch_bounds__(128) cells_kernel(const OpposedParams p) {
     float sums[3] = {0.0f, 0.0f, 0.0f};
     unsigned counts[3] = {0, 0, 0};
     unsigned flags = 0;
-    for (int y = 2 * cy; y < min(2 * cy + 2, p.H); ++y)
-      for (int x = 2 * cx; x < min(2 * cx + 2, p.W); ++x) {
+#pragma unroll
+    for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+      for (int dx = 0; dx < 2; ++dx) {
+        const int y = 2 * cy + dy, x = 2 * cx + dx;
+        if (y >= p.H || x >= p.W) continue;
         const int ch = color_at(p.cfa, x, y);
         const float s = p.mosaic[(long long)y * p.W + x];
-        if (s >= p.levels[ch]) {
+        const bool susp = s >= p.levels[ch], clean = !susp && s > 0.0f;
+        if (susp) {
           flags |= 1u << (ch + 3);
-          smask |= 1u << (2 * (y - 2 * cy) + (x - 2 * cx));
-          n_ch[ch] += 1;
-        } else if (s > 0.0f) {
-          sums[ch] += s;
-          counts[ch] += 1;
+          smask |= 1u << (2 * dy + dx);
+        }
+        // Channel selects keep the per-channel values in registers.
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          if (c == ch && susp) n_ch[c] += 1;
+          if (c == ch && clean) {
+            sums[c] += s;
+            counts[c] += 1;
+          }
         }
       }
     float m[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
     for (int ch = 0; ch < 3; ++ch)
       if (counts[ch] != 0) {
         m[ch] = sums[ch] / (float)counts[ch];

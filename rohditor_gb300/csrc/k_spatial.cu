@@ -317,13 +317,25 @@ __global__ void __launch_bounds__(256) optics_kernel(const OpticsParams p) {
 }
 
 // Horizontal area pass: one thread per (row, target column, channel-plane).
+template <bool VIG>
+__device__ __forceinline__ float area_row(const float* __restrict__ row, const float* __restrict__ mrow,
+                                          const float* __restrict__ hw, int hn) {
+  float mid = 0.0f;
+  for (int j = 0; j < hn; ++j) {
+    float sample = __ldg(row + j);
+    if (VIG) sample = sample * __ldg(mrow + j);
+    mid += sample * __ldg(hw + j);
+  }
+  return mid;
+}
+
 // Exact separable area reduction in one pass: a thread owns one output
-// column and channel of a tile of AREA_ROWS output rows and walks the tile's
-// input rows in order. Each input row's horizontal sum is computed once (a row
-// shared by two consecutive output rows is kept from the row before) and added
-// to the vertical sum of the output row it belongs to, so neither pass stores
-// the intermediate rows. Both sums accumulate their taps in table order from
-// 0, as the two-pass form (and resample.rs) does, so the outputs are the same
+// column and channel of a tile of AREA_ROWS output rows and streams the
+// tile's input rows in order. Each input row's horizontal sum is computed
+// once and added to the vertical sum of every output row it belongs to (the
+// row where two output rows meet goes to both), so neither pass stores the
+// intermediate rows. Both sums accumulate their taps in table order from 0,
+// as the two-pass form (and resample.rs) does, so the outputs are the same
 // bit for bit.
 constexpr int AREA_ROWS = 16;
 
@@ -344,32 +356,26 @@ __global__ void __launch_bounds__(128) area_kernel(const float* __restrict__ in,
   const float* hw = hweights + hoffset[s];
   const int hn = hcount[s];
   float* o = out + (long long)c * tw * th + s;
-  int last_r = -1;
-  float last_mid = 0.0f;
-  for (int t = t0; t < t1; ++t) {
-    const int r0 = vfirst[t], vn = vcount[t];
-    const float* vw = vweights + voffset[t];
-    float acc = 0.0f;
-    for (int k = 0; k < vn; ++k) {
-      const int r = r0 + k;
-      float mid;
-      if (r == last_r) {
-        mid = last_mid;
-      } else {
-        const float* row = plane + (long long)r * W;
-        const float* mrow = VIG ? mplane + (long long)r * W : nullptr;
-        mid = 0.0f;
-        for (int j = 0; j < hn; ++j) {
-          float sample = __ldg(row + j);
-          if (VIG) sample = sample * __ldg(mrow + j);
-          mid += sample * __ldg(hw + j);
-        }
-        last_r = r;
-        last_mid = mid;
-      }
-      acc += mid * __ldg(vw + k);
+  int t = t0;
+  int first = vfirst[t], end = first + vcount[t];
+  const float* vw = vweights + voffset[t];
+  float acc = 0.0f;
+  const int r_end = vfirst[t1 - 1] + vcount[t1 - 1];
+  for (int r = first; r < r_end; ++r) {
+    const float mid = area_row<VIG>(plane + (long long)r * W, VIG ? mplane + (long long)r * W : nullptr, hw, hn);
+    acc += mid * __ldg(vw + (r - first));
+    if (r == end - 1) {
+      o[(long long)t * tw] = acc;
+      if (++t == t1) break;
+      const int nf = vfirst[t];
+      vw = vweights + voffset[t];
+      // The next output row starts at or before this input row (they share
+      // at most this one).
+      acc = 0.0f;
+      if (nf <= r) acc += mid * __ldg(vw + (r - nf));
+      first = nf;
+      end = nf + vcount[t];
     }
-    o[(long long)t * tw] = acc;
   }
 }
 
