@@ -715,12 +715,11 @@ __global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict
             float b = win[j] * w[0];
 #pragma unroll
             for (int t = 1; t < T; ++t) b += win[j + t] * w[t];
-            float e = (j < N2 ? ed[j] : ec[j - N2]) * b;
+            const float e = (j < N2 ? ed[j] : ec[j - N2]) * b;
             const float g = TMA ? gb[j * G::EWP + N2 + tid] : go[j];
-            const float lo = g * 0.5f, hi = g * 2.0f;
-            if (e < lo) e = lo;
-            if (e > hi) e = hi;
-            eo[j] = e;
+            // The develop rejects non-finite capture input, so e is never NaN
+            // here, and min / max give the reference's compare-and-replace.
+            eo[j] = fminf(fmaxf(e, g * 0.5f), g * 2.0f);
           }
           if (E - N2 >= y0 && E - N2 + BH <= y1) {
 #pragma unroll
@@ -1466,7 +1465,10 @@ Status prepare_vignetting(Context& ctx, const rd_optics_desc& o, int W, int H, V
   RD_TRY(upload(ctx, t.incr, incr.data(), sizeof(float) * W));
   RD_TRY(upload(ctx, t.r2_start, r2s.data(), sizeof(float) * H));
   const int smem = (int)(sizeof(float) * W);
-  RD_CUDA_TRY(cudaFuncSetAttribute(vignette_scan_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  // The limit is set to the largest size the kernel takes, never to this
+  // launch's: contexts on other threads launch it with other widths.
+  RD_CUDA_TRY(cudaFuncSetAttribute(vignette_scan_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)(sizeof(float) * VIGNETTE_MAX_WIDTH)));
   RD_LAUNCH(ctx, K_VIGNETTE, vignette_scan_kernel<<<(H + 63) / 64, 64, smem, ctx.stream>>>(t.incr, t.r2_start, W, H,
                                                                                          t.checkpoints, t.segs));
   RD_CUDA_TRY(cudaGetLastError());
@@ -1534,8 +1536,10 @@ Status run_vignette_plane(Context& ctx, const rd_optics_desc& optics, float* mul
   VignetteTables vt;
   RD_TRY(prepare_vignetting(ctx, optics, W, H, vt));
   const size_t smem = vignette_plane_smem(W);
-  cudaError_t launch =
-      cudaFuncSetAttribute(vignette_plane_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // The largest size the kernel takes (contexts on other threads launch it
+  // with other widths), not this launch's.
+  cudaError_t launch = cudaFuncSetAttribute(vignette_plane_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)vignette_plane_smem(VIGNETTE_MAX_WIDTH));
   if (launch == cudaSuccess) {
     RD_LAUNCH(ctx, K_VIGNETTE, vignette_plane_kernel<<<(H + VP_WARPS - 1) / VP_WARPS, VP_WARPS * 32, smem, ctx.stream>>>(
                                    vt.incr, vt.checkpoints, W, H, vt.segs, optics.vignetting_k[0],

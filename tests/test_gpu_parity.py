@@ -417,6 +417,33 @@ def test_develop_with_opposed(device, oracle):
     assert float(np.max(np.abs(got - ref))) <= 1e-4
 
 
+def test_concurrent_lanes_with_different_widths_repeat_exactly(device):
+    """Lanes on several threads launch the same kernels with different image
+    widths at once (per-launch shared-memory sizes, work counters, tuning
+    runs); repeated runs and a single lane give the same bytes."""
+    from rohditor_gb300 import CaptureContract, ColorContract, OpticsExecution, SensorDescription, clip_levels
+    from rohditor_gb300.batch import BatchImage, develop_batch
+    from rohditor_gb300.workloads import CAMERA_TO_REC2020, preview_dimensions
+
+    images = []
+    for k, (w, h) in enumerate([(1024, 96), (260, 300), (704, 128), (392, 200), (896, 72), (264, 264),
+                                (640, 160), (512, 112)]):
+        wb = (2.0, 1.0, 1.6)
+        sensor = SensorDescription(w, h, cfa="RGGB", black=(256.0,), white=(4095.0,), highlight="clip",
+                                   clip_levels=clip_levels(1.0, wb), demosaic="amaze", demosaic_balance=wb)
+        cap = CaptureContract(amount=0.5, radius=0.3 + 0.3 * (k % 4), noise_protection=0.5,
+                              ceilings=clip_levels(1.0, wb), iterations=3)
+        optics = OpticsExecution(w, h, vignetting_k=(-0.3, 0.05, -0.01))
+        images.append(BatchImage(raw_mosaic(w, h, w, seed=90 + k), sensor, cap, optics,
+                                 preview_dimensions(w, h, 256), wb, CAMERA_TO_REC2020,
+                                 ColorContract(wb_gains=wb, camera_to_rec2020=CAMERA_TO_REC2020)))
+    ref = develop_batch(images, lanes=1)[0]
+    for _ in range(3):
+        outs = develop_batch(images, lanes=4)[0]
+        for (a, ha), (b, hb) in zip(outs, ref):
+            assert np.array_equal(a, b) and np.array_equal(ha, hb)
+
+
 @pytest.mark.parametrize("graph", [False, True])
 def test_batched_develop_matches_one_at_a_time(device, graph):
     """rd_develop_batch (concurrent lanes) and rd_develop_batch_graph (one
