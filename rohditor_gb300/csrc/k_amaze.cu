@@ -48,6 +48,11 @@ namespace {
 
 constexpr int TS = 256, TSH = 128, BORDER = 16, VALID = TS - 2 * BORDER;
 constexpr int THREADS = 1024;
+static_assert(THREADS == 512 || THREADS == 1024, "thread roles below");
+// First thread of the vcd column chains: warps 16.. with 1024 threads, else
+// the same threads as the hcd chains, after them.
+constexpr int VCD_T0 = THREADS == 1024 ? 512 : 0;
+constexpr int AREA_THREADS = THREADS - 64;  // warps 2.. in phase B
 constexpr int BH = 8;  // rows per streaming step
 
 constexpr float EPS = 1.0e-5f, EPSSQ = 1.0e-10f, ARTHRESH = 0.75f;
@@ -441,9 +446,11 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
               last_b = __shfl_sync(FULL, cb, 31);
             }
           }
-        } else if (t >= 512 && t < 512 + 2 * (TS - 8)) {
-          // vcd column chains, lag 6: column vc, rows 4+par, 6+par, ... in order.
-          const int u = t - 512, vc = 4 + u % (TS - 8), par = u / (TS - 8);
+        }
+        if (t >= VCD_T0 && t < VCD_T0 + 2 * (TS - 8)) {
+          // vcd column chains, lag 6: column vc, rows 4+par, 6+par, ... in order
+          // (beside the hcd chains with 1024 threads, after them with fewer).
+          const int u = t - VCD_T0, vc = 4 + u % (TS - 8), par = u / (TS - 8);
           const int lo = max(F - BH - 6, 4), hi = min(F - 6, TS - 4);
           const bool vg4 = ((vc - 4) & 1) == 1;
           for (int rr = lo + ((lo ^ par) & 1); rr < hi; rr += 2) {
@@ -465,7 +472,7 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
         // -- cdd at red/blue sites (green.rs:187-222 tail), lag 6
         {
           const int lo = max(F - BH - 6, 4), hi = min(F - 6, TS - 4);
-          constexpr int per_row = 128;  // site slots per row: one pass of 1024 threads over 8 rows
+          constexpr int per_row = 128;  // site slots per row: 8 rows per step
           for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
             const int rr = lo + (k >> 7);
             const int cc = 4 + (g0 ^ (rr & 1)) + 2 * (k & 127);
@@ -476,7 +483,7 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
         // -- direction_weights (green.rs:225-292), lag 9, red/blue sites of [6, 250)^2
         {
           const int lo = max(F - BH - 9, 6), hi = min(F - 9, TS - 6);
-          constexpr int per_row = 128;  // site slots per row: one pass of 1024 threads over 8 rows
+          constexpr int per_row = 128;  // site slots per row: 8 rows per step
           for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
             const int rr = lo + (k >> 7);
             const int cc = 6 + (g0 ^ (rr & 1)) + 2 * (k & 127);
@@ -525,7 +532,7 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
         // -- Nyquist test (nyquist.rs:25-95), lag 8, red/blue sites of [6, 250)^2
         {
           const int lo = max(F - BH - 8, 6), hi = min(F - 8, TS - 6);
-          constexpr int per_row = 128;  // site slots per row: one pass of 1024 threads over 8 rows
+          constexpr int per_row = 128;  // site slots per row: 8 rows per step
           for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
             const int rr = lo + (k >> 7);
             const int cc = 6 + (g0 ^ (rr & 1)) + 2 * (k & 127);
@@ -604,7 +611,7 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
         //    diagonal_gradients (diagonal.rs:15-45), lag 6, rows [6, 250)
         {
           const int lo = max(F - BH - 2, 8), hi = min(F - 2, TS - 8);
-          constexpr int per_row = 128;  // site slots per row: one pass of 1024 threads over 8 rows
+          constexpr int per_row = 128;  // site slots per row: 8 rows per step
           for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
             const int rr = lo + (k >> 7);
             const int cc = 8 + (g0 ^ (rr & 1)) + 2 * (k & 127);
@@ -621,7 +628,7 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
         }
         {
           const int lo = max(F - BH - 6, 6), hi = min(F - 6, TS - 6);
-          constexpr int per_row = 128;  // site slots per row: one pass of 1024 threads over 8 rows
+          constexpr int per_row = 128;  // site slots per row: 8 rows per step
           for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
             const int rr = lo + (k >> 7);
             const int cc = 6 + 2 * (k & 127);
@@ -661,8 +668,9 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
             const int lo = max(F - BH - 8, 8), hi = min(F - 8, TS - 8);
             constexpr int per_row = (TS - 16) / 2;
             const int u = t - 64, par = (F / BH) & 1;
-            {
-              const int k = u;
+            // The step's sites are a multiple of 32 apart per pass, so every
+            // lane of a warp takes the same number of passes.
+            for (int k = u; k - (u & 31) < (hi - lo) * per_row; k += AREA_THREADS) {
               bool flagged = false;
               if (k < (hi - lo) * per_row) {
                 const int rr = lo + k / per_row;
@@ -677,9 +685,9 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
                 if (flagged) s_nyq_queue[base + __popc(ballot & ((1u << lane) - 1u))] = (unsigned short)k;
               }
             }
-            asm volatile("bar.sync 1, 960;" ::: "memory");
+            asm volatile("bar.sync 1, %0;" ::"n"(AREA_THREADS) : "memory");
             const int queued = s_nyq_n[par];
-            for (int q = u; q < queued; q += THREADS - 64) {
+            for (int q = u; q < queued; q += AREA_THREADS) {
               const int k = s_nyq_queue[q];
               const int rr = lo + k / per_row;
               const int cc = 8 + (g0 ^ (rr & 1)) + 2 * (k % per_row);
@@ -718,7 +726,7 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
           {
             const int lo = max(F - BH - 8, 8), hi = min(F - 8, TS - 8);
             constexpr int per_row = (TS - 16) / 2;
-            for (int k = t - 64; k < (hi - lo) * per_row; k += THREADS - 64) {
+            for (int k = t - 64; k < (hi - lo) * per_row; k += AREA_THREADS) {
               const int rr = lo + k / per_row;
               const int cc = 8 + (g0 ^ (rr & 1)) + 2 * (k % per_row);
               const int j = cc >> 1;
@@ -776,7 +784,7 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
         //    interpolation of combine_diagonals (lag 17, [10, 246)^2)
         {
           const int lo = max(F - BH - 17, 8), hi = min(F - 17, TS - 8);
-          constexpr int per_row = 128;  // site slots per row: one pass of 1024 threads over 8 rows
+          constexpr int per_row = 128;  // site slots per row: 8 rows per step
           for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
             const int rr = lo + (k >> 7);
             const int cc = 8 + (g0 ^ (rr & 1)) + 2 * (k & 127);
@@ -794,7 +802,7 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
         }
         {
           const int lo = max(F - BH - 17, 10), hi = min(F - 17, TS - 10);
-          constexpr int per_row = 128;  // site slots per row: one pass of 1024 threads over 8 rows
+          constexpr int per_row = 128;  // site slots per row: 8 rows per step
           for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
             const int rr = lo + (k >> 7);
             const int cc = 10 + (g0 ^ (rr & 1)) + 2 * (k & 127);
@@ -808,7 +816,7 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
         // -- refine_green (nyquist.rs:225-236), lag 19, refined Nyquist sites
         {
           const int lo = max(F - BH - 19, 8), hi = min(F - 19, TS - 8);
-          constexpr int per_row = 128;  // site slots per row: one pass of 1024 threads over 8 rows
+          constexpr int per_row = 128;  // site slots per row: 8 rows per step
           for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
             const int rr = lo + (k >> 7);
             const int cc = 8 + (g0 ^ (rr & 1)) + 2 * (k & 127);
@@ -846,7 +854,7 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
         //    differences to dgrb1 (chroma.rs:23-44), lag 19, [12, 244)^2
         {
           const int lo = max(F - BH - 19, 12), hi = min(F - 19, TS - 12);
-          constexpr int per_row = 128;  // site slots per row: one pass of 1024 threads over 8 rows
+          constexpr int per_row = 128;  // site slots per row: 8 rows per step
           for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
             const int rr = lo + (k >> 7);
             const int cc = 12 + (g0 ^ (rr & 1)) + 2 * (k & 127);
@@ -894,7 +902,7 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
         //    writes of each plane fall on different rows
         {
           const int lo = max(F - BH - 22, 14), hi = min(F - 22, TS - 14);
-          constexpr int per_row = 128;  // site slots per row: one pass of 1024 threads over 8 rows
+          constexpr int per_row = 128;  // site slots per row: 8 rows per step
           for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
             const int rr = lo + (k >> 7);
             const int start = 14 + (g0 ^ (rr & 1));
