@@ -77,7 +77,7 @@ __device__ __forceinline__ void color_pixel(const ColorParams& p, long long i, l
   atomicAdd(&bins[768 + (2126u * q[0] + 7152u * q[1] + 722u * q[2] + 5000u) / 10000u], 1u);
 }
 
-__global__ void __launch_bounds__(256) color_kernel(const ColorParams p) {
+__global__ void __launch_bounds__(256, 4) color_kernel(const ColorParams p) {
   __shared__ unsigned int bins[1024];
   for (int k = threadIdx.x; k < 1024; k += blockDim.x) bins[k] = 0;
   __syncthreads();
