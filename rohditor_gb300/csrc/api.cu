@@ -136,6 +136,7 @@ Status check_kernel_error(Context& ctx, const char* stage) {
     if (word & 8u) what += " optics footprint outside the image or non-finite coordinate;";
     if (word & 16u) what += " highlight reconstruction failed;";
     if (word & 32u) what += " capture-sharpening tensor copy timed out;";
+    if (word & 64u) what += " demosaic tile wait timed out;";
     return Status{RD_INVALID_INPUT, std::string(stage) + ":" + what};
   }
   return Status{};
@@ -540,7 +541,7 @@ void rd_ctx_destroy(rd_ctx* h) {
   if (!h) return;
   rd::Context& c = h->c;
   cudaSetDevice(c.device);
-  if (c.amaze_scratch) rd::device_free(c, c.amaze_scratch, 0);
+  if (c.amaze_scratch) rd::device_free(c, c.amaze_scratch, c.amaze_bytes);
   if (c.flush_buf) rd::device_free(c, c.flush_buf, c.flush_bytes);
   cudaStreamSynchronize(c.stream);
   for (void* p : c.pinned_uploads) cudaFreeHost(p);

@@ -86,9 +86,13 @@ extern "C" rd_status rd_develop_batch_graph(int device, rd_batch_item* items, in
   chains = std::min(chains, count);
   std::vector<rd_ctx*> ctxs(chains, nullptr);
   rd_status status = RD_OK;
+  // AMaZE scratch for the largest image: launches inside the capture never allocate.
+  size_t max_tiles = 1;
+  for (int k = 0; k < count; ++k)
+    max_tiles = std::max(max_tiles, rd::amaze_tiles((int)items[k].sensor.crop_width, (int)items[k].sensor.crop_height));
   for (int c = 0; c < chains && status == RD_OK; ++c) {
     status = rd_ctx_create(device, 0, &ctxs[c]);
-    if (status == RD_OK && !rd::reserve_amaze_scratch(ctxs[c]->c).ok()) status = RD_OVER_BUDGET;
+    if (status == RD_OK && !rd::reserve_amaze_scratch(ctxs[c]->c, max_tiles).ok()) status = RD_OVER_BUDGET;
     if (status == RD_OK && cudaStreamSynchronize(ctxs[c]->c.stream) != cudaSuccess) status = RD_SYNCHRONIZATION;
   }
   // Pinned staging for each image's mosaic, sRGB8 output and histogram,

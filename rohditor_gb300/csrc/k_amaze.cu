@@ -173,7 +173,16 @@ struct AmazeParams {
   int count_clip;          // 1: accumulate Clip statistics of core pixels
   unsigned long long* clip_stats;
   unsigned int* error;
+  unsigned* flags;         // per tile: 1 once its phase A is complete (zeroed per launch)
+  unsigned* work;          // work-item counter (zeroed per launch)
 };
+
+constexpr unsigned AMAZE_WAIT_TIMEOUT = 64u;
+__device__ __forceinline__ unsigned load_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
 
 // Mosaic sample at image coordinates (x, y), mirrored into the image when outside it.
 __device__ __forceinline__ float tile_sample(const MosaicSource& src, int x, int y, int W, int H) {
@@ -264,11 +273,7 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
   const float clip_pt8 = 0.8f * clip_pt;
   const int W = src.width, H = src.height;
   const long long plane = (long long)W * H;
-  float* slab = prm.slab + (size_t)blockIdx.x * SLAB_FLOATS;
-  float* g_hv = slab;
-  float* g_vrb = slab + TS * TSH;
-  float* g_hrb = slab + 2 * TS * TSH;
-  unsigned char* g_nyq = reinterpret_cast<unsigned char*>(slab + 3 * TS * TSH);
+
   // Rows holding blue sites: interpolate_chroma moves their differences to dgrb1 (chroma.rs:23-44).
   int ey;
   {
@@ -284,14 +289,32 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
   const int g0 = gae(pattern, 0);
   const unsigned ctab = pattern == 0 ? 0x94u : pattern == 1 ? 0x16u : pattern == 2 ? 0x61u : 0x49u;
 
+  // Work items from the launch's counter: item k < ntiles is phase A of tile
+  // k, item ntiles + k its phase B. All phase-A items are handed out first,
+  // so a phase-B item only waits for a phase A that a running CTA has taken
+  // (and phase A waits for nothing), and the 2 x ntiles half-tile items fill
+  // the SMs far more evenly than whole tiles would.
   const int ntiles = prm.tiles_x * prm.tiles_y;
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  __shared__ int s_item;
+  for (;;) {
+    __syncthreads();
+    if (t == 0) s_item = (int)atomicAdd(prm.work, 1u);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= 2 * ntiles) break;
+    const bool phase_b = item >= ntiles;
+    const int tile = phase_b ? item - ntiles : item;
     const int ox = (tile % prm.tiles_x) * VALID, oy = (tile / prm.tiles_x) * VALID;
+    // Per-tile slab: written by phase A, read by phase B (possibly on another SM).
+    float* slab = prm.slab + (size_t)tile * SLAB_FLOATS;
+    float* g_hv = slab;
+    float* g_vrb = slab + TS * TSH;
+    float* g_hrb = slab + 2 * TS * TSH;
+    unsigned char* g_nyq = reinterpret_cast<unsigned char*>(slab + 3 * TS * TSH);
 
+    if (!phase_b) {
     // ================= phase A: green.rs:13-292, nyquist.rs:25-95 =================
     for (int k = t; k < A_FLOATS; k += THREADS) sm[k] = 0.0f;
-    if (t < 6) s_stats[t] = 0;
-    if (t == 0) s_bad = 0;
     __syncthreads();
     {
       const Ring<16, TS> cfa{sm + A_CFA * 16 * TS}, w0{sm + A_W0 * 16 * TS}, w1{sm + A_W1 * 16 * TS},
@@ -566,6 +589,26 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
         __syncthreads();
       }
     }
+    // Publish the slab: every thread's writes, then the tile's flag.
+    __threadfence();
+    __syncthreads();
+    if (t == 0) atomicExch(&prm.flags[tile], 1u);
+    continue;
+    }
+
+    // Phase B waits (bounded) until the tile's phase A has published its slab.
+    if (t == 0) {
+      unsigned tries = 0;
+      while (load_acquire(&prm.flags[tile]) == 0u) {
+        if (++tries > (1u << 22)) {
+          atomicOr(prm.error, AMAZE_WAIT_TIMEOUT);
+          break;
+        }
+        __nanosleep(128);
+      }
+      s_bad = 0;
+    }
+    if (t < 6) s_stats[t] = 0;
 
     // ================= phase B: nyquist.rs:108-236, diagonal.rs, chroma.rs, mod.rs:196-268 =================
     for (int k = t; k < B_FLOATS; k += THREADS) sm[k] = 0.0f;
@@ -598,10 +641,11 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
           const int rr = lo + (k >> 7), j = k & (TSH - 1);
           if (rr < 6 || rr >= TS - 6) continue;
           const int o = rr * TSH + j;
-          hv.row(rr)[j] = g_hv[o];
-          vrb.row(rr)[j] = g_vrb[o];
-          hrb.row(rr)[j] = g_hrb[o];
-          nyq.row(rr)[j] = g_nyq[o];
+          // L2 reads: the slab may have been written by another SM.
+          hv.row(rr)[j] = __ldcg(g_hv + o);
+          vrb.row(rr)[j] = __ldcg(g_vrb + o);
+          hrb.row(rr)[j] = __ldcg(g_hrb + o);
+          nyq.row(rr)[j] = __ldcg(g_nyq + o);
         }
       };
       for (int F = BH; F <= TS + BH; F += BH) {
@@ -1009,41 +1053,41 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
 
 }  // namespace
 
-// Allocates the per-CTA slabs for the largest grid (one CTA per SM) up front,
-// so that later launches never allocate (a graph capture needs that).
-Status reserve_amaze_scratch(Context& ctx) {
-  const size_t sms = ctx.sm_count > 0 ? (size_t)ctx.sm_count : 152;
-  if (ctx.amaze_slots >= sms) return Status{};
-  if (ctx.amaze_scratch) device_free(ctx, ctx.amaze_scratch, ctx.amaze_slots * SLAB_FLOATS * sizeof(float));
+// Per-tile slabs and tile flags for `tiles` tiles, kept between calls and only
+// grown; reserved ahead of a graph capture so that launches never allocate.
+Status reserve_amaze_scratch(Context& ctx, size_t tiles) {
+  if (ctx.amaze_slots >= tiles) return Status{};
+  if (ctx.amaze_scratch) device_free(ctx, ctx.amaze_scratch, ctx.amaze_bytes);
   ctx.amaze_scratch = nullptr;
   ctx.amaze_slots = 0;
+  ctx.amaze_bytes = 0;
+  const size_t bytes = tiles * SLAB_FLOATS * sizeof(float) + tiles * sizeof(unsigned);
   void* p = nullptr;
-  RD_TRY(device_alloc(ctx, sms * SLAB_FLOATS * sizeof(float), &p));
-  RD_CUDA_TRY(cudaMemsetAsync(p, 0, sms * SLAB_FLOATS * sizeof(float), ctx.stream));
+  RD_TRY(device_alloc(ctx, bytes, &p));
   ctx.amaze_scratch = static_cast<float*>(p);
-  ctx.amaze_slots = sms;
+  ctx.amaze_slots = tiles;
+  ctx.amaze_bytes = bytes;
   return Status{};
+}
+
+size_t amaze_tiles(int width, int height) {
+  return (size_t)((width + VALID - 1) / VALID) * (size_t)((height + VALID - 1) / VALID);
 }
 
 Status run_amaze(Context& ctx, const MosaicSource& src, const float gains[3], float clip_point, float* rgb,
                  int count_clip, unsigned long long* clip_stats) {
   const int tiles_x = (src.width + VALID - 1) / VALID, tiles_y = (src.height + VALID - 1) / VALID;
   const int ntiles = tiles_x * tiles_y;
-  // One resident CTA per SM; balance the tiles so every CTA gets the same count or one fewer.
+  // One resident CTA per SM (shared memory); the CTAs take half-tile items
+  // from the counter.
   const int sms = ctx.sm_count > 0 ? ctx.sm_count : 152;
-  const int waves = (ntiles + sms - 1) / sms;
-  const int grid = (ntiles + waves - 1) / waves;
-  if ((size_t)grid > ctx.amaze_slots) {
-    // Slabs are kept between calls and only grow, to the grid of the largest image seen.
-    if (ctx.amaze_scratch) device_free(ctx, ctx.amaze_scratch, ctx.amaze_slots * SLAB_FLOATS * sizeof(float));
-    ctx.amaze_scratch = nullptr;
-    ctx.amaze_slots = 0;
-    void* p = nullptr;
-    RD_TRY(device_alloc(ctx, (size_t)grid * SLAB_FLOATS * sizeof(float), &p));
-    RD_CUDA_TRY(cudaMemsetAsync(p, 0, (size_t)grid * SLAB_FLOATS * sizeof(float), ctx.stream));
-    ctx.amaze_scratch = static_cast<float*>(p);
-    ctx.amaze_slots = grid;
-  }
+  const int grid = std::min(2 * ntiles, sms);
+  if (ctx.capturing && ctx.amaze_slots < (size_t)ntiles)
+    return Status{RD_INVALID_INPUT, "demosaic scratch was not reserved before the capture"};
+  RD_TRY(reserve_amaze_scratch(ctx, (size_t)ntiles));
+  unsigned* flags = reinterpret_cast<unsigned*>(ctx.amaze_scratch + ctx.amaze_slots * SLAB_FLOATS);
+  RD_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(unsigned) * ntiles, ctx.stream));
+  RD_CUDA_TRY(cudaMemsetAsync(ctx.d_work, 0, sizeof(uint32_t), ctx.stream));
   RD_CUDA_TRY(cudaFuncSetAttribute(amaze_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
   AmazeParams prm;
   prm.src = src;
@@ -1056,6 +1100,8 @@ Status run_amaze(Context& ctx, const MosaicSource& src, const float gains[3], fl
   prm.count_clip = count_clip;
   prm.clip_stats = clip_stats;
   prm.error = ctx.d_error;
+  prm.flags = flags;
+  prm.work = ctx.d_work;
   RD_LAUNCH(ctx, K_AMAZE, amaze_kernel<<<grid, THREADS, SMEM_BYTES, ctx.stream>>>(prm));
   RD_CUDA_TRY(cudaGetLastError());
   return Status{};

@@ -59,7 +59,8 @@ struct Context {
   uint32_t* d_work = nullptr;  // work-item counter of the dynamically scheduled kernels (beside d_error)
   // AMaZE per-CTA scratch slots (kept across calls).
   float* amaze_scratch = nullptr;
-  size_t amaze_slots = 0;
+  size_t amaze_slots = 0;  // tiles the AMaZE scratch holds slabs and flags for
+  size_t amaze_bytes = 0;
   int sm_count = 0;
   cudaEvent_t ev[8] = {};
   // Sizes of the allocations handed out through rd_device_alloc.
@@ -251,7 +252,9 @@ Status run_display_output(Context& ctx, const float* rgb, const rd_color_desc& c
 // Exhaustive device checks of the correctly rounded arithmetic (rd_check_math).
 Status run_math_check(Context& ctx, int which, uint64_t* result);
 
-Status reserve_amaze_scratch(Context& ctx);
+Status reserve_amaze_scratch(Context& ctx, size_t tiles);
+// AMaZE tiles of a width x height mosaic (224-pixel cores).
+size_t amaze_tiles(int width, int height);
 // Folds the timed RL iterations of a tuning run into the process-wide table of
 // launch shapes (k_capture.cu); called after a synchronisation.
 void resolve_rl_tuning(Context& ctx);
