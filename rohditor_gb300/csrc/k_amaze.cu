@@ -6,17 +6,19 @@
 // recurrences whose start depends on the tile edge. This kernel keeps the grid
 // and the arithmetic bit-identical and maps one tile onto one SM:
 //
-//  * one persistent 1024-thread CTA per SM walks tiles; a tile is processed
-//    top to bottom in steps of 8 rows. Every stage runs a fixed number of rows
+//  * one persistent 1024-thread CTA per SM takes half-tile work items (phase
+//    A or phase B of a tile, all phase-A items first) from a counter; a phase
+//    is processed top to bottom in steps of 8 rows. Every stage runs a fixed number of rows
 //    behind the rows loaded so far (its lag is the sum of the stencil reaches
 //    of the stages feeding it), and each plane lives in a shared-memory ring
 //    that holds just the rows still to be read;
 //  * phase A (gradients .. Nyquist test, green.rs + nyquist.rs:25-95) writes
 //    four small planes per tile (direction weight, bounded vertical and
 //    horizontal colour differences at red/blue sites, Nyquist flag: 416 KB)
-//    to an L2-resident per-CTA slab; phase B (Nyquist area .. output,
-//    nyquist.rs:108-236, diagonal.rs, chroma.rs, mod.rs:196-268) streams them
-//    back with the mosaic;
+//    to the tile's slab and publishes it with a release flag; phase B (Nyquist
+//    area .. output, nyquist.rs:108-236, diagonal.rs, chroma.rs,
+//    mod.rs:196-268), possibly on another SM, waits for the flag (bounded,
+//    error word on timeout) and streams the slab back from L2 with the mosaic;
 //  * the per-tile Nyquist bounding box (nyquist.rs:60-105) only prunes work:
 //    a site outside it has at most three flagged voters and is never refined,
 //    so the streamed stages evaluate every site of [8, 248)^2 and get the same
