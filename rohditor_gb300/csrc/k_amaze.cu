@@ -300,7 +300,12 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
   __shared__ int s_item;
   for (;;) {
     __syncthreads();
-    if (t == 0) s_item = (int)atomicAdd(prm.work, 1u);
+    if (t == 0) {
+      // The launch's last fetch (one past the items per CTA) resets the counter.
+      const unsigned v = atomicAdd(prm.work, 1u);
+      if (v == 2u * ntiles + gridDim.x - 1u) atomicExch(prm.work, 0u);
+      s_item = (int)v;
+    }
     __syncthreads();
     const int item = s_item;
     if (item >= 2 * ntiles) break;
@@ -1089,7 +1094,6 @@ Status run_amaze(Context& ctx, const MosaicSource& src, const float gains[3], fl
   RD_TRY(reserve_amaze_scratch(ctx, (size_t)ntiles));
   unsigned* flags = reinterpret_cast<unsigned*>(ctx.amaze_scratch + ctx.amaze_slots * SLAB_FLOATS);
   RD_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(unsigned) * ntiles, ctx.stream));
-  RD_CUDA_TRY(cudaMemsetAsync(ctx.d_work, 0, sizeof(uint32_t), ctx.stream));
   RD_CUDA_TRY(cudaFuncSetAttribute(amaze_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
   AmazeParams prm;
   prm.src = src;

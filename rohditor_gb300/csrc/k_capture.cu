@@ -460,12 +460,19 @@ __device__ __forceinline__ void strip_item(int idx, int strips, int segs, int& s
   seg = j / ni;
 }
 
-// Next work item of the CTA from the launch's counter (zeroed before the
-// launch), broadcast through shared memory; the barrier in front also ends
-// every read of the previous item's shared buffers.
-__device__ __forceinline__ int next_item(unsigned* work, int& s_item) {
+// Next work item of the CTA from the context's counter, broadcast through
+// shared memory; the barrier in front also ends every read of the previous
+// item's shared buffers. Every CTA stops at its first fetch past the last item,
+// so the launch makes exactly items + gridDim.x fetches; the one that returns
+// the largest value is the launch's last and puts the counter back to 0 for
+// the next launch.
+__device__ __forceinline__ int next_item(unsigned* work, int items, int& s_item) {
   __syncthreads();
-  if (threadIdx.x == 0) s_item = (int)atomicAdd(work, 1u);
+  if (threadIdx.x == 0) {
+    const unsigned v = atomicAdd(work, 1u);
+    if (v == (unsigned)items + gridDim.x - 1u) atomicExch(work, 0u);
+    s_item = (int)v;
+  }
   __syncthreads();
   return s_item;
 }
@@ -561,7 +568,7 @@ __global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict
   const int h1_row = tid / G::H1_RUNS, h1_col = (tid % G::H1_RUNS) * G::RUN;
   const int h2_row = tid / G::H2_RUNS, h2_col = (tid % G::H2_RUNS) * G::RUN;
   __shared__ int s_item;
-  for (int item = next_item(work, s_item); item < items; item = next_item(work, s_item)) {
+  for (int item = next_item(work, items, s_item); item < items; item = next_item(work, items, s_item)) {
     int strip, seg;
     strip_item(item, strips, sg.segs, strip, seg);
     const int x0 = strip * SW;
@@ -773,7 +780,6 @@ Status launch_rl_step_t(Context& ctx, const float* est, const float* guide, floa
   const int items = strips * sg.segs;
   const int grid = std::min(items, slots);
   CUtensorMap none{};
-  RD_CUDA_TRY(cudaMemsetAsync(ctx.d_work, 0, sizeof(uint32_t), ctx.stream));
   RD_LAUNCH(ctx, K_RL_ITER, rl_step_kernel<R, TMA><<<grid, 128, smem, ctx.stream>>>(
                                 est, guide, out, W, H, strips, sg, items, taps, est_map ? *est_map : none,
                                 guide_map ? *guide_map : none, ctx.d_work, ctx.d_error));
@@ -971,7 +977,7 @@ __global__ void __launch_bounds__(128, 4) rl_prep_step_kernel(const float* __res
   const bool h_on = tid < G::H_RUNS * BH;
   const int h_row = tid / G::H_RUNS, h_col = (tid % G::H_RUNS) * G::RUN;
   __shared__ int s_item;
-  for (int item = next_item(work, s_item); item < items; item = next_item(work, s_item)) {
+  for (int item = next_item(work, items, s_item); item < items; item = next_item(work, items, s_item)) {
     int strip, seg;
     strip_item(item, strips, segs, strip, seg);
     const int x0 = strip * SW;
@@ -1139,7 +1145,6 @@ Status launch_rl_prep_step(Context& ctx, const Taps& taps, const float* rgb, lon
   const int items = strips * segs;
   const int grid = std::min(items, slots);
   CUtensorMap none{};
-  RD_CUDA_TRY(cudaMemsetAsync(ctx.d_work, 0, sizeof(uint32_t), ctx.stream));
   RD_LAUNCH(ctx, K_RL_MASK, rl_prep_step_kernel<R, TMA><<<grid, 128, smem, ctx.stream>>>(
                                 rgb, plane, ceil[0], ceil[1], ceil[2], noise, guide, mask, W, H, strips, segs, items,
                                 taps, rgb_map ? *rgb_map : none, ctx.d_work, ctx.d_error));

@@ -56,7 +56,9 @@ struct Context {
   std::string last_error;
   // Error word written by kernels (bounds/footprint/non-finite), read after a stage.
   uint32_t* d_error = nullptr;
-  uint32_t* d_work = nullptr;  // work-item counter of the dynamically scheduled kernels (beside d_error)
+  // Work-item counter of the dynamically scheduled kernels (beside d_error):
+  // zero between launches, put back to zero by each launch's last fetch.
+  uint32_t* d_work = nullptr;
   // AMaZE per-CTA scratch slots (kept across calls).
   float* amaze_scratch = nullptr;
   size_t amaze_slots = 0;  // tiles the AMaZE scratch holds slabs and flags for
