@@ -134,8 +134,8 @@ class ClockSampler:
 # (dram__bytes_read.sum + dram__bytes_write.sum); the traffic grows with the pixel count, so the
 # bench workload's traffic is this figure times its pixels.
 MEASURED_TRAFFIC_BPP = {
-    "amaze": (26.8, "profiles/amaze_kernel_4096x3072.md"),
-    "rl_iteration": (10.4, "profiles/rl_step_kernel_4096x3072.md"),
+    "amaze": (34.1, "profiles/amaze_kernel_4096x3072.md"),
+    "rl_iteration": (10.3, "profiles/rl_step_kernel_4096x3072.md"),
     "rl_mask": (17.1, "profiles/rl_prep_step_kernel_4096x3072.md"),
     "optics_gather": (24.8, "profiles/optics_kernel_4096x3072.md"),
     "area_reduce": (15.0, "profiles/area_kernel_4096x3072.md"),
