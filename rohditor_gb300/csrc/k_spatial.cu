@@ -361,12 +361,13 @@ __global__ void __launch_bounds__(128) area_kernel(const float* __restrict__ in,
   const float* vw = vweights + voffset[t];
   float acc = 0.0f;
   const int r_end = vfirst[t1 - 1] + vcount[t1 - 1];
-  for (int r = first; r < r_end; ++r) {
-    const float mid = area_row<VIG>(plane + (long long)r * W, VIG ? mplane + (long long)r * W : nullptr, hw, hn);
+  // Adds one input row's horizontal sum to the vertical sum(s) it belongs to;
+  // false once the tile's last output row is written.
+  auto take = [&](int r, float mid) {
     acc += mid * __ldg(vw + (r - first));
     if (r == end - 1) {
       o[(long long)t * tw] = acc;
-      if (++t == t1) break;
+      if (++t == t1) return false;
       const int nf = vfirst[t];
       vw = vweights + voffset[t];
       // The next output row starts at or before this input row (they share
@@ -376,7 +377,47 @@ __global__ void __launch_bounds__(128) area_kernel(const float* __restrict__ in,
       first = nf;
       end = nf + vcount[t];
     }
+    return true;
+  };
+  if (hn <= 4) {
+    // Up to four taps per row (reductions up to 3x): the samples of four rows
+    // are loaded together before any of their sums, so their latencies
+    // overlap; each sum still adds its taps in order from 0.
+    float w[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) w[j] = j < hn ? __ldg(hw + j) : 0.0f;
+    for (int r0 = first; r0 < r_end; r0 += 4) {
+      float smp[4][4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float* row = plane + (long long)(r0 + q) * W;
+        const float* mrow = VIG ? mplane + (long long)(r0 + q) * W : nullptr;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          float v = 0.0f;
+          if (r0 + q < r_end && j < hn) {
+            v = __ldg(row + j);
+            if (VIG) v = v * __ldg(mrow + j);
+          }
+          smp[q][j] = v;
+        }
+      }
+      bool more = true;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (!more || r0 + q >= r_end) break;
+        float mid = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          if (j < hn) mid += smp[q][j] * w[j];
+        more = take(r0 + q, mid);
+      }
+      if (!more) break;
+    }
+    return;
   }
+  for (int r = first; r < r_end; ++r)
+    if (!take(r, area_row<VIG>(plane + (long long)r * W, VIG ? mplane + (long long)r * W : nullptr, hw, hn))) break;
 }
 
 struct AxisTable {
