@@ -354,8 +354,9 @@ __global__ void __launch_bounds__(256) rcd_kernel(const MosaicSource src, float 
 
 // Normalize (+ Clip) into an f32 mosaic: the input of Opposed and of the
 // stage entry point. Each sample is visited once, so Clip statistics are exact.
-// Four consecutive samples of a row per thread (one 16-byte store when aligned).
-constexpr int NPX = 4;
+// Eight consecutive samples of a row per thread, loaded together (their
+// latencies overlap), stored as two 16-byte stores when aligned.
+constexpr int NPX = 8;
 
 __global__ void __launch_bounds__(256) normalize_kernel(const MosaicSource src, float* out, int count_clip,
                                                         unsigned long long* clip_stats) {
@@ -368,7 +369,8 @@ __global__ void __launch_bounds__(256) normalize_kernel(const MosaicSource src, 
     for (int j = 0; j < NPX; ++j) v[j] = j < n ? source_linear(src, x0 + j, y) : 0.0f;
     float* o = out + (long long)y * src.width + x0;
     if (n == NPX && (reinterpret_cast<uintptr_t>(o) & 15) == 0) {
-      *reinterpret_cast<float4*>(o) = make_float4(v[0], v[1], v[2], v[3]);
+      reinterpret_cast<float4*>(o)[0] = make_float4(v[0], v[1], v[2], v[3]);
+      reinterpret_cast<float4*>(o)[1] = make_float4(v[4], v[5], v[6], v[7]);
     } else {
       for (int j = 0; j < n; ++j) o[j] = v[j];
     }
