@@ -259,8 +259,6 @@ def run_ours(args, world, rank, local, pg):
     for _ in range(args.warmup):
         step_device()
     dev.synchronize()
-    lib.rd_ctx_reset_kernel_timing(h)
-    lib.rd_ctx_enable_kernel_timing(h, 1)
     launches0 = dev.kernel_launches
     barrier(pg)
     dev.synchronize()
@@ -268,9 +266,16 @@ def run_ours(args, world, rank, local, pg):
     total_ms, per = timed(step_device, args.steps)
     dev.synchronize()
     launches = dev.kernel_launches - launches0
-    lib.rd_ctx_enable_kernel_timing(h, 0)
     barrier(pg)
     total_ms = max_over_ranks(pg, total_ms)
+    # Per-kernel device times from extra steps with every launch bracketed by
+    # events (outside the timed region: the events add work between launches).
+    lib.rd_ctx_reset_kernel_timing(h)
+    lib.rd_ctx_enable_kernel_timing(h, 1)
+    timing_steps = min(args.steps, 10)
+    timed(step_device, timing_steps)
+    dev.synchronize()
+    lib.rd_ctx_enable_kernel_timing(h, 0)
     families = {}
     for f in range(KERNEL_FAMILIES):
         name = ctypes.c_char_p()
@@ -309,7 +314,7 @@ def run_ours(args, world, rank, local, pg):
             entry["algorithmic_gbs"] = round(gbs, 1)
             entry["hbm_frac"] = round(gbs / hbm_peak, 3)
         kernels[name] = entry
-    step_kernel_ms = sum(r["ms"] for r in families.values()) / args.steps
+    step_kernel_ms = sum(r["ms"] for r in families.values()) / timing_steps
     # The dominant kernel is the family with the most device time in the timed region.
     dominant = max(families.items(), key=lambda kv: kv[1]["ms"])[0] if families else None
     roofline = None
