@@ -384,6 +384,10 @@ __device__ __forceinline__ void warp_or(unsigned* word, unsigned key, unsigned b
   if (peers.thread_rank() == 0 && v) atomicOr(&word[key], v);
 }
 
+// Final compact label of each cell, the per-region clipped channels, and
+// 5. the wanted (channel, support) slots per region
+// (region_correction.rs:134-178), in one pass: both need only the cell's own
+// label.
 __global__ void relabel_kernel(const OpposedParams p) {
   if (p.counters[0] == 0) return;
   const int cx = blockIdx.x * blockDim.x + threadIdx.x, cy = blockIdx.y;
@@ -396,19 +400,9 @@ __global__ void relabel_kernel(const OpposedParams p) {
     label = 0;
   }
   p.labels[i] = label;
-  const unsigned clipped = __float_as_uint(p.cells[i].w) >> 3;
-  if (label && clipped) warp_or(p.region_clipped, label, clipped);
-}
-
-// 5. wanted (channel, support) slots per region (region_correction.rs:134-178)
-__global__ void wanted_kernel(const OpposedParams p) {
-  if (p.counters[0] == 0) return;
-  const int cx = blockIdx.x * blockDim.x + threadIdx.x, cy = blockIdx.y;
-  if (cx >= p.cw) return;
-  const long long i = (long long)cy * p.cw + cx;
-  const unsigned label = p.labels[i];
   const Cell c = load_cell(p, cx, cy);
   const unsigned clipped = c.flags >> 3;
+  if (label && clipped) warp_or(p.region_clipped, label, clipped);
   if (label == 0 || clipped == 0) return;
   unsigned bits = 0;
   for (int ch = 0; ch < 3; ++ch) {
@@ -765,7 +759,6 @@ Status run_opposed_labels(Context& ctx, float* mosaic, int W, int H, int cfa, co
   RD_LAUNCH(ctx, K_OPPOSED, scan_blocks_kernel<<<1, 1024, 0, ctx.stream>>>(p, scan_blocks));
   RD_LAUNCH(ctx, K_OPPOSED, root_ids_kernel<<<scan_blocks, SCAN_BLOCK, 0, ctx.stream>>>(p));
   RD_LAUNCH(ctx, K_OPPOSED, relabel_kernel<<<cgrid, 128, 0, ctx.stream>>>(p));
-  RD_LAUNCH(ctx, K_OPPOSED, wanted_kernel<<<cgrid, 128, 0, ctx.stream>>>(p));
   RD_LAUNCH(ctx, K_OPPOSED, border_kernel<<<cgrid, 128, 0, ctx.stream>>>(p, 0));
   RD_LAUNCH(ctx, K_OPPOSED, finish_moments_kernel<<<256, 256, 0, ctx.stream>>>(p));
   RD_LAUNCH(ctx, K_OPPOSED, border_kernel<<<cgrid, 128, 0, ctx.stream>>>(p, 1));
