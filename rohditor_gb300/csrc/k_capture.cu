@@ -1046,15 +1046,18 @@ __global__ void __launch_bounds__(128, 4) rl_prep_step_kernel(const float* __res
         for (int j = 0; j < BH; ++j) {
           const float r = pr[j * G::CWP], g = pr[(BH + j) * G::CWP], b = pr[(2 * BH + j) * G::CWP];
           if (!isfinite(r) || !isfinite(g) || !isfinite(b)) bad = true;
+          // fmaxf returns the non-NaN operand, as rmax does; the two can only
+          // differ in the sign of a zero, which neither the guide (floored
+          // at 1e-6) nor the smoothstep of the peak can see.
           float s = -0.0f;
-          s += rmax(r, 0.0f) / 3.0f;
-          s += rmax(g, 0.0f) / 3.0f;
-          s += rmax(b, 0.0f) / 3.0f;
+          s += fmaxf(r, 0.0f) / 3.0f;
+          s += fmaxf(g, 0.0f) / 3.0f;
+          s += fmaxf(b, 0.0f) / 3.0f;
           float peak = 0.0f;
-          peak = rmax(peak, r / c0);
-          peak = rmax(peak, g / c1);
-          peak = rmax(peak, b / c2);
-          gcur[j] = rmax(s, FLOOR);
+          peak = fmaxf(peak, r / c0);
+          peak = fmaxf(peak, g / c1);
+          peak = fmaxf(peak, b / c2);
+          gcur[j] = fmaxf(s, FLOOR);
           mcur[j] = 1.0f - smoothstep(0.85f, 0.98f, peak);
           S.g[j][tid] = gcur[j];
           S.m[j][tid] = mcur[j];
@@ -1100,7 +1103,7 @@ __global__ void __launch_bounds__(128, 4) rl_prep_step_kernel(const float* __res
             const float m0 = j < R ? cm[j] : mcur[j - R];
             const float g = j < R ? cg[j] : gcur[j - R];
             const float b2 = bm * bm;
-            float m = rmin(m0, b2 * b2);
+            float m = fminf(m0, b2 * b2);  // m0 >= +0, never NaN: as rmin
             const float threshold = 0.0005f + noise * 0.008f + bg * noise * 0.02f;
             const float detail = fabsf(g - bg);
             m *= smoothstep(threshold, threshold * 3.0f, detail) * smoothstep(0.001f, 0.01f, g);
