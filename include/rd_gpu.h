@@ -450,7 +450,7 @@ rd_status rd_ctx_flush_l2(rd_ctx* ctx);
  * bracketed by CUDA events; totals are resolved at each call's final sync. */
 rd_status rd_ctx_enable_kernel_timing(rd_ctx* ctx, int enable);
 /* family: index 0..RD_KERNEL_FAMILIES-1; returns its name, total ms and launch count. */
-#define RD_KERNEL_FAMILIES 16
+#define RD_KERNEL_FAMILIES 15
 rd_status rd_ctx_kernel_timing(const rd_ctx* ctx, int family, const char** name, double* total_ms,
                                uint64_t* launches);
 rd_status rd_ctx_reset_kernel_timing(rd_ctx* ctx);

@@ -50,7 +50,7 @@ void device_free(Context& ctx, void* ptr, size_t bytes) {
 
 const char* kernel_family_name(int family) {
   static const char* names[K_FAMILY_COUNT] = {
-      "normalize", "opposed", "mhc_bilinear", "rcd", "amaze", "rl_init", "rl_mask", "rl_iteration",
+      "normalize", "opposed", "mhc_bilinear", "rcd", "amaze", "rl_mask", "rl_iteration",
       "rl_apply", "vignetting", "optics_gather", "area_reduce", "wb_matrix",
       "color_output", "synth", "display_output"};
   return family >= 0 && family < K_FAMILY_COUNT ? names[family] : "unknown";

@@ -41,7 +41,7 @@ struct Status {
 // ------------------------------------------------------------------ context
 // Kernel families timed by the optional per-launch event bracketing.
 enum KernelFamily {
-  K_NORMALIZE, K_OPPOSED, K_MHC, K_RCD, K_AMAZE, K_RL_INIT, K_RL_MASK, K_RL_ITER, K_RL_APPLY, K_VIGNETTE,
+  K_NORMALIZE, K_OPPOSED, K_MHC, K_RCD, K_AMAZE, K_RL_MASK, K_RL_ITER, K_RL_APPLY, K_VIGNETTE,
   K_OPTICS, K_AREA, K_WB_MATRIX, K_COLOR, K_SYNTH, K_OUTPUT, K_FAMILY_COUNT
 };
 static_assert(K_FAMILY_COUNT == RD_KERNEL_FAMILIES, "family table size");
