@@ -269,7 +269,11 @@ rd_status rd_render_output_device(rd_ctx* ctx, const rd_base* base, const rd_col
  * quantisation computes it) differs from the correctly rounded one, expected 0.
  * which = 3: the number of (f32 in that domain, 8- or 16-bit, three dither
  * offsets) whose quantised code differs from the code of the correctly
- * rounded power, expected 0. */
+ * rounded power, expected 0. which = 4: the number of sampled f32 pairs (x
+ * over every f32 in [2^-12, 2), y hashed with 2^-18 <= |y| < 2, and y = 0)
+ * whose hypot in the optics remap differs from f32::hypot as glibc computes
+ * it (the double square root of the double sum of squares, narrowed once),
+ * expected 0. */
 rd_status rd_check_math(rd_ctx* ctx, int32_t which, uint64_t* result);
 /* Launch shape of the capture-sharpening iteration chosen for one image shape
  * (no reference counterpart). The first develop of a (width, height, kernel

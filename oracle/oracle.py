@@ -109,6 +109,9 @@ def load():
                                               ctypes.c_float, ctypes.c_float]),
             "ro_optics_apply": (ctypes.c_int, [ctypes.POINTER(OpticsDesc), F32P, F32P]),
             "ro_optics_map": (ctypes.c_int, [ctypes.POINTER(OpticsDesc), ctypes.c_int, ctypes.c_int, F32P]),
+            "ro_optics_radial": (ctypes.c_int, [ctypes.POINTER(OpticsDesc), F32P, F32P, ctypes.POINTER(ctypes.c_int),
+                                                F32P, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+            "ro_optics_map_lut": (ctypes.c_int, [ctypes.POINTER(OpticsDesc), ctypes.c_int, ctypes.c_int, F32P]),
             "ro_area_reduce": (ctypes.c_int, [F32P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, F32P]),
             "ro_white_balance": (None, [F32P, ctypes.c_size_t, F32P]),
             "ro_camera_matrix": (None, [F32P, ctypes.c_size_t, F32P]),
@@ -343,6 +346,30 @@ def optics_plan(width, height, distortion_model, distortion, tca_model, tca_red,
     if load().ro_optics_plan(ctypes.byref(d), crop, focal, center[0], center[1]) != 0:
         raise ValueError("no safe scale")
     return d
+
+
+RADIAL_GUARDS = {-1: "no table", 0: "accepted", 1: "non-finite", 2: "tripwire", 3: "break collision",
+                 4: "freeze ambiguity", 5: "unexplained jump"}
+
+
+def optics_radial(desc: OpticsDesc):
+    """RadialMultipliers::build: (guard name, step, table [1024, 3], pinned segments [(index, radius)])."""
+    table = np.zeros((1024, 3), dtype=np.float32)
+    step = np.zeros(1, dtype=np.float32)
+    idx = (ctypes.c_int * 64)()
+    rad = np.zeros(64, dtype=np.float32)
+    n = ctypes.c_int(0)
+    g = load().ro_optics_radial(ctypes.byref(desc), ptr(table), ptr(step), idx, ptr(rad), 64, ctypes.byref(n))
+    segs = [(idx[i], float(rad[i])) for i in range(min(n.value, 64))]
+    return RADIAL_GUARDS[g], float(step[0]), table, segs
+
+
+def optics_map_lut(desc: OpticsDesc, x: int, y: int) -> np.ndarray:
+    """The table branch's six source coordinates at output pixel (x, y)."""
+    out = np.zeros(6, dtype=np.float32)
+    if load().ro_optics_map_lut(ctypes.byref(desc), x, y, ptr(out)) != 0:
+        raise ValueError("no radial table")
+    return out
 
 
 def optics_apply(desc: OpticsDesc, rgb: np.ndarray) -> np.ndarray:

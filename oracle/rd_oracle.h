@@ -76,6 +76,13 @@ int ro_optics_plan(ro_optics* plan, float crop_factor, float real_focal, float l
                    float lens_center_y);
 int ro_optics_apply(const ro_optics* plan, const float* rgb_in, float* rgb_out);
 int ro_optics_map(const ro_optics* plan, int x, int y, float coords[6]);
+/* RadialMultipliers::build: -1 no table, 0 accepted, 1 non-finite, 2 tripwire,
+ * 3 break collision, 4 freeze ambiguity, 5 unexplained jump. table gets
+ * 1024 x 3 multipliers, the pinned segments up to max_segments. */
+int ro_optics_radial(const ro_optics* plan, float* table, float* step, int* seg_index, float* seg_radius,
+                     int max_segments, int* n_segments);
+/* The table branch's source coordinates (whatever the guard says). */
+int ro_optics_map_lut(const ro_optics* plan, int x, int y, float coords[6]);
 
 /* ---- area reduction (spatial.cpp) ---- */
 int ro_area_reduce(const float* rgb, int w, int h, int tw, int th, float* out);

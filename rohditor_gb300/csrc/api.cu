@@ -868,8 +868,9 @@ rd_status rd_render_output(rd_ctx* h, const rd_base* base, const rd_color_desc* 
 }
 
 rd_status rd_check_math(rd_ctx* h, int32_t which, uint64_t* result) {
-  if (!h || !result || which < 0 || which > 3) return finish(h, Status{RD_INVALID_INPUT, "bad argument"});
+  if (!h || !result || which < 0 || which > 4) return finish(h, Status{RD_INVALID_INPUT, "bad argument"});
   cudaSetDevice(h->c.device);
+  if (which == 4) return finish(h, rd::run_hypot_check(h->c, result));
   return finish(h, rd::run_math_check(h->c, which, result));
 }
 

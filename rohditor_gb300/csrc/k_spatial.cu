@@ -21,12 +21,11 @@
 #include <cstring>
 #include <vector>
 
+#include "lens_model.cuh"
 #include "rd_internal.cuh"
 
 namespace rd {
 namespace {
-
-constexpr double NEWTON_EPS = 0.00001;
 
 struct FastOptics {
   float cxh, cxl, cyh, cyl, uh, ul;  // f64 constants split into FP32 pairs
@@ -49,62 +48,11 @@ struct OpticsParams {
 };
 
 __device__ __forceinline__ void undistort(const OpticsParams& p, float x, float y, float& ox, float& oy) {
-  ox = x;
-  oy = y;
-  if (p.dist_model == 0) return;
-  const double rd = sqrt((double)(x * x + y * y));
-  if (rd == 0.0) return;
-  const double a = p.d0, b = p.d1, c = p.d2;
-  double ru = rd;
-  bool converged = false;
-  if (p.dist_model == RD_DISTORTION_POLY3) {
-    const double inv_k1 = (double)(1.0f / p.d0);
-    const double rd_div_k1 = (double)(float)(rd * inv_k1);
-    for (int s = 0; s < 7; ++s) {
-      const double f = ru * ru * ru + ru * inv_k1 - rd_div_k1;
-      if (fabs(f) < NEWTON_EPS) { converged = true; break; }
-      ru -= f / (3.0 * ru * ru + inv_k1);
-    }
-    if (!converged || ru < 0.0) { ox = nanf(""); oy = nanf(""); return; }
-  } else if (p.dist_model == RD_DISTORTION_POLY5) {
-    for (int s = 0; s < 7; ++s) {
-      const double ru2 = ru * ru;
-      const double f = ru * (1.0 + a * ru2 + b * ru2 * ru2) - rd;
-      if (fabs(f) < NEWTON_EPS) { converged = true; break; }
-      ru -= f / (1.0 + 3.0 * a * ru2 + 5.0 * b * ru2 * ru2);
-    }
-    if (!converged || ru < 0.0) return;
-  } else {
-    for (int s = 0; s < 7; ++s) {
-      const double f = ru * (a * ru * ru * ru + b * ru * ru + c * ru + 1.0) - rd;
-      if (fabs(f) < NEWTON_EPS) { converged = true; break; }
-      ru -= f / (4.0 * a * ru * ru * ru + 3.0 * b * ru * ru + 2.0 * c * ru + 1.0);
-    }
-    if (!converged || ru < 0.0) return;
-  }
-  const double ratio = ru / rd;
-  ox = (float)((double)x * ratio);
-  oy = (float)((double)y * ratio);
+  lens_undistort(p.dist_model, p.d0, p.d1, p.d2, x, y, ox, oy);
 }
 
 __device__ __forceinline__ void tca_poly3(const float* ch, float x, float y, float& ox, float& oy) {
-  ox = x;
-  oy = y;
-  const double rd = sqrt((double)(x * x + y * y));
-  if (rd == 0.0) return;
-  const double v = ch[0], c = ch[1], b = ch[2];
-  double ru = rd;
-  bool converged = false;
-  for (int s = 0; s < 7; ++s) {
-    const double ru2 = ru * ru;
-    const double f = b * ru2 * ru + c * ru2 + v * ru - rd;
-    if (fabs(f) < NEWTON_EPS) { converged = true; break; }
-    ru -= f / (3.0 * b * ru2 + 2.0 * c * ru + v);
-  }
-  if (!converged || ru <= 0.0) return;
-  const double ratio = ru / rd;
-  ox = (float)((double)x * ratio);
-  oy = (float)((double)y * ratio);
+  lens_tca_poly3(ch, x, y, ox, oy);
 }
 
 // ---- exact FP32 fast path -------------------------------------------------
@@ -316,6 +264,87 @@ __global__ void __launch_bounds__(256) optics_kernel(const OpticsParams p) {
   if (bad) atomicOr(p.error, 8u);
 }
 
+// f32 hypot as the reference gets it (f32::hypot, glibc hypotf): the double
+// sum of the two exact double squares, its double square root, narrowed once.
+// Here the square root is taken in double-float from the exact FP32-pair sum
+// of squares (one Newton correction of sqrtf); the rare result too close to
+// an f32 rounding boundary (or zero, tiny, huge) is recomputed in f64.
+__device__ __forceinline__ float hypot_f32(float x, float y) {
+  const df s = df_add(two_prod(x, x), two_prod(y, y));
+  const float r0 = sqrtf(s.h);
+  const df r2 = two_prod(r0, r0);
+  const float residual = ((s.h - r2.h) - r2.l) + s.l;  // s.h - r2.h is exact
+  bool amb = false;
+  const float r = df_round(fast_two_sum(r0, __fdividef(residual, 2.0f * r0)), amb);
+  if (!amb) return r;
+  return (float)sqrt((double)x * (double)x + (double)y * (double)y);
+}
+
+// Self-check of hypot_f32: x runs over every f32 in [first, last), y is a
+// hashed f32 of either sign with |y| < 2; counts results that differ from the
+// double computation.
+__global__ void hypot_check_kernel(unsigned first, unsigned last, unsigned long long* mismatches) {
+  unsigned long long bad = 0;
+  for (unsigned b = first + blockIdx.x * blockDim.x + threadIdx.x; b < last; b += gridDim.x * blockDim.x) {
+    unsigned h = b * 2654435761u;
+    h ^= h >> 15;
+    h *= 2246822519u;
+    h ^= h >> 13;
+    const float x = __uint_as_float(b);
+    const float y = __uint_as_float((h & 0x807fffffu) | ((109u + (h >> 23) % 19u) << 23));  // 2^-18 <= |y| < 2
+    const float want = (float)sqrt((double)x * (double)x + (double)y * (double)y);
+    if (__float_as_uint(hypot_f32(x, y)) != __float_as_uint(want)) ++bad;
+    if (__float_as_uint(hypot_f32(x, 0.0f)) != __float_as_uint(x)) ++bad;
+  }
+  if (bad) atomicAdd(mismatches, bad);
+}
+
+// The radial-table branch of the remap (correction.rs:122-151): the three
+// channel multipliers come from one lookup at the pixel's input radius
+// (RadialMultipliers::lookup, radial.rs:212-229: nearest knot on the pixel's
+// side of a pinned freeze boundary, else the linear blend of the two knots),
+// then plan.rs:136-141's post-transform and the Catmull-Rom gather per
+// channel. `knots` holds [m_r, m_g, m_b, pin] per knot; it is 16 KB and stays
+// in L1.
+template <bool VIG>
+__global__ void __launch_bounds__(256) optics_lut_kernel(const OpticsParams p, const float4* __restrict__ knots,
+                                                         float step) {
+  const int x = blockIdx.x * 32 + (threadIdx.x & 31);
+  const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
+  if (x >= p.W || y >= p.H) return;
+  const float ix = p.ix[x], iy = p.iy[y];
+  const float radius = hypot_f32(ix, iy);
+  const float position = radius / step;
+  const int index = position < (float)(RADIAL_KNOTS - 2) ? (int)position : RADIAL_KNOTS - 2;
+  const float4 lo = __ldg(knots + index), hi = __ldg(knots + index + 1);
+  float m[3];
+  if (lo.w == lo.w) {  // pinned segment
+    const float4 k = radius >= lo.w ? hi : lo;
+    m[0] = k.x;
+    m[1] = k.y;
+    m[2] = k.z;
+  } else {
+    float blend = position - (float)index;
+    if (blend > 1.0f) blend = 1.0f;
+    m[0] = lo.x * (1.0f - blend) + hi.x * blend;
+    m[1] = lo.y * (1.0f - blend) + hi.y * blend;
+    m[2] = lo.z * (1.0f - blend) + hi.z * blend;
+  }
+  const long long plane = (long long)p.W * p.H;
+  const long long o = (long long)y * p.W + x;
+  bool bad = false;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    bool fell_back = false;
+    const float sx = post_transform(ix * m[c], p.fast.cxh, p.fast.cxl, p.fast, p.cx, p.unscale, fell_back);
+    const float sy = post_transform(iy * m[c], p.fast.cyh, p.fast.cyl, p.fast, p.cy, p.unscale, fell_back);
+    float v = 0.0f;
+    if (!bad && !cubic_sample<VIG>(p.in + c * plane, p.mult, p.W, p.H, sx, sy, v)) bad = true;
+    p.out[c * plane + o] = v;
+  }
+  if (bad) atomicOr(p.error, 8u);
+}
+
 // Horizontal area pass: one thread per (row, target column, channel-plane).
 template <bool VIG>
 __device__ __forceinline__ float area_row(const float* __restrict__ row, const float* __restrict__ mrow,
@@ -460,10 +489,18 @@ Status run_optics_gather(Context& ctx, const rd_optics_desc& o, const float* rgb
     const double mapped = cpy + ((double)y - cpy) / (double)o.scale;
     tab[W + y] = (float)(mapped * o.norm_scale - o.center_y);
   }
+  // The remap's branch is decided once per apply (correction.rs:110-121).
+  const RadialTable radial = build_radial_table(o, tab.data(), tab.data() + W);
+  const bool lut = radial.guard == RD_RADIAL_ACCEPTED;
+  std::vector<float> staged = lut ? radial.knots : std::vector<float>();
+  const size_t knot_floats = staged.size();  // a multiple of 4: the coordinate tables stay 16-byte aligned
+  staged.insert(staged.end(), tab.begin(), tab.end());
+  const size_t bytes = sizeof(float) * staged.size();
   void* d = nullptr;
-  RD_TRY(device_alloc(ctx, sizeof(float) * tab.size(), &d));
-  float* dtab = static_cast<float*>(d);
-  RD_TRY(upload(ctx, dtab, tab.data(), sizeof(float) * tab.size()));
+  RD_TRY(device_alloc(ctx, bytes, &d));
+  float* dbuf = static_cast<float*>(d);
+  RD_TRY(upload(ctx, dbuf, staged.data(), bytes));
+  const float* dtab = dbuf + knot_floats;
   OpticsParams p{};
   p.in = rgb_in;
   p.mult = mult;
@@ -493,17 +530,43 @@ Status run_optics_gather(Context& ctx, const rd_optics_desc& o, const float* rgb
   split(o.center_y, p.fast.cyh, p.fast.cyl);
   split(o.norm_unscale, p.fast.uh, p.fast.ul);
   dim3 grid((W + 31) / 32, (H + 7) / 8);
-  if (p.mult) {
+  const float4* knots = reinterpret_cast<const float4*>(dbuf);
+  if (lut && p.mult) {
+    RD_LAUNCH(ctx, K_OPTICS, optics_lut_kernel<true><<<grid, 256, 0, ctx.stream>>>(p, knots, radial.step));
+  } else if (lut) {
+    RD_LAUNCH(ctx, K_OPTICS, optics_lut_kernel<false><<<grid, 256, 0, ctx.stream>>>(p, knots, radial.step));
+  } else if (p.mult) {
     RD_LAUNCH(ctx, K_OPTICS, optics_kernel<true><<<grid, 256, 0, ctx.stream>>>(p));
   } else {
     RD_LAUNCH(ctx, K_OPTICS, optics_kernel<false><<<grid, 256, 0, ctx.stream>>>(p));
   }
   const cudaError_t launch = cudaGetLastError();
-  device_free(ctx, dtab, sizeof(float) * tab.size());
+  device_free(ctx, dbuf, bytes);
   if (launch != cudaSuccess) return Status{RD_SYNCHRONIZATION, cudaGetErrorString(launch)};
   return Status{};
 }
 
+
+Status run_hypot_check(Context& ctx, uint64_t* result) {
+  void* p = nullptr;
+  RD_TRY(device_alloc(ctx, 16, &p));
+  RD_CUDA_TRY(cudaMemsetAsync(p, 0, 16, ctx.stream));
+  const float lo = 0x1p-12f, hi = 2.0f;
+  unsigned first = 0, last = 0;
+  std::memcpy(&first, &lo, 4);
+  std::memcpy(&last, &hi, 4);
+  const int grid = (ctx.sm_count > 0 ? ctx.sm_count : 152) * 8;
+  RD_LAUNCH(ctx, K_OPTICS, (hypot_check_kernel<<<grid, 256, 0, ctx.stream>>>(
+                               first, last, static_cast<unsigned long long*>(p))));
+  Status st;
+  uint64_t v = 0;
+  if (cudaGetLastError() != cudaSuccess || cudaMemcpyAsync(&v, p, 8, cudaMemcpyDeviceToHost, ctx.stream) != cudaSuccess ||
+      cudaStreamSynchronize(ctx.stream) != cudaSuccess)
+    st = Status{RD_SYNCHRONIZATION, "hypot check failed"};
+  device_free(ctx, p, 16);
+  if (st.ok()) *result = v;
+  return st;
+}
 
 Status run_area_reduce(Context& ctx, const float* rgb, const float* mult, int W, int H, int tw, int th, float* out) {
   const AxisTable ha = build_axis(W, tw), va = build_axis(H, th);

@@ -211,6 +211,27 @@ Status run_demosaic(Context& ctx, const MosaicSource& src, int algorithm, float*
 Status run_capture(Context& ctx, float* rgb, int width, int height, const rd_detail_desc& detail);
 // Vignetting multiplier plane (width*height f32) of an optics execution.
 Status run_vignette_plane(Context& ctx, const rd_optics_desc& optics, float* mult);
+// Radial multiplier table of one optics execution (RadialMultipliers,
+// crates/optics/src/radial.rs:157-229): RADIAL_KNOTS knots of
+// [m_red, m_green, m_blue, pin] at radii i * step, where pin is the break
+// radius of a freeze boundary pinned inside segment [i, i + 1], or NaN.
+constexpr int RADIAL_KNOTS = 1024;
+enum {
+  RD_RADIAL_NONE = -1,  // no radial work: the remap needs no table
+  RD_RADIAL_ACCEPTED = 0,
+  RD_RADIAL_NON_FINITE = 1,
+  RD_RADIAL_TRIPWIRE = 2,
+  RD_RADIAL_BREAK_COLLISION = 3,
+  RD_RADIAL_FREEZE_AMBIGUITY = 4,
+  RD_RADIAL_UNEXPLAINED_JUMP = 5,
+};
+struct RadialTable {
+  int guard = RD_RADIAL_NONE;
+  float step = 0.0f;
+  std::vector<float> knots;  // 4 per knot
+};
+// `input_x` / `input_y`: the per-column and per-row input (lens) coordinates.
+RadialTable build_radial_table(const rd_optics_desc& optics, const float* input_x, const float* input_y);
 // Distortion / TCA gather; `mult` (optional) is the vignetting plane applied to
 // each source sample as it is read.
 Status run_optics_gather(Context& ctx, const rd_optics_desc& optics, const float* rgb_in, const float* mult,
@@ -253,6 +274,8 @@ Status run_display_output(Context& ctx, const float* rgb, const rd_color_desc& c
                           unsigned long long* d_gamut);
 // Exhaustive device checks of the correctly rounded arithmetic (rd_check_math).
 Status run_math_check(Context& ctx, int which, uint64_t* result);
+// Sampled device check of the optics branch's f32 hypot (rd_check_math 4).
+Status run_hypot_check(Context& ctx, uint64_t* result);
 
 Status reserve_amaze_scratch(Context& ctx, size_t tiles);
 // AMaZE tiles of a width x height mosaic (224-pixel cores).

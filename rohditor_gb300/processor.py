@@ -589,7 +589,8 @@ class Stages:
         return out, hist, gamut
 
     def check_math(self, which: int) -> int:
-        """rd_check_math: 0 -> cube roots not correctly rounded; 1 -> largest powf distance in ulps."""
+        """rd_check_math: 0 -> cube roots not correctly rounded; 1 -> largest powf distance in ulps;
+        2, 3 -> transfer powers / quantised codes off the correctly rounded ones; 4 -> optics hypot mismatches."""
         v = ctypes.c_uint64()
         self.device.check(self.lib.rd_check_math(self.device.handle, which, ctypes.byref(v)))
         return v.value

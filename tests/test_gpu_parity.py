@@ -227,6 +227,49 @@ def test_optics(stages, oracle, size):
     assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32))
 
 
+RADIAL_CASES = {
+    "poly5_linear_tca": dict(distortion="poly5", distortion_k=(-0.02, 0.005, 0.0), tca="linear",
+                             tca_red=(1.0003, 0, 0), tca_blue=(0.9997, 0, 0)),
+    "ptlens": dict(distortion="ptlens", distortion_k=(0.01, -0.03, 0.02)),
+    "linear_tca_only": dict(tca="linear", tca_red=(1.0003, 0, 0), tca_blue=(0.9997, 0, 0)),
+    "poly3": dict(distortion="poly3", distortion_k=(-0.01, 0, 0)),
+    "poly5_poly3_tca": dict(distortion="poly5", distortion_k=(-0.02, 0.005, 0.0), tca="poly3",
+                            tca_red=(1.0002, 0.0001, -0.0001), tca_blue=(0.9998, -0.0001, 0.0001)),
+}
+
+
+@pytest.mark.parametrize("vignetting", [False, True])
+@pytest.mark.parametrize("name", sorted(RADIAL_CASES))
+@pytest.mark.parametrize("size", [(97, 61), (517, 389), (1536, 1024)])
+def test_optics_radial_table_and_newton_branches(stages, oracle, name, size, vignetting):
+    """The remap takes the radial multiplier table when its build accepts it and
+    the Newton path otherwise (correction.rs:110-181), bit for bit with the
+    oracle either way. Poly3 is refused (freeze ambiguity) at every size, the
+    symmetric Poly3 TCA pair collides except at 97x61, where it is accepted with
+    three pinned freeze boundaries."""
+    from rohditor_gb300 import OpticsExecution
+
+    w, h = size
+    kw = dict(RADIAL_CASES[name])
+    if vignetting:
+        kw["vignetting_k"] = (-0.3, 0.05, -0.01)
+    ex = OpticsExecution(w, h, **kw)
+    desc = oracle.optics_desc_from(ex.to_c())
+    guard, _, _, pins = oracle.optics_radial(desc)
+    refused = name == "poly3" or (name == "poly5_poly3_tca" and size != (97, 61))
+    assert (guard != "accepted") == refused
+    rgb = smooth_rgb(w, h, seed=17)
+    ours = stages.optics(rgb, ex)
+    ref = oracle.optics_apply(desc, rgb)
+    assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32))
+
+
+def test_optics_hypot_matches_glibc(stages):
+    """The table branch looks up f32::hypot of the input coordinates; the device
+    hypot equals glibc's double-evaluated one on ~110 M sampled pairs."""
+    assert stages.check_math(4) == 0
+
+
 def test_vignetting_only(stages, oracle):
     from rohditor_gb300 import OpticsExecution
 

@@ -10,8 +10,11 @@ by tests/golden/make_golden.py):
 Plus restated behavioural tests: normalization 1.3 / 0.5 at all crop-shifted
 phases (crates/core/src/pipeline/sensor.rs:767-803), MHC kernel impulses
 (malvar_he_cutler.rs:124-148), constant reconstruction (demosaic.rs:17-64),
-Clip >= vs > semantics (highlight/tests/clip.rs) and histogram luma rounding
-(analysis/histogram.rs:185-195).
+Clip >= vs > semantics (highlight/tests/clip.rs), histogram luma rounding
+(analysis/histogram.rs:185-195) and the radial multiplier table's guard
+decisions, pinned freeze boundaries and formula-bound coordinate parity
+(crates/optics/src/radial/tests.rs: radial_lut_parity,
+radial_lut_freeze_ambiguity_guard, radial_lut_determinism).
 """
 
 import json
@@ -205,3 +208,68 @@ def test_counted_amaze_build_is_bit_exact_and_counts(oracle):
         assert np.array_equal(ref.view(np.uint32), out.view(np.uint32))
         per_px = {k: v / m.size for k, v in ops.items()}
         assert 300 < per_px["add_sub"] < 600 and 100 < per_px["mul"] < 400 and per_px["div"] > 10
+
+
+# Lens models for the radial multiplier table (distortion model, k, TCA model,
+# red, blue) and the rule the build applies to each on a 320x213 frame.
+RADIAL_LENSES = {
+    "poly5_linear_tca": ((2, (-0.02, 0.005, 0.0), 1, (1.0003, 0, 0), (0.9997, 0, 0)), "accepted"),
+    "ptlens": ((3, (0.01, -0.03, 0.02), 0, (1, 0, 0), (1, 0, 0)), "accepted"),
+    "linear_tca_only": ((0, (0, 0, 0), 1, (1.0003, 0, 0), (0.9997, 0, 0)), "accepted"),
+    # Poly3 truncates rd / k1 to f32 in its step-0 residual: its freeze band is
+    # too wide, as radial.rs:44-57 measures for every bundled Poly3 profile.
+    "poly3": ((1, (-0.01, 0, 0), 0, (1, 0, 0), (1, 0, 0)), "freeze ambiguity"),
+    # Symmetric red / blue TCA flips land in the same knot segment.
+    "poly5_poly3_tca": ((2, (-0.02, 0.005, 0.0), 2, (1.0002, 0.0001, -0.0001), (0.9998, -0.0001, 0.0001)),
+                        "break collision"),
+}
+
+
+def radial_lens(oracle, name, w=320, h=213):
+    (dm, dk, tm, red, blue), _ = RADIAL_LENSES[name]
+    return oracle.optics_plan(w, h, dm, dk, tm, red, blue)
+
+
+@pytest.mark.parametrize("name", sorted(RADIAL_LENSES))
+def test_radial_table_guard_decisions(oracle, name):
+    guard, step, table, segments = oracle.optics_radial(radial_lens(oracle, name))
+    assert guard == RADIAL_LENSES[name][1]
+    assert step > 0 and np.all(np.isfinite(table))
+
+
+@pytest.mark.parametrize("name", ["poly5_linear_tca", "ptlens"])
+def test_radial_table_pins_each_freeze_boundary_inside_its_segment(oracle, name):
+    d = radial_lens(oracle, name)
+    guard, step, table, segments = oracle.optics_radial(d)
+    assert guard == "accepted" and len(segments) == 1
+    for index, radius in segments:
+        assert np.float32(index) * np.float32(step) <= radius <= np.float32(index + 1) * np.float32(step)
+    # Inside the freeze radius the kernel returns its input: the multiplier is 1.
+    kr = d.tca_red[0] if d.tca_model == 1 else 1.0
+    kb = d.tca_blue[0] if d.tca_model == 1 else 1.0
+    assert np.array_equal(table[0], np.array([kr, 1.0, kb], dtype=np.float32))
+
+
+@pytest.mark.parametrize("name", ["poly5_linear_tca", "ptlens", "linear_tca_only"])
+def test_radial_table_coordinates_within_the_formula_bound(oracle, name):
+    """radial.rs:60-72: B = max(0.15 px, 1.5 * NEWTON_EPS * norm_unscale) between
+    the table branch and the Newton path, here checked on every fourth pixel."""
+    import ctypes
+
+    d = radial_lens(oracle, name)
+    bound = max(0.15, 1.5e-5 * d.norm_unscale)
+    newton = np.zeros(6, dtype=np.float32)
+    worst = 0.0
+    for y in range(0, d.height, 4):
+        for x in range(0, d.width, 4):
+            lut = oracle.optics_map_lut(d, x, y)
+            assert oracle.load().ro_optics_map(ctypes.byref(d), x, y, oracle.ptr(newton)) == 0
+            worst = max(worst, float(np.max(np.abs(lut - newton))))
+    assert worst <= bound
+
+
+def test_radial_table_is_deterministic(oracle):
+    a = oracle.optics_radial(radial_lens(oracle, "poly5_linear_tca"))
+    b = oracle.optics_radial(radial_lens(oracle, "poly5_linear_tca"))
+    assert a[0] == b[0] and a[1] == b[1] and a[3] == b[3]
+    assert np.array_equal(a[2].view(np.uint32), b[2].view(np.uint32))
