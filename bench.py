@@ -137,7 +137,7 @@ MEASURED_TRAFFIC_BPP = {
     "amaze": (34.1, "profiles/amaze_kernel_4096x3072.md"),
     "rl_iteration": (10.3, "profiles/rl_step_kernel_4096x3072.md"),
     "rl_mask": (17.1, "profiles/rl_prep_step_kernel_4096x3072.md"),
-    "optics_gather": (24.8, "profiles/optics_kernel_4096x3072.md"),
+    "optics_gather": (25.0, "profiles/optics_lut_kernel_4096x3072.md"),
     "area_reduce": (14.9, "profiles/area_kernel_4096x3072.md"),
 }
 
