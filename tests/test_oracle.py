@@ -273,3 +273,39 @@ def test_radial_table_is_deterministic(oracle):
     b = oracle.optics_radial(radial_lens(oracle, "poly5_linear_tca"))
     assert a[0] == b[0] and a[1] == b[1] and a[3] == b[3]
     assert np.array_equal(a[2].view(np.uint32), b[2].view(np.uint32))
+
+
+def test_newton_and_table_coordinates_against_the_converged_root(oracle):
+    """The 24 MP workload's lens (Poly5 k1 = -0.02, k2 = 0.005, Linear TCA
+    1.0003 / 0.9997, crop 1, 35 mm, centred): the lensfun-style Newton path
+    (break at |F| < 1e-5) and the radial table both stay within the formula bound
+    B = max(0.15 px, 1.5 * 1e-5 * norm_unscale) (radial.rs:60-72) of the root
+    solved to convergence in f64, on a 63 x 42 grid of pixels."""
+    import ctypes
+
+    w, h = 6048, 4024
+    d = oracle.optics_plan(w, h, 2, (-0.02, 0.005, 0.0), 1, (1.0003, 0, 0), (0.9997, 0, 0))
+    k1, k2 = -0.02, 0.005
+    bound = max(0.15, 1.5e-5 * d.norm_unscale)
+    cpx, cpy = d.center_x * d.norm_unscale, d.center_y * d.norm_unscale
+    newton = np.zeros(6, dtype=np.float32)
+    worst_newton = worst_table = 0.0
+    for y in np.linspace(0, h - 1, 42).astype(int):
+        for x in np.linspace(0, w - 1, 63).astype(int):
+            ix = np.float32((cpx + (x - cpx) / np.float64(d.scale)) * d.norm_scale - d.center_x)
+            iy = np.float32((cpy + (y - cpy) / np.float64(d.scale)) * d.norm_scale - d.center_y)
+            rd = np.sqrt(np.float64(ix * ix + iy * iy))
+            ru = rd
+            for _ in range(60):
+                ru -= (ru * (1 + k1 * ru * ru + k2 * ru ** 4) - rd) / (1 + 3 * k1 * ru * ru + 5 * k2 * ru ** 4)
+            ratio = ru / rd if rd > 0 else 1.0
+            gx, gy = np.float64(ix) * ratio, np.float64(iy) * ratio
+            exact = []
+            for m in (1.0003, 1.0, 0.9997):
+                exact += [(gx * m + d.center_x) * d.norm_unscale, (gy * m + d.center_y) * d.norm_unscale]
+            exact = np.array(exact)
+            assert oracle.load().ro_optics_map(ctypes.byref(d), int(x), int(y), oracle.ptr(newton)) == 0
+            table = oracle.optics_map_lut(d, int(x), int(y))
+            worst_newton = max(worst_newton, float(np.max(np.abs(newton - exact))))
+            worst_table = max(worst_table, float(np.max(np.abs(table - exact))))
+    assert worst_newton <= bound and worst_table <= bound, (worst_newton, worst_table, bound)
