@@ -1373,7 +1373,13 @@ __global__ void __launch_bounds__(64) vignette_scan_kernel(const float* __restri
                                                            const float* __restrict__ r2_start, int W, int H,
                                                            float* __restrict__ checkpoints, int segs) {
   extern __shared__ __align__(16) float s_incr[];
-  for (int i = threadIdx.x; i < W; i += blockDim.x) s_incr[i] = incr[i];
+  // Staged 16 bytes at a time, four loads in flight per thread (incr is the
+  // start of a device allocation, so 16-byte aligned).
+  const int n4 = W >> 2;
+#pragma unroll 4
+  for (int i = threadIdx.x; i < n4; i += blockDim.x)
+    reinterpret_cast<float4*>(s_incr)[i] = __ldg(reinterpret_cast<const float4*>(incr) + i);
+  for (int i = 4 * n4 + threadIdx.x; i < W; i += blockDim.x) s_incr[i] = incr[i];
   __syncthreads();
   const int y = blockIdx.x * blockDim.x + threadIdx.x;
   if (y >= H) return;
@@ -1502,7 +1508,17 @@ __global__ void __launch_bounds__(VP_WARPS * 32) vignette_plane_kernel(const flo
   extern __shared__ float vsm[];
   float* s_incr = vsm;
   float* tbuf = vsm + W + W / 32 + 1;
-  for (int i = threadIdx.x; i < W; i += blockDim.x) s_incr[i + (i >> 5)] = incr[i];
+  const int n4 = W >> 2;  // four consecutive increments never straddle a pad word
+#pragma unroll 4
+  for (int i = threadIdx.x; i < n4; i += blockDim.x) {
+    const float4 v = __ldg(reinterpret_cast<const float4*>(incr) + i);
+    float* d = s_incr + 4 * i + (i >> 3);
+    d[0] = v.x;
+    d[1] = v.y;
+    d[2] = v.z;
+    d[3] = v.w;
+  }
+  for (int i = 4 * n4 + threadIdx.x; i < W; i += blockDim.x) s_incr[i + (i >> 5)] = incr[i];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int y = blockIdx.x * VP_WARPS + warp;
