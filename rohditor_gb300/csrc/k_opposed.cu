@@ -400,7 +400,7 @@ __global__ void relabel_kernel(const OpposedParams p) {
     label = 0;
   }
   p.labels[i] = label;
-  const Cell c = load_cell(p, cx, cy);
+  const Cell c = label != 0 ? load_cell(p, cx, cy) : Cell{};  // a cell outside every region needs no summary
   const unsigned clipped = c.flags >> 3;
   if (label && clipped) warp_or(p.region_clipped, label, clipped);
   if (label == 0 || clipped == 0) return;
@@ -434,7 +434,8 @@ __global__ void border_kernel(const OpposedParams p, int pass) {
   if (cx < p.cw) {
     const long long i = (long long)cy * p.cw + cx;
     const unsigned label = p.labels[i];
-    const Cell c = load_cell(p, cx, cy);
+    // Only cells inside a region contribute: the others skip the summary load.
+    const Cell c = label != 0 ? load_cell(p, cx, cy) : Cell{};
     if (label != 0 && (c.flags >> 3) == 0) {
       const unsigned rclip = p.region_clipped[label];
       const unsigned want_r = p.wanted[label], want_any = p.wanted[0];
