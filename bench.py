@@ -515,7 +515,9 @@ def batched_throughput(args, count: int = 24, lanes: int = 3) -> dict:
                          w.color.camera_to_rec2020, w.color) for w in wls]
     dev.close()
     pixels = sum(w.width * w.height for w in wls)
-    develop_batch(images[:lanes], lanes=lanes)  # warm-up
+    # Warm-up over the whole batch: every image shape takes its first-develop
+    # costs (launch-shape tuning, scratch and pool growth) outside the timing.
+    develop_batch(images, lanes=lanes)
     _, _, wall = develop_batch(images, lanes=lanes)
     _, _, wall1 = develop_batch(images, lanes=1)
     # With the mosaics and outputs in pinned host memory (a decoder writing
