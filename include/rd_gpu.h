@@ -326,6 +326,15 @@ rd_status rd_stage_output(rd_ctx* ctx, const float* rgb_in, uint32_t width, uint
  * for a lens given crop factor, real focal length and lens centre offsets. */
 rd_status rd_optics_plan(rd_optics_desc* optics, float crop_factor, float real_focal, float lens_center_x,
                          float lens_center_y);
+/* RadialMultipliers::build (crates/optics/src/radial.rs:172-208, 400-491): the
+ * table rd_spatial remaps through when its build accepts it. guard: -1 no
+ * table (no distortion and no TCA, or a degenerate grid), 0 accepted, else the
+ * refusing rule: 1 non-finite knot, 2 radiality tripwire, 3 two freeze flips in
+ * one segment, 4 ambiguous freeze band, 5 unexplained jump. knots (1024 x 4,
+ * optional) receives [m_red, m_green, m_blue, pin] per knot, pin being the
+ * break radius of a freeze boundary pinned in the segment that starts at the
+ * knot, or NaN; step the radius between knots. Host only. */
+rd_status rd_optics_radial_table(const rd_optics_desc* optics, float* knots, float* step, int32_t* guard);
 /* BaseRenderingLut::standard_v1 (crates/core/src/rendering.rs:36-50). */
 void rd_standard_base_lut(float* lut4096);
 

@@ -197,6 +197,7 @@ SIGNATURES = {
                                             ctypes.c_uint32, F32P]),
     "rd_stage_color": (ctypes.c_int, [VOIDP, F32P, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ColorDesc),
                                       U8P, U64P, U64P]),
+    "rd_optics_radial_table": (ctypes.c_int, [ctypes.POINTER(OpticsDesc), F32P, F32P, ctypes.POINTER(ctypes.c_int32)]),
     "rd_optics_plan": (ctypes.c_int, [ctypes.POINTER(OpticsDesc), ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                       ctypes.c_float]),
     "rd_standard_base_lut": (None, [F32P]),

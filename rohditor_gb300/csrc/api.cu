@@ -1206,6 +1206,16 @@ rd_status rd_optics_plan(rd_optics_desc* o, float crop, float real_focal, float 
   return rd::optics_plan(*o, crop, real_focal, cx, cy).code;
 }
 
+rd_status rd_optics_radial_table(const rd_optics_desc* o, float* knots, float* step, int32_t* guard) {
+  if (!o || !guard || o->width == 0 || o->height == 0) return RD_INVALID_INPUT;
+  const std::vector<float> tab = rd::optics_input_coordinates(*o);
+  const rd::RadialTable t = rd::build_radial_table(*o, tab.data(), tab.data() + o->width);
+  *guard = t.guard;
+  if (step) *step = t.step;
+  if (knots && t.guard >= 0) std::copy(t.knots.begin(), t.knots.end(), knots);
+  return RD_OK;
+}
+
 void rd_standard_base_lut(float* lut) {
   if (lut) rd::standard_base_lut(lut);
 }

@@ -475,10 +475,9 @@ AxisTable build_axis(int source, int target) {
 
 }  // namespace
 
-Status run_optics_gather(Context& ctx, const rd_optics_desc& o, const float* rgb_in, const float* mult,
-                         float* rgb_out) {
+// Per-axis pre-transform, plan.rs:448-455 / correction.rs input_coordinate_x,y.
+std::vector<float> optics_input_coordinates(const rd_optics_desc& o) {
   const int W = (int)o.width, H = (int)o.height;
-  // Per-axis pre-transform, plan.rs:448-455 / correction.rs input_coordinate_x,y.
   std::vector<float> tab((size_t)W + H);
   const double cpx = o.center_x * o.norm_unscale, cpy = o.center_y * o.norm_unscale;
   for (int x = 0; x < W; ++x) {
@@ -489,6 +488,13 @@ Status run_optics_gather(Context& ctx, const rd_optics_desc& o, const float* rgb
     const double mapped = cpy + ((double)y - cpy) / (double)o.scale;
     tab[W + y] = (float)(mapped * o.norm_scale - o.center_y);
   }
+  return tab;
+}
+
+Status run_optics_gather(Context& ctx, const rd_optics_desc& o, const float* rgb_in, const float* mult,
+                         float* rgb_out) {
+  const int W = (int)o.width, H = (int)o.height;
+  const std::vector<float> tab = optics_input_coordinates(o);
   // The remap's branch is decided once per apply (correction.rs:110-121).
   const RadialTable radial = build_radial_table(o, tab.data(), tab.data() + W);
   const bool lut = radial.guard == RD_RADIAL_ACCEPTED;

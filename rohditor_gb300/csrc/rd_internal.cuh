@@ -230,6 +230,9 @@ struct RadialTable {
   float step = 0.0f;
   std::vector<float> knots;  // 4 per knot
 };
+// The per-column then per-row input (lens) coordinates of an optics execution
+// (plan.rs:119-130, narrowed to f32): width + height values.
+std::vector<float> optics_input_coordinates(const rd_optics_desc& optics);
 // `input_x` / `input_y`: the per-column and per-row input (lens) coordinates.
 RadialTable build_radial_table(const rd_optics_desc& optics, const float* input_x, const float* input_y);
 // Distortion / TCA gather; `mult` (optional) is the vignetting plane applied to
