@@ -460,6 +460,46 @@ def test_develop_with_opposed(device, oracle):
     assert float(np.max(np.abs(got - ref))) <= 1e-4
 
 
+def test_full_24mp_workload_against_the_oracle(device, oracle):
+    """The bench's 6048x4024 workload end to end (Opposed + AMaZE + RL K=10, then
+    table-branch optics with vignetting, area reduction to 2560x1703, WB +
+    matrix, adjustments, sRGB8 + histogram) against the oracle at full size:
+    Opposed statistics exact; developed RGB within 5e-4 (the gate after 10 RL
+    iterations); the spatial stage, fed the GPU's own developed RGB, bit-exact;
+    sRGB8 within one code on at most 0.1% of samples; histogram exact."""
+    from rohditor_gb300 import GpuPreviewProcessor, GpuSensorProcessor, GpuSpatialProcessor
+    from rohditor_gb300.workloads import full_24mp
+
+    wl = full_24mp()
+    w, h = wl.width, wl.height
+    raw = wl.mosaic(device)
+    src = GpuSensorProcessor(device).develop(raw, wl.sensor, wl.capture)
+    odesc = oracle.sensor_desc(w, h, w, (0, 0, w, h), 0, [512.0], (1, 1), [16383.0])
+    m, pattern = oracle.normalize(raw, odesc)
+    m, stats, _, _ = oracle.opposed(m, pattern, wl.sensor.detection_levels, wl.sensor.neutral_ceiling)
+    ref = oracle.demosaic(m, pattern, wl.as_shot, 3)
+    ref = oracle.capture(ref, 0.5, 0.7, 0.5, wl.capture.ceilings, 10)
+    got = src.download()
+    assert list(src.metrics.highlight_stats) == stats.tolist()
+    assert float(np.max(np.abs(got - ref))) <= 5e-4
+    del ref, m
+    c = wl.color
+    base = GpuSpatialProcessor(device).reduce_preview(src, wl.optics, wl.target, c.wb_gains, c.camera_to_rec2020)
+    ref_o = oracle.optics_apply(oracle.optics_desc_from(wl.optics.to_c()), got)
+    ref_b = oracle.camera_matrix(oracle.white_balance(oracle.area_reduce(ref_o, wl.target), c.wb_gains),
+                                 c.camera_to_rec2020)
+    got_b = base.download()
+    assert np.array_equal(got_b.view(np.uint32), ref_b.view(np.uint32))
+    out, hist = GpuPreviewProcessor(device).render(base, c)
+    x = oracle.adjust(got_b, c.exposure_ev, c.base_lut, c.tone_lut, c.saturation, c.vibrance, c.hsl, c.grading)
+    diff = np.abs(out.astype(int) - oracle.display_srgb8(x).astype(int))
+    assert diff.max() <= 1 and (diff > 0).mean() <= 1e-3
+    ref_hist, _ = oracle.histogram(out)
+    assert np.array_equal(np.concatenate([hist.red, hist.green, hist.blue, hist.luminance]), ref_hist)
+    base.release()
+    src.release()
+
+
 def test_concurrent_lanes_with_different_widths_repeat_exactly(device):
     """Lanes on several threads launch the same kernels with different image
     widths at once (per-launch shared-memory sizes, work counters, tuning
