@@ -121,13 +121,18 @@ typedef struct rd_optics_desc {
 } rd_optics_desc;
 
 /* White balance, camera matrix and the global adjustment chain
- * (crates/core/src/cpu/stages.rs:380-528) with LUTs resolved on the host. */
+ * (crates/core/src/cpu/stages.rs:380-528) with LUTs resolved on the host.
+ * The chain runs exposure, base rendering, Light tone, tone curve,
+ * saturation / vibrance, HSL and grading, each step only when its has_ flag
+ * is set (stages.rs:434-452 decides the same per recipe). */
 typedef struct rd_color_desc {
   float wb_gains[3];
   float camera_to_rec2020[9];   /* row-major */
   float exposure_ev;
   int32_t has_base_lut;
   float base_lut[4096];         /* BaseRenderingLut values */
+  int32_t has_light_tone_lut;   /* set when contrast, highlights, shadows, whites or blacks is non-zero */
+  float light_tone_lut[4096];   /* LightToneLut values (crates/edit/src/light.rs:27-47), see rd_light_tone_lut */
   int32_t has_tone_lut;
   float tone_lut[4096];         /* ToneCurveLut values */
   float saturation, vibrance;
@@ -191,7 +196,7 @@ rd_status rd_render_device(rd_ctx* ctx, rd_base* base, const rd_color_desc* colo
  *   d_hist      device 4*256 u64 (R, G, B, luma); cleared by this call
  *   stream      cudaStream_t the work is enqueued on (NULL: legacy default)
  * Returns after enqueueing; results are ready when `stream` completes. No
- * context, no device allocation: the two 4096-entry LUTs (32 KB, the only
+ * context, no device allocation: the three 4096-entry LUTs (48 KB, the only
  * scratch; LUT length is fixed by rd_color_desc, image size is not limited)
  * are staged in a static device array of this library. The first call on a
  * device resolves that array's address and may load the module there; make
@@ -337,6 +342,11 @@ rd_status rd_optics_plan(rd_optics_desc* optics, float crop_factor, float real_f
 rd_status rd_optics_radial_table(const rd_optics_desc* optics, float* knots, float* step, int32_t* guard);
 /* BaseRenderingLut::standard_v1 (crates/core/src/rendering.rs:36-50). */
 void rd_standard_base_lut(float* lut4096);
+/* LightToneLut::new (crates/edit/src/light.rs:27-47, evaluate_light_tone
+ * :90-137): the 4096-entry Light transfer table for the contrast, highlights,
+ * shadows, whites and blacks sliders, made monotone, into lut4096. Host only;
+ * uses the platform exp2f / powf as the reference's f32::exp2 / f32::powf do. */
+void rd_light_tone_lut(float contrast, float highlights, float shadows, float whites, float blacks, float* lut4096);
 
 /* ---- batched develop ----
  * Many mosaics of uneven sizes, CFA phases and settings through the whole path

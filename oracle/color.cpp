@@ -4,7 +4,8 @@
 //  white balance / matrix  crates/core/src/cpu/stages.rs:250-308, crates/color/src/matrix.rs:45-61,173-175
 //  adjustments             crates/core/src/cpu/stages.rs:380-901
 //  base rendering LUT      crates/core/src/rendering.rs:36-92, 223-234
-//  LUT sampling            crates/edit/src/light.rs:78-88
+//  LUT sampling            crates/edit/src/light.rs:49-88
+//  Light tone LUT          crates/edit/src/light.rs:27-47, 90-142; applied at stages.rs:631-645
 //  output                  crates/core/src/cpu/stages.rs:1028-1094, crates/core/src/color/display_output.rs:24-59,
 //                          crates/color/src/gamut.rs:110-122,209-222, crates/color/src/transfer.rs:5-11
 //  histogram               crates/core/src/analysis/histogram.rs:92-128, clipping.rs:12-22
@@ -242,6 +243,60 @@ extern "C" void ro_standard_base_lut(float* lut) {
   }
 }
 
+// LightToneLut::new (light.rs:27-47): evaluate_light_tone at index/4095 for
+// every index, then the running-maximum projection.
+namespace {
+float lt_smoothstep(float edge0, float edge1, float value) {
+  const float normalized = rclamp((value - edge0) / (edge1 - edge0), 0.0f, 1.0f);
+  return normalized * normalized * (3.0f - 2.0f * normalized);
+}
+// bounded_move (light.rs:131-137)
+float lt_move(float value, float amount, float weight) {
+  if (amount >= 0.0f) return value + (1.0f - value) * amount * weight;
+  return value + value * amount * weight;
+}
+// protected_contrast (light.rs:119-129), pivot 0.18
+float lt_contrast(float input, float contrast) {
+  if (contrast == 0.0f) return input;
+  const float exponent = std::exp2(contrast);
+  const float pivot = 0.18f;
+  if (input <= pivot) return pivot * std::pow(input / pivot, exponent);
+  return 1.0f - (1.0f - pivot) * std::pow((1.0f - input) / (1.0f - pivot), exponent);
+}
+// evaluate_light_tone (light.rs:90-117): strengths 0.45 shadows/highlights, 0.25 blacks/whites
+float lt_evaluate(float input, float contrast, float highlights, float shadows, float whites, float blacks) {
+  float output = lt_contrast(input, contrast);
+  const float shadow_weight = lt_smoothstep(0.0f, 0.16f, input) * (1.0f - lt_smoothstep(0.38f, 0.68f, input));
+  const float highlight_weight = lt_smoothstep(0.32f, 0.62f, input) * (1.0f - lt_smoothstep(0.84f, 1.0f, input));
+  output = lt_move(output, shadows, 0.45f * shadow_weight);
+  output = lt_move(output, highlights, 0.45f * highlight_weight);
+  const float black_weight = 1.0f - lt_smoothstep(0.0f, 0.32f, input);
+  const float white_weight = lt_smoothstep(0.68f, 1.0f, input);
+  output = lt_move(output, blacks, 0.25f * black_weight);
+  output = lt_move(output, whites, 0.25f * white_weight);
+  return rclamp(output, 0.0f, 1.0f);
+}
+// apply_light_tone (stages.rs:631-645) with LightToneLut::sample / sample_extended (light.rs:49-64).
+void apply_light_tone(float* p, const float* lut, bool extended) {
+  const float current = luminance(p);
+  const float target = (extended && std::isfinite(current) && current > 1.0f) ? current + lut[4095] - 1.0f
+                                                                               : lut_sample(lut, current);
+  if (!std::isfinite(target) || std::fabs(target - current) <= F32_EPSILON) return;
+  apply_luminance_delta(p, current, target);
+}
+}  // namespace
+
+extern "C" void ro_light_tone_lut(float contrast, float highlights, float shadows, float whites, float blacks,
+                                  float* lut) {
+  for (int index = 0; index < 4096; ++index)
+    lut[index] = lt_evaluate((float)index / 4095.0f, contrast, highlights, shadows, whites, blacks);
+  float previous = lut[0];
+  for (int index = 1; index < 4096; ++index) {
+    lut[index] = rmax(lut[index], previous);
+    previous = lut[index];
+  }
+}
+
 // apply_adjustments_with_local, stages.rs:380-528, for the global (no local mask) path.
 extern "C" void ro_adjust_apply(float* rgb, size_t pixels, const ro_adjust* a) {
   const float gain = std::exp2(a->exposure_ev);
@@ -252,6 +307,7 @@ extern "C" void ro_adjust_apply(float* rgb, size_t pixels, const ro_adjust* a) {
     if (a->exposure_ev != 0.0f)
       for (int c = 0; c < 3; ++c) p[c] *= gain;
     if (a->base_lut) apply_lut_tone(p, a->base_lut, true);
+    if (a->light_lut) apply_light_tone(p, a->light_lut, a->extended != 0);
     if (a->tone_lut) apply_lut_tone(p, a->tone_lut, false);
     if (has_sat) {
       const float lum = luminance(p);

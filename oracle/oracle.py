@@ -65,7 +65,8 @@ class OpticsDesc(ctypes.Structure):
 
 class AdjustDesc(ctypes.Structure):
     _fields_ = [
-        ("exposure_ev", ctypes.c_float), ("base_lut", F32P), ("tone_lut", F32P),
+        ("exposure_ev", ctypes.c_float), ("base_lut", F32P), ("light_lut", F32P), ("extended", ctypes.c_int),
+        ("tone_lut", F32P),
         ("saturation", ctypes.c_float), ("vibrance", ctypes.c_float),
         ("has_hsl", ctypes.c_int), ("hsl", (ctypes.c_float * 3) * 8),
         ("has_grading", ctypes.c_int), ("grading", (ctypes.c_float * 3) * 3),
@@ -117,6 +118,7 @@ def load():
             "ro_camera_matrix": (None, [F32P, ctypes.c_size_t, F32P]),
             "ro_adjust_apply": (None, [F32P, ctypes.c_size_t, ctypes.POINTER(AdjustDesc)]),
             "ro_standard_base_lut": (None, [F32P]),
+            "ro_light_tone_lut": (None, [ctypes.c_float] * 5 + [F32P]),
             "ro_display_srgb8": (None, [F32P, ctypes.c_size_t, U8P]),
             "ro_histogram": (None, [U8P, ctypes.c_size_t, U64P, U64P]),
             "ro_set_exact_math": (None, [ctypes.c_int]),
@@ -405,15 +407,20 @@ def camera_matrix(rgb: np.ndarray, m) -> np.ndarray:
 
 
 def adjust(rgb: np.ndarray, exposure_ev=0.0, base_lut=None, tone_lut=None, saturation=1.0, vibrance=0.0,
-           hsl=None, grading=None) -> np.ndarray:
+           hsl=None, grading=None, light_lut=None, extended=False) -> np.ndarray:
     out = f32(rgb).copy()
     a = AdjustDesc()
     a.exposure_ev = exposure_ev
+    a.extended = 1 if extended else 0
     keep = []
     if base_lut is not None:
         b = f32(base_lut)
         keep.append(b)
         a.base_lut = ptr(b)
+    if light_lut is not None:
+        lt = f32(light_lut)
+        keep.append(lt)
+        a.light_lut = ptr(lt)
     if tone_lut is not None:
         t = f32(tone_lut)
         keep.append(t)
@@ -432,6 +439,14 @@ def adjust(rgb: np.ndarray, exposure_ev=0.0, base_lut=None, tone_lut=None, satur
 def standard_base_lut() -> np.ndarray:
     out = np.zeros(4096, dtype=np.float32)
     load().ro_standard_base_lut(ptr(out))
+    return out
+
+
+def light_tone_lut(contrast=0.0, highlights=0.0, shadows=0.0, whites=0.0, blacks=0.0) -> np.ndarray:
+    """LightToneLut::new (crates/edit/src/light.rs:27-47) values."""
+    out = np.zeros(4096, dtype=np.float32)
+    f = ctypes.c_float
+    load().ro_light_tone_lut(f(contrast), f(highlights), f(shadows), f(whites), f(blacks), ptr(out))
     return out
 
 

@@ -93,6 +93,8 @@ void ro_camera_matrix(float* rgb, size_t pixels, const float m[9]);
 typedef struct ro_adjust {
   float exposure_ev;
   const float* base_lut;    /* 4096 entries or NULL */
+  const float* light_lut;   /* LightToneLut, 4096 entries or NULL */
+  int extended;             /* 1: extended rendition (LightToneLut::sample_extended) */
   const float* tone_lut;    /* 4096 entries or NULL */
   float saturation, vibrance;
   int has_hsl;
@@ -102,6 +104,7 @@ typedef struct ro_adjust {
 } ro_adjust;
 void ro_adjust_apply(float* rgb, size_t pixels, const ro_adjust* a);
 void ro_standard_base_lut(float* lut4096);
+void ro_light_tone_lut(float contrast, float highlights, float shadows, float whites, float blacks, float* lut4096);
 void ro_display_srgb8(const float* rgb, size_t pixels, uint8_t* out);
 void ro_histogram(const uint8_t* rgb8, size_t pixels, uint64_t hist[4 * 256], uint64_t clipped[6]);
 

@@ -5,11 +5,11 @@ reference's `rohditor-gpu` processor interface."""
 from .processor import (CaptureContract, ColorContract, Device, GamutDiagnostics, GpuBase, GpuDevelopedSource,
                         GpuPreviewError, GpuPreviewProcessor, GpuSensorProcessor, GpuSpatialProcessor, Histogram,
                         OpticsExecution, OutputSpec, RlLaunchShape, SensorDescription, Stages, clip_levels,
-                        opposed_levels, rl_launch_shape, standard_base_lut)
+                        light_tone_lut, opposed_levels, rl_launch_shape, standard_base_lut)
 
 __all__ = [
     "CaptureContract", "ColorContract", "Device", "GamutDiagnostics", "GpuBase", "GpuDevelopedSource", "GpuPreviewError",
     "GpuPreviewProcessor", "GpuSensorProcessor", "GpuSpatialProcessor", "Histogram", "OpticsExecution",
-    "OutputSpec", "RlLaunchShape", "SensorDescription", "Stages", "clip_levels", "opposed_levels", "rl_launch_shape",
+    "OutputSpec", "RlLaunchShape", "SensorDescription", "Stages", "clip_levels", "light_tone_lut", "opposed_levels", "rl_launch_shape",
     "standard_base_lut",
 ]

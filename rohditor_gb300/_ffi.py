@@ -77,6 +77,7 @@ class ColorDesc(ctypes.Structure):
         ("camera_to_rec2020", ctypes.c_float * 9),
         ("exposure_ev", ctypes.c_float),
         ("has_base_lut", ctypes.c_int32), ("base_lut", ctypes.c_float * 4096),
+        ("has_light_tone_lut", ctypes.c_int32), ("light_tone_lut", ctypes.c_float * 4096),
         ("has_tone_lut", ctypes.c_int32), ("tone_lut", ctypes.c_float * 4096),
         ("saturation", ctypes.c_float), ("vibrance", ctypes.c_float),
         ("has_hsl", ctypes.c_int32), ("hsl", (ctypes.c_float * 3) * 8),
@@ -201,6 +202,7 @@ SIGNATURES = {
     "rd_optics_plan": (ctypes.c_int, [ctypes.POINTER(OpticsDesc), ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                       ctypes.c_float]),
     "rd_standard_base_lut": (None, [F32P]),
+    "rd_light_tone_lut": (None, [ctypes.c_float] * 5 + [F32P]),
     "rd_synth_mosaic_device": (ctypes.c_int, [VOIDP, ctypes.POINTER(SynthDesc), VOIDP]),
     "rd_develop_batch": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(BatchItem), ctypes.c_int32, ctypes.c_int32,
                                         ctypes.POINTER(ctypes.c_double)]),

@@ -366,6 +366,56 @@ void standard_base_lut(float* lut) {
   }
 }
 
+// LightToneLut::new (crates/edit/src/light.rs:27-47) with evaluate_light_tone
+// (:90-117), protected_contrast (:119-129), bounded_move (:131-137) and
+// smoothstep (:139-142), in f32 with each operation rounded on its own.
+namespace {
+constexpr float LIGHT_CONTRAST_PIVOT = 0.18f;
+constexpr float LIGHT_SHADOW_STRENGTH = 0.45f, LIGHT_HIGHLIGHT_STRENGTH = 0.45f;
+constexpr float LIGHT_BLACK_STRENGTH = 0.25f, LIGHT_WHITE_STRENGTH = 0.25f;
+
+float light_smoothstep(float edge0, float edge1, float v) {
+  float n = (v - edge0) / (edge1 - edge0);
+  if (n < 0.0f) n = 0.0f;
+  if (n > 1.0f) n = 1.0f;
+  return n * n * (3.0f - 2.0f * n);
+}
+float light_bounded_move(float value, float amount, float weight) {
+  return amount >= 0.0f ? value + (1.0f - value) * amount * weight : value + value * amount * weight;
+}
+float light_contrast(float input, float contrast) {
+  if (contrast == 0.0f) return input;
+  const float exponent = std::exp2(contrast);
+  if (input <= LIGHT_CONTRAST_PIVOT) return LIGHT_CONTRAST_PIVOT * std::pow(input / LIGHT_CONTRAST_PIVOT, exponent);
+  return 1.0f - (1.0f - LIGHT_CONTRAST_PIVOT) * std::pow((1.0f - input) / (1.0f - LIGHT_CONTRAST_PIVOT), exponent);
+}
+}  // namespace
+
+void light_tone_lut(float contrast, float highlights, float shadows, float whites, float blacks, float* lut) {
+  for (int i = 0; i < 4096; ++i) {
+    const float input = (float)i / 4095.0f;
+    float out = light_contrast(input, contrast);
+    const float shadow_w = light_smoothstep(0.0f, 0.16f, input) * (1.0f - light_smoothstep(0.38f, 0.68f, input));
+    const float highlight_w = light_smoothstep(0.32f, 0.62f, input) * (1.0f - light_smoothstep(0.84f, 1.0f, input));
+    out = light_bounded_move(out, shadows, LIGHT_SHADOW_STRENGTH * shadow_w);
+    out = light_bounded_move(out, highlights, LIGHT_HIGHLIGHT_STRENGTH * highlight_w);
+    const float black_w = 1.0f - light_smoothstep(0.0f, 0.32f, input);
+    const float white_w = light_smoothstep(0.68f, 1.0f, input);
+    out = light_bounded_move(out, blacks, LIGHT_BLACK_STRENGTH * black_w);
+    out = light_bounded_move(out, whites, LIGHT_WHITE_STRENGTH * white_w);
+    if (out < 0.0f) out = 0.0f;
+    if (out > 1.0f) out = 1.0f;
+    lut[i] = out;
+  }
+  // Monotone projection: each value is at least its predecessor (f32::max,
+  // which returns the other operand for a NaN).
+  float previous = lut[0];
+  for (int i = 1; i < 4096; ++i) {
+    if (std::isnan(lut[i]) || previous > lut[i]) lut[i] = previous;
+    previous = lut[i];
+  }
+}
+
 }  // namespace rd
 
 using rd::Status;
@@ -1218,6 +1268,10 @@ rd_status rd_optics_radial_table(const rd_optics_desc* o, float* knots, float* s
 
 void rd_standard_base_lut(float* lut) {
   if (lut) rd::standard_base_lut(lut);
+}
+
+void rd_light_tone_lut(float contrast, float highlights, float shadows, float whites, float blacks, float* lut) {
+  if (lut) rd::light_tone_lut(contrast, highlights, shadows, whites, blacks, lut);
 }
 
 rd_status rd_synth_mosaic_device(rd_ctx* h, const rd_synth_desc* d, uint16_t* d_out) {

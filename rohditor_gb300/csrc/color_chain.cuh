@@ -1,9 +1,10 @@
 // The global adjustment chain of the colour stage, shared by the preview
 // render (k_color.cu) and the display / extended-range output (k_output.cu).
 //
-//  exposure, base rendering LUT, tone curve LUT, saturation / vibrance, 8-band
-//  HSL and 3-way grading: crates/core/src/cpu/stages.rs:380-528 and helpers
-//  :605-901 (local masks are not part of this path). Every operation is a
+//  exposure, base rendering LUT, Light tone LUT, tone curve LUT, saturation /
+//  vibrance, 8-band HSL and 3-way grading: crates/core/src/cpu/stages.rs:380-528
+//  and helpers :605-901 (local masks are not part of this path); Light tone
+//  sampling crates/edit/src/light.rs:49-88. Every operation is a
 //  separately rounded f32 operation in the reference's order (the library is
 //  compiled without FMA contraction).
 #pragma once
@@ -11,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstring>
 
 #include "rd_internal.cuh"
 
@@ -221,7 +223,9 @@ __device__ void apply_grading(float* p, const float (*gr)[3]) {
 struct AdjustParams {
   float exposure_gain;
   int has_exposure;
+  int extended;               // 1: extended-range rendition (Light tone continues above 1)
   const float* base_lut;
+  const float* light_lut;
   const float* tone_lut;
   int has_sat;
   float saturation, vibrance;
@@ -242,6 +246,16 @@ __device__ __forceinline__ void apply_adjustments(const AdjustParams& a, float* 
   if (a.base_lut) {
     const float cur = luminance(v);
     const float tgt = base_sample(a.base_lut, cur);
+    if (isfinite(tgt) && fabsf(tgt - cur) > F32_EPS) luminance_delta(v, cur, tgt);
+  }
+  if (a.light_lut) {
+    // apply_light_tone (stages.rs:631-645): LightToneLut::sample, or
+    // sample_extended (light.rs:59-64) for an extended rendition, where a
+    // finite luminance above 1 continues from the table's last value with
+    // unit slope.
+    const float cur = luminance(v);
+    const float tgt = (a.extended && isfinite(cur) && cur > 1.0f) ? (cur + __ldg(a.light_lut + 4095)) - 1.0f
+                                                                  : lut_sample(a.light_lut, cur);
     if (isfinite(tgt) && fabsf(tgt - cur) > F32_EPS) luminance_delta(v, cur, tgt);
   }
   if (a.tone_lut) {
@@ -391,6 +405,29 @@ __device__ __forceinline__ void quantize_srgb3(const float* lin, float scale, fl
   }
 #pragma unroll
   for (int c = 0; c < 3; ++c) code[c] = rclamp(code[c], 0.0f, scale);
+}
+
+// The LUTs of one colour description are staged together on the device:
+// base rendering at [0, 4096), Light tone at [4096, 8192), tone curve at
+// [8192, 12288).
+constexpr int LUT_ENTRIES = 4096;
+constexpr int LUT_SET_ENTRIES = 3 * LUT_ENTRIES;
+constexpr size_t LUT_SET_BYTES = sizeof(float) * LUT_SET_ENTRIES;
+
+inline bool has_any_lut(const rd_color_desc& c) { return c.has_base_lut || c.has_light_tone_lut || c.has_tone_lut; }
+
+// Copies the description's LUTs into a host staging set laid out as above.
+inline void stage_luts(const rd_color_desc& c, float* host_set) {
+  if (c.has_base_lut) std::memcpy(host_set, c.base_lut, sizeof(float) * LUT_ENTRIES);
+  if (c.has_light_tone_lut) std::memcpy(host_set + LUT_ENTRIES, c.light_tone_lut, sizeof(float) * LUT_ENTRIES);
+  if (c.has_tone_lut) std::memcpy(host_set + 2 * LUT_ENTRIES, c.tone_lut, sizeof(float) * LUT_ENTRIES);
+}
+
+// Points the chain at a device LUT set laid out as above (null for an absent LUT).
+inline void set_lut_pointers(AdjustParams& a, const rd_color_desc& c, const float* device_set) {
+  a.base_lut = c.has_base_lut ? device_set : nullptr;
+  a.light_lut = c.has_light_tone_lut ? device_set + LUT_ENTRIES : nullptr;
+  a.tone_lut = c.has_tone_lut ? device_set + 2 * LUT_ENTRIES : nullptr;
 }
 
 // Scalar adjustment parameters of a colour description; the caller stages the

@@ -149,23 +149,20 @@ Status run_color_output(Context& ctx, const float* rgb, int W, int H, const rd_c
   p.out = srgb;
   p.hist = d_hist;
   float* luts = nullptr;
-  const size_t lut_bytes = sizeof(float) * 8192;
-  if (c.has_base_lut || c.has_tone_lut) {
+  if (has_any_lut(c)) {
     void* d = nullptr;
-    RD_TRY(device_alloc(ctx, lut_bytes, &d));
+    RD_TRY(device_alloc(ctx, LUT_SET_BYTES, &d));
     luts = static_cast<float*>(d);
-    if (c.has_base_lut)
-      RD_TRY(upload(ctx, luts, c.base_lut, sizeof(float) * 4096));
-    if (c.has_tone_lut)
-      RD_TRY(upload(ctx, luts + 4096, c.tone_lut, sizeof(float) * 4096));
+    if (c.has_base_lut) RD_TRY(upload(ctx, luts, c.base_lut, sizeof(float) * LUT_ENTRIES));
+    if (c.has_light_tone_lut) RD_TRY(upload(ctx, luts + LUT_ENTRIES, c.light_tone_lut, sizeof(float) * LUT_ENTRIES));
+    if (c.has_tone_lut) RD_TRY(upload(ctx, luts + 2 * LUT_ENTRIES, c.tone_lut, sizeof(float) * LUT_ENTRIES));
   }
-  p.adj.base_lut = c.has_base_lut ? luts : nullptr;
-  p.adj.tone_lut = c.has_tone_lut ? luts + 4096 : nullptr;
+  set_lut_pointers(p.adj, c, luts);
   const long long pixels = (long long)W * H;
   const int grid = (int)std::min<long long>((pixels + 255) / 256, (long long)(ctx.sm_count > 0 ? ctx.sm_count : 152) * 8);
   RD_LAUNCH(ctx, K_COLOR, color_kernel<<<grid, 256, 0, ctx.stream>>>(p));
   const cudaError_t launch = cudaGetLastError();
-  if (luts) device_free(ctx, luts, lut_bytes);
+  if (luts) device_free(ctx, luts, LUT_SET_BYTES);
   if (launch != cudaSuccess) return Status{RD_SYNCHRONIZATION, cudaGetErrorString(launch)};
   return Status{};
 }
@@ -193,7 +190,7 @@ size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 }  // namespace
 
 size_t color_batch_staging_bytes(int n) {
-  return align256(sizeof(ColorParams) * n) + align256(sizeof(int) * (n + 1)) + sizeof(float) * 8192 * (size_t)n;
+  return align256(sizeof(ColorParams) * n) + align256(sizeof(int) * (n + 1)) + LUT_SET_BYTES * (size_t)n;
 }
 
 Status run_color_batch(Context& ctx, const ColorBatchItem* items, int n, void* d_staging, void* h_staging) {
@@ -215,11 +212,8 @@ Status run_color_batch(Context& ctx, const ColorBatchItem* items, int n, void* d
     p.H = it.height;
     p.out = it.srgb;
     p.hist = it.hist;
-    float* lut = hl + (size_t)8192 * k;
-    if (it.color->has_base_lut) std::memcpy(lut, it.color->base_lut, sizeof(float) * 4096);
-    if (it.color->has_tone_lut) std::memcpy(lut + 4096, it.color->tone_lut, sizeof(float) * 4096);
-    p.adj.base_lut = it.color->has_base_lut ? dl + (size_t)8192 * k : nullptr;
-    p.adj.tone_lut = it.color->has_tone_lut ? dl + (size_t)8192 * k + 4096 : nullptr;
+    stage_luts(*it.color, hl + (size_t)LUT_SET_ENTRIES * k);
+    set_lut_pointers(p.adj, *it.color, dl + (size_t)LUT_SET_ENTRIES * k);
     hp[k] = p;
     hs[k] = blocks;
     const long long pixels = (long long)it.width * it.height;
@@ -245,15 +239,15 @@ Status run_color_batch(Context& ctx, const ColorBatchItem* items, int n, void* d
 // frame-callback thread, where a device allocation can block on the allocator
 // or on device-wide synchronisation, and where the device working set has
 // been sized and reserved up front under a fixed budget. The only per-call
-// scratch of the render, the two 4096-entry LUTs, is staged in the file-scope
-// array below instead of a stream-ordered buffer.
+// scratch of the render, the three 4096-entry LUTs, is staged in the
+// file-scope array below instead of a stream-ordered buffer.
 namespace rd {
 namespace {
 
-constexpr int NOALLOC_LUT_ENTRIES = 4096;
 constexpr int NOALLOC_MAX_DEVICES = 64;
-// Base rendering LUT at [0, 4096), tone curve LUT at [4096, 8192): 32 KB.
-__device__ __align__(256) float g_noalloc_luts[2 * NOALLOC_LUT_ENTRIES];
+// One LUT set (base rendering, Light tone, tone curve; 48 KB), laid out as
+// set_lut_pointers expects.
+__device__ __align__(256) float g_noalloc_luts[LUT_SET_ENTRIES];
 
 struct NoallocDevice {
   float* luts = nullptr;  // device address of g_noalloc_luts on this device
@@ -321,19 +315,17 @@ extern "C" rd_status rd_render_device_noalloc(const float* d_base, uint32_t widt
     cudaGetLastError();
     return RD_SYNCHRONIZATION;
   }
-  if (c.has_base_lut &&
-      cudaMemcpyAsync(dev.luts, c.base_lut, sizeof(float) * NOALLOC_LUT_ENTRIES, cudaMemcpyHostToDevice, s) !=
-          cudaSuccess) {
-    cudaGetLastError();
-    return RD_SYNCHRONIZATION;
+  const float* tables[3] = {c.has_base_lut ? c.base_lut : nullptr,
+                            c.has_light_tone_lut ? c.light_tone_lut : nullptr,
+                            c.has_tone_lut ? c.tone_lut : nullptr};
+  for (int t = 0; t < 3; ++t) {
+    if (tables[t] && cudaMemcpyAsync(dev.luts + t * LUT_ENTRIES, tables[t], sizeof(float) * LUT_ENTRIES,
+                                     cudaMemcpyHostToDevice, s) != cudaSuccess) {
+      cudaGetLastError();
+      return RD_SYNCHRONIZATION;
+    }
   }
-  if (c.has_tone_lut && cudaMemcpyAsync(dev.luts + NOALLOC_LUT_ENTRIES, c.tone_lut,
-                                        sizeof(float) * NOALLOC_LUT_ENTRIES, cudaMemcpyHostToDevice, s) != cudaSuccess) {
-    cudaGetLastError();
-    return RD_SYNCHRONIZATION;
-  }
-  p.adj.base_lut = c.has_base_lut ? dev.luts : nullptr;
-  p.adj.tone_lut = c.has_tone_lut ? dev.luts + NOALLOC_LUT_ENTRIES : nullptr;
+  set_lut_pointers(p.adj, c, dev.luts);
   const long long pixels = (long long)width * height;
   const int grid = (int)std::min<long long>((pixels + 255) / 256, (long long)dev.sm_count * 8);
   color_kernel<<<grid, 256, 0, s>>>(p);

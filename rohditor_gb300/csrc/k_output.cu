@@ -650,19 +650,17 @@ Status run_display_output(Context& ctx, const float* rgb, const rd_color_desc& c
   p.out = d_out;
   p.hist = o.format == RD_OUTPUT_SRGB8 ? d_hist : nullptr;
   p.gamut = d_gamut;
+  p.adj.extended = extended ? 1 : 0;
   float* luts = nullptr;
-  const size_t lut_bytes = sizeof(float) * 8192;
-  if (c.has_base_lut || c.has_tone_lut) {
+  if (has_any_lut(c)) {
     void* d = nullptr;
-    RD_TRY(device_alloc(ctx, lut_bytes, &d));
+    RD_TRY(device_alloc(ctx, LUT_SET_BYTES, &d));
     luts = static_cast<float*>(d);
-    if (c.has_base_lut)
-      RD_TRY(upload(ctx, luts, c.base_lut, sizeof(float) * 4096));
-    if (c.has_tone_lut)
-      RD_TRY(upload(ctx, luts + 4096, c.tone_lut, sizeof(float) * 4096));
+    if (c.has_base_lut) RD_TRY(upload(ctx, luts, c.base_lut, sizeof(float) * LUT_ENTRIES));
+    if (c.has_light_tone_lut) RD_TRY(upload(ctx, luts + LUT_ENTRIES, c.light_tone_lut, sizeof(float) * LUT_ENTRIES));
+    if (c.has_tone_lut) RD_TRY(upload(ctx, luts + 2 * LUT_ENTRIES, c.tone_lut, sizeof(float) * LUT_ENTRIES));
   }
-  p.adj.base_lut = c.has_base_lut ? luts : nullptr;
-  p.adj.tone_lut = c.has_tone_lut ? luts + 4096 : nullptr;
+  set_lut_pointers(p.adj, c, luts);
   if (p.hist) RD_CUDA_TRY(cudaMemsetAsync(p.hist, 0, 1024 * sizeof(unsigned long long), ctx.stream));
   if (p.gamut) RD_CUDA_TRY(cudaMemsetAsync(p.gamut, 0, 5 * sizeof(unsigned long long), ctx.stream));
   const long long tiles = (long long)((g.width + TILE - 1) / TILE) * ((g.height + TILE - 1) / TILE);
@@ -681,7 +679,7 @@ Status run_display_output(Context& ctx, const float* rgb, const rd_color_desc& c
   }
 #undef RD_OUTPUT_LAUNCH
   const cudaError_t launch = cudaGetLastError();
-  if (luts) device_free(ctx, luts, lut_bytes);
+  if (luts) device_free(ctx, luts, LUT_SET_BYTES);
   if (launch != cudaSuccess) return Status{RD_SYNCHRONIZATION, cudaGetErrorString(launch)};
   return Status{};
 }

@@ -291,5 +291,6 @@ void resolve_rl_tuning(Context& ctx);
 int gaussian_kernel(float sigma, float* weights, int max_taps);
 Status optics_plan(rd_optics_desc& optics, float crop, float real_focal, float cx, float cy);
 void standard_base_lut(float* lut);
+void light_tone_lut(float contrast, float highlights, float shadows, float whites, float blacks, float* lut);
 
 }  // namespace rd

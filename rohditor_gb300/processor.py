@@ -182,6 +182,7 @@ class ColorContract:
     camera_to_rec2020: tuple[float, ...] = (1, 0, 0, 0, 1, 0, 0, 0, 1)
     exposure_ev: float = 0.0
     base_lut: np.ndarray | None = None
+    light_tone_lut: np.ndarray | None = None  # LightToneLut values, see light_tone_lut()
     tone_lut: np.ndarray | None = None
     saturation: float = 1.0
     vibrance: float = 0.0
@@ -198,6 +199,9 @@ class ColorContract:
         if self.base_lut is not None:
             d.has_base_lut = 1
             ctypes.memmove(d.base_lut, _f32(self.base_lut).ctypes.data, 4096 * 4)
+        if self.light_tone_lut is not None:
+            d.has_light_tone_lut = 1
+            ctypes.memmove(d.light_tone_lut, _f32(self.light_tone_lut).ctypes.data, 4096 * 4)
         if self.tone_lut is not None:
             d.has_tone_lut = 1
             ctypes.memmove(d.tone_lut, _f32(self.tone_lut).ctypes.data, 4096 * 4)
@@ -296,6 +300,19 @@ def standard_base_lut() -> np.ndarray:
     """BaseRenderingLut::standard_v1 values (crates/core/src/rendering.rs:36-50)."""
     out = np.zeros(4096, dtype=np.float32)
     _ffi.load().rd_standard_base_lut(_ptr(out, ctypes.c_float))
+    return out
+
+
+def light_tone_lut(contrast: float = 0.0, highlights: float = 0.0, shadows: float = 0.0, whites: float = 0.0,
+                   blacks: float = 0.0) -> np.ndarray | None:
+    """LightToneLut::new (crates/edit/src/light.rs:27-47) for the Light sliders, or None when all
+    five are zero: the reference builds the table only then (crates/core/src/cpu/stages.rs:434-439)."""
+    if contrast == 0.0 and highlights == 0.0 and shadows == 0.0 and whites == 0.0 and blacks == 0.0:
+        return None
+    out = np.zeros(4096, dtype=np.float32)
+    f = ctypes.c_float
+    _ffi.load().rd_light_tone_lut(f(contrast), f(highlights), f(shadows), f(whites), f(blacks),
+                                  _ptr(out, ctypes.c_float))
     return out
 
 

@@ -48,7 +48,8 @@ def adjustments(**kw):
 
 def oracle_output(oracle, rgb, color, spec, exact):
     x = oracle.adjust(rgb, color.exposure_ev, color.base_lut, color.tone_lut, color.saturation, color.vibrance,
-                      color.hsl, color.grading)
+                      color.hsl, color.grading, light_lut=color.light_tone_lut,
+                      extended=spec.format.startswith("extended"))
     fmt = "extended_f32" if spec.format == "extended_f16" else spec.format
     desc = oracle.output_desc(fmt, spec.primaries, spec.policy, spec.dither, spec.orientation, spec.crop,
                               spec.headroom)
@@ -99,6 +100,30 @@ def test_output_bit_exact_against_exact_math(stages, oracle, fmt, policy, primar
     if fmt == "srgb8":
         ref_hist, _ = oracle.histogram(ref)
         assert np.array_equal(hist, ref_hist)
+
+
+@pytest.mark.parametrize("fmt", FORMATS)
+@pytest.mark.parametrize("sliders", [(0.5, -0.6, 0.4, -1.0, 0.3), (-0.7, 0.8, -0.5, 0.6, -0.4)])
+def test_light_tone_in_every_rendition(stages, oracle, fmt, sliders):
+    """The Light tone step (contrast, highlights, shadows, whites, blacks) between the base
+    rendering and the tone curve: SDR formats sample the table, extended formats continue it
+    above 1 with unit slope (LightToneLut::sample_extended); lowered Whites make the two differ."""
+    from rohditor_gb300 import light_tone_lut
+
+    rgb = wide_gamut_image(127, 67, seed=21, highlights=3.0)
+    color = adjustments(light_tone_lut=light_tone_lut(*sliders))
+    spec = OutputSpec(format=fmt, primaries="srgb", policy="clip", headroom=4.0)
+    ours, hist, gamut = stages.output(rgb, color, spec, histogram=fmt == "srgb8")
+    ref, ref_gamut = oracle_output(oracle, rgb, color, spec, exact=True)
+    assert same_bits(ours, ref)
+    assert np.array_equal(gamut, ref_gamut)
+    if fmt.startswith("extended"):
+        # The step is live above 1 in the extended rendition: an SDR-sampled table gives other values.
+        sdr = oracle.adjust(rgb, color.exposure_ev, color.base_lut, color.tone_lut, color.saturation,
+                            color.vibrance, color.hsl, color.grading, light_lut=color.light_tone_lut, extended=False)
+        ext = oracle.adjust(rgb, color.exposure_ev, color.base_lut, color.tone_lut, color.saturation,
+                            color.vibrance, color.hsl, color.grading, light_lut=color.light_tone_lut, extended=True)
+        assert not np.array_equal(sdr, ext)
 
 
 @pytest.mark.parametrize("fmt", FORMATS)

@@ -302,11 +302,12 @@ def colour_contract(**kw):
 def oracle_colour(oracle, rgb, c):
     x = oracle.white_balance(rgb, c.wb_gains)
     x = oracle.camera_matrix(x, c.camera_to_rec2020)
-    x = oracle.adjust(x, c.exposure_ev, c.base_lut, c.tone_lut, c.saturation, c.vibrance, c.hsl, c.grading)
+    x = oracle.adjust(x, c.exposure_ev, c.base_lut, c.tone_lut, c.saturation, c.vibrance, c.hsl, c.grading,
+                      light_lut=c.light_tone_lut)
     return oracle.display_srgb8(x)
 
 
-@pytest.mark.parametrize("variant", ["config", "grading_saturation", "neutral"])
+@pytest.mark.parametrize("variant", ["config", "grading_saturation", "neutral", "light", "light_extreme"])
 def test_colour_output_and_histogram(stages, oracle, variant):
     rng = np.random.default_rng(17)
     u = rng.uniform(-0.05, 0.8, size=(173, 3 * 251))
@@ -317,6 +318,17 @@ def test_colour_output_and_histogram(stages, oracle, variant):
     elif variant == "grading_saturation":
         c = colour_contract(saturation=1.2, vibrance=0.3,
                             grading=np.array([[0.2, -0.1, 0.05], [0.0, 0.1, -0.2], [-0.1, 0.0, 0.3]], np.float32))
+    elif variant == "light":
+        from rohditor_gb300 import light_tone_lut
+
+        # Light sliders (contrast, highlights, shadows, whites, blacks) between
+        # the base rendering and the tone curve.
+        c = colour_contract(light_tone_lut=light_tone_lut(0.4, -0.5, 0.35, -0.2, 0.15))
+        assert np.array_equal(c.light_tone_lut, oracle.light_tone_lut(0.4, -0.5, 0.35, -0.2, 0.15))
+    elif variant == "light_extreme":
+        from rohditor_gb300 import light_tone_lut
+
+        c = colour_contract(tone_lut=None, light_tone_lut=light_tone_lut(1.0, 1.0, -1.0, -1.0, 1.0))
     else:
         c = colour_contract(exposure_ev=0.0, base_lut=None, tone_lut=None, hsl=None)
     ours, hist, clipped = stages.color(rgb, c)
