@@ -1,11 +1,12 @@
 """Benchmark: full-sensor 24 MP develops per second on one GB300.
 
-Workload (the reference's full-sensor configuration): 6048x4024 RGGB u16
-14-bit synthetic mosaic, ~5% clipped in Gaussian blobs; Opposed highlight;
-AMaZE; masked RL capture sharpening, 10 iterations, sigma 0.7; optics (Poly5
-distortion -0.02/0.005, PA vignetting, linear TCA 1.0003/0.9997); exact area
-reduction to 2560x1703; WB + camera matrix; exposure +0.5 EV, 16-knot tone
-curve, 8-band HSL; sRGB 8-bit + histogram.
+Headline workload (the reference's full-sensor configuration, defined in
+workload_spec.full_24mp): 6048x4024 RGGB u16 14-bit synthetic mosaic, ~5%
+clipped in Gaussian blobs; Opposed highlight; AMaZE; masked RL capture
+sharpening, 10 iterations, sigma 0.7; optics (Poly5 distortion -0.02/0.005,
+PA vignetting, linear TCA 1.0003/0.9997); exact area reduction to 2560x1703;
+WB + camera matrix; exposure +0.5 EV, 16-knot tone curve, 8-band HSL; sRGB
+8-bit + histogram.
 
 A step is one complete develop of one mosaic. `value` is measured with the
 mosaic already resident in HBM (rd_develop_device -> rd_spatial ->
@@ -13,12 +14,24 @@ rd_render_device); `e2e` goes through the host-buffer C ABI (rd_develop from
 pinned host memory -> rd_spatial -> rd_render into host memory), copies
 included. L2 is flushed before every timed step (outside the step's events).
 
+After the headline, rank 0 measures the other configurations of the
+reference workload set, each under its own key: the 3008x2008 Clip + AMaZE
+full-resolution render and the 24 MP develop with RCD and with MHC
+(`configs`), the 48-image uneven batch (`batched`), the served trace over
+16 mixed-size images under a 120 GB budget (`edit_latency`), the
+full-resolution output formats (`export`) and the 102 MP export stream
+(`export_stream`); then the CPU baseline, the oracle developing the very
+same mosaic on the host cores, whose outputs also give the per-stage parity
+of the GPU develop (`parity`).
+
 Multi-GPU: images are independent, so N GPUs run N replicas; value = N x
-per-GPU develops/s (max step time over ranks).
+per-GPU develops/s from the max step time over ranks. `--gpus N` without a
+launcher starts N ranks itself.
 
 `--impl reference` times the reference algorithm on the host cores: the
 reference is Rust and cannot be built here, so its CPU restatement (the
-oracle) runs on a bounded band of the same workload per step.
+oracle) develops the whole seeded mosaic each step. It loads no part of the
+GPU library.
 """
 
 from __future__ import annotations
@@ -27,6 +40,7 @@ import argparse
 import ctypes
 import json
 import os
+import shutil
 import statistics
 import subprocess
 import sys
@@ -38,12 +52,30 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+import workload_spec as spec  # noqa: E402
+
 METRIC = "24MP develops/s"
 UNIT = "develops/s"
 KERNEL_FAMILIES = 15  # RD_KERNEL_FAMILIES of include/rd_gpu.h
 
+# Algorithmic FP32 operations per output pixel of AMaZE, counted on the bench
+# mosaic by the oracle's counting-float build (oracle/flops/census.py), and the
+# non-FMA FP32 issue rate at the maximum SM clock (152 SMs x 128 lanes x 2.07
+# GHz; the kernel is built without FMA contraction). No FP32 peak is measured
+# for this pool, so the nominal rate is the denominator.
+AMAZE_FP32_OPS_PER_PX = 478.18
+FP32_PEAK_TOPS = 152 * 128 * 2.07e9 / 1e12
 
-def dist_setup(gpus: int):
+
+# ------------------------------------------------------------------ ranks
+def relaunch_with_ranks(gpus: int) -> int:
+    """`--gpus N` without a launcher: run this command under torch.distributed.run with N ranks."""
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={gpus}",
+           "--master-addr", "127.0.0.1", "--master-port", os.environ.get("BENCH_MASTER_PORT", "29531")]
+    return subprocess.call(cmd + [os.path.abspath(__file__)] + sys.argv[1:])
+
+
+def dist_setup(backend: str = "gloo"):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -51,7 +83,7 @@ def dist_setup(gpus: int):
     if world > 1:
         import torch.distributed as dist
 
-        dist.init_process_group("gloo", init_method="env://")
+        dist.init_process_group(backend, init_method="env://")
         pg = dist
     return world, rank, local, pg
 
@@ -71,6 +103,14 @@ def max_over_ranks(pg, value: float) -> float:
     return float(t.item())
 
 
+def replica_throughput(pg, world: int, steps: int, local_ms: float) -> tuple[float, float]:
+    """Whole-job units/s of `world` replicas that each ran `steps` units in `local_ms`:
+    world x steps over the slowest rank's time. Returns (units/s, slowest ms)."""
+    slowest = max_over_ranks(pg, local_ms)
+    return world * steps / (slowest / 1e3), slowest
+
+
+# ------------------------------------------------------------------ clocks
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
 
@@ -130,27 +170,25 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-# DRAM bytes per pixel of one launch, measured with ncu on the 4096x3072 case of this workload
-# (dram__bytes_read.sum + dram__bytes_write.sum); the traffic grows with the pixel count, so the
-# bench workload's traffic is this figure times its pixels.
-MEASURED_TRAFFIC_BPP = {
-    "amaze": (34.1, "profiles/amaze_kernel_4096x3072.md"),
-    "rl_iteration": (10.3, "profiles/rl_step_kernel_4096x3072.md"),
-    "rl_mask": (17.1, "profiles/rl_prep_step_kernel_4096x3072.md"),
-    "optics_gather": (25.0, "profiles/optics_lut_kernel_4096x3072.md"),
-    "area_reduce": (14.9, "profiles/area_kernel_4096x3072.md"),
-}
+# ------------------------------------------------------------------ rooflines
+def load_peaks() -> tuple[float, str]:
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(peaks["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, ValueError, KeyError):
+        return 6800.0, "fallback 6.8 TB/s"
 
 
-# Algorithmic FP32 operations per output pixel of AMaZE, from the oracle census
-# (profiles/amaze_fp32_census.md), and the non-FMA FP32 issue rate of the GPU
-# at its maximum SM clock (152 SMs x 128 lanes x 2.07 GHz).
-AMAZE_FP32_OPS_PER_PX = 478.18
-FP32_PEAK_TOPS = 152 * 128 * 2.07e9 / 1e12
+def load_traffic() -> dict:
+    """DRAM bytes per pixel of one launch per kernel family, from the ncu captures in profiles/."""
+    try:
+        return json.load(open(os.path.join(ROOT, "profiles", "dram_traffic.json")))["kernels"]
+    except (OSError, ValueError, KeyError):
+        return {}
 
 
-# Algorithmic bytes per launch of each kernel family, per pixel of the image it covers.
-def family_bytes(name: str, N: int, n: int, H: int, tw: int) -> float | None:
+def family_bytes(name: str, N: int, n: int) -> float | None:
+    """Algorithmic bytes of one launch of a kernel family (N input pixels, n preview pixels)."""
     table = {
         "amaze": 14.0 * N,          # u16 mosaic in, planar f32 RGB out
         "rl_iteration": 12.0 * N,   # estimate in, guide in, estimate out
@@ -166,6 +204,9 @@ def family_bytes(name: str, N: int, n: int, H: int, tw: int) -> float | None:
         "rcd": 14.0 * N,
     }
     return table.get(name)
+
+
+FP32_BOUND = ("amaze", "rcd")
 
 
 def family_timing(lib, h, family: str) -> tuple[float, int]:
@@ -190,61 +231,76 @@ def rl_shape_record(W: int, H: int, radius: float) -> dict | None:
             "tuned_iteration_ms": round(s.best_ms, 4), "default_iteration_ms": round(s.default_ms, 4)}
 
 
-def run_ours(args, world, rank, local, pg):
-    from rohditor_gb300 import Device
-    from rohditor_gb300 import _ffi
-    from rohditor_gb300.workloads import full_24mp
+# ------------------------------------------------------------------ one workload on the device
+class DevelopBench:
+    """One workload's develop -> spatial -> render on a device context, resident or end to end."""
 
-    dev = Device(local)
-    lib = dev.lib
-    h = dev.handle
-    wl = full_24mp(demosaic=args.demosaic, iterations=args.iterations, highlight=args.highlight,
-                   width=args.width, height=args.height)
-    W, H = wl.width, wl.height
-    tw, th = wl.target
-    N, n = W * H, tw * th
-    sensor = wl.sensor.to_c()
-    detail = wl.capture.to_c()
-    optics = wl.optics.to_c()
-    color = wl.color.to_c()
-    wb = np.ascontiguousarray(wl.color.wb_gains, dtype=np.float32)
-    cam = np.ascontiguousarray(wl.color.camera_to_rec2020, dtype=np.float32)
-    wbp = wb.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
-    camp = cam.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
-    d_mosaic = wl.mosaic_device(dev)
-    # Pinned host copy of the same mosaic and pinned host outputs for the end-to-end leg.
-    mos_bytes = 2 * N
-    h_mosaic = ctypes.c_void_p()
-    dev.check(lib.rd_host_alloc(mos_bytes, ctypes.byref(h_mosaic)))
-    dev.check(lib.rd_copy_to_host(h, h_mosaic, ctypes.c_void_p(d_mosaic), mos_bytes))
-    h_out = ctypes.c_void_p()
-    dev.check(lib.rd_host_alloc(3 * n, ctypes.byref(h_out)))
-    hist = np.zeros(1024, dtype=np.uint64)
-    clipped = np.zeros(6, dtype=np.uint64)
+    def __init__(self, dev, wl):
+        self.dev, self.lib, self.h, self.wl = dev, dev.lib, dev.handle, wl
+        self.W, self.H = wl.width, wl.height
+        self.tw, self.th = wl.target
+        self.N, self.n = self.W * self.H, self.tw * self.th
+        self.sensor = wl.sensor.to_c()
+        self.detail = wl.capture.to_c() if wl.capture is not None else None
+        self.optics = wl.optics.to_c() if wl.optics is not None else None
+        self.color = wl.color.to_c()
+        self.wb = np.ascontiguousarray(wl.color.wb_gains, dtype=np.float32)
+        self.cam = np.ascontiguousarray(wl.color.camera_to_rec2020, dtype=np.float32)
+        self.d_mosaic = wl.mosaic_device(dev)
+        self.mos_bytes = 2 * self.N
+        lib = self.lib
+        self.h_mosaic = ctypes.c_void_p()
+        dev.check(lib.rd_host_alloc(self.mos_bytes, ctypes.byref(self.h_mosaic)))
+        dev.check(lib.rd_copy_to_host(self.h, self.h_mosaic, ctypes.c_void_p(self.d_mosaic), self.mos_bytes))
+        self.h_out = ctypes.c_void_p()
+        dev.check(lib.rd_host_alloc(3 * self.n, ctypes.byref(self.h_out)))
+        self.hist = np.zeros(1024, dtype=np.uint64)
+        self.clipped = np.zeros(6, dtype=np.uint64)
+        self.d2h_bytes = 3 * self.n + 1024 * 8 + 6 * 8
 
-    def step_device():
+    def _ptrs(self):
+        d = ctypes.byref(self.detail) if self.detail is not None else None
+        o = ctypes.byref(self.optics) if self.optics is not None else None
+        return d, o, self.wb.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), \
+            self.cam.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+    def step_device(self):
+        lib, h, dev = self.lib, self.h, self.dev
+        d, o, wbp, camp = self._ptrs()
         src, base = ctypes.c_void_p(), ctypes.c_void_p()
-        dev.check(lib.rd_develop_device(h, ctypes.c_void_p(d_mosaic), W, ctypes.byref(sensor), ctypes.byref(detail),
+        dev.check(lib.rd_develop_device(h, ctypes.c_void_p(self.d_mosaic), self.W, ctypes.byref(self.sensor), d,
                                         None, ctypes.byref(src), None))
-        dev.check(lib.rd_spatial(h, src, ctypes.byref(optics), tw, th, wbp, camp, ctypes.byref(base), None))
-        dev.check(lib.rd_render_device(h, base, ctypes.byref(color), None))
+        dev.check(lib.rd_spatial(h, src, o, self.tw, self.th, wbp, camp, ctypes.byref(base), None))
+        dev.check(lib.rd_render_device(h, base, ctypes.byref(self.color), None))
         lib.rd_source_release(src)
         lib.rd_base_release(base)
 
-    def step_e2e():
+    def step_e2e(self, keep: bool = False):
+        lib, h, dev = self.lib, self.h, self.dev
+        d, o, wbp, camp = self._ptrs()
         src, base = ctypes.c_void_p(), ctypes.c_void_p()
-        dev.check(lib.rd_develop(h, ctypes.cast(h_mosaic, ctypes.POINTER(ctypes.c_uint16)), W, ctypes.byref(sensor),
-                                 ctypes.byref(detail), None, ctypes.byref(src), None))
-        dev.check(lib.rd_spatial(h, src, ctypes.byref(optics), tw, th, wbp, camp, ctypes.byref(base), None))
-        dev.check(lib.rd_render(h, base, ctypes.byref(color), ctypes.cast(h_out, ctypes.POINTER(ctypes.c_uint8)),
-                                hist.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
-                                clipped.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), None))
+        dev.check(lib.rd_develop(h, ctypes.cast(self.h_mosaic, ctypes.POINTER(ctypes.c_uint16)), self.W,
+                                 ctypes.byref(self.sensor), d, None, ctypes.byref(src), None))
+        dev.check(lib.rd_spatial(h, src, o, self.tw, self.th, wbp, camp, ctypes.byref(base), None))
+        dev.check(lib.rd_render(h, base, ctypes.byref(self.color), ctypes.cast(self.h_out, ctypes.POINTER(ctypes.c_uint8)),
+                                self.hist.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                self.clipped.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), None))
+        kept = None
+        if keep:
+            source = np.empty((self.H, 3 * self.W), dtype=np.float32)
+            dev.check(lib.rd_source_download(h, src, source.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+            b = np.empty((self.th, 3 * self.tw), dtype=np.float32)
+            dev.check(lib.rd_base_download(h, base, b.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+            srgb = np.empty((self.th, 3 * self.tw), dtype=np.uint8)
+            ctypes.memmove(srgb.ctypes.data, self.h_out, srgb.nbytes)
+            kept = {"source": source, "base": b, "srgb8": srgb, "hist": self.hist.copy()}
         lib.rd_source_release(src)
         lib.rd_base_release(base)
+        return kept
 
-    def timed(step, steps):
-        total = 0.0
-        per = []
+    def timed(self, step, steps: int) -> tuple[float, list[float]]:
+        lib, h, dev = self.lib, self.h, self.dev
+        total, per = 0.0, []
         for _ in range(steps):
             dev.check(lib.rd_ctx_flush_l2(h))
             dev.check(lib.rd_ctx_event_record(h, 0))
@@ -256,119 +312,148 @@ def run_ours(args, world, rank, local, pg):
             total += ms.value
         return total, per
 
+    def kernel_table(self, steps: int) -> tuple[dict, dict, float]:
+        """Per-kernel device times from `steps` extra steps with every launch bracketed by events
+        (outside any timed region: the events add work between launches)."""
+        lib, h = self.lib, self.h
+        lib.rd_ctx_reset_kernel_timing(h)
+        lib.rd_ctx_enable_kernel_timing(h, 1)
+        self.timed(self.step_device, steps)
+        self.dev.synchronize()
+        lib.rd_ctx_enable_kernel_timing(h, 0)
+        families = {}
+        for f in range(KERNEL_FAMILIES):
+            name, ms, cnt = ctypes.c_char_p(), ctypes.c_double(), ctypes.c_uint64()
+            lib.rd_ctx_kernel_timing(h, f, ctypes.byref(name), ctypes.byref(ms), ctypes.byref(cnt))
+            if ms.value > 0:
+                families[name.value.decode()] = {"ms": ms.value, "launches": int(cnt.value)}
+        hbm_peak, _ = load_peaks()
+        kernels = {}
+        for name, rec in families.items():
+            b = family_bytes(name, self.N, self.n)
+            per_launch_ms = rec["ms"] / max(rec["launches"], 1)
+            entry = {"total_ms_per_step": round(rec["ms"] / steps, 4), "launches_per_step": rec["launches"] / steps,
+                     "ms_per_launch": round(per_launch_ms, 4)}
+            if b is not None:
+                gbs = b / (per_launch_ms / 1e3) / 1e9
+                entry["algorithmic_gbs"] = round(gbs, 1)
+                entry["hbm_frac"] = round(gbs / hbm_peak, 3)
+            if name == "amaze":
+                tops = AMAZE_FP32_OPS_PER_PX * self.N / (per_launch_ms / 1e3) / 1e12
+                entry["fp32_tops"] = round(tops, 2)
+                entry["fp32_frac"] = round(tops / FP32_PEAK_TOPS, 3)
+            kernels[name] = entry
+        kernel_ms = sum(r["ms"] for r in families.values()) / steps
+        return families, kernels, kernel_ms
+
+    def close(self):
+        self.lib.rd_host_free(self.h_mosaic)
+        self.lib.rd_host_free(self.h_out)
+        self.dev.check(self.lib.rd_device_free(self.h, ctypes.c_void_p(self.d_mosaic)))
+
+
+def rooflines(families: dict, N: int, n: int) -> tuple[dict | None, dict | None]:
+    """(roofline of the dominant kernel, HBM roofline of the dominant bandwidth-bound kernel)."""
+    hbm_peak, peak_src = load_peaks()
+    traffic = load_traffic()
+
+    def hbm_line(name):
+        rec = families[name]
+        per_launch_s = rec["ms"] / rec["launches"] / 1e3
+        b = family_bytes(name, N, n)
+        achieved = b / per_launch_s / 1e9
+        t = traffic.get(name)
+        return {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
+                "frac": round(achieved / hbm_peak, 3), "traffic": round(t["bytes_per_px"] * N) if t else None,
+                "traffic_source": (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on the {t['case']} "
+                                   f"case ({t['bytes_per_px']} B/px, profiles/{t['summary']}), scaled to {N} px")
+                if t else None,
+                "algorithmic_bytes": round(b), "peak_source": peak_src}
+
+    if not families:
+        return None, None
+    dominant = max(families.items(), key=lambda kv: kv[1]["ms"])[0]
+    hbm_kernels = [k for k in families if k not in FP32_BOUND and family_bytes(k, N, n) is not None]
+    hbm_dominant = max(hbm_kernels, key=lambda k: families[k]["ms"]) if hbm_kernels else None
+    hbm = hbm_line(hbm_dominant) if hbm_dominant else None
+    if dominant == "amaze":
+        rec = families["amaze"]
+        per_launch_s = rec["ms"] / rec["launches"] / 1e3
+        tops = AMAZE_FP32_OPS_PER_PX * N / per_launch_s / 1e12
+        t = traffic.get("amaze")
+        primary = {"bound": "fp32", "kernel": "amaze", "achieved": round(tops, 2), "peak": round(FP32_PEAK_TOPS, 1),
+                   "unit": "TFLOP/s", "frac": round(tops / FP32_PEAK_TOPS, 3),
+                   "traffic": round(t["bytes_per_px"] * N) if t else None,
+                   "algorithmic_bytes": round(family_bytes("amaze", N, n)),
+                   "hbm_frac": round(family_bytes("amaze", N, n) / per_launch_s / 1e9 / hbm_peak, 4),
+                   "ops_per_px": AMAZE_FP32_OPS_PER_PX,
+                   "ops_source": "FP32 operations per pixel counted by the oracle's counting-float AMaZE build",
+                   "peak_source": "nominal non-FMA FP32 rate at 2070 MHz (no FP32 peak is measured; the kernel "
+                                  "runs without FMA contraction)"}
+        return primary, hbm
+    if dominant in hbm_kernels:
+        return hbm_line(dominant), hbm
+    return None, hbm
+
+
+# ------------------------------------------------------------------ the GPU arm
+def run_ours(args, world, rank, local, pg):
+    from rohditor_gb300 import Device
+    from rohditor_gb300.workloads import full_24mp
+
+    dev = Device(local)
+    wl = full_24mp(demosaic=args.demosaic, iterations=args.iterations, highlight=args.highlight,
+                   width=args.width, height=args.height)
+    b = DevelopBench(dev, wl)
     for _ in range(args.warmup):
-        step_device()
+        b.step_device()
     dev.synchronize()
     launches0 = dev.kernel_launches
     barrier(pg)
     dev.synchronize()
     clocks = ClockSampler(local).__enter__()
-    total_ms, per = timed(step_device, args.steps)
+    total_ms, _ = b.timed(b.step_device, args.steps)
     dev.synchronize()
     launches = dev.kernel_launches - launches0
     barrier(pg)
-    total_ms = max_over_ranks(pg, total_ms)
-    # Per-kernel device times from extra steps with every launch bracketed by
-    # events (outside the timed region: the events add work between launches).
-    lib.rd_ctx_reset_kernel_timing(h)
-    lib.rd_ctx_enable_kernel_timing(h, 1)
+    value, total_ms = replica_throughput(pg, world, args.steps, total_ms)
     timing_steps = min(args.steps, 10)
-    timed(step_device, timing_steps)
-    dev.synchronize()
-    lib.rd_ctx_enable_kernel_timing(h, 0)
-    families = {}
-    for f in range(KERNEL_FAMILIES):
-        name = ctypes.c_char_p()
-        ms = ctypes.c_double()
-        cnt = ctypes.c_uint64()
-        lib.rd_ctx_kernel_timing(h, f, ctypes.byref(name), ctypes.byref(ms), ctypes.byref(cnt))
-        if ms.value > 0:
-            families[name.value.decode()] = {"ms": ms.value, "launches": int(cnt.value)}
+    families, kernels, kernel_ms = b.kernel_table(timing_steps)
     # e2e through host buffers
     for _ in range(max(1, args.warmup // 2)):
-        step_e2e()
+        b.step_e2e()
     barrier(pg)
-    e2e_ms, e2e_per = timed(step_e2e, args.steps)
+    e2e_local, _ = b.timed(b.step_e2e, args.steps)
     clocks.__exit__(None, None, None)  # sampled across both timed legs
-    e2e_ms = max_over_ranks(pg, e2e_ms)
-
-    ms_per_step = total_ms / args.steps
-    value = world * args.steps / (total_ms / 1e3)
-    e2e_value = world * args.steps / (e2e_ms / 1e3)
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except (OSError, ValueError):
-        pass
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    # Dominant HBM-bound kernel (largest device time among the bandwidth-bound families).
-    kernels = {}
-    for name, rec in families.items():
-        b = family_bytes(name, N, n, H, tw)
-        per_launch_ms = rec["ms"] / max(rec["launches"], 1)
-        entry = {"total_ms": round(rec["ms"], 3), "launches": rec["launches"],
-                 "ms_per_launch": round(per_launch_ms, 4)}
-        if b is not None:
-            gbs = b / (per_launch_ms / 1e3) / 1e9
-            entry["algorithmic_gbs"] = round(gbs, 1)
-            entry["hbm_frac"] = round(gbs / hbm_peak, 3)
-        kernels[name] = entry
-    step_kernel_ms = sum(r["ms"] for r in families.values()) / timing_steps
-    # The dominant kernel is the family with the most device time in the timed region.
-    dominant = max(families.items(), key=lambda kv: kv[1]["ms"])[0] if families else None
-    roofline = None
-    if dominant and family_bytes(dominant, N, n, H, tw) is not None:
-        rec = families[dominant]
-        per_launch_s = rec["ms"] / rec["launches"] / 1e3
-        achieved = family_bytes(dominant, N, n, H, tw) / per_launch_s / 1e9
-        bpp = MEASURED_TRAFFIC_BPP.get(dominant)
-        roofline = {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1), "peak": hbm_peak,
-                    "unit": "GB/s", "frac": round(achieved / hbm_peak, 3),
-                    "traffic": round(bpp[0] * N) if bpp else None,
-                    "traffic_source": (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on "
-                                       f"4096x3072 ({bpp[0]} B/px, {bpp[1]}), scaled to {N} px") if bpp else None,
-                    "algorithmic_bytes": round(family_bytes(dominant, N, n, H, tw)),
-                    "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
-                    else "fallback 6.8 TB/s"}
-    fp32_roofline = None
-    if "amaze" in families:
-        rec = families["amaze"]
-        per_launch_s = rec["ms"] / rec["launches"] / 1e3
-        tops = AMAZE_FP32_OPS_PER_PX * N / per_launch_s / 1e12
-        fp32_roofline = {"bound": "fp32", "kernel": "amaze", "achieved": round(tops, 2), "peak": round(FP32_PEAK_TOPS, 1),
-                         "unit": "Top/s", "frac": round(tops / FP32_PEAK_TOPS, 3),
-                         "ops_per_px": AMAZE_FP32_OPS_PER_PX,
-                         "ops_source": "oracle census, profiles/amaze_fp32_census.md",
-                         "peak_source": "nominal non-FMA FP32 rate at 2070 MHz (the kernel runs without FMA)"}
+    e2e_value, e2e_ms = replica_throughput(pg, world, args.steps, e2e_local)
+    kept = b.step_e2e(keep=True) if rank == 0 and not args.no_cpu_baseline else None
+    roofline, hbm_roofline = rooflines(families, b.N, b.n)
+    dv = wl.spec
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3), "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
-        "config": {"workload": f"full_24mp {W}x{H} RGGB 14-bit, {args.highlight} + {args.demosaic} + "
-                               f"RL{args.iterations} + optics(poly5, PA vignetting, linear TCA) + area->{tw}x{th} "
-                               f"+ WB/matrix + exposure/tone/HSL + sRGB8 + histogram",
-                   "mp_per_s": round(value * N / 1e6, 1), "parallelism": f"replicas x{world}",
+        "config": {"workload": dv.describe(), "mp_per_s": round(value * b.N / 1e6, 1),
+                   "parallelism": f"replicas x{world}",
                    "l2": "flushed before every timed step (256 MB write outside the step events)"},
-        "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": mos_bytes,
-                "d2h_bytes_per_step": 3 * n + 1024 * 8 + 6 * 8, "ms_per_step": round(e2e_ms / args.steps, 3)},
+        "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": b.mos_bytes,
+                "d2h_bytes_per_step": b.d2h_bytes, "ms_per_step": round(e2e_ms / args.steps, 3)},
         "gpu_launches": int(launches),
         "roofline": roofline,
-        "fp32_roofline": fp32_roofline,
+        "hbm_roofline": hbm_roofline,
         "kernels": kernels,
-        "dominant_kernel": dominant,
-        "kernel_ms_per_step": round(step_kernel_ms, 3),
-        "rl_launch_shape": rl_shape_record(W, H, wl.capture.radius),
+        "kernel_ms_per_step": round(kernel_ms, 3),
+        "rl_launch_shape": rl_shape_record(b.W, b.H, wl.capture.radius),
         "clocks": clocks.summary(),
     }
-    lib.rd_host_free(h_mosaic)
-    lib.rd_host_free(h_out)
-    dev.check(lib.rd_device_free(h, ctypes.c_void_p(d_mosaic)))
+    b.close()
     dev.close()
+    if rank == 0 and not args.no_configs:
+        line["configs"] = other_configs(args)
     if rank == 0 and not args.no_edit_latency:
         line["edit_latency"] = edit_latency(args)
     if rank == 0 and not args.no_batched:
-        line["batched"] = batched_throughput(args)
+        line["batched"] = batched_throughput(args, count=args.batch_images)
     if rank == 0 and not args.no_export:
         line["export"] = export_output(args)
     if rank == 0 and args.export_stream:
@@ -376,41 +461,63 @@ def run_ours(args, world, rank, local, pg):
     # Last: the oracle's OpenMP threads stay busy for a while after a run and
     # would compete with the host threads of the latency measurements.
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(args, sample_rows=args.cpu_baseline_rows)
+        line["cpu_baseline"], line["parity"] = cpu_baseline(dv, kept, seconds=args.cpu_baseline_seconds)
     return line
 
 
+def other_configs(args, steps: int = 20) -> dict:
+    """The 3008x2008 Clip + AMaZE full-resolution render and the 24 MP develop with RCD and with
+    MHC: device-resident develops/s, end to end through host buffers, and per-kernel tables."""
+    from rohditor_gb300 import Device
+    from rohditor_gb300.workloads import full_24mp, plain_3mp
+
+    out = {}
+    cases = {"plain_3mp_clip_amaze": plain_3mp(),
+             "full_24mp_rcd": full_24mp(demosaic="rcd", iterations=args.iterations),
+             "full_24mp_mhc": full_24mp(demosaic="mhc", iterations=args.iterations)}
+    dev = Device(0)
+    for name, wl in cases.items():
+        b = DevelopBench(dev, wl)
+        for _ in range(3):
+            b.step_device()
+        dev.synchronize()
+        total, _ = b.timed(b.step_device, steps)
+        _, kernels, kernel_ms = b.kernel_table(min(steps, 5))
+        b.step_e2e()
+        e2e, _ = b.timed(b.step_e2e, steps)
+        out[name] = {"workload": wl.spec.describe(), "develops_per_s": round(steps / (total / 1e3), 2),
+                     "ms_per_develop": round(total / steps, 3), "mp_per_s": round(steps * b.N / 1e6 / (total / 1e3), 1),
+                     "e2e_develops_per_s": round(steps / (e2e / 1e3), 2), "kernel_ms_per_develop": round(kernel_ms, 3),
+                     "kernels": kernels}
+        b.close()
+    dev.close()
+    return out
+
+
 def edit_latency(args, images: int = 16, seconds: float = 2.0, rate: float = 200.0, develop_share: float = 0.1,
-                 seed: int = 4) -> dict:
+                 seed: int = 4, budget_gb: float = 120.0) -> dict:
     """Preview edit latency, served vs plain, on one seeded Poisson trace.
 
-    `images` 24 MP images are open; requests arrive at `rate` per second for
-    `seconds`; a share are full re-develops (jittered capture amount), the rest
-    preview edits of a resident base (jittered exposure, tone curve and HSL),
-    with per-image increasing revisions. Served: the trace is submitted to the
-    served loop (rd_server_*), latency = submit -> result with the sRGB8 image
-    and histogram on the host. Plain: the same trace run in arrival order, one
-    request at a time, through rd_develop/rd_spatial/rd_render on one context
-    (each edit a synchronous render of its image's current base).
+    `images` open images of the uneven batch's mixed sizes (12-60 MP, random
+    CFA phase, Opposed + AMaZE + RL K=5 + optics, 2560-px preview bases);
+    requests arrive at `rate` per second for `seconds`; a share are full
+    re-develops (jittered capture amount), the rest preview edits of a
+    resident base (jittered exposure, tone curve, HSL and grading), with
+    per-image increasing revisions. Served: the trace is submitted to the
+    served loop (rd_server_*) under a `budget_gb` admission budget, latency =
+    submit -> result with the sRGB8 image and histogram on the host. Plain:
+    the same trace run in arrival order, one request at a time, through
+    rd_develop/rd_spatial/rd_render on one context (each edit a synchronous
+    render of its image's current base).
     """
     from rohditor_gb300 import (CaptureContract, Device, GpuPreviewProcessor, GpuSensorProcessor,
                                 GpuSpatialProcessor)
     from rohditor_gb300.served import EDIT, PreviewServer
-    from rohditor_gb300.workloads import full_24mp, hsl_bands, sixteen_knot_curve
+    from rohditor_gb300.workloads import batched_uneven, hsl_bands, sixteen_knot_curve
 
-    wl = full_24mp(demosaic=args.demosaic, iterations=args.iterations, highlight=args.highlight,
-                   width=args.width, height=args.height)
+    wls = batched_uneven(images, seed=11)
     dev = Device(0)
-    lib = dev.lib
-    mosaics = []
-    for i in range(images):
-        w = full_24mp(demosaic=args.demosaic, iterations=args.iterations, highlight=args.highlight, seed=100 + i,
-                      width=args.width, height=args.height)
-        host = np.empty((w.height, w.width), dtype=np.uint16)
-        d = w.synth_desc()
-        dev.check(lib.rd_synth_mosaic(dev.handle, ctypes.byref(d),
-                                      host.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16))))
-        mosaics.append(host)
+    mosaics = [w.mosaic(dev) for w in wls]
     rng = np.random.default_rng(seed)
     trace = []
     t = 0.0
@@ -421,6 +528,7 @@ def edit_latency(args, images: int = 16, seconds: float = 2.0, rate: float = 200
             break
         img = int(rng.integers(images))
         revision[img] += 1
+        wl = wls[img]
         if rng.random() < develop_share:
             cap = CaptureContract(amount=float(rng.uniform(0.3, 0.7)), radius=wl.capture.radius,
                                   noise_protection=wl.capture.noise_protection, ceilings=wl.capture.ceilings,
@@ -428,10 +536,11 @@ def edit_latency(args, images: int = 16, seconds: float = 2.0, rate: float = 200
             trace.append((t, 1, img, revision[img], cap))
         else:
             c = wl.color
+            grading = rng.uniform(-0.2, 0.2, size=(3, 3)).astype(np.float32)
             color = type(c)(wb_gains=c.wb_gains, camera_to_rec2020=c.camera_to_rec2020,
-                            exposure_ev=float(0.5 + rng.uniform(-0.3, 0.3)), base_lut=c.base_lut,
+                            exposure_ev=float(c.exposure_ev + rng.uniform(-0.3, 0.3)), base_lut=c.base_lut,
                             tone_lut=sixteen_knot_curve(seed=int(rng.integers(1 << 30))),
-                            hsl=hsl_bands(seed=int(rng.integers(1 << 30))))
+                            hsl=hsl_bands(seed=int(rng.integers(1 << 30))), grading=grading)
             trace.append((t, 0, img, revision[img], color))
 
     def pct(v):
@@ -442,8 +551,8 @@ def edit_latency(args, images: int = 16, seconds: float = 2.0, rate: float = 200
                 "mean_ms": round(float(v.mean()), 3), "n": int(v.size)}
 
     # Served.
-    server = PreviewServer(0)
-    for i in range(images):
+    server = PreviewServer(0, budget_bytes=int(budget_gb * (1 << 30)))
+    for i, wl in enumerate(wls):
         server.open(i, mosaics[i], wl.sensor, wl.capture, wl.optics, wl.target, wl.color.wb_gains,
                     wl.color.camera_to_rec2020)
     server.drain(120000)
@@ -456,8 +565,9 @@ def edit_latency(args, images: int = 16, seconds: float = 2.0, rate: float = 200
         if kind == 0:
             server.submit_edit(img, rev, colors[k])
         else:
-            server.submit_develop(img, rev, payload, wl.optics)
+            server.submit_develop(img, rev, payload, wls[img].optics)
     server.drain(120000)
+    t_served = time.perf_counter() - t0
     res = server.poll(1 << 16)
     stats = server.stats()
     server.close()
@@ -467,7 +577,7 @@ def edit_latency(args, images: int = 16, seconds: float = 2.0, rate: float = 200
     # Plain: one request at a time in arrival order.
     sensor_p, spatial_p, preview_p = GpuSensorProcessor(dev), GpuSpatialProcessor(dev), GpuPreviewProcessor(dev)
     bases = []
-    for i in range(images):
+    for i, wl in enumerate(wls):
         src = sensor_p.develop(mosaics[i], wl.sensor, wl.capture)
         bases.append(spatial_p.reduce_preview(src, wl.optics, wl.target, wl.color.wb_gains,
                                               wl.color.camera_to_rec2020))
@@ -477,6 +587,7 @@ def edit_latency(args, images: int = 16, seconds: float = 2.0, rate: float = 200
     for ts, kind, img, rev, payload in trace:
         while time.perf_counter() - t0 < ts:
             time.sleep(0.0002)
+        wl = wls[img]
         if kind == 0:
             preview_p.render(bases[img], payload)
             plain_edits.append(1e3 * (time.perf_counter() - t0 - ts))
@@ -487,24 +598,30 @@ def edit_latency(args, images: int = 16, seconds: float = 2.0, rate: float = 200
             bases[img].release()
             bases[img] = base
             plain_dev.append(1e3 * (time.perf_counter() - t0 - ts))
+    t_plain = time.perf_counter() - t0
     for b in bases:
         b.release()
     dev.close()
+    sizes = sorted({f"{w.width}x{w.height}" for w in wls})
+    done = len(served_edits) + len(served_dev)
     return {
-        "trace": {"images": images, "image": f"{wl.width}x{wl.height}", "seconds": seconds, "rate_per_s": rate,
-                  "develop_share": develop_share, "requests": len(trace), "seed": seed},
+        "trace": {"images": images, "sizes": sizes, "seconds": seconds, "rate_per_s": rate,
+                  "develop_share": develop_share, "requests": len(trace), "seed": seed, "budget_gb": budget_gb},
         "served": {"edit": pct(served_edits), "develop": pct(served_dev), "coalesced": stats["coalesced"],
-                   "batches": stats["batches"], "batched_edits": stats["batched_edits"]},
-        "plain": {"edit": pct(plain_edits), "develop": pct(plain_dev)},
+                   "batches": stats["batches"], "batched_edits": stats["batched_edits"],
+                   "completed_per_s": round(done / t_served, 1), "evictions": stats.get("evictions")},
+        "plain": {"edit": pct(plain_edits), "develop": pct(plain_dev),
+                  "completed_per_s": round((len(plain_edits) + len(plain_dev)) / t_plain, 1)},
     }
 
 
-def batched_throughput(args, count: int = 24, lanes: int = 3) -> dict:
-    """The uneven batch (rohditor_gb300.workloads.batched_uneven: 12-60 MP,
-    random CFA phase, black, WB and matrices; Opposed + AMaZE + RL K=5 +
-    optics + 2560-px preview, sRGB8 + histogram to the host) through
-    rd_develop_batch with `lanes` concurrent lanes, and the same images one at
-    a time (one lane). Host mosaics in, host outputs out, timed end to end."""
+def batched_throughput(args, count: int = 48, lanes: int = 3) -> dict:
+    """The uneven batch (workload_spec.batched_uneven: 12-60 MP, random CFA
+    phase, black, WB and matrices; Opposed + AMaZE + RL K=5 + optics + 2560-px
+    preview, sRGB8 + histogram to the host) through rd_develop_batch with
+    `lanes` concurrent lanes, the same images one at a time (one lane), and the
+    batch as one captured CUDA graph. Host mosaics in, host outputs out, timed
+    end to end."""
     from rohditor_gb300 import Device
     from rohditor_gb300.batch import BatchImage, PinnedBatch, develop_batch
     from rohditor_gb300.workloads import batched_uneven
@@ -542,7 +659,8 @@ def batched_throughput(args, count: int = 24, lanes: int = 3) -> dict:
             "develops_per_s": round(count / (wall / 1e3), 2), "mp_per_s": round(pixels / 1e6 / (wall / 1e3), 1),
             "one_lane_wall_ms": round(wall1, 1), "speedup_vs_one_lane": round(wall1 / wall, 3),
             "pinned_host": pinned_runs,
-            "workload": "uneven batch: 12/24/45/60 MP, random CFA phase, Opposed + AMaZE + RL5 + optics + preview"}
+            "workload": f"uneven batch of {count}: 12/24/45/60 MP, random CFA phase, Opposed + AMaZE + RL5 + optics "
+                        f"+ preview"}
 
 
 def export_output(args, reps: int = 5) -> dict:
@@ -569,12 +687,7 @@ def export_output(args, reps: int = 5) -> dict:
     dev.check(lib.rd_spatial(h, src, ctypes.byref(optics), W, H, wb.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
                              cam.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), ctypes.byref(base), None))
     lib.rd_source_release(src)
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except (OSError, ValueError):
-        pass
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    hbm_peak, _ = load_peaks()
     specs = {
         "extended_f16_p3_compress_h4": OutputSpec(format="extended_f16", primaries="display_p3",
                                                   policy="chroma_compress", headroom=4.0),
@@ -586,9 +699,9 @@ def export_output(args, reps: int = 5) -> dict:
     d_out, d_gamut = ctypes.c_void_p(), ctypes.c_void_p()
     dev.check(lib.rd_device_alloc(h, 12 * W * H, ctypes.byref(d_out)))
     dev.check(lib.rd_device_alloc(h, 64, ctypes.byref(d_gamut)))
-    for name, spec in specs.items():
-        oc = spec.to_c()
-        bpp = {"srgb8": 3, "srgb16": 6, "extended_f32": 12, "extended_f16": 6}[spec.format]
+    for name, sp in specs.items():
+        oc = sp.to_c()
+        bpp = {"srgb8": 3, "srgb16": 6, "extended_f32": 12, "extended_f16": 6}[sp.format]
         dev.check(lib.rd_render_output_device(h, base, ctypes.byref(color), ctypes.byref(oc), d_out, None, d_gamut,
                                               None))
         dev.synchronize()
@@ -617,7 +730,7 @@ def export_output(args, reps: int = 5) -> dict:
 
 def export_stream(args, count: int = 24, window: int = 3, cap_gb: float = 60.0) -> dict:
     """The large-sensor export stream through the served loop: `count` 101.8 MP
-    16-bit mosaics with hot pixels and specular blobs (workloads.large_export:
+    16-bit mosaics with hot pixels and specular blobs (workload_spec.large_export:
     Opposed + AMaZE + RL K = 20 + full optics) are opened in one rd_server with
     a `cap_gb` budget (each open develops and keeps the image's layers), then
     each is exported at full resolution as extended f16 (Display P3, chroma
@@ -626,7 +739,7 @@ def export_stream(args, count: int = 24, window: int = 3, cap_gb: float = 60.0) 
     and the polled results."""
     from rohditor_gb300 import Device, OutputSpec
     from rohditor_gb300 import _ffi
-    from rohditor_gb300.workloads import CAMERA_TO_REC2020, hot_pixels, large_export
+    from rohditor_gb300.workloads import large_export
 
     wls = large_export(count)
     dev = Device(0)
@@ -634,12 +747,13 @@ def export_stream(args, count: int = 24, window: int = 3, cap_gb: float = 60.0) 
     server = ctypes.c_void_p()
     dev.check(lib.rd_server_create(0, int(cap_gb * (1 << 30)), ctypes.byref(server)))
     W, H = wls[0].width, wls[0].height
+    raws = [wl.mosaic(dev) for wl in wls]
     t0 = time.perf_counter()
     for k, wl in enumerate(wls):
-        raw = hot_pixels(wl.mosaic(dev), seed=k)
+        raw = raws[k]
         s, d, o = wl.sensor.to_c(), wl.capture.to_c(), wl.optics.to_c()
         wb = np.ascontiguousarray(wl.color.wb_gains, dtype=np.float32)
-        cam = np.ascontiguousarray(CAMERA_TO_REC2020, dtype=np.float32)
+        cam = np.ascontiguousarray(wl.color.camera_to_rec2020, dtype=np.float32)
         dev.check(lib.rd_server_open(server, k, raw.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16)), W,
                                      ctypes.byref(s), ctypes.byref(d), ctypes.byref(o), wl.target[0], wl.target[1],
                                      wb.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
@@ -697,6 +811,7 @@ def export_stream(args, count: int = 24, window: int = 3, cap_gb: float = 60.0) 
             "pipeline": "Opposed + AMaZE + RL20 + optics; export: extended f16 Display P3 chroma-compressed "
                         "headroom 4 + sRGB8, full resolution",
             "open_develop_s": round(t1 - t0, 2), "opens_ok": sum(1 for v in opened if v == 0),
+            "develops_per_s": round(count / (t1 - t0), 2),
             "export_s": round(t3 - t2, 3), "exports_ok": sum(1 for v in statuses if v == 0),
             "exports_per_s": round(count / (t3 - t2), 2), "export_mp_per_s": round(count * mp / (t3 - t2), 1),
             "export_latency_p50_ms": round(float(np.percentile(latencies, 50)), 1) if latencies else None,
@@ -704,78 +819,116 @@ def export_stream(args, count: int = 24, window: int = 3, cap_gb: float = 60.0) 
             "evictions": int(st.evictions)}
 
 
-def cpu_develop_band(rows: int, args) -> tuple[float, float]:
-    """Run the oracle pipeline on a `rows`-high band of the 24 MP workload; returns (seconds, fraction)."""
+# ------------------------------------------------------------------ the CPU side
+def probe_cargo() -> str:
+    """The reference's own bench needs cargo; record whether this host has it."""
+    path = shutil.which("cargo")
+    if not path:
+        return "cargo absent on this host (the Rust reference and its pipeline_stages bench cannot be built)"
+    try:
+        return subprocess.run([path, "--version"], capture_output=True, text=True, timeout=20).stdout.strip()
+    except (OSError, subprocess.TimeoutExpired) as e:
+        return f"cargo present but failed: {e}"
+
+
+def native_libraries() -> list[str]:
+    """Shared libraries of this repository mapped into this process."""
+    found = set()
+    try:
+        for line in open("/proc/self/maps"):
+            path = line.split()[-1] if line.strip() else ""
+            if path.startswith(ROOT) and path.endswith(".so"):
+                found.add(os.path.relpath(path, ROOT))
+    except OSError:
+        pass
+    return sorted(found)
+
+
+def oracle_develops(dv, raw, steps: int, warmup: int = 1) -> tuple[list[float], dict, dict]:
+    """`warmup` + `steps` whole develops of `raw` through the oracle; returns the per-step seconds,
+    the median per-stage ms (StageTimings names) and the last develop's outputs."""
+    from oracle import develop as od
     from oracle import oracle as o
-    from rohditor_gb300.workloads import full_24mp, preview_dimensions
 
-    wl = full_24mp(demosaic=args.demosaic, iterations=args.iterations, highlight=args.highlight)
-    W, H = wl.width, wl.height
-    rng = np.random.default_rng(5)
-    # A band with the workload's statistics: smooth scene, ~5% clipped blobs, 14-bit levels.
-    yy, xx = np.mgrid[0:rows, 0:W].astype(np.float32)
-    scene = 0.35 + 0.2 * np.sin(xx / 97.0) * np.cos(yy / 61.0)
-    blobs = ((xx % 900 - 450) ** 2 + (yy % 700 - 350) ** 2) < 110 ** 2
-    scene[blobs] = 2.0
-    raw = np.clip(512 + scene * 15871 + rng.normal(0, 20, scene.shape), 0, 16383).astype(np.uint16)
-    odesc = o.sensor_desc(W, rows, W, (0, 0, W, rows), 0, [512.0], (1, 1), [16383.0])
-    t0 = time.perf_counter()
-    m, pattern = o.normalize(raw, odesc)
-    if args.highlight == "opposed":
-        m, _, _, _ = o.opposed(m, pattern, wl.sensor.detection_levels, wl.sensor.neutral_ceiling)
-    else:
-        m, _ = o.clip(m, pattern, wl.sensor.clip_levels)
-    algo = {"bilinear": 0, "mhc": 1, "rcd": 2, "amaze": 3}[args.demosaic]
-    rgb = o.demosaic(m, pattern, wl.sensor.demosaic_balance, algo)
-    cap = wl.capture
-    rgb = o.capture(rgb, cap.amount, cap.radius, cap.noise_protection, cap.ceilings, cap.iterations)
-    plan = o.optics_plan(W, rows, 2, (-0.02, 0.005, 0.0), 1, (1.0003, 0, 0), (0.9997, 0, 0))
-    plan.vignetting_model = 1
-    for k, v in enumerate(wl.optics.vignetting_k):
-        plan.vignetting[k] = v
-    rgb = o.optics_apply(plan, rgb)
-    tw, th = preview_dimensions(W, rows, 2560)
-    base = o.camera_matrix(o.white_balance(o.area_reduce(rgb, (tw, th)), wl.color.wb_gains),
-                           wl.color.camera_to_rec2020)
-    c = wl.color
-    x = o.adjust(base, c.exposure_ev, c.base_lut, c.tone_lut, c.saturation, c.vibrance, c.hsl, c.grading)
-    o.histogram(o.display_srgb8(x))
-    return time.perf_counter() - t0, rows / H
+    luts = {"base": o.standard_base_lut()}
+    secs, stages, res = [], {}, None
+    for i in range(warmup + steps):
+        t = time.perf_counter()
+        res = od.develop(dv, raw, luts)
+        dt = time.perf_counter() - t
+        if i >= warmup:
+            secs.append(dt)
+            for k, v in res["timings"].items():
+                stages.setdefault(k, []).append(v)
+    return secs, {k: round(statistics.median(v), 1) for k, v in stages.items()}, res
 
 
-def cpu_baseline(args, sample_rows: int) -> dict:
-    secs, frac = cpu_develop_band(sample_rows, args)
+def parity_summary(gpu: dict, ref: dict) -> dict:
+    """Per-stage agreement of one GPU develop with the oracle's develop of the same mosaic,
+    against the tolerances the tests hold."""
+    src = float(np.max(np.abs(gpu["source"] - ref["source"])))
+    base = float(np.max(np.abs(gpu["base"] - ref["base"])))
+    d8 = np.abs(gpu["srgb8"].astype(np.int16) - ref["srgb8"].astype(np.int16))
+    from oracle import oracle as o
+
+    own_hist, _ = o.histogram(gpu["srgb8"])
+    return {
+        "developed_rgb": {"max_abs": src, "bound": 5e-4, "ok": src <= 5e-4,
+                          "note": "Opposed + demosaic + RL K iterations, white-normalised scale"},
+        "preview_base": {"max_abs": base, "bound": 5e-4 * max(1.0, float(np.max(np.abs(ref["base"])))),
+                         "note": "optics + area reduction + WB/matrix of the GPU's own source vs the oracle's"},
+        "srgb8": {"max_lsb": int(d8.max()), "frac_differing": float((d8 > 0).mean()),
+                  "ok": int(d8.max()) <= 1 and float((d8 > 0).mean()) <= 1e-3},
+        "histogram_of_own_output": {"exact": bool(np.array_equal(gpu["hist"], own_hist))},
+    }
+
+
+def cpu_baseline(dv, kept: dict | None, seconds: float = 10.0) -> tuple[dict, dict | None]:
+    """The oracle developing the same seeded mosaic (generated by the oracle's own generator) on all
+    host cores, repeated for about `seconds`; with the GPU's outputs of that mosaic, the parity."""
+    from oracle import develop as od
+
+    raw = od.mosaic(dv)
+    # One develop to learn the time, then as many as fit in `seconds` (at least 2).
+    first, _, _ = oracle_develops(dv, raw, steps=1, warmup=0)
+    reps = max(2, int(seconds / max(first[0], 1e-3)))
+    secs, stages, res = oracle_develops(dv, raw, steps=reps, warmup=0)
     cores = os.cpu_count() or 1
-    return {"value": round(frac / secs, 4), "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"oracle (C++ restatement of the reference CPU pipeline, OpenMP on {cores} threads) on a "
-                      f"6048x{sample_rows} band of the 24 MP workload ({frac:.3f} of a develop) in {secs:.1f} s; "
-                      f"value = develop-fraction / seconds"}
+    cpu = {"value": round(len(secs) / sum(secs), 4), "unit": UNIT, "cores": cores, "kind": "port",
+           "sample": f"{len(secs)} whole develops of the same seeded {dv.scene.width}x{dv.scene.height} mosaic through "
+                     f"the oracle (C++ restatement of the reference CPU pipeline, OpenMP on {cores} threads), "
+                     f"{sum(secs):.1f} s", "stage_ms": stages, "cargo": probe_cargo()}
+    parity = parity_summary(kept, res) if kept is not None else None
+    return cpu, parity
 
 
 def run_reference(args, world, rank, pg):
+    """The reference algorithm on the host cores: the oracle develops the whole headline mosaic each step."""
     if rank != 0:
         return None
-    rows = args.cpu_rows
-    times = []
-    for i in range(args.warmup + args.steps):
-        secs, frac = cpu_develop_band(rows, args)
-        if i >= args.warmup:
-            times.append(secs)
-    total = sum(times)
-    value = args.steps * frac / total
+    from oracle import develop as od
+
+    dv = spec.full_24mp(demosaic=args.demosaic, iterations=args.iterations, highlight=args.highlight,
+                        width=args.width, height=args.height)
+    raw = od.mosaic(dv)
+    secs, stages, _ = oracle_develops(dv, raw, steps=args.steps, warmup=args.warmup)
+    total = sum(secs)
+    value = args.steps / total
     cores = os.cpu_count() or 1
     cpu = {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": "port",
-           "sample": f"6048x{rows} band ({frac:.3f} of a 24 MP develop) per step through the oracle"}
+           "sample": f"whole {dv.scene.width}x{dv.scene.height} develop of the same seeded mosaic per step through the "
+                     f"oracle (the Rust reference cannot be built: {probe_cargo()})"}
     return {
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps / frac, 1),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded)",
-        "config": {"workload": f"full_24mp 6048x4024, {args.highlight} + {args.demosaic} + RL{args.iterations} + "
-                               f"optics + area->2560x1703 + colour + sRGB8 + histogram (CPU restatement; the Rust "
-                               f"reference cannot be built on this image)"},
+        "data": "synthetic (seeded generator)",
+        "config": {"workload": dv.describe(), "mp_per_s": round(value * dv.scene.width * dv.scene.height / 1e6, 2),
+                   "parallelism": "host cores (OpenMP), rank 0 only"},
         "cpu_baseline": cpu,
+        "stage_ms": stages,
         "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "native_so_loaded": native_libraries(),
     }
 
 
@@ -788,19 +941,25 @@ def main():
     p.add_argument("--highlight", default="opposed", choices=["opposed", "clip"])
     p.add_argument("--demosaic", default="amaze", choices=["amaze", "rcd", "mhc"])
     p.add_argument("--iterations", type=int, default=10)
-    p.add_argument("--cpu-rows", type=int, default=256)
     p.add_argument("--width", type=int, default=6048, help="mosaic width (smaller cases for profiling)")
     p.add_argument("--height", type=int, default=4024)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-configs", action="store_true", help="skip the 3 MP, RCD and MHC configurations")
     p.add_argument("--no-edit-latency", action="store_true", help="skip the served-vs-plain edit latency trace")
     p.add_argument("--no-batched", action="store_true", help="skip the uneven batched-develop measurement")
     p.add_argument("--no-export", action="store_true", help="skip the full-resolution output measurement")
-    p.add_argument("--export-stream", type=int, default=0, metavar="N",
-                   help="also run the large-sensor export stream through the served loop with N images")
-    p.add_argument("--cpu-baseline-rows", type=int, default=2048,
-                   help="band height of the CPU baseline sample (2048 rows = half a 24 MP develop)")
+    p.add_argument("--batch-images", type=int, default=48, help="images in the uneven batch")
+    p.add_argument("--export-stream", type=int, default=24, metavar="N",
+                   help="images in the large-sensor export stream through the served loop (0 skips it)")
+    p.add_argument("--cpu-baseline-seconds", type=float, default=10.0,
+                   help="about how long the CPU baseline develops the mosaic")
     args = p.parse_args()
-    world, rank, local, pg = dist_setup(args.gpus)
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(relaunch_with_ranks(args.gpus))
+    world, rank, local, pg = dist_setup()
+    if world != args.gpus:
+        print(f"bench: --gpus {args.gpus} but {world} ranks were launched", file=sys.stderr)
+        sys.exit(2)
     if args.impl == "reference":
         line = run_reference(args, world, rank, pg)
     else:

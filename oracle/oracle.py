@@ -63,6 +63,15 @@ class OpticsDesc(ctypes.Structure):
     ]
 
 
+class SynthDesc(ctypes.Structure):
+    _fields_ = [
+        ("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("cfa", ctypes.c_int32), ("bits", ctypes.c_uint32),
+        ("black", ctypes.c_float), ("white", ctypes.c_float), ("clip_fraction", ctypes.c_float),
+        ("gains", ctypes.c_float * 3), ("seed", ctypes.c_uint64), ("highlight_blobs", ctypes.c_int32),
+        ("hot_pixel_fraction", ctypes.c_float),
+    ]
+
+
 class AdjustDesc(ctypes.Structure):
     _fields_ = [
         ("exposure_ev", ctypes.c_float), ("base_lut", F32P), ("light_lut", F32P), ("extended", ctypes.c_int),
@@ -119,6 +128,7 @@ def load():
             "ro_adjust_apply": (None, [F32P, ctypes.c_size_t, ctypes.POINTER(AdjustDesc)]),
             "ro_standard_base_lut": (None, [F32P]),
             "ro_light_tone_lut": (None, [ctypes.c_float] * 5 + [F32P]),
+            "ro_synth_mosaic": (ctypes.c_int, [ctypes.POINTER(SynthDesc), U16P]),
             "ro_display_srgb8": (None, [F32P, ctypes.c_size_t, U8P]),
             "ro_histogram": (None, [U8P, ctypes.c_size_t, U64P, U64P]),
             "ro_set_exact_math": (None, [ctypes.c_int]),
@@ -439,6 +449,24 @@ def adjust(rgb: np.ndarray, exposure_ev=0.0, base_lut=None, tone_lut=None, satur
 def standard_base_lut() -> np.ndarray:
     out = np.zeros(4096, dtype=np.float32)
     load().ro_standard_base_lut(ptr(out))
+    return out
+
+
+def synth_mosaic(width, height, cfa=0, bits=14, black=512.0, white=16383.0, clip_fraction=0.05,
+                 gains=(0.5, 1.0, 0.625), seed=2, highlight_blobs=True, hot_pixel_fraction=0.0) -> np.ndarray:
+    """The seeded synthetic Bayer mosaic [height][width] u16 (synth.cpp), equal bit for bit to the
+    library's device generator for the same description."""
+    d = SynthDesc()
+    d.width, d.height, d.cfa, d.bits = width, height, cfa, bits
+    d.black, d.white, d.clip_fraction = black, white, clip_fraction
+    for c in range(3):
+        d.gains[c] = gains[c]
+    d.seed = seed
+    d.highlight_blobs = 1 if highlight_blobs else 0
+    d.hot_pixel_fraction = hot_pixel_fraction
+    out = np.empty((height, width), dtype=np.uint16)
+    if load().ro_synth_mosaic(ctypes.byref(d), out.ctypes.data_as(U16P)) != 0:
+        raise ValueError("synthetic mosaic must be at least 2x2")
     return out
 
 

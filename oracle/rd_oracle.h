@@ -134,6 +134,21 @@ void ro_source_coordinate(int w, int h, int orientation, int x, int y, int* sx, 
  * clipped_fallback, invalid}. Returns 0, or -1 for an invalid geometry or headroom. */
 int ro_render_output(const float* rgb, int w, int h, const ro_output* o, void* out, uint64_t gamut[5]);
 
+/* ---- seeded synthetic scenes (synth.cpp) ---- */
+typedef struct ro_synth {
+  uint32_t width, height;
+  int32_t cfa;
+  uint32_t bits;
+  float black, white;
+  float clip_fraction;
+  float gains[3];
+  uint64_t seed;
+  int32_t highlight_blobs;
+  float hot_pixel_fraction;
+} ro_synth;
+/* out: [height][width] u16. Returns 0, or -1 below 2x2. */
+int ro_synth_mosaic(const ro_synth* desc, uint16_t* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -2,13 +2,13 @@
 built from csrc/ into _lib/librd_gpu.so, with a host-side mirror of the
 reference's `rohditor-gpu` processor interface."""
 
-from .processor import (CaptureContract, ColorContract, Device, GamutDiagnostics, GpuBase, GpuDevelopedSource,
+from .processor import (CaptureContract, capture_ceilings, ColorContract, Device, GamutDiagnostics, GpuBase, GpuDevelopedSource,
                         GpuPreviewError, GpuPreviewProcessor, GpuSensorProcessor, GpuSpatialProcessor, Histogram,
                         OpticsExecution, OutputSpec, RlLaunchShape, SensorDescription, Stages, clip_levels,
                         light_tone_lut, opposed_levels, rl_launch_shape, standard_base_lut)
 
 __all__ = [
-    "CaptureContract", "ColorContract", "Device", "GamutDiagnostics", "GpuBase", "GpuDevelopedSource", "GpuPreviewError",
+    "CaptureContract", "capture_ceilings", "ColorContract", "Device", "GamutDiagnostics", "GpuBase", "GpuDevelopedSource", "GpuPreviewError",
     "GpuPreviewProcessor", "GpuSensorProcessor", "GpuSpatialProcessor", "Histogram", "OpticsExecution",
     "OutputSpec", "RlLaunchShape", "SensorDescription", "Stages", "clip_levels", "light_tone_lut", "opposed_levels", "rl_launch_shape",
     "standard_base_lut",

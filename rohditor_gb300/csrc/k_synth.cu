@@ -3,6 +3,9 @@
 // A counter-based generator (SplitMix64 keyed by seed, pixel index and draw
 // number) makes every sample a pure function of its coordinates, so a mosaic
 // of any size is produced in one parallel pass and is identical run to run.
+// The per-pixel arithmetic uses no library function whose last bit differs
+// between host and device, so a host build of the same steps (the CPU oracle
+// has one) reproduces the mosaic bit for bit.
 // Scene: smooth colour gradients, random sharp-edged rectangles and 1-pixel
 // lines, optional Gaussian highlight blobs whose cores clip, then photon
 // (Poisson, 0.5 e-/DN) and Gaussian read noise (sigma 3 DN), quantised to u16
@@ -48,16 +51,48 @@ __host__ __device__ inline unsigned long long splitmix(unsigned long long x) {
   x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
   return x ^ (x >> 31);
 }
+__host__ __device__ inline unsigned long long draw_bits(unsigned long long seed, unsigned long long index,
+                                                        unsigned draw) {
+  return splitmix(seed ^ splitmix(index * 0x100000001B3ull + draw));
+}
+// Every value below is built from integer operations and IEEE f32 +, -, *, /
+// and sqrt, each rounded on its own (no contraction on either side), so the
+// host and the device give the same bits.
+//
+// A uniform in (0, 1) from 23 bits of a draw: (k + 1/2) / 2^23, exact.
+__host__ __device__ inline float unit_from(unsigned long long bits) {
+  return ((float)(bits & 0x7FFFFFull) + 0.5f) * 1.1920928955078125e-7f;
+}
 __host__ __device__ inline float uniform(unsigned long long seed, unsigned long long index, unsigned draw) {
-  const unsigned long long h = splitmix(seed ^ splitmix(index * 0x100000001B3ull + draw));
-  return (float)((h >> 40) + 0.5) * (1.0f / 16777216.0f);  // (0, 1)
+  return unit_from(draw_bits(seed, index, draw) >> 41);
+}
+// A standard normal deviate as the Irwin-Hall sum of twelve uniforms minus 6
+// (mean 0, variance 1, support [-6, 6]); two uniforms per draw, from bits
+// 41..63 and 18..40.
+__host__ __device__ inline float normal(unsigned long long seed, unsigned long long index, unsigned draw) {
+  float sum = 0.0f;
+  for (unsigned j = 0; j < 6; ++j) {
+    const unsigned long long h = draw_bits(seed, index, draw + j);
+    sum += unit_from(h >> 41);
+    sum += unit_from(h >> 18);
+  }
+  return sum - 6.0f;
+}
+// e^-x for 0 <= x < 80: x = k ln2 + r with k = trunc(x / ln2), then
+// 2^-k (exact halvings) times the Taylor series of e^-r to the r^12 term,
+// evaluated by Horner's rule.
+__host__ __device__ inline float exp_neg(float x) {
+  const float ln2 = 0.693147182f;
+  const int k = (int)(x / ln2);
+  const float r = x - (float)k * ln2;
+  float t = 1.0f;
+  for (int n = 12; n >= 1; --n) t = 1.0f - r * t / (float)n;
+  for (int i = 0; i < k; ++i) t *= 0.5f;
+  return t;
 }
 
-__device__ float normal(unsigned long long seed, unsigned long long index, unsigned draw) {
-  const float u1 = uniform(seed, index, draw), u2 = uniform(seed, index, draw + 1);
-  return sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2);
-}
-
+// Draw numbers of one pixel: photon noise 0..5 (normal) or 16.. (Poisson
+// products), read noise 8..13, hot pixel 300.
 __global__ void synth_kernel(const SynthParams* __restrict__ pp, uint16_t* __restrict__ out) {
   const SynthParams& p = *pp;
   const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
@@ -82,7 +117,7 @@ __global__ void synth_kernel(const SynthParams* __restrict__ pp, uint16_t* __res
     const float dx = (float)x - b.x, dy = (float)y - b.y;
     const float d2 = dx * dx + dy * dy;
     const float e = d2 * b.inv2s2;
-    if (e < 12.0f) refl += b.amp * expf(-e);
+    if (e < 12.0f) refl += b.amp * exp_neg(e);
   }
   // Camera response of this channel, in DN above black.
   const float signal = fmaxf(refl * p.gains[ch] * p.span, 0.0f);
@@ -94,16 +129,16 @@ __global__ void synth_kernel(const SynthParams* __restrict__ pp, uint16_t* __res
     electrons = electrons_mean + sqrtf(electrons_mean) * normal(p.seed, index, 0);
   } else {
     // Knuth's product method for small means.
-    const float limit = expf(-electrons_mean);
-    float prod = uniform(p.seed, index, 0);
+    const float limit = exp_neg(electrons_mean);
+    float prod = uniform(p.seed, index, 16);
     int k = 0;
     while (prod > limit && k < 200) {
       ++k;
-      prod *= uniform(p.seed, index, 8 + k);
+      prod *= uniform(p.seed, index, 16 + k);
     }
     electrons = (float)k;
   }
-  float dn = electrons / 0.5f + 3.0f * normal(p.seed, index, 4);
+  float dn = electrons / 0.5f + 3.0f * normal(p.seed, index, 8);
   if (p.hot_fraction > 0.0f && uniform(p.seed, index, 300) < p.hot_fraction) dn = p.span * 2.0f;
   float value = rintf(p.black + dn);
   value = fminf(fmaxf(value, 0.0f), p.white);
@@ -150,7 +185,7 @@ Status run_synth(Context& ctx, const rd_synth_desc& d, uint16_t* out) {
   if (d.clip_fraction > 0.0f) {
     const int n = d.highlight_blobs ? 48 : 96;
     const float amp = 3.0f;
-    const float area_per = std::log(amp / 0.55f) * 3.14159265f;
+    const float area_per = 1.6964493f * 3.14159265f;  // ln(3 / 0.55) * pi
     const float s2 = d.clip_fraction * (float)p.W * (float)p.H / (n * area_per);
     p.nblobs = n;
     for (int k = 0; k < n; ++k) {

@@ -114,6 +114,18 @@ def opposed_levels(threshold: float, as_shot) -> tuple[tuple[float, ...], tuple[
     return (float(level),) * 3, tuple(float(np.float32(common / x)) for x in g)
 
 
+def capture_ceilings(highlight: str, threshold: float, gains) -> tuple[float, float, float]:
+    """Capture-sharpening mask ceilings (crates/core/src/pipeline/detail.rs:323-337): Clip's common
+    ceiling threshold * min(gains) / gain (no safety margin), Opposed's detection threshold, else 1."""
+    if highlight == "clip":
+        g = [np.float32(x) for x in gains]
+        common = np.float32(np.float32(threshold) * min(g[0], g[1], g[2]))
+        return tuple(float(np.float32(common / x)) for x in g)
+    if highlight == "opposed":
+        return (float(np.float32(threshold)),) * 3
+    return (1.0, 1.0, 1.0)
+
+
 @dataclass
 class CaptureContract:
     """CaptureSharpeningContract (sharpening.rs:17-68) with an explicit iteration count."""
