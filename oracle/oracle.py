@@ -308,6 +308,8 @@ def opposed(mosaic: np.ndarray, pattern: int, levels, ceiling=None):
     count = ctypes.c_uint32()
     rc = load().ro_opposed(ptr(m), w, h, pattern, ptr(lv), ptr(ce) if ce is not None else None,
                            ptr(stats, ctypes.c_uint64), ptr(labels, ctypes.c_uint32), ctypes.byref(count))
+    if rc == -2:
+        raise ValueError("invalid level: levels must be finite and positive")
     if rc != 0:
         raise ValueError("non-finite sample")
     return m, stats, labels, count.value

@@ -246,6 +246,12 @@ extern "C" int ro_opposed(float* m, int w, int h, int pattern, const float level
                           uint64_t stats[9], uint32_t* labels_out, uint32_t* region_count) {
   for (int k = 0; k < 9; ++k) stats[k] = 0;
   if (region_count) *region_count = 0;
+  // ChannelDetectionLevels / ChannelClipLevels::validate (crates/highlight/src/lib.rs:63-118):
+  // every level finite and positive, checked before any sample is read.
+  for (int c = 0; c < 3; ++c) {
+    if (!std::isfinite(levels[c]) || !(levels[c] > 0.0f)) return -2;
+    if (ceiling && (!std::isfinite(ceiling[c]) || !(ceiling[c] > 0.0f))) return -2;
+  }
   // validate_visible_samples, opposed.rs:182-219
   uint64_t suspected = 0, sc[3] = {0, 0, 0};
   for (int y = 0; y < h; ++y)
