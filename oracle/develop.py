@@ -119,6 +119,7 @@ def develop(dv: spec.Develop, raw: np.ndarray, luts: dict | None = None) -> dict
         m, stats, _, _ = o.opposed(m, pattern, det, ceiling)
     elif dv.highlight == "clip":
         m, stats = o.clip(m, pattern, clip_levels(dv.highlight_threshold, dv.wb_gains))
+    highlighted = m
     clock.lap("highlight_processing")
     rgb = o.demosaic(m, pattern, s.as_shot, DEMOSAIC_CODES[dv.demosaic])
     clock.lap("demosaic")
@@ -149,5 +150,5 @@ def develop(dv: spec.Develop, raw: np.ndarray, luts: dict | None = None) -> dict
     clock.lap("output_conversion")
     timings = dict(clock.ms)
     timings["total"] = 1e3 * (time.perf_counter() - start)
-    return {"source": source, "base": base, "adjusted": x, "srgb8": srgb8, "hist": hist, "clipped": clipped,
+    return {"highlighted": highlighted, "source": source, "base": base, "adjusted": x, "srgb8": srgb8, "hist": hist, "clipped": clipped,
             "highlight_stats": stats, "timings": timings}
