@@ -220,14 +220,22 @@ class CudaExecutor : public Executor {
   }
   Status ensure_outputs(ServedImage& im) override {
     if (im.d_out) return Status{};
+    // All three buffers are allocated before any is published on the image,
+    // so a failed allocation leaves the image without outputs and nothing leaks.
     void* p = nullptr;
-    RD_TRY(from_code(rd_device_alloc(dev, im.out_bytes(), &p), "output allocation failed"));
-    im.d_hist = static_cast<unsigned long long*>(p);
-    im.d_out = reinterpret_cast<uint8_t*>(im.d_hist + 1024);
     void* a = nullptr;
     void* b = nullptr;
-    RD_TRY(from_code(rd_host_alloc(3 * (size_t)im.tw * im.th, &a), "pinned allocation failed"));
-    RD_TRY(from_code(rd_host_alloc(3 * (size_t)im.tw * im.th, &b), "pinned allocation failed"));
+    Status st = from_code(rd_device_alloc(dev, im.out_bytes(), &p), "output allocation failed");
+    if (st.ok()) st = from_code(rd_host_alloc(3 * (size_t)im.tw * im.th, &a), "pinned allocation failed");
+    if (st.ok()) st = from_code(rd_host_alloc(3 * (size_t)im.tw * im.th, &b), "pinned allocation failed");
+    if (!st.ok()) {
+      if (p) rd_device_free(dev, p);
+      if (a) rd_host_free(a);
+      if (b) rd_host_free(b);
+      return st;
+    }
+    im.d_hist = static_cast<unsigned long long*>(p);
+    im.d_out = reinterpret_cast<uint8_t*>(im.d_hist + 1024);
     im.h_front = static_cast<uint8_t*>(a);
     im.h_back = static_cast<uint8_t*>(b);
     return Status{};

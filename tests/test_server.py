@@ -303,3 +303,84 @@ def test_served_edits_match_the_render_entry_point(device):
         base.release()
         src.release()
     server.close()
+
+
+@pytest.mark.gpu
+def test_edits_overlapping_a_develop_equal_their_solo_renders(device):
+    """Continuous batching: edits of three images submitted while a large
+    develop of a fourth image runs on the develop lane render on the render
+    lane meanwhile (they finish before the develop does), and every result is
+    the same as alone: each edited image's output equals rd_render of its base
+    with its last settings, and the developed image's re-render equals a solo
+    develop + spatial pass + render with the new capture settings
+    (the newest-wins mailbox of crates/engine/src/coordinator/scheduler.rs:44-166)."""
+    from rohditor_gb300 import GpuPreviewProcessor, GpuSensorProcessor, GpuSpatialProcessor, standard_base_lut
+    from rohditor_gb300.workloads import CAMERA_TO_REC2020, hsl_bands, sixteen_knot_curve
+
+    server = PreviewServer(0)
+    images = {}
+    for i in range(3):
+        raw, desc, cap, optics, wb = _image(w=640, h=480, seed=30 + i)
+        images[i] = (raw, desc, cap, optics, wb, (320, 240))
+    big = 3
+    raw, desc, cap, optics, wb = _image(w=8256, h=5504, seed=40)
+    images[big] = (raw, desc, cap, optics, wb, (2560, 1707))
+    for i, (raw, desc, cap, optics, wb, target) in images.items():
+        server.open(i, raw, desc, cap, optics, target, wb, CAMERA_TO_REC2020)
+    server.drain(120000)
+    assert all(r["status"] == RD_OK for r in server.poll(64))
+
+    def colour(i, k):
+        return ColorContract(wb_gains=images[i][4], camera_to_rec2020=CAMERA_TO_REC2020, exposure_ev=0.1 * k - 0.2,
+                             base_lut=standard_base_lut(), tone_lut=sixteen_knot_curve(seed=7 * i + k),
+                             hsl=hsl_bands(seed=11 * i + k))
+
+    big_colour = colour(big, 0)
+    server.submit_edit(big, 1, big_colour)
+    server.drain(60000)
+    server.poll(64)
+    new_cap = CaptureContract(amount=0.8, radius=0.9, noise_protection=0.3, ceilings=images[big][2].ceilings,
+                              iterations=20)
+    submitted = {}
+    t0 = time.perf_counter()
+    dev_id = server.submit_develop(big, 2, new_cap, images[big][3])
+    submitted[dev_id] = 0.0
+    last = {}
+    for k in range(1, 4):
+        for i in range(3):
+            rid = server.submit_edit(i, 1 + k, colour(i, k))
+            submitted[rid] = 1e3 * (time.perf_counter() - t0)
+            last[i] = (rid, k)
+        time.sleep(0.002)
+    server.drain(120000)
+    res = {r["request_id"]: r for r in server.poll(256)}
+    develop = res[dev_id]
+    assert develop["kind"] == DEVELOP and develop["status"] == RD_OK
+    develop_done = develop["latency_ms"]
+    overlapped = [rid for rid, r in res.items()
+                  if r["kind"] == EDIT and r["status"] == RD_OK and submitted[rid] + r["latency_ms"] < develop_done]
+    assert overlapped, "no edit finished while the develop was running"
+
+    preview = GpuPreviewProcessor(device)
+    for i in range(3):
+        raw, desc, cap, optics, wb, target = images[i]
+        rid, k = last[i]
+        assert res[rid]["status"] == RD_OK
+        src = GpuSensorProcessor(device).develop(raw, desc, cap)
+        base = GpuSpatialProcessor(device).reduce_preview(src, optics, target, wb, CAMERA_TO_REC2020)
+        ref, hist = preview.render(base, colour(i, k))
+        out, served_hist, rev = server.read_output(i)
+        assert rev == 1 + k
+        assert np.array_equal(out, ref)
+        assert np.array_equal(served_hist[:256], hist.red) and np.array_equal(served_hist[768:], hist.luminance)
+        base.release()
+        src.release()
+    raw, desc, cap, optics, wb, target = images[big]
+    src = GpuSensorProcessor(device).develop(raw, desc, new_cap)
+    base = GpuSpatialProcessor(device).reduce_preview(src, optics, target, wb, CAMERA_TO_REC2020)
+    ref, _ = preview.render(base, big_colour)
+    out, _, _ = server.read_output(big)
+    assert np.array_equal(out, ref)
+    base.release()
+    src.release()
+    server.close()
