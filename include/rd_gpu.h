@@ -161,6 +161,19 @@ const char* rd_ctx_last_error(const rd_ctx* ctx);
 rd_status rd_ctx_synchronize(rd_ctx* ctx);
 /* Number of this library's kernels launched on the context so far. */
 uint64_t rd_ctx_kernel_launches(const rd_ctx* ctx);
+/* Test facility for the bounded device waits (no reference counterpart).
+ * Every spin-wait of this library's kernels gives up after an iteration
+ * limit, records why in the context's error word and returns, so the call
+ * fails with RD_INVALID_INPUT and the context stays usable. This setting
+ * makes a wait run out on purpose: `wait_limit` (0: the built-in limits)
+ * shortens every wait, and `withhold` names a completion the next calls
+ * never deliver: RD_WAIT_AMAZE_TILE (phase A of AMaZE tile 0 does not
+ * publish its slab, so its phase B waits) or RD_WAIT_RL_COPY (every block
+ * of the capture-sharpening kernels skips its first tensor copy but waits
+ * for it, then drains its other copies in flight). RD_WAIT_NONE restores
+ * normal operation. */
+enum { RD_WAIT_NONE = 0, RD_WAIT_AMAZE_TILE = 1, RD_WAIT_RL_COPY = 2 };
+rd_status rd_ctx_set_wait_test(rd_ctx* ctx, uint32_t wait_limit, int32_t withhold);
 
 /* ---- routing ---- */
 int rd_supports(const rd_sensor_desc* sensor);

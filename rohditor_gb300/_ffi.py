@@ -154,6 +154,7 @@ SIGNATURES = {
     "rd_ctx_last_error": (ctypes.c_char_p, [VOIDP]),
     "rd_ctx_synchronize": (ctypes.c_int, [VOIDP]),
     "rd_ctx_kernel_launches": (ctypes.c_uint64, [VOIDP]),
+    "rd_ctx_set_wait_test": (ctypes.c_int, [VOIDP, ctypes.c_uint32, ctypes.c_int32]),
     "rd_supports": (ctypes.c_int, [ctypes.POINTER(SensorDesc)]),
     "rd_develop": (ctypes.c_int, [VOIDP, U16P, ctypes.c_size_t, ctypes.POINTER(SensorDesc),
                                   ctypes.POINTER(DetailDesc), ctypes.POINTER(ctypes.c_uint32),

@@ -177,6 +177,8 @@ struct AmazeParams {
   unsigned int* error;
   unsigned* flags;         // per tile: 1 once its phase A is complete (zeroed per launch)
   unsigned* work;          // work-item counter (zeroed per launch)
+  unsigned wait_tries;     // iteration limit of the phase-B wait
+  int withhold_tile;       // a tile whose phase A does not publish (tests of the bounded wait), or -1
 };
 
 constexpr unsigned AMAZE_WAIT_TIMEOUT = 64u;
@@ -599,7 +601,7 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
     // Publish the slab: every thread's writes, then the tile's flag.
     __threadfence();
     __syncthreads();
-    if (t == 0) atomicExch(&prm.flags[tile], 1u);
+    if (t == 0 && tile != prm.withhold_tile) atomicExch(&prm.flags[tile], 1u);
     continue;
     }
 
@@ -607,7 +609,7 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
     if (t == 0) {
       unsigned tries = 0;
       while (load_acquire(&prm.flags[tile]) == 0u) {
-        if (++tries > (1u << 22)) {
+        if (++tries > prm.wait_tries) {
           atomicOr(prm.error, AMAZE_WAIT_TIMEOUT);
           break;
         }
@@ -1108,6 +1110,8 @@ Status run_amaze(Context& ctx, const MosaicSource& src, const float gains[3], fl
   prm.error = ctx.d_error;
   prm.flags = flags;
   prm.work = ctx.d_work;
+  prm.wait_tries = ctx.wait_limit ? ctx.wait_limit : AMAZE_DEFAULT_WAIT_TRIES;
+  prm.withhold_tile = ctx.wait_withhold == RD_WAIT_AMAZE_TILE ? 0 : -1;
   RD_LAUNCH(ctx, K_AMAZE, amaze_kernel<<<grid, THREADS, SMEM_BYTES, ctx.stream>>>(prm));
   RD_CUDA_TRY(cudaGetLastError());
   return Status{};

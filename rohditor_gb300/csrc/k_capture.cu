@@ -141,16 +141,56 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       "l"(map), "r"(x), "r"(y), "r"(smem_addr(bar))
       : "memory");
 }
-// Bounded wait for a block's copy: sets `failed` (and the error word) instead
-// of spinning forever.
+// Every thread's view of a kernel's tensor-copy barriers: the parity of each
+// barrier's next completion, which blocks have a copy issued and not yet
+// waited for, and whether a wait gave up. Each wait is bounded: after `tries`
+// polls it sets `failed` and the error word instead of spinning forever.
+// From then on no copy is issued, and before the block exits `drain` waits
+// (bounded again) for the copies still in flight, so no copy lands in shared
+// memory the block has released. All threads call issue_block / wait / drain
+// at the same points, so their views agree. `withhold` (tests of the bounded
+// wait) makes every block skip its first copy while still waiting for it.
 constexpr unsigned RL_TMA_TIMEOUT = 32u;
-__device__ __forceinline__ void tma_wait(unsigned long long* bar, unsigned parity, bool& failed, unsigned* error) {
-  if (failed) return;
-  for (int i = 0; i < (1 << 20); ++i)
-    if (mbar_try_wait(bar, parity)) return;
-  failed = true;
-  atomicOr(error, RL_TMA_TIMEOUT);
-}
+struct CopyWaits {
+  unsigned phases = 0, pending = 0, tries;
+  bool failed = false, withhold;
+  unsigned* error;
+  __device__ CopyWaits(unsigned tries_, bool withhold_, unsigned* error_)
+      : tries(tries_), withhold(withhold_), error(error_) {}
+  // Whether block b's copy is issued now (thread 0 then issues it).
+  __device__ __forceinline__ bool issue_block(int b) {
+    if (failed) return false;
+    if (withhold) {
+      withhold = false;
+      return false;
+    }
+    pending |= 1u << b;
+    return true;
+  }
+  __device__ __forceinline__ bool poll(unsigned long long* bar, int b) {
+    const unsigned parity = (phases >> b) & 1u;
+    for (unsigned i = 0; i < tries; ++i)
+      if (mbar_try_wait(bar, parity)) {
+        phases ^= 1u << b;
+        pending &= ~(1u << b);
+        return true;
+      }
+    return false;
+  }
+  __device__ __forceinline__ void wait(unsigned long long* bar, int b) {
+    if (failed) return;
+    if (!poll(bar, b)) {
+      failed = true;
+      atomicOr(error, RL_TMA_TIMEOUT);
+    }
+  }
+  // After a failed wait: the copies still in flight, each waited for (bounded).
+  __device__ __forceinline__ void drain(unsigned long long* bars, int n) {
+    if (!failed) return;
+    for (int b = 0; b < n; ++b)
+      if (pending & (1u << b)) poll(&bars[b], b);
+  }
+};
 
 __device__ __forceinline__ void cp_async4(float* smem, const float* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
@@ -202,7 +242,7 @@ __global__ void __launch_bounds__(128) rl_stream_kernel(const float* __restrict_
                                                         float* __restrict__ est_out, int W, int H, int strips,
                                                         int seg_h, int items, const Taps taps,
                                                         const __grid_constant__ CUtensorMap est_map, int use_tma,
-                                                        unsigned* error) {
+                                                        unsigned* error, unsigned wait_tries, int withhold) {
   using G = StreamGeom<R>;
   constexpr int T = G::T, SW = G::SW, QW = G::QW, EW = G::EW, BH = G::BH;
   extern __shared__ __align__(128) float4 rl_smem_raw[];
@@ -218,8 +258,7 @@ __global__ void __launch_bounds__(128) rl_stream_kernel(const float* __restrict_
     }
     __syncthreads();
   }
-  unsigned phases = 0;  // parity of the next completion of each block's barrier
-  bool tma_failed = false;
+  CopyWaits cw(wait_tries, withhold != 0, error);
   for (int item = blockIdx.x; item < items; item += gridDim.x) {
     const int x0 = (item % strips) * SW, y0 = (item / strips) * seg_h;
     const int y1 = min(y0 + seg_h, H);
@@ -243,8 +282,8 @@ __global__ void __launch_bounds__(128) rl_stream_kernel(const float* __restrict_
     auto issue = [&](int r0, int r1) {
       if (r0 >= r1) return;
       if (tma) {
-        if (tid == 0) {
-          const int b = ((r0 - ebase) / BH) % 3;
+        const int b = ((r0 - ebase) / BH) % 3;
+        if (cw.issue_block(b) && tid == 0) {
           asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
           mbar_expect_tx(&S.bar[b], BH * G::EWP * sizeof(float));
           tma_load_2d(S.e[b * BH], &est_map, xal, r0, &S.bar[b]);
@@ -287,11 +326,7 @@ __global__ void __launch_bounds__(128) rl_stream_kernel(const float* __restrict_
       issue(e_hi, min(e_hi + BH, e_end));
       cp_async_commit();
       cp_async_wait1();
-      if (tma && e_hi > e_next) {
-        const int b = ((e_next - ebase) / BH) % 3;
-        tma_wait(&S.bar[b], (phases >> b) & 1u, tma_failed, error);
-        phases ^= 1u << b;
-      }
+      if (tma && e_hi > e_next) cw.wait(&S.bar[((e_next - ebase) / BH) % 3], ((e_next - ebase) / BH) % 3);
       __syncthreads();
       // 1. horizontal pass of blur #1 on rows [e_next, e_hi)
       const int eslot = (e_next - ebase) % G::RIN;  // first slot of this step's block
@@ -390,6 +425,7 @@ __global__ void __launch_bounds__(128) rl_stream_kernel(const float* __restrict_
     asm volatile("cp.async.wait_all;\n" ::: "memory");
     __syncthreads();
   }
+  if (use_tma) cw.drain(S.bar, 3);
 }
 
 template <int R>
@@ -410,7 +446,8 @@ Status launch_rl_iter(Context& ctx, const float* est, const float* guide, float*
   CUtensorMap none{};
   RD_LAUNCH(ctx, K_RL_ITER, rl_stream_kernel<R><<<grid, 128, smem, ctx.stream>>>(
                                 est, guide, out, W, H, strips, seg_h, items, taps, est_map ? *est_map : none,
-                                est_map ? 1 : 0, ctx.d_error));
+                                est_map ? 1 : 0, ctx.d_error, ctx.wait_limit ? ctx.wait_limit : RL_DEFAULT_WAIT_TRIES,
+                                ctx.wait_withhold == RD_WAIT_RL_COPY ? 1 : 0));
   return Status{};
 }
 
@@ -547,7 +584,8 @@ __global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict
                                                           const StepSegments sg, int items, const Taps taps,
                                                           const __grid_constant__ CUtensorMap est_map,
                                                           const __grid_constant__ CUtensorMap guide_map,
-                                                          unsigned* work, unsigned* error) {
+                                                          unsigned* work, unsigned* error, unsigned wait_tries,
+                                                          int withhold) {
   using G = StepGeom<R>;
   constexpr int T = G::T, SW = G::SW, BH = G::BH, N2 = 2 * R;
   extern __shared__ __align__(128) float4 rl_step_raw[];
@@ -561,8 +599,7 @@ __global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   __syncthreads();
-  unsigned phases = 0;
-  bool tma_failed = false;
+  CopyWaits cw(wait_tries, TMA && withhold != 0, error);
   // The run each thread computes in the horizontal passes (row, first column).
   const bool h1_on = tid < G::H1_RUNS * BH, h2_on = tid < G::H2_RUNS * BH;
   const int h1_row = tid / G::H1_RUNS, h1_col = (tid % G::H1_RUNS) * G::RUN;
@@ -601,7 +638,7 @@ __global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict
       if (k >= nsteps) return;
       const int r0 = E0 + BH * k, b = k % 3;
       const bool et = e_by_tma(k);
-      if (TMA && tid == 0) {
+      if (TMA && cw.issue_block(b) && tid == 0) {
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         mbar_expect_tx(&S.bar[b], (et ? BH * G::EWP * sizeof(float) : 0) + G::GH * G::EWP * sizeof(float));
         if (et) tma_load_2d(S.e[b * BH], &est_map, xal, r0, &S.bar[b]);
@@ -641,11 +678,7 @@ __global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict
         }
       }
       asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-      if (TMA) {
-        const int b = k % 3;
-        tma_wait(&S.bar[b], (phases >> b) & 1u, tma_failed, error);
-        phases ^= 1u << b;
-      }
+      if (TMA) cw.wait(&S.bar[k % 3], k % 3);
       __syncthreads();
       // Block k + 2 reuses the slots of block k - 1, whose estimate rows were
       // last read before the second barrier of step k - 1 and whose guide rows
@@ -749,6 +782,7 @@ __global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict
     }
   }
   asm volatile("cp.async.wait_all;\n" ::: "memory");
+  if (TMA) cw.drain(S.bar, 3);
 }
 
 // The constant-lag kernel serves images of at least 256 x 64; smaller ones
@@ -782,7 +816,9 @@ Status launch_rl_step_t(Context& ctx, const float* est, const float* guide, floa
   CUtensorMap none{};
   RD_LAUNCH(ctx, K_RL_ITER, rl_step_kernel<R, TMA><<<grid, 128, smem, ctx.stream>>>(
                                 est, guide, out, W, H, strips, sg, items, taps, est_map ? *est_map : none,
-                                guide_map ? *guide_map : none, ctx.d_work, ctx.d_error));
+                                guide_map ? *guide_map : none, ctx.d_work, ctx.d_error,
+                                ctx.wait_limit ? ctx.wait_limit : RL_DEFAULT_WAIT_TRIES,
+                                ctx.wait_withhold == RD_WAIT_RL_COPY ? 1 : 0));
   return Status{};
 }
 
@@ -958,7 +994,8 @@ __global__ void __launch_bounds__(128, 4) rl_prep_step_kernel(const float* __res
                                                                float* __restrict__ guide, float* __restrict__ mask,
                                                                int W, int H, int strips, int segs, int items,
                                                                const Taps taps, const __grid_constant__ CUtensorMap rgb_map,
-                                                               unsigned* work, unsigned* error) {
+                                                               unsigned* work, unsigned* error, unsigned wait_tries,
+                                                               int withhold) {
   using G = PrepGeom<R>;
   constexpr int T = G::T, SW = G::SW, BH = G::BH, N2 = 2 * R;
   extern __shared__ __align__(128) float4 rl_prep_raw[];
@@ -972,8 +1009,8 @@ __global__ void __launch_bounds__(128, 4) rl_prep_step_kernel(const float* __res
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   __syncthreads();
-  unsigned phases = 0;
-  bool tma_failed = false, bad = false;
+  CopyWaits cw(wait_tries, TMA && withhold != 0, error);
+  bool bad = false;
   const bool h_on = tid < G::H_RUNS * BH;
   const int h_row = tid / G::H_RUNS, h_col = (tid % G::H_RUNS) * G::RUN;
   __shared__ int s_item;
@@ -999,7 +1036,7 @@ __global__ void __launch_bounds__(128, 4) rl_prep_step_kernel(const float* __res
       if (k >= nsteps) return;
       const int r0 = E0 + BH * k, b = k & 1;
       if (by_tma(k)) {
-        if (tid == 0) {
+        if (cw.issue_block(b) && tid == 0) {
           asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
           mbar_expect_tx(&S.bar[b], 3 * BH * G::CWP * sizeof(float));
 #pragma unroll
@@ -1015,10 +1052,7 @@ __global__ void __launch_bounds__(128, 4) rl_prep_step_kernel(const float* __res
       }
     };
     auto arrive = [&](int k) {  // this thread's view of block k is complete
-      if (by_tma(k)) {
-        tma_wait(&S.bar[k & 1], (phases >> (k & 1)) & 1u, tma_failed, error);
-        phases ^= 1u << (k & 1);
-      }
+      if (by_tma(k)) cw.wait(&S.bar[k & 1], k & 1);
     };
     issue(0);
     cp_async_commit();
@@ -1127,6 +1161,7 @@ __global__ void __launch_bounds__(128, 4) rl_prep_step_kernel(const float* __res
     }
   }
   asm volatile("cp.async.wait_all;\n" ::: "memory");
+  if (TMA) cw.drain(S.bar, 2);
   if (bad) atomicOr(error, 2u);
 }
 
@@ -1150,7 +1185,9 @@ Status launch_rl_prep_step(Context& ctx, const Taps& taps, const float* rgb, lon
   CUtensorMap none{};
   RD_LAUNCH(ctx, K_RL_MASK, rl_prep_step_kernel<R, TMA><<<grid, 128, smem, ctx.stream>>>(
                                 rgb, plane, ceil[0], ceil[1], ceil[2], noise, guide, mask, W, H, strips, segs, items,
-                                taps, rgb_map ? *rgb_map : none, ctx.d_work, ctx.d_error));
+                                taps, rgb_map ? *rgb_map : none, ctx.d_work, ctx.d_error,
+                                ctx.wait_limit ? ctx.wait_limit : RL_DEFAULT_WAIT_TRIES,
+                                ctx.wait_withhold == RD_WAIT_RL_COPY ? 1 : 0));
   return Status{};
 }
 

@@ -86,7 +86,15 @@ struct Context {
   // stage's synchronisation: (candidate segment count, start, end).
   int tune_shape[3] = {0, 0, 0};
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> tune_runs;
+  // Bounded device waits (rd_ctx_set_wait_test): the iteration limit of each
+  // wait, and which completion a test withholds so that a wait runs out.
+  uint32_t wait_limit = 0;      // 0: the built-in limits
+  int32_t wait_withhold = 0;    // RD_WAIT_* of include/rd_gpu.h
 };
+
+// Iteration limits of the device waits when no test sets one.
+constexpr uint32_t AMAZE_DEFAULT_WAIT_TRIES = 1u << 22;
+constexpr uint32_t RL_DEFAULT_WAIT_TRIES = 1u << 20;
 
 // Brackets one kernel launch with events when kernel timing is enabled, and
 // counts the launch either way.
