@@ -628,8 +628,9 @@ def batched_throughput(args, count: int = 48, lanes: int = 3) -> dict:
     phase, black, WB and matrices; Opposed + AMaZE + RL K=5 + optics + 2560-px
     preview, sRGB8 + histogram to the host) through rd_develop_batch with
     `lanes` concurrent lanes, the same images one at a time (one lane), and the
-    batch as one captured CUDA graph. Host mosaics in, host outputs out, timed
-    end to end."""
+    batch as one captured CUDA graph, and stage by stage with one AMaZE launch
+    over the tiles of all images (rd_develop_batch_flat). Host mosaics in, host
+    outputs out, timed end to end."""
     from rohditor_gb300 import Device
     from rohditor_gb300.batch import BatchImage, PinnedBatch, develop_batch
     from rohditor_gb300.workloads import batched_uneven
@@ -645,6 +646,9 @@ def batched_throughput(args, count: int = 48, lanes: int = 3) -> dict:
     develop_batch(images, lanes=lanes)
     _, _, wall = develop_batch(images, lanes=lanes)
     _, _, wall1 = develop_batch(images, lanes=1)
+    # Stage by stage, with one AMaZE launch over the tiles of all images.
+    develop_batch(images, lanes=lanes, flat=True)
+    _, _, wall_flat = develop_batch(images, lanes=lanes, flat=True)
     # With the mosaics and outputs in pinned host memory (a decoder writing
     # into pinned buffers): one lane, concurrent lanes, and the batch as one
     # captured CUDA graph (rd_develop_batch_graph) with `chains` branches,
@@ -653,6 +657,7 @@ def batched_throughput(args, count: int = 48, lanes: int = 3) -> dict:
     pinned.run(lanes=lanes)  # warm-up
     p1 = pinned.run(lanes=1)["wall_ms"]
     pl = pinned.run(lanes=lanes)["wall_ms"]
+    pf = pinned.run(lanes=lanes, flat=True)["wall_ms"]
     graph = {}
     for chains in (lanes, 2 * lanes):
         g = pinned.run(lanes=chains, graph=True)
@@ -662,10 +667,15 @@ def batched_throughput(args, count: int = 48, lanes: int = 3) -> dict:
                               "speedup_vs_one_lane": round(p1 / g["launch_ms"], 3)}
     pinned.close()
     pinned_runs = {"one_lane_wall_ms": round(p1, 1), "lanes_wall_ms": round(pl, 1),
-                   "lanes_mp_per_s": round(pixels / 1e6 / (pl / 1e3), 1), "graph_chains": graph}
+                   "lanes_mp_per_s": round(pixels / 1e6 / (pl / 1e3), 1), "flat_wall_ms": round(pf, 1),
+                   "flat_mp_per_s": round(pixels / 1e6 / (pf / 1e3), 1),
+                   "flat_speedup_vs_one_lane": round(p1 / pf, 3), "graph_chains": graph}
     return {"images": count, "megapixels": round(pixels / 1e6, 1), "lanes": lanes, "wall_ms": round(wall, 1),
             "develops_per_s": round(count / (wall / 1e3), 2), "mp_per_s": round(pixels / 1e6 / (wall / 1e3), 1),
             "one_lane_wall_ms": round(wall1, 1), "speedup_vs_one_lane": round(wall1 / wall, 3),
+            "flat": {"wall_ms": round(wall_flat, 1), "develops_per_s": round(count / (wall_flat / 1e3), 2),
+                     "mp_per_s": round(pixels / 1e6 / (wall_flat / 1e3), 1),
+                     "speedup_vs_one_lane": round(wall1 / wall_flat, 3)},
             "pinned_host": pinned_runs,
             "workload": f"uneven batch of {count}: 12/24/45/60 MP, random CFA phase, Opposed + AMaZE + RL5 + optics "
                         f"+ preview"}

@@ -397,6 +397,15 @@ rd_status rd_develop_batch(int device, rd_batch_item* items, int32_t count, int3
  * wall_ms (launch plus staging copies). Per-item `ms` is 0. */
 rd_status rd_develop_batch_graph(int device, rd_batch_item* items, int32_t count, int32_t chains,
                                  int32_t host_pinned, double* wall_ms, double* capture_ms, double* launch_ms);
+/* The same batch stage by stage: `lanes` lanes upload their images
+ * (k % lanes) and normalize / highlight them, then one AMaZE launch works
+ * through the half-tile items of every image from a shared queue (images of
+ * other demosaic algorithms, or of 32 px or less, are demosaiced one by
+ * one), then the lanes finish their images (capture sharpening, spatial
+ * pass, render). Outputs equal rd_develop + rd_spatial + rd_render per image
+ * bit for bit; device memory holds every image's intermediates at once.
+ * Per-item `ms` covers the finishing stage only. */
+rd_status rd_develop_batch_flat(int device, rd_batch_item* items, int32_t count, int32_t lanes, double* wall_ms);
 
 /* ---- served preview loop ----
  * Replaces the engine's preview worker and caches

@@ -5,7 +5,8 @@ Each image goes through the whole path (develop, spatial pass, render) with
 host buffers. With `graph=False`, `lanes` contexts on their own streams work
 through a shared queue concurrently so their kernels overlap on the GPU. With
 `graph=True` the whole batch is captured into one CUDA graph of `lanes`
-parallel branches and runs as a single launch.
+parallel branches and runs as a single launch. With `flat=True` the batch
+runs stage by stage, with one AMaZE launch over the tiles of every image.
 """
 
 from __future__ import annotations
@@ -75,11 +76,13 @@ class PinnedBatch:
             it.hist = ctypes.cast(ptrs[2], ctypes.POINTER(ctypes.c_uint64))
             self.outs.append((ptrs[1], ptrs[2], im.target))
 
-    def run(self, lanes: int = 3, graph: bool = False) -> dict:
+    def run(self, lanes: int = 3, graph: bool = False, flat: bool = False) -> dict:
         """Times of one run: wall_ms, and for a graph capture_ms and launch_ms."""
         wall, cap, launch = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
         n = len(self.items)
-        if graph:
+        if flat:
+            rc = self.lib.rd_develop_batch_flat(self.device, self.items, n, lanes, ctypes.byref(wall))
+        elif graph:
             rc = self.lib.rd_develop_batch_graph(self.device, self.items, n, lanes, 1, ctypes.byref(wall),
                                                  ctypes.byref(cap), ctypes.byref(launch))
         else:
@@ -107,10 +110,12 @@ class PinnedBatch:
         self.buffers = []
 
 
-def develop_batch(images: list[BatchImage], lanes: int = 3, device: int = 0, graph: bool = False):
+def develop_batch(images: list[BatchImage], lanes: int = 3, device: int = 0, graph: bool = False,
+                  flat: bool = False):
     """Returns (outputs [(srgb8, hist)], per-image ms, wall ms); with `graph`,
     the per-image ms are 0 and the capture + instantiation ms is the last
-    element of the returned tuple."""
+    element of the returned tuple. With `flat` the batch runs stage by stage
+    with one AMaZE launch over every image's tiles (rd_develop_batch_flat)."""
     lib = _ffi.load()
     items = (_ffi.BatchItem * len(images))()
     keep = []
@@ -135,7 +140,10 @@ def develop_batch(images: list[BatchImage], lanes: int = 3, device: int = 0, gra
         if rc != 0:
             raise GpuPreviewError(rc, f"batched graph develop failed: {lib.rd_status_name(rc).decode()}")
         return outs, [0.0] * len(images), wall.value, capture.value
-    rc = lib.rd_develop_batch(device, items, len(images), lanes, ctypes.byref(wall))
+    if flat:
+        rc = lib.rd_develop_batch_flat(device, items, len(images), lanes, ctypes.byref(wall))
+    else:
+        rc = lib.rd_develop_batch(device, items, len(images), lanes, ctypes.byref(wall))
     if rc != 0:
         raise GpuPreviewError(rc, f"batched develop failed: {lib.rd_status_name(rc).decode()}")
     return outs, [items[k].ms for k in range(len(images))], wall.value

@@ -6,10 +6,12 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "rd_internal.cuh"
@@ -1407,3 +1409,186 @@ rd_status rd_copy_to_host(rd_ctx* h, void* dst, const void* src, size_t bytes) {
 }
 
 }  // extern "C"
+
+// ---- batched develop over one AMaZE work queue -------------------------------
+// rd_develop_batch_flat: the batch stage by stage. Lanes (contexts on their own
+// streams, one host thread each) upload their images and normalize / Opposed
+// them; one AMaZE launch then takes the half-tile work items of every image
+// from a shared counter (run_amaze_images), so no image's last wave leaves SMs
+// idle; the lanes finish their images (capture sharpening, spatial pass,
+// render with host outputs). Image k belongs to lane k % lanes throughout, and
+// its device buffers come from that lane's pool.
+namespace {
+
+struct FlatJob {
+  uint16_t* d_raw = nullptr;
+  size_t raw_bytes = 0;
+  float* d_mosaic = nullptr;
+  size_t mosaic_bytes = 0;
+  unsigned long long* d_stats = nullptr;
+  rd::MosaicSource src{};
+  rd_source* source = nullptr;
+  Status st;
+};
+
+Status flat_prepare(rd_ctx* h, const rd_batch_item& it, FlatJob& j) {
+  rd::Context& ctx = h->c;
+  const rd_sensor_desc& s = it.sensor;
+  Status st;
+  validate_sensor(s, st);
+  if (!st.ok()) return st;
+  if (!it.mosaic) return Status{RD_INVALID_INPUT, "null mosaic"};
+  if (it.row_stride < s.sensor_width) return Status{RD_INVALID_DIMENSIONS, "row stride is shorter than the sensor width"};
+  const int W = (int)s.crop_width, H = (int)s.crop_height;
+  void* p = nullptr;
+  j.raw_bytes = sizeof(uint16_t) * it.row_stride * s.sensor_height;
+  RD_TRY(rd::device_alloc(ctx, j.raw_bytes, &p));
+  j.d_raw = static_cast<uint16_t*>(p);
+  RD_CUDA_TRY(cudaMemcpyAsync(j.d_raw, it.mosaic, j.raw_bytes, cudaMemcpyHostToDevice, ctx.stream));
+  RD_TRY(rd::device_alloc(ctx, sizeof(unsigned long long) * 16, &p));
+  j.d_stats = static_cast<unsigned long long*>(p);
+  RD_CUDA_TRY(cudaMemsetAsync(j.d_stats, 0, sizeof(unsigned long long) * 16, ctx.stream));
+  j.src = rd::make_source(s, j.d_raw, it.row_stride);
+  if (s.highlight == RD_HIGHLIGHT_OPPOSED) {
+    j.mosaic_bytes = sizeof(float) * (size_t)W * H;
+    RD_TRY(rd::device_alloc(ctx, j.mosaic_bytes, &p));
+    j.d_mosaic = static_cast<float*>(p);
+    rd::MosaicSource norm = j.src;
+    norm.clip = 0;
+    RD_TRY(rd::launch_normalize(ctx, norm, j.d_mosaic, nullptr));
+    RD_TRY(rd::run_opposed(ctx, j.d_mosaic, W, H, j.src.cfa, s.detection_levels,
+                           s.has_neutral_ceiling ? s.neutral_ceiling : nullptr, j.d_stats, nullptr));
+    j.src.f32 = j.d_mosaic;
+    j.src.clip = 0;
+  }
+  j.source = new (std::nothrow) rd_source{h, nullptr, W, H, sizeof(float) * 3 * (size_t)W * H};
+  if (!j.source) return Status{RD_OVER_BUDGET, "host allocation failed"};
+  RD_TRY(rd::device_alloc(ctx, j.source->bytes, &p));
+  j.source->rgb = static_cast<float*>(p);
+  return Status{};
+}
+
+void flat_release_staging(rd_ctx* h, FlatJob& j) {
+  rd::Context& ctx = h->c;
+  if (j.d_mosaic) rd::device_free(ctx, j.d_mosaic, j.mosaic_bytes);
+  if (j.d_raw) rd::device_free(ctx, j.d_raw, j.raw_bytes);
+  if (j.d_stats) rd::device_free(ctx, j.d_stats, sizeof(unsigned long long) * 16);
+  j.d_mosaic = nullptr;
+  j.d_raw = nullptr;
+  j.d_stats = nullptr;
+}
+
+}  // namespace
+
+extern "C" rd_status rd_develop_batch_flat(int device, rd_batch_item* items, int32_t count, int32_t lanes,
+                                           double* wall_ms) {
+  using Clock = std::chrono::steady_clock;
+  if (!items || count < 0 || lanes <= 0) return RD_INVALID_INPUT;
+  if (wall_ms) *wall_ms = 0.0;
+  if (count == 0) return RD_OK;
+  lanes = std::min(lanes, count);
+  std::vector<rd_ctx*> ctxs(lanes, nullptr);
+  std::vector<cudaEvent_t> prepared(lanes, nullptr);
+  cudaEvent_t demosaiced = nullptr;
+  rd_status status = RD_OK;
+  for (int l = 0; l < lanes && status == RD_OK; ++l) {
+    status = rd_ctx_create(device, 0, &ctxs[l]);
+    if (status == RD_OK && cudaEventCreateWithFlags(&prepared[l], cudaEventDisableTiming) != cudaSuccess)
+      status = RD_SYNCHRONIZATION;
+  }
+  if (status == RD_OK && cudaEventCreateWithFlags(&demosaiced, cudaEventDisableTiming) != cudaSuccess)
+    status = RD_SYNCHRONIZATION;
+  std::vector<FlatJob> jobs((size_t)count);
+  const auto t0 = Clock::now();
+  auto on_lanes = [&](auto&& body) {
+    std::vector<std::thread> threads;
+    for (int l = 1; l < lanes; ++l) threads.emplace_back(body, l);
+    body(0);
+    for (std::thread& t : threads) t.join();
+  };
+  if (status == RD_OK) {
+    // 1. upload + normalize + highlight, lane by lane.
+    on_lanes([&](int l) {
+      rd_ctx* h = ctxs[l];
+      cudaSetDevice(h->c.device);
+      for (int k = l; k < count; k += lanes) jobs[k].st = flat_prepare(h, items[k], jobs[k]);
+      cudaEventRecord(prepared[l], h->c.stream);
+    });
+    // 2. demosaic on lane 0: AMaZE of every image larger than 32x32 in one launch.
+    rd::Context& c0 = ctxs[0]->c;
+    cudaSetDevice(c0.device);
+    for (int l = 1; l < lanes; ++l) cudaStreamWaitEvent(c0.stream, prepared[l], 0);
+    std::vector<rd::AmazeJob> amaze;
+    std::vector<int> amaze_images;
+    Status dm;
+    for (int k = 0; k < count && dm.ok(); ++k) {
+      FlatJob& j = jobs[k];
+      if (!j.st.ok()) continue;
+      const int alg = items[k].sensor.demosaic;
+      if (alg == RD_DEMOSAIC_AMAZE && j.source->W > 32 && j.source->H > 32) {
+        amaze.push_back(rd::demosaic_job(j.src, alg, j.source->rgb, j.d_stats));
+        amaze_images.push_back(k);
+      } else {
+        j.st = rd::run_demosaic(c0, j.src, alg, j.source->rgb, j.d_stats);
+      }
+    }
+    if (!amaze.empty()) dm = rd::run_amaze_images(c0, amaze.data(), (int)amaze.size());
+    if (dm.ok()) dm = rd::check_kernel_error(c0, "batch demosaic");
+    if (!dm.ok())
+      for (int k : amaze_images)
+        if (jobs[k].st.ok()) jobs[k].st = dm;
+    cudaEventRecord(demosaiced, c0.stream);
+    // 3. capture sharpening, spatial pass and render, lane by lane.
+    on_lanes([&](int l) {
+      rd_ctx* h = ctxs[l];
+      rd::Context& ctx = h->c;
+      cudaSetDevice(ctx.device);
+      cudaStreamWaitEvent(ctx.stream, demosaiced, 0);
+      for (int k = l; k < count; k += lanes) {
+        FlatJob& j = jobs[k];
+        rd_batch_item& it = items[k];
+        const auto s0 = Clock::now();
+        Status st = j.st;
+        if (st.ok()) st = rd::run_capture(ctx, j.source->rgb, j.source->W, j.source->H, it.detail);
+        flat_release_staging(h, j);
+        if (st.ok()) st = rd::check_kernel_error(ctx, "batch develop");
+        rd_status code = finish(h, st);
+        rd_base* base = nullptr;
+        if (code == RD_OK)
+          code = rd_spatial(h, j.source, &it.optics, it.target_width, it.target_height, it.wb_gains,
+                            it.camera_to_rec2020, &base, nullptr);
+        if (j.source) {
+          if (j.source->rgb) {
+            rd_source_release(j.source);
+          } else {
+            delete j.source;
+          }
+          j.source = nullptr;
+        }
+        if (code == RD_OK) code = rd_render(h, base, &it.color, it.srgb_out, it.hist, nullptr, nullptr);
+        if (base) rd_base_release(base);
+        it.status = code;
+        it.ms = std::chrono::duration<double, std::milli>(Clock::now() - s0).count();
+      }
+    });
+  }
+  if (wall_ms) *wall_ms = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+  for (FlatJob& j : jobs)
+    if (j.source) {
+      if (j.source->rgb) rd_source_release(j.source);
+      else delete j.source;
+    }
+  for (int l = 0; l < lanes; ++l) {
+    if (prepared[l]) cudaEventDestroy(prepared[l]);
+  }
+  if (demosaiced) cudaEventDestroy(demosaiced);
+  for (int l = 0; l < lanes; ++l)
+    if (ctxs[l]) {
+      for (int k = l; k < count; k += lanes) flat_release_staging(ctxs[l], jobs[k]);
+      rd_ctx_destroy(ctxs[l]);
+    }
+  if (status != RD_OK) return status;
+  for (int k = 0; k < count; ++k)
+    if (items[k].status != RD_OK) return (rd_status)items[k].status;
+  return RD_OK;
+}

@@ -43,6 +43,10 @@
 // the reference.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cstdint>
+#include <vector>
+
 #include "rd_internal.cuh"
 
 namespace rd {
@@ -165,20 +169,36 @@ constexpr size_t SMEM_BYTES = sizeof(float) * SMEM_FLOATS;
 // planes) and the Nyquist flags (u8 half plane).
 constexpr size_t SLAB_FLOATS = 3 * (size_t)TS * TSH + (size_t)TS * TSH / 4;
 
-struct AmazeParams {
+// One image of a launch: its mosaic source, output planes and balance, and
+// the global index of its first tile (slabs and flags are per global tile).
+struct AmazeImage {
   MosaicSource src;
   float* out;              // planar RGB, 3 * width * height
-  float* slab;             // SLAB_FLOATS per CTA
+  unsigned long long* clip_stats;
   int tiles_x, tiles_y;
+  int tile0;               // global index of the image's tile 0
+  int count_clip;          // 1: accumulate Clip statistics of core pixels
   float clip_point;
   float gains[3];          // inverse balance applied to the output
-  int count_clip;          // 1: accumulate Clip statistics of core pixels
-  unsigned long long* clip_stats;
+};
+
+// A run of consecutive work items: phase A or phase B of tiles
+// [0, count) of one image, in the order the counter hands them out.
+struct AmazeSegment {
+  int first_item, count, image, phase_b;
+};
+
+struct AmazeParams {
+  const AmazeImage* images;
+  const AmazeSegment* segs;
+  int nsegs;
+  int total_items;
+  float* slab;             // SLAB_FLOATS per global tile
   unsigned int* error;
-  unsigned* flags;         // per tile: 1 once its phase A is complete (zeroed per launch)
+  unsigned* flags;         // per global tile: 1 once its phase A is complete (zeroed per launch)
   unsigned* work;          // work-item counter (zeroed per launch)
   unsigned wait_tries;     // iteration limit of the phase-B wait
-  int withhold_tile;       // a tile whose phase A does not publish (tests of the bounded wait), or -1
+  int withhold_tile;       // a global tile whose phase A does not publish (tests of the bounded wait), or -1
 };
 
 constexpr unsigned AMAZE_WAIT_TIMEOUT = 64u;
@@ -269,53 +289,80 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
   // Refined Nyquist sites of a step (phase B), by step parity.
   __shared__ unsigned short s_nyq_queue[BH * (TS - 16) / 2];
   __shared__ int s_nyq_n[2];
-  const MosaicSource& src = prm.src;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const unsigned FULL = 0xffffffffu;
-  const int pattern = src.cfa;
-  const float clip_pt = prm.clip_point;
-  const float clip_pt8 = 0.8f * clip_pt;
-  const int W = src.width, H = src.height;
-  const long long plane = (long long)W * H;
+  // The image of the current item, copied from the launch's table when the
+  // CTA moves to another image.
+  __shared__ AmazeImage s_img;
+  __shared__ int s_item, s_image, s_tile, s_phase;
+  int loaded = -1;
 
-  // Rows holding blue sites: interpolate_chroma moves their differences to dgrb1 (chroma.rs:23-44).
-  int ey;
-  {
-    const int c00 = color_at(pattern, 0, 0), c10 = color_at(pattern, 1, 0);
-    if (c00 == 1 && c10 == 0) ey = 0;
-    else if (c00 == 1) ey = 1;
-    else if (c00 == 0) ey = 0;
-    else ey = 1;
-  }
-  const int blue_par = (13 - ey) & 1;
-  // Red/blue sites of row r sit at columns of parity g0 ^ (r & 1) (gae of the
-  // reference); ctab is the packed 2x2 colour table of the pattern (color_at).
-  const int g0 = gae(pattern, 0);
-  const unsigned ctab = pattern == 0 ? 0x94u : pattern == 1 ? 0x16u : pattern == 2 ? 0x61u : 0x49u;
-
-  // Work items from the launch's counter: item k < ntiles is phase A of tile
-  // k, item ntiles + k its phase B. All phase-A items are handed out first,
-  // so a phase-B item only waits for a phase A that a running CTA has taken
-  // (and phase A waits for nothing), and the 2 x ntiles half-tile items fill
-  // the SMs far more evenly than whole tiles would.
-  const int ntiles = prm.tiles_x * prm.tiles_y;
-  __shared__ int s_item;
+  // Work items from the launch's counter, in the order of the segment table:
+  // phase A of every tile of an image is handed out before any phase B of
+  // that image (the table puts the images' phase-A runs one image ahead of
+  // their phase-B runs), so a phase-B item only waits for a phase A that a
+  // running CTA has taken, and phase A waits for nothing. The half-tile items
+  // of all images fill the SMs far more evenly than whole tiles would.
   for (;;) {
     __syncthreads();
     if (t == 0) {
       // The launch's last fetch (one past the items per CTA) resets the counter.
       const unsigned v = atomicAdd(prm.work, 1u);
-      if (v == 2u * ntiles + gridDim.x - 1u) atomicExch(prm.work, 0u);
+      if (v == (unsigned)prm.total_items + gridDim.x - 1u) atomicExch(prm.work, 0u);
+      int image = -1, tile = 0, phase = 0;
+      if ((int)v < prm.total_items) {
+        int lo = 0, hi = prm.nsegs;
+        while (hi - lo > 1) {
+          const int mid = (lo + hi) >> 1;
+          if (prm.segs[mid].first_item <= (int)v) lo = mid;
+          else hi = mid;
+        }
+        const AmazeSegment sg = prm.segs[lo];
+        image = sg.image;
+        tile = (int)v - sg.first_item;
+        phase = sg.phase_b;
+      }
       s_item = (int)v;
+      s_image = image;
+      s_tile = tile;
+      s_phase = phase;
     }
     __syncthreads();
-    const int item = s_item;
-    if (item >= 2 * ntiles) break;
-    const bool phase_b = item >= ntiles;
-    const int tile = phase_b ? item - ntiles : item;
-    const int ox = (tile % prm.tiles_x) * VALID, oy = (tile / prm.tiles_x) * VALID;
+    if (s_item >= prm.total_items) break;
+    const int tile = s_tile;
+    const bool phase_b = s_phase != 0;
+    if (s_image != loaded) {
+      loaded = s_image;
+      const int* from = reinterpret_cast<const int*>(prm.images + loaded);
+      int* to = reinterpret_cast<int*>(&s_img);
+      for (int k = t; k < (int)(sizeof(AmazeImage) / sizeof(int)); k += THREADS) to[k] = from[k];
+      __syncthreads();
+    }
+    const AmazeImage& im = s_img;
+    const MosaicSource& src = im.src;
+    const int pattern = src.cfa;
+    const float clip_pt = im.clip_point;
+    const float clip_pt8 = 0.8f * clip_pt;
+    const int W = src.width, H = src.height;
+    const long long plane = (long long)W * H;
+    // Rows holding blue sites: interpolate_chroma moves their differences to dgrb1 (chroma.rs:23-44).
+    int ey;
+    {
+      const int c00 = color_at(pattern, 0, 0), c10 = color_at(pattern, 1, 0);
+      if (c00 == 1 && c10 == 0) ey = 0;
+      else if (c00 == 1) ey = 1;
+      else if (c00 == 0) ey = 0;
+      else ey = 1;
+    }
+    const int blue_par = (13 - ey) & 1;
+    // Red/blue sites of row r sit at columns of parity g0 ^ (r & 1) (gae of the
+    // reference); ctab is the packed 2x2 colour table of the pattern (color_at).
+    const int g0 = gae(pattern, 0);
+    const unsigned ctab = pattern == 0 ? 0x94u : pattern == 1 ? 0x16u : pattern == 2 ? 0x61u : 0x49u;
+    const int ox = (tile % im.tiles_x) * VALID, oy = (tile / im.tiles_x) * VALID;
+    const int gtile = im.tile0 + tile;
     // Per-tile slab: written by phase A, read by phase B (possibly on another SM).
-    float* slab = prm.slab + (size_t)tile * SLAB_FLOATS;
+    float* slab = prm.slab + (size_t)gtile * SLAB_FLOATS;
     float* g_hv = slab;
     float* g_vrb = slab + TS * TSH;
     float* g_hrb = slab + 2 * TS * TSH;
@@ -601,14 +648,14 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
     // Publish the slab: every thread's writes, then the tile's flag.
     __threadfence();
     __syncthreads();
-    if (t == 0 && tile != prm.withhold_tile) atomicExch(&prm.flags[tile], 1u);
+    if (t == 0 && gtile != prm.withhold_tile) atomicExch(&prm.flags[gtile], 1u);
     continue;
     }
 
     // Phase B waits (bounded) until the tile's phase A has published its slab.
     if (t == 0) {
       unsigned tries = 0;
-      while (load_acquire(&prm.flags[tile]) == 0u) {
+      while (load_acquire(&prm.flags[gtile]) == 0u) {
         if (++tries > prm.wait_tries) {
           atomicOr(prm.error, AMAZE_WAIT_TIMEOUT);
           break;
@@ -1015,15 +1062,15 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
             float rgb0 = ch == 0 ? sample : r;
             float rgb1 = ch == 1 ? sample : fmax_(gv, 0.0f);
             float rgb2 = ch == 2 ? sample : b;
-            rgb0 = rgb0 * prm.gains[0];
-            rgb1 = rgb1 * prm.gains[1];
-            rgb2 = rgb2 * prm.gains[2];
+            rgb0 = rgb0 * im.gains[0];
+            rgb1 = rgb1 * im.gains[1];
+            rgb2 = rgb2 * im.gains[2];
             if (!isfinite(rgb0) || !isfinite(rgb1) || !isfinite(rgb2)) bad = 1;
             const long long o = (long long)gy * W + gx;
-            prm.out[o] = rgb0;
-            prm.out[plane + o] = rgb1;
-            prm.out[2 * plane + o] = rgb2;
-            if (prm.count_clip) {
+            im.out[o] = rgb0;
+            im.out[plane + o] = rgb1;
+            im.out[2 * plane + o] = rgb2;
+            if (im.count_clip) {
               const float v = source_normalized(src, gx, gy);
               const float limit = src.clip_levels[ch];
               if (v >= limit) {
@@ -1039,7 +1086,7 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
         }
         __syncthreads();
       }
-      if (prm.count_clip) {
+      if (im.count_clip) {
         unsigned long long vals[6] = {affected, changed, over, ac0, ac1, ac2};
         for (int c = 0; c < 6; ++c) {
           unsigned long long v = vals[c];
@@ -1051,9 +1098,9 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
     }
     __syncthreads();
     if (t == 0) {
-      if (prm.count_clip)
+      if (im.count_clip)
         for (int c = 0; c < 6; ++c)
-          if (s_stats[c]) atomicAdd(&prm.clip_stats[c], s_stats[c]);
+          if (s_stats[c]) atomicAdd(&im.clip_stats[c], s_stats[c]);
       if (s_bad) atomicOr(prm.error, 1u);
     }
     __syncthreads();
@@ -1083,38 +1130,92 @@ size_t amaze_tiles(int width, int height) {
   return (size_t)((width + VALID - 1) / VALID) * (size_t)((height + VALID - 1) / VALID);
 }
 
-Status run_amaze(Context& ctx, const MosaicSource& src, const float gains[3], float clip_point, float* rgb,
-                 int count_clip, unsigned long long* clip_stats) {
-  const int tiles_x = (src.width + VALID - 1) / VALID, tiles_y = (src.height + VALID - 1) / VALID;
-  const int ntiles = tiles_x * tiles_y;
+Status run_amaze_images(Context& ctx, const AmazeJob* jobs, int n) {
+  if (n <= 0) return Status{};
+  std::vector<AmazeImage> images((size_t)n);
+  std::vector<AmazeSegment> segs;
+  segs.reserve(2 * (size_t)n);
+  size_t total_tiles = 0;
+  for (int i = 0; i < n; ++i) {
+    const AmazeJob& j = jobs[i];
+    AmazeImage& im = images[i];
+    im.src = j.src;
+    im.out = j.rgb;
+    im.clip_stats = j.clip_stats;
+    im.tiles_x = (j.src.width + VALID - 1) / VALID;
+    im.tiles_y = (j.src.height + VALID - 1) / VALID;
+    im.tile0 = (int)total_tiles;
+    im.count_clip = j.count_clip;
+    im.clip_point = j.clip_point;
+    for (int c = 0; c < 3; ++c) im.gains[c] = j.gains[c];
+    total_tiles += (size_t)im.tiles_x * im.tiles_y;
+  }
+  if (total_tiles > (size_t)(INT32_MAX / 2)) return Status{RD_INVALID_DIMENSIONS, "too many demosaic tiles in one launch"};
+  // Hand-out order: phase A of image 0; then, image after image, phase A of
+  // image i followed by phase B of image i - 1; phase B of the last image.
+  int item = 0;
+  auto add = [&](int image, int phase_b) {
+    const int count = images[image].tiles_x * images[image].tiles_y;
+    segs.push_back(AmazeSegment{item, count, image, phase_b});
+    item += count;
+  };
+  add(0, 0);
+  for (int i = 1; i < n; ++i) {
+    add(i, 0);
+    add(i - 1, 1);
+  }
+  add(n - 1, 1);
   // One resident CTA per SM (shared memory); the CTAs take half-tile items
   // from the counter.
   const int sms = ctx.sm_count > 0 ? ctx.sm_count : 152;
-  const int grid = std::min(2 * ntiles, sms);
-  if (ctx.capturing && ctx.amaze_slots < (size_t)ntiles)
+  const int grid = std::min(item, sms);
+  if (ctx.capturing && ctx.amaze_slots < total_tiles)
     return Status{RD_INVALID_INPUT, "demosaic scratch was not reserved before the capture"};
-  RD_TRY(reserve_amaze_scratch(ctx, (size_t)ntiles));
+  RD_TRY(reserve_amaze_scratch(ctx, total_tiles));
   unsigned* flags = reinterpret_cast<unsigned*>(ctx.amaze_scratch + ctx.amaze_slots * SLAB_FLOATS);
-  RD_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(unsigned) * ntiles, ctx.stream));
-  RD_CUDA_TRY(cudaFuncSetAttribute(amaze_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
-  AmazeParams prm;
-  prm.src = src;
-  prm.out = rgb;
-  prm.slab = ctx.amaze_scratch;
-  prm.tiles_x = tiles_x;
-  prm.tiles_y = tiles_y;
-  prm.clip_point = clip_point;
-  for (int c = 0; c < 3; ++c) prm.gains[c] = gains[c];
-  prm.count_clip = count_clip;
-  prm.clip_stats = clip_stats;
-  prm.error = ctx.d_error;
-  prm.flags = flags;
-  prm.work = ctx.d_work;
-  prm.wait_tries = ctx.wait_limit ? ctx.wait_limit : AMAZE_DEFAULT_WAIT_TRIES;
-  prm.withhold_tile = ctx.wait_withhold == RD_WAIT_AMAZE_TILE ? 0 : -1;
-  RD_LAUNCH(ctx, K_AMAZE, amaze_kernel<<<grid, THREADS, SMEM_BYTES, ctx.stream>>>(prm));
-  RD_CUDA_TRY(cudaGetLastError());
-  return Status{};
+  const size_t img_bytes = sizeof(AmazeImage) * (size_t)n;
+  const size_t seg_off = (img_bytes + 255) & ~(size_t)255;
+  const size_t table_bytes = seg_off + sizeof(AmazeSegment) * segs.size();
+  void* table = nullptr;
+  RD_TRY(device_alloc(ctx, table_bytes, &table));
+  unsigned char* tb = static_cast<unsigned char*>(table);
+  Status st = upload(ctx, tb, images.data(), img_bytes);
+  if (st.ok()) st = upload(ctx, tb + seg_off, segs.data(), sizeof(AmazeSegment) * segs.size());
+  if (st.ok() && cudaMemsetAsync(flags, 0, sizeof(unsigned) * total_tiles, ctx.stream) != cudaSuccess)
+    st = Status{RD_SYNCHRONIZATION, "demosaic flag reset failed"};
+  if (st.ok() &&
+      cudaFuncSetAttribute(amaze_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES) != cudaSuccess)
+    st = Status{RD_SYNCHRONIZATION, "demosaic shared-memory limit"};
+  if (st.ok()) {
+    AmazeParams prm;
+    prm.images = reinterpret_cast<const AmazeImage*>(tb);
+    prm.segs = reinterpret_cast<const AmazeSegment*>(tb + seg_off);
+    prm.nsegs = (int)segs.size();
+    prm.total_items = item;
+    prm.slab = ctx.amaze_scratch;
+    prm.error = ctx.d_error;
+    prm.flags = flags;
+    prm.work = ctx.d_work;
+    prm.wait_tries = ctx.wait_limit ? ctx.wait_limit : AMAZE_DEFAULT_WAIT_TRIES;
+    prm.withhold_tile = ctx.wait_withhold == RD_WAIT_AMAZE_TILE ? 0 : -1;
+    RD_LAUNCH(ctx, K_AMAZE, amaze_kernel<<<grid, THREADS, SMEM_BYTES, ctx.stream>>>(prm));
+    const cudaError_t launch = cudaGetLastError();
+    if (launch != cudaSuccess) st = Status{RD_SYNCHRONIZATION, cudaGetErrorString(launch)};
+  }
+  device_free(ctx, table, table_bytes);
+  return st;
+}
+
+Status run_amaze(Context& ctx, const MosaicSource& src, const float gains[3], float clip_point, float* rgb,
+                 int count_clip, unsigned long long* clip_stats) {
+  AmazeJob job;
+  job.src = src;
+  job.rgb = rgb;
+  job.count_clip = count_clip;
+  job.clip_stats = clip_stats;
+  job.clip_point = clip_point;
+  for (int c = 0; c < 3; ++c) job.gains[c] = gains[c];
+  return run_amaze_images(ctx, &job, 1);
 }
 
 }  // namespace rd

@@ -391,26 +391,41 @@ Status launch_normalize(Context& ctx, const MosaicSource& src, float* out, unsig
 
 // demosaic_cancellable (crates/demosaic/src/lib.rs:302-370): RCD and AMaZE run
 // on the balanced mosaic (largest gain = 1) and undo it on the output.
-Status run_demosaic(Context& ctx, const MosaicSource& src_in, int algorithm, float* rgb,
-                    unsigned long long* clip_stats) {
-  MosaicSource src = src_in;
-  const int W = src.width, H = src.height;
-  if (W < 2 || H < 2) return Status{RD_INVALID_DIMENSIONS, "demosaicing requires at least 2x2 samples"};
-  const int count_clip = (src.f32 == nullptr && src.clip) ? 1 : 0;
-  float gains[3] = {1.0f, 1.0f, 1.0f};
-  float clip_point = 1.0f;
+// ChannelBalance (crates/demosaic/src/balance.rs:24-94): RCD and AMaZE scale
+// the mosaic by gains / max(gains) and undo it on output; AMaZE's clip point
+// is the smallest forward gain.
+AmazeJob demosaic_job(const MosaicSource& src_in, int algorithm, float* rgb, unsigned long long* clip_stats) {
+  AmazeJob job;
+  job.src = src_in;
+  job.rgb = rgb;
+  job.clip_stats = clip_stats;
+  job.count_clip = (src_in.f32 == nullptr && src_in.clip) ? 1 : 0;
+  for (int c = 0; c < 3; ++c) job.gains[c] = 1.0f;
+  job.clip_point = 1.0f;
   const float* bal = src_in.fwd;  // caller passes the as-shot balance in fwd
   float largest = bal[0] > bal[1] ? bal[0] : bal[1];
   largest = largest > bal[2] ? largest : bal[2];
   float fwd[3] = {bal[0] / largest, bal[1] / largest, bal[2] / largest};
   const bool identity = fwd[0] == 1.0f && fwd[1] == 1.0f && fwd[2] == 1.0f;
   const bool balanced = (algorithm == RD_DEMOSAIC_RCD || algorithm == RD_DEMOSAIC_AMAZE) && !identity;
-  for (int c = 0; c < 3; ++c) src.fwd[c] = balanced ? fwd[c] : 1.0f;
+  for (int c = 0; c < 3; ++c) job.src.fwd[c] = balanced ? fwd[c] : 1.0f;
   if (balanced) {
-    for (int c = 0; c < 3; ++c) gains[c] = 1.0f / fwd[c];
-    clip_point = fwd[0] < fwd[1] ? fwd[0] : fwd[1];
-    clip_point = clip_point < fwd[2] ? clip_point : fwd[2];
+    for (int c = 0; c < 3; ++c) job.gains[c] = 1.0f / fwd[c];
+    job.clip_point = fwd[0] < fwd[1] ? fwd[0] : fwd[1];
+    job.clip_point = job.clip_point < fwd[2] ? job.clip_point : fwd[2];
   }
+  return job;
+}
+
+Status run_demosaic(Context& ctx, const MosaicSource& src_in, int algorithm, float* rgb,
+                    unsigned long long* clip_stats) {
+  const int W = src_in.width, H = src_in.height;
+  if (W < 2 || H < 2) return Status{RD_INVALID_DIMENSIONS, "demosaicing requires at least 2x2 samples"};
+  const AmazeJob job = demosaic_job(src_in, algorithm, rgb, clip_stats);
+  const MosaicSource& src = job.src;
+  const int count_clip = job.count_clip;
+  const float* gains = job.gains;
+  const float clip_point = job.clip_point;
   switch (algorithm) {
     case RD_DEMOSAIC_BILINEAR:
     case RD_DEMOSAIC_MHC: {

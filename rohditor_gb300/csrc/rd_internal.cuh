@@ -288,6 +288,24 @@ Status run_math_check(Context& ctx, int which, uint64_t* result);
 // Sampled device check of the optics branch's f32 hypot (rd_check_math 4).
 Status run_hypot_check(Context& ctx, uint64_t* result);
 
+// One image of a (multi-image) AMaZE launch: its mosaic source with the
+// forward channel balance in fwd, the planar RGB output, and the inverse
+// balance and clip point of demosaic_cancellable (crates/demosaic/src/lib.rs:302-392).
+struct AmazeJob {
+  MosaicSource src;
+  float* rgb;
+  int count_clip;
+  unsigned long long* clip_stats;
+  float gains[3];
+  float clip_point;
+};
+// The launch parameters of demosaicing `src_in` (as-shot balance in fwd) with
+// `algorithm` into `rgb`: the balanced source, inverse gains, clip point and
+// whether Clip statistics are counted.
+AmazeJob demosaic_job(const MosaicSource& src_in, int algorithm, float* rgb, unsigned long long* clip_stats);
+// AMaZE of n images (each larger than 32x32) in one launch over a shared
+// queue of half-tile work items.
+Status run_amaze_images(Context& ctx, const AmazeJob* jobs, int n);
 Status reserve_amaze_scratch(Context& ctx, size_t tiles);
 // AMaZE tiles of a width x height mosaic (224-pixel cores).
 size_t amaze_tiles(int width, int height);

@@ -554,11 +554,13 @@ def test_concurrent_lanes_with_different_widths_repeat_exactly(device):
             assert np.array_equal(a, b) and np.array_equal(ha, hb)
 
 
-@pytest.mark.parametrize("graph", [False, True])
-def test_batched_develop_matches_one_at_a_time(device, graph):
-    """rd_develop_batch (concurrent lanes) and rd_develop_batch_graph (one
-    captured CUDA graph) over uneven sizes, CFA phases and capture radii equal
-    the per-image path, bit for bit."""
+@pytest.mark.parametrize("mode", ["lanes", "graph", "flat"])
+def test_batched_develop_matches_one_at_a_time(device, mode):
+    """rd_develop_batch (concurrent lanes), rd_develop_batch_graph (one
+    captured CUDA graph) and rd_develop_batch_flat (stage by stage, one AMaZE
+    launch over every image's tiles) over uneven sizes, CFA phases, highlight
+    modes and capture radii equal the per-image path, bit for bit."""
+    graph = mode == "graph"
     from rohditor_gb300 import (CaptureContract, ColorContract, GpuPreviewProcessor, GpuSensorProcessor,
                                 GpuSpatialProcessor, OpticsExecution, SensorDescription, clip_levels, opposed_levels)
     from rohditor_gb300.batch import BatchImage, develop_batch
@@ -588,7 +590,7 @@ def test_batched_develop_matches_one_at_a_time(device, graph):
                               tone_lut=sixteen_knot_curve(seed=k), hsl=hsl_bands(seed=k))
         images.append(BatchImage(raw, sensor, cap, optics, preview_dimensions(w, h, 256), wb, CAMERA_TO_REC2020,
                                  color))
-    res = develop_batch(images, lanes=3, graph=graph)
+    res = develop_batch(images, lanes=3, graph=graph, flat=mode == "flat")
     outs, ms, wall = res[:3]
     assert wall > 0 and (graph or all(m > 0 for m in ms))
     if graph:
