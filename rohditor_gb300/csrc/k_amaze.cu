@@ -135,6 +135,64 @@ __device__ __forceinline__ float green_from_rb(float sample, float centre, float
 }
 
 
+// 64-bit shared-memory access of two adjacent floats (the address is 8-byte aligned).
+__device__ __forceinline__ float2 ld2(const float* p) { return *reinterpret_cast<const float2*>(p); }
+__device__ __forceinline__ void st2(float* p, float a, float b) { *reinterpret_cast<float2*>(p) = make_float2(a, b); }
+
+// The colour differences of one pixel (green.rs:46-139), from its stencil:
+// the mosaic at the pixel (cur), one and two rows up / down and columns left /
+// right, the vertical gradient weights w0 at the pixel and two rows up / down
+// (and one row up / down for the vertical weight), the horizontal weights w1
+// at the pixel, two columns left / right and one column left / right.
+struct ColourDiff {
+  float dgv, dgh, v, h, va, ha;
+};
+__device__ __forceinline__ void colour_difference(float cur, float up, float up2, float down, float down2, float left,
+                                                  float left2, float right, float right2, float w0c, float w0u2,
+                                                  float w0d2, float w0u, float w0d, float w1c, float w1l2, float w1r2,
+                                                  float w1l, float w1r, bool fcswitch, float clip_pt8,
+                                                  ColourDiff& out) {
+  const float cru = up * (w0u2 + w0c) / (w0u2 * (EPS + cur) + w0c * (EPS + up2));
+  const float crd = down * (w0d2 + w0c) / (w0d2 * (EPS + cur) + w0c * (EPS + down2));
+  const float crl = left * (w1l2 + w1c) / (w1l2 * (EPS + cur) + w1c * (EPS + left2));
+  const float crr = right * (w1r2 + w1c) / (w1r2 * (EPS + cur) + w1c * (EPS + right2));
+  const float guha = up + 0.5f * (cur - up2);
+  const float gdha = down + 0.5f * (cur - down2);
+  const float glha = left + 0.5f * (cur - left2);
+  const float grha = right + 0.5f * (cur - right2);
+  float guar = adaptive_or(cru, cur, guha);
+  float gdar = adaptive_or(crd, cur, gdha);
+  float glar = adaptive_or(crl, cur, glha);
+  float grar = adaptive_or(crr, cur, grha);
+  const float hwt = w1l / (w1l + w1r);
+  const float vwt = w0u / (w0d + w0u);
+  const float gintvha = vwt * gdha + (1.0f - vwt) * guha;
+  const float ginthha = hwt * grha + (1.0f - hwt) * glha;
+  float v, h, va, ha;
+  if (fcswitch) {
+    v = cur - (vwt * gdar + (1.0f - vwt) * guar);
+    h = cur - (hwt * grar + (1.0f - hwt) * glar);
+    va = cur - gintvha;
+    ha = cur - ginthha;
+  } else {
+    v = (vwt * gdar + (1.0f - vwt) * guar) - cur;
+    h = (hwt * grar + (1.0f - hwt) * glar) - cur;
+    va = gintvha - cur;
+    ha = ginthha - cur;
+  }
+  const bool clipped = (cur > clip_pt8) | (gintvha > clip_pt8) | (ginthha > clip_pt8);
+  if (clipped) {
+    guar = guha; gdar = gdha; glar = glha; grar = grha;
+    v = va; h = ha;
+  }
+  out.dgv = fmin_(sqr(guha - gdha), sqr(guar - gdar));
+  out.dgh = fmin_(sqr(glha - grha), sqr(glar - grar));
+  out.v = v;
+  out.h = h;
+  out.va = va;
+  out.ha = ha;
+}
+
 // A ring of RS rows (a power of two) of LEN elements; row r lives in slot r mod RS.
 template <int RS, int LEN, typename T = float>
 struct Ring {
@@ -408,62 +466,36 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
           }
         }
         __syncthreads();
-        // -- colour differences (green.rs:46-139), lag 4, rows/cols [4, 252)
+        // -- colour differences (green.rs:46-139), lag 4, rows/cols [4, 252): a
+        //    thread takes two horizontally adjacent pixels (an even column and
+        //    the next), so their stencils come in 64-bit shared loads
         {
           const int lo = max(F - BH - 4, 4), hi = min(F - 4, TS - 4);
-          for (int k = t; k < (hi - lo) * TS; k += THREADS) {
-            const int rr = lo + (k >> 8), cc = 4 + (k & (TS - 1));
-            if (cc >= TS - 4) continue;
+          for (int k = t; k < BH * 128; k += THREADS) {
+            const int rr = lo + (k >> 7), pair = k & 127;
+            if (rr >= hi || pair >= (TS - 8) / 2) continue;
+            const int a = 4 + 2 * pair;
             const bool green_first = (g0 ^ (rr & 1)) == 1;
-            const bool fcswitch = green_first == ((cc & 1) == 0);
             const float* c0 = cfa.row(rr);
-            const float cur = c0[cc];
-            const float up = cfa.row(rr - 1)[cc], up2 = cfa.row(rr - 2)[cc];
-            const float down = cfa.row(rr + 1)[cc], down2 = cfa.row(rr + 2)[cc];
-            const float left = c0[cc - 1], left2 = c0[cc - 2], right = c0[cc + 1], right2 = c0[cc + 2];
-            const float w0c = w0.row(rr)[cc], w0u2 = w0.row(rr - 2)[cc], w0d2 = w0.row(rr + 2)[cc];
+            const float2 cl = ld2(c0 + a - 2), cm = ld2(c0 + a), cr = ld2(c0 + a + 2);
+            const float2 u1 = ld2(cfa.row(rr - 1) + a), u2 = ld2(cfa.row(rr - 2) + a);
+            const float2 d1 = ld2(cfa.row(rr + 1) + a), d2 = ld2(cfa.row(rr + 2) + a);
+            const float2 wc = ld2(w0.row(rr) + a), wu2 = ld2(w0.row(rr - 2) + a), wd2 = ld2(w0.row(rr + 2) + a);
+            const float2 wu1 = ld2(w0.row(rr - 1) + a), wd1 = ld2(w0.row(rr + 1) + a);
             const float* w1r = w1.row(rr);
-            const float w1c = w1r[cc];
-            const float cru = up * (w0u2 + w0c) / (w0u2 * (EPS + cur) + w0c * (EPS + up2));
-            const float crd = down * (w0d2 + w0c) / (w0d2 * (EPS + cur) + w0c * (EPS + down2));
-            const float crl = left * (w1r[cc - 2] + w1c) / (w1r[cc - 2] * (EPS + cur) + w1c * (EPS + left2));
-            const float crr = right * (w1r[cc + 2] + w1c) / (w1r[cc + 2] * (EPS + cur) + w1c * (EPS + right2));
-            const float guha = up + 0.5f * (cur - up2);
-            const float gdha = down + 0.5f * (cur - down2);
-            const float glha = left + 0.5f * (cur - left2);
-            const float grha = right + 0.5f * (cur - right2);
-            float guar = adaptive_or(cru, cur, guha);
-            float gdar = adaptive_or(crd, cur, gdha);
-            float glar = adaptive_or(crl, cur, glha);
-            float grar = adaptive_or(crr, cur, grha);
-            const float hwt = w1r[cc - 1] / (w1r[cc - 1] + w1r[cc + 1]);
-            const float w0u = w0.row(rr - 1)[cc], w0d = w0.row(rr + 1)[cc];
-            const float vwt = w0u / (w0d + w0u);
-            const float gintvha = vwt * gdha + (1.0f - vwt) * guha;
-            const float ginthha = hwt * grha + (1.0f - hwt) * glha;
-            float v, h, va, ha;
-            if (fcswitch) {
-              v = cur - (vwt * gdar + (1.0f - vwt) * guar);
-              h = cur - (hwt * grar + (1.0f - hwt) * glar);
-              va = cur - gintvha;
-              ha = cur - ginthha;
-            } else {
-              v = (vwt * gdar + (1.0f - vwt) * guar) - cur;
-              h = (hwt * grar + (1.0f - hwt) * glar) - cur;
-              va = gintvha - cur;
-              ha = ginthha - cur;
-            }
-            const bool clipped = (cur > clip_pt8) | (gintvha > clip_pt8) | (ginthha > clip_pt8);
-            if (clipped) {
-              guar = guha; gdar = gdha; glar = glha; grar = grha;
-              v = va; h = ha;
-            }
-            dgv.row(rr)[cc] = fmin_(sqr(guha - gdha), sqr(guar - gdar));
-            dgh.row(rr)[cc] = fmin_(sqr(glha - grha), sqr(glar - grar));
-            vcd.row(rr)[cc] = v;
-            hcd.row(rr)[cc] = h;
-            valt.row(rr)[cc] = va;
-            halt.row(rr)[cc] = ha;
+            const float2 hl = ld2(w1r + a - 2), hm = ld2(w1r + a), hr = ld2(w1r + a + 2);
+            ColourDiff e, o;
+            // Even column a: green_first decides the sign; the odd column a + 1 takes the other.
+            colour_difference(cm.x, u1.x, u2.x, d1.x, d2.x, cl.y, cl.x, cm.y, cr.x, wc.x, wu2.x, wd2.x, wu1.x,
+                              wd1.x, hm.x, hl.x, hr.x, hl.y, hm.y, green_first, clip_pt8, e);
+            colour_difference(cm.y, u1.y, u2.y, d1.y, d2.y, cm.x, cl.y, cr.x, cr.y, wc.y, wu2.y, wd2.y, wu1.y,
+                              wd1.y, hm.y, hl.y, hr.y, hm.x, hr.x, !green_first, clip_pt8, o);
+            st2(dgv.row(rr) + a, e.dgv, o.dgv);
+            st2(dgh.row(rr) + a, e.dgh, o.dgh);
+            st2(vcd.row(rr) + a, e.v, o.v);
+            st2(hcd.row(rr) + a, e.h, o.h);
+            st2(valt.row(rr) + a, e.va, o.va);
+            st2(halt.row(rr) + a, e.ha, o.ha);
           }
         }
         __syncthreads();
