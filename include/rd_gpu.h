@@ -303,6 +303,16 @@ rd_status rd_check_math(rd_ctx* ctx, int32_t which, uint64_t* result);
  * be NULL except segments. RD_UNSUPPORTED when the shape has not been tuned. */
 rd_status rd_rl_launch_shape(uint32_t width, uint32_t height, float radius, int32_t* segments,
                              int32_t* default_segments, float* best_ms, float* default_ms);
+/* Launch shapes tuned across calls (no reference counterpart): the RL guide /
+ * mask kernel's row segments per strip (stage RD_SHAPE_RL_MASK, `radius` the
+ * capture radius) and the colour kernel's CTAs per SM (RD_SHAPE_COLOR,
+ * `radius` ignored). The first calls for an image shape each launch one
+ * candidate, timed; once every candidate has been timed twice the fastest is
+ * used for that shape by every context of the process. Results never depend
+ * on the shape. RD_UNSUPPORTED until the shape is tuned. */
+enum { RD_SHAPE_RL_MASK = 0, RD_SHAPE_COLOR = 1 };
+rd_status rd_launch_shape(int32_t stage, uint32_t width, uint32_t height, float radius, int32_t* value,
+                          int32_t* default_value, float* best_ms, float* default_ms);
 
 rd_status rd_source_dimensions(const rd_source* source, uint32_t* width, uint32_t* height);
 rd_status rd_source_download(rd_ctx* ctx, const rd_source* source, float* rgb_interleaved);

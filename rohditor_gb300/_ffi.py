@@ -180,6 +180,9 @@ SIGNATURES = {
     "rd_rl_launch_shape": (ctypes.c_int, [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float,
                                           ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
                                           ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
+    "rd_launch_shape": (ctypes.c_int, [ctypes.c_int32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float,
+                                       ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
+                                       ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "rd_stage_output": (ctypes.c_int, [VOIDP, F32P, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ColorDesc),
                                        ctypes.POINTER(OutputDesc), VOIDP, ctypes.c_size_t, U64P, U64P]),
     "rd_source_dimensions": (ctypes.c_int, [VOIDP, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32)]),

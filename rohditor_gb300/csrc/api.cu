@@ -129,6 +129,7 @@ Status check_kernel_error(Context& ctx, const char* stage) {
   RD_CUDA_TRY(cudaStreamSynchronize(ctx.stream));
   if (!ctx.pending.empty()) resolve_kernel_timing(ctx);
   if (!ctx.tune_runs.empty()) resolve_rl_tuning(ctx);
+  if (!ctx.shape_runs.empty()) resolve_shape_tuning(ctx);
   if (word) {
     RD_CUDA_TRY(cudaMemsetAsync(ctx.d_error, 0, sizeof(uint32_t), ctx.stream));
     std::string what;
@@ -601,6 +602,10 @@ void rd_ctx_destroy(rd_ctx* h) {
   for (auto& r : c.tune_runs) {
     cudaEventDestroy(r.second.first);
     cudaEventDestroy(r.second.second);
+  }
+  for (auto& r : c.shape_runs) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
   }
   for (auto e : c.event_pool) cudaEventDestroy(e);
   for (auto& e : c.user_ev)

@@ -1178,8 +1178,17 @@ Status launch_rl_prep_step(Context& ctx, const Taps& taps, const float* rgb, lon
   const int sms = ctx.sm_count > 0 ? ctx.sm_count : 152;
   const int slots = std::max(1, occ) * sms;
   const int strips = (W + G::SW - 1) / G::SW;
-  // About three work items per resident CTA, each at least 32 rows.
-  const int segs = std::max(1, std::min(3 * std::max(1, slots / strips), H / 32));
+  // Row segments per strip: tuned across calls per image shape (the
+  // segmentation changes only the schedule), from about three work items per
+  // resident CTA, each at least 32 rows.
+  const int per_round = std::max(1, slots / strips);
+  const int fallback = std::max(1, std::min(3 * per_round, H / 32));
+  std::vector<int> cands;
+  for (int m : {2, 3, 4, 5, 6})
+    if (H / (m * per_round) >= 32) cands.push_back(m * per_round);
+  const ShapeKey key{TUNE_RL_PREP, W, H, R};
+  const ShapePick pick = shape_begin(ctx, key, fallback, cands);
+  const int segs = pick.value;
   const int items = strips * segs;
   const int grid = std::min(items, slots);
   CUtensorMap none{};
@@ -1188,6 +1197,7 @@ Status launch_rl_prep_step(Context& ctx, const Taps& taps, const float* rgb, lon
                                 taps, rgb_map ? *rgb_map : none, ctx.d_work, ctx.d_error,
                                 ctx.wait_limit ? ctx.wait_limit : RL_DEFAULT_WAIT_TRIES,
                                 ctx.wait_withhold == RD_WAIT_RL_COPY ? 1 : 0));
+  shape_end(ctx, key, pick);
   return Status{};
 }
 
@@ -1737,5 +1747,26 @@ extern "C" rd_status rd_rl_launch_shape(uint32_t width, uint32_t height, float r
   if (default_segments) *default_segments = it->second.default_segs;
   if (best_ms) *best_ms = it->second.best_ms;
   if (default_ms) *default_ms = it->second.default_ms;
+  return RD_OK;
+}
+
+extern "C" rd_status rd_launch_shape(int32_t stage, uint32_t width, uint32_t height, float radius, int32_t* value,
+                                     int32_t* default_value, float* best_ms, float* default_ms) {
+  if (!value || (stage != RD_SHAPE_RL_MASK && stage != RD_SHAPE_COLOR)) return RD_INVALID_INPUT;
+  int c = 0;
+  if (stage == RD_SHAPE_RL_MASK) {
+    float w[rd::MAX_TAPS];
+    const int taps = rd::gaussian_kernel(radius, w, rd::MAX_TAPS);
+    if (taps < 0) return RD_INVALID_INPUT;
+    c = taps / 2;
+  }
+  const rd::ShapeKey key{stage == RD_SHAPE_RL_MASK ? rd::TUNE_RL_PREP : rd::TUNE_COLOR, (int)width, (int)height, c};
+  int v = 0, d = 0;
+  float b = 0.0f, dm = 0.0f;
+  if (!rd::shape_record(key, &v, &d, &b, &dm)) return RD_UNSUPPORTED;
+  *value = v;
+  if (default_value) *default_value = d;
+  if (best_ms) *best_ms = b;
+  if (default_ms) *default_ms = dm;
   return RD_OK;
 }

@@ -159,8 +159,14 @@ Status run_color_output(Context& ctx, const float* rgb, int W, int H, const rd_c
   }
   set_lut_pointers(p.adj, c, luts);
   const long long pixels = (long long)W * H;
-  const int grid = (int)std::min<long long>((pixels + 255) / 256, (long long)(ctx.sm_count > 0 ? ctx.sm_count : 152) * 8);
+  // Grid-stride CTAs per SM: tuned across calls per image shape (the grid
+  // changes only which CTA takes which pixels; the histogram is integer).
+  const int sms = ctx.sm_count > 0 ? ctx.sm_count : 152;
+  const ShapeKey key{TUNE_COLOR, W, H, 0};
+  const ShapePick pick = shape_begin(ctx, key, 8, {4, 16, 32});
+  const int grid = (int)std::min<long long>((pixels + 255) / 256, (long long)sms * pick.value);
   RD_LAUNCH(ctx, K_COLOR, color_kernel<<<grid, 256, 0, ctx.stream>>>(p));
+  shape_end(ctx, key, pick);
   const cudaError_t launch = cudaGetLastError();
   if (luts) device_free(ctx, luts, LUT_SET_BYTES);
   if (launch != cudaSuccess) return Status{RD_SYNCHRONIZATION, cudaGetErrorString(launch)};

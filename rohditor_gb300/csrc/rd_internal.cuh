@@ -47,6 +47,22 @@ enum KernelFamily {
 static_assert(K_FAMILY_COUNT == RD_KERNEL_FAMILIES, "family table size");
 const char* kernel_family_name(int family);
 
+// Keys of the cross-call launch-shape tuner (see shape_begin below): the
+// kernel and three shape parameters (width, height, radius or 0).
+enum TunedKernel { TUNE_RL_PREP = 0, TUNE_COLOR = 1, TUNE_KERNEL_COUNT };
+struct ShapeKey {
+  int kernel, a, b, c;
+  bool operator<(const ShapeKey& o) const {
+    if (kernel != o.kernel) return kernel < o.kernel;
+    if (a != o.a) return a < o.a;
+    if (b != o.b) return b < o.b;
+    return c < o.c;
+  }
+};
+struct ShapePick {
+  int value = 0;
+  cudaEvent_t start = nullptr;  // set when this launch is timed
+};
 struct Context {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -86,6 +102,13 @@ struct Context {
   // stage's synchronisation: (candidate segment count, start, end).
   int tune_shape[3] = {0, 0, 0};
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> tune_runs;
+  // Timed candidate launches of the cross-call shape tuner: (key, value, start, end).
+  struct ShapeRun {
+    ShapeKey key;
+    int value;
+    cudaEvent_t a, b;
+  };
+  std::vector<ShapeRun> shape_runs;
   // Bounded device waits (rd_ctx_set_wait_test): the iteration limit of each
   // wait, and which completion a test withholds so that a wait runs out.
   uint32_t wait_limit = 0;      // 0: the built-in limits
@@ -95,6 +118,24 @@ struct Context {
 // Iteration limits of the device waits when no test sets one.
 constexpr uint32_t AMAZE_DEFAULT_WAIT_TRIES = 1u << 22;
 constexpr uint32_t RL_DEFAULT_WAIT_TRIES = 1u << 20;
+
+// ---- launch-shape tuning across calls (tuner.cu) ----
+// Kernels launched once per call whose launch shape (a work-item count or a
+// grid size) changes only the schedule, never a value. The first calls for a
+// (kernel, shape) key each launch one candidate, bracketed by events on the
+// context stream and resolved at the call's synchronisation; once every
+// candidate has been timed twice, the fastest is used for the key from then
+// on, in every context of the process.
+//
+// The shape to launch with now: the tuned one, the next candidate still to
+// time (start event recorded), or the default (under stream capture).
+ShapePick shape_begin(Context& ctx, const ShapeKey& key, int default_value, const std::vector<int>& candidates);
+// After the launch: records the end event of a timed launch.
+void shape_end(Context& ctx, const ShapeKey& key, const ShapePick& pick);
+// Folds the context's timed launches into the table (after a synchronisation).
+void resolve_shape_tuning(Context& ctx);
+// The table's entry for a key: tuned value, default, their best times; false until tuned.
+bool shape_record(const ShapeKey& key, int* value, int* default_value, float* best_ms, float* default_ms);
 
 // Brackets one kernel launch with events when kernel timing is enabled, and
 // counts the launch either way.

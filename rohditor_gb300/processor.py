@@ -308,6 +308,21 @@ def rl_launch_shape(width: int, height: int, radius: float) -> RlLaunchShape | N
     return RlLaunchShape(segs.value, dflt.value, best.value, dms.value)
 
 
+def launch_shape(stage: str, width: int, height: int, radius: float = 0.0) -> RlLaunchShape | None:
+    """rd_launch_shape: the launch shape tuned across calls for `stage` ("rl_mask": row segments of the
+    capture guide / mask kernel; "color": CTAs per SM of the colour kernel) at this image size, or None
+    while it is still being tuned."""
+    value, dflt = ctypes.c_int32(), ctypes.c_int32()
+    best, dms = ctypes.c_float(), ctypes.c_float()
+    code = _ffi.load().rd_launch_shape({"rl_mask": 0, "color": 1}[stage], width, height, radius, ctypes.byref(value),
+                                      ctypes.byref(dflt), ctypes.byref(best), ctypes.byref(dms))
+    if code == _ffi.STATUS_NAMES.index("Unsupported"):
+        return None
+    if code != 0:
+        raise GpuPreviewError(code, "rd_launch_shape")
+    return RlLaunchShape(value.value, dflt.value, best.value, dms.value)
+
+
 def standard_base_lut() -> np.ndarray:
     """BaseRenderingLut::standard_v1 values (crates/core/src/rendering.rs:36-50)."""
     out = np.zeros(4096, dtype=np.float32)

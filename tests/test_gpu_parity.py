@@ -200,6 +200,30 @@ def test_capture_launch_shape_tuning_keeps_results(stages, oracle):
     assert np.array_equal(second.view(np.uint32), ref.view(np.uint32))
 
 
+def test_cross_call_shape_tuning_keeps_results(stages, oracle):
+    """The guide / mask kernel's row segments and the colour kernel's grid are
+    tuned across calls: the first calls of an image shape each launch one
+    candidate, timed, until every candidate has two timings. Every call's
+    result equals the oracle bit for bit, and the shape is then reported."""
+    from rohditor_gb300 import CaptureContract, ColorContract, launch_shape, standard_base_lut
+
+    w, h = 1532, 1020
+    rgb = np.abs(textured_mosaic(3 * w, h, seed=43)).reshape(h, 3 * w)
+    cap = CaptureContract(amount=0.5, radius=0.8, noise_protection=0.4, ceilings=(1.0, 1.0, 1.0), iterations=2)
+    ref = oracle.capture(rgb, 0.5, 0.8, 0.4, (1.0, 1.0, 1.0), 2)
+    assert launch_shape("rl_mask", w, h, 0.8) is None
+    for _ in range(14):
+        assert np.array_equal(stages.capture(rgb, cap).view(np.uint32), ref.view(np.uint32))
+    shape = launch_shape("rl_mask", w, h, 0.8)
+    assert shape is not None and shape.segments >= 1 and shape.best_ms <= shape.default_ms
+    color = ColorContract(wb_gains=(1.8, 1.0, 1.5), exposure_ev=0.2, base_lut=standard_base_lut())
+    base = np.abs(textured_mosaic(3 * 900, 700, seed=44)).reshape(700, 3 * 900)
+    outs = [stages.color(base, color) for _ in range(10)]
+    for out, hist, _ in outs[1:]:
+        assert np.array_equal(out, outs[0][0]) and np.array_equal(hist, outs[0][1])
+    assert launch_shape("color", 900, 700) is not None
+
+
 def smooth_rgb(w, h, seed):
     rng = np.random.default_rng(seed)
     yy, xx = np.mgrid[0:h, 0:w].astype(np.float32)
