@@ -471,13 +471,10 @@ Status develop_impl(rd_ctx* h, const uint16_t* d_raw, size_t row_stride, const r
     st = rd::device_alloc(ctx, mosaic_bytes, &p);
     if (st.ok()) {
       d_mosaic = static_cast<float*>(p);
-      rd::MosaicSource norm = src;
-      norm.clip = 0;
-      st = rd::launch_normalize(ctx, norm, d_mosaic, nullptr);
-    }
-    if (st.ok())
-      st = rd::run_opposed(ctx, d_mosaic, W, H, src.cfa, s.detection_levels,
+      // The cell pass of Opposed normalizes the raw samples into d_mosaic.
+      st = rd::run_opposed(ctx, src, d_mosaic, s.detection_levels,
                            s.has_neutral_ceiling ? s.neutral_ceiling : nullptr, d_stats, nullptr);
+    }
     src.f32 = d_mosaic;
     src.clip = 0;
   }
@@ -1027,12 +1024,12 @@ rd_status rd_stage_highlight(rd_ctx* h, const uint16_t* mosaic, size_t row_strid
     st = Status{RD_SYNCHRONIZATION, "memset failed"};
   if (st.ok()) {
     rd::MosaicSource src = rd::make_source(*s, static_cast<const uint16_t*>(praw), row_stride);
-    if (s->highlight == RD_HIGHLIGHT_OPPOSED) src.clip = 0;
-    st = rd::launch_normalize(ctx, src, static_cast<float*>(pout), static_cast<unsigned long long*>(pst));
-    if (st.ok() && s->highlight == RD_HIGHLIGHT_OPPOSED)
-      st = rd::run_opposed(ctx, static_cast<float*>(pout), W, H, src.cfa, s->detection_levels,
+    if (s->highlight == RD_HIGHLIGHT_OPPOSED)
+      st = rd::run_opposed(ctx, src, static_cast<float*>(pout), s->detection_levels,
                            s->has_neutral_ceiling ? s->neutral_ceiling : nullptr,
                            static_cast<unsigned long long*>(pst), nullptr);
+    else
+      st = rd::launch_normalize(ctx, src, static_cast<float*>(pout), static_cast<unsigned long long*>(pst));
   }
   uint64_t host_stats[16] = {};
   if (st.ok() && (cudaMemcpyAsync(out, pout, out_bytes, cudaMemcpyDeviceToHost, ctx.stream) != cudaSuccess ||
@@ -1073,9 +1070,18 @@ rd_status rd_stage_opposed(rd_ctx* h, const float* mosaic, uint32_t W, uint32_t 
                   cudaMemsetAsync(ps, 0, 16 * sizeof(unsigned long long), ctx.stream) != cudaSuccess))
     st = Status{RD_SYNCHRONIZATION, "upload failed"};
   uint32_t count = 0;
-  if (st.ok())
-    st = rd::run_opposed_labels(ctx, static_cast<float*>(pm), (int)W, (int)H, cfa, levels, ceiling,
+  if (st.ok()) {
+    // The normalized mosaic is the source and is reconstructed in place.
+    rd::MosaicSource src{};
+    src.f32 = static_cast<const float*>(pm);
+    src.width = (int)W;
+    src.height = (int)H;
+    src.cfa = cfa;
+    src.black_w = src.black_h = 1;
+    src.white_count = 1;
+    st = rd::run_opposed_labels(ctx, src, static_cast<float*>(pm), levels, ceiling,
                                 static_cast<unsigned long long*>(ps), static_cast<uint32_t*>(pl), &count);
+  }
   uint64_t host_stats[16] = {};
   if (st.ok() && (cudaMemcpyAsync(out, pm, bytes, cudaMemcpyDeviceToHost, ctx.stream) != cudaSuccess ||
                   cudaMemcpyAsync(host_stats, ps, sizeof(host_stats), cudaMemcpyDeviceToHost, ctx.stream) !=
@@ -1458,10 +1464,7 @@ Status flat_prepare(rd_ctx* h, const rd_batch_item& it, FlatJob& j) {
     j.mosaic_bytes = sizeof(float) * (size_t)W * H;
     RD_TRY(rd::device_alloc(ctx, j.mosaic_bytes, &p));
     j.d_mosaic = static_cast<float*>(p);
-    rd::MosaicSource norm = j.src;
-    norm.clip = 0;
-    RD_TRY(rd::launch_normalize(ctx, norm, j.d_mosaic, nullptr));
-    RD_TRY(rd::run_opposed(ctx, j.d_mosaic, W, H, j.src.cfa, s.detection_levels,
+    RD_TRY(rd::run_opposed(ctx, j.src, j.d_mosaic, s.detection_levels,
                            s.has_neutral_ceiling ? s.neutral_ceiling : nullptr, j.d_stats, nullptr));
     j.src.f32 = j.d_mosaic;
     j.src.clip = 0;

@@ -5,13 +5,19 @@
 //   1. suspected-site count (early exit as opposed.rs:75-81 when zero: every
 //      later kernel reads the count and returns), in the same pass as
 //   2. cell summaries (cells.rs:41-113): per 2x2 cell, channel means of the
-//      clean positive samples and usable / suspected flags;
+//      clean positive samples and usable / suspected flags. The pass reads the
+//      raw u16 samples and normalizes them itself (writing the f32 mosaic the
+//      estimate and the demosaic read), so no separate normalize pass runs;
 //   3. dilated mask (regions.rs:127-182): a cell is inside when any cell of
 //      its 3x3 neighbourhood holds a suspected sample (DILATION_CELLS = 1);
+//      the inside cells are also appended to a list, and every labelling
+//      kernel after this one runs over that list only (a few percent of the
+//      cells in a typical frame) instead of over the whole cell grid;
 //   4. 8-connected labelling (regions.rs:188-281) as a lock-free union-find
-//      whose root is always the smallest cell index of the component; a prefix
-//      sum over roots in raster order then gives exactly the reference's
-//      compact labels (numbered by first appearance in raster order);
+//      whose root is always the smallest cell index of the component; the
+//      roots are marked in a bitmap of the cell grid, and the prefix count of
+//      that bitmap in raster order gives exactly the reference's compact
+//      labels (numbered by first appearance in raster order);
 //   5. per-region clipped channels and wanted (channel, support) slots
 //      (region_correction.rs:134-178);
 //   6. two-pass trimmed means over each region's clean border ring plus the
@@ -51,7 +57,9 @@ struct Cell {
 };
 
 struct OpposedParams {
-  float* mosaic;
+  MosaicSource src;          // normalized samples (raw u16, or the f32 mosaic itself)
+  float* mosaic;             // reconstructed crop-sized mosaic
+  int write_mosaic;          // 1: the cell pass stores every normalized sample to `mosaic`
   int W, H, cw, ch, cfa;
   float levels[3];
   int has_ceiling;
@@ -60,16 +68,19 @@ struct OpposedParams {
   unsigned char* dilated;
   unsigned char* suspected;  // per cell: suspected-channel bits
   unsigned* sites;           // linear indices of the suspected sites (counters[2] of them)
-  unsigned* parent;
-  unsigned* labels;
-  unsigned* block_sums;
+  unsigned* cell_list;       // the dilated cells, counters[3] of them
+  unsigned* parent;          // union-find links (dilated cells only)
+  unsigned* labels;          // per dilated cell: its root, then its compact label
+  unsigned* root_bits;       // one bit per cell: the component roots
+  unsigned* word_prefix;     // per root_bits word: roots in the earlier words of its block
+  unsigned* block_sums;      // per RANK_BLOCK words: roots, then their exclusive prefix
   unsigned* region_clipped;  // per label
   unsigned* wanted;          // per label; wanted[0] = union over regions
   double* acc;               // per (label, slot): count, kept, accum, second (4 doubles)
   float* trim;               // per (label, slot): mean, tolerance
   unsigned max_labels;
   unsigned long long* stats; // 9 counters (reconstructed etc. at [1..5])
-  unsigned* counters;        // [0] suspected count, [1] region count
+  unsigned* counters;        // [0] suspected count, [1] region count, [2] sites, [3] dilated cells
   unsigned* error;
 };
 
@@ -173,6 +184,28 @@ __global__ void __launch_bounds__(128) cells_kernel(const OpposedParams p) {
     float sums[3] = {0.0f, 0.0f, 0.0f};
     unsigned counts[3] = {0, 0, 0};
     unsigned flags = 0;
+    float v[2][2];
+#pragma unroll
+    for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+      for (int dx = 0; dx < 2; ++dx) {
+        const int y = 2 * cy + dy, x = 2 * cx + dx;
+        v[dy][dx] = (y < p.H && x < p.W) ? source_normalized(p.src, x, y) : 0.0f;
+      }
+    if (p.write_mosaic) {
+#pragma unroll
+      for (int dy = 0; dy < 2; ++dy) {
+        const int y = 2 * cy + dy, x = 2 * cx;
+        if (y >= p.H) continue;
+        float* row = p.mosaic + (long long)y * p.W;
+        if (x + 1 < p.W && ((((long long)y * p.W + x) & 1) == 0)) {
+          *reinterpret_cast<float2*>(row + x) = make_float2(v[dy][0], v[dy][1]);
+        } else {
+          row[x] = v[dy][0];
+          if (x + 1 < p.W) row[x + 1] = v[dy][1];
+        }
+      }
+    }
 #pragma unroll
     for (int dy = 0; dy < 2; ++dy)
 #pragma unroll
@@ -180,7 +213,7 @@ __global__ void __launch_bounds__(128) cells_kernel(const OpposedParams p) {
         const int y = 2 * cy + dy, x = 2 * cx + dx;
         if (y >= p.H || x >= p.W) continue;
         const int ch = color_at(p.cfa, x, y);
-        const float s = p.mosaic[(long long)y * p.W + x];
+        const float s = v[dy][dx];
         const bool susp = s >= p.levels[ch], clean = !susp && s > 0.0f;
         if (susp) {
           flags |= 1u << (ch + 3);
@@ -236,18 +269,52 @@ __global__ void __launch_bounds__(128) cells_kernel(const OpposedParams p) {
   }
 }
 
-// 3. dilation + union-find initialisation
-__global__ void dilate_kernel(const OpposedParams p) {
+// 3. dilation + union-find initialisation, DILATE_CELLS cells of a row per
+// thread (their 3x3 neighbourhoods share columns, and the loads of a thread
+// are independent); the inside cells are appended to the cell list, one
+// atomic per warp.
+constexpr int DILATE_CELLS = 4;
+__global__ void __launch_bounds__(128) dilate_kernel(const OpposedParams p) {
   if (p.counters[0] == 0) return;
-  const int cx = blockIdx.x * blockDim.x + threadIdx.x, cy = blockIdx.y;
-  if (cx >= p.cw) return;
-  bool inside = false;
-  for (int y = max(cy - 1, 0); y <= min(cy + 1, p.ch - 1); ++y)
-    for (int x = max(cx - 1, 0); x <= min(cx + 1, p.cw - 1); ++x)
-      inside |= p.suspected[(long long)y * p.cw + x] != 0;
-  const long long i = (long long)cy * p.cw + cx;
-  p.dilated[i] = inside;
-  p.parent[i] = inside ? (unsigned)i : NONE;
+  const int cx0 = (blockIdx.x * blockDim.x + threadIdx.x) * DILATE_CELLS, cy = blockIdx.y;
+  unsigned inside = 0;  // bit j: cell cx0 + j is inside
+  if (cx0 < p.cw) {
+    const int y0 = max(cy - 1, 0), y1 = min(cy + 1, p.ch - 1);
+    unsigned cols = 0;  // bit k: column cx0 - 1 + k holds a suspected cell in rows y0..y1
+#pragma unroll
+    for (int k = 0; k < DILATE_CELLS + 2; ++k) {
+      const int x = cx0 - 1 + k;
+      if (x < 0 || x >= p.cw) continue;
+      unsigned v = 0;
+      for (int y = y0; y <= y1; ++y) v |= p.suspected[(long long)y * p.cw + x];
+      if (v) cols |= 1u << k;
+    }
+#pragma unroll
+    for (int j = 0; j < DILATE_CELLS; ++j) {
+      const int x = cx0 + j;
+      if (x >= p.cw) break;
+      const bool in = ((cols >> j) & 7u) != 0;  // columns x - 1, x, x + 1
+      const long long i = (long long)cy * p.cw + x;
+      p.dilated[i] = in;
+      if (in) {
+        p.parent[i] = (unsigned)i;
+        inside |= 1u << j;
+      }
+    }
+  }
+  const unsigned FULL = 0xffffffffu, lane = threadIdx.x & 31;
+  const unsigned n = __popc(inside);
+  unsigned incl = n;
+  for (int off = 1; off < 32; off <<= 1) {
+    const unsigned v = __shfl_up_sync(FULL, incl, off);
+    if (lane >= (unsigned)off) incl += v;
+  }
+  const unsigned total = __shfl_sync(FULL, incl, 31);
+  unsigned base = 0;
+  if (lane == 31 && total) base = atomicAdd(&p.counters[3], total);
+  base = __shfl_sync(FULL, base, 31) + incl - n;
+  for (int j = 0; j < DILATE_CELLS; ++j)
+    if (inside & (1u << j)) p.cell_list[base++] = (unsigned)((long long)cy * p.cw + cx0 + j);
 }
 
 // Root of i. Links only ever point to smaller indices, so shortening a path
@@ -282,45 +349,69 @@ __device__ void unite(unsigned* parent, unsigned a, unsigned b, unsigned* error)
   atomicOr(error, OPPOSED_ERROR);
 }
 
-__global__ void union_kernel(const OpposedParams p) {
-  if (p.counters[0] == 0) return;
-  const int cx = blockIdx.x * blockDim.x + threadIdx.x, cy = blockIdx.y;
-  if (cx >= p.cw) return;
-  const unsigned i = (unsigned)((long long)cy * p.cw + cx);
-  if (!p.dilated[i]) return;
-  if (cx > 0 && p.dilated[i - 1]) unite(p.parent, i, i - 1, p.error);
-  if (cy > 0) {
-    const unsigned up = i - p.cw;
-    if (cx > 0 && p.dilated[up - 1]) unite(p.parent, i, up - 1, p.error);
-    if (p.dilated[up]) unite(p.parent, i, up, p.error);
-    if (cx + 1 < p.cw && p.dilated[up + 1]) unite(p.parent, i, up + 1, p.error);
+// Grid-stride loops over the dilated cells of the list.
+#define FOR_LISTED_CELLS(k) \
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x, k##_n = p.counters[3]; k < k##_n; \
+       k += gridDim.x * blockDim.x)
+
+__global__ void __launch_bounds__(256) union_kernel(const OpposedParams p) {
+  FOR_LISTED_CELLS(k) {
+    const unsigned i = p.cell_list[k];
+    const unsigned cy = i / (unsigned)p.cw, cx = i - cy * (unsigned)p.cw;
+    if (cx > 0 && p.dilated[i - 1]) unite(p.parent, i, i - 1, p.error);
+    if (cy > 0) {
+      const unsigned up = i - p.cw;
+      if (cx > 0 && p.dilated[up - 1]) unite(p.parent, i, up - 1, p.error);
+      if (p.dilated[up]) unite(p.parent, i, up, p.error);
+      if (cx + 1 < (unsigned)p.cw && p.dilated[up + 1]) unite(p.parent, i, up + 1, p.error);
+    }
   }
 }
 
-// Flatten and count roots per block (raster order of the flat cell index).
-constexpr int SCAN_BLOCK = 1024;
-__global__ void flatten_kernel(const OpposedParams p) {
-  if (p.counters[0] == 0) return;
-  __shared__ unsigned warp_sums[SCAN_BLOCK / 32];
-  const long long n = (long long)p.cw * p.ch;
-  const long long i = (long long)blockIdx.x * SCAN_BLOCK + threadIdx.x;
-  unsigned root = 0;
-  if (i < n && p.dilated[i]) {
-    const unsigned r = find_root(p.parent, (unsigned)i, p.error);
-    p.labels[i] = r;  // provisional: the component's smallest cell index
-    root = (r == (unsigned)i);
+// Root of every dilated cell (provisional label: the component's smallest
+// cell index), and the roots marked in the bitmap.
+__global__ void __launch_bounds__(256) flatten_kernel(const OpposedParams p) {
+  FOR_LISTED_CELLS(k) {
+    const unsigned i = p.cell_list[k];
+    const unsigned r = find_root(p.parent, i, p.error);
+    p.labels[i] = r;
+    if (r == i) atomicOr(&p.root_bits[i >> 5], 1u << (i & 31));
   }
-  const unsigned ballot = __ballot_sync(0xffffffffu, root);
-  if ((threadIdx.x & 31) == 0) warp_sums[threadIdx.x >> 5] = __popc(ballot);
+}
+
+// Roots before each bitmap word within its block of RANK_BLOCK words, and
+// each block's roots.
+constexpr int RANK_BLOCK = 1024;
+__global__ void __launch_bounds__(RANK_BLOCK) rank_words_kernel(const OpposedParams p, unsigned words) {
+  if (p.counters[0] == 0) return;
+  __shared__ unsigned warp_sums[RANK_BLOCK / 32];
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned w = blockIdx.x * RANK_BLOCK + threadIdx.x;
+  const unsigned c = w < words ? __popc(p.root_bits[w]) : 0u;
+  unsigned x = c;
+  for (int off = 1; off < 32; off <<= 1) {
+    const unsigned y = __shfl_up_sync(FULL, x, off);
+    if (lane >= off) x += y;
+  }
+  if (lane == 31) warp_sums[warp] = x;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned s = 0;
-    for (int k = 0; k < SCAN_BLOCK / 32; ++k) s += warp_sums[k];
-    p.block_sums[blockIdx.x] = s;
+  if (warp == 0) {
+    unsigned v = warp_sums[lane];
+    for (int off = 1; off < 32; off <<= 1) {
+      const unsigned y = __shfl_up_sync(FULL, v, off);
+      if (lane >= off) v += y;
+    }
+    warp_sums[lane] = v;
   }
+  __syncthreads();
+  const unsigned before = (warp ? warp_sums[warp - 1] : 0u) + x - c;
+  if (w < words) p.word_prefix[w] = before;
+  if (threadIdx.x == RANK_BLOCK - 1) p.block_sums[blockIdx.x] = before + c;
 }
 
-// Exclusive scan of the per-block root counts (one block).
+// Exclusive scan of the per-block root counts (one block); the total is the
+// region count.
 __global__ void scan_blocks_kernel(const OpposedParams p, int blocks) {
   if (p.counters[0] == 0) return;
   __shared__ unsigned carry;
@@ -356,22 +447,17 @@ __global__ void scan_blocks_kernel(const OpposedParams p, int blocks) {
   if (threadIdx.x == 0) p.counters[1] = carry;
 }
 
-// Compact ids for roots: block offset + rank of the root inside its block.
-__global__ void root_ids_kernel(const OpposedParams p) {
+// Zero the per-label tables of the labels in use (label 0 is the pool).
+__global__ void clear_tables_kernel(const OpposedParams p) {
   if (p.counters[0] == 0) return;
-  __shared__ unsigned warp_sums[SCAN_BLOCK / 32];
-  const long long n = (long long)p.cw * p.ch;
-  const long long i = (long long)blockIdx.x * SCAN_BLOCK + threadIdx.x;
-  const bool root = i < n && p.dilated[i] && p.labels[i] == (unsigned)i;
-  const unsigned ballot = __ballot_sync(0xffffffffu, root);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane == 0) warp_sums[warp] = __popc(ballot);
-  __syncthreads();
-  unsigned before = p.block_sums[blockIdx.x];
-  for (int k = 0; k < warp; ++k) before += warp_sums[k];
-  before += __popc(ballot & ((1u << lane) - 1u));
-  // Roots keep their compact id (1-based) in `parent`, which is no longer needed.
-  if (root) p.parent[i] = before + 1;
+  const unsigned labels = min(p.counters[1] + 1u, p.max_labels);
+  const unsigned stride = gridDim.x * blockDim.x, t = blockIdx.x * blockDim.x + threadIdx.x;
+  for (unsigned k = t; k < labels; k += stride) {
+    p.region_clipped[k] = 0;
+    p.wanted[k] = 0;
+  }
+  const unsigned long long doubles = (unsigned long long)labels * SLOTS * 4;
+  for (unsigned long long k = t; k < doubles; k += stride) p.acc[k] = 0.0;
 }
 
 // OR `bits` into word[key] once per distinct key of the warp (neighbouring
@@ -384,44 +470,47 @@ __device__ __forceinline__ void warp_or(unsigned* word, unsigned key, unsigned b
   if (peers.thread_rank() == 0 && v) atomicOr(&word[key], v);
 }
 
-// Final compact label of each cell, the per-region clipped channels, and
-// 5. the wanted (channel, support) slots per region
-// (region_correction.rs:134-178), in one pass: both need only the cell's own
-// label.
-__global__ void relabel_kernel(const OpposedParams p) {
-  if (p.counters[0] == 0) return;
-  const int cx = blockIdx.x * blockDim.x + threadIdx.x, cy = blockIdx.y;
-  if (cx >= p.cw) return;
-  const long long i = (long long)cy * p.cw + cx;
-  unsigned label = 0;
-  if (p.dilated[i]) label = p.parent[p.labels[i]];
-  if (label >= p.max_labels) {  // cannot happen for 8-connected regions of a 3x3 dilation
-    atomicOr(p.error, OPPOSED_ERROR);
-    label = 0;
-  }
-  p.labels[i] = label;
-  const Cell c = label != 0 ? load_cell(p, cx, cy) : Cell{};  // a cell outside every region needs no summary
-  const unsigned clipped = c.flags >> 3;
-  if (label && clipped) warp_or(p.region_clipped, label, clipped);
-  if (label == 0 || clipped == 0) return;
-  unsigned bits = 0;
-  for (int ch = 0; ch < 3; ++ch) {
-    if (!(clipped & (1u << ch))) continue;
-    bool has_clean = false;
-    for (int o = 0; o < 3; ++o)
-      if (o != ch && usable(c, o) && clean(c, o)) has_clean = true;
-    if (!has_clean) continue;
-    const int pos = pattern_position(ch, support_mask(c, ch, p.levels));
-    if (pos >= 0) bits |= 1u << (ch * PATTERNS + pos);
-  }
-  if (bits) {
-    warp_or(p.wanted, label, bits);
-    warp_or(p.wanted, 0u, bits);
+// Final compact label of each dilated cell (1 + the roots before its root in
+// raster order), the per-region clipped channels, and 5. the wanted
+// (channel, support) slots per region (region_correction.rs:134-178), in one
+// pass: both need only the cell's own label.
+__global__ void __launch_bounds__(256) relabel_kernel(const OpposedParams p) {
+  FOR_LISTED_CELLS(k) {
+    const unsigned i = p.cell_list[k];
+    const unsigned r = p.labels[i], w = r >> 5;
+    unsigned label =
+        p.block_sums[w / RANK_BLOCK] + p.word_prefix[w] + __popc(p.root_bits[w] & ((1u << (r & 31)) - 1u)) + 1u;
+    if (label >= p.max_labels) {  // cannot happen for 8-connected regions of a 3x3 dilation
+      atomicOr(p.error, OPPOSED_ERROR);
+      label = 0;
+    }
+    p.labels[i] = label;
+    if (label == 0) continue;
+    const unsigned cy = i / (unsigned)p.cw, cx = i - cy * (unsigned)p.cw;
+    const Cell c = load_cell(p, (int)cx, (int)cy);
+    const unsigned clipped = c.flags >> 3;
+    if (clipped == 0) continue;
+    warp_or(p.region_clipped, label, clipped);
+    unsigned bits = 0;
+    for (int ch = 0; ch < 3; ++ch) {
+      if (!(clipped & (1u << ch))) continue;
+      bool has_clean = false;
+      for (int o = 0; o < 3; ++o)
+        if (o != ch && usable(c, o) && clean(c, o)) has_clean = true;
+      if (!has_clean) continue;
+      const int pos = pattern_position(ch, support_mask(c, ch, p.levels));
+      if (pos >= 0) bits |= 1u << (ch * PATTERNS + pos);
+    }
+    if (bits) {
+      warp_or(p.wanted, label, bits);
+      warp_or(p.wanted, 0u, bits);
+    }
   }
 }
 
-// 6. region border statistics; pass 0 = moments, pass 1 = trimmed sums.
-__global__ void border_kernel(const OpposedParams p, int pass) {
+// 6. region border statistics over the dilated cells; pass 0 = moments, pass
+// 1 = trimmed sums.
+__global__ void __launch_bounds__(256) border_kernel(const OpposedParams p, int pass) {
   if (p.counters[0] == 0) return;
   __shared__ double pool[SLOTS][3];
   __shared__ unsigned pool_n[SLOTS];
@@ -430,13 +519,13 @@ __global__ void border_kernel(const OpposedParams p, int pass) {
     pool_n[threadIdx.x] = 0;
   }
   __syncthreads();
-  const int cx = blockIdx.x * blockDim.x + threadIdx.x, cy = blockIdx.y;
-  if (cx < p.cw) {
-    const long long i = (long long)cy * p.cw + cx;
+  FOR_LISTED_CELLS(k) {
+    const unsigned i = p.cell_list[k];
     const unsigned label = p.labels[i];
-    // Only cells inside a region contribute: the others skip the summary load.
-    const Cell c = label != 0 ? load_cell(p, cx, cy) : Cell{};
-    if (label != 0 && (c.flags >> 3) == 0) {
+    if (label == 0) continue;
+    const unsigned cy = i / (unsigned)p.cw, cx = i - cy * (unsigned)p.cw;
+    const Cell c = load_cell(p, (int)cx, (int)cy);
+    if ((c.flags >> 3) == 0) {
       const unsigned rclip = p.region_clipped[label];
       const unsigned want_r = p.wanted[label], want_any = p.wanted[0];
       for (int ch = 0; ch < 3; ++ch) {
@@ -683,25 +772,33 @@ __global__ void __launch_bounds__(256) estimate_kernel(const OpposedParams p) {
     const unsigned sum = __reduce_add_sync(0xffffffffu, counts[k]);
     if ((threadIdx.x & 31) == 0 && sum) atomicAdd(&p.stats[1 + k], (unsigned long long)sum);
   }
+  if (threadIdx.x == 0 && blockIdx.x == 0) p.stats[0] = p.counters[0];
 }
 
-__global__ void copy_suspected_kernel(const OpposedParams p) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) p.stats[0] = p.counters[0];
+// The compact label of every dilated cell into a zeroed cell grid.
+__global__ void __launch_bounds__(256) labels_out_kernel(const OpposedParams p, uint32_t* out) {
+  FOR_LISTED_CELLS(k) {
+    const unsigned i = p.cell_list[k];
+    out[i] = p.labels[i];
+  }
 }
 
 }  // namespace
 
-// reconstruct_opposed_cancellable on a crop-sized normalized mosaic, in place.
-// d_stats (9 counters) follows OpposedStats; labels_out (optional, device,
+// reconstruct_opposed_cancellable on the crop-sized normalized mosaic of
+// `src`, written to `mosaic` (in place when src.f32 == mosaic). d_stats (9
+// counters) follows OpposedStats; labels_out (optional, device,
 // ceil(w/2)*ceil(h/2)) receives the compact region labels.
-Status run_opposed_labels(Context& ctx, float* mosaic, int W, int H, int cfa, const float levels[3],
+Status run_opposed_labels(Context& ctx, const MosaicSource& src, float* mosaic, const float levels[3],
                           const float* ceiling, unsigned long long* d_stats, uint32_t* labels_out,
                           uint32_t* region_count_out) {
+  const int W = src.width, H = src.height;
   const int cw = W / 2 + W % 2, chh = H / 2 + H % 2;
   const long long cells = (long long)cw * chh;
   // max_regions (regions.rs:117-124): raw-mask cells of separate regions are >= 4 cells apart.
   const unsigned max_labels = (unsigned)(((cw + 3) / 4) * ((chh + 3) / 4) + 1);
-  const int scan_blocks = (int)((cells + SCAN_BLOCK - 1) / SCAN_BLOCK);
+  const unsigned words = (unsigned)((cells + 31) / 32);
+  const int rank_blocks = (int)((words + RANK_BLOCK - 1) / RANK_BLOCK);
   size_t bytes = 0;
   auto take = [&](size_t n) {
     const size_t at = bytes;
@@ -713,23 +810,30 @@ Status run_opposed_labels(Context& ctx, float* mosaic, int W, int H, int cfa, co
   const size_t o_susp = take(cells);
   const size_t o_parent = take(sizeof(unsigned) * cells);
   const size_t o_labels = take(sizeof(unsigned) * cells);
+  const size_t o_list = take(sizeof(unsigned) * cells);
   const size_t o_sites = take(sizeof(unsigned) * (size_t)W * H);
-  const size_t o_bsum = take(sizeof(unsigned) * scan_blocks);
+  const size_t o_prefix = take(sizeof(unsigned) * words);
+  const size_t o_bsum = take(sizeof(unsigned) * rank_blocks);
   const size_t o_rclip = take(sizeof(unsigned) * max_labels);
   const size_t o_wanted = take(sizeof(unsigned) * max_labels);
   const size_t o_acc = take(sizeof(double) * 4 * SLOTS * (size_t)max_labels);
   const size_t o_trim = take(sizeof(float) * 2 * SLOTS * (size_t)max_labels);
+  // The root bitmap and the counters, the only memory zeroed before the kernels.
+  const size_t o_bits = take(sizeof(unsigned) * words);
   const size_t o_cnt = take(sizeof(unsigned) * 4);
   void* base = nullptr;
   RD_TRY(device_alloc(ctx, bytes, &base));
   char* b = static_cast<char*>(base);
   OpposedParams p{};
+  p.src = src;
+  p.src.clip = 0;
   p.mosaic = mosaic;
+  p.write_mosaic = src.f32 == mosaic ? 0 : 1;
   p.W = W;
   p.H = H;
   p.cw = cw;
   p.ch = chh;
-  p.cfa = cfa;
+  p.cfa = src.cfa;
   for (int c = 0; c < 3; ++c) {
     p.levels[c] = levels[c];
     p.ceiling[c] = ceiling ? ceiling[c] : 0.0f;
@@ -739,8 +843,11 @@ Status run_opposed_labels(Context& ctx, float* mosaic, int W, int H, int cfa, co
   p.dilated = reinterpret_cast<unsigned char*>(b + o_dil);
   p.suspected = reinterpret_cast<unsigned char*>(b + o_susp);
   p.sites = reinterpret_cast<unsigned*>(b + o_sites);
+  p.cell_list = reinterpret_cast<unsigned*>(b + o_list);
   p.parent = reinterpret_cast<unsigned*>(b + o_parent);
   p.labels = reinterpret_cast<unsigned*>(b + o_labels);
+  p.root_bits = reinterpret_cast<unsigned*>(b + o_bits);
+  p.word_prefix = reinterpret_cast<unsigned*>(b + o_prefix);
   p.block_sums = reinterpret_cast<unsigned*>(b + o_bsum);
   p.region_clipped = reinterpret_cast<unsigned*>(b + o_rclip);
   p.wanted = reinterpret_cast<unsigned*>(b + o_wanted);
@@ -750,32 +857,30 @@ Status run_opposed_labels(Context& ctx, float* mosaic, int W, int H, int cfa, co
   p.stats = d_stats;
   p.counters = reinterpret_cast<unsigned*>(b + o_cnt);
   p.error = ctx.d_error;
-  // Zero the per-label tables and counters (labels, dilation and cells are fully written).
-  RD_CUDA_TRY(cudaMemsetAsync(b + o_rclip, 0, o_cnt + 256 - o_rclip, ctx.stream));
+  RD_CUDA_TRY(cudaMemsetAsync(b + o_bits, 0, bytes - o_bits, ctx.stream));
+  const int sms = ctx.sm_count > 0 ? ctx.sm_count : 152;
   const dim3 cgrid((cw + 127) / 128, chh);
+  const dim3 dgrid((cw + 128 * DILATE_CELLS - 1) / (128 * DILATE_CELLS), chh);
+  const int lgrid = sms * 8;  // list kernels: 256-thread blocks, grid-stride
   RD_LAUNCH(ctx, K_OPPOSED, cells_kernel<<<cgrid, 128, 0, ctx.stream>>>(p));
-  RD_LAUNCH(ctx, K_OPPOSED, dilate_kernel<<<cgrid, 128, 0, ctx.stream>>>(p));
-  RD_LAUNCH(ctx, K_OPPOSED, union_kernel<<<cgrid, 128, 0, ctx.stream>>>(p));
-  RD_LAUNCH(ctx, K_OPPOSED, flatten_kernel<<<scan_blocks, SCAN_BLOCK, 0, ctx.stream>>>(p));
-  RD_LAUNCH(ctx, K_OPPOSED, scan_blocks_kernel<<<1, 1024, 0, ctx.stream>>>(p, scan_blocks));
-  RD_LAUNCH(ctx, K_OPPOSED, root_ids_kernel<<<scan_blocks, SCAN_BLOCK, 0, ctx.stream>>>(p));
-  RD_LAUNCH(ctx, K_OPPOSED, relabel_kernel<<<cgrid, 128, 0, ctx.stream>>>(p));
-  RD_LAUNCH(ctx, K_OPPOSED, border_kernel<<<cgrid, 128, 0, ctx.stream>>>(p, 0));
+  RD_LAUNCH(ctx, K_OPPOSED, dilate_kernel<<<dgrid, 128, 0, ctx.stream>>>(p));
+  RD_LAUNCH(ctx, K_OPPOSED, union_kernel<<<lgrid, 256, 0, ctx.stream>>>(p));
+  RD_LAUNCH(ctx, K_OPPOSED, flatten_kernel<<<lgrid, 256, 0, ctx.stream>>>(p));
+  RD_LAUNCH(ctx, K_OPPOSED, rank_words_kernel<<<rank_blocks, RANK_BLOCK, 0, ctx.stream>>>(p, words));
+  RD_LAUNCH(ctx, K_OPPOSED, scan_blocks_kernel<<<1, 1024, 0, ctx.stream>>>(p, rank_blocks));
+  RD_LAUNCH(ctx, K_OPPOSED, clear_tables_kernel<<<sms * 2, 256, 0, ctx.stream>>>(p));
+  RD_LAUNCH(ctx, K_OPPOSED, relabel_kernel<<<lgrid, 256, 0, ctx.stream>>>(p));
+  RD_LAUNCH(ctx, K_OPPOSED, border_kernel<<<lgrid, 256, 0, ctx.stream>>>(p, 0));
   RD_LAUNCH(ctx, K_OPPOSED, finish_moments_kernel<<<256, 256, 0, ctx.stream>>>(p));
-  RD_LAUNCH(ctx, K_OPPOSED, border_kernel<<<cgrid, 128, 0, ctx.stream>>>(p, 1));
-  RD_LAUNCH(ctx, K_OPPOSED, estimate_kernel<<<(ctx.sm_count > 0 ? ctx.sm_count : 152) * 8, 256, 0, ctx.stream>>>(p));
-  RD_LAUNCH(ctx, K_OPPOSED, copy_suspected_kernel<<<1, 32, 0, ctx.stream>>>(p));
+  RD_LAUNCH(ctx, K_OPPOSED, border_kernel<<<lgrid, 256, 0, ctx.stream>>>(p, 1));
+  RD_LAUNCH(ctx, K_OPPOSED, estimate_kernel<<<sms * 8, 256, 0, ctx.stream>>>(p));
   cudaError_t launch = cudaGetLastError();
   if (launch == cudaSuccess && labels_out) {
-    // With no suspected site the labelling kernels returned early: report empty labels.
+    // Cells outside every region keep label 0 (with no suspected site, all of them).
     launch = cudaMemsetAsync(labels_out, 0, sizeof(uint32_t) * cells, ctx.stream);
     if (launch == cudaSuccess) {
-      unsigned suspected = 0;
-      launch = cudaMemcpyAsync(&suspected, p.counters, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx.stream);
-      if (launch == cudaSuccess) launch = cudaStreamSynchronize(ctx.stream);
-      if (launch == cudaSuccess && suspected)
-        launch = cudaMemcpyAsync(labels_out, p.labels, sizeof(uint32_t) * cells, cudaMemcpyDeviceToDevice,
-                                 ctx.stream);
+      RD_LAUNCH(ctx, K_OPPOSED, labels_out_kernel<<<lgrid, 256, 0, ctx.stream>>>(p, labels_out));
+      launch = cudaGetLastError();
     }
   }
   if (launch == cudaSuccess && region_count_out) {
@@ -789,9 +894,9 @@ Status run_opposed_labels(Context& ctx, float* mosaic, int W, int H, int cfa, co
   return Status{};
 }
 
-Status run_opposed(Context& ctx, float* mosaic, int W, int H, int cfa, const float levels[3], const float* ceiling,
+Status run_opposed(Context& ctx, const MosaicSource& src, float* mosaic, const float levels[3], const float* ceiling,
                    unsigned long long* d_stats, uint32_t* region_count) {
-  return run_opposed_labels(ctx, mosaic, W, H, cfa, levels, ceiling, d_stats, nullptr, region_count);
+  return run_opposed_labels(ctx, src, mosaic, levels, ceiling, d_stats, nullptr, region_count);
 }
 
 }  // namespace rd

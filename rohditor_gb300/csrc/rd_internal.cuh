@@ -251,9 +251,13 @@ __device__ __forceinline__ int mirror_index(int index, int length) {
 // ------------------------------------------------------------------ stage launchers
 // Each returns after enqueueing on ctx.stream. Planar RGB outputs.
 Status launch_normalize(Context& ctx, const MosaicSource& src, float* out, unsigned long long* clip_stats);
-Status run_opposed(Context& ctx, float* mosaic, int width, int height, int cfa, const float levels[3],
-                   const float* ceiling, unsigned long long* d_stats, uint32_t* region_count);
-Status run_opposed_labels(Context& ctx, float* mosaic, int width, int height, int cfa, const float levels[3],
+// Opposed on the normalized samples of `src` (Clip is never applied here): the
+// reconstructed crop-sized mosaic is written to `mosaic` (width*height f32).
+// With src.f32 == mosaic the reconstruction is in place; otherwise the cell
+// pass normalizes the raw samples and writes every one of them to `mosaic`.
+Status run_opposed(Context& ctx, const MosaicSource& src, float* mosaic, const float levels[3], const float* ceiling,
+                   unsigned long long* d_stats, uint32_t* region_count);
+Status run_opposed_labels(Context& ctx, const MosaicSource& src, float* mosaic, const float levels[3],
                           const float* ceiling, unsigned long long* d_stats, uint32_t* labels_out,
                           uint32_t* region_count);
 Status run_demosaic(Context& ctx, const MosaicSource& src, int algorithm, float* rgb, unsigned long long* clip_stats);
