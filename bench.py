@@ -38,6 +38,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes
+import gc
 import json
 import os
 import shutil
@@ -335,15 +336,21 @@ class DevelopBench:
     def timed(self, step, steps: int) -> tuple[float, list[float]]:
         lib, h, dev = self.lib, self.h, self.dev
         total, per = 0.0, []
-        for _ in range(steps):
-            dev.check(lib.rd_ctx_flush_l2(h))
-            dev.check(lib.rd_ctx_event_record(h, 0))
-            step()
-            dev.check(lib.rd_ctx_event_record(h, 1))
-            ms = ctypes.c_float()
-            dev.check(lib.rd_ctx_event_elapsed(h, 0, 1, ctypes.byref(ms)))
-            per.append(ms.value)
-            total += ms.value
+        # No garbage-collector pause may stall the host between the launches of a step.
+        gc.collect()
+        gc.disable()
+        try:
+            for _ in range(steps):
+                dev.check(lib.rd_ctx_flush_l2(h))
+                dev.check(lib.rd_ctx_event_record(h, 0))
+                step()
+                dev.check(lib.rd_ctx_event_record(h, 1))
+                ms = ctypes.c_float()
+                dev.check(lib.rd_ctx_event_elapsed(h, 0, 1, ctypes.byref(ms)))
+                per.append(ms.value)
+                total += ms.value
+        finally:
+            gc.enable()
         return total, per
 
     def kernel_table(self, steps: int) -> tuple[dict, dict, float]:
@@ -447,7 +454,7 @@ def run_ours(args, world, rank, local, pg):
     barrier(pg)
     dev.synchronize()
     clocks = ClockSampler(local).__enter__()
-    total_ms, _ = b.timed(b.step_device, args.steps)
+    total_ms, step_ms = b.timed(b.step_device, args.steps)
     dev.synchronize()
     launches = dev.kernel_launches - launches0
     barrier(pg)
@@ -474,6 +481,8 @@ def run_ours(args, world, rank, local, pg):
         "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": b.mos_bytes,
                 "d2h_bytes_per_step": b.d2h_bytes, "ms_per_step": round(e2e_ms / args.steps, 3)},
         "gpu_launches": int(launches),
+        "step_ms": {"min": round(min(step_ms), 3), "median": round(statistics.median(step_ms), 3),
+                    "max": round(max(step_ms), 3)},
         "roofline": roofline,
         "hbm_roofline": hbm_roofline,
         "kernels": kernels,

@@ -29,6 +29,8 @@
 // scan; the trimmed means agree to f64 rounding, which is far below f32.
 // Every retry loop carries an iteration limit and reports through the error
 // word instead of spinning.
+#include <algorithm>
+
 #include <cooperative_groups.h>
 #include <cooperative_groups/reduce.h>
 #include <cuda_runtime.h>
@@ -51,6 +53,11 @@ constexpr unsigned NONE = 0xFFFFFFFFu;
 constexpr int UNION_LIMIT = 1 << 20;
 constexpr unsigned OPPOSED_ERROR = 16u;
 
+// The estimate runs on tiles of ETX x ETY target cells; a tile stages the
+// cells within LAST_RADIUS of its own (ESW x ESH) in shared memory.
+constexpr int ETX = 16, ETY = 8, ETHREADS = 128;
+constexpr int ESW = ETX + 2 * LAST_RADIUS, ESH = ETY + 2 * LAST_RADIUS, ESN = ESW * ESH;
+
 struct Cell {
   float m[3];
   unsigned flags;
@@ -67,7 +74,8 @@ struct OpposedParams {
   float4* cells;             // xyz = means, w = flags (as bits)
   unsigned char* dilated;
   unsigned char* suspected;  // per cell: suspected-channel bits
-  unsigned* sites;           // linear indices of the suspected sites (counters[2] of them)
+  unsigned* tile_flags;      // per estimate tile: 1 once a cell of it holds a suspected sample
+  unsigned* tile_list;       // the flagged estimate tiles, counters[2] of them
   unsigned* cell_list;       // the dilated cells, counters[3] of them
   unsigned* parent;          // union-find links (dilated cells only)
   unsigned* labels;          // per dilated cell: its root, then its compact label
@@ -80,7 +88,9 @@ struct OpposedParams {
   float* trim;               // per (label, slot): mean, tolerance
   unsigned max_labels;
   unsigned long long* stats; // 9 counters (reconstructed etc. at [1..5])
-  unsigned* counters;        // [0] suspected count, [1] region count, [2] sites, [3] dilated cells
+  unsigned* counters;        // [0] suspected count, [1] region count, [2] estimate tiles, [3] dilated cells,
+                             // [4] estimate tiles handed out
+  int tiles_x;               // estimate tiles per row
   unsigned* error;
 };
 
@@ -171,8 +181,9 @@ __device__ __forceinline__ int pattern_position(int ch, unsigned support) {
 // 1 + 2. suspected sites and cell summaries (cells.rs:41-113) in one pass over
 // the mosaic: per 2x2 cell the channel means of the clean positive samples
 // (summed in raster order), the usable / suspected flags, a byte of suspected
-// bits for the dilation, and the suspected-site counts per channel, reduced
-// per block before they reach the global counters.
+// bits for the dilation, the estimate tiles holding suspected samples, and the
+// suspected-site counts per channel, reduced per block before they reach the
+// global counters.
 __global__ void __launch_bounds__(128) cells_kernel(const OpposedParams p) {
   __shared__ unsigned block_counts[4];
   if (threadIdx.x < 4) block_counts[threadIdx.x] = 0;
@@ -240,21 +251,10 @@ __global__ void __launch_bounds__(128) cells_kernel(const OpposedParams p) {
     p.cells[i] = make_float4(m[0], m[1], m[2], __uint_as_float(flags));
     p.suspected[i] = (unsigned char)(flags >> 3);
   }
-  // Append the cell's suspected sites to the list: one atomic per warp.
-  {
-    const unsigned FULL = 0xffffffffu, lane = threadIdx.x & 31;
-    const unsigned n_sites = __popc(smask);
-    unsigned incl = n_sites;
-    for (int off = 1; off < 32; off <<= 1) {
-      const unsigned v = __shfl_up_sync(FULL, incl, off);
-      if (lane >= (unsigned)off) incl += v;
-    }
-    const unsigned total = __shfl_sync(FULL, incl, 31);
-    unsigned base = 0;
-    if (lane == 31 && total) base = atomicAdd(&p.counters[2], total);
-    base = __shfl_sync(FULL, base, 31) + incl - n_sites;
-    for (unsigned k = 0; k < 4; ++k)
-      if (smask & (1u << k)) p.sites[base++] = (unsigned)((long long)(2 * cy + (k >> 1)) * p.W + 2 * cx + (k & 1));
+  // Flag the cell's estimate tile; its first flagging appends it to the tile list.
+  if (smask) {
+    const unsigned tile = (unsigned)((cy / ETY) * p.tiles_x + cx / ETX);
+    if (atomicExch(&p.tile_flags[tile], 1u) == 0u) p.tile_list[atomicAdd(&p.counters[2], 1u)] = tile;
   }
   // A cell holds at most four sites, so the per-channel counts of a warp fit
   // 8-bit fields of one word.
@@ -639,138 +639,242 @@ __constant__ char2 c_ring[48] = {
     {3, 2}, {-3, 3}, {-2, 3}, {-1, 3}, {0, 3}, {1, 3}, {2, 3}, {3, 3},
 };
 
-// 7. per-site estimate (opposed.rs:86-180, 236-330)
-// The estimate of one suspected site (x, y); counts[5]: reconstructed,
-// changed, fallback, unsupported, neutralised.
-__device__ void estimate_site(const OpposedParams& p, int x, int y, unsigned (&counts)[5]) {
-  unsigned& n_rec = counts[0];
-  unsigned& n_changed = counts[1];
-  unsigned& n_fallback = counts[2];
-  unsigned& n_unsup = counts[3];
-  unsigned& n_neutral = counts[4];
-  {
-    float& s = p.mosaic[(long long)y * p.W + x];
-    const int ch = color_at(p.cfa, x, y);
-    const float level = p.levels[ch];
-    {
-      const int tx = x / 2, ty = y / 2;
-      const Cell target = load_cell(p, tx, ty);
-      int support_count = 0;
-      for (int o = 0; o < 3; ++o)
-        if (o != ch && usable(target, o) && clean(target, o)) support_count++;
-      bool ok = false;
-      float estimate = 0.0f;
-      if (support_count != 0) {
-        const unsigned support = support_mask(target, ch, p.levels);
-        float ref;
-        if (reference_value(target, support, ref)) {
-          float tratio = 0.0f;
-          const bool has_tratio = log_ratio(target, support, tratio);
-          float corr[MAX_CANDIDATES];
-          int count = 0;
-          bool has_local = false;
-          float local = 0.0f;
-          int local_radius = 0;
-          for (int radius = 1; radius <= LAST_RADIUS && !has_local; ++radius) {
-            // The ring's cells from the offset table (no pass over the square's
-            // interior); the candidates are sorted below, so the visiting order
-            // does not matter, and the three rings hold 48 = MAX_CANDIDATES cells.
-            const int ring0 = 4 * radius * (radius - 1), ring_n = 8 * radius;
-            for (int q = 0; q < ring_n; ++q) {
-              const int cx = tx + c_ring[ring0 + q].x, cy = ty + c_ring[ring0 + q].y;
-              if ((unsigned)cx >= (unsigned)p.cw || (unsigned)cy >= (unsigned)p.ch) continue;
-              const Cell cand = load_cell(p, cx, cy);
-              if (!(usable(cand, ch) && clean(cand, ch))) continue;
-              float value;
-              if (!correction(cand, ch, support, p.levels, value)) continue;
-              float cratio = 0.0f;
-              const bool has_cratio = log_ratio(cand, support, cratio);
-              if (!chroma_agrees(support, has_tratio, tratio, has_cratio, cratio)) continue;
-              if (count < MAX_CANDIDATES) corr[count++] = value;
-            }
-            if (count >= MIN_CANDIDATES) {
-              for (int a = 1; a < count; ++a) {  // insertion sort, total order
-                const float v = corr[a];
-                int b = a - 1;
-                while (b >= 0 && total_less(v, corr[b])) {
-                  corr[b + 1] = corr[b];
-                  --b;
-                }
-                corr[b + 1] = v;
-              }
-              const int mid = count / 2;
-              local = count % 2 == 0 ? (corr[mid - 1] + corr[mid]) * 0.5f : corr[mid];
-              local_radius = radius;
-              has_local = true;
-            }
-          }
-          const unsigned label = p.labels[(long long)ty * p.cw + tx];
-          bool has_region = false;
-          float region = 0.0f;
-          const int pos = pattern_position(ch, support);
-          if (pos >= 0) {
-            const int off = ch * PATTERNS + pos;
-            const bool want_ratio = __popc(support) == 2;
-            float bratio = 0.0f;
-            bool has_bratio = false;
-            if (slot_value(p, (long long)label * SLOTS + off, want_ratio, region, has_bratio, bratio) ||
-                slot_value(p, off, want_ratio, region, has_bratio, bratio))
-              has_region = chroma_agrees(support, has_tratio, tratio, has_bratio, bratio);
-          }
-          float correction_value = 0.0f;
-          bool have = true;
-          if (has_local && has_region) {
-            const float weight = (float)(LAST_RADIUS + 1 - local_radius) / (float)LAST_RADIUS;
-            correction_value = weight * local + (1.0f - weight) * region;
-          } else if (has_local) {
-            correction_value = local;
-          } else if (has_region) {
-            correction_value = region;
-          } else {
-            have = false;
-          }
-          if (have) {
-            estimate = ref + correction_value;
-            ok = isfinite(estimate) && estimate > 0.0f;
-          }
-        }
-      }
-      bool neutralise = false;
-      if (!ok) {
-        n_fallback++;
-        if (support_count == 0) n_unsup++;
-        neutralise = true;
-      } else {
-        n_rec++;
-        float bounded = MAX_ESTIMATE_MULT * level;
-        if (estimate < bounded) bounded = estimate;  // f32::min of finite values
-        if (bounded > s) {
-          s = bounded;
-          n_changed++;
-        } else {
-          neutralise = true;
-        }
-      }
-      if (neutralise && p.has_ceiling && s > p.ceiling[ch]) {
-        s = p.ceiling[ch];
-        n_neutral++;
-      }
+// 7. per-site estimate (opposed.rs:86-180, 236-330) on tiles of target cells.
+// A candidate cell's correction for (channel, support) and its log ratio for
+// a channel pair depend only on the cell, so a tile computes them once for
+// every cell it stages (9 corrections, 3 pair ratios; NaN = the candidate is
+// skipped) and its sites read them from shared memory. The values are the
+// ones correction() and log_ratio() return, so the candidates, their median
+// and every estimate are unchanged.
+struct EstimateSmem {
+  float4 cell[ESN];
+  float root[ESN][3];   // cube root of each bright-clean channel's mean (else 0)
+  float corr[ESN][9];   // [channel * PATTERNS + pattern]
+  float ratio[ESN][3];  // [channel]: log ratio of the other two channels when both are bright-clean
+};
+
+__device__ void stage_candidate(const OpposedParams& p, EstimateSmem& S, int k, int gx, int gy) {
+  const float qnan = __int_as_float(0x7fc00000);
+  if ((unsigned)gx >= (unsigned)p.cw || (unsigned)gy >= (unsigned)p.ch) {
+    S.cell[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    for (int j = 0; j < 3; ++j) S.root[k][j] = 0.0f;
+    for (int j = 0; j < 9; ++j) S.corr[k][j] = qnan;
+    for (int j = 0; j < 3; ++j) S.ratio[k][j] = qnan;
+    return;
+  }
+  const Cell c = load_cell(p, gx, gy);
+  S.cell[k] = make_float4(c.m[0], c.m[1], c.m[2], __uint_as_float(c.flags));
+  // correction(), reference_value() and log_ratio() restated from the
+  // bright-clean channels. A bright-clean mean is finite and positive (it
+  // exceeds a positive level), so reference_value() succeeds for any
+  // non-empty support of them, and its pair reference sums the two cube roots
+  // in channel order from 0 (0 + r = r): each root is taken once per cell.
+  bool bright[3];
+  float root[3];
+#pragma unroll
+  for (int ch = 0; ch < 3; ++ch) {
+    bright[ch] = bright_clean(c, ch, p.levels);
+    root[ch] = bright[ch] ? cbrtf(c.m[ch]) : 0.0f;
+    S.root[k][ch] = root[ch];
+  }
+#pragma unroll
+  for (int ch = 0; ch < 3; ++ch) {
+    const int o0 = ch == 0 ? 1 : 0, o1 = ch == 2 ? 1 : 2;  // support_patterns: {o0}, {o1}, {o0, o1}
+    const bool pair = bright[o0] && bright[o1];
+    const float mean_root = (root[o0] + root[o1]) / 2.0f;
+    const float ref[3] = {c.m[o0], c.m[o1], mean_root * mean_root * mean_root};
+    const bool ok[3] = {bright[ch] && bright[o0], bright[ch] && bright[o1], bright[ch] && pair};
+#pragma unroll
+    for (int q = 0; q < PATTERNS; ++q) {
+      const float v = c.m[ch] - ref[q];
+      S.corr[k][ch * PATTERNS + q] = ok[q] && isfinite(v) ? v : qnan;
     }
+    float r = qnan;
+    if (pair) {
+      const float ratio = c.m[o0] / c.m[o1];
+      if (isfinite(ratio) && ratio > 0.0f) r = log2f(ratio);
+    }
+    S.ratio[k][ch] = r;
   }
 }
 
-// 7. per-site estimate over the suspected sites listed by the cell pass, a
-// grid-stride loop whose warps are made of suspected sites only.
-__global__ void __launch_bounds__(256) estimate_kernel(const OpposedParams p) {
-  const unsigned n = p.counters[2];
+// The estimate of one suspected site (x, y) of target cell (lx, ly) of the
+// tile (staged coordinates); counts[5]: reconstructed, changed, fallback,
+// unsupported, neutralised.
+__device__ void estimate_site(const OpposedParams& p, const EstimateSmem& S, int x, int y, int lx, int ly,
+                              unsigned (&counts)[5]) {
+  float& s = p.mosaic[(long long)y * p.W + x];
+  const int ch = color_at(p.cfa, x, y);
+  const float level = p.levels[ch];
+  const int sx = lx + LAST_RADIUS, sy = ly + LAST_RADIUS;
+  const float4 tv = S.cell[sy * ESW + sx];
+  Cell target;
+  target.m[0] = tv.x;
+  target.m[1] = tv.y;
+  target.m[2] = tv.z;
+  target.flags = __float_as_uint(tv.w);
+  int support_count = 0;
+  for (int o = 0; o < 3; ++o)
+    if (o != ch && usable(target, o) && clean(target, o)) support_count++;
+  bool ok = false;
+  float estimate = 0.0f;
+  if (support_count != 0) {
+    const unsigned support = support_mask(target, ch, p.levels);
+    // reference_value(target, support) and log_ratio(target, support) from the
+    // staged roots and ratio (the support channels are bright-clean).
+    if (support != 0) {
+      const int t = sy * ESW + sx;
+      const bool pair = __popc(support) == 2;
+      float ref;
+      if (pair) {
+        const int o0 = ch == 0 ? 1 : 0, o1 = ch == 2 ? 1 : 2;
+        const float mean_root = (S.root[t][o0] + S.root[t][o1]) / 2.0f;
+        ref = mean_root * mean_root * mean_root;
+      } else {
+        ref = target.m[__ffs(support) - 1];
+      }
+      const float tratio = pair ? S.ratio[t][ch] : 0.0f;
+      const bool has_tratio = pair && tratio == tratio;
+      const int col = ch * PATTERNS + pattern_position(ch, support);  // support != 0 here
+      float corr[MAX_CANDIDATES];
+      int count = 0;
+      bool has_local = false;
+      float local = 0.0f;
+      int local_radius = 0;
+      for (int radius = 1; radius <= LAST_RADIUS && !has_local; ++radius) {
+        // The ring's cells from the offset table (no pass over the square's
+        // interior); the candidates are sorted below, so the visiting order
+        // does not matter, and the three rings hold 48 = MAX_CANDIDATES cells.
+        const int ring0 = 4 * radius * (radius - 1), ring_n = 8 * radius;
+        for (int q = 0; q < ring_n; ++q) {
+          const int k = (sy + c_ring[ring0 + q].y) * ESW + sx + c_ring[ring0 + q].x;
+          const float value = S.corr[k][col];
+          if (value != value) continue;  // not a usable candidate (or outside the image)
+          if (pair) {  // chroma_agrees with both ratios required
+            const float cratio = S.ratio[k][ch];
+            if (!has_tratio || cratio != cratio || !(fabsf(tratio - cratio) <= CROSS_CHANNEL_TOLERANCE_EV)) continue;
+          }
+          corr[count++] = value;
+        }
+        if (count >= MIN_CANDIDATES) {
+          for (int a = 1; a < count; ++a) {  // insertion sort, total order
+            const float v = corr[a];
+            int b = a - 1;
+            while (b >= 0 && total_less(v, corr[b])) {
+              corr[b + 1] = corr[b];
+              --b;
+            }
+            corr[b + 1] = v;
+          }
+          const int mid = count / 2;
+          local = count % 2 == 0 ? (corr[mid - 1] + corr[mid]) * 0.5f : corr[mid];
+          local_radius = radius;
+          has_local = true;
+        }
+      }
+      const unsigned label = p.labels[(long long)(y / 2) * p.cw + x / 2];
+      bool has_region = false;
+      float region = 0.0f;
+      const int pos = pattern_position(ch, support);
+      if (pos >= 0) {
+        const int off = ch * PATTERNS + pos;
+        float bratio = 0.0f;
+        bool has_bratio = false;
+        if (slot_value(p, (long long)label * SLOTS + off, pair, region, has_bratio, bratio) ||
+            slot_value(p, off, pair, region, has_bratio, bratio))
+          has_region = chroma_agrees(support, has_tratio, tratio, has_bratio, bratio);
+      }
+      float correction_value = 0.0f;
+      bool have = true;
+      if (has_local && has_region) {
+        const float weight = (float)(LAST_RADIUS + 1 - local_radius) / (float)LAST_RADIUS;
+        correction_value = weight * local + (1.0f - weight) * region;
+      } else if (has_local) {
+        correction_value = local;
+      } else if (has_region) {
+        correction_value = region;
+      } else {
+        have = false;
+      }
+      if (have) {
+        estimate = ref + correction_value;
+        ok = isfinite(estimate) && estimate > 0.0f;
+      }
+    }
+  }
+  bool neutralise = false;
+  if (!ok) {
+    counts[2]++;
+    if (support_count == 0) counts[3]++;
+    neutralise = true;
+  } else {
+    counts[0]++;
+    float bounded = MAX_ESTIMATE_MULT * level;
+    if (estimate < bounded) bounded = estimate;  // f32::min of finite values
+    if (bounded > s) {
+      s = bounded;
+      counts[1]++;
+    } else {
+      neutralise = true;
+    }
+  }
+  if (neutralise && p.has_ceiling && s > p.ceiling[ch]) {
+    s = p.ceiling[ch];
+    counts[4]++;
+  }
+}
+
+// 7. the estimate over the flagged tiles, a grid-stride loop: stage the tile's
+// cells and their candidate values, queue the suspected samples of the tile's
+// target cells (the cell pass's test, s >= level), then estimate them (each
+// site reads and writes only its own sample).
+__global__ void __launch_bounds__(ETHREADS) estimate_kernel(const OpposedParams p) {
+  __shared__ EstimateSmem S;
+  __shared__ unsigned short queue[ETX * ETY * 4];  // the tile's suspected samples
+  __shared__ int queued;
+  __shared__ unsigned s_tile;
   unsigned counts[5] = {0, 0, 0, 0, 0};
-  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const unsigned idx = p.sites[i];
-    estimate_site(p, (int)(idx % (unsigned)p.W), (int)(idx / (unsigned)p.W), counts);
+  const unsigned FULL = 0xffffffffu, lane = threadIdx.x & 31;
+  const unsigned tiles = p.counters[2];
+  for (;;) {
+    __syncthreads();  // the previous tile's sites are done with S and the queue
+    // Tiles from a counter: a CTA takes the next one as soon as it is free, so
+    // tiles with many sites do not pile up on some CTAs.
+    if (threadIdx.x == 0) {
+      s_tile = atomicAdd(&p.counters[4], 1u);
+      queued = 0;
+    }
+    __syncthreads();
+    const unsigned t = s_tile;
+    if (t >= tiles) break;
+    const unsigned tile = p.tile_list[t];
+    const int tx0 = (int)(tile % (unsigned)p.tiles_x) * ETX, ty0 = (int)(tile / (unsigned)p.tiles_x) * ETY;
+    for (int k = threadIdx.x; k < ESN; k += blockDim.x)
+      stage_candidate(p, S, k, tx0 - LAST_RADIUS + k % ESW, ty0 - LAST_RADIUS + k / ESW);
+    // Queue the suspected samples, so that full warps take the sites.
+    for (int q = threadIdx.x; q < ETX * ETY * 4; q += blockDim.x) {
+      const int lc = q >> 2;
+      const int x = 2 * (tx0 + lc % ETX) + (q & 1), y = 2 * (ty0 + lc / ETX) + ((q >> 1) & 1);
+      bool suspected = false;
+      if (x < p.W && y < p.H) suspected = p.mosaic[(long long)y * p.W + x] >= p.levels[color_at(p.cfa, x, y)];
+      const unsigned ballot = __ballot_sync(FULL, suspected);
+      if (ballot) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&queued, __popc(ballot));
+        base = __shfl_sync(FULL, base, 0);
+        if (suspected) queue[base + __popc(ballot & ((1u << lane) - 1u))] = (unsigned short)q;
+      }
+    }
+    __syncthreads();
+    const int n = queued;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const int q = queue[i], lc = q >> 2, lx = lc % ETX, ly = lc / ETX;
+      estimate_site(p, S, 2 * (tx0 + lx) + (q & 1), 2 * (ty0 + ly) + ((q >> 1) & 1), lx, ly, counts);
+    }
   }
   for (int k = 0; k < 5; ++k) {
-    const unsigned sum = __reduce_add_sync(0xffffffffu, counts[k]);
-    if ((threadIdx.x & 31) == 0 && sum) atomicAdd(&p.stats[1 + k], (unsigned long long)sum);
+    const unsigned sum = __reduce_add_sync(FULL, counts[k]);
+    if (lane == 0 && sum) atomicAdd(&p.stats[1 + k], (unsigned long long)sum);
   }
   if (threadIdx.x == 0 && blockIdx.x == 0) p.stats[0] = p.counters[0];
 }
@@ -811,16 +915,20 @@ Status run_opposed_labels(Context& ctx, const MosaicSource& src, float* mosaic, 
   const size_t o_parent = take(sizeof(unsigned) * cells);
   const size_t o_labels = take(sizeof(unsigned) * cells);
   const size_t o_list = take(sizeof(unsigned) * cells);
-  const size_t o_sites = take(sizeof(unsigned) * (size_t)W * H);
+  const int tiles_x = (cw + ETX - 1) / ETX;
+  const size_t tiles = (size_t)tiles_x * ((chh + ETY - 1) / ETY);
+  const size_t o_tiles = take(sizeof(unsigned) * tiles);
   const size_t o_prefix = take(sizeof(unsigned) * words);
   const size_t o_bsum = take(sizeof(unsigned) * rank_blocks);
   const size_t o_rclip = take(sizeof(unsigned) * max_labels);
   const size_t o_wanted = take(sizeof(unsigned) * max_labels);
   const size_t o_acc = take(sizeof(double) * 4 * SLOTS * (size_t)max_labels);
   const size_t o_trim = take(sizeof(float) * 2 * SLOTS * (size_t)max_labels);
-  // The root bitmap and the counters, the only memory zeroed before the kernels.
+  // The root bitmap, the tile flags and the counters, the only memory zeroed
+  // before the kernels.
   const size_t o_bits = take(sizeof(unsigned) * words);
-  const size_t o_cnt = take(sizeof(unsigned) * 4);
+  const size_t o_flags = take(sizeof(unsigned) * tiles);
+  const size_t o_cnt = take(sizeof(unsigned) * 8);
   void* base = nullptr;
   RD_TRY(device_alloc(ctx, bytes, &base));
   char* b = static_cast<char*>(base);
@@ -842,7 +950,9 @@ Status run_opposed_labels(Context& ctx, const MosaicSource& src, float* mosaic, 
   p.cells = reinterpret_cast<float4*>(b + o_cells);
   p.dilated = reinterpret_cast<unsigned char*>(b + o_dil);
   p.suspected = reinterpret_cast<unsigned char*>(b + o_susp);
-  p.sites = reinterpret_cast<unsigned*>(b + o_sites);
+  p.tile_list = reinterpret_cast<unsigned*>(b + o_tiles);
+  p.tile_flags = reinterpret_cast<unsigned*>(b + o_flags);
+  p.tiles_x = tiles_x;
   p.cell_list = reinterpret_cast<unsigned*>(b + o_list);
   p.parent = reinterpret_cast<unsigned*>(b + o_parent);
   p.labels = reinterpret_cast<unsigned*>(b + o_labels);
@@ -873,7 +983,9 @@ Status run_opposed_labels(Context& ctx, const MosaicSource& src, float* mosaic, 
   RD_LAUNCH(ctx, K_OPPOSED, border_kernel<<<lgrid, 256, 0, ctx.stream>>>(p, 0));
   RD_LAUNCH(ctx, K_OPPOSED, finish_moments_kernel<<<256, 256, 0, ctx.stream>>>(p));
   RD_LAUNCH(ctx, K_OPPOSED, border_kernel<<<lgrid, 256, 0, ctx.stream>>>(p, 1));
-  RD_LAUNCH(ctx, K_OPPOSED, estimate_kernel<<<sms * 8, 256, 0, ctx.stream>>>(p));
+  int est_occ = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&est_occ, estimate_kernel, ETHREADS, 0) != cudaSuccess) est_occ = 0;
+  RD_LAUNCH(ctx, K_OPPOSED, estimate_kernel<<<sms * std::max(est_occ, 1), ETHREADS, 0, ctx.stream>>>(p));
   cudaError_t launch = cudaGetLastError();
   if (launch == cudaSuccess && labels_out) {
     // Cells outside every region keep label 0 (with no suspected site, all of them).
