@@ -7,8 +7,9 @@
 // and the arithmetic bit-identical and maps one tile onto one SM:
 //
 //  * one persistent 1024-thread CTA per SM takes half-tile work items (phase
-//    A or phase B of a tile, all phase-A items first) from a counter; a phase
-//    is processed top to bottom in steps of 8 rows. Every stage runs a fixed number of rows
+//    A or phase B of a tile, all phase-A items first) from a counter (or, on a
+//    context that yields its SMs, one CTA per item); a phase is processed top
+//    to bottom in steps of 8 rows. Every stage runs a fixed number of rows
 //    behind the rows loaded so far (its lag is the sum of the stencil reaches
 //    of the stages feeding it), and each plane lives in a shared-memory ring
 //    that holds just the rows still to be read;
@@ -257,6 +258,7 @@ struct AmazeParams {
   unsigned* work;          // work-item counter (zeroed per launch)
   unsigned wait_tries;     // iteration limit of the phase-B wait
   int withhold_tile;       // a global tile whose phase A does not publish (tests of the bounded wait), or -1
+  int one_item;            // 1: one work item per CTA (grid = items), else CTAs loop over items
 };
 
 constexpr unsigned AMAZE_WAIT_TIMEOUT = 64u;
@@ -360,13 +362,16 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
   // that image (the table puts the images' phase-A runs one image ahead of
   // their phase-B runs), so a phase-B item only waits for a phase A that a
   // running CTA has taken, and phase A waits for nothing. The half-tile items
-  // of all images fill the SMs far more evenly than whole tiles would.
-  for (;;) {
+  // of all images fill the SMs far more evenly than whole tiles would. With
+  // one_item each CTA ends after its item (the grid has one CTA per item), so
+  // kernels of higher-priority streams get SMs within one item.
+  do {
     __syncthreads();
     if (t == 0) {
-      // The launch's last fetch (one past the items per CTA) resets the counter.
+      // The launch's last fetch resets the counter: with CTAs that loop, the
+      // one past the items per CTA; with one item per CTA, the last item's.
       const unsigned v = atomicAdd(prm.work, 1u);
-      if (v == (unsigned)prm.total_items + gridDim.x - 1u) atomicExch(prm.work, 0u);
+      if (v == (unsigned)prm.total_items + (prm.one_item ? 0u : gridDim.x) - 1u) atomicExch(prm.work, 0u);
       int image = -1, tile = 0, phase = 0;
       if ((int)v < prm.total_items) {
         int lo = 0, hi = prm.nsegs;
@@ -1136,7 +1141,7 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
       if (s_bad) atomicOr(prm.error, 1u);
     }
     __syncthreads();
-  }
+  } while (!prm.one_item);
 }
 
 }  // namespace
@@ -1198,9 +1203,10 @@ Status run_amaze_images(Context& ctx, const AmazeJob* jobs, int n) {
   }
   add(n - 1, 1);
   // One resident CTA per SM (shared memory); the CTAs take half-tile items
-  // from the counter.
+  // from the counter, looping over them, or one each when the context yields
+  // its SMs between items.
   const int sms = ctx.sm_count > 0 ? ctx.sm_count : 152;
-  const int grid = std::min(item, sms);
+  const int grid = ctx.yield_sms ? item : std::min(item, sms);
   if (ctx.capturing && ctx.amaze_slots < total_tiles)
     return Status{RD_INVALID_INPUT, "demosaic scratch was not reserved before the capture"};
   RD_TRY(reserve_amaze_scratch(ctx, total_tiles));
@@ -1230,6 +1236,7 @@ Status run_amaze_images(Context& ctx, const AmazeJob* jobs, int n) {
     prm.work = ctx.d_work;
     prm.wait_tries = ctx.wait_limit ? ctx.wait_limit : AMAZE_DEFAULT_WAIT_TRIES;
     prm.withhold_tile = ctx.wait_withhold == RD_WAIT_AMAZE_TILE ? 0 : -1;
+    prm.one_item = ctx.yield_sms ? 1 : 0;
     RD_LAUNCH(ctx, K_AMAZE, amaze_kernel<<<grid, THREADS, SMEM_BYTES, ctx.stream>>>(prm));
     const cudaError_t launch = cudaGetLastError();
     if (launch != cudaSuccess) st = Status{RD_SYNCHRONIZATION, cudaGetErrorString(launch)};

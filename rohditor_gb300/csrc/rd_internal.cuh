@@ -97,6 +97,11 @@ struct Context {
   // host tables reach the device from pinned copies kept until the context
   // is destroyed.
   bool capturing = false;
+  // A low-priority lane beside a latency-sensitive one: kernels that would
+  // otherwise keep their CTAs resident across work items (AMaZE) end each CTA
+  // after one item, so that a higher-priority stream's kernels get SMs within
+  // one item.
+  bool yield_sms = false;
   std::vector<void*> pinned_uploads;
   // Timed RL iterations of a launch-shape tuning run, resolved after the
   // stage's synchronisation: (candidate segment count, start, end).

@@ -184,6 +184,7 @@ class CudaExecutor : public Executor {
     RD_TRY(from_code(rd_ctx_create(device, 0, &dev), "develop context"));
     RD_TRY(from_code(rd_ctx_create(device, 0, &ren), "render context"));
     RD_TRY(set_stream_priority(dev->c, false));
+    dev->c.yield_sms = true;  // renders get SMs within one demosaic work item
     return set_stream_priority(ren->c, true);
   }
   ~CudaExecutor() override {
