@@ -407,7 +407,7 @@ def rooflines(families: dict, N: int, n: int) -> tuple[dict | None, dict | None]
         return {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
                 "frac": round(achieved / hbm_peak, 3), "traffic": round(t["bytes_per_px"] * N) if t else None,
                 "traffic_source": (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on the {t['case']} "
-                                   f"case ({t['bytes_per_px']} B/px, profiles/{t['summary']}), scaled to {N} px")
+                                   f"frame, cold L2 ({t['bytes_per_px']} B/px, profiles/{t['summary']}), times {N} px")
                 if t else None,
                 "algorithmic_bytes": round(b), "peak_source": peak_src}
 
