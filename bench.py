@@ -482,7 +482,7 @@ def run_ours(args, world, rank, local, pg):
                 "d2h_bytes_per_step": b.d2h_bytes, "ms_per_step": round(e2e_ms / args.steps, 3)},
         "gpu_launches": int(launches),
         "step_ms": {"min": round(min(step_ms), 3), "median": round(statistics.median(step_ms), 3),
-                    "max": round(max(step_ms), 3)},
+                    "max": round(max(step_ms), 3), "max_at": int(max(range(len(step_ms)), key=step_ms.__getitem__))},
         "roofline": roofline,
         "hbm_roofline": hbm_roofline,
         "kernels": kernels,
