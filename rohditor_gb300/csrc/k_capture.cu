@@ -42,7 +42,18 @@ constexpr int MAX_TAPS = 9;  // radius <= 4 for sigma <= 1.2 (CAPTURE_RADIUS_RAN
 // with different radii never share them.
 struct Taps {
   float w[MAX_TAPS];
+  // -0.0f, the addend of the packed products below. As a launch argument the
+  // compiler cannot fold it, so a packed product is never contracted with the
+  // packed sum that takes it.
+  float neg_zero;
 };
+
+// Packed FP32 (two lanes per instruction): the product x * w rounded once,
+// as fma(x, w, -0.0) (x * w + -0.0 is x * w for every x * w, signed zeros
+// included), and the sum a + p rounded once. A tap sum built from these is
+// the scalar sum of separate multiplies and adds bit for bit.
+__device__ __forceinline__ float2 pmul(float2 x, float2 w, float2 z) { return __ffma2_rn(x, w, z); }
+__device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
 
 __device__ __forceinline__ float smoothstep(float low, float high, float value) {
   float t = (value - low) / (high - low);
@@ -545,17 +556,43 @@ struct __align__(128) StepSmem {
 
 template <int R, int RUN>
 __device__ __forceinline__ void hrun_full(const float* __restrict__ src, float* __restrict__ dst,
-                                          const float (&w)[2 * R + 1]) {
-  constexpr int T = 2 * R + 1;
+                                          const float (&w)[2 * R + 1], const float2 (&w2)[2 * R + 1], float2 z) {
+  constexpr int T = 2 * R + 1, HALF = RUN / 2;
   float win[RUN + 2 * R];
 #pragma unroll
   for (int k = 0; k < RUN + 2 * R; ++k) win[k] = src[k];
+  // Outputs j and j + HALF in the two lanes of a packed sum.
 #pragma unroll
-  for (int j = 0; j < RUN; ++j) {
+  for (int j = 0; j < HALF; ++j) {
+    float2 v = pmul(make_float2(win[j], win[j + HALF]), w2[0], z);
+#pragma unroll
+    for (int t = 1; t < T; ++t) v = padd(v, pmul(make_float2(win[j + t], win[j + HALF + t]), w2[t], z));
+    dst[j] = v.x;
+    dst[j + HALF] = v.y;
+  }
+#pragma unroll
+  for (int j = 2 * HALF; j < RUN; ++j) {
     float v = win[j] * w[0];
 #pragma unroll
     for (int t = 1; t < T; ++t) v += win[j + t] * w[t];
     dst[j] = v;
+  }
+}
+
+// The vertical tap sums of BH consecutive rows from a window of BH + 2R rows:
+// out[j] = sum_t win[j + t] w[t], rows j and j + BH/2 in the two lanes.
+template <int R, int BH>
+__device__ __forceinline__ void vsum_packed(const float (&win)[BH + 2 * R], const float2 (&w2)[2 * R + 1], float2 z,
+                                            float (&out)[BH]) {
+  constexpr int T = 2 * R + 1, HALF = BH / 2;
+  static_assert(BH % 2 == 0, "rows pair up");
+#pragma unroll
+  for (int j = 0; j < HALF; ++j) {
+    float2 v = pmul(make_float2(win[j], win[j + HALF]), w2[0], z);
+#pragma unroll
+    for (int t = 1; t < T; ++t) v = padd(v, pmul(make_float2(win[j + t], win[j + HALF + t]), w2[t], z));
+    out[j] = v.x;
+    out[j + HALF] = v.y;
   }
 }
 
@@ -591,8 +628,13 @@ __global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict
   extern __shared__ __align__(128) float4 rl_step_raw[];
   StepSmem<R, TMA>& S = *reinterpret_cast<StepSmem<R, TMA>*>(rl_step_raw);
   float w[T];
+  float2 w2[T];
 #pragma unroll
-  for (int k = 0; k < T; ++k) w[k] = taps.w[k];
+  for (int k = 0; k < T; ++k) {
+    w[k] = taps.w[k];
+    w2[k] = make_float2(taps.w[k], taps.w[k]);
+  }
+  const float2 z2 = make_float2(taps.neg_zero, taps.neg_zero);
   const int tid = threadIdx.x;
   if (TMA && tid == 0) {
     for (int b = 0; b < 3; ++b) mbar_init(&S.bar[b]);
@@ -688,7 +730,7 @@ __global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict
       const float* eb = S.e[(k % 3) * BH] + rem;
       const float* gb = S.g[TMA ? k % 3 : 0] + rem + (xal - gx);
       // 1. blur #1, horizontal: rows E..E+7, columns x0-R .. x0-R+134
-      if (h1_on) hrun_full<R, G::RUN>(eb + h1_row * G::EWP + h1_col, S.t[h1_row] + h1_col, w);
+      if (h1_on) hrun_full<R, G::RUN>(eb + h1_row * G::EWP + h1_col, S.t[h1_row] + h1_col, w, w2, z2);
       float ec[BH];
 #pragma unroll
       for (int j = 0; j < BH; ++j) ec[j] = eb[j * G::EWP + tid + N2];
@@ -700,11 +742,11 @@ __global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict
         for (int i = 0; i < N2; ++i) win[i] = c1[i];
 #pragma unroll
         for (int j = 0; j < BH; ++j) win[N2 + j] = S.t[j][tid];
+        float bs[BH];
+        vsum_packed<R, BH>(win, w2, z2, bs);
 #pragma unroll
         for (int j = 0; j < BH; ++j) {
-          float b = win[j] * w[0];
-#pragma unroll
-          for (int t = 1; t < T; ++t) b += win[j + t] * w[t];
+          const float b = bs[j];
           const float g = TMA ? gb[(R + j) * G::EWP + R + tid] : gq[j];
           // fmaxf(b, FLOOR) equals rmax(b, FLOOR): the floor is not NaN, and
           // a NaN b gives the floor either way.
@@ -725,7 +767,7 @@ __global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict
       }
       // 3. blur #2, horizontal: rows E-R .. E-R+7, output columns (over blur #1,
       //    whose rows every thread has read before the barrier above)
-      if (h2_on) hrun_full<R, G::RUN>(S.q[h2_row] + h2_col, S.t[h2_row] + h2_col, w);
+      if (h2_on) hrun_full<R, G::RUN>(S.q[h2_row] + h2_col, S.t[h2_row] + h2_col, w, w2, z2);
       __syncthreads();
       // 4. blur #2, vertical, and the bounded update: rows E-2R .. E-2R+7
       {
@@ -750,11 +792,11 @@ __global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict
         if (oko && E - N2 + BH > y0) {
           float* po = est_out + (long long)(E - N2) * W + xo;
           float eo[BH];
+          float bs[BH];
+          vsum_packed<R, BH>(win, w2, z2, bs);
 #pragma unroll
           for (int j = 0; j < BH; ++j) {
-            float b = win[j] * w[0];
-#pragma unroll
-            for (int t = 1; t < T; ++t) b += win[j + t] * w[t];
+            const float b = bs[j];
             const float e = (j < N2 ? ed[j] : ec[j - N2]) * b;
             const float g = TMA ? gb[j * G::EWP + N2 + tid] : go[j];
             // The develop rejects non-finite capture input, so e is never NaN
@@ -1001,8 +1043,13 @@ __global__ void __launch_bounds__(128, 4) rl_prep_step_kernel(const float* __res
   extern __shared__ __align__(128) float4 rl_prep_raw[];
   PrepStepSmem<R>& S = *reinterpret_cast<PrepStepSmem<R>*>(rl_prep_raw);
   float w[T];
+  float2 w2[T];
 #pragma unroll
-  for (int k = 0; k < T; ++k) w[k] = taps.w[k];
+  for (int k = 0; k < T; ++k) {
+    w[k] = taps.w[k];
+    w2[k] = make_float2(taps.w[k], taps.w[k]);
+  }
+  const float2 z2 = make_float2(taps.neg_zero, taps.neg_zero);
   const int tid = threadIdx.x;
   if (TMA && tid == 0) {
     for (int b = 0; b < 2; ++b) mbar_init(&S.bar[b]);
@@ -1103,8 +1150,8 @@ __global__ void __launch_bounds__(128, 4) rl_prep_step_kernel(const float* __res
       cp_async_commit();
       // 2. horizontal blurs of rows E..E+7, output columns of the window
       if (h_on) {
-        hrun_full<R, G::RUN>(S.g[h_row] + h_col, S.tg[h_row] + R + h_col, w);
-        hrun_full<R, G::RUN>(S.m[h_row] + h_col, S.tm[h_row] + R + h_col, w);
+        hrun_full<R, G::RUN>(S.g[h_row] + h_col, S.tg[h_row] + R + h_col, w, w2, z2);
+        hrun_full<R, G::RUN>(S.m[h_row] + h_col, S.tm[h_row] + R + h_col, w, w2, z2);
       }
       asm volatile("cp.async.wait_group 1;\n" ::: "memory");
       if (k + 1 < nsteps) arrive(k + 1);
@@ -1639,6 +1686,7 @@ Status run_capture(Context& ctx, float* rgb, int W, int H, const rd_detail_desc&
       if (!std::isfinite(detail.ceilings[c]) || !(detail.ceilings[c] > 0.0f))
         return Status{RD_INVALID_INPUT, "capture ceilings must be finite and positive"};
     const int ntaps = gaussian_kernel(detail.radius, taps.w, MAX_TAPS);
+    taps.neg_zero = -0.0f;
     if (ntaps < 0) return Status{RD_INVALID_INPUT, "capture radius too large"};
     r = ntaps / 2;
     plane_bytes = sizeof(float) * (size_t)plane * 4;
