@@ -140,6 +140,7 @@ Status check_kernel_error(Context& ctx, const char* stage) {
     if (word & 16u) what += " highlight reconstruction failed;";
     if (word & 32u) what += " capture-sharpening tensor copy timed out;";
     if (word & 64u) what += " demosaic tile wait timed out;";
+    if (word & 128u) what += " demosaic tile copy timed out;";
     return Status{RD_INVALID_INPUT, std::string(stage) + ":" + what};
   }
   return Status{};
@@ -630,7 +631,7 @@ uint64_t rd_ctx_kernel_launches(const rd_ctx* h) { return h ? h->c.launches : 0;
 
 rd_status rd_ctx_set_wait_test(rd_ctx* h, uint32_t wait_limit, int32_t withhold) {
   if (!h) return RD_INVALID_INPUT;
-  if (withhold < RD_WAIT_NONE || withhold > RD_WAIT_RL_COPY)
+  if (withhold < RD_WAIT_NONE || withhold > RD_WAIT_DEMOSAIC_COPY)
     return finish(h, Status{RD_INVALID_INPUT, "unknown withheld completion"});
   h->c.wait_limit = wait_limit;
   h->c.wait_withhold = withhold;

@@ -23,7 +23,6 @@
 // Iterator::sum does) and its half-sample mirror at the image edges. Field
 // values outside the image are filled from their mirror position, so every
 // stencil read equals the reference's mirrored read bit for bit.
-#include <cuda.h>  // CUtensorMap and its enums; the encoder is reached through the runtime
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -32,6 +31,7 @@
 #include <vector>
 
 #include "rd_internal.cuh"
+#include "tma.cuh"
 
 namespace rd {
 namespace {
@@ -127,31 +127,6 @@ struct __align__(128) StreamSmem {
   unsigned long long bar[3];  // one mbarrier per 8-row block of the estimate ring
 };
 
-// ---- TMA and mbarrier (inline PTX) -------------------------------------------
-__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void mbar_init(unsigned long long* bar) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(bar)) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
-  unsigned done;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(done)
-      : "r"(smem_addr(bar)), "r"(parity)
-      : "memory");
-  return done != 0;
-}
-// 2D tensor copy of the box at (x, y) into shared memory, completing on `bar`.
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, unsigned long long* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::"r"(
-          smem_addr(dst)),
-      "l"(map), "r"(x), "r"(y), "r"(smem_addr(bar))
-      : "memory");
-}
 // Every thread's view of a kernel's tensor-copy barriers: the parity of each
 // barrier's next completion, which blocks have a copy issued and not yet
 // waited for, and whether a wait gave up. Each wait is bounded: after `tries`
@@ -295,7 +270,7 @@ __global__ void __launch_bounds__(128) rl_stream_kernel(const float* __restrict_
       if (tma) {
         const int b = ((r0 - ebase) / BH) % 3;
         if (cw.issue_block(b) && tid == 0) {
-          asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+          fence_proxy_async();
           mbar_expect_tx(&S.bar[b], BH * G::EWP * sizeof(float));
           tma_load_2d(S.e[b * BH], &est_map, xal, r0, &S.bar[b]);
         }
@@ -681,7 +656,7 @@ __global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict
       const int r0 = E0 + BH * k, b = k % 3;
       const bool et = e_by_tma(k);
       if (TMA && cw.issue_block(b) && tid == 0) {
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        fence_proxy_async();
         mbar_expect_tx(&S.bar[b], (et ? BH * G::EWP * sizeof(float) : 0) + G::GH * G::EWP * sizeof(float));
         if (et) tma_load_2d(S.e[b * BH], &est_map, xal, r0, &S.bar[b]);
         tma_load_2d(S.g[b], &guide_map, gx, r0 - N2, &S.bar[b]);
@@ -1084,7 +1059,7 @@ __global__ void __launch_bounds__(128, 4) rl_prep_step_kernel(const float* __res
       const int r0 = E0 + BH * k, b = k & 1;
       if (by_tma(k)) {
         if (cw.issue_block(b) && tid == 0) {
-          asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+          fence_proxy_async();
           mbar_expect_tx(&S.bar[b], 3 * BH * G::CWP * sizeof(float));
 #pragma unroll
           for (int c = 0; c < 3; ++c) tma_load_2d(S.rgb[b][c * BH], &rgb_map, xal, c * H + r0, &S.bar[b]);
@@ -1388,26 +1363,6 @@ void resolve_rl_tuning(Context& ctx) {
 
 namespace {
 
-// cuTensorMapEncodeTiled through the runtime's driver entry-point query (no
-// link against the driver library); null when unavailable.
-using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-EncodeTiled tensor_map_encoder() {
-  static EncodeTiled fn = nullptr;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q{};
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<EncodeTiled>(p);
-    else
-      cudaGetLastError();
-  });
-  return fn;
-}
-
 // Estimate-ring box width (floats) of the kernel that runs an iteration.
 int rl_box_width(int W, int H, int R) {
   if (!rl_uses_step_kernel(W, H, R)) return StreamGeom<1>::EWP;
@@ -1418,16 +1373,8 @@ int rl_box_width(int W, int H, int R) {
 // when TMA cannot address it (row stride not a multiple of 16 bytes, or no
 // encoder).
 bool make_plane_map(CUtensorMap* map, const float* plane, int W, int H, int box_w, int box_h = 8) {
-  if (W % 4 != 0 || reinterpret_cast<uintptr_t>(plane) % 16 != 0) return false;
-  const EncodeTiled enc = tensor_map_encoder();
-  if (!enc) return false;
-  const cuuint64_t dims[2] = {(cuuint64_t)W, (cuuint64_t)H};
-  const cuuint64_t strides[1] = {(cuuint64_t)W * sizeof(float)};
-  const cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)box_h};
-  const cuuint32_t elem[2] = {1, 1};
-  return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(plane), dims, strides, box, elem,
-             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  return make_tensor_map_2d(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, plane, W, H, (uint64_t)W * sizeof(float), box_w,
+                            box_h);
 }
 
 Status rl_iteration(Context& ctx, int r, const Taps& taps, const float* est, const float* guide, float* out, int W,

@@ -211,12 +211,9 @@ __host__ __device__ inline int shifted_cfa(int pattern, int x, int y) {
   return p;
 }
 
-// Normalized sample at crop coordinates (x, y) before any highlight step:
-// NormalizationContract::normalize with levels at sensor coordinates.
-__device__ __forceinline__ float source_normalized(const MosaicSource& s, int x, int y) {
-  if (s.f32) return s.f32[(long long)y * s.width + x];
-  const int sx = s.crop_x + x, sy = s.crop_y + y;
-  const float sample = (float)s.raw[(long long)sy * s.row_stride + sx];
+// NormalizationContract::normalize of one raw sample at sensor coordinates
+// (sx, sy), with the black / white levels of that position.
+__device__ __forceinline__ float normalize_raw(const MosaicSource& s, float sample, int sx, int sy) {
   // Level patterns repeat every 1, 2 or 4 samples in practice: mask instead of divide.
   const int by = (s.black_h & (s.black_h - 1)) == 0 ? (sy & (s.black_h - 1)) : sy % s.black_h;
   const int bx = (s.black_w & (s.black_w - 1)) == 0 ? (sx & (s.black_w - 1)) : sx % s.black_w;
@@ -227,6 +224,14 @@ __device__ __forceinline__ float source_normalized(const MosaicSource& s, int x,
   else if (s.white_count == 3) white = s.white[color_at(s.sensor_cfa, sx, sy)];
   else white = s.white[bi];
   return __fdiv_rn(__fsub_rn(sample, black), __fsub_rn(white, black));
+}
+
+// Normalized sample at crop coordinates (x, y) before any highlight step:
+// NormalizationContract::normalize with levels at sensor coordinates.
+__device__ __forceinline__ float source_normalized(const MosaicSource& s, int x, int y) {
+  if (s.f32) return s.f32[(long long)y * s.width + x];
+  const int sx = s.crop_x + x, sy = s.crop_y + y;
+  return normalize_raw(s, (float)s.raw[(long long)sy * s.row_stride + sx], sx, sy);
 }
 
 // Normalized, highlight-processed sample (Clip applied when selected), before balance.

@@ -1,12 +1,13 @@
 """The kernels' bounded device waits, made to run out on purpose.
 
-Two kernels wait on the device: AMaZE's phase B waits for its tile's phase A
+Three kernels wait on the device: AMaZE's phase B waits for its tile's phase A
 to publish the tile's slab (a flag in global memory), and the
-capture-sharpening kernels wait on shared-memory barriers for their tensor
-copies. Each wait gives up after an iteration limit, records why in the
+capture-sharpening, bilinear / MHC and RCD kernels wait on shared-memory
+barriers for their tensor copies. Each wait gives up after an iteration limit, records why in the
 context's error word and returns. Here rd_ctx_set_wait_test shortens the
 limits and withholds one completion (the flag of AMaZE tile 0; the first
-tensor copy of every capture-sharpening block), so the wait runs out: the
+tensor copy of every capture-sharpening block; the tile copy of every
+bilinear / MHC and RCD block), so the wait runs out: the
 call must fail with RD_INVALID_INPUT naming the wait, nothing may trap or
 hang, and the same context must then give the oracle's result again.
 """
@@ -19,7 +20,7 @@ from rohditor_gb300 import CaptureContract, GpuPreviewError
 pytestmark = pytest.mark.gpu
 
 RD_INVALID_INPUT = 8
-RD_WAIT_NONE, RD_WAIT_AMAZE_TILE, RD_WAIT_RL_COPY = 0, 1, 2
+RD_WAIT_NONE, RD_WAIT_AMAZE_TILE, RD_WAIT_RL_COPY, RD_WAIT_DEMOSAIC_COPY = 0, 1, 2, 3
 
 
 def mosaic(w, h, seed):
@@ -58,6 +59,22 @@ def test_capture_copy_wait_runs_out_and_the_context_stays_usable(device, stages,
     assert err.value.code == RD_INVALID_INPUT
     assert "tensor copy timed out" in str(err.value)
     out = stages.capture(rgb, cap)
+    assert np.array_equal(out.view(np.uint32), ref.view(np.uint32))
+
+
+@pytest.mark.parametrize("algorithm", ["mhc", "bilinear", "rcd"])
+def test_demosaic_tile_copy_wait_runs_out_and_the_context_stays_usable(device, stages, oracle, algorithm):
+    m = mosaic(640, 320, 3)  # rows of 2560 bytes: the tiles arrive by tensor copy
+    ref = oracle.demosaic(m, 0, (1.0, 1.0, 1.0), {"bilinear": 0, "mhc": 1, "rcd": 2}[algorithm])
+    device.check(device.lib.rd_ctx_set_wait_test(device.handle, 2000, RD_WAIT_DEMOSAIC_COPY))
+    try:
+        with pytest.raises(GpuPreviewError) as err:
+            stages.demosaic(m, "RGGB", algorithm)
+    finally:
+        device.check(device.lib.rd_ctx_set_wait_test(device.handle, 0, RD_WAIT_NONE))
+    assert err.value.code == RD_INVALID_INPUT
+    assert "demosaic tile copy timed out" in str(err.value)
+    out = stages.demosaic(m, "RGGB", algorithm)
     assert np.array_equal(out.view(np.uint32), ref.view(np.uint32))
 
 

@@ -49,7 +49,7 @@ def test_amaze_golden_hashes_on_gpu(stages, oracle, name):
 
 @pytest.mark.parametrize("algorithm", ["bilinear", "mhc", "rcd", "amaze"])
 @pytest.mark.parametrize("layout", ["RGGB", "BGGR", "GRBG", "GBRG"])
-@pytest.mark.parametrize("size", [(517, 389), (53, 47)])
+@pytest.mark.parametrize("size", [(517, 389), (53, 47), (256, 200)])
 def test_demosaic_bit_exact(stages, oracle, algorithm, layout, size):
     w, h = size
     mosaic = textured_mosaic(w, h, seed=w * 7 + h)
@@ -97,6 +97,36 @@ def test_normalize_and_clip_bit_exact(stages, oracle, layout, highlight):
         ref, ref_stats = oracle.clip(ref, crop_pattern, (0.91, 0.987, 0.8))
         assert stats[:6].tolist() == ref_stats.tolist()
     assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32))
+
+
+@pytest.mark.parametrize("algorithm", ["mhc", "bilinear", "rcd"])
+@pytest.mark.parametrize("crop", [(8, 2, 496, 380), (0, 0, 512, 389), (3, 5, 500, 377), (16, 0, 130, 70)])
+def test_raw_tile_staging_bit_exact(device, oracle, algorithm, crop):
+    """MHC, bilinear and RCD stage each tile from the raw u16 samples: by a
+    tensor copy when the crop's x and the row pitch lie on the 16-byte grid
+    (the first, second and last crops; RCD windows that cross the image edge
+    are always loaded with their mirrored samples), by plain loads otherwise
+    (x = 3). Both must give the staged oracle's output and the Clip
+    statistics bit for bit."""
+    from rohditor_gb300 import GpuSensorProcessor, SensorDescription
+
+    sw, sh, stride = 512, 389, 520
+    raw = raw_mosaic(sw, sh, stride, seed=31)
+    black = (200.0, 210.0, 190.0, 205.0)
+    white = (4000.0, 4095.0, 3900.0)
+    levels = (0.91, 0.987, 0.8)
+    desc = SensorDescription(sw, sh, cfa="GBRG", crop=crop, black=black, black_repeat=(2, 2), white=white,
+                             highlight="clip", clip_levels=levels, demosaic=algorithm,
+                             demosaic_balance=(2.0, 1.0, 1.6))
+    src = GpuSensorProcessor(device).develop(raw, desc)
+    ours = src.download()
+    odesc = oracle.sensor_desc(sw, sh, stride, crop, PATTERNS["GBRG"], black, (2, 2), white)
+    m, pattern = oracle.normalize(raw, odesc)
+    m, stats = oracle.clip(m, pattern, levels)
+    ref = oracle.demosaic(m, pattern, (2.0, 1.0, 1.6), ALGOS[algorithm])
+    assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32)), float(np.max(np.abs(ours - ref)))
+    assert list(src.metrics.highlight_stats)[:6] == stats.tolist()
+    src.release()
 
 
 def test_fused_develop_matches_staged_oracle(device, oracle):
