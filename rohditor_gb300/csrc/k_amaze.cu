@@ -49,6 +49,7 @@
 #include <vector>
 
 #include "rd_internal.cuh"
+#include "tma.cuh"
 
 namespace rd {
 namespace {
@@ -222,7 +223,10 @@ constexpr int B_H16_OFF = B_H32_OFF + B_N32 * 32 * TSH;
 constexpr int B_U8_OFF = B_H16_OFF + B_N16 * 16 * TSH;
 constexpr int B_FLOATS = B_U8_OFF + (16 * TSH + 32 * TSH) / 4;
 constexpr int SMEM_FLOATS = A_FLOATS > B_FLOATS ? A_FLOATS : B_FLOATS;
-constexpr size_t SMEM_BYTES = sizeof(float) * SMEM_FLOATS;
+// After the rings: the staging block of the mosaic-row tensor copies (8 rows
+// of 256 f32 or u16 samples), 128-byte aligned.
+constexpr int STAGE_FLOATS = BH * TS;
+constexpr size_t SMEM_BYTES = sizeof(float) * (SMEM_FLOATS + STAGE_FLOATS) + 128;
 
 // Per-CTA slab in global memory: hvwt, vcd, hcd at red/blue sites (half
 // planes) and the Nyquist flags (u8 half plane).
@@ -231,6 +235,7 @@ constexpr size_t SLAB_FLOATS = 3 * (size_t)TS * TSH + (size_t)TS * TSH / 4;
 // One image of a launch: its mosaic source, output planes and balance, and
 // the global index of its first tile (slabs and flags are per global tile).
 struct AmazeImage {
+  CUtensorMap map;         // the mosaic for 256 x 8 boxes (f32 mosaic or raw u16), when copy != 0
   MosaicSource src;
   float* out;              // planar RGB, 3 * width * height
   unsigned long long* clip_stats;
@@ -239,7 +244,10 @@ struct AmazeImage {
   int count_clip;          // 1: accumulate Clip statistics of core pixels
   float clip_point;
   float gains[3];          // inverse balance applied to the output
+  int copy;                // AMAZE_COPY_*: how rows inside the image are staged
 };
+static_assert(sizeof(AmazeImage) % 64 == 0, "tensor maps in the image table stay 64-byte aligned");
+enum { AMAZE_COPY_NONE = 0, AMAZE_COPY_F32 = 1, AMAZE_COPY_U16 = 2 };
 
 // A run of consecutive work items: phase A or phase B of tiles
 // [0, count) of one image, in the order the counter hands them out.
@@ -262,6 +270,9 @@ struct AmazeParams {
 };
 
 constexpr unsigned AMAZE_WAIT_TIMEOUT = 64u;
+// Error-word bit of a mosaic-row copy whose wait ran out (shared with the
+// other demosaic kernels' tile copies).
+constexpr unsigned AMAZE_COPY_TIMEOUT = 128u;
 __device__ __forceinline__ unsigned load_acquire(const unsigned* p) {
   unsigned v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -342,8 +353,12 @@ __device__ __forceinline__ float bound_sel(bool green_site, float d, float cur, 
 }
 
 __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm) {
-  extern __shared__ float4 amaze_smem4[];
+  extern __shared__ __align__(128) float4 amaze_smem4[];
   float* sm = reinterpret_cast<float*>(amaze_smem4);
+  // Staging block of the mosaic-row tensor copies, and their barrier.
+  float* const stage =
+      reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(sm + SMEM_FLOATS) + 127) & ~static_cast<uintptr_t>(127));
+  __shared__ __align__(8) unsigned long long s_copy_bar;
   __shared__ unsigned long long s_stats[6];
   __shared__ int s_bad;
   // Refined Nyquist sites of a step (phase B), by step parity.
@@ -356,6 +371,15 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
   __shared__ AmazeImage s_img;
   __shared__ int s_item, s_image, s_tile, s_phase;
   int loaded = -1;
+  // Every thread's view of the copy barrier: the parity of its next
+  // completion, whether a wait ran out (then no copy is issued again and rows
+  // are loaded directly), and whether a copy is issued and not yet waited for.
+  unsigned copy_parity = 0;
+  bool copy_failed = false, copy_pending = false;
+  if (t == 0) {
+    mbar_init(&s_copy_bar);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
 
   // Work items from the launch's counter, in the order of the segment table:
   // phase A of every tile of an image is handed out before any phase B of
@@ -430,6 +454,60 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
     float* g_vrb = slab + TS * TSH;
     float* g_hrb = slab + 2 * TS * TSH;
     unsigned char* g_nyq = reinterpret_cast<unsigned char*>(slab + 3 * TS * TSH);
+    // Mosaic rows [lo, lo + 8) arrive by one tensor copy into the staging
+    // block when they and the tile's columns lie inside the image; rows with
+    // mirrored samples are loaded directly (tile_sample).
+    const bool cols_inside = ox - BORDER >= 0 && ox - BORDER + TS <= W;
+    auto copy_ok = [&](int lo) {
+      const int y = oy - BORDER + lo;
+      return im.copy != AMAZE_COPY_NONE && !copy_failed && cols_inside && y >= 0 && y + BH <= H;
+    };
+    // After a barrier that ended every read of the staging block.
+    auto issue_copy = [&](int lo) {
+      if (t == 0) {
+        fence_proxy_async();
+        const CUtensorMap* map = &prm.images[loaded].map;
+        if (im.copy == AMAZE_COPY_F32) {
+          mbar_expect_tx(&s_copy_bar, BH * TS * sizeof(float));
+          tma_load_2d(stage, map, ox - BORDER, oy - BORDER + lo, &s_copy_bar);
+        } else {
+          mbar_expect_tx(&s_copy_bar, BH * TS * sizeof(uint16_t));
+          tma_load_2d(stage, map, src.crop_x + ox - BORDER, src.crop_y + oy - BORDER + lo, &s_copy_bar);
+        }
+      }
+      copy_pending = true;
+    };
+    // Bounded wait for the copy; false when it ran out (reported in the error
+    // word; the caller then loads the rows directly).
+    auto wait_copy = [&]() -> bool {
+      bool done = false;
+      for (unsigned i = 0; i < prm.wait_tries && !done; ++i) done = mbar_try_wait(&s_copy_bar, copy_parity);
+      if (__syncthreads_or(!done)) {
+        copy_failed = true;
+        if (t == 0) atomicOr(prm.error, AMAZE_COPY_TIMEOUT);
+        return false;
+      }
+      copy_parity ^= 1u;
+      copy_pending = false;
+      return true;
+    };
+    // Staged rows [lo, lo + 8) into a mosaic ring: normalized (raw samples),
+    // Clip when selected, balanced (source_balanced of the same positions).
+    auto convert_rows = [&](const auto& ring, int lo) {
+      const uint16_t* raw = reinterpret_cast<const uint16_t*>(stage);
+      for (int k = t; k < BH * TS; k += THREADS) {
+        const int rr = lo + (k >> 8), cc = k & (TS - 1);
+        const int x = ox - BORDER + cc, y = oy - BORDER + rr;
+        const int ch = (ctab >> (2 * (((y & 1) << 1) | (x & 1)))) & 3;
+        float v = im.copy == AMAZE_COPY_F32 ? stage[k]
+                                            : normalize_raw(src, (float)raw[k], src.crop_x + x, src.crop_y + y);
+        if (src.clip) {
+          const float limit = src.clip_levels[ch];
+          if (v > limit) v = limit;
+        }
+        ring.row(rr)[cc] = __fmul_rn(v, src.fwd[ch]);
+      }
+    };
 
     if (!phase_b) {
     // ================= phase A: green.rs:13-292, nyquist.rs:25-95 =================
@@ -585,6 +663,10 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
           }
         }
         __syncthreads();
+        // The next step's rows start arriving now (the staging block's last
+        // reads ended with the step before).
+        const bool copied = F < TS && copy_ok(F);
+        if (copied) issue_copy(F);
         // -- cdd at red/blue sites (green.rs:187-222 tail), lag 6
         {
           const int lo = max(F - BH - 6, 4), hi = min(F - 6, TS - 4);
@@ -678,7 +760,10 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
           }
         }
         // -- rows of the next step (their ring slots held rows no stage reads any more)
-        if (F < TS) load_rows(F);
+        if (F < TS) {
+          if (copied && wait_copy()) convert_rows(cfa, F);
+          else load_rows(F);
+        }
         __syncthreads();
       }
     }
@@ -724,11 +809,19 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
       int bad = 0;
       // Updated weights of the row above, four half-indices per lane (warps 0 and 1).
       float hv_up[4] = {0.0f, 0.0f, 0.0f, 0.0f}, pm_up[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-      // Rows [lo, lo+8) of the mosaic and of the slab ([6, 250) only).
+      // Rows [lo, lo+8) of the mosaic (staged by a tensor copy when one was
+      // issued for them) and of the slab ([6, 250) only).
+      bool copied = copy_ok(0);
+      if (copied) issue_copy(0);
       auto load_rows = [&](int lo) {
-        for (int k = t; k < BH * TS; k += THREADS) {
-          const int rr = lo + (k >> 8), cc = k & (TS - 1);
-          cfa.row(rr)[cc] = tile_sample(src, ox - BORDER + cc, oy - BORDER + rr, W, H);
+        const bool staged = copied && wait_copy();
+        if (staged) {
+          convert_rows(cfa, lo);
+        } else {
+          for (int k = t; k < BH * TS; k += THREADS) {
+            const int rr = lo + (k >> 8), cc = k & (TS - 1);
+            cfa.row(rr)[cc] = tile_sample(src, ox - BORDER + cc, oy - BORDER + rr, W, H);
+          }
         }
         for (int k = t; k < BH * TSH; k += THREADS) {
           const int rr = lo + (k >> 7), j = k & (TSH - 1);
@@ -744,6 +837,9 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
       for (int F = BH; F <= TS + BH; F += BH) {
         if (F - BH < TS) load_rows(F - BH);
         __syncthreads();
+        // The next step's rows start arriving now (the staging block was read above).
+        copied = F < TS && copy_ok(F);
+        if (copied) issue_copy(F);
         // -- Nyquist flag refinement (nyquist.rs:108-130), lag 2, red/blue sites of [8, 248)^2;
         //    diagonal_gradients (diagonal.rs:15-45), lag 6, rows [6, 250)
         {
@@ -1142,6 +1238,11 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
     }
     __syncthreads();
   } while (!prm.one_item);
+  // A copy whose wait ran out may still land: wait for it once more (bounded)
+  // before the block's shared memory is released.
+  if (copy_pending && t == 0)
+    for (unsigned i = 0; i < prm.wait_tries && !mbar_try_wait(&s_copy_bar, copy_parity); ++i) {
+    }
 }
 
 }  // namespace
@@ -1185,6 +1286,20 @@ Status run_amaze_images(Context& ctx, const AmazeJob* jobs, int n) {
     im.count_clip = j.count_clip;
     im.clip_point = j.clip_point;
     for (int c = 0; c < 3; ++c) im.gains[c] = j.gains[c];
+    // Rows of 256 samples by tensor copy: the f32 mosaic with a 16-byte row
+    // pitch, or raw samples with a 16-byte pitch and a crop x on the 8-sample
+    // grid (tile x starts 224 k - 16 then lie on the 16-byte grid).
+    const MosaicSource& ms = j.src;
+    im.copy = AMAZE_COPY_NONE;
+    if (ms.f32) {
+      if (make_tensor_map_2d(&im.map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, ms.f32, ms.width, ms.height,
+                             (uint64_t)ms.width * sizeof(float), TS, BH))
+        im.copy = AMAZE_COPY_F32;
+    } else if (ms.crop_x % 8 == 0 &&
+               make_tensor_map_2d(&im.map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, ms.raw, (uint64_t)ms.crop_x + ms.width,
+                                  (uint64_t)ms.crop_y + ms.height, (uint64_t)ms.row_stride * sizeof(uint16_t), TS, BH)) {
+      im.copy = AMAZE_COPY_U16;
+    }
     total_tiles += (size_t)im.tiles_x * im.tiles_y;
   }
   if (total_tiles > (size_t)(INT32_MAX / 2)) return Status{RD_INVALID_DIMENSIONS, "too many demosaic tiles in one launch"};
@@ -1214,9 +1329,11 @@ Status run_amaze_images(Context& ctx, const AmazeJob* jobs, int n) {
   const size_t img_bytes = sizeof(AmazeImage) * (size_t)n;
   const size_t seg_off = (img_bytes + 255) & ~(size_t)255;
   const size_t table_bytes = seg_off + sizeof(AmazeSegment) * segs.size();
+  // The image table starts on a 64-byte boundary (its tensor maps need it).
   void* table = nullptr;
-  RD_TRY(device_alloc(ctx, table_bytes, &table));
-  unsigned char* tb = static_cast<unsigned char*>(table);
+  RD_TRY(device_alloc(ctx, table_bytes + 64, &table));
+  unsigned char* tb =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(table) + 63) & ~static_cast<uintptr_t>(63));
   Status st = upload(ctx, tb, images.data(), img_bytes);
   if (st.ok()) st = upload(ctx, tb + seg_off, segs.data(), sizeof(AmazeSegment) * segs.size());
   if (st.ok() && cudaMemsetAsync(flags, 0, sizeof(unsigned) * total_tiles, ctx.stream) != cudaSuccess)
@@ -1241,7 +1358,7 @@ Status run_amaze_images(Context& ctx, const AmazeJob* jobs, int n) {
     const cudaError_t launch = cudaGetLastError();
     if (launch != cudaSuccess) st = Status{RD_SYNCHRONIZATION, cudaGetErrorString(launch)};
   }
-  device_free(ctx, table, table_bytes);
+  device_free(ctx, table, table_bytes + 64);
   return st;
 }
 

@@ -49,7 +49,7 @@ def test_amaze_golden_hashes_on_gpu(stages, oracle, name):
 
 @pytest.mark.parametrize("algorithm", ["bilinear", "mhc", "rcd", "amaze"])
 @pytest.mark.parametrize("layout", ["RGGB", "BGGR", "GRBG", "GBRG"])
-@pytest.mark.parametrize("size", [(517, 389), (53, 47), (256, 200)])
+@pytest.mark.parametrize("size", [(517, 389), (53, 47), (256, 200), (704, 480)])
 def test_demosaic_bit_exact(stages, oracle, algorithm, layout, size):
     w, h = size
     mosaic = textured_mosaic(w, h, seed=w * 7 + h)
@@ -99,15 +99,15 @@ def test_normalize_and_clip_bit_exact(stages, oracle, layout, highlight):
     assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32))
 
 
-@pytest.mark.parametrize("algorithm", ["mhc", "bilinear", "rcd"])
+@pytest.mark.parametrize("algorithm", ["mhc", "bilinear", "rcd", "amaze"])
 @pytest.mark.parametrize("crop", [(8, 2, 496, 380), (0, 0, 512, 389), (3, 5, 500, 377), (16, 0, 130, 70)])
 def test_raw_tile_staging_bit_exact(device, oracle, algorithm, crop):
-    """MHC, bilinear and RCD stage each tile from the raw u16 samples: by a
-    tensor copy when the crop's x and the row pitch lie on the 16-byte grid
-    (the first, second and last crops; RCD windows that cross the image edge
-    are always loaded with their mirrored samples), by plain loads otherwise
-    (x = 3). Both must give the staged oracle's output and the Clip
-    statistics bit for bit."""
+    """Every demosaic stages its tiles (AMaZE: its tiles' rows) from the raw
+    u16 samples: by a tensor copy when the crop's x and the row pitch lie on
+    the 16-byte grid (the first, second and last crops; windows or rows that
+    reach past the image edge are always loaded with their mirrored samples),
+    by plain loads otherwise (x = 3). Both must give the staged oracle's
+    output and the Clip statistics bit for bit."""
     from rohditor_gb300 import GpuSensorProcessor, SensorDescription
 
     sw, sh, stride = 512, 389, 520
