@@ -289,6 +289,11 @@ RADIAL_CASES = {
     "poly3": dict(distortion="poly3", distortion_k=(-0.01, 0, 0)),
     "poly5_poly3_tca": dict(distortion="poly5", distortion_k=(-0.02, 0.005, 0.0), tca="poly3",
                             tca_red=(1.0002, 0.0001, -0.0001), tca_blue=(0.9998, -0.0001, 0.0001)),
+    # Blue sampled 5% nearer the centre: away from the centre a tile's three
+    # channel footprints no longer fit the shared-memory box and the gather
+    # reads global memory, near the centre they do.
+    "strong_linear_tca": dict(distortion="poly5", distortion_k=(-0.02, 0.005, 0.0), tca="linear",
+                              tca_red=(1.0, 0, 0), tca_blue=(0.95, 0, 0)),
 }
 
 

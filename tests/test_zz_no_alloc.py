@@ -3,8 +3,10 @@
 The allocation-free render runs the same colour kernel with its LUTs staged in a
 static device array. With unit white balance and an identity camera matrix,
 rd_stage_color applies exactly the same arithmetic to the same base, so the
-8-bit output and the histogram must be identical. Two calls in a row with
-different LUTs check that nothing stale survives in the static array or in the
+8-bit output and the histogram must be identical; both are also checked
+against the oracle directly (the adjustment chain, the sRGB8 conversion and
+the histogram of the kernel's own output). Two calls in a row with different
+LUTs check that nothing stale survives in the static array or in the
 histogram. This file is collected last so it also runs after every other GPU
 test in one process.
 """
@@ -40,7 +42,7 @@ def _contract(variant: str):
                          grading=np.array([[0.2, -0.1, 0.05], [0.0, 0.1, -0.2], [-0.1, 0.0, 0.3]], np.float32))
 
 
-def test_noalloc_render_matches_render_entry_point(device, stages):
+def test_noalloc_render_matches_render_entry_point(device, stages, oracle):
     torch = pytest.importorskip("torch")
     lib = device.lib
     h, w = 181, 263
@@ -63,6 +65,11 @@ def test_noalloc_render_matches_render_entry_point(device, stages):
         hist = d_hist.cpu().numpy().view(np.uint64)
         assert np.array_equal(out, ref_out)
         assert np.array_equal(hist, ref_hist)
+        c = contract
+        x = oracle.adjust(rgb, c.exposure_ev, c.base_lut, c.tone_lut, c.saturation, c.vibrance, c.hsl, c.grading)
+        diff = np.abs(out.astype(np.int32) - oracle.display_srgb8(x).astype(np.int32))
+        assert diff.max() <= 1 and (diff > 0).mean() <= 1e-3  # the sRGB8 bar: 1 code on at most 0.1%
+        assert np.array_equal(hist, oracle.histogram(out)[0])
 
 
 def test_noalloc_render_rejects_bad_arguments(device):
