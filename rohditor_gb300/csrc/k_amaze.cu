@@ -1046,7 +1046,13 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
           }
         }
         __syncthreads();
-        // -- refine_green (nyquist.rs:225-236), lag 19, refined Nyquist sites
+        // -- refine_green (nyquist.rs:225-236) at the refined Nyquist sites of
+        //    [8, 248)^2, then refine_green_with_rb (diagonal.rs:205-247) and the
+        //    move of blue-row differences to dgrb1 (chroma.rs:23-44) at the sites
+        //    of [12, 244)^2, lag 19. The three run site by site in one pass: each
+        //    writes only its own site's green / dgrb0 / dgrb1 and none reads
+        //    what another writes at a different site, so every site sees the
+        //    reference's stage order.
         {
           const int lo = max(F - BH - 19, 8), hi = min(F - 19, TS - 8);
           constexpr int per_row = 128;  // site slots per row: 8 rows per step
@@ -1055,44 +1061,33 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
             const int cc = 8 + (g0 ^ (rr & 1)) + 2 * (k & 127);
             if (cc >= TS - 8) continue;
             const int j = cc >> 1;
-            if (nyq2.row(rr)[j] == 0) continue;
-            // d2h / d2v rows outside [8, 248) were never written: zero.
-            const float* hm2 = rr - 2 >= 8 ? d2h.row(rr - 2) : nullptr;
-            const float* hp2 = rr + 2 < TS - 8 ? d2h.row(rr + 2) : nullptr;
-            const float* hm1 = rr - 1 >= 8 ? d2h.row(rr - 1) : nullptr;
-            const float* hp1 = rr + 1 < TS - 8 ? d2h.row(rr + 1) : nullptr;
-            const float* vm2 = rr - 2 >= 8 ? d2v.row(rr - 2) : nullptr;
-            const float* vp2 = rr + 2 < TS - 8 ? d2v.row(rr + 2) : nullptr;
-            const float* vm1 = rr - 1 >= 8 ? d2v.row(rr - 1) : nullptr;
-            const float* vp1 = rr + 1 < TS - 8 ? d2v.row(rr + 1) : nullptr;
-            const float* h0 = d2h.row(rr);
-            const float* v0 = d2v.row(rr);
-            const int jm = (cc - 1) >> 1, jp = (cc + 1) >> 1;
-            auto at = [](const float* r, int x) { return r ? r[x] : 0.0f; };
-            const float gvarh = EPSSQ + (GQUINC[0] * h0[j] +
-                                         GQUINC[1] * (at(hm1, jm) + at(hm1, jp) + at(hp1, jm) + at(hp1, jp)) +
-                                         GQUINC[2] * (at(hm2, j) + h0[j - 1] + h0[j + 1] + at(hp2, j)) +
-                                         GQUINC[3] * (at(hm2, j - 1) + at(hm2, j + 1) + at(hp2, j - 1) + at(hp2, j + 1)));
-            const float gvarv = EPSSQ + (GQUINC[0] * v0[j] +
-                                         GQUINC[1] * (at(vm1, jm) + at(vm1, jp) + at(vp1, jm) + at(vp1, jp)) +
-                                         GQUINC[2] * (at(vm2, j) + v0[j - 1] + v0[j + 1] + at(vp2, j)) +
-                                         GQUINC[3] * (at(vm2, j - 1) + at(vm2, j + 1) + at(vp2, j - 1) + at(vp2, j + 1)));
-            const float dg = (hrb.row(rr)[j] * gvarv + vrb.row(rr)[j] * gvarh) / (gvarv + gvarh);
-            dgrb0.row(rr)[j] = dg;
-            green.row(rr)[j] = cfa.row(rr)[cc] + dg;
-          }
-        }
-        __syncthreads();
-        // -- refine_green_with_rb (diagonal.rs:205-247) and the move of blue-row
-        //    differences to dgrb1 (chroma.rs:23-44), lag 19, [12, 244)^2
-        {
-          const int lo = max(F - BH - 19, 12), hi = min(F - 19, TS - 12);
-          constexpr int per_row = 128;  // site slots per row: 8 rows per step
-          for (int k = t; k < (hi - lo) * per_row; k += THREADS) {
-            const int rr = lo + (k >> 7);
-            const int cc = 12 + (g0 ^ (rr & 1)) + 2 * (k & 127);
-            if (cc >= TS - 12) continue;
-            const int j = cc >> 1;
+            if (nyq2.row(rr)[j] != 0) {
+              // d2h / d2v rows outside [8, 248) were never written: zero.
+              const float* hm2 = rr - 2 >= 8 ? d2h.row(rr - 2) : nullptr;
+              const float* hp2 = rr + 2 < TS - 8 ? d2h.row(rr + 2) : nullptr;
+              const float* hm1 = rr - 1 >= 8 ? d2h.row(rr - 1) : nullptr;
+              const float* hp1 = rr + 1 < TS - 8 ? d2h.row(rr + 1) : nullptr;
+              const float* vm2 = rr - 2 >= 8 ? d2v.row(rr - 2) : nullptr;
+              const float* vp2 = rr + 2 < TS - 8 ? d2v.row(rr + 2) : nullptr;
+              const float* vm1 = rr - 1 >= 8 ? d2v.row(rr - 1) : nullptr;
+              const float* vp1 = rr + 1 < TS - 8 ? d2v.row(rr + 1) : nullptr;
+              const float* h0 = d2h.row(rr);
+              const float* v0 = d2v.row(rr);
+              const int jm = (cc - 1) >> 1, jp = (cc + 1) >> 1;
+              auto at = [](const float* r, int x) { return r ? r[x] : 0.0f; };
+              const float gvarh = EPSSQ + (GQUINC[0] * h0[j] +
+                                           GQUINC[1] * (at(hm1, jm) + at(hm1, jp) + at(hp1, jm) + at(hp1, jp)) +
+                                           GQUINC[2] * (at(hm2, j) + h0[j - 1] + h0[j + 1] + at(hp2, j)) +
+                                           GQUINC[3] * (at(hm2, j - 1) + at(hm2, j + 1) + at(hp2, j - 1) + at(hp2, j + 1)));
+              const float gvarv = EPSSQ + (GQUINC[0] * v0[j] +
+                                           GQUINC[1] * (at(vm1, jm) + at(vm1, jp) + at(vp1, jm) + at(vp1, jp)) +
+                                           GQUINC[2] * (at(vm2, j) + v0[j - 1] + v0[j + 1] + at(vp2, j)) +
+                                           GQUINC[3] * (at(vm2, j - 1) + at(vm2, j + 1) + at(vp2, j - 1) + at(vp2, j + 1)));
+              const float dg = (hrb.row(rr)[j] * gvarv + vrb.row(rr)[j] * gvarh) / (gvarv + gvarh);
+              dgrb0.row(rr)[j] = dg;
+              green.row(rr)[j] = cfa.row(rr)[cc] + dg;
+            }
+            if (rr < 12 || rr >= TS - 12 || cc < 12 || cc >= TS - 12) continue;
             const float pm = pmwt.row(rr)[j];
             const float hvv = hv.row(rr)[j];
             if (!(fabsf(0.5f - pm) < fabsf(0.5f - hvv))) {
