@@ -451,6 +451,34 @@ def test_cancellation_before_start(device):
     assert err.value.variant == "Cancelled" and not err.value.is_routing()
 
 
+def test_develop_rejects_invalid_geometry_and_keeps_the_context(device, oracle):
+    """Inputs the reference refuses before any work (NormalizationContract
+    validation, sensor.rs): a sensor or crop below 2x2, a crop outside the
+    sensor, a row stride shorter than the sensor width. Each call fails with
+    its status and the context then develops a valid mosaic bit-exact."""
+    from rohditor_gb300 import GpuPreviewError, GpuSensorProcessor, SensorDescription
+
+    proc = GpuSensorProcessor(device)
+    raw = raw_mosaic(64, 48, 64, seed=2)
+    cases = [
+        (raw[:1, :1], SensorDescription(1, 1, black=(0.0,), white=(4095.0,)), "InvalidInput"),
+        (raw, SensorDescription(64, 48, crop=(0, 0, 1, 48), black=(0.0,), white=(4095.0,)), "InvalidInput"),
+        (raw, SensorDescription(64, 48, crop=(40, 0, 32, 48), black=(0.0,), white=(4095.0,)), "InvalidInput"),
+        (raw[:, :60], SensorDescription(64, 48, black=(0.0,), white=(4095.0,)), "InvalidDimensions"),
+    ]
+    for mosaic, desc, variant in cases:
+        with pytest.raises(GpuPreviewError) as err:
+            proc.develop(mosaic, desc)
+        assert err.value.variant == variant, (desc, str(err.value))
+        assert not err.value.is_routing()
+    desc = SensorDescription(64, 48, cfa="GRBG", black=(256.0,), white=(4095.0,), demosaic="mhc")
+    got = proc.develop(raw, desc).download()
+    odesc = oracle.sensor_desc(64, 48, 64, (0, 0, 64, 48), PATTERNS["GRBG"], [256.0], (1, 1), [4095.0])
+    m, pattern = oracle.normalize(raw, odesc)
+    ref = oracle.demosaic(m, pattern, (1.0, 1.0, 1.0), ALGOS["mhc"])
+    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+
+
 def test_budget_is_a_routing_answer(device):
     from rohditor_gb300 import GpuPreviewError, GpuSensorProcessor, SensorDescription
 
@@ -582,6 +610,46 @@ def test_full_24mp_workload_against_the_oracle(device, stages, oracle):
     assert diff.max() <= 1 and (diff > 0).mean() <= 1e-3
     ref_hist, _ = oracle.histogram(out)
     assert np.array_equal(np.concatenate([hist.red, hist.green, hist.blue, hist.luminance]), ref_hist)
+    base.release()
+    src.release()
+
+
+def test_largest_export_workload_against_the_oracle(device, stages, oracle):
+    """The largest configured frame, one image of the export stream: 11648x8736
+    RGGB 16-bit (white 65535, black 1024) with 0.5% hot pixels and specular
+    blobs, Opposed + AMaZE + RL K=20, then the full optics (Poly5 distortion,
+    linear TCA, vignetting) and the area reduction to 2560x1920 with WB +
+    matrix. Checked at full size like the 24 MP workload: Opposed statistics
+    exact and samples within 1e-4; AMaZE + 20 RL iterations from the GPU's
+    own highlight output bit-exact; the spatial stage bit-exact."""
+    from rohditor_gb300 import GpuSensorProcessor, GpuSpatialProcessor
+    from rohditor_gb300.workloads import large_export
+
+    wl = large_export(count=1)[0]
+    w, h = wl.width, wl.height
+    raw = wl.mosaic(device)
+    src = GpuSensorProcessor(device).develop(raw, wl.sensor, wl.capture)
+    got = src.download()
+    odesc = oracle.sensor_desc(w, h, w, (0, 0, w, h), 0, [wl.black], (1, 1), [wl.white])
+    m, pattern = oracle.normalize(raw, odesc)
+    ref_h, stats, _, _ = oracle.opposed(m, pattern, wl.sensor.detection_levels, wl.sensor.neutral_ceiling)
+    del m
+    gpu_h, gpu_stats = stages.highlight(raw, wl.sensor)
+    assert list(src.metrics.highlight_stats) == stats.tolist() == gpu_stats.tolist()
+    assert float(np.max(np.abs(gpu_h - ref_h))) <= 1e-4
+    del ref_h, raw
+    cap = wl.capture
+    ref = oracle.capture(oracle.demosaic(gpu_h, pattern, wl.as_shot, 3), cap.amount, cap.radius,
+                         cap.noise_protection, cap.ceilings, cap.iterations)
+    assert cap.iterations == 20
+    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+    del ref, gpu_h
+    c = wl.color
+    base = GpuSpatialProcessor(device).reduce_preview(src, wl.optics, wl.target, c.wb_gains, c.camera_to_rec2020)
+    ref_o = oracle.optics_apply(oracle.optics_desc_from(wl.optics.to_c()), got)
+    ref_b = oracle.camera_matrix(oracle.white_balance(oracle.area_reduce(ref_o, wl.target), c.wb_gains),
+                                 c.camera_to_rec2020)
+    assert np.array_equal(base.download().view(np.uint32), ref_b.view(np.uint32))
     base.release()
     src.release()
 
