@@ -170,13 +170,20 @@ uint64_t rd_ctx_kernel_launches(const rd_ctx* ctx);
  * never deliver: RD_WAIT_AMAZE_TILE (phase A of AMaZE tile 0 does not
  * publish its slab, so its phase B waits), RD_WAIT_RL_COPY (every block
  * of the capture-sharpening kernels skips its first tensor copy but waits
- * for it, then drains its other copies in flight) or RD_WAIT_DEMOSAIC_COPY
+ * for it, then drains its other copies in flight), RD_WAIT_DEMOSAIC_COPY
  * (every block of the bilinear / MHC and RCD kernels skips the tensor copy
  * of its tile but waits for it; sources that TMA cannot address, and RCD
  * windows that cross the image edge, are staged by plain loads and have no
- * such wait). RD_WAIT_NONE restores normal
- * operation. */
-enum { RD_WAIT_NONE = 0, RD_WAIT_AMAZE_TILE = 1, RD_WAIT_RL_COPY = 2, RD_WAIT_DEMOSAIC_COPY = 3 };
+ * such wait) or RD_WAIT_AMAZE_COPY (AMaZE issues none of its mosaic-row
+ * tensor copies but waits for the first of each block, then loads the rows
+ * directly). RD_WAIT_NONE restores normal operation. */
+enum {
+  RD_WAIT_NONE = 0,
+  RD_WAIT_AMAZE_TILE = 1,
+  RD_WAIT_RL_COPY = 2,
+  RD_WAIT_DEMOSAIC_COPY = 3,
+  RD_WAIT_AMAZE_COPY = 4
+};
 rd_status rd_ctx_set_wait_test(rd_ctx* ctx, uint32_t wait_limit, int32_t withhold);
 
 /* ---- routing ---- */

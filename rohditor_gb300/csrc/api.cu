@@ -631,7 +631,7 @@ uint64_t rd_ctx_kernel_launches(const rd_ctx* h) { return h ? h->c.launches : 0;
 
 rd_status rd_ctx_set_wait_test(rd_ctx* h, uint32_t wait_limit, int32_t withhold) {
   if (!h) return RD_INVALID_INPUT;
-  if (withhold < RD_WAIT_NONE || withhold > RD_WAIT_DEMOSAIC_COPY)
+  if (withhold < RD_WAIT_NONE || withhold > RD_WAIT_AMAZE_COPY)
     return finish(h, Status{RD_INVALID_INPUT, "unknown withheld completion"});
   h->c.wait_limit = wait_limit;
   h->c.wait_withhold = withhold;

@@ -266,6 +266,7 @@ struct AmazeParams {
   unsigned* work;          // work-item counter (zeroed per launch)
   unsigned wait_tries;     // iteration limit of the phase-B wait
   int withhold_tile;       // a global tile whose phase A does not publish (tests of the bounded wait), or -1
+  int withhold_copy;       // 1: no mosaic-row copy is issued, each is still waited for (tests of the bounded wait)
   int one_item;            // 1: one work item per CTA (grid = items), else CTAs loop over items
 };
 
@@ -464,7 +465,7 @@ __global__ void __launch_bounds__(THREADS, 1) amaze_kernel(const AmazeParams prm
     };
     // After a barrier that ended every read of the staging block.
     auto issue_copy = [&](int lo) {
-      if (t == 0) {
+      if (t == 0 && !prm.withhold_copy) {
         fence_proxy_async();
         const CUtensorMap* map = &prm.images[loaded].map;
         if (im.copy == AMAZE_COPY_F32) {
@@ -1348,6 +1349,7 @@ Status run_amaze_images(Context& ctx, const AmazeJob* jobs, int n) {
     prm.work = ctx.d_work;
     prm.wait_tries = ctx.wait_limit ? ctx.wait_limit : AMAZE_DEFAULT_WAIT_TRIES;
     prm.withhold_tile = ctx.wait_withhold == RD_WAIT_AMAZE_TILE ? 0 : -1;
+    prm.withhold_copy = ctx.wait_withhold == RD_WAIT_AMAZE_COPY ? 1 : 0;
     prm.one_item = ctx.yield_sms ? 1 : 0;
     RD_LAUNCH(ctx, K_AMAZE, amaze_kernel<<<grid, THREADS, SMEM_BYTES, ctx.stream>>>(prm));
     const cudaError_t launch = cudaGetLastError();

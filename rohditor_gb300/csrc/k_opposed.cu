@@ -49,7 +49,6 @@ constexpr float TRIM_FLOOR = 1e-5f;
 constexpr float BORDER_MIN_FRACTION = 0.5f;
 constexpr int LAST_RADIUS = 3, MAX_CANDIDATES = 48, MIN_CANDIDATES = 3;
 constexpr float MAX_ESTIMATE_MULT = 4.0f;
-constexpr unsigned NONE = 0xFFFFFFFFu;
 constexpr int UNION_LIMIT = 1 << 20;
 constexpr unsigned OPPOSED_ERROR = 16u;
 

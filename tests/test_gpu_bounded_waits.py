@@ -1,12 +1,12 @@
 """The kernels' bounded device waits, made to run out on purpose.
 
-Three kernels wait on the device: AMaZE's phase B waits for its tile's phase A
-to publish the tile's slab (a flag in global memory), and the
-capture-sharpening, bilinear / MHC and RCD kernels wait on shared-memory
-barriers for their tensor copies. Each wait gives up after an iteration limit, records why in the
-context's error word and returns. Here rd_ctx_set_wait_test shortens the
-limits and withholds one completion (the flag of AMaZE tile 0; the first
-tensor copy of every capture-sharpening block; the tile copy of every
+AMaZE's phase B waits for its tile's phase A to publish the tile's slab (a
+flag in global memory), and AMaZE and the capture-sharpening, bilinear / MHC
+and RCD kernels wait on shared-memory barriers for their tensor copies. Each
+wait gives up after an iteration limit, records why in the context's error
+word and returns. Here rd_ctx_set_wait_test shortens the limits and withholds
+one completion (the flag of AMaZE tile 0; AMaZE's mosaic-row copies; the
+first tensor copy of every capture-sharpening block; the tile copy of every
 bilinear / MHC and RCD block), so the wait runs out: the
 call must fail with RD_INVALID_INPUT naming the wait, nothing may trap or
 hang, and the same context must then give the oracle's result again.
@@ -20,7 +20,7 @@ from rohditor_gb300 import CaptureContract, GpuPreviewError
 pytestmark = pytest.mark.gpu
 
 RD_INVALID_INPUT = 8
-RD_WAIT_NONE, RD_WAIT_AMAZE_TILE, RD_WAIT_RL_COPY, RD_WAIT_DEMOSAIC_COPY = 0, 1, 2, 3
+RD_WAIT_NONE, RD_WAIT_AMAZE_TILE, RD_WAIT_RL_COPY, RD_WAIT_DEMOSAIC_COPY, RD_WAIT_AMAZE_COPY = 0, 1, 2, 3, 4
 
 
 def mosaic(w, h, seed):
@@ -75,6 +75,21 @@ def test_demosaic_tile_copy_wait_runs_out_and_the_context_stays_usable(device, s
     assert err.value.code == RD_INVALID_INPUT
     assert "demosaic tile copy timed out" in str(err.value)
     out = stages.demosaic(m, "RGGB", algorithm)
+    assert np.array_equal(out.view(np.uint32), ref.view(np.uint32))
+
+
+def test_amaze_row_copy_wait_runs_out_and_the_context_stays_usable(device, stages, oracle):
+    m = mosaic(704, 480, 4)  # rows of 2816 bytes: the inner tiles' rows arrive by tensor copy
+    ref = oracle.demosaic(m, 0, (1.0, 1.0, 1.0), 3)
+    device.check(device.lib.rd_ctx_set_wait_test(device.handle, 2000, RD_WAIT_AMAZE_COPY))
+    try:
+        with pytest.raises(GpuPreviewError) as err:
+            stages.demosaic(m, "RGGB", "amaze")
+    finally:
+        device.check(device.lib.rd_ctx_set_wait_test(device.handle, 0, RD_WAIT_NONE))
+    assert err.value.code == RD_INVALID_INPUT
+    assert "demosaic tile copy timed out" in str(err.value)
+    out = stages.demosaic(m, "RGGB", "amaze")
     assert np.array_equal(out.view(np.uint32), ref.view(np.uint32))
 
 
