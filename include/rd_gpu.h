@@ -422,10 +422,13 @@ rd_status rd_develop_batch_graph(int device, rd_batch_item* items, int32_t count
  * (k % lanes) and normalize / highlight them, then one AMaZE launch works
  * through the half-tile items of every image from a shared queue (images of
  * other demosaic algorithms, or of 32 px or less, are demosaiced one by
- * one), then the lanes finish their images (capture sharpening, spatial
- * pass, render). Outputs equal rd_develop + rd_spatial + rd_render per image
- * bit for bit; device memory holds every image's intermediates at once.
- * Per-item `ms` covers the finishing stage only. */
+ * one), then each capture-sharpening iteration is one launch over the work
+ * items of every image that shares its taps (the guide / mask pass and the
+ * gain run image by image; images below 256x64 take the per-image path),
+ * then the lanes finish their images (spatial pass, render). Outputs equal
+ * rd_develop + rd_spatial + rd_render per image bit for bit; device memory
+ * holds every image's intermediates at once. Per-item `ms` covers the
+ * finishing stage only. */
 rd_status rd_develop_batch_flat(int device, rd_batch_item* items, int32_t count, int32_t lanes, double* wall_ms);
 
 /* ---- served preview loop ----

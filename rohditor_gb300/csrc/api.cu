@@ -1427,9 +1427,11 @@ rd_status rd_copy_to_host(rd_ctx* h, void* dst, const void* src, size_t bytes) {
 // streams, one host thread each) upload their images and normalize / Opposed
 // them; one AMaZE launch then takes the half-tile work items of every image
 // from a shared counter (run_amaze_images), so no image's last wave leaves SMs
-// idle; the lanes finish their images (capture sharpening, spatial pass,
-// render with host outputs). Image k belongs to lane k % lanes throughout, and
-// its device buffers come from that lane's pool.
+// idle; capture sharpening follows on the same stream, each RL iteration one
+// launch over the work items of every image that shares its taps
+// (run_capture_images); the lanes finish their images (spatial pass, render
+// with host outputs). Image k belongs to lane k % lanes throughout, and its
+// device buffers come from that lane's pool.
 namespace {
 
 struct FlatJob {
@@ -1546,8 +1548,26 @@ extern "C" rd_status rd_develop_batch_flat(int device, rd_batch_item* items, int
     if (!dm.ok())
       for (int k : amaze_images)
         if (jobs[k].st.ok()) jobs[k].st = dm;
+    // 3. capture sharpening on lane 0: each iteration of every image that
+    //    shares its taps in one launch over all their work items.
+    std::vector<rd::CaptureJob> capture;
+    std::vector<int> capture_images;
+    for (int k = 0; k < count; ++k) {
+      FlatJob& j = jobs[k];
+      if (!j.st.ok()) continue;
+      capture.push_back(rd::CaptureJob{j.source->rgb, j.source->W, j.source->H, items[k].detail, Status{}});
+      capture_images.push_back(k);
+    }
+    Status cs;
+    if (!capture.empty()) cs = rd::run_capture_images(c0, capture.data(), (int)capture.size());
+    if (cs.ok()) cs = rd::check_kernel_error(c0, "batch capture");
+    for (size_t i = 0; i < capture.size(); ++i) {
+      FlatJob& j = jobs[capture_images[i]];
+      if (!capture[i].st.ok()) j.st = capture[i].st;
+      else if (!cs.ok()) j.st = cs;
+    }
     cudaEventRecord(demosaiced, c0.stream);
-    // 3. capture sharpening, spatial pass and render, lane by lane.
+    // 4. spatial pass and render, lane by lane.
     on_lanes([&](int l) {
       rd_ctx* h = ctxs[l];
       rd::Context& ctx = h->c;
@@ -1558,7 +1578,6 @@ extern "C" rd_status rd_develop_batch_flat(int device, rd_batch_item* items, int
         rd_batch_item& it = items[k];
         const auto s0 = Clock::now();
         Status st = j.st;
-        if (st.ok()) st = rd::run_capture(ctx, j.source->rgb, j.source->W, j.source->H, it.detail);
         flat_release_staging(h, j);
         if (st.ok()) st = rd::check_kernel_error(ctx, "batch develop");
         rd_status code = finish(h, st);

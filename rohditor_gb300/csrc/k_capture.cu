@@ -26,6 +26,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
+#include <cstring>
 #include <map>
 #include <mutex>
 #include <vector>
@@ -502,7 +504,6 @@ __device__ __forceinline__ int next_item(unsigned* work, int items, int& s_item)
 
 template <int R>
 struct StepGeom {
-  static constexpr int T = 2 * R + 1;
   static constexpr int QW = 128;         // blur #1 / ratio columns [x0 - R, x0 - R + 128)
   static constexpr int SW = QW - 2 * R;  // output columns of a strip
   static constexpr int EW = QW + 2 * R;  // estimate columns [x0 - 2R, x0 - 2R + EW)
@@ -589,6 +590,241 @@ StepSegments step_segments(int H, int R, int want) {
   return {n8 / segs, n8 % segs, (H - m) % 8, segs};
 }
 
+// One image of an iteration launch: its estimate (in and out) and guide
+// planes, its size, strips, row segments and work items, and the tensor maps
+// of its estimate and guide planes (null without tensor copies).
+struct StepImage {
+  const float* est_in;
+  const float* guide;
+  float* est_out;
+  int W, H, strips, items;
+  StepSegments sg;
+  const CUtensorMap* est_map;
+  const CUtensorMap* guide_map;
+};
+
+// A thread's part of an iteration launch: the taps (scalar and packed), the
+// -0.0 addend of the packed products, and the run it computes in each
+// horizontal pass (row, first column).
+template <int R>
+struct StepThread {
+  using G = StepGeom<R>;
+  float w[2 * R + 1];
+  float2 w2[2 * R + 1];
+  float2 z2;
+  bool h1_on, h2_on;
+  int h1_row, h1_col, h2_row, h2_col;
+  __device__ __forceinline__ explicit StepThread(const Taps& taps) {
+#pragma unroll
+    for (int k = 0; k < 2 * R + 1; ++k) {
+      w[k] = taps.w[k];
+      w2[k] = make_float2(taps.w[k], taps.w[k]);
+    }
+    z2 = make_float2(taps.neg_zero, taps.neg_zero);
+    const int tid = threadIdx.x;
+    h1_on = tid < G::H1_RUNS * G::BH;
+    h2_on = tid < G::H2_RUNS * G::BH;
+    h1_row = tid / G::H1_RUNS;
+    h1_col = (tid % G::H1_RUNS) * G::RUN;
+    h2_row = tid / G::H2_RUNS;
+    h2_col = (tid % G::H2_RUNS) * G::RUN;
+  }
+};
+
+// One work item (a strip and a row segment) of one image's iteration. Every
+// thread of the CTA calls it.
+template <int R, bool TMA>
+__device__ __forceinline__ void step_item(StepSmem<R, TMA>& S, const StepImage& im, int item, const StepThread<R>& th,
+                                          CopyWaits& cw) {
+  using G = StepGeom<R>;
+  constexpr int SW = G::SW, BH = G::BH, N2 = 2 * R;
+  const int tid = threadIdx.x;
+  const float(&w)[2 * R + 1] = th.w;
+  const float2(&w2)[2 * R + 1] = th.w2;
+  const float2 z2 = th.z2;
+  const bool h1_on = th.h1_on, h2_on = th.h2_on;
+  const int h1_row = th.h1_row, h1_col = th.h1_col, h2_row = th.h2_row, h2_col = th.h2_col;
+  const float* __restrict__ est_in = im.est_in;
+  const float* __restrict__ guide = im.guide;
+  float* __restrict__ est_out = im.est_out;
+  const int W = im.W, H = im.H, strips = im.strips;
+  const StepSegments sg = im.sg;
+  int strip, seg;
+  strip_item(item, strips, sg.segs, strip, seg);
+  const int x0 = strip * SW;
+  const int y0 = seg_row(sg, seg, H), y1 = seg_row(sg, seg + 1, H);
+  const int E0 = y0 - N2;
+  const int nsteps = (y1 - y0 + 2 * N2 - BH + 7) / BH + 1;
+  const bool inside = x0 - N2 >= 0 && x0 - N2 + G::EW <= W;
+  const bool tma_strip = TMA && inside;
+  const bool edge_q = x0 < R || x0 + SW + R > W;
+  const int xal = (x0 - N2) & ~3;  // rounds down, also below 0
+  const int rem = TMA ? (x0 - N2) - xal : 0;
+  // Guide boxes stay inside the image columns (a box crossing the image edge
+  // takes the tensor unit much longer); reads shift by xal - gx. Columns the
+  // shifted box misses lie outside the image and only feed ratio columns
+  // that are overwritten by their mirrors and outputs that are not stored.
+  const int gx = TMA ? min(max(xal, 0), W - G::EWP) : 0;
+  const int xa = x0 - N2 + tid, xb = xa + 128;
+  const int sxa = (unsigned)xa < (unsigned)W ? xa : mirror_half(xa, W);
+  const bool has_b = tid + 128 < G::EW;
+  const int sxb = has_b ? ((unsigned)xb < (unsigned)W ? xb : mirror_half(xb, W)) : 0;
+  // Step k's estimate block (rows [E0 + 8k, +8)) goes to ring block k % 3, by
+  // one tensor copy when the rows and the window lie inside the image, else
+  // by per-thread copies with rows and columns mirrored into the image; its
+  // guide rows go to guide slot k % 3 by one tensor copy.
+  auto e_by_tma = [&](int k) {
+    const int r0 = E0 + BH * k;
+    return tma_strip && r0 >= 0 && r0 + BH <= H;
+  };
+  auto issue = [&](int k) {
+    if (k >= nsteps) return;
+    const int r0 = E0 + BH * k, b = k % 3;
+    const bool et = e_by_tma(k);
+    if (TMA && cw.issue_block(b) && tid == 0) {
+      fence_proxy_async();
+      mbar_expect_tx(&S.bar[b], (et ? BH * G::EWP * sizeof(float) : 0) + G::GH * G::EWP * sizeof(float));
+      if (et) tma_load_2d(S.e[b * BH], im.est_map, xal, r0, &S.bar[b]);
+      tma_load_2d(S.g[b], im.guide_map, gx, r0 - N2, &S.bar[b]);
+    }
+    if (et) return;
+#pragma unroll
+    for (int j = 0; j < BH; ++j) {
+      const float* src = est_in + (long long)mirror_row(r0 + j, H) * W;
+      float* dst = S.e[b * BH + j] + rem;
+      cp_async4(dst + tid, src + sxa);
+      if (has_b) cp_async4(dst + tid + 128, src + sxb);
+    }
+  };
+  issue(0);
+  cp_async_commit();
+  issue(1);
+  cp_async_commit();
+  // Carried rows: blur #1 rows [E-2R, E), blur #2 rows [E-3R, E-R), estimate
+  // rows [E-2R, E) of this thread's output column.
+  float c1[N2], c2[N2], ed[N2];
+#pragma unroll
+  for (int i = 0; i < N2; ++i) c1[i] = c2[i] = ed[i] = 1.0f;
+  const int xq = x0 - R + tid, xo = x0 + tid;
+  const bool okq = (unsigned)xq < (unsigned)W;
+  const bool oko = tid < SW && xo < W;
+  for (int k = 0; k < nsteps; ++k) {
+    const int E = E0 + BH * k;
+    // Without tensor maps: guide values of the ratio rows and of the update rows.
+    float gq[BH], go[BH];
+    if (!TMA) {
+#pragma unroll
+      for (int j = 0; j < BH; ++j) {
+        const int rq = E - R + j, ro = E - N2 + j;
+        gq[j] = okq && (unsigned)rq < (unsigned)H ? __ldg(guide + (long long)rq * W + xq) : 0.0f;
+        go[j] = oko && ro >= y0 && ro < y1 ? __ldg(guide + (long long)ro * W + xo) : 0.0f;
+      }
+    }
+    asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    if (TMA) cw.wait(&S.bar[k % 3], k % 3);
+    __syncthreads();
+    // Block k + 2 reuses the slots of block k - 1, whose estimate rows were
+    // last read before the second barrier of step k - 1 and whose guide rows
+    // before the barrier above.
+    issue(k + 2);
+    cp_async_commit();
+    const float* eb = S.e[(k % 3) * BH] + rem;
+    const float* gb = S.g[TMA ? k % 3 : 0] + rem + (xal - gx);
+    // 1. blur #1, horizontal: rows E..E+7, columns x0-R .. x0-R+134
+    if (h1_on) hrun_full<R, G::RUN>(eb + h1_row * G::EWP + h1_col, S.t[h1_row] + h1_col, w, w2, z2);
+    float ec[BH];
+#pragma unroll
+    for (int j = 0; j < BH; ++j) ec[j] = eb[j * G::EWP + tid + N2];
+    __syncthreads();
+    // 2. blur #1, vertical, and the ratio: rows E-R .. E-R+7, column x0-R+tid
+    {
+      float win[BH + N2];
+#pragma unroll
+      for (int i = 0; i < N2; ++i) win[i] = c1[i];
+#pragma unroll
+      for (int j = 0; j < BH; ++j) win[N2 + j] = S.t[j][tid];
+      float bs[BH];
+      vsum_packed<R, BH>(win, w2, z2, bs);
+#pragma unroll
+      for (int j = 0; j < BH; ++j) {
+        const float b = bs[j];
+        const float g = TMA ? gb[(R + j) * G::EWP + R + tid] : gq[j];
+        // fmaxf(b, FLOOR) equals rmax(b, FLOOR): the floor is not NaN, and
+        // a NaN b gives the floor either way.
+        S.q[j][tid] = g / fmaxf(b, FLOOR);
+      }
+#pragma unroll
+      for (int i = 0; i < N2; ++i) c1[i] = win[BH + i];
+    }
+    __syncthreads();
+    if (edge_q) {
+      // Ratio columns outside the image within R of it take their mirror's value.
+      if ((unsigned)xq >= (unsigned)W && xq >= -R && xq < W + R) {
+        const int src = mirror_half(xq, W) - (x0 - R);
+#pragma unroll
+        for (int j = 0; j < BH; ++j) S.q[j][tid] = S.q[j][src];
+      }
+      __syncthreads();
+    }
+    // 3. blur #2, horizontal: rows E-R .. E-R+7, output columns (over blur #1,
+    //    whose rows every thread has read before the barrier above)
+    if (h2_on) hrun_full<R, G::RUN>(S.q[h2_row] + h2_col, S.t[h2_row] + h2_col, w, w2, z2);
+    __syncthreads();
+    // 4. blur #2, vertical, and the bounded update: rows E-2R .. E-2R+7
+    {
+      float win[BH + N2];
+#pragma unroll
+      for (int i = 0; i < N2; ++i) win[i] = c2[i];
+#pragma unroll
+      for (int j = 0; j < BH; ++j) win[N2 + j] = S.t[j][tid];
+#pragma unroll
+      for (int i = 0; i < N2; ++i) c2[i] = win[BH + i];
+      if (y0 == 0 && k == R / 2) {
+        // Window position p holds row E - 3R + p; rows -1 .. -R take rows 0 .. R-1.
+        constexpr int P0 = 5 * R - 8 * (R / 2);
+#pragma unroll
+        for (int i = 1; i <= R; ++i) win[P0 - i] = win[P0 + i - 1];
+      }
+      if (y1 == H && k == nsteps - 1) {
+        // This step ends at row H - 1: rows H .. H+R-1 take rows H-1 .. H-R.
+#pragma unroll
+        for (int i = 0; i < R; ++i) win[BH + R + i] = win[BH + R - 1 - i];
+      }
+      if (oko && E - N2 + BH > y0) {
+        float* po = est_out + (long long)(E - N2) * W + xo;
+        float eo[BH];
+        float bs[BH];
+        vsum_packed<R, BH>(win, w2, z2, bs);
+#pragma unroll
+        for (int j = 0; j < BH; ++j) {
+          const float b = bs[j];
+          const float e = (j < N2 ? ed[j] : ec[j - N2]) * b;
+          const float g = TMA ? gb[j * G::EWP + N2 + tid] : go[j];
+          // The develop rejects non-finite capture input, so e is never NaN
+          // here, and min / max give the reference's compare-and-replace.
+          eo[j] = fminf(fmaxf(e, g * 0.5f), g * 2.0f);
+        }
+        if (E - N2 >= y0 && E - N2 + BH <= y1) {
+#pragma unroll
+          for (int j = 0; j < BH; ++j) {
+            *po = eo[j];
+            po += W;
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < BH; ++j) {
+            const int o = E - N2 + j;
+            if (o >= y0 && o < y1) *po = eo[j];
+            po += W;
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < N2; ++i) ed[i] = ec[BH - N2 + i];
+  }
+}
+
 template <int R, bool TMA>
 __global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict__ est_in,
                                                           const float* __restrict__ guide,
@@ -598,205 +834,66 @@ __global__ void __launch_bounds__(128, 5) rl_step_kernel(const float* __restrict
                                                           const __grid_constant__ CUtensorMap guide_map,
                                                           unsigned* work, unsigned* error, unsigned wait_tries,
                                                           int withhold) {
-  using G = StepGeom<R>;
-  constexpr int T = G::T, SW = G::SW, BH = G::BH, N2 = 2 * R;
   extern __shared__ __align__(128) float4 rl_step_raw[];
   StepSmem<R, TMA>& S = *reinterpret_cast<StepSmem<R, TMA>*>(rl_step_raw);
-  float w[T];
-  float2 w2[T];
-#pragma unroll
-  for (int k = 0; k < T; ++k) {
-    w[k] = taps.w[k];
-    w2[k] = make_float2(taps.w[k], taps.w[k]);
-  }
-  const float2 z2 = make_float2(taps.neg_zero, taps.neg_zero);
-  const int tid = threadIdx.x;
-  if (TMA && tid == 0) {
+  const StepThread<R> th(taps);
+  if (TMA && threadIdx.x == 0) {
     for (int b = 0; b < 3; ++b) mbar_init(&S.bar[b]);
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   __syncthreads();
   CopyWaits cw(wait_tries, TMA && withhold != 0, error);
-  // The run each thread computes in the horizontal passes (row, first column).
-  const bool h1_on = tid < G::H1_RUNS * BH, h2_on = tid < G::H2_RUNS * BH;
-  const int h1_row = tid / G::H1_RUNS, h1_col = (tid % G::H1_RUNS) * G::RUN;
-  const int h2_row = tid / G::H2_RUNS, h2_col = (tid % G::H2_RUNS) * G::RUN;
+  const StepImage im{est_in, guide, est_out, W, H, strips, items, sg, &est_map, &guide_map};
   __shared__ int s_item;
-  for (int item = next_item(work, items, s_item); item < items; item = next_item(work, items, s_item)) {
-    int strip, seg;
-    strip_item(item, strips, sg.segs, strip, seg);
-    const int x0 = strip * SW;
-    const int y0 = seg_row(sg, seg, H), y1 = seg_row(sg, seg + 1, H);
-    const int E0 = y0 - N2;
-    const int nsteps = (y1 - y0 + 2 * N2 - BH + 7) / BH + 1;
-    const bool inside = x0 - N2 >= 0 && x0 - N2 + G::EW <= W;
-    const bool tma_strip = TMA && inside;
-    const bool edge_q = x0 < R || x0 + SW + R > W;
-    const int xal = (x0 - N2) & ~3;  // rounds down, also below 0
-    const int rem = TMA ? (x0 - N2) - xal : 0;
-    // Guide boxes stay inside the image columns (a box crossing the image edge
-    // takes the tensor unit much longer); reads shift by xal - gx. Columns the
-    // shifted box misses lie outside the image and only feed ratio columns
-    // that are overwritten by their mirrors and outputs that are not stored.
-    const int gx = TMA ? min(max(xal, 0), W - G::EWP) : 0;
-    const int xa = x0 - N2 + tid, xb = xa + 128;
-    const int sxa = (unsigned)xa < (unsigned)W ? xa : mirror_half(xa, W);
-    const bool has_b = tid + 128 < G::EW;
-    const int sxb = has_b ? ((unsigned)xb < (unsigned)W ? xb : mirror_half(xb, W)) : 0;
-    // Step k's estimate block (rows [E0 + 8k, +8)) goes to ring block k % 3, by
-    // one tensor copy when the rows and the window lie inside the image, else
-    // by per-thread copies with rows and columns mirrored into the image; its
-    // guide rows go to guide slot k % 3 by one tensor copy.
-    auto e_by_tma = [&](int k) {
-      const int r0 = E0 + BH * k;
-      return tma_strip && r0 >= 0 && r0 + BH <= H;
-    };
-    auto issue = [&](int k) {
-      if (k >= nsteps) return;
-      const int r0 = E0 + BH * k, b = k % 3;
-      const bool et = e_by_tma(k);
-      if (TMA && cw.issue_block(b) && tid == 0) {
-        fence_proxy_async();
-        mbar_expect_tx(&S.bar[b], (et ? BH * G::EWP * sizeof(float) : 0) + G::GH * G::EWP * sizeof(float));
-        if (et) tma_load_2d(S.e[b * BH], &est_map, xal, r0, &S.bar[b]);
-        tma_load_2d(S.g[b], &guide_map, gx, r0 - N2, &S.bar[b]);
-      }
-      if (et) return;
-#pragma unroll
-      for (int j = 0; j < BH; ++j) {
-        const float* src = est_in + (long long)mirror_row(r0 + j, H) * W;
-        float* dst = S.e[b * BH + j] + rem;
-        cp_async4(dst + tid, src + sxa);
-        if (has_b) cp_async4(dst + tid + 128, src + sxb);
-      }
-    };
-    issue(0);
-    cp_async_commit();
-    issue(1);
-    cp_async_commit();
-    // Carried rows: blur #1 rows [E-2R, E), blur #2 rows [E-3R, E-R), estimate
-    // rows [E-2R, E) of this thread's output column.
-    float c1[N2], c2[N2], ed[N2];
-#pragma unroll
-    for (int i = 0; i < N2; ++i) c1[i] = c2[i] = ed[i] = 1.0f;
-    const int xq = x0 - R + tid, xo = x0 + tid;
-    const bool okq = (unsigned)xq < (unsigned)W;
-    const bool oko = tid < SW && xo < W;
-    for (int k = 0; k < nsteps; ++k) {
-      const int E = E0 + BH * k;
-      // Without tensor maps: guide values of the ratio rows and of the update rows.
-      float gq[BH], go[BH];
-      if (!TMA) {
-#pragma unroll
-        for (int j = 0; j < BH; ++j) {
-          const int rq = E - R + j, ro = E - N2 + j;
-          gq[j] = okq && (unsigned)rq < (unsigned)H ? __ldg(guide + (long long)rq * W + xq) : 0.0f;
-          go[j] = oko && ro >= y0 && ro < y1 ? __ldg(guide + (long long)ro * W + xo) : 0.0f;
+  for (int item = next_item(work, items, s_item); item < items; item = next_item(work, items, s_item))
+    step_item<R, TMA>(S, im, item, th, cw);
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+  if (TMA) cw.drain(S.bar, 3);
+}
+
+// One iteration of several images in one launch (the batched develop's flat
+// pass): work items of every image from one counter, image by image in the
+// table's order; first_item[i] is image i's first item (first_item[n] = items).
+// The images share the taps; each brings its own planes, size and tensor maps
+// (kept in global memory).
+template <int R, bool TMA>
+__global__ void __launch_bounds__(128, 5) rl_step_images_kernel(const StepImage* __restrict__ images,
+                                                                 const int* __restrict__ first_item, int nimages,
+                                                                 int items, const Taps taps, unsigned* work,
+                                                                 unsigned* error, unsigned wait_tries, int withhold) {
+  extern __shared__ __align__(128) float4 rl_step_raw[];
+  StepSmem<R, TMA>& S = *reinterpret_cast<StepSmem<R, TMA>*>(rl_step_raw);
+  const StepThread<R> th(taps);
+  if (TMA && threadIdx.x == 0) {
+    for (int b = 0; b < 3; ++b) mbar_init(&S.bar[b]);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncthreads();
+  CopyWaits cw(wait_tries, TMA && withhold != 0, error);
+  __shared__ int s_item, s_local;
+  __shared__ StepImage s_im;
+  for (;;) {
+    // The barrier in front ends every read of the previous item's buffers.
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const unsigned v = atomicAdd(work, 1u);
+      if (v == (unsigned)items + gridDim.x - 1u) atomicExch(work, 0u);
+      s_item = (int)v;
+      if ((int)v < items) {
+        int lo = 0, hi = nimages;
+        while (hi - lo > 1) {
+          const int mid = (lo + hi) >> 1;
+          if (first_item[mid] <= (int)v) lo = mid;
+          else hi = mid;
         }
+        s_im = images[lo];
+        s_local = (int)v - first_item[lo];
       }
-      asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-      if (TMA) cw.wait(&S.bar[k % 3], k % 3);
-      __syncthreads();
-      // Block k + 2 reuses the slots of block k - 1, whose estimate rows were
-      // last read before the second barrier of step k - 1 and whose guide rows
-      // before the barrier above.
-      issue(k + 2);
-      cp_async_commit();
-      const float* eb = S.e[(k % 3) * BH] + rem;
-      const float* gb = S.g[TMA ? k % 3 : 0] + rem + (xal - gx);
-      // 1. blur #1, horizontal: rows E..E+7, columns x0-R .. x0-R+134
-      if (h1_on) hrun_full<R, G::RUN>(eb + h1_row * G::EWP + h1_col, S.t[h1_row] + h1_col, w, w2, z2);
-      float ec[BH];
-#pragma unroll
-      for (int j = 0; j < BH; ++j) ec[j] = eb[j * G::EWP + tid + N2];
-      __syncthreads();
-      // 2. blur #1, vertical, and the ratio: rows E-R .. E-R+7, column x0-R+tid
-      {
-        float win[BH + N2];
-#pragma unroll
-        for (int i = 0; i < N2; ++i) win[i] = c1[i];
-#pragma unroll
-        for (int j = 0; j < BH; ++j) win[N2 + j] = S.t[j][tid];
-        float bs[BH];
-        vsum_packed<R, BH>(win, w2, z2, bs);
-#pragma unroll
-        for (int j = 0; j < BH; ++j) {
-          const float b = bs[j];
-          const float g = TMA ? gb[(R + j) * G::EWP + R + tid] : gq[j];
-          // fmaxf(b, FLOOR) equals rmax(b, FLOOR): the floor is not NaN, and
-          // a NaN b gives the floor either way.
-          S.q[j][tid] = g / fmaxf(b, FLOOR);
-        }
-#pragma unroll
-        for (int i = 0; i < N2; ++i) c1[i] = win[BH + i];
-      }
-      __syncthreads();
-      if (edge_q) {
-        // Ratio columns outside the image within R of it take their mirror's value.
-        if ((unsigned)xq >= (unsigned)W && xq >= -R && xq < W + R) {
-          const int src = mirror_half(xq, W) - (x0 - R);
-#pragma unroll
-          for (int j = 0; j < BH; ++j) S.q[j][tid] = S.q[j][src];
-        }
-        __syncthreads();
-      }
-      // 3. blur #2, horizontal: rows E-R .. E-R+7, output columns (over blur #1,
-      //    whose rows every thread has read before the barrier above)
-      if (h2_on) hrun_full<R, G::RUN>(S.q[h2_row] + h2_col, S.t[h2_row] + h2_col, w, w2, z2);
-      __syncthreads();
-      // 4. blur #2, vertical, and the bounded update: rows E-2R .. E-2R+7
-      {
-        float win[BH + N2];
-#pragma unroll
-        for (int i = 0; i < N2; ++i) win[i] = c2[i];
-#pragma unroll
-        for (int j = 0; j < BH; ++j) win[N2 + j] = S.t[j][tid];
-#pragma unroll
-        for (int i = 0; i < N2; ++i) c2[i] = win[BH + i];
-        if (y0 == 0 && k == R / 2) {
-          // Window position p holds row E - 3R + p; rows -1 .. -R take rows 0 .. R-1.
-          constexpr int P0 = 5 * R - 8 * (R / 2);
-#pragma unroll
-          for (int i = 1; i <= R; ++i) win[P0 - i] = win[P0 + i - 1];
-        }
-        if (y1 == H && k == nsteps - 1) {
-          // This step ends at row H - 1: rows H .. H+R-1 take rows H-1 .. H-R.
-#pragma unroll
-          for (int i = 0; i < R; ++i) win[BH + R + i] = win[BH + R - 1 - i];
-        }
-        if (oko && E - N2 + BH > y0) {
-          float* po = est_out + (long long)(E - N2) * W + xo;
-          float eo[BH];
-          float bs[BH];
-          vsum_packed<R, BH>(win, w2, z2, bs);
-#pragma unroll
-          for (int j = 0; j < BH; ++j) {
-            const float b = bs[j];
-            const float e = (j < N2 ? ed[j] : ec[j - N2]) * b;
-            const float g = TMA ? gb[j * G::EWP + N2 + tid] : go[j];
-            // The develop rejects non-finite capture input, so e is never NaN
-            // here, and min / max give the reference's compare-and-replace.
-            eo[j] = fminf(fmaxf(e, g * 0.5f), g * 2.0f);
-          }
-          if (E - N2 >= y0 && E - N2 + BH <= y1) {
-#pragma unroll
-            for (int j = 0; j < BH; ++j) {
-              *po = eo[j];
-              po += W;
-            }
-          } else {
-#pragma unroll
-            for (int j = 0; j < BH; ++j) {
-              const int o = E - N2 + j;
-              if (o >= y0 && o < y1) *po = eo[j];
-              po += W;
-            }
-          }
-        }
-      }
-#pragma unroll
-      for (int i = 0; i < N2; ++i) ed[i] = ec[BH - N2 + i];
     }
+    __syncthreads();
+    if (s_item >= items) break;
+    const StepImage im = s_im;
+    step_item<R, TMA>(S, im, s_local, th, cw);
   }
   asm volatile("cp.async.wait_all;\n" ::: "memory");
   if (TMA) cw.drain(S.bar, 3);
@@ -1724,6 +1821,220 @@ Status run_capture(Context& ctx, float* rgb, int W, int H, const rd_detail_desc&
     if (cudaGetLastError() != cudaSuccess) st = Status{RD_SYNCHRONIZATION, "capture apply failed to launch"};
   }
   if (planes) device_free(ctx, planes, plane_bytes);
+  return st;
+}
+
+
+// ---- capture sharpening of several images at once ---------------------------
+namespace {
+
+template <int R, bool TMA>
+Status launch_rl_step_images(Context& ctx, const StepImage* d_images, const int* d_first, int nimages, int items,
+                             const Taps& taps) {
+  const size_t smem = sizeof(StepSmem<R, TMA>);
+  RD_CUDA_TRY(
+      cudaFuncSetAttribute(rl_step_images_kernel<R, TMA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int occ = 0;
+  RD_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, rl_step_images_kernel<R, TMA>, 128, smem));
+  const int sms = ctx.sm_count > 0 ? ctx.sm_count : 152;
+  const int grid = std::min(items, std::max(1, occ) * sms);
+  RD_LAUNCH(ctx, K_RL_ITER,
+            rl_step_images_kernel<R, TMA><<<grid, 128, smem, ctx.stream>>>(
+                d_images, d_first, nimages, items, taps, ctx.d_work, ctx.d_error,
+                ctx.wait_limit ? ctx.wait_limit : RL_DEFAULT_WAIT_TRIES, ctx.wait_withhold == RD_WAIT_RL_COPY ? 1 : 0));
+  return Status{};
+}
+
+Status rl_step_images(Context& ctx, int r, bool tma, const StepImage* d_images, const int* d_first, int nimages,
+                      int items, const Taps& taps) {
+  switch (r) {
+#define RD_STEP_IMAGES_CASE(RR)                                                                       \
+  case RR:                                                                                            \
+    return tma ? launch_rl_step_images<RR, true>(ctx, d_images, d_first, nimages, items, taps)        \
+               : launch_rl_step_images<RR, false>(ctx, d_images, d_first, nimages, items, taps);
+    RD_STEP_IMAGES_CASE(1)
+    RD_STEP_IMAGES_CASE(2)
+    RD_STEP_IMAGES_CASE(3)
+    RD_STEP_IMAGES_CASE(4)
+#undef RD_STEP_IMAGES_CASE
+    default:
+      return Status{RD_INVALID_INPUT, "capture radius outside 1..4"};
+  }
+}
+
+// Per image of run_capture_images: its RL planes, taps and step geometry, and
+// the device copies of its four tensor maps (guide, the two estimates, and
+// the guide for the step kernel's 8 + R row boxes).
+struct CapturePlanes {
+  int job = -1, r = 0, iterations = 0;
+  Taps taps{};
+  float* planes = nullptr;
+  size_t bytes = 0;
+  bool tma = false;
+  CUtensorMap maps[4];
+  StepSegments sg{};
+  int strips = 0, items = 0;
+};
+
+}  // namespace
+
+Status run_capture_images(Context& ctx, CaptureJob* jobs, int n) {
+  std::vector<CapturePlanes> prepared;
+  const int sms = ctx.sm_count > 0 ? ctx.sm_count : 152;
+  // 1. Settings, planes and the guide / mask pass, image by image; images the
+  //    step kernel does not serve take the per-image path whole.
+  for (int j = 0; j < n; ++j) {
+    CaptureJob& job = jobs[j];
+    const rd_detail_desc& d = job.detail;
+    if (!job.st.ok() || !(d.enabled && d.amount > 0.0f)) continue;
+    const int W = job.W, H = job.H;
+    CapturePlanes cp;
+    cp.job = j;
+    const int ntaps = gaussian_kernel(d.radius, cp.taps.w, MAX_TAPS);
+    cp.taps.neg_zero = -0.0f;
+    cp.r = ntaps / 2;
+    if (ntaps < 0 || !rl_uses_step_kernel(W, H, cp.r) || d.iterations < 1) {
+      job.st = run_capture(ctx, job.rgb, W, H, d);
+      continue;
+    }
+    if (!(d.radius >= 0.3f && d.radius <= 1.2f) || !(d.amount <= 1.0f) ||
+        !(d.noise_protection >= 0.0f && d.noise_protection <= 1.0f)) {
+      job.st = Status{RD_INVALID_INPUT, "capture sharpening settings are outside their ranges"};
+      continue;
+    }
+    bool ceilings_ok = true;
+    for (int c = 0; c < 3; ++c)
+      if (!std::isfinite(d.ceilings[c]) || !(d.ceilings[c] > 0.0f)) ceilings_ok = false;
+    if (!ceilings_ok) {
+      job.st = Status{RD_INVALID_INPUT, "capture ceilings must be finite and positive"};
+      continue;
+    }
+    const long long plane = (long long)W * H;
+    cp.bytes = sizeof(float) * (size_t)plane * 4;
+    void* p = nullptr;
+    job.st = device_alloc(ctx, cp.bytes, &p);
+    if (!job.st.ok()) continue;
+    cp.planes = static_cast<float*>(p);
+    float* guide = cp.planes;
+    float* mask = cp.planes + plane;
+    CUtensorMap rgb_map;
+    const bool rgb_tma =
+        rl_prep_uses_step_kernel(W, H, cp.r) && make_plane_map(&rgb_map, job.rgb, W, 3 * H, PrepGeom<1>::CWP, 8);
+    job.st = rl_prep(ctx, cp.r, cp.taps, job.rgb, plane, d.ceilings, d.noise_protection, guide, mask, W, H,
+                     rgb_tma ? &rgb_map : nullptr);
+    if (!job.st.ok()) {
+      device_free(ctx, cp.planes, cp.bytes);
+      continue;
+    }
+    const int box_w = rl_box_width(W, H, cp.r);
+    cp.tma = make_plane_map(&cp.maps[0], guide, W, H, box_w) &&
+             make_plane_map(&cp.maps[1], cp.planes + 2 * plane, W, H, box_w) &&
+             make_plane_map(&cp.maps[2], cp.planes + 3 * plane, W, H, box_w) &&
+             make_plane_map(&cp.maps[3], guide, W, H, box_w, 8 + cp.r);
+    int segs = 0;
+    {
+      std::lock_guard<std::mutex> lk(g_rl_tune_mutex);
+      auto it = g_rl_tuned.find(RlShape{W, H, cp.r});
+      if (it != g_rl_tuned.end()) segs = it->second.segs;
+    }
+    if (segs == 0) segs = rl_default_segments(W, H, cp.r, sms);
+    cp.sg = step_segments(H, cp.r, segs);
+    cp.iterations = d.iterations;
+    prepared.push_back(cp);
+  }
+  // 2. The iterations: images with the same taps and tensor-copy ability
+  //    share one launch per iteration; an image leaves after its last one.
+  Status st;
+  std::vector<bool> done(prepared.size(), false);
+  for (size_t g = 0; g < prepared.size() && st.ok(); ++g) {
+    if (done[g]) continue;
+    std::vector<size_t> group;
+    for (size_t k = g; k < prepared.size(); ++k)
+      if (!done[k] && prepared[k].r == prepared[g].r && prepared[k].tma == prepared[g].tma &&
+          std::memcmp(prepared[k].taps.w, prepared[g].taps.w, sizeof(float) * (2 * prepared[g].r + 1)) == 0) {
+        group.push_back(k);
+        done[k] = true;
+      }
+    const int r = prepared[g].r;
+    const bool tma = prepared[g].tma;
+    int max_k = 0;
+    for (size_t k : group) max_k = std::max(max_k, prepared[k].iterations);
+    // Device tables: the group's tensor maps, then per iteration the image
+    // table and its first-item offsets.
+    const size_t map_bytes = sizeof(CUtensorMap) * 4 * group.size();
+    const size_t img_bytes = (sizeof(StepImage) * group.size() + 63) & ~(size_t)63;
+    const size_t first_bytes = (sizeof(int) * (group.size() + 1) + 63) & ~(size_t)63;
+    const size_t table_bytes = map_bytes + (size_t)max_k * (img_bytes + first_bytes);
+    void* t = nullptr;
+    st = device_alloc(ctx, table_bytes + 64, &t);
+    if (!st.ok()) break;
+    unsigned char* tb =
+        reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(t) + 63) & ~static_cast<uintptr_t>(63));
+    std::vector<unsigned char> host(table_bytes, 0);
+    const CUtensorMap* d_maps = reinterpret_cast<const CUtensorMap*>(tb);
+    for (size_t i = 0; i < group.size(); ++i)
+      std::memcpy(host.data() + sizeof(CUtensorMap) * 4 * i, prepared[group[i]].maps, sizeof(CUtensorMap) * 4);
+    std::vector<int> counts((size_t)max_k, 0), totals((size_t)max_k, 0);
+    for (int it = 0; it < max_k; ++it) {
+      StepImage* images = reinterpret_cast<StepImage*>(host.data() + map_bytes + (size_t)it * (img_bytes + first_bytes));
+      int* first = reinterpret_cast<int*>(host.data() + map_bytes + (size_t)it * (img_bytes + first_bytes) + img_bytes);
+      int m = 0, items = 0;
+      for (size_t i = 0; i < group.size(); ++i) {
+        const CapturePlanes& cp = prepared[group[i]];
+        if (cp.iterations <= it) continue;
+        const CaptureJob& job = jobs[cp.job];
+        const long long plane = (long long)job.W * job.H;
+        float* est[2] = {cp.planes + 2 * plane, cp.planes + 3 * plane};
+        StepImage& im = images[m];
+        im.est_in = it == 0 ? cp.planes : est[(it - 1) & 1];
+        im.guide = cp.planes;
+        im.est_out = est[it & 1];
+        im.W = job.W;
+        im.H = job.H;
+        im.strips = (job.W + StepGeom<1>::QW - 2 * r - 1) / (StepGeom<1>::QW - 2 * r);
+        im.sg = cp.sg;
+        im.items = im.strips * cp.sg.segs;
+        // The first iteration reads the guide, later ones the estimate the one before wrote.
+        im.est_map = tma ? d_maps + 4 * i + (it == 0 ? 0 : 1 + ((it - 1) & 1)) : nullptr;
+        im.guide_map = tma ? d_maps + 4 * i + 3 : nullptr;
+        first[m] = items;
+        items += im.items;
+        ++m;
+      }
+      first[m] = items;
+      counts[(size_t)it] = m;
+      totals[(size_t)it] = items;
+    }
+    st = upload(ctx, tb, host.data(), table_bytes);
+    for (int it = 0; it < max_k && st.ok(); ++it) {
+      const unsigned char* base = tb + map_bytes + (size_t)it * (img_bytes + first_bytes);
+      st = rl_step_images(ctx, r, tma, reinterpret_cast<const StepImage*>(base),
+                          reinterpret_cast<const int*>(base + img_bytes), counts[(size_t)it], totals[(size_t)it],
+                          prepared[g].taps);
+    }
+    if (st.ok() && cudaGetLastError() != cudaSuccess) st = Status{RD_SYNCHRONIZATION, "capture kernels failed to launch"};
+    device_free(ctx, t, table_bytes + 64);
+  }
+  // 3. The gain, image by image (sharpening.rs:110-118), then the planes go.
+  for (CapturePlanes& cp : prepared) {
+    CaptureJob& job = jobs[cp.job];
+    const long long plane = (long long)job.W * job.H;
+    if (st.ok()) {
+      ApplyParams ap{};
+      ap.rgb = job.rgb;
+      ap.plane = plane;
+      ap.W = job.W;
+      ap.H = job.H;
+      ap.amount = job.detail.amount;
+      ap.mask = cp.planes + plane;
+      ap.est = cp.planes + (2 + ((cp.iterations - 1) & 1)) * plane;
+      ap.guide = cp.planes;
+      RD_LAUNCH(ctx, K_RL_APPLY, rl_apply_kernel<<<(unsigned)((plane + 255) / 256), 256, 0, ctx.stream>>>(ap));
+      if (cudaGetLastError() != cudaSuccess) st = Status{RD_SYNCHRONIZATION, "capture apply failed to launch"};
+    }
+    if (!st.ok()) job.st = st;
+    device_free(ctx, cp.planes, cp.bytes);
+  }
   return st;
 }
 

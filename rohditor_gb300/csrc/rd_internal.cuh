@@ -272,6 +272,18 @@ Status run_opposed_labels(Context& ctx, const MosaicSource& src, float* mosaic, 
                           uint32_t* region_count);
 Status run_demosaic(Context& ctx, const MosaicSource& src, int algorithm, float* rgb, unsigned long long* clip_stats);
 Status run_capture(Context& ctx, float* rgb, int width, int height, const rd_detail_desc& detail);
+// Capture sharpening of several images (the batched develop's flat pass): the
+// guide / mask pass image by image, every iteration of the images that share
+// their taps in one launch over all their work items, then the gain image by
+// image; each image ends bit for bit as run_capture leaves it. A job's status
+// reports its own failure; the return value the first launch failure.
+struct CaptureJob {
+  float* rgb;
+  int W, H;
+  rd_detail_desc detail;
+  Status st;
+};
+Status run_capture_images(Context& ctx, CaptureJob* jobs, int n);
 // Vignetting multiplier plane (width*height f32) of an optics execution.
 Status run_vignette_plane(Context& ctx, const rd_optics_desc& optics, float* mult);
 // Radial multiplier table of one optics execution (RadialMultipliers,

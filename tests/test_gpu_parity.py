@@ -684,9 +684,13 @@ def test_concurrent_lanes_with_different_widths_repeat_exactly(device):
 @pytest.mark.parametrize("mode", ["lanes", "graph", "flat"])
 def test_batched_develop_matches_one_at_a_time(device, mode):
     """rd_develop_batch (concurrent lanes), rd_develop_batch_graph (one
-    captured CUDA graph) and rd_develop_batch_flat (stage by stage, one AMaZE
-    launch over every image's tiles) over uneven sizes, CFA phases, highlight
-    modes and capture radii equal the per-image path, bit for bit."""
+    captured CUDA graph) and rd_develop_batch_flat (stage by stage: one AMaZE
+    launch over every image's tiles, one launch per RL iteration over the work
+    items of the images that share their taps) over uneven sizes, CFA phases,
+    highlight modes, capture radii and iteration counts equal the per-image
+    path, bit for bit. The 702-wide image has no tensor maps (its rows are not
+    a multiple of 16 bytes) and the 200x150 one is below the step kernel's
+    size, so both leave the flat RL launches of the others."""
     graph = mode == "graph"
     from rohditor_gb300 import (CaptureContract, ColorContract, GpuPreviewProcessor, GpuSensorProcessor,
                                 GpuSpatialProcessor, OpticsExecution, SensorDescription, clip_levels, opposed_levels)
@@ -694,7 +698,7 @@ def test_batched_develop_matches_one_at_a_time(device, mode):
     from rohditor_gb300.workloads import CAMERA_TO_REC2020, hsl_bands, preview_dimensions, sixteen_knot_curve
 
     shapes = [(700, 467, "RGGB", "clip"), (1024, 768, "GBRG", "opposed"), (512, 384, "BGGR", "clip"),
-              (640, 480, "GRBG", "opposed")]
+              (640, 480, "GRBG", "opposed"), (702, 300, "RGGB", "clip"), (200, 150, "GBRG", "clip")]
     images = []
     for k, (w, h, cfa, hl) in enumerate(shapes):
         raw = raw_mosaic(w, h, w, seed=70 + k)
@@ -710,7 +714,7 @@ def test_batched_develop_matches_one_at_a_time(device, mode):
                                        demosaic_balance=wb)
             ceil = (1.0, 1.0, 1.0)
         cap = CaptureContract(amount=0.5, radius=0.7 if k % 2 == 0 else 1.1, noise_protection=0.5, ceilings=ceil,
-                              iterations=5)
+                              iterations=5 - k % 3)
         optics = OpticsExecution(w, h, distortion="poly5", distortion_k=(-0.02, 0.005, 0.0), tca="linear",
                                  tca_red=(1.0003, 0, 0), tca_blue=(0.9997, 0, 0), vignetting_k=(-0.3, 0.05, -0.01))
         color = ColorContract(wb_gains=wb, camera_to_rec2020=CAMERA_TO_REC2020, exposure_ev=0.1 * k,
