@@ -703,11 +703,18 @@ def batched_throughput(args, count: int = 48, lanes: int = 3) -> dict:
                               "develops_per_s": round(count / (g["launch_ms"] / 1e3), 2),
                               "mp_per_s": round(pixels / 1e6 / (g["launch_ms"] / 1e3), 1),
                               "speedup_vs_one_lane": round(p1 / g["launch_ms"], 3)}
+    # The stage-by-stage batch as one captured graph (rd_develop_batch_flat_graph).
+    pinned.run(lanes=lanes, graph=True, flat=True)  # warm-up
+    fg = pinned.run(lanes=lanes, graph=True, flat=True)
+    flat_graph = {"launch_ms": round(fg["launch_ms"], 1), "capture_ms": round(fg["capture_ms"], 1),
+                  "develops_per_s": round(count / (fg["launch_ms"] / 1e3), 2),
+                  "mp_per_s": round(pixels / 1e6 / (fg["launch_ms"] / 1e3), 1),
+                  "speedup_vs_one_lane": round(p1 / fg["launch_ms"], 3)}
     pinned.close()
     pinned_runs = {"one_lane_wall_ms": round(p1, 1), "lanes_wall_ms": round(pl, 1),
                    "lanes_mp_per_s": round(pixels / 1e6 / (pl / 1e3), 1), "flat_wall_ms": round(pf, 1),
                    "flat_mp_per_s": round(pixels / 1e6 / (pf / 1e3), 1),
-                   "flat_speedup_vs_one_lane": round(p1 / pf, 3), "graph_chains": graph}
+                   "flat_speedup_vs_one_lane": round(p1 / pf, 3), "graph_chains": graph, "flat_graph": flat_graph}
     return {"images": count, "megapixels": round(pixels / 1e6, 1), "lanes": lanes, "wall_ms": round(wall, 1),
             "develops_per_s": round(count / (wall / 1e3), 2), "mp_per_s": round(pixels / 1e6 / (wall / 1e3), 1),
             "one_lane_wall_ms": round(wall1, 1), "speedup_vs_one_lane": round(wall1 / wall, 3),

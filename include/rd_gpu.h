@@ -430,6 +430,15 @@ rd_status rd_develop_batch_graph(int device, rd_batch_item* items, int32_t count
  * holds every image's intermediates at once. Per-item `ms` covers the
  * finishing stage only. */
 rd_status rd_develop_batch_flat(int device, rd_batch_item* items, int32_t count, int32_t lanes, double* wall_ms);
+/* The stage-by-stage batch captured into one CUDA graph and run as a single
+ * launch: `chains` branches upload and normalize / highlight the images
+ * (k % chains), then one branch runs the AMaZE launch over every image's
+ * tiles and the capture sharpening with one launch per RL iteration over the
+ * batch, then the branches finish their images (spatial pass, render). Host
+ * buffers and timings as rd_develop_batch_graph; outputs equal the per-image
+ * path bit for bit. */
+rd_status rd_develop_batch_flat_graph(int device, rd_batch_item* items, int32_t count, int32_t chains,
+                                      int32_t host_pinned, double* wall_ms, double* capture_ms, double* launch_ms);
 
 /* ---- served preview loop ----
  * Replaces the engine's preview worker and caches

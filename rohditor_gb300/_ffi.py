@@ -215,6 +215,9 @@ SIGNATURES = {
                                               ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "rd_develop_batch_flat": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(BatchItem), ctypes.c_int32, ctypes.c_int32,
                                              ctypes.POINTER(ctypes.c_double)]),
+    "rd_develop_batch_flat_graph": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(BatchItem), ctypes.c_int32,
+                                                   ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_double),
+                                                   ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "rd_server_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(VOIDP)]),
     "rd_server_set_dry_timing": (ctypes.c_int, [VOIDP, ctypes.c_uint32, ctypes.c_uint32]),
     "rd_server_destroy": (None, [VOIDP]),

@@ -6,7 +6,9 @@ host buffers. With `graph=False`, `lanes` contexts on their own streams work
 through a shared queue concurrently so their kernels overlap on the GPU. With
 `graph=True` the whole batch is captured into one CUDA graph of `lanes`
 parallel branches and runs as a single launch. With `flat=True` the batch
-runs stage by stage, with one AMaZE launch over the tiles of every image.
+runs stage by stage, with one AMaZE launch over the tiles of every image and
+one launch per RL iteration over the batch; `flat=True` with `graph=True`
+captures that stage-by-stage batch into one CUDA graph.
 """
 
 from __future__ import annotations
@@ -80,7 +82,10 @@ class PinnedBatch:
         """Times of one run: wall_ms, and for a graph capture_ms and launch_ms."""
         wall, cap, launch = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
         n = len(self.items)
-        if flat:
+        if flat and graph:
+            rc = self.lib.rd_develop_batch_flat_graph(self.device, self.items, n, lanes, 1, ctypes.byref(wall),
+                                                      ctypes.byref(cap), ctypes.byref(launch))
+        elif flat:
             rc = self.lib.rd_develop_batch_flat(self.device, self.items, n, lanes, ctypes.byref(wall))
         elif graph:
             rc = self.lib.rd_develop_batch_graph(self.device, self.items, n, lanes, 1, ctypes.byref(wall),
@@ -115,7 +120,9 @@ def develop_batch(images: list[BatchImage], lanes: int = 3, device: int = 0, gra
     """Returns (outputs [(srgb8, hist)], per-image ms, wall ms); with `graph`,
     the per-image ms are 0 and the capture + instantiation ms is the last
     element of the returned tuple. With `flat` the batch runs stage by stage
-    with one AMaZE launch over every image's tiles (rd_develop_batch_flat)."""
+    with one AMaZE launch over every image's tiles and one launch per RL
+    iteration over the batch (rd_develop_batch_flat; with `graph` too, the
+    same captured into one CUDA graph, rd_develop_batch_flat_graph)."""
     lib = _ffi.load()
     items = (_ffi.BatchItem * len(images))()
     keep = []
@@ -135,8 +142,8 @@ def develop_batch(images: list[BatchImage], lanes: int = 3, device: int = 0, gra
     wall = ctypes.c_double()
     if graph:
         capture = ctypes.c_double()
-        rc = lib.rd_develop_batch_graph(device, items, len(images), lanes, 0, ctypes.byref(wall), ctypes.byref(capture),
-                                        None)
+        run = lib.rd_develop_batch_flat_graph if flat else lib.rd_develop_batch_graph
+        rc = run(device, items, len(images), lanes, 0, ctypes.byref(wall), ctypes.byref(capture), None)
         if rc != 0:
             raise GpuPreviewError(rc, f"batched graph develop failed: {lib.rd_status_name(rc).decode()}")
         return outs, [0.0] * len(images), wall.value, capture.value

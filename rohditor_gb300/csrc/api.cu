@@ -1620,3 +1620,187 @@ extern "C" rd_status rd_develop_batch_flat(int device, rd_batch_item* items, int
     if (items[k].status != RD_OK) return (rd_status)items[k].status;
   return RD_OK;
 }
+
+// rd_develop_batch_flat_graph: the stage-by-stage batch captured into one CUDA
+// graph. Branches (one context and stream each, image k on branch k %
+// chains) upload and normalize / highlight their images; after a join, branch
+// 0 runs the one AMaZE launch over every image's half-tile items and the
+// capture sharpening with one launch per RL iteration over the batch; after a
+// fork the branches finish their images (spatial pass, render into pinned
+// outputs). Every device buffer is allocated and freed inside the graph;
+// the AMaZE scratch for the whole batch is reserved before the capture.
+extern "C" rd_status rd_develop_batch_flat_graph(int device, rd_batch_item* items, int32_t count, int32_t chains,
+                                                 int32_t host_pinned, double* wall_ms, double* capture_ms,
+                                                 double* launch_ms) {
+  using Clock = std::chrono::steady_clock;
+  if (!items || count < 0 || chains <= 0) return RD_INVALID_INPUT;
+  if (wall_ms) *wall_ms = 0.0;
+  if (capture_ms) *capture_ms = 0.0;
+  if (launch_ms) *launch_ms = 0.0;
+  if (count == 0) return RD_OK;
+  chains = std::min(chains, count);
+  std::vector<rd_ctx*> ctxs(chains, nullptr);
+  rd_status status = RD_OK;
+  size_t all_tiles = 1;
+  for (int k = 0; k < count; ++k)
+    all_tiles += rd::amaze_tiles((int)items[k].sensor.crop_width, (int)items[k].sensor.crop_height);
+  for (int c = 0; c < chains && status == RD_OK; ++c) {
+    status = rd_ctx_create(device, 0, &ctxs[c]);
+    if (status == RD_OK && c == 0 && !rd::reserve_amaze_scratch(ctxs[c]->c, all_tiles).ok()) status = RD_OVER_BUDGET;
+    if (status == RD_OK && cudaStreamSynchronize(ctxs[c]->c.stream) != cudaSuccess) status = RD_SYNCHRONIZATION;
+  }
+  // Pinned staging for each image's mosaic, sRGB8 output and histogram,
+  // unless the caller's buffers are pinned already (read and written in place).
+  std::vector<size_t> in_off(count), out_off(count), hist_off(count);
+  size_t total = 0;
+  for (int k = 0; k < count && !host_pinned; ++k) {
+    const rd_batch_item& it = items[k];
+    in_off[k] = total;
+    total += (sizeof(uint16_t) * it.row_stride * it.sensor.sensor_height + 255) & ~(size_t)255;
+    out_off[k] = total;
+    total += ((size_t)3 * it.target_width * it.target_height + 255) & ~(size_t)255;
+    hist_off[k] = total;
+    total += 1024 * sizeof(uint64_t);
+  }
+  unsigned char* stage = nullptr;
+  if (status == RD_OK && !host_pinned &&
+      cudaHostAlloc(reinterpret_cast<void**>(&stage), total, cudaHostAllocDefault) != cudaSuccess)
+    status = RD_OVER_BUDGET;
+  cudaStream_t main = nullptr;
+  cudaEvent_t fork = nullptr, mid = nullptr;
+  std::vector<cudaEvent_t> join(chains, nullptr), prepared(chains, nullptr);
+  if (status == RD_OK && (cudaStreamCreateWithFlags(&main, cudaStreamNonBlocking) != cudaSuccess ||
+                          cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess ||
+                          cudaEventCreateWithFlags(&mid, cudaEventDisableTiming) != cudaSuccess))
+    status = RD_SYNCHRONIZATION;
+  for (int c = 0; c < chains && status == RD_OK; ++c)
+    if (cudaEventCreateWithFlags(&join[c], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&prepared[c], cudaEventDisableTiming) != cudaSuccess)
+      status = RD_SYNCHRONIZATION;
+  for (int k = 0; k < count; ++k) items[k].status = RD_CANCELLED;
+  std::vector<FlatJob> jobs((size_t)count);
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  const auto c0 = Clock::now();
+  if (status == RD_OK) {
+    cudaSetDevice(device);
+    if (cudaStreamBeginCapture(main, cudaStreamCaptureModeRelaxed) != cudaSuccess ||
+        cudaEventRecord(fork, main) != cudaSuccess)
+      status = RD_SYNCHRONIZATION;
+    for (int c = 0; c < chains && status == RD_OK; ++c) {
+      if (cudaStreamWaitEvent(ctxs[c]->c.stream, fork, 0) != cudaSuccess) status = RD_SYNCHRONIZATION;
+      ctxs[c]->c.capturing = true;
+    }
+    // 1. upload + normalize + highlight on the branches.
+    for (int k = 0; k < count && status == RD_OK; ++k) {
+      rd_batch_item it = items[k];
+      if (!host_pinned) it.mosaic = reinterpret_cast<const uint16_t*>(stage + in_off[k]);
+      const Status st = flat_prepare(ctxs[k % chains], it, jobs[k]);
+      if (!st.ok()) status = st.code;
+    }
+    for (int c = 0; c < chains && status == RD_OK; ++c)
+      if (cudaEventRecord(prepared[c], ctxs[c]->c.stream) != cudaSuccess ||
+          cudaStreamWaitEvent(ctxs[0]->c.stream, prepared[c], 0) != cudaSuccess)
+        status = RD_SYNCHRONIZATION;
+    // 2. demosaic and capture sharpening over the batch on branch 0.
+    rd::Context& b0 = ctxs[0]->c;
+    if (status == RD_OK) {
+      std::vector<rd::AmazeJob> amaze;
+      Status st;
+      for (int k = 0; k < count && st.ok(); ++k) {
+        FlatJob& j = jobs[k];
+        const int alg = items[k].sensor.demosaic;
+        if (alg == RD_DEMOSAIC_AMAZE && j.source->W > 32 && j.source->H > 32)
+          amaze.push_back(rd::demosaic_job(j.src, alg, j.source->rgb, j.d_stats));
+        else
+          st = rd::run_demosaic(b0, j.src, alg, j.source->rgb, j.d_stats);
+      }
+      if (st.ok() && !amaze.empty()) st = rd::run_amaze_images(b0, amaze.data(), (int)amaze.size());
+      std::vector<rd::CaptureJob> capture;
+      for (int k = 0; k < count && st.ok(); ++k)
+        capture.push_back(
+            rd::CaptureJob{jobs[k].source->rgb, jobs[k].source->W, jobs[k].source->H, items[k].detail, Status{}});
+      if (st.ok() && !capture.empty()) st = rd::run_capture_images(b0, capture.data(), (int)capture.size());
+      for (const rd::CaptureJob& cj : capture)
+        if (st.ok() && !cj.st.ok()) st = cj.st;
+      if (!st.ok()) status = st.code;
+    }
+    if (status == RD_OK && cudaEventRecord(mid, b0.stream) != cudaSuccess) status = RD_SYNCHRONIZATION;
+    for (int c = 1; c < chains && status == RD_OK; ++c)
+      if (cudaStreamWaitEvent(ctxs[c]->c.stream, mid, 0) != cudaSuccess) status = RD_SYNCHRONIZATION;
+    // 3. spatial pass and render on the branches.
+    for (int k = 0; k < count && status == RD_OK; ++k) {
+      rd_batch_item& it = items[k];
+      rd_ctx* h = ctxs[k % chains];
+      FlatJob& j = jobs[k];
+      flat_release_staging(h, j);
+      rd_base* base = nullptr;
+      rd_status st = rd_spatial(h, j.source, &it.optics, it.target_width, it.target_height, it.wb_gains,
+                                it.camera_to_rec2020, &base, nullptr);
+      rd_source_release(j.source);
+      j.source = nullptr;
+      uint8_t* srgb = host_pinned ? it.srgb_out : stage + out_off[k];
+      uint64_t* hist = host_pinned ? it.hist : reinterpret_cast<uint64_t*>(stage + hist_off[k]);
+      if (st == RD_OK) st = rd_render(h, base, &it.color, srgb, hist, nullptr, nullptr);
+      if (base) rd_base_release(base);
+      if (st != RD_OK) status = st;
+    }
+    for (int c = 0; c < chains; ++c) {
+      ctxs[c]->c.capturing = false;
+      if (cudaEventRecord(join[c], ctxs[c]->c.stream) != cudaSuccess ||
+          cudaStreamWaitEvent(main, join[c], 0) != cudaSuccess)
+        if (status == RD_OK) status = RD_SYNCHRONIZATION;
+    }
+    const cudaError_t end = cudaStreamEndCapture(main, &graph);
+    if (end != cudaSuccess && status == RD_OK) status = RD_SYNCHRONIZATION;
+    if (status == RD_OK && cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) status = RD_SYNCHRONIZATION;
+    cudaGetLastError();
+  }
+  const auto c1 = Clock::now();
+  if (capture_ms) *capture_ms = std::chrono::duration<double, std::milli>(c1 - c0).count();
+  if (status == RD_OK) {
+    const auto t0 = Clock::now();
+    for (int k = 0; k < count && !host_pinned; ++k) {
+      const rd_batch_item& it = items[k];
+      std::memcpy(stage + in_off[k], it.mosaic, sizeof(uint16_t) * it.row_stride * it.sensor.sensor_height);
+    }
+    const auto l0 = Clock::now();
+    if (cudaGraphLaunch(exec, main) != cudaSuccess || cudaStreamSynchronize(main) != cudaSuccess)
+      status = RD_SYNCHRONIZATION;
+    if (launch_ms) *launch_ms = std::chrono::duration<double, std::milli>(Clock::now() - l0).count();
+    for (int c = 0; c < chains && status == RD_OK; ++c) {
+      const Status st = rd::check_kernel_error(ctxs[c]->c, "batch flat graph");
+      if (!st.ok()) status = st.code;
+    }
+    if (status == RD_OK)
+      for (int k = 0; k < count; ++k) {
+        rd_batch_item& it = items[k];
+        if (!host_pinned && it.srgb_out)
+          std::memcpy(it.srgb_out, stage + out_off[k], (size_t)3 * it.target_width * it.target_height);
+        if (!host_pinned && it.hist) std::memcpy(it.hist, stage + hist_off[k], 1024 * sizeof(uint64_t));
+        it.status = RD_OK;
+        it.ms = 0.0;
+      }
+    if (wall_ms) *wall_ms = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+  }
+  // A capture that failed part way leaves host-side handles behind; their
+  // device buffers were graph allocations that no launch made.
+  for (FlatJob& j : jobs) delete j.source;
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  for (cudaEvent_t e : join)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : prepared)
+    if (e) cudaEventDestroy(e);
+  if (fork) cudaEventDestroy(fork);
+  if (mid) cudaEventDestroy(mid);
+  if (main) cudaStreamDestroy(main);
+  for (rd_ctx* c : ctxs)
+    if (c) rd_ctx_destroy(c);
+  if (stage) cudaFreeHost(stage);
+  if (status != RD_OK)
+    for (int k = 0; k < count; ++k)
+      if (items[k].status == RD_OK) items[k].status = status;
+  return status;
+}
+

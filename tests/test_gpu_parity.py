@@ -681,17 +681,18 @@ def test_concurrent_lanes_with_different_widths_repeat_exactly(device):
             assert np.array_equal(a, b) and np.array_equal(ha, hb)
 
 
-@pytest.mark.parametrize("mode", ["lanes", "graph", "flat"])
+@pytest.mark.parametrize("mode", ["lanes", "graph", "flat", "flat_graph"])
 def test_batched_develop_matches_one_at_a_time(device, mode):
     """rd_develop_batch (concurrent lanes), rd_develop_batch_graph (one
-    captured CUDA graph) and rd_develop_batch_flat (stage by stage: one AMaZE
+    captured CUDA graph), rd_develop_batch_flat (stage by stage: one AMaZE
     launch over every image's tiles, one launch per RL iteration over the work
-    items of the images that share their taps) over uneven sizes, CFA phases,
+    items of the images that share their taps) and rd_develop_batch_flat_graph
+    (the stage-by-stage batch as one CUDA graph) over uneven sizes, CFA phases,
     highlight modes, capture radii and iteration counts equal the per-image
     path, bit for bit. The 702-wide image has no tensor maps (its rows are not
     a multiple of 16 bytes) and the 200x150 one is below the step kernel's
     size, so both leave the flat RL launches of the others."""
-    graph = mode == "graph"
+    graph = mode in ("graph", "flat_graph")
     from rohditor_gb300 import (CaptureContract, ColorContract, GpuPreviewProcessor, GpuSensorProcessor,
                                 GpuSpatialProcessor, OpticsExecution, SensorDescription, clip_levels, opposed_levels)
     from rohditor_gb300.batch import BatchImage, develop_batch
@@ -721,14 +722,14 @@ def test_batched_develop_matches_one_at_a_time(device, mode):
                               tone_lut=sixteen_knot_curve(seed=k), hsl=hsl_bands(seed=k))
         images.append(BatchImage(raw, sensor, cap, optics, preview_dimensions(w, h, 256), wb, CAMERA_TO_REC2020,
                                  color))
-    res = develop_batch(images, lanes=3, graph=graph, flat=mode == "flat")
+    res = develop_batch(images, lanes=3, graph=graph, flat=mode.startswith("flat"))
     outs, ms, wall = res[:3]
     assert wall > 0 and (graph or all(m > 0 for m in ms))
     if graph:
         # Pinned buffers used in place by the graph give the same outputs.
         from rohditor_gb300.batch import PinnedBatch
         pinned = PinnedBatch(images)
-        pinned.run(lanes=2, graph=True)
+        pinned.run(lanes=2, graph=True, flat=mode == "flat_graph")
         for (a, ha), (b, hb) in zip(outs, pinned.outputs()):
             assert np.array_equal(a, b) and np.array_equal(ha, hb)
         pinned.close()
