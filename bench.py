@@ -229,6 +229,8 @@ def settle_launch_shapes(b, limit: int = 16) -> int:
     def pending() -> bool:
         if launch_shape("color", b.tw, b.th) is None:
             return True
+        if b.wl.optics is not None and launch_shape("optics", b.W, b.H) is None:
+            return True
         cap = b.wl.capture
         return cap is not None and launch_shape("rl_mask", b.W, b.H, cap.radius) is None
 
@@ -242,7 +244,7 @@ def settle_launch_shapes(b, limit: int = 16) -> int:
 def rl_shape_record(W: int, H: int, radius: float, tw: int, th: int) -> dict | None:
     """Launch shapes the warm-up develops picked by timing, beside the heuristics' defaults: row
     segments per strip of the RL iteration and of the RL guide / mask kernel, CTAs per SM of the
-    colour kernel."""
+    colour kernel, rows of the optics gather's tiles."""
     from rohditor_gb300 import launch_shape, rl_launch_shape
 
     out = {}
@@ -250,7 +252,7 @@ def rl_shape_record(W: int, H: int, radius: float, tw: int, th: int) -> dict | N
     if s is not None:
         out["rl_iteration"] = {"segments": s.segments, "default_segments": s.default_segments,
                                "tuned_ms": round(s.best_ms, 4), "default_ms": round(s.default_ms, 4)}
-    for stage, (w, h) in (("rl_mask", (W, H)), ("color", (tw, th))):
+    for stage, (w, h) in (("rl_mask", (W, H)), ("color", (tw, th)), ("optics", (W, H))):
         t = launch_shape(stage, w, h, radius)
         if t is not None:
             out[stage] = {"value": t.segments, "default": t.default_segments, "tuned_ms": round(t.best_ms, 4),

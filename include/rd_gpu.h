@@ -316,12 +316,13 @@ rd_status rd_rl_launch_shape(uint32_t width, uint32_t height, float radius, int3
                              int32_t* default_segments, float* best_ms, float* default_ms);
 /* Launch shapes tuned across calls (no reference counterpart): the RL guide /
  * mask kernel's row segments per strip (stage RD_SHAPE_RL_MASK, `radius` the
- * capture radius) and the colour kernel's CTAs per SM (RD_SHAPE_COLOR,
- * `radius` ignored). The first calls for an image shape each launch one
+ * capture radius), the colour kernel's CTAs per SM (RD_SHAPE_COLOR, `radius`
+ * ignored) and the rows of the optics gather's 32-column tiles
+ * (RD_SHAPE_OPTICS, `radius` ignored). The first calls for an image shape each launch one
  * candidate, timed; once every candidate has been timed twice the fastest is
  * used for that shape by every context of the process. Results never depend
  * on the shape. RD_UNSUPPORTED until the shape is tuned. */
-enum { RD_SHAPE_RL_MASK = 0, RD_SHAPE_COLOR = 1 };
+enum { RD_SHAPE_RL_MASK = 0, RD_SHAPE_COLOR = 1, RD_SHAPE_OPTICS = 2 };
 rd_status rd_launch_shape(int32_t stage, uint32_t width, uint32_t height, float radius, int32_t* value,
                           int32_t* default_value, float* best_ms, float* default_ms);
 

@@ -2058,7 +2058,8 @@ extern "C" rd_status rd_rl_launch_shape(uint32_t width, uint32_t height, float r
 
 extern "C" rd_status rd_launch_shape(int32_t stage, uint32_t width, uint32_t height, float radius, int32_t* value,
                                      int32_t* default_value, float* best_ms, float* default_ms) {
-  if (!value || (stage != RD_SHAPE_RL_MASK && stage != RD_SHAPE_COLOR)) return RD_INVALID_INPUT;
+  if (!value || (stage != RD_SHAPE_RL_MASK && stage != RD_SHAPE_COLOR && stage != RD_SHAPE_OPTICS))
+    return RD_INVALID_INPUT;
   int c = 0;
   if (stage == RD_SHAPE_RL_MASK) {
     float w[rd::MAX_TAPS];
@@ -2066,7 +2067,8 @@ extern "C" rd_status rd_launch_shape(int32_t stage, uint32_t width, uint32_t hei
     if (taps < 0) return RD_INVALID_INPUT;
     c = taps / 2;
   }
-  const rd::ShapeKey key{stage == RD_SHAPE_RL_MASK ? rd::TUNE_RL_PREP : rd::TUNE_COLOR, (int)width, (int)height, c};
+  const int kernel = stage == RD_SHAPE_RL_MASK ? rd::TUNE_RL_PREP : stage == RD_SHAPE_COLOR ? rd::TUNE_COLOR : rd::TUNE_OPTICS;
+  const rd::ShapeKey key{kernel, (int)width, (int)height, c};
   int v = 0, d = 0;
   float b = 0.0f, dm = 0.0f;
   if (!rd::shape_record(key, &v, &d, &b, &dm)) return RD_UNSUPPORTED;

@@ -226,9 +226,9 @@ __device__ __forceinline__ bool cubic_sample(const float* __restrict__ plane, co
 }
 
 template <bool VIG>
-__global__ void __launch_bounds__(256) optics_kernel(const OpticsParams p) {
+__global__ void __launch_bounds__(512) optics_kernel(const OpticsParams p) {
   const int x = blockIdx.x * 32 + (threadIdx.x & 31);
-  const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
+  const int y = blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (x >= p.W || y >= p.H) return;
   float gx, gy;
   const float ix = p.ix[x], iy = p.iy[y];
@@ -307,10 +307,10 @@ __global__ void hypot_check_kernel(unsigned first, unsigned last, unsigned long 
 // channel. `knots` holds [m_r, m_g, m_b, pin] per knot; it is 16 KB and stays
 // in L1.
 template <bool VIG>
-__global__ void __launch_bounds__(256) optics_lut_kernel(const OpticsParams p, const float4* __restrict__ knots,
+__global__ void __launch_bounds__(512) optics_lut_kernel(const OpticsParams p, const float4* __restrict__ knots,
                                                          float step) {
   const int x = blockIdx.x * 32 + (threadIdx.x & 31);
-  const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
+  const int y = blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (x >= p.W || y >= p.H) return;
   const float ix = p.ix[x], iy = p.iy[y];
   const float radius = hypot_f32(ix, iy);
@@ -535,17 +535,24 @@ Status run_optics_gather(Context& ctx, const rd_optics_desc& o, const float* rgb
   split(o.center_x, p.fast.cxh, p.fast.cxl);
   split(o.center_y, p.fast.cyh, p.fast.cyl);
   split(o.norm_unscale, p.fast.uh, p.fast.ul);
-  dim3 grid((W + 31) / 32, (H + 7) / 8);
+  // Tiles of 32 columns and `rows` rows (one warp per row), tuned across
+  // calls per image shape: the tile only decides which CTA takes which pixel.
+  const ShapeKey key{TUNE_OPTICS, W, H, 0};
+  const ShapePick pick = shape_begin(ctx, key, 8, {4, 16});
+  const int rows = pick.value;
+  const dim3 grid((W + 31) / 32, (H + rows - 1) / rows);
+  const unsigned block = 32u * (unsigned)rows;
   const float4* knots = reinterpret_cast<const float4*>(dbuf);
   if (lut && p.mult) {
-    RD_LAUNCH(ctx, K_OPTICS, optics_lut_kernel<true><<<grid, 256, 0, ctx.stream>>>(p, knots, radial.step));
+    RD_LAUNCH(ctx, K_OPTICS, optics_lut_kernel<true><<<grid, block, 0, ctx.stream>>>(p, knots, radial.step));
   } else if (lut) {
-    RD_LAUNCH(ctx, K_OPTICS, optics_lut_kernel<false><<<grid, 256, 0, ctx.stream>>>(p, knots, radial.step));
+    RD_LAUNCH(ctx, K_OPTICS, optics_lut_kernel<false><<<grid, block, 0, ctx.stream>>>(p, knots, radial.step));
   } else if (p.mult) {
-    RD_LAUNCH(ctx, K_OPTICS, optics_kernel<true><<<grid, 256, 0, ctx.stream>>>(p));
+    RD_LAUNCH(ctx, K_OPTICS, optics_kernel<true><<<grid, block, 0, ctx.stream>>>(p));
   } else {
-    RD_LAUNCH(ctx, K_OPTICS, optics_kernel<false><<<grid, 256, 0, ctx.stream>>>(p));
+    RD_LAUNCH(ctx, K_OPTICS, optics_kernel<false><<<grid, block, 0, ctx.stream>>>(p));
   }
+  shape_end(ctx, key, pick);
   const cudaError_t launch = cudaGetLastError();
   device_free(ctx, dbuf, bytes);
   if (launch != cudaSuccess) return Status{RD_SYNCHRONIZATION, cudaGetErrorString(launch)};

@@ -49,7 +49,7 @@ const char* kernel_family_name(int family);
 
 // Keys of the cross-call launch-shape tuner (see shape_begin below): the
 // kernel and three shape parameters (width, height, radius or 0).
-enum TunedKernel { TUNE_RL_PREP = 0, TUNE_COLOR = 1, TUNE_KERNEL_COUNT };
+enum TunedKernel { TUNE_RL_PREP = 0, TUNE_COLOR = 1, TUNE_OPTICS = 2, TUNE_KERNEL_COUNT };
 struct ShapeKey {
   int kernel, a, b, c;
   bool operator<(const ShapeKey& o) const {

@@ -310,11 +310,12 @@ def rl_launch_shape(width: int, height: int, radius: float) -> RlLaunchShape | N
 
 def launch_shape(stage: str, width: int, height: int, radius: float = 0.0) -> RlLaunchShape | None:
     """rd_launch_shape: the launch shape tuned across calls for `stage` ("rl_mask": row segments of the
-    capture guide / mask kernel; "color": CTAs per SM of the colour kernel) at this image size, or None
-    while it is still being tuned."""
+    capture guide / mask kernel; "color": CTAs per SM of the colour kernel; "optics": rows of the optics
+    gather's 32-column tiles) at this image size, or None while it is still being tuned."""
     value, dflt = ctypes.c_int32(), ctypes.c_int32()
     best, dms = ctypes.c_float(), ctypes.c_float()
-    code = _ffi.load().rd_launch_shape({"rl_mask": 0, "color": 1}[stage], width, height, radius, ctypes.byref(value),
+    code = _ffi.load().rd_launch_shape({"rl_mask": 0, "color": 1, "optics": 2}[stage], width, height, radius,
+                                      ctypes.byref(value),
                                       ctypes.byref(dflt), ctypes.byref(best), ctypes.byref(dms))
     if code == _ffi.STATUS_NAMES.index("Unsupported"):
         return None

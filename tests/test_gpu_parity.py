@@ -231,10 +231,11 @@ def test_capture_launch_shape_tuning_keeps_results(stages, oracle):
 
 
 def test_cross_call_shape_tuning_keeps_results(stages, oracle):
-    """The guide / mask kernel's row segments and the colour kernel's grid are
-    tuned across calls: the first calls of an image shape each launch one
-    candidate, timed, until every candidate has two timings. Every call's
-    result equals the oracle bit for bit, and the shape is then reported."""
+    """The guide / mask kernel's row segments, the colour kernel's grid and
+    the optics gather's tile rows are tuned across calls: the first calls of
+    an image shape each launch one candidate, timed, until every candidate has
+    two timings. Every call's result equals the oracle (or the first call)
+    bit for bit, and the shape is then reported."""
     from rohditor_gb300 import CaptureContract, ColorContract, launch_shape, standard_base_lut
 
     w, h = 1532, 1020
@@ -252,6 +253,17 @@ def test_cross_call_shape_tuning_keeps_results(stages, oracle):
     for out, hist, _ in outs[1:]:
         assert np.array_equal(out, outs[0][0]) and np.array_equal(hist, outs[0][1])
     assert launch_shape("color", 900, 700) is not None
+    from rohditor_gb300 import OpticsExecution
+
+    ow, oh = 523, 391  # a size no other test remaps
+    orgb = smooth_rgb(ow, oh, seed=45)
+    ex = OpticsExecution(ow, oh, distortion="poly5", distortion_k=(-0.02, 0.005, 0.0), tca="linear",
+                         tca_red=(1.0003, 0, 0), tca_blue=(0.9997, 0, 0), vignetting_k=(-0.3, 0.05, -0.01))
+    oref = oracle.optics_apply(oracle.optics_desc_from(ex.to_c()), orgb)
+    assert launch_shape("optics", ow, oh) is None
+    for _ in range(8):
+        assert np.array_equal(stages.optics(orgb, ex).view(np.uint32), oref.view(np.uint32))
+    assert launch_shape("optics", ow, oh) is not None
 
 
 def smooth_rgb(w, h, seed):
