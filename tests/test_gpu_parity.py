@@ -754,3 +754,44 @@ def test_batched_develop_matches_one_at_a_time(device, mode):
         src.release()
         assert np.array_equal(srgb, ref)
         assert np.array_equal(hist[:256], ref_hist.red) and np.array_equal(hist[768:], ref_hist.luminance)
+
+
+@pytest.mark.parametrize("mode", ["lanes", "graph", "flat", "flat_graph"])
+def test_batched_develop_reports_an_invalid_image_and_recovers(device, mode):
+    """A batch holding an image the develop refuses (its crop lies outside the
+    sensor) fails with that status in every batched form, including the
+    captured ones, whose graph is then abandoned; the next batch of valid
+    images runs and equals the per-image path."""
+    from rohditor_gb300 import (CaptureContract, ColorContract, GpuPreviewError, GpuPreviewProcessor,
+                                GpuSensorProcessor, GpuSpatialProcessor, OpticsExecution, SensorDescription,
+                                clip_levels)
+    from rohditor_gb300.batch import BatchImage, develop_batch
+    from rohditor_gb300.workloads import CAMERA_TO_REC2020, preview_dimensions
+
+    def image(k, crop=None):
+        w, h = 512, 320
+        wb = (2.0, 1.0, 1.6)
+        sensor = SensorDescription(w, h, cfa="RGGB", crop=crop, black=(256.0,), white=(4095.0,), highlight="clip",
+                                   clip_levels=clip_levels(1.0, wb), demosaic="amaze", demosaic_balance=wb)
+        cap = CaptureContract(amount=0.5, radius=0.7, noise_protection=0.5, ceilings=clip_levels(1.0, wb),
+                              iterations=3)
+        return BatchImage(raw_mosaic(w, h, w, seed=110 + k), sensor, cap, OpticsExecution(w, h),
+                          preview_dimensions(w, h, 256), wb, CAMERA_TO_REC2020,
+                          ColorContract(wb_gains=wb, camera_to_rec2020=CAMERA_TO_REC2020))
+
+    graph, flat = mode in ("graph", "flat_graph"), mode.startswith("flat")
+    bad = [image(0), image(1, crop=(400, 0, 200, 320)), image(2)]
+    with pytest.raises(GpuPreviewError) as err:
+        develop_batch(bad, lanes=2, graph=graph, flat=flat)
+    assert err.value.variant == "InvalidInput", str(err.value)
+    good = [image(3), image(4)]
+    outs = develop_batch(good, lanes=2, graph=graph, flat=flat)[0]
+    for im, (srgb, hist) in zip(good, outs):
+        src = GpuSensorProcessor(device).develop(im.mosaic, im.sensor, im.capture)
+        base = GpuSpatialProcessor(device).reduce_preview(src, im.optics, im.target, im.wb_gains,
+                                                          im.camera_to_rec2020)
+        ref, ref_hist = GpuPreviewProcessor(device).render(base, im.color)
+        base.release()
+        src.release()
+        assert np.array_equal(srgb, ref)
+        assert np.array_equal(hist[:256], ref_hist.red)
