@@ -703,27 +703,30 @@ def test_batched_develop_matches_one_at_a_time(device, mode):
     highlight modes, capture radii and iteration counts equal the per-image
     path, bit for bit. The 702-wide image has no tensor maps (its rows are not
     a multiple of 16 bytes) and the 200x150 one is below the step kernel's
-    size, so both leave the flat RL launches of the others."""
+    size, so both leave the flat RL launches of the others; the last two
+    images are demosaiced with RCD and MHC, outside the flat AMaZE launch."""
     graph = mode in ("graph", "flat_graph")
     from rohditor_gb300 import (CaptureContract, ColorContract, GpuPreviewProcessor, GpuSensorProcessor,
                                 GpuSpatialProcessor, OpticsExecution, SensorDescription, clip_levels, opposed_levels)
     from rohditor_gb300.batch import BatchImage, develop_batch
     from rohditor_gb300.workloads import CAMERA_TO_REC2020, hsl_bands, preview_dimensions, sixteen_knot_curve
 
-    shapes = [(700, 467, "RGGB", "clip"), (1024, 768, "GBRG", "opposed"), (512, 384, "BGGR", "clip"),
-              (640, 480, "GRBG", "opposed"), (702, 300, "RGGB", "clip"), (200, 150, "GBRG", "clip")]
+    shapes = [(700, 467, "RGGB", "clip", "amaze"), (1024, 768, "GBRG", "opposed", "amaze"),
+              (512, 384, "BGGR", "clip", "amaze"), (640, 480, "GRBG", "opposed", "amaze"),
+              (702, 300, "RGGB", "clip", "amaze"), (200, 150, "GBRG", "clip", "amaze"),
+              (384, 256, "GRBG", "opposed", "rcd"), (320, 240, "BGGR", "clip", "mhc")]
     images = []
-    for k, (w, h, cfa, hl) in enumerate(shapes):
+    for k, (w, h, cfa, hl, dm) in enumerate(shapes):
         raw = raw_mosaic(w, h, w, seed=70 + k)
         wb = (2.0 - 0.1 * k, 1.0, 1.6 + 0.1 * k)
         if hl == "clip":
             sensor = SensorDescription(w, h, cfa=cfa, black=(256.0,), white=(4095.0,), highlight="clip",
-                                       clip_levels=clip_levels(1.0, wb), demosaic="amaze", demosaic_balance=wb)
+                                       clip_levels=clip_levels(1.0, wb), demosaic=dm, demosaic_balance=wb)
             ceil = clip_levels(1.0, wb)
         else:
             det, neutral = opposed_levels(1.0, wb)
             sensor = SensorDescription(w, h, cfa=cfa, black=(256.0,), white=(4095.0,), highlight="opposed",
-                                       detection_levels=det, neutral_ceiling=neutral, demosaic="amaze",
+                                       detection_levels=det, neutral_ceiling=neutral, demosaic=dm,
                                        demosaic_balance=wb)
             ceil = (1.0, 1.0, 1.0)
         cap = CaptureContract(amount=0.5, radius=0.7 if k % 2 == 0 else 1.1, noise_protection=0.5, ceilings=ceil,
