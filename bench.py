@@ -57,7 +57,7 @@ import workload_spec as spec  # noqa: E402
 
 METRIC = "24MP develops/s"
 UNIT = "develops/s"
-KERNEL_FAMILIES = 15  # RD_KERNEL_FAMILIES of include/rd_gpu.h
+KERNEL_FAMILIES = 16  # RD_KERNEL_FAMILIES of include/rd_gpu.h
 
 # Algorithmic FP32 operations per output pixel of AMaZE, counted on the bench
 # mosaic by the oracle's counting-float build (oracle/flops/census.py), and the
@@ -785,12 +785,79 @@ def export_output(args, reps: int = 5) -> dict:
         dev.check(lib.rd_copy_to_host(h, gamut.ctypes.data_as(ctypes.c_void_p), d_gamut, 40))
         out[name] = {"ms": round(per, 4), "algorithmic_gbs": round(gbs, 1), "hbm_frac": round(gbs / hbm_peak, 3),
                      "out_bytes_per_px": bpp, "gamut": [int(v) for v in gamut]}
+    png = png_files(dev, base, color, specs, d_out, d_gamut, W, H, reps)
     dev.check(lib.rd_device_free(h, d_out))
     dev.check(lib.rd_device_free(h, d_gamut))
     lib.rd_base_release(base)
     dev.check(lib.rd_device_free(h, ctypes.c_void_p(d_mosaic)))
     dev.close()
-    return {"image": f"{W}x{H}", "peak_gbs": hbm_peak, "outputs": out}
+    return {"image": f"{W}x{H}", "peak_gbs": hbm_peak, "outputs": out, "png": png}
+
+
+def png_files(dev, base, color, specs, d_out, d_gamut, W: int, H: int, reps: int) -> dict:
+    """PNG files of the 8-bit and 16-bit outputs (export::encode's PNG arms).
+    Resident: rd_encode_png_device from the output rows in HBM to a file in
+    HBM, device time of the encoder's four kernels per file, L2 flushed before
+    each. End to end: rd_encode_png from host rows to host bytes (wall clock,
+    upload and readback included). CPU: the oracle's filter selection plus
+    zlib level 6 on one core over the same 8-bit rows (one pass)."""
+    from rohditor_gb300 import PngEncoder
+
+    lib, h = dev.lib, dev.handle
+    enc = PngEncoder(dev)
+    result = {}
+    for name, depth in (("srgb8_clip", 8), ("srgb16_compress_dither", 16)):
+        oc = specs[name].to_c()
+        dev.check(lib.rd_render_output_device(h, base, ctypes.byref(color), ctypes.byref(oc), d_out, None, d_gamut,
+                                              None))
+        cap = int(lib.rd_png_bound(W, H, depth, 0, 0))
+        d_png, d_size = ctypes.c_void_p(), ctypes.c_void_p()
+        dev.check(lib.rd_device_alloc(h, cap, ctypes.byref(d_png)))
+        dev.check(lib.rd_device_alloc(h, 16, ctypes.byref(d_size)))
+
+        def encode():
+            dev.check(lib.rd_encode_png_device(h, d_out, W, H, 3 * W, depth, None, 0, None, 0, d_png, cap, d_size))
+
+        encode()
+        dev.synchronize()
+        lib.rd_ctx_reset_kernel_timing(h)
+        lib.rd_ctx_enable_kernel_timing(h, 1)
+        for _ in range(reps):
+            dev.check(lib.rd_ctx_flush_l2(h))
+            encode()
+        dev.synchronize()
+        lib.rd_ctx_enable_kernel_timing(h, 0)
+        ms, launches = family_timing(lib, h, "png_encode")
+        per = ms / reps
+        size = np.zeros(1, dtype=np.uint64)
+        dev.check(lib.rd_copy_to_host(h, size.ctypes.data_as(ctypes.c_void_p), d_size, 8))
+        dtype = np.uint8 if depth == 8 else np.uint16
+        rows = np.empty((H, W, 3), dtype=dtype)
+        dev.check(lib.rd_copy_to_host(h, rows.ctypes.data_as(ctypes.c_void_p), d_out, rows.nbytes))
+        enc.encode(rows)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            data = enc.encode(rows)
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / reps
+        entry = {"ms": round(per, 4), "launches_per_file": launches // max(reps, 1),
+                 "mp_per_s": round(W * H / (per / 1e3) / 1e6, 1),
+                 "input_gbs": round(rows.nbytes / (per / 1e3) / 1e9, 1),
+                 "file_bytes": int(size[0]), "ratio": round(int(size[0]) / rows.nbytes, 4),
+                 "e2e_ms": round(e2e_ms, 3), "e2e_h2d_bytes": rows.nbytes, "e2e_d2h_bytes": len(data)}
+        if depth == 8:
+            import zlib
+
+            from oracle import oracle as orc
+
+            t0 = time.perf_counter()
+            z = zlib.compress(orc.png_filter(rows), 6)
+            entry["cpu_baseline"] = {"ms": round((time.perf_counter() - t0) * 1e3, 1), "cores": 1, "kind": "port",
+                                     "sample": "the whole 8-bit frame once: oracle filter selection + zlib level 6",
+                                     "idat_bytes": len(z)}
+        result[name] = entry
+        dev.check(lib.rd_device_free(h, d_png))
+        dev.check(lib.rd_device_free(h, d_size))
+    return result
 
 
 def export_stream(args, count: int = 24, window: int = 3, cap_gb: float = 60.0) -> dict:

@@ -33,6 +33,7 @@
  *                            crates/core/src/cpu/stages.rs:250-308,380-528,1028-1094;
  *                            crates/core/src/analysis/histogram.rs:92-128
  *     rd_stage_output        apply_adjustments_with_local + the output conversions above
+ *   rd_encode_png            export::encode, PNG arms     crates/core/src/export.rs:155-219
  */
 #ifndef RD_GPU_H
 #define RD_GPU_H
@@ -288,6 +289,31 @@ rd_status rd_render_output(rd_ctx* ctx, const rd_base* base, const rd_color_desc
 rd_status rd_render_output_device(rd_ctx* ctx, const rd_base* base, const rd_color_desc* color,
                                   const rd_output_desc* output, void* d_out, uint64_t* d_hist, uint64_t* d_gamut,
                                   rd_metrics* metrics);
+/* ---- PNG encode: the PNG arms of export::encode (crates/core/src/export.rs:176-211),
+ * which hand tightly packed RGB rows, the output colour space's ICC profile and
+ * optional EXIF to the image crate's PngEncoder.
+ * Samples are 8-bit (bit_depth 8, u8 rows) or 16-bit (bit_depth 16, u16 rows in
+ * host byte order; the file stores them most significant byte first). rgb is
+ * interleaved [height][3*width]; row_stride is in samples and must equal
+ * 3*width, as the reference rejects padded rows (ExportError::InvalidImageLayout,
+ * export.rs:136-150): RD_INVALID_INPUT otherwise, and for another bit depth. icc
+ * (icc_len bytes) becomes an iCCP chunk and exif an eXIf chunk; either may be
+ * NULL with length 0. Decoding the file gives back exactly the input samples.
+ * rd_png_bound: the largest file for these sizes (0 for invalid arguments). */
+uint64_t rd_png_bound(uint32_t width, uint32_t height, int32_t bit_depth, uint64_t icc_len, uint64_t exif_len);
+/* Host rows in, host file out: png receives *png_bytes bytes. When capacity is
+ * smaller than the file, RD_INVALID_DIMENSIONS with *png_bytes set to its size.
+ * metrics->total_ms: device time of the encode (copies excluded). */
+rd_status rd_encode_png(rd_ctx* ctx, const void* rgb, uint32_t width, uint32_t height, uint64_t row_stride,
+                        int32_t bit_depth, const uint8_t* icc, uint64_t icc_len, const uint8_t* exif,
+                        uint64_t exif_len, uint8_t* png, uint64_t capacity, uint64_t* png_bytes,
+                        rd_metrics* metrics);
+/* Device rows in, device file out, ordered on the context's stream: d_png (4-byte
+ * aligned, capacity >= rd_png_bound) receives the file and *d_png_bytes (device
+ * u64) its size. */
+rd_status rd_encode_png_device(rd_ctx* ctx, const void* d_rgb, uint32_t width, uint32_t height, uint64_t row_stride,
+                               int32_t bit_depth, const uint8_t* icc, uint64_t icc_len, const uint8_t* exif,
+                               uint64_t exif_len, uint8_t* d_png, uint64_t capacity, uint64_t* d_png_bytes);
 /* Self-check of the correctly rounded arithmetic on the device, for test
  * suites (no reference counterpart). which = 0: the number of positive finite
  * f32 whose cube root is not correctly rounded (or not odd-symmetric), exact
@@ -529,7 +555,7 @@ rd_status rd_ctx_flush_l2(rd_ctx* ctx);
  * bracketed by CUDA events; totals are resolved at each call's final sync. */
 rd_status rd_ctx_enable_kernel_timing(rd_ctx* ctx, int enable);
 /* family: index 0..RD_KERNEL_FAMILIES-1; returns its name, total ms and launch count. */
-#define RD_KERNEL_FAMILIES 15
+#define RD_KERNEL_FAMILIES 16
 rd_status rd_ctx_kernel_timing(const rd_ctx* ctx, int family, const char** name, double* total_ms,
                                uint64_t* launches);
 rd_status rd_ctx_reset_kernel_timing(rd_ctx* ctx);

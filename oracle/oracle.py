@@ -143,6 +143,8 @@ def load():
             "ro_oklab_inverse": (None, [ctypes.c_int, F32P, F32P]),
             "ro_render_output": (ctypes.c_int, [F32P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(OutputDesc),
                                                 ctypes.c_void_p, U64P]),
+            "ro_png_filter": (None, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, U8P]),
+            "ro_png_unfilter": (ctypes.c_int, [U8P, ctypes.c_int, ctypes.c_int, ctypes.c_int, U8P]),
         }
         for name, (res, args) in list(sig.items()) + list(optional.items()):
             if not hasattr(lib, name):
@@ -567,3 +569,28 @@ def oklab(rgb, primaries="srgb", inverse=False) -> np.ndarray:
     fn = load().ro_oklab_inverse if inverse else load().ro_oklab
     fn(1 if primaries == "display_p3" else 0, ptr(v), ptr(out))
     return out
+
+
+def png_filter(image: np.ndarray) -> bytes:
+    """Filtered PNG scanlines (filter byte + bytes per line) of RGB rows [h][w][3], u8 or u16."""
+    image = np.ascontiguousarray(image)
+    depth = 16 if image.dtype == np.uint16 else 8
+    h, w = image.shape[:2]
+    stream = np.zeros(h * (1 + w * 3 * depth // 8), dtype=np.uint8)
+    load().ro_png_filter(image.ctypes.data_as(ctypes.c_void_p), w, h, depth, ptr(stream, ctypes.c_uint8))
+    return stream.tobytes()
+
+
+def png_unfilter(stream: bytes, width: int, height: int, depth: int) -> np.ndarray:
+    """Samples [h][w][3] (u8, or u16 from the file's big-endian bytes) of a filtered stream."""
+    line = 1 + width * 3 * depth // 8
+    if len(stream) != height * line:
+        raise ValueError(f"stream holds {len(stream)} bytes, expected {height * line}")
+    src = np.frombuffer(stream, dtype=np.uint8).copy()
+    out = np.zeros(height * (line - 1), dtype=np.uint8)
+    if load().ro_png_unfilter(ptr(src, ctypes.c_uint8), width, height, depth, ptr(out, ctypes.c_uint8)) != 0:
+        raise ValueError("unknown PNG filter type")
+    if depth == 16:
+        return out.view(">u2").astype(np.uint16).reshape(height, width, 3)
+    return out.reshape(height, width, 3)
+

@@ -149,6 +149,15 @@ typedef struct ro_synth {
 /* out: [height][width] u16. Returns 0, or -1 below 2x2. */
 int ro_synth_mosaic(const ro_synth* desc, uint16_t* out);
 
+/* ---- PNG scanlines (encode.cpp) ----
+ * ro_png_filter: image is interleaved RGB [h][3w], u8 (depth 8) or u16 in host
+ * byte order (depth 16); stream receives h scanlines of 1 + w*3*depth/8 bytes
+ * (filter type, filtered bytes). ro_png_unfilter inverts a stream into the
+ * file's sample bytes (16-bit most significant byte first); -1 for a filter
+ * type above 4. */
+void ro_png_filter(const uint8_t* image, int w, int h, int depth, uint8_t* stream);
+int ro_png_unfilter(const uint8_t* stream, int w, int h, int depth, uint8_t* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -4,12 +4,12 @@ reference's `rohditor-gpu` processor interface."""
 
 from .processor import (CaptureContract, capture_ceilings, ColorContract, Device, GamutDiagnostics, GpuBase, GpuDevelopedSource,
                         GpuPreviewError, GpuPreviewProcessor, GpuSensorProcessor, GpuSpatialProcessor, Histogram, launch_shape,
-                        OpticsExecution, OutputSpec, RlLaunchShape, SensorDescription, Stages, clip_levels,
+                        OpticsExecution, OutputSpec, PngEncoder, RlLaunchShape, SensorDescription, Stages, clip_levels,
                         light_tone_lut, opposed_levels, rl_launch_shape, standard_base_lut)
 
 __all__ = [
     "CaptureContract", "capture_ceilings", "ColorContract", "Device", "GamutDiagnostics", "GpuBase", "GpuDevelopedSource", "GpuPreviewError",
     "GpuPreviewProcessor", "GpuSensorProcessor", "GpuSpatialProcessor", "Histogram", "launch_shape", "OpticsExecution",
-    "OutputSpec", "RlLaunchShape", "SensorDescription", "Stages", "clip_levels", "light_tone_lut", "opposed_levels", "rl_launch_shape",
+    "OutputSpec", "PngEncoder", "RlLaunchShape", "SensorDescription", "Stages", "clip_levels", "light_tone_lut", "opposed_levels", "rl_launch_shape",
     "standard_base_lut",
 ]

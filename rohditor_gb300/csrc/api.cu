@@ -54,7 +54,7 @@ const char* kernel_family_name(int family) {
   static const char* names[K_FAMILY_COUNT] = {
       "normalize", "opposed", "mhc_bilinear", "rcd", "amaze", "rl_mask", "rl_iteration",
       "rl_apply", "vignetting", "optics_gather", "area_reduce", "wb_matrix",
-      "color_output", "synth", "display_output"};
+      "color_output", "synth", "display_output", "png_encode"};
   return family >= 0 && family < K_FAMILY_COUNT ? names[family] : "unknown";
 }
 
@@ -928,6 +928,101 @@ rd_status rd_render_output(rd_ctx* h, const rd_base* base, const rd_color_desc* 
     metrics->total_ms = ms;
     metrics->kernel_launches = h->c.launches;
   }
+  return finish(h, st);
+}
+
+// ---- PNG encode ----------------------------------------------------------
+static Status png_args(const void* rgb, uint32_t width, uint32_t height, uint64_t row_stride, int32_t bit_depth,
+                       const uint8_t* icc, uint64_t icc_len, const uint8_t* exif, uint64_t exif_len) {
+  if (!rgb || (icc_len && !icc) || (exif_len && !exif)) return Status{RD_INVALID_INPUT, "null argument"};
+  if (bit_depth != 8 && bit_depth != 16) return Status{RD_INVALID_INPUT, "PNG samples are 8 or 16 bits"};
+  if (width == 0 || height == 0 || width > (uint32_t)INT32_MAX || height > (uint32_t)INT32_MAX)
+    return Status{RD_INVALID_DIMENSIONS, "PNG dimensions out of range"};
+  // ExportError::InvalidImageLayout (crates/core/src/export.rs:136-150).
+  if (row_stride != 3ull * width)
+    return Status{RD_INVALID_INPUT, "encoders require tightly packed RGB rows"};
+  if (bit_depth == 16 && reinterpret_cast<uintptr_t>(rgb) % 2)
+    return Status{RD_INVALID_INPUT, "16-bit rows must be 2-byte aligned"};
+  return Status{};
+}
+
+uint64_t rd_png_bound(uint32_t width, uint32_t height, int32_t bit_depth, uint64_t icc_len, uint64_t exif_len) {
+  if ((bit_depth != 8 && bit_depth != 16) || width == 0 || height == 0 || width > (uint32_t)INT32_MAX ||
+      height > (uint32_t)INT32_MAX)
+    return 0;
+  // The header's size depends only on the metadata lengths.
+  const std::vector<uint8_t> icc(icc_len), exif(exif_len);
+  std::vector<uint8_t> header;
+  if (!rd::png_header((int)width, (int)height, bit_depth, icc.data(), icc_len, exif.data(), exif_len, &header).ok())
+    return 0;
+  return rd::png_bound((int)width, (int)height, bit_depth, header.size());
+}
+
+rd_status rd_encode_png_device(rd_ctx* h, const void* d_rgb, uint32_t width, uint32_t height, uint64_t row_stride,
+                               int32_t bit_depth, const uint8_t* icc, uint64_t icc_len, const uint8_t* exif,
+                               uint64_t exif_len, uint8_t* d_png, uint64_t capacity, uint64_t* d_png_bytes) {
+  if (!h || !d_png || !d_png_bytes) return finish(h, Status{RD_INVALID_INPUT, "null argument"});
+  Status st = png_args(d_rgb, width, height, row_stride, bit_depth, icc, icc_len, exif, exif_len);
+  if (st.ok() && (reinterpret_cast<uintptr_t>(d_png) % 4 || reinterpret_cast<uintptr_t>(d_png_bytes) % 8))
+    st = Status{RD_INVALID_INPUT, "the PNG buffer must be 4-byte aligned and its byte count 8-byte aligned"};
+  if (!st.ok()) return finish(h, st);
+  rd::Context& ctx = h->c;
+  cudaSetDevice(ctx.device);
+  std::vector<uint8_t> header;
+  st = rd::png_header((int)width, (int)height, bit_depth, icc, icc_len, exif, exif_len, &header);
+  if (st.ok() && capacity < rd::png_bound((int)width, (int)height, bit_depth, header.size()))
+    st = Status{RD_INVALID_DIMENSIONS, "the PNG buffer is smaller than rd_png_bound"};
+  if (st.ok()) st = rd::run_png_encode(ctx, d_rgb, (int)width, (int)height, bit_depth, header, d_png, d_png_bytes);
+  if (st.ok()) st = rd::check_kernel_error(ctx, "png encode");
+  return finish(h, st);
+}
+
+rd_status rd_encode_png(rd_ctx* h, const void* rgb, uint32_t width, uint32_t height, uint64_t row_stride,
+                        int32_t bit_depth, const uint8_t* icc, uint64_t icc_len, const uint8_t* exif,
+                        uint64_t exif_len, uint8_t* png, uint64_t capacity, uint64_t* png_bytes,
+                        rd_metrics* metrics) {
+  if (!h || !png || !png_bytes) return finish(h, Status{RD_INVALID_INPUT, "null argument"});
+  Status st = png_args(rgb, width, height, row_stride, bit_depth, icc, icc_len, exif, exif_len);
+  if (!st.ok()) return finish(h, st);
+  rd::Context& ctx = h->c;
+  cudaSetDevice(ctx.device);
+  std::vector<uint8_t> header;
+  st = rd::png_header((int)width, (int)height, bit_depth, icc, icc_len, exif, exif_len, &header);
+  if (!st.ok()) return finish(h, st);
+  const uint64_t in_bytes = 3ull * width * height * (uint64_t)(bit_depth / 8);
+  const uint64_t in_room = (in_bytes + 255) & ~255ull;
+  const uint64_t bound = rd::png_bound((int)width, (int)height, bit_depth, header.size());
+  const uint64_t total = in_room + ((bound + 255) & ~255ull) + 16;
+  void* p = nullptr;
+  st = rd::device_alloc(ctx, total, &p);
+  if (!st.ok()) return finish(h, st);
+  uint8_t* d_in = static_cast<uint8_t*>(p);
+  uint8_t* d_png = d_in + in_room;
+  uint64_t* d_size = reinterpret_cast<uint64_t*>(d_png + ((bound + 255) & ~255ull));
+  Timer tm(ctx);
+  if (cudaMemcpyAsync(d_in, rgb, in_bytes, cudaMemcpyHostToDevice, ctx.stream) != cudaSuccess)
+    st = Status{RD_SYNCHRONIZATION, "image upload failed"};
+  tm.mark();
+  if (st.ok()) st = rd::run_png_encode(ctx, d_in, (int)width, (int)height, bit_depth, header, d_png, d_size);
+  tm.mark();
+  uint64_t size = 0;
+  if (st.ok() && (cudaMemcpyAsync(&size, d_size, sizeof(size), cudaMemcpyDeviceToHost, ctx.stream) != cudaSuccess ||
+                  cudaStreamSynchronize(ctx.stream) != cudaSuccess))
+    st = Status{RD_READBACK, "PNG size readback failed"};
+  if (st.ok()) st = rd::check_kernel_error(ctx, "png encode");
+  if (st.ok()) {
+    *png_bytes = size;
+    if (size > capacity) st = Status{RD_INVALID_DIMENSIONS, "the PNG buffer is smaller than the file"};
+  }
+  if (st.ok() && (cudaMemcpyAsync(png, d_png, size, cudaMemcpyDeviceToHost, ctx.stream) != cudaSuccess ||
+                  cudaStreamSynchronize(ctx.stream) != cudaSuccess))
+    st = Status{RD_READBACK, "PNG readback failed"};
+  if (st.ok() && metrics) {
+    std::memset(metrics, 0, sizeof(*metrics));
+    metrics->total_ms = tm.span(0, 1);
+    metrics->kernel_launches = ctx.launches;
+  }
+  rd::device_free(ctx, p, total);
   return finish(h, st);
 }
 

@@ -42,7 +42,7 @@ struct Status {
 // Kernel families timed by the optional per-launch event bracketing.
 enum KernelFamily {
   K_NORMALIZE, K_OPPOSED, K_MHC, K_RCD, K_AMAZE, K_RL_MASK, K_RL_ITER, K_RL_APPLY, K_VIGNETTE,
-  K_OPTICS, K_AREA, K_WB_MATRIX, K_COLOR, K_SYNTH, K_OUTPUT, K_FAMILY_COUNT
+  K_OPTICS, K_AREA, K_WB_MATRIX, K_COLOR, K_SYNTH, K_OUTPUT, K_ENCODE, K_FAMILY_COUNT
 };
 static_assert(K_FAMILY_COUNT == RD_KERNEL_FAMILIES, "family table size");
 const char* kernel_family_name(int family);
@@ -322,6 +322,18 @@ Status run_wb_matrix(Context& ctx, float* rgb, size_t pixels, const float gains[
 Status run_color_output(Context& ctx, const float* rgb, int width, int height, const rd_color_desc& color,
                         bool camera_native, uint8_t* srgb, unsigned long long* d_hist);
 Status run_synth(Context& ctx, const rd_synth_desc& desc, uint16_t* out);
+
+// PNG encoding (k_encode.cu) of interleaved RGB rows, 8 or 16 bits per sample.
+// png_header builds the signature, IHDR and the optional iCCP / eXIf chunks;
+// png_bound is the largest file the encoder writes after that header;
+// run_png_encode writes header + IDAT chunks + IEND into d_png and the file's
+// byte count into *d_png_bytes (device memory), on the context's stream.
+uint64_t png_stream_bytes(int W, int H, int depth);
+Status png_header(int W, int H, int depth, const uint8_t* icc, size_t icc_len, const uint8_t* exif, size_t exif_len,
+                  std::vector<uint8_t>* out);
+uint64_t png_bound(int W, int H, int depth, uint64_t header_bytes);
+Status run_png_encode(Context& ctx, const void* d_rgb, int W, int H, int depth, const std::vector<uint8_t>& header,
+                      uint8_t* d_png, uint64_t* d_png_bytes);
 // One launch rendering several bases (render path of the served loop). The
 // staging buffers (host pinned and device, color_batch_staging_bytes(n) each)
 // carry the per-image parameters and LUTs.

@@ -549,6 +549,46 @@ class GpuPreviewProcessor:
         self.device.check(self.device.lib.rd_render_device(self.device.handle, base.handle, ctypes.byref(color_c), None))
 
 
+class PngEncoder:
+    """The PNG arms of export::encode (crates/core/src/export.rs:155-219) on the device.
+
+    `encode` takes interleaved RGB rows ([h][w][3] or [h][3w]; uint8 or uint16)
+    and returns the file's bytes with the ICC profile in an iCCP chunk and EXIF
+    in an eXIf chunk. Like the reference (ExportError::InvalidImageLayout,
+    export.rs:136-150) it refuses rows that are not tightly packed: pass
+    `row_stride` (samples) to describe a padded [h][row_stride] array.
+    """
+
+    def __init__(self, device: Device):
+        self.device = device
+
+    @staticmethod
+    def bound(width: int, height: int, bit_depth: int, icc_len: int = 0, exif_len: int = 0) -> int:
+        return int(_ffi.load().rd_png_bound(width, height, bit_depth, icc_len, exif_len))
+
+    def encode(self, rgb: np.ndarray, icc_profile: bytes = b"", exif: bytes | None = None,
+               row_stride: int | None = None, width: int | None = None) -> bytes:
+        rgb = np.ascontiguousarray(rgb)
+        if rgb.dtype not in (np.uint8, np.uint16):
+            raise GpuPreviewError(8, f"PNG samples are uint8 or uint16, not {rgb.dtype}")
+        depth = 16 if rgb.dtype == np.uint16 else 8
+        height = rgb.shape[0]
+        if width is None:
+            width = rgb.shape[1] if rgb.ndim == 3 else rgb.shape[1] // 3
+        stride = 3 * width if row_stride is None else row_stride
+        icc = np.frombuffer(icc_profile, dtype=np.uint8) if icc_profile else None
+        ex = np.frombuffer(exif, dtype=np.uint8) if exif else None
+        capacity = self.bound(width, height, depth, len(icc_profile or b""), len(exif or b""))
+        out = np.empty(max(capacity, 1), dtype=np.uint8)
+        size = ctypes.c_uint64(0)
+        self.device.check(self.device.lib.rd_encode_png(
+            self.device.handle, rgb.ctypes.data_as(ctypes.c_void_p), width, height, stride, depth,
+            _ptr(icc, ctypes.c_uint8) if icc is not None else None, len(icc_profile or b""),
+            _ptr(ex, ctypes.c_uint8) if ex is not None else None, len(exif or b""),
+            _ptr(out, ctypes.c_uint8), out.nbytes, ctypes.byref(size), None))
+        return out[:size.value].tobytes()
+
+
 # ---------------------------------------------------------------- stage API
 class Stages:
     """The crates' stage functions, each run on the device with host buffers."""
