@@ -223,12 +223,13 @@ rd_status rd_render_device(rd_ctx* ctx, rd_base* base, const rd_color_desc* colo
  * Returns after enqueueing; results are ready when `stream` completes. No
  * context, no device allocation: the three 4096-entry LUTs (48 KB, the only
  * scratch; LUT length is fixed by rd_color_desc, image size is not limited)
- * are staged in a static device array of this library. The first call on a
- * device resolves that array's address and may load the module there; make
- * it before any stream capture. Calls overlapping in time on one device
- * (any streams, any threads) share the array and race: serialise them.
- * RD_INVALID_INPUT for null pointers, zero or > INT32_MAX sizes or device
- * ordinals >= 64; RD_SYNCHRONIZATION when a CUDA call fails. */
+ * are staged in a static device array of this library, copied there from
+ * `color` on every call. The first call on a device resolves that array's
+ * address and may load the module there. Calls overlapping in time on one
+ * device (any streams, any threads) share the array and race: serialise them.
+ * RD_INVALID_INPUT for null pointers, zero or > INT32_MAX sizes, device
+ * ordinals >= 64, or a stream that is being captured into a CUDA graph (the
+ * call enqueues nothing then); RD_SYNCHRONIZATION when a CUDA call fails. */
 rd_status rd_render_device_noalloc(const float* d_base, uint32_t width, uint32_t height,
                                    const rd_color_desc* color, uint8_t* d_srgb_out, uint64_t* d_hist,
                                    void* stream);

@@ -301,10 +301,19 @@ extern "C" rd_status rd_render_device_noalloc(const float* d_base, uint32_t widt
     return RD_SYNCHRONIZATION;
   }
   if (device < 0 || device >= NOALLOC_MAX_DEVICES) return RD_INVALID_INPUT;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // The LUTs are copied from the caller's pageable descriptor on every call,
+  // which a stream being captured cannot record: such a call is refused
+  // before anything is enqueued.
+  cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &capture) != cudaSuccess) {
+    cudaGetLastError();
+    return RD_INVALID_INPUT;
+  }
+  if (capture != cudaStreamCaptureStatusNone) return RD_INVALID_INPUT;
   NoallocDevice dev;
   const rd_status setup = noalloc_device(device, &dev);
   if (setup != RD_OK) return setup;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
   const rd_color_desc& c = *color;
   ColorParams p{};
   p.in = d_base;

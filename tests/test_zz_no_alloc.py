@@ -83,3 +83,29 @@ def test_noalloc_render_rejects_bad_arguments(device):
     assert lib.rd_render_device_noalloc(None, 4, 4, ctypes.byref(desc), ptr, ptr, None) != 0
     assert lib.rd_render_device_noalloc(ptr, 0, 4, ctypes.byref(desc), ptr, ptr, None) != 0
     assert lib.rd_render_device_noalloc(ptr, 4, 4, None, ptr, ptr, None) != 0
+
+
+def test_noalloc_render_refuses_a_capturing_stream(device):
+    # The LUT copies come from the caller's descriptor on every call, which a
+    # graph cannot record: the call is refused and enqueues nothing.
+    torch = pytest.importorskip("torch")
+    lib = device.lib
+    from rohditor_gb300 import ColorContract
+
+    desc = ColorContract(wb_gains=(1.0, 1.0, 1.0), camera_to_rec2020=IDENTITY).to_c()
+    buf = torch.zeros(4096, dtype=torch.float32, device="cuda")
+    ptr = buf.data_ptr()
+    side = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(side):
+        graph.capture_begin()
+        rc = lib.rd_render_device_noalloc(ptr, 4, 4, ctypes.byref(desc), ptr, ptr, side.cuda_stream)
+        buf.add_(1.0)
+        graph.capture_end()
+    assert rc == 8  # RD_INVALID_INPUT
+    graph.replay()
+    torch.cuda.synchronize()
+    assert float(buf[0]) == 1.0
+    assert lib.rd_render_device_noalloc(ptr, 4, 4, ctypes.byref(desc), ptr, ptr, side.cuda_stream) == 0
+    torch.cuda.synchronize()
