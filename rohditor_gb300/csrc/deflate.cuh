@@ -35,12 +35,14 @@ constexpr int CLEN_SYMBOLS = 19;          // code-length alphabet
 constexpr int CLEN_MAX_BITS = 7;
 constexpr int MAX_RUN = 258;              // longest deflate match
 constexpr int HEADER_ITEMS = LIT_SYMBOLS + 2;  // code lengths sent: HLIT + HDIST (HDIST = 2)
+constexpr int HEADER_WORDS = 130;          // >= 3 + 14 + 19*3 + (286 + 2) * (7 + 7) header bits, in words
 constexpr uint32_t ADLER_MOD = 65521u;
 constexpr uint32_t CRC_POLY = 0xEDB88320u;  // CRC-32 of PNG / zlib, reflected
 
 static_assert(SEG_CAP % 16 == 0, "segment slots hold 16-byte vectors");
 static_assert(SEG + STORED_OVERHEAD <= SEG_CAP, "a stored segment fits its slot");
 static_assert(SEG <= 65535, "one stored block holds a segment");
+static_assert(32 * HEADER_WORDS >= 3 + 14 + 3 * CLEN_SYMBOLS + HEADER_ITEMS * (7 + 7), "header words");
 
 RD_HD int floor_log2(uint32_t v) {
 #if defined(__CUDA_ARCH__)
@@ -87,69 +89,135 @@ RD_HD int run_token(int p, int a, int b) {
   return 1;
 }
 
+RD_HD int clz64(uint64_t v) {
+#if defined(__CUDA_ARCH__)
+  return __clzll((long long)v);
+#else
+  return __builtin_clzll(v);
+#endif
+}
+RD_HD int ctz64(uint64_t v) {
+#if defined(__CUDA_ARCH__)
+  return __ffsll((long long)v) - 1;
+#else
+  return __builtin_ctzll(v);
+#endif
+}
+
+// A thread's share of a segment: CHUNK bytes at segment position c0, held in
+// 16 little-endian words (registers on the device when indexed by constants).
+constexpr int CHUNK = 32;  // below 64, so (1ull << count) - 1 is the mask of a full chunk
+constexpr int CHUNK_WORDS = CHUNK / 4;
+
+RD_HD uint32_t chunk_byte(const uint32_t* w, int j) { return (w[j >> 2] >> (8 * (j & 3))) & 0xFFu; }
+
+// Bit j set when byte j of the chunk differs from the byte before it (`prev`
+// for j = 0), and always for the first byte of a segment; bits at and above
+// `count` are clear. The set bits are where a run of repeated bytes cannot
+// continue: every token of the segment starts at one, or inside a run.
+RD_HD uint64_t chunk_breaks(const uint32_t* w, int count, uint32_t prev, bool segment_start) {
+  uint64_t m = 0;
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+  for (int j = 0; j < CHUNK; ++j) {
+    const uint32_t b = chunk_byte(w, j);
+    if (b != prev) m |= 1ull << j;
+    prev = b;
+  }
+  if (segment_start) m |= 1ull;
+  if (count < CHUNK) m &= (1ull << count) - 1ull;
+  return m;
+}
+
 // Calls visit(literal, 0) or visit(0, length) for each token that starts in
-// [c0, c1). `before` is the last position before c0 that differs from its
-// predecessor (position 0 always does) and `after` the first such position
-// at or after c1 (or the segment length).
+// the chunk's first `count` bytes. `before` is the segment position of the
+// last break before the chunk (position 0 always is one) and `after` the
+// first break at or after its end (or the segment length): together with the
+// chunk's own breaks they bound the run each repeated byte belongs to.
 template <class Visit>
-RD_HD void for_each_token(const uint8_t* in, int c0, int c1, int before, int after, Visit&& visit) {
-  int brk = before;
-  int run_end = -1;
-  for (int p = c0; p < c1; ++p) {
-    const uint8_t x = in[p];
-    if (p == 0 || x != in[p - 1]) {
-      brk = p;
-      visit((uint32_t)x, 0);
+RD_HD void chunk_tokens(const uint32_t* w, uint64_t breaks, int c0, int count, int before, int after,
+                        Visit&& visit) {
+  if (breaks == (1ull << count) - 1ull) {  // no byte repeats its predecessor: all literals
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+    for (int j = 0; j < CHUNK; ++j) {
+      if (j >= count) break;
+      visit(chunk_byte(w, j), 0);
+    }
+    return;
+  }
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+  for (int j = 0; j < CHUNK; ++j) {
+    if (j >= count) break;
+    const uint32_t x = chunk_byte(w, j);
+    if ((breaks >> j) & 1ull) {
+      visit(x, 0);
       continue;
     }
-    if (p >= run_end) {
-      int q = p + 1;
-      while (q < c1 && in[q] == in[q - 1]) ++q;
-      run_end = q < c1 ? q : after;
-    }
-    const int t = run_token(p, brk + 1, run_end);
+    const uint64_t upto = j == CHUNK - 1 ? ~0ull : (2ull << j) - 1ull;
+    const uint64_t below = breaks & upto;
+    const uint64_t above = breaks & ~upto;
+    const int a = (below ? c0 + 63 - clz64(below) : before) + 1;
+    const int b = above ? c0 + ctz64(above) : after;
+    const int t = run_token(c0 + j, a, b);
     if (t == 1)
-      visit((uint32_t)x, 0);
+      visit(x, 0);
     else if (t >= 3)
       visit(0u, t);
   }
 }
 
+// The low `len` (1..16) bits of code in reverse order.
 RD_HD uint32_t reverse_bits(uint32_t code, int len) {
+#if defined(__CUDA_ARCH__)
+  return __brev(code) >> (32 - len);
+#else
   uint32_t r = 0;
   for (int i = 0; i < len; ++i) {
     r = (r << 1) | (code & 1u);
     code >>= 1;
   }
   return r;
+#endif
+}
+
+// Huffman tree over n >= 2 leaf weights in ascending order: leaves and merged
+// nodes are taken from two queues (both stay sorted), which builds an optimal
+// tree in O(n). Nodes n..2n-2 are the merged ones, 2n-2 the root; parent[i]
+// is the node that absorbed node i. Scratch weight[2n].
+RD_HD void huffman_tree(const uint32_t* leaf, int n, uint32_t* weight, uint16_t* parent) {
+  for (int i = 0; i < n; ++i) weight[i] = leaf[i];
+  int next_leaf = 0, next_node = n, created = n;
+  for (int k = 0; k < n - 1; ++k) {
+    int pick[2];
+    for (int j = 0; j < 2; ++j) {
+      if (next_leaf < n && (next_node >= created || weight[next_leaf] <= weight[next_node]))
+        pick[j] = next_leaf++;
+      else
+        pick[j] = next_node++;
+    }
+    weight[created] = weight[pick[0]] + weight[pick[1]];
+    parent[pick[0]] = (uint16_t)created;
+    parent[pick[1]] = (uint16_t)created;
+    ++created;
+  }
 }
 
 // Huffman code lengths of n >= 2 symbols whose indices `order` lists by
-// ascending (frequency, symbol). Leaves and merged nodes are taken from two
-// queues (both stay sorted), which builds an optimal tree in O(n). When the
-// tree is deeper than `limit`, every frequency is halved (rounding up, so none
-// reaches zero and the order is kept) and the tree is rebuilt; a tree built
-// this way is always complete, which inflaters require of the code. Scratch:
-// leaf[n], weight[2n], parent[2n], depth[2n]. Writes len[order[i]].
+// ascending (frequency, symbol). When the tree is deeper than `limit`, every
+// frequency is halved (rounding up, so none reaches zero and the order is
+// kept) and the tree is rebuilt; a tree built this way is always complete,
+// which inflaters require of the code. Scratch: leaf[n], weight[2n],
+// parent[2n], depth[2n]. Writes len[order[i]].
 RD_HD void huffman_lengths(const uint32_t* freq, const uint16_t* order, int n, int limit, uint32_t* leaf,
                            uint32_t* weight, uint16_t* parent, uint8_t* depth, uint8_t* len) {
   for (int i = 0; i < n; ++i) leaf[i] = freq[order[i]];
   for (;;) {
-    for (int i = 0; i < n; ++i) weight[i] = leaf[i];
-    int next_leaf = 0, next_node = n, created = n;
-    for (int k = 0; k < n - 1; ++k) {
-      int pick[2];
-      for (int j = 0; j < 2; ++j) {
-        if (next_leaf < n && (next_node >= created || weight[next_leaf] <= weight[next_node]))
-          pick[j] = next_leaf++;
-        else
-          pick[j] = next_node++;
-      }
-      weight[created] = weight[pick[0]] + weight[pick[1]];
-      parent[pick[0]] = (uint16_t)created;
-      parent[pick[1]] = (uint16_t)created;
-      ++created;
-    }
+    huffman_tree(leaf, n, weight, parent);
     // Every node's parent was created after it, so depths resolve from the
     // root (the last node) downwards.
     const int root = 2 * n - 2;

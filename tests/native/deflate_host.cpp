@@ -1,8 +1,9 @@
 // Host harness of the PNG encoder's deflate arithmetic (test infrastructure).
 //
 // Compiles rohditor_gb300/csrc/deflate.cuh for the CPU and runs the segment
-// encoder the way png_deflate_kernel does, with its 512 threads played one
-// after another: the same per-thread byte ranges, run boundaries, token walk,
+// encoder the way png_histogram_kernel and png_pack_kernel do, with their
+// 1024 threads played one after another: the same per-thread byte ranges, run
+// boundaries, token walk,
 // Huffman construction, header, bit offsets and stored-block decision. The
 // tests feed its zlib stream to Python's zlib, so the block format is checked
 // without a GPU.
@@ -23,8 +24,7 @@ using namespace rd::png;
 
 namespace {
 
-constexpr int THREADS = 512;
-constexpr int PER = SEG / THREADS;
+constexpr int THREADS = SEG / CHUNK;
 
 struct Segment {
   std::vector<uint8_t> bytes;
@@ -32,41 +32,48 @@ struct Segment {
   bool stored = false;
 };
 
+struct ThreadChunk {
+  uint32_t w[CHUNK_WORDS] = {};
+  int c0 = 0, count = 0, before = -1, after = 0;
+  uint64_t breaks = 0;
+};
+
 Segment encode_segment(const uint8_t* in, int n, bool last) {
   Segment out;
-  std::vector<int> c0(THREADS), c1(THREADS), first(THREADS), lastb(THREADS), before(THREADS), after(THREADS);
+  std::vector<ThreadChunk> ch(THREADS);
   unsigned long long s1 = 0, s2 = 0;
   for (int t = 0; t < THREADS; ++t) {
-    c0[t] = std::min(t * PER, n);
-    c1[t] = std::min(c0[t] + PER, n);
-    first[t] = n;
-    lastb[t] = -1;
-    for (int p = c0[t]; p < c1[t]; ++p) {
-      if (p == 0 || in[p] != in[p - 1]) {
-        if (first[t] == n) first[t] = p;
-        lastb[t] = p;
-      }
-      s1 += in[p];
-      s2 += (unsigned long long)(n - p) * in[p];
+    ThreadChunk& c = ch[t];
+    c.c0 = std::min(t * CHUNK, n);
+    c.count = std::min(CHUNK, n - c.c0);
+    std::memcpy(c.w, in + c.c0, (size_t)c.count);  // little-endian host: byte j is chunk_byte(w, j)
+    c.breaks = chunk_breaks(c.w, c.count, c.c0 > 0 ? in[c.c0 - 1] : 0u, c.c0 == 0);
+    for (int j = 0; j < c.count; ++j) {
+      s1 += in[c.c0 + j];
+      s2 += (unsigned long long)(n - c.c0 - j) * in[c.c0 + j];
     }
   }
   int run = -1;
   for (int t = 0; t < THREADS; ++t) {
-    before[t] = run;
-    run = std::max(run, lastb[t]);
+    ch[t].before = run;
+    if (ch[t].breaks) run = std::max(run, ch[t].c0 + 63 - clz64(ch[t].breaks));
   }
   run = n;
   for (int t = THREADS - 1; t >= 0; --t) {
-    after[t] = run;
-    run = std::min(run, first[t]);
+    ch[t].after = run;
+    if (ch[t].breaks) run = std::min(run, ch[t].c0 + ctz64(ch[t].breaks));
   }
   out.s1 = (uint32_t)(s1 % ADLER_MOD);
   out.s2 = (uint32_t)(s2 % ADLER_MOD);
+  auto tokens = [&](int t, auto&& visit) {
+    const ThreadChunk& c = ch[t];
+    chunk_tokens(c.w, c.breaks, c.c0, c.count, c.before, c.after, visit);
+  };
 
   uint32_t freq[LIT_SYMBOLS] = {};
   freq[END_OF_BLOCK] = 1;
   for (int t = 0; t < THREADS; ++t)
-    for_each_token(in, c0[t], c1[t], before[t], after[t], [&](uint32_t lit, int len) {
+    tokens(t, [&](uint32_t lit, int len) {
       int eb, ev;
       freq[len ? length_symbol(len, &eb, &ev) : (int)lit]++;
     });
@@ -92,7 +99,7 @@ Segment encode_segment(const uint8_t* in, int n, bool last) {
 
   std::vector<uint32_t> bits(THREADS, 0), offset(THREADS);
   for (int t = 0; t < THREADS; ++t)
-    for_each_token(in, c0[t], c1[t], before[t], after[t], [&](uint32_t lit, int l) {
+    tokens(t, [&](uint32_t lit, int l) {
       int eb, ev;
       bits[t] += l ? len[length_symbol(l, &eb, &ev)] + eb + 1 : len[lit];
     });
@@ -109,7 +116,7 @@ Segment encode_segment(const uint8_t* in, int n, bool last) {
   if (!out.stored) {
     for (int t = 0; t < THREADS; ++t) {
       BitWriter tw{words.data(), offset[t]};
-      for_each_token(in, c0[t], c1[t], before[t], after[t], [&](uint32_t lit, int l) {
+      tokens(t, [&](uint32_t lit, int l) {
         if (l) {
           int eb, ev;
           const int sym = length_symbol(l, &eb, &ev);
