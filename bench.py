@@ -827,7 +827,7 @@ def png_files(dev, base, color, specs, d_out, d_gamut, W: int, H: int, reps: int
             encode()
         dev.synchronize()
         lib.rd_ctx_enable_kernel_timing(h, 0)
-        ms, launches = family_timing(lib, h, "png_encode")
+        ms, launches = family_timing(lib, h, "file_encode")
         per = ms / reps
         size = np.zeros(1, dtype=np.uint64)
         dev.check(lib.rd_copy_to_host(h, size.ctypes.data_as(ctypes.c_void_p), d_size, 8))
@@ -857,7 +857,56 @@ def png_files(dev, base, color, specs, d_out, d_gamut, W: int, H: int, reps: int
         result[name] = entry
         dev.check(lib.rd_device_free(h, d_png))
         dev.check(lib.rd_device_free(h, d_size))
+        if depth == 8:
+            result["jpeg_q90"] = jpeg_file(dev, d_out, rows, W, H, reps)
     return result
+
+
+def jpeg_file(dev, d_out, rows, W: int, H: int, reps: int, quality: int = 90) -> dict:
+    """JPEG file of the 8-bit output (export::encode's JPEG arm): rd_encode_jpeg_device
+    from the rows in HBM, the encoder's kernel time per file (L2 flushed before
+    each) and its wall time (it reads the symbol counts back once to build the
+    Huffman tables); end to end through rd_encode_jpeg from host rows."""
+    from rohditor_gb300 import JpegEncoder
+
+    lib, h = dev.lib, dev.handle
+    cap = int(lib.rd_jpeg_bound(W, H, 0, 0))
+    d_file, d_size = ctypes.c_void_p(), ctypes.c_void_p()
+    dev.check(lib.rd_device_alloc(h, cap, ctypes.byref(d_file)))
+    dev.check(lib.rd_device_alloc(h, 16, ctypes.byref(d_size)))
+
+    def encode():
+        dev.check(lib.rd_encode_jpeg_device(h, d_out, W, H, 3 * W, quality, None, 0, None, 0, d_file, cap, d_size))
+
+    encode()
+    dev.synchronize()
+    lib.rd_ctx_reset_kernel_timing(h)
+    lib.rd_ctx_enable_kernel_timing(h, 1)
+    wall = 0.0
+    for _ in range(reps):
+        dev.check(lib.rd_ctx_flush_l2(h))
+        dev.synchronize()
+        t0 = time.perf_counter()
+        encode()
+        dev.synchronize()
+        wall += time.perf_counter() - t0
+    lib.rd_ctx_enable_kernel_timing(h, 0)
+    ms, launches = family_timing(lib, h, "file_encode")
+    size = np.zeros(1, dtype=np.uint64)
+    dev.check(lib.rd_copy_to_host(h, size.ctypes.data_as(ctypes.c_void_p), d_size, 8))
+    enc = JpegEncoder(dev)
+    enc.encode(rows, quality)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        data = enc.encode(rows, quality)
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / reps
+    dev.check(lib.rd_device_free(h, d_file))
+    dev.check(lib.rd_device_free(h, d_size))
+    per = ms / reps
+    return {"quality": quality, "kernel_ms": round(per, 4), "wall_ms": round(wall * 1e3 / reps, 4),
+            "launches_per_file": launches // max(reps, 1), "mp_per_s": round(W * H / (per / 1e3) / 1e6, 1),
+            "file_bytes": int(size[0]), "bits_per_px": round(8.0 * int(size[0]) / (W * H), 3),
+            "e2e_ms": round(e2e_ms, 3), "e2e_h2d_bytes": rows.nbytes, "e2e_d2h_bytes": len(data)}
 
 
 def export_stream(args, count: int = 24, window: int = 3, cap_gb: float = 60.0) -> dict:

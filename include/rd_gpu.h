@@ -34,6 +34,7 @@
  *                            crates/core/src/analysis/histogram.rs:92-128
  *     rd_stage_output        apply_adjustments_with_local + the output conversions above
  *   rd_encode_png            export::encode, PNG arms     crates/core/src/export.rs:155-219
+ *   rd_encode_jpeg           export::encode, JPEG arm     crates/core/src/export.rs:166-175
  */
 #ifndef RD_GPU_H
 #define RD_GPU_H
@@ -315,6 +316,29 @@ rd_status rd_encode_png(rd_ctx* ctx, const void* rgb, uint32_t width, uint32_t h
 rd_status rd_encode_png_device(rd_ctx* ctx, const void* d_rgb, uint32_t width, uint32_t height, uint64_t row_stride,
                                int32_t bit_depth, const uint8_t* icc, uint64_t icc_len, const uint8_t* exif,
                                uint64_t exif_len, uint8_t* d_png, uint64_t capacity, uint64_t* d_png_bytes);
+/* ---- JPEG encode: the JPEG arm of export::encode (crates/core/src/export.rs:166-175),
+ * which hands tightly packed 8-bit RGB rows and a quality of 1..100, with the ICC
+ * profile and optional EXIF, to the image crate's JpegEncoder.
+ * The file is a baseline JPEG (ITU-T T.81): JFIF, Y/Cb/Cr at 4:4:4, the Annex K
+ * quantisation tables scaled by quality, Huffman tables built for the image,
+ * a restart marker every 32 MCUs, the profile in APP2 ICC_PROFILE segments and
+ * the EXIF block (a TIFF structure) in an APP1 Exif segment. rgb is interleaved
+ * u8 [height][3*width]; row_stride (samples) must equal 3*width. RD_INVALID_INPUT
+ * for padded rows or a quality outside 1..100, RD_INVALID_DIMENSIONS above 65535
+ * pixels a side. The encoder reads the image's symbol counts back once to build
+ * its tables (one synchronisation of the context's stream).
+ * rd_jpeg_bound: the largest file for these sizes (0 for invalid sizes). */
+uint64_t rd_jpeg_bound(uint32_t width, uint32_t height, uint64_t icc_len, uint64_t exif_len);
+/* Host rows in, host file out; as rd_encode_png for the buffer and metrics. */
+rd_status rd_encode_jpeg(rd_ctx* ctx, const uint8_t* rgb, uint32_t width, uint32_t height, uint64_t row_stride,
+                         int32_t quality, const uint8_t* icc, uint64_t icc_len, const uint8_t* exif,
+                         uint64_t exif_len, uint8_t* jpeg, uint64_t capacity, uint64_t* jpeg_bytes,
+                         rd_metrics* metrics);
+/* Device rows in, device file out (capacity >= rd_jpeg_bound; *d_jpeg_bytes a device u64). */
+rd_status rd_encode_jpeg_device(rd_ctx* ctx, const uint8_t* d_rgb, uint32_t width, uint32_t height,
+                                uint64_t row_stride, int32_t quality, const uint8_t* icc, uint64_t icc_len,
+                                const uint8_t* exif, uint64_t exif_len, uint8_t* d_jpeg, uint64_t capacity,
+                                uint64_t* d_jpeg_bytes);
 /* Self-check of the correctly rounded arithmetic on the device, for test
  * suites (no reference counterpart). which = 0: the number of positive finite
  * f32 whose cube root is not correctly rounded (or not odd-symmetric), exact

@@ -144,6 +144,11 @@ def load():
             "ro_render_output": (ctypes.c_int, [F32P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(OutputDesc),
                                                 ctypes.c_void_p, U64P]),
             "ro_png_filter": (None, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, U8P]),
+            "ro_jpeg_coefficients": (None, [U8P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                            ctypes.POINTER(ctypes.c_int16)]),
+            "ro_jpeg_decode": (ctypes.c_int, [U8P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_int),
+                                              ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), U8P,
+                                              ctypes.POINTER(ctypes.c_int16), ctypes.c_size_t]),
             "ro_png_unfilter": (ctypes.c_int, [U8P, ctypes.c_int, ctypes.c_int, ctypes.c_int, U8P]),
         }
         for name, (res, args) in list(sig.items()) + list(optional.items()):
@@ -593,4 +598,55 @@ def png_unfilter(stream: bytes, width: int, height: int, depth: int) -> np.ndarr
     if depth == 16:
         return out.view(">u2").astype(np.uint16).reshape(height, width, 3)
     return out.reshape(height, width, 3)
+
+
+def jpeg_coefficients(rgb: np.ndarray, quality: int) -> np.ndarray:
+    """Quantised coefficients [blocks][3][64] (zigzag order) of 8-bit RGB rows [h][w][3]."""
+    rgb = np.ascontiguousarray(rgb, dtype=np.uint8)
+    h, w = rgb.shape[:2]
+    out = np.zeros((((w + 7) // 8) * ((h + 7) // 8), 3, 64), dtype=np.int16)
+    load().ro_jpeg_coefficients(ptr(rgb, ctypes.c_uint8), w, h, quality, ptr(out, ctypes.c_int16))
+    return out
+
+
+def jpeg_decode(data: bytes) -> dict:
+    """Baseline JPEG back to its coefficients: width, height, restart interval, quant tables, coef."""
+    src = np.frombuffer(data, dtype=np.uint8).copy()
+    w, h, ri = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    quant = np.zeros((3, 64), dtype=np.uint8)
+    # The coefficient buffer is sized from the frame header's dimensions.
+    pos = 2
+    while pos + 9 < len(data) and not (data[pos] == 0xFF and data[pos + 1] == 0xC0):
+        pos += 2 + int.from_bytes(data[pos + 2:pos + 4], "big")
+    fh, fw = int.from_bytes(data[pos + 5:pos + 7], "big"), int.from_bytes(data[pos + 7:pos + 9], "big")
+    coef = np.zeros((((fw + 7) // 8) * ((fh + 7) // 8), 3, 64), dtype=np.int16)
+    rc = load().ro_jpeg_decode(ptr(src, ctypes.c_uint8), len(data), ctypes.byref(w), ctypes.byref(h),
+                               ctypes.byref(ri), ptr(quant, ctypes.c_uint8), ptr(coef, ctypes.c_int16), coef.size)
+    if rc != 0:
+        raise ValueError(f"JPEG decode failed ({rc})")
+    return {"width": w.value, "height": h.value, "restart": ri.value, "quant": quant, "coef": coef}
+
+
+def jpeg_pixels(decoded: dict) -> np.ndarray:
+    """RGB u8 [h][w][3] from decoded coefficients: dequantisation, the inverse DCT and
+    the JFIF colour conversion in floating point."""
+    w, h = decoded["width"], decoded["height"]
+    bw, bh = (w + 7) // 8, (h + 7) // 8
+    nat = _zigzag_natural()
+    coef = decoded["coef"].astype(np.float64)
+    blocks = np.zeros((bw * bh, 3, 64))
+    blocks[:, :, nat] = coef * decoded["quant"][None, :, nat]
+    blocks = blocks.reshape(bw * bh, 3, 8, 8)
+    u = np.arange(8)
+    basis = np.cos((2 * u[None, :] + 1) * u[:, None] * np.pi / 16) * np.where(u == 0, np.sqrt(0.5), 1.0)[:, None] / 2
+    spatial = np.einsum("vy,bcvu,ux->bcyx", basis, blocks, basis) + 128.0
+    img = spatial.reshape(bh, bw, 3, 8, 8).transpose(0, 3, 1, 4, 2).reshape(bh * 8, bw * 8, 3)[:h, :w]
+    y, cb, cr = img[..., 0], img[..., 1] - 128.0, img[..., 2] - 128.0
+    rgb = np.stack([y + 1.402 * cr, y - 0.344136 * cb - 0.714136 * cr, y + 1.772 * cb], axis=-1)
+    return np.clip(np.rint(rgb), 0, 255).astype(np.uint8)
+
+
+def _zigzag_natural() -> np.ndarray:
+    order = sorted(((r + c, r if (r + c) % 2 else c, r, c) for r in range(8) for c in range(8)))
+    return np.array([r * 8 + c for _, _, r, c in order])
 

@@ -158,6 +158,16 @@ int ro_synth_mosaic(const ro_synth* desc, uint16_t* out);
 void ro_png_filter(const uint8_t* image, int w, int h, int depth, uint8_t* stream);
 int ro_png_unfilter(const uint8_t* stream, int w, int h, int depth, uint8_t* out);
 
+/* ---- JPEG (jpeg.cpp) ----
+ * ro_jpeg_coefficients: the quantised coefficients of 8-bit RGB rows [h][3w] at
+ * quality 1..100, [block (raster order)][Y, Cb, Cr][64 in zigzag order].
+ * ro_jpeg_decode: a baseline JPEG (three 1x1 components, restart intervals) back
+ * into its coefficients in the same layout; quant receives each component's
+ * table (3 x 64, natural order). 0 on success, negative for a malformed file. */
+void ro_jpeg_coefficients(const uint8_t* rgb, int w, int h, int quality, int16_t* coef);
+int ro_jpeg_decode(const uint8_t* data, size_t n, int* width, int* height, int* restart, uint8_t* quant,
+                   int16_t* coef, size_t coef_capacity);
+
 #ifdef __cplusplus
 }
 #endif

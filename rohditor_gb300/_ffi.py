@@ -184,6 +184,13 @@ SIGNATURES = {
     "rd_encode_png_device": (ctypes.c_int, [VOIDP, VOIDP, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64,
                                             ctypes.c_int32, U8P, ctypes.c_uint64, U8P, ctypes.c_uint64, VOIDP,
                                             ctypes.c_uint64, VOIDP]),
+    "rd_jpeg_bound": (ctypes.c_uint64, [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64]),
+    "rd_encode_jpeg": (ctypes.c_int, [VOIDP, VOIDP, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int32,
+                                      U8P, ctypes.c_uint64, U8P, ctypes.c_uint64, U8P, ctypes.c_uint64, U64P,
+                                      ctypes.POINTER(Metrics)]),
+    "rd_encode_jpeg_device": (ctypes.c_int, [VOIDP, VOIDP, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64,
+                                             ctypes.c_int32, U8P, ctypes.c_uint64, U8P, ctypes.c_uint64, VOIDP,
+                                             ctypes.c_uint64, VOIDP]),
     "rd_check_math": (ctypes.c_int, [VOIDP, ctypes.c_int32, U64P]),
     "rd_rl_launch_shape": (ctypes.c_int, [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float,
                                           ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),

@@ -54,7 +54,7 @@ const char* kernel_family_name(int family) {
   static const char* names[K_FAMILY_COUNT] = {
       "normalize", "opposed", "mhc_bilinear", "rcd", "amaze", "rl_mask", "rl_iteration",
       "rl_apply", "vignetting", "optics_gather", "area_reduce", "wb_matrix",
-      "color_output", "synth", "display_output", "png_encode"};
+      "color_output", "synth", "display_output", "file_encode"};
   return family >= 0 && family < K_FAMILY_COUNT ? names[family] : "unknown";
 }
 
@@ -1017,6 +1017,87 @@ rd_status rd_encode_png(rd_ctx* h, const void* rgb, uint32_t width, uint32_t hei
   if (st.ok() && (cudaMemcpyAsync(png, d_png, size, cudaMemcpyDeviceToHost, ctx.stream) != cudaSuccess ||
                   cudaStreamSynchronize(ctx.stream) != cudaSuccess))
     st = Status{RD_READBACK, "PNG readback failed"};
+  if (st.ok() && metrics) {
+    std::memset(metrics, 0, sizeof(*metrics));
+    metrics->total_ms = tm.span(0, 1);
+    metrics->kernel_launches = ctx.launches;
+  }
+  rd::device_free(ctx, p, total);
+  return finish(h, st);
+}
+
+// ---- JPEG encode ---------------------------------------------------------
+static Status jpeg_args(const void* rgb, uint32_t width, uint32_t height, uint64_t row_stride, int32_t quality,
+                        const uint8_t* icc, uint64_t icc_len, const uint8_t* exif, uint64_t exif_len) {
+  // The JPEG arm takes 8-bit rows only (export.rs:166 matches ExportImage::Rgb8).
+  RD_TRY(png_args(rgb, width, height, row_stride, 8, icc, icc_len, exif, exif_len));
+  return rd::jpeg_check((int)width, (int)height, quality);
+}
+
+uint64_t rd_jpeg_bound(uint32_t width, uint32_t height, uint64_t icc_len, uint64_t exif_len) {
+  if (width == 0 || height == 0 || width > 65535 || height > 65535) return 0;
+  return rd::jpeg_bound((int)width, (int)height, icc_len, exif_len);
+}
+
+rd_status rd_encode_jpeg_device(rd_ctx* h, const uint8_t* d_rgb, uint32_t width, uint32_t height,
+                                uint64_t row_stride, int32_t quality, const uint8_t* icc, uint64_t icc_len,
+                                const uint8_t* exif, uint64_t exif_len, uint8_t* d_jpeg, uint64_t capacity,
+                                uint64_t* d_jpeg_bytes) {
+  if (!h || !d_jpeg || !d_jpeg_bytes) return finish(h, Status{RD_INVALID_INPUT, "null argument"});
+  Status st = jpeg_args(d_rgb, width, height, row_stride, quality, icc, icc_len, exif, exif_len);
+  if (st.ok() && reinterpret_cast<uintptr_t>(d_jpeg_bytes) % 8)
+    st = Status{RD_INVALID_INPUT, "the byte count must be 8-byte aligned"};
+  if (st.ok() && capacity < rd::jpeg_bound((int)width, (int)height, icc_len, exif_len))
+    st = Status{RD_INVALID_DIMENSIONS, "the JPEG buffer is smaller than rd_jpeg_bound"};
+  if (!st.ok()) return finish(h, st);
+  rd::Context& ctx = h->c;
+  cudaSetDevice(ctx.device);
+  st = rd::run_jpeg_encode(ctx, d_rgb, (int)width, (int)height, quality, icc, icc_len, exif, exif_len, d_jpeg,
+                           d_jpeg_bytes);
+  if (st.ok()) st = rd::check_kernel_error(ctx, "jpeg encode");
+  return finish(h, st);
+}
+
+rd_status rd_encode_jpeg(rd_ctx* h, const uint8_t* rgb, uint32_t width, uint32_t height, uint64_t row_stride,
+                         int32_t quality, const uint8_t* icc, uint64_t icc_len, const uint8_t* exif,
+                         uint64_t exif_len, uint8_t* jpeg, uint64_t capacity, uint64_t* jpeg_bytes,
+                         rd_metrics* metrics) {
+  if (!h || !jpeg || !jpeg_bytes) return finish(h, Status{RD_INVALID_INPUT, "null argument"});
+  Status st = jpeg_args(rgb, width, height, row_stride, quality, icc, icc_len, exif, exif_len);
+  if (!st.ok()) return finish(h, st);
+  rd::Context& ctx = h->c;
+  cudaSetDevice(ctx.device);
+  const uint64_t in_bytes = 3ull * width * height;
+  const uint64_t in_room = (in_bytes + 255) & ~255ull;
+  const uint64_t bound = rd::jpeg_bound((int)width, (int)height, icc_len, exif_len);
+  const uint64_t out_room = (bound + 255) & ~255ull;
+  const uint64_t total = in_room + out_room + 16;
+  void* p = nullptr;
+  st = rd::device_alloc(ctx, total, &p);
+  if (!st.ok()) return finish(h, st);
+  uint8_t* d_in = static_cast<uint8_t*>(p);
+  uint8_t* d_file = d_in + in_room;
+  uint64_t* d_size = reinterpret_cast<uint64_t*>(d_file + out_room);
+  Timer tm(ctx);
+  if (cudaMemcpyAsync(d_in, rgb, in_bytes, cudaMemcpyHostToDevice, ctx.stream) != cudaSuccess)
+    st = Status{RD_SYNCHRONIZATION, "image upload failed"};
+  tm.mark();
+  if (st.ok())
+    st = rd::run_jpeg_encode(ctx, d_in, (int)width, (int)height, quality, icc, icc_len, exif, exif_len, d_file,
+                             d_size);
+  tm.mark();
+  uint64_t size = 0;
+  if (st.ok() && (cudaMemcpyAsync(&size, d_size, sizeof(size), cudaMemcpyDeviceToHost, ctx.stream) != cudaSuccess ||
+                  cudaStreamSynchronize(ctx.stream) != cudaSuccess))
+    st = Status{RD_READBACK, "JPEG size readback failed"};
+  if (st.ok()) st = rd::check_kernel_error(ctx, "jpeg encode");
+  if (st.ok()) {
+    *jpeg_bytes = size;
+    if (size > capacity) st = Status{RD_INVALID_DIMENSIONS, "the JPEG buffer is smaller than the file"};
+  }
+  if (st.ok() && (cudaMemcpyAsync(jpeg, d_file, size, cudaMemcpyDeviceToHost, ctx.stream) != cudaSuccess ||
+                  cudaStreamSynchronize(ctx.stream) != cudaSuccess))
+    st = Status{RD_READBACK, "JPEG readback failed"};
   if (st.ok() && metrics) {
     std::memset(metrics, 0, sizeof(*metrics));
     metrics->total_ms = tm.span(0, 1);

@@ -207,7 +207,7 @@ RD_HD void huffman_tree(const uint32_t* leaf, int n, uint32_t* weight, uint16_t*
   }
 }
 
-// Huffman code lengths of n >= 2 symbols whose indices `order` lists by
+// Huffman code lengths of the n symbols whose indices `order` lists by
 // ascending (frequency, symbol). When the tree is deeper than `limit`, every
 // frequency is halved (rounding up, so none reaches zero and the order is
 // kept) and the tree is rebuilt; a tree built this way is always complete,
@@ -215,6 +215,10 @@ RD_HD void huffman_tree(const uint32_t* leaf, int n, uint32_t* weight, uint16_t*
 // parent[2n], depth[2n]. Writes len[order[i]].
 RD_HD void huffman_lengths(const uint32_t* freq, const uint16_t* order, int n, int limit, uint32_t* leaf,
                            uint32_t* weight, uint16_t* parent, uint8_t* depth, uint8_t* len) {
+  if (n < 2) {  // a lone symbol still needs a one-bit code
+    if (n == 1) len[order[0]] = 1;
+    return;
+  }
   for (int i = 0; i < n; ++i) leaf[i] = freq[order[i]];
   for (;;) {
     huffman_tree(leaf, n, weight, parent);

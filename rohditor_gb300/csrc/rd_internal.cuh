@@ -334,6 +334,16 @@ Status png_header(int W, int H, int depth, const uint8_t* icc, size_t icc_len, c
 uint64_t png_bound(int W, int H, int depth, uint64_t header_bytes);
 Status run_png_encode(Context& ctx, const void* d_rgb, int W, int H, int depth, const std::vector<uint8_t>& header,
                       uint8_t* d_png, uint64_t* d_png_bytes);
+
+// JPEG encoding (k_jpeg.cu) of interleaved 8-bit RGB rows at quality 1..100.
+// jpeg_bound is the largest file; run_jpeg_encode writes the whole file into
+// d_file and its byte count into *d_file_bytes (device memory). It reads the
+// image's symbol counts back to build the Huffman tables, so it synchronises
+// the stream once and cannot run under graph capture.
+Status jpeg_check(int W, int H, int quality);
+uint64_t jpeg_bound(int W, int H, uint64_t icc_len, uint64_t exif_len);
+Status run_jpeg_encode(Context& ctx, const uint8_t* d_rgb, int W, int H, int quality, const uint8_t* icc,
+                       size_t icc_len, const uint8_t* exif, size_t exif_len, uint8_t* d_file, uint64_t* d_file_bytes);
 // One launch rendering several bases (render path of the served loop). The
 // staging buffers (host pinned and device, color_batch_staging_bytes(n) each)
 // carry the per-image parameters and LUTs.

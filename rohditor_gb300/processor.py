@@ -589,6 +589,45 @@ class PngEncoder:
         return out[:size.value].tobytes()
 
 
+class JpegEncoder:
+    """The JPEG arm of export::encode (crates/core/src/export.rs:166-175) on the device.
+
+    `encode` takes 8-bit interleaved RGB rows ([h][w][3] or [h][3w]) and a
+    quality of 1..100 and returns a baseline JPEG file with the ICC profile in
+    APP2 segments and the EXIF block in an APP1 segment. Rows that are not
+    tightly packed (`row_stride` samples per row) and qualities outside 1..100
+    are refused.
+    """
+
+    def __init__(self, device: Device):
+        self.device = device
+
+    @staticmethod
+    def bound(width: int, height: int, icc_len: int = 0, exif_len: int = 0) -> int:
+        return int(_ffi.load().rd_jpeg_bound(width, height, icc_len, exif_len))
+
+    def encode(self, rgb: np.ndarray, quality: int, icc_profile: bytes = b"", exif: bytes | None = None,
+               row_stride: int | None = None, width: int | None = None) -> bytes:
+        rgb = np.ascontiguousarray(rgb)
+        if rgb.dtype != np.uint8:
+            raise GpuPreviewError(8, f"JPEG samples are uint8, not {rgb.dtype}")
+        height = rgb.shape[0]
+        if width is None:
+            width = rgb.shape[1] if rgb.ndim == 3 else rgb.shape[1] // 3
+        stride = 3 * width if row_stride is None else row_stride
+        icc = np.frombuffer(icc_profile, dtype=np.uint8) if icc_profile else None
+        ex = np.frombuffer(exif, dtype=np.uint8) if exif else None
+        capacity = max(self.bound(width, height, len(icc_profile or b""), len(exif or b"")), 1)
+        out = np.empty(capacity, dtype=np.uint8)
+        size = ctypes.c_uint64(0)
+        self.device.check(self.device.lib.rd_encode_jpeg(
+            self.device.handle, rgb.ctypes.data_as(ctypes.c_void_p), width, height, stride, quality,
+            _ptr(icc, ctypes.c_uint8) if icc is not None else None, len(icc_profile or b""),
+            _ptr(ex, ctypes.c_uint8) if ex is not None else None, len(exif or b""),
+            _ptr(out, ctypes.c_uint8), out.nbytes, ctypes.byref(size), None))
+        return out[:size.value].tobytes()
+
+
 # ---------------------------------------------------------------- stage API
 class Stages:
     """The crates' stage functions, each run on the device with host buffers."""
