@@ -41,6 +41,8 @@ using namespace jpeg;
 constexpr unsigned FULL = 0xFFFFFFFFu;
 constexpr int COEF_THREADS = 256;  // 8 pixel rows x 32 blocks
 constexpr int COEF_BLOCKS = 32;
+constexpr int COEF_STRIDE = 194;  // int16 per block in shared memory: 3 x 64, padded to an odd word count
+constexpr int BLOCK_STRIDE = 66;  // int16 per block-component in shared memory: 64, padded to 33 words
 constexpr int HIST_THREADS = 256;
 constexpr int PACK_THREADS = INTERVAL_BLOCKS;  // one per block of the interval
 constexpr int LAYOUT_THREADS = 1024;
@@ -59,6 +61,7 @@ __global__ void __launch_bounds__(COEF_THREADS) jpeg_coef_kernel(const __grid_co
   // t[c][y][u][block]: the row pass result, the block index innermost so that
   // the lanes of a warp (consecutive blocks) hit consecutive banks.
   __shared__ int t[3][8][8][COEF_BLOCKS];
+  __shared__ __align__(16) int16_t q[COEF_BLOCKS * COEF_STRIDE];
   const int lane = threadIdx.x & 31, rowu = threadIdx.x >> 5;
   const int bx = blockIdx.x * COEF_BLOCKS + lane, by = blockIdx.y;
   {
@@ -84,10 +87,10 @@ __global__ void __launch_bounds__(COEF_THREADS) jpeg_coef_kernel(const __grid_co
     }
   }
   __syncthreads();
-  if (bx >= P.bw) return;
-  // Column pass: column u = rowu of block `lane`.
+  // Column pass: column u = rowu of block `lane`; the quantised coefficients
+  // gather in q[block][component][zigzag], a block's 192 values padded to 97
+  // words so that the 32 lanes (blocks) of a warp store to 32 banks.
   const int u = rowu;
-  int16_t* dst = P.coef + ((int64_t)by * P.bw + bx) * 3 * 64;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     int col[8], f[8];
@@ -97,9 +100,16 @@ __global__ void __launch_bounds__(COEF_THREADS) jpeg_coef_kernel(const __grid_co
 #pragma unroll
     for (int v = 0; v < 8; ++v) {
       const int nat = v * 8 + u;
-      dst[c * 64 + P.zigzag_of[nat]] = (int16_t)quantize(f[v], P.quant[c == 0 ? 0 : 1][nat]);
+      q[lane * COEF_STRIDE + c * 64 + P.zigzag_of[nat]] = (int16_t)quantize(f[v], P.quant[c == 0 ? 0 : 1][nat]);
     }
   }
+  __syncthreads();
+  // The CTA's blocks are consecutive in raster order: one contiguous run of
+  // 384-byte blocks, stored as 32-bit words.
+  const int nb = min(COEF_BLOCKS, P.bw - (int)blockIdx.x * COEF_BLOCKS);
+  uint32_t* dst = reinterpret_cast<uint32_t*>(P.coef + ((int64_t)by * P.bw + blockIdx.x * COEF_BLOCKS) * 3 * 64);
+  const uint32_t* src = reinterpret_cast<const uint32_t*>(q);
+  for (int w = threadIdx.x; w < nb * 96; w += COEF_THREADS) dst[w] = src[(w / 96) * (COEF_STRIDE / 2) + w % 96];
 }
 
 // Symbols of one block: the DC difference's category, then (run, category)
@@ -127,23 +137,35 @@ __device__ __forceinline__ void block_symbols(const int16_t* z, int pred, Visit&
   if (run > 0) visit(false, 0x00, 0u, 0);
 }
 
-// DC prediction: the previous block of the component, reset to 0 at the
-// first MCU of every restart interval.
-__device__ __forceinline__ int dc_prediction(const int16_t* coef, int64_t blk, int c) {
-  return blk % RESTART_MCUS == 0 ? 0 : coef[((blk - 1) * 3 + c) * 64];
+// Block-components [g0, g0 + n) (64 coefficients each, contiguous in
+// global memory) into dst with BLOCK_STRIDE per block-component, as 32-bit
+// words: coalesced loads, and lanes reading their own blocks later hit 32
+// different banks.
+template <int THREADS>
+__device__ __forceinline__ void stage_blocks(const int16_t* __restrict__ coef, int64_t g0, int n, int16_t* dst) {
+  const uint32_t* src = reinterpret_cast<const uint32_t*>(coef + g0 * 64);
+  uint32_t* d = reinterpret_cast<uint32_t*>(dst);
+  for (int w = threadIdx.x; w < n * 32; w += THREADS) d[(w >> 5) * (BLOCK_STRIDE / 2) + (w & 31)] = src[w];
 }
 
 __global__ void __launch_bounds__(HIST_THREADS)
     jpeg_hist_kernel(const int16_t* __restrict__ coef, int64_t blocks, uint32_t* __restrict__ hist) {
   __shared__ uint32_t h[TABLES][256];
+  __shared__ __align__(16) int16_t z[HIST_THREADS * BLOCK_STRIDE];
   for (int i = threadIdx.x; i < TABLES * 256; i += HIST_THREADS) (&h[0][0])[i] = 0u;
+  const int64_t g0 = (int64_t)blockIdx.x * HIST_THREADS;
+  const int n = (int)min((int64_t)HIST_THREADS, blocks * 3 - g0);
+  stage_blocks<HIST_THREADS>(coef, g0, n, z);
   __syncthreads();
-  const int64_t g = (int64_t)blockIdx.x * HIST_THREADS + threadIdx.x;
-  if (g < blocks * 3) {
+  const int local = threadIdx.x;
+  if (local < n) {
+    const int64_t g = g0 + local;
     const int64_t blk = g / 3;
     const int c = (int)(g % 3);
     const int table = c == 0 ? 0 : 2;
-    block_symbols(coef + g * 64, dc_prediction(coef, blk, c), [&](bool dc, int sym, uint32_t, int) {
+    // DC prediction: the previous block of the component, 0 at the first MCU of an interval.
+    const int pred = blk % RESTART_MCUS == 0 ? 0 : (local >= 3 ? z[(local - 3) * BLOCK_STRIDE] : coef[(g - 3) * 64]);
+    block_symbols(z + local * BLOCK_STRIDE, pred, [&](bool dc, int sym, uint32_t, int) {
       atomicAdd(&h[table + (dc ? 0 : 1)][sym], 1u);
     });
   }
@@ -185,18 +207,22 @@ __global__ void __launch_bounds__(PACK_THREADS)
   __shared__ uint32_t s_codes[TABLES][256];  // code | length << 16
   __shared__ __align__(16) uint32_t words[(INTERVAL_BYTES + 3) / 4 + 1];
   __shared__ uint32_t warp_sum[PACK_THREADS / 32];
+  __shared__ __align__(16) int16_t s_coef[INTERVAL_BLOCKS * BLOCK_STRIDE];
   const int64_t interval = blockIdx.x;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int i = tid; i < TABLES * 256; i += PACK_THREADS) (&s_codes[0][0])[i] = codes[i];
   for (int i = tid; i < (INTERVAL_BYTES + 3) / 4 + 1; i += PACK_THREADS) words[i] = 0u;
-  const int64_t g = interval * INTERVAL_BLOCKS + tid;  // block-component of this thread
-  const bool active = g < blocks * 3;
-  const int64_t blk = g / 3;
-  const int c = (int)(g % 3);
-  const int table = c == 0 ? 0 : 2;
-  const int16_t* z = coef + g * 64;
-  const int pred = active ? dc_prediction(coef, blk, c) : 0;
+  const int64_t g0 = interval * INTERVAL_BLOCKS;
+  const int n = (int)min((int64_t)INTERVAL_BLOCKS, blocks * 3 - g0);
+  stage_blocks<PACK_THREADS>(coef, g0, n, s_coef);
   __syncthreads();
+  // Thread tid codes block-component tid of the interval: MCU tid / 3,
+  // component tid % 3; the interval starts a new DC prediction.
+  const bool active = tid < n;
+  const int c = tid % 3;
+  const int table = c == 0 ? 0 : 2;
+  const int16_t* z = s_coef + tid * BLOCK_STRIDE;
+  const int pred = (active && tid >= 3) ? s_coef[(tid - 3) * BLOCK_STRIDE] : 0;
 
   uint32_t bits = 0;
   if (active)
