@@ -545,6 +545,27 @@ int32_t rd_server_poll(rd_server* server, rd_server_result* out, int32_t max_res
 rd_status rd_server_submit_export(rd_server* server, uint32_t image_id, uint64_t revision, const rd_color_desc* color,
                                   const rd_output_desc* outputs, int32_t n_outputs, void* const* dst,
                                   const size_t* capacities, uint64_t* request_id);
+/* Files of a served export (export::encode, crates/core/src/export.rs:155-219):
+ * output k of rd_server_submit_export_files is encoded as described by files[k]
+ * and dst[k] receives the file's bytes (capacity: rd_png_bound / rd_jpeg_bound of
+ * the output's dimensions and the metadata lengths). PNG takes an RD_OUTPUT_SRGB8
+ * or RD_OUTPUT_SRGB16 output, JPEG an RD_OUTPUT_SRGB8 one; RD_FILE_ROWS keeps the
+ * rows as rd_server_submit_export does. The profile and EXIF bytes are copied at
+ * submission; *file_bytes (may be NULL) receives the size when the export ends. */
+enum { RD_FILE_ROWS = 0, RD_FILE_PNG = 1, RD_FILE_JPEG = 2 };
+typedef struct rd_export_file {
+  int32_t format;          /* RD_FILE_* */
+  int32_t quality;         /* JPEG: 1..100 */
+  const uint8_t* icc;      /* ICC profile, or NULL */
+  uint64_t icc_len;
+  const uint8_t* exif;     /* EXIF block (a TIFF structure), or NULL */
+  uint64_t exif_len;
+  uint64_t* file_bytes;
+} rd_export_file;
+rd_status rd_server_submit_export_files(rd_server* server, uint32_t image_id, uint64_t revision,
+                                        const rd_color_desc* color, const rd_output_desc* outputs,
+                                        const rd_export_file* files, int32_t n_outputs, void* const* dst,
+                                        const size_t* capacities, uint64_t* request_id);
 /* The latest rendered output of an image: sRGB8 [h][3w], 1024 histogram bins, its revision. */
 rd_status rd_server_read_output(rd_server* server, uint32_t image_id, uint8_t* srgb, uint64_t* hist,
                                 uint64_t* revision);

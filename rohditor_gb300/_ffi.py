@@ -122,6 +122,17 @@ class ServerResult(ctypes.Structure):
     ]
 
 
+class ExportFile(ctypes.Structure):
+    _fields_ = [
+        ("format", ctypes.c_int32), ("quality", ctypes.c_int32),
+        ("icc", U8P), ("icc_len", ctypes.c_uint64), ("exif", U8P), ("exif_len", ctypes.c_uint64),
+        ("file_bytes", U64P),
+    ]
+
+
+FILE_FORMAT = {"rows": 0, "png": 1, "jpeg": 2}
+
+
 class ServerStats(ctypes.Structure):
     _fields_ = [(name, ctypes.c_uint64) for name in (
         "requested", "completed", "coalesced", "failed", "redeveloped", "evictions", "batches", "batched_edits",
@@ -246,6 +257,10 @@ SIGNATURES = {
     "rd_server_submit_export": (ctypes.c_int, [VOIDP, ctypes.c_uint32, ctypes.c_uint64, ctypes.POINTER(ColorDesc),
                                                ctypes.POINTER(OutputDesc), ctypes.c_int32, ctypes.POINTER(VOIDP),
                                                ctypes.POINTER(ctypes.c_size_t), U64P]),
+    "rd_server_submit_export_files": (ctypes.c_int, [VOIDP, ctypes.c_uint32, ctypes.c_uint64,
+                                                     ctypes.POINTER(ColorDesc), ctypes.POINTER(OutputDesc),
+                                                     ctypes.POINTER(ExportFile), ctypes.c_int32,
+                                                     ctypes.POINTER(VOIDP), ctypes.POINTER(ctypes.c_size_t), U64P]),
     "rd_server_poll": (ctypes.c_int32, [VOIDP, ctypes.POINTER(ServerResult), ctypes.c_int32, ctypes.c_int32]),
     "rd_server_read_output": (ctypes.c_int, [VOIDP, ctypes.c_uint32, U8P, U64P, U64P]),
     "rd_server_get_stats": (ctypes.c_int, [VOIDP, ctypes.POINTER(ServerStats)]),

@@ -94,9 +94,11 @@ struct ExportRequest {
   Ticket ticket;
   rd_color_desc color;
   std::vector<rd_output_desc> outputs;
+  std::vector<rd_export_file> files;  // one per output; RD_FILE_ROWS when no file is asked for
+  std::vector<std::vector<uint8_t>> icc, exif;  // the files' metadata, copied at submission
   std::vector<void*> dst;
   std::vector<size_t> capacity;
-  size_t largest_output = 0;  // bytes of the largest output
+  size_t largest_output = 0;  // bytes of the largest output with its file encoder's working set
   Clock::time_point submitted;
 };
 
@@ -256,11 +258,52 @@ class CudaExecutor : public Executor {
                                 im.cam, &base, nullptr),
                      "export spatial pass failed"));
     rd_status st = RD_OK;
-    for (size_t k = 0; k < rq.outputs.size() && st == RD_OK; ++k)
-      st = rd_render_output(dev, base, &rq.color, &rq.outputs[k], rq.dst[k], rq.capacity[k], nullptr, nullptr,
-                            nullptr);
+    for (size_t k = 0; k < rq.outputs.size() && st == RD_OK; ++k) {
+      if (rq.files[k].format == RD_FILE_ROWS)
+        st = rd_render_output(dev, base, &rq.color, &rq.outputs[k], rq.dst[k], rq.capacity[k], nullptr, nullptr,
+                              nullptr);
+      else
+        st = export_file(base, rq, k);
+    }
     rd_base_release(base);
     return from_code(st, "export output failed");
+  }
+  // Output k rendered into device rows, encoded on the device, and the file
+  // copied into the client's buffer.
+  rd_status export_file(rd_base* base, const ExportRequest& rq, size_t k) {
+    const rd_output_desc& out = rq.outputs[k];
+    const rd_export_file& f = rq.files[k];
+    uint32_t ow = 0, oh = 0, bpp = 0;
+    rd_status st = rd_output_dimensions((uint32_t)base->W, (uint32_t)base->H, &out, &ow, &oh, &bpp);
+    if (st != RD_OK) return st;
+    const size_t rows = (size_t)ow * oh * bpp;
+    const uint64_t bound = f.format == RD_FILE_PNG ? rd_png_bound(ow, oh, out.format == RD_OUTPUT_SRGB16 ? 16 : 8,
+                                                                  f.icc_len, f.exif_len)
+                                                   : rd_jpeg_bound(ow, oh, f.icc_len, f.exif_len);
+    void *d_rows = nullptr, *d_file = nullptr, *d_size = nullptr;
+    st = rd_device_alloc(dev, rows, &d_rows);
+    if (st == RD_OK) st = rd_device_alloc(dev, bound, &d_file);
+    if (st == RD_OK) st = rd_device_alloc(dev, 16, &d_size);
+    if (st == RD_OK) st = rd_render_output_device(dev, base, &rq.color, &out, d_rows, nullptr, nullptr, nullptr);
+    if (st == RD_OK) {
+      uint8_t* file = static_cast<uint8_t*>(d_file);
+      uint64_t* size_at = static_cast<uint64_t*>(d_size);
+      st = f.format == RD_FILE_PNG
+               ? rd_encode_png_device(dev, d_rows, ow, oh, 3ull * ow, out.format == RD_OUTPUT_SRGB16 ? 16 : 8, f.icc,
+                                      f.icc_len, f.exif, f.exif_len, file, bound, size_at)
+               : rd_encode_jpeg_device(dev, static_cast<const uint8_t*>(d_rows), ow, oh, 3ull * ow, f.quality, f.icc,
+                                       f.icc_len, f.exif, f.exif_len, file, bound, size_at);
+    }
+    uint64_t size = 0;
+    if (st == RD_OK) st = rd_copy_to_host(dev, &size, d_size, sizeof(size));
+    if (st == RD_OK) {
+      if (f.file_bytes) *f.file_bytes = size;
+      st = size > rq.capacity[k] ? RD_INVALID_DIMENSIONS : rd_copy_to_host(dev, rq.dst[k], d_file, size);
+    }
+    if (d_size) rd_device_free(dev, d_size);
+    if (d_file) rd_device_free(dev, d_file);
+    if (d_rows) rd_device_free(dev, d_rows);
+    return st;
   }
   Status render(const std::vector<ServedImage*>& ims, const std::vector<rd_base*>& bases,
                 const std::vector<const rd_color_desc*>& colors) override {
@@ -337,7 +380,10 @@ class DryExecutor : public Executor {
   Status export_outputs(ServedImage&, const ExportRequest& rq) override {
     std::this_thread::sleep_for(std::chrono::microseconds(develop_us));
     const uint8_t v = (uint8_t)(rq.color.exposure_ev * 10.0f);
-    for (size_t k = 0; k < rq.dst.size(); ++k) std::memset(rq.dst[k], v, rq.capacity[k]);
+    for (size_t k = 0; k < rq.dst.size(); ++k) {
+      std::memset(rq.dst[k], v, rq.capacity[k]);
+      if (rq.files[k].format != RD_FILE_ROWS && rq.files[k].file_bytes) *rq.files[k].file_bytes = rq.capacity[k];
+    }
     return Status{};
   }
   Status render(const std::vector<ServedImage*>& ims, const std::vector<rd_base*>&,
@@ -858,9 +904,9 @@ rd_status rd_server_submit_develop(rd_server* s, uint32_t image_id, uint64_t rev
   return RD_OK;
 }
 
-rd_status rd_server_submit_export(rd_server* s, uint32_t image_id, uint64_t revision, const rd_color_desc* color,
-                                  const rd_output_desc* outputs, int32_t n_outputs, void* const* dst,
-                                  const size_t* capacities, uint64_t* request_id) {
+static rd_status submit_export(rd_server* s, uint32_t image_id, uint64_t revision, const rd_color_desc* color,
+                               const rd_output_desc* outputs, const rd_export_file* files, int32_t n_outputs,
+                               void* const* dst, const size_t* capacities, uint64_t* request_id) {
   if (!s || !color || !outputs || !dst || !capacities || n_outputs <= 0) return RD_INVALID_INPUT;
   std::lock_guard<std::mutex> lk(s->mu);
   auto it = s->images.find(image_id);
@@ -872,11 +918,35 @@ rd_status rd_server_submit_export(rd_server* s, uint32_t image_id, uint64_t revi
     const rd_status st = rd_output_dimensions(im.sensor.crop_width, im.sensor.crop_height, &outputs[k], &ow, &oh, &bpp);
     if (st != RD_OK) return st;
     const size_t bytes = (size_t)ow * oh * bpp;
-    if (!dst[k] || capacities[k] < bytes) return RD_INVALID_DIMENSIONS;
+    rd_export_file f{};
+    if (files) f = files[k];
+    size_t need = bytes, working = bytes;
+    if (f.format == RD_FILE_PNG || f.format == RD_FILE_JPEG) {
+      const bool png = f.format == RD_FILE_PNG;
+      if ((f.icc_len && !f.icc) || (f.exif_len && !f.exif)) return RD_INVALID_INPUT;
+      if (png ? (outputs[k].format != RD_OUTPUT_SRGB8 && outputs[k].format != RD_OUTPUT_SRGB16)
+              : (outputs[k].format != RD_OUTPUT_SRGB8 || f.quality < 1 || f.quality > 100))
+        return RD_INVALID_INPUT;
+      need = png ? rd_png_bound(ow, oh, outputs[k].format == RD_OUTPUT_SRGB16 ? 16 : 8, f.icc_len, f.exif_len)
+                 : rd_jpeg_bound(ow, oh, f.icc_len, f.exif_len);
+      if (need == 0) return RD_INVALID_DIMENSIONS;
+      // Rows, the file, and the encoder's scratch (at most three times the rows).
+      working = bytes + need + 3 * bytes;
+    } else if (f.format != RD_FILE_ROWS) {
+      return RD_INVALID_INPUT;
+    }
+    if (!dst[k] || capacities[k] < need) return RD_INVALID_DIMENSIONS;
+    rq.icc.emplace_back(f.icc ? f.icc : nullptr, f.icc ? f.icc + f.icc_len : nullptr);
+    rq.exif.emplace_back(f.exif ? f.exif : nullptr, f.exif ? f.exif + f.exif_len : nullptr);
     rq.outputs.push_back(outputs[k]);
+    rq.files.push_back(f);
     rq.dst.push_back(dst[k]);
     rq.capacity.push_back(capacities[k]);
-    rq.largest_output = std::max(rq.largest_output, bytes);
+    rq.largest_output = std::max(rq.largest_output, working);
+  }
+  for (size_t k = 0; k < rq.files.size(); ++k) {  // the files read the request's own copies
+    rq.files[k].icc = rq.icc[k].empty() ? nullptr : rq.icc[k].data();
+    rq.files[k].exif = rq.exif[k].empty() ? nullptr : rq.exif[k].data();
   }
   rq.id = s->next_request++;
   rq.ticket = {revision, ++s->sequence};
@@ -896,6 +966,19 @@ rd_status rd_server_submit_export(rd_server* s, uint32_t image_id, uint64_t revi
   im.has_export = true;
   s->wake();
   return RD_OK;
+}
+
+rd_status rd_server_submit_export(rd_server* s, uint32_t image_id, uint64_t revision, const rd_color_desc* color,
+                                  const rd_output_desc* outputs, int32_t n_outputs, void* const* dst,
+                                  const size_t* capacities, uint64_t* request_id) {
+  return submit_export(s, image_id, revision, color, outputs, nullptr, n_outputs, dst, capacities, request_id);
+}
+
+rd_status rd_server_submit_export_files(rd_server* s, uint32_t image_id, uint64_t revision, const rd_color_desc* color,
+                                        const rd_output_desc* outputs, const rd_export_file* files, int32_t n_outputs,
+                                        void* const* dst, const size_t* capacities, uint64_t* request_id) {
+  if (!files) return RD_INVALID_INPUT;
+  return submit_export(s, image_id, revision, color, outputs, files, n_outputs, dst, capacities, request_id);
 }
 
 int32_t rd_server_poll(rd_server* s, rd_server_result* out, int32_t max_results, int32_t wait_ms) {

@@ -95,6 +95,48 @@ class PreviewServer:
         self._export_buffers[int(rid.value)] = arrays  # alive until the result is polled
         return int(rid.value), arrays
 
+    def submit_export_files(self, image_id: int, revision: int, color: ColorContract, outputs: list[OutputSpec],
+                            files: list[dict]) -> tuple[int, list[np.ndarray], np.ndarray]:
+        """Export whose outputs are encoded as files (export::encode): files[k] is
+        {"format": "png" | "jpeg" | "rows", "quality": q, "icc": bytes, "exif": bytes}.
+        Returns the request id, one byte buffer per output and the array that
+        receives each file's size; file k is buffers[k][:sizes[k]] once the
+        export's result is polled."""
+        cw, ch = self._crops[image_id]
+        arrays, descs_c, files_c = [], [], []
+        sizes = np.zeros(len(outputs), dtype=np.uint64)
+        keep = []
+        for k, (spec, f) in enumerate(zip(outputs, files)):
+            ow, oh = spec.dimensions(cw, ch)
+            fmt = _ffi.FILE_FORMAT[f.get("format", "rows")]
+            icc, exif = f.get("icc") or b"", f.get("exif") or b""
+            if fmt == 1:
+                cap = int(self.lib.rd_png_bound(ow, oh, 16 if spec.format == "srgb16" else 8, len(icc), len(exif)))
+                arrays.append(np.empty(max(cap, 1), dtype=np.uint8))
+            elif fmt == 2:
+                arrays.append(np.empty(max(int(self.lib.rd_jpeg_bound(ow, oh, len(icc), len(exif))), 1), dtype=np.uint8))
+            else:
+                arrays.append(np.empty((oh, 3 * ow), dtype=spec.dtype))
+            icc_a = np.frombuffer(icc, dtype=np.uint8) if icc else None
+            exif_a = np.frombuffer(exif, dtype=np.uint8) if exif else None
+            keep += [icc_a, exif_a]
+            files_c.append(_ffi.ExportFile(
+                fmt, int(f.get("quality", 90)),
+                icc_a.ctypes.data_as(_ffi.U8P) if icc_a is not None else None, len(icc),
+                exif_a.ctypes.data_as(_ffi.U8P) if exif_a is not None else None, len(exif),
+                ctypes.cast(sizes.ctypes.data + 8 * k, _ffi.U64P)))
+            descs_c.append(spec.to_c())
+        descs = (_ffi.OutputDesc * len(outputs))(*descs_c)
+        fc = (_ffi.ExportFile * len(outputs))(*files_c)
+        dst = (ctypes.c_void_p * len(outputs))(*[a.ctypes.data for a in arrays])
+        caps = (ctypes.c_size_t * len(outputs))(*[a.nbytes for a in arrays])
+        c = color.to_c()
+        rid = ctypes.c_uint64()
+        self._check(self.lib.rd_server_submit_export_files(self.handle, image_id, revision, ctypes.byref(c), descs,
+                                                           fc, len(outputs), dst, caps, ctypes.byref(rid)))
+        self._export_buffers[int(rid.value)] = (arrays, sizes)  # alive until the result is polled
+        return int(rid.value), arrays, sizes
+
     def poll(self, max_results: int = 256, wait_ms: int = 0) -> list[dict]:
         buf = (_ffi.ServerResult * max_results)()
         n = self.lib.rd_server_poll(self.handle, buf, max_results, wait_ms)

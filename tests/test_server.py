@@ -237,6 +237,76 @@ def test_dry_close_cancels_a_pending_export():
     s.close()
 
 
+def test_dry_export_files_fill_the_client_buffers():
+    s = PreviewServer.dry(develop_us=1000, render_us=100)
+    _open(s, 3)
+    _results(s)
+    specs = [OutputSpec(format="srgb8"), OutputSpec(format="srgb16"), OutputSpec(format="srgb8")]
+    files = [{"format": "png"}, {"format": "png", "icc": b"profile"}, {"format": "jpeg", "quality": 80}]
+    rid, outs, sizes = s.submit_export_files(3, 1, _edit(0.7), specs, files)
+    res = {r["request_id"]: r for r in _results(s)}
+    assert res[rid]["kind"] == EXPORT and res[rid]["status"] == RD_OK
+    assert [int(n) for n in sizes] == [o.nbytes for o in outs]  # the dry executor fills whole buffers
+    assert np.all(outs[2] == 7)
+    s.close()
+
+
+def test_export_files_are_validated_at_submission():
+    from rohditor_gb300.processor import GpuPreviewError
+
+    s = PreviewServer.dry(develop_us=1000, render_us=100)
+    _open(s, 0)
+    _results(s)
+    bad = [
+        ([OutputSpec(format="srgb16")], [{"format": "jpeg"}]),                        # JPEG takes 8-bit rows
+        ([OutputSpec(format="extended_f16", headroom=2.0)], [{"format": "png"}]),  # PNG takes display rows
+        ([OutputSpec(format="srgb8")], [{"format": "jpeg", "quality": 0}]),
+        ([OutputSpec(format="srgb8")], [{"format": "jpeg", "quality": 101}]),
+    ]
+    for specs, files in bad:
+        with pytest.raises(GpuPreviewError) as err:
+            s.submit_export_files(0, 1, _edit(0.1), specs, files)
+        assert err.value.code == 8
+    s.close()
+
+
+@pytest.mark.gpu
+def test_served_export_files_match_the_direct_encoders(device):
+    """Served PNG and JPEG exports equal the encoders run on the direct path's
+    output rows, byte for byte, metadata included."""
+    from rohditor_gb300 import GpuSensorProcessor, GpuSpatialProcessor, GpuPreviewProcessor, JpegEncoder, PngEncoder
+    from rohditor_gb300.workloads import CAMERA_TO_REC2020, sixteen_knot_curve
+
+    server = PreviewServer(0, budget_bytes=2 << 30)
+    raw, desc, cap, optics, wb = _image(w=640, h=480, seed=31)
+    server.open(6, raw, desc, cap, optics, (320, 240), wb, CAMERA_TO_REC2020)
+    color = ColorContract(wb_gains=wb, camera_to_rec2020=CAMERA_TO_REC2020, exposure_ev=0.2,
+                          tone_lut=sixteen_knot_curve(seed=6))
+    icc, exif = bytes(range(256)) * 3, b"II*\x00" + bytes(40)
+    specs = [OutputSpec(format="srgb8"), OutputSpec(format="srgb16", dither="ordered8x8"),
+             OutputSpec(format="srgb8", orientation="rotate90")]
+    files = [{"format": "png", "icc": icc, "exif": exif}, {"format": "png"},
+             {"format": "jpeg", "quality": 85, "icc": icc, "exif": exif}]
+    rid, outs, sizes = server.submit_export_files(6, 1, color, specs, files)
+    server.drain()
+    res = {r["request_id"]: r for r in server.poll(64)}
+    assert res[rid]["kind"] == EXPORT and res[rid]["status"] == RD_OK
+    src = GpuSensorProcessor(device).develop(raw, desc, cap)
+    base = GpuSpatialProcessor(device).reduce_preview(src, optics, (640, 480), wb, CAMERA_TO_REC2020)
+    preview = GpuPreviewProcessor(device)
+    for spec, f, out, n in zip(specs, files, outs, sizes):
+        rows, _, _ = preview.render_output(base, color, spec)
+        rows = rows.reshape(rows.shape[0], -1, 3)
+        if f["format"] == "png":
+            ref = PngEncoder(device).encode(rows, f.get("icc", b""), f.get("exif"))
+        else:
+            ref = JpegEncoder(device).encode(rows, f["quality"], f.get("icc", b""), f.get("exif"))
+        assert out[:int(n)].tobytes() == ref, (spec.format, f["format"])
+    base.release()
+    src.release()
+    server.close()
+
+
 @pytest.mark.gpu
 def test_served_export_matches_the_direct_path(device):
     """A served full-resolution export equals develop + spatial pass at the crop
