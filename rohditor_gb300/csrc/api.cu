@@ -943,6 +943,7 @@ static Status png_args(const void* rgb, uint32_t width, uint32_t height, uint64_
     return Status{RD_INVALID_INPUT, "encoders require tightly packed RGB rows"};
   if (bit_depth == 16 && reinterpret_cast<uintptr_t>(rgb) % 2)
     return Status{RD_INVALID_INPUT, "16-bit rows must be 2-byte aligned"};
+  if (!rd::png_metadata_ok(icc_len, exif_len)) return Status{RD_INVALID_INPUT, "metadata too large for a PNG chunk"};
   return Status{};
 }
 
@@ -950,12 +951,8 @@ uint64_t rd_png_bound(uint32_t width, uint32_t height, int32_t bit_depth, uint64
   if ((bit_depth != 8 && bit_depth != 16) || width == 0 || height == 0 || width > (uint32_t)INT32_MAX ||
       height > (uint32_t)INT32_MAX)
     return 0;
-  // The header's size depends only on the metadata lengths.
-  const std::vector<uint8_t> icc(icc_len), exif(exif_len);
-  std::vector<uint8_t> header;
-  if (!rd::png_header((int)width, (int)height, bit_depth, icc.data(), icc_len, exif.data(), exif_len, &header).ok())
-    return 0;
-  return rd::png_bound((int)width, (int)height, bit_depth, header.size());
+  if (!rd::png_metadata_ok(icc_len, exif_len)) return 0;
+  return rd::png_bound((int)width, (int)height, bit_depth, rd::png_header_bytes(icc_len, exif_len));
 }
 
 rd_status rd_encode_png_device(rd_ctx* h, const void* d_rgb, uint32_t width, uint32_t height, uint64_t row_stride,
@@ -1031,11 +1028,13 @@ static Status jpeg_args(const void* rgb, uint32_t width, uint32_t height, uint64
                         const uint8_t* icc, uint64_t icc_len, const uint8_t* exif, uint64_t exif_len) {
   // The JPEG arm takes 8-bit rows only (export.rs:166 matches ExportImage::Rgb8).
   RD_TRY(png_args(rgb, width, height, row_stride, 8, icc, icc_len, exif, exif_len));
+  if (!rd::jpeg_metadata_ok(icc_len, exif_len)) return Status{RD_INVALID_INPUT, "metadata too large for JPEG segments"};
   return rd::jpeg_check((int)width, (int)height, quality);
 }
 
 uint64_t rd_jpeg_bound(uint32_t width, uint32_t height, uint64_t icc_len, uint64_t exif_len) {
-  if (width == 0 || height == 0 || width > 65535 || height > 65535) return 0;
+  if (width == 0 || height == 0 || width > 65535 || height > 65535 || !rd::jpeg_metadata_ok(icc_len, exif_len))
+    return 0;
   return rd::jpeg_bound((int)width, (int)height, icc_len, exif_len);
 }
 

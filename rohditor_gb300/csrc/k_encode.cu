@@ -820,8 +820,27 @@ uint64_t png_stream_bytes(int W, int H, int depth) { return (uint64_t)H * (1ull 
 
 uint64_t png_segments(uint64_t stream_bytes) { return (stream_bytes + SEG - 1) / SEG; }
 
+// Largest metadata a PNG chunk carries: the chunk length is a 31-bit count
+// and the profile's chunk adds its name and zlib framing.
+constexpr uint64_t PNG_METADATA_LIMIT = 0x7FF00000ull;
+
+bool png_metadata_ok(uint64_t icc_len, uint64_t exif_len) {
+  return icc_len <= PNG_METADATA_LIMIT && exif_len <= PNG_METADATA_LIMIT;
+}
+
+uint64_t png_header_bytes(uint64_t icc_len, uint64_t exif_len) {
+  uint64_t n = 8 + 25;  // signature, IHDR
+  if (icc_len) {
+    const uint64_t blocks = (icc_len + 65534) / 65535;
+    n += 12 + std::strlen(ICC_PROFILE_NAME) + 2 + 2 + 5 * blocks + icc_len + 4;
+  }
+  if (exif_len) n += 12 + exif_len;
+  return n;
+}
+
 Status png_header(int W, int H, int depth, const uint8_t* icc, size_t icc_len, const uint8_t* exif, size_t exif_len,
                   std::vector<uint8_t>* out) {
+  if (!png_metadata_ok(icc_len, exif_len)) return Status{RD_INVALID_INPUT, "metadata too large for a PNG chunk"};
   std::vector<uint8_t>& h = *out;
   h = {0x89, 'P', 'N', 'G', 0x0D, 0x0A, 0x1A, 0x0A};
   std::vector<uint8_t> ihdr;

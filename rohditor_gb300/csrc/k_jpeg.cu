@@ -393,6 +393,12 @@ void marker(std::vector<uint8_t>& v, uint8_t m, const std::vector<uint8_t>& body
 
 }  // namespace
 
+bool jpeg_metadata_ok(uint64_t icc_len, uint64_t exif_len) {
+  // APP1 holds "Exif\0\0" and the block in one segment; APP2 segments carry
+  // up to 65519 profile bytes each, numbered 1..255.
+  return exif_len <= 65527 && icc_len <= 255ull * 65519;
+}
+
 Status jpeg_check(int W, int H, int quality) {
   if (quality < 1 || quality > 100) return Status{RD_INVALID_INPUT, "JPEG quality must be 1..100"};
   if (W > 65535 || H > 65535) return Status{RD_INVALID_DIMENSIONS, "JPEG dimensions are limited to 65535"};
@@ -411,6 +417,7 @@ uint64_t jpeg_bound(int W, int H, uint64_t icc_len, uint64_t exif_len) {
 Status run_jpeg_encode(Context& ctx, const uint8_t* d_rgb, int W, int H, int quality, const uint8_t* icc,
                        size_t icc_len, const uint8_t* exif, size_t exif_len, uint8_t* d_file, uint64_t* d_file_bytes) {
   RD_TRY(jpeg_check(W, H, quality));
+  if (!jpeg_metadata_ok(icc_len, exif_len)) return Status{RD_INVALID_INPUT, "metadata too large for JPEG segments"};
   if (ctx.capturing) return Status{RD_INVALID_INPUT, "the JPEG encoder reads its symbol counts back mid-way"};
   const int bw = (W + 7) / 8, bh = (H + 7) / 8;
   const int64_t blocks = (int64_t)bw * bh;
@@ -473,13 +480,11 @@ Status run_jpeg_encode(Context& ctx, const uint8_t* d_rgb, int W, int H, int qua
     if (exif && exif_len) {
       std::vector<uint8_t> b = {'E', 'x', 'i', 'f', 0, 0};
       b.insert(b.end(), exif, exif + exif_len);
-      if (b.size() > 65533) st = Status{RD_INVALID_INPUT, "EXIF block does not fit in an APP1 segment"};
       marker(header, 0xE1, b);
     }
     const size_t chunk = 65519;
     const size_t nchunks = (icc_len + chunk - 1) / chunk;
-    if (icc && icc_len && nchunks > 255) st = Status{RD_INVALID_INPUT, "ICC profile too large for APP2 segments"};
-    for (size_t k = 0; st.ok() && icc && k < nchunks; ++k) {
+    for (size_t k = 0; icc && k < nchunks; ++k) {
       std::vector<uint8_t> b = {'I', 'C', 'C', '_', 'P', 'R', 'O', 'F', 'I', 'L', 'E', 0, (uint8_t)(k + 1),
                                 (uint8_t)nchunks};
       const size_t a = k * chunk, e = std::min(icc_len, a + chunk);

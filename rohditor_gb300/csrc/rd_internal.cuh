@@ -332,6 +332,8 @@ uint64_t png_stream_bytes(int W, int H, int depth);
 Status png_header(int W, int H, int depth, const uint8_t* icc, size_t icc_len, const uint8_t* exif, size_t exif_len,
                   std::vector<uint8_t>* out);
 uint64_t png_bound(int W, int H, int depth, uint64_t header_bytes);
+bool png_metadata_ok(uint64_t icc_len, uint64_t exif_len);
+uint64_t png_header_bytes(uint64_t icc_len, uint64_t exif_len);
 Status run_png_encode(Context& ctx, const void* d_rgb, int W, int H, int depth, const std::vector<uint8_t>& header,
                       uint8_t* d_png, uint64_t* d_png_bytes);
 
@@ -341,6 +343,7 @@ Status run_png_encode(Context& ctx, const void* d_rgb, int W, int H, int depth, 
 // image's symbol counts back to build the Huffman tables, so it synchronises
 // the stream once and cannot run under graph capture.
 Status jpeg_check(int W, int H, int quality);
+bool jpeg_metadata_ok(uint64_t icc_len, uint64_t exif_len);
 uint64_t jpeg_bound(int W, int H, uint64_t icc_len, uint64_t exif_len);
 Status run_jpeg_encode(Context& ctx, const uint8_t* d_rgb, int W, int H, int quality, const uint8_t* icc,
                        size_t icc_len, const uint8_t* exif, size_t exif_len, uint8_t* d_file, uint64_t* d_file_bytes);

@@ -924,6 +924,8 @@ static rd_status submit_export(rd_server* s, uint32_t image_id, uint64_t revisio
     if (f.format == RD_FILE_PNG || f.format == RD_FILE_JPEG) {
       const bool png = f.format == RD_FILE_PNG;
       if ((f.icc_len && !f.icc) || (f.exif_len && !f.exif)) return RD_INVALID_INPUT;
+      if (png ? !rd::png_metadata_ok(f.icc_len, f.exif_len) : !rd::jpeg_metadata_ok(f.icc_len, f.exif_len))
+        return RD_INVALID_INPUT;
       if (png ? (outputs[k].format != RD_OUTPUT_SRGB8 && outputs[k].format != RD_OUTPUT_SRGB16)
               : (outputs[k].format != RD_OUTPUT_SRGB8 || f.quality < 1 || f.quality > 100))
         return RD_INVALID_INPUT;
