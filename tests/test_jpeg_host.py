@@ -1,10 +1,46 @@
-"""JPEG pieces that run without a GPU: the oracle's integer coefficients against
-the floating-point FDCT of T.81 (A.3.3), and the oracle's baseline decoder on a
+"""JPEG pieces that run without a GPU: the encoder's own integer arithmetic
+(rohditor_gb300/csrc/jpeg.cuh compiled for the host) against the oracle's
+independent restatement, the oracle's integer coefficients against the
+floating-point FDCT of T.81 (A.3.3), and the oracle's baseline decoder on a
 file written here in plain Python (fixed Huffman tables, restart markers, byte
 stuffing), so that the decoder the GPU tests rely on is itself checked."""
 
+import os
+import shutil
+import subprocess
+
 import numpy as np
 import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def jpeg_harness(tmp_path_factory):
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no host C++ compiler")
+    exe = tmp_path_factory.mktemp("jpeg") / "jpeg_host"
+    subprocess.run([cxx, "-O2", "-std=c++17", "-Wall", "-o", str(exe),
+                    os.path.join(ROOT, "tests", "native", "jpeg_host.cpp")], check=True)
+    return exe
+
+
+@pytest.mark.parametrize("quality", [1, 25, 50, 75, 90, 100])
+def test_encoder_arithmetic_matches_the_oracle(jpeg_harness, oracle, tmp_path, quality):
+    rng = np.random.default_rng(quality)
+    for h, w, kind in ((1, 1, "random"), (13, 21, "random"), (40, 56, "smooth"), (64, 64, "extreme")):
+        if kind == "random":
+            img = rng.integers(0, 256, (h, w, 3), dtype=np.uint8)
+        elif kind == "extreme":
+            img = np.where(rng.random((h, w, 3)) < 0.5, 0, 255).astype(np.uint8)
+        else:
+            img = _smooth(rng, h, w)
+        src, dst = tmp_path / "in.rgb", tmp_path / "out.coef"
+        src.write_bytes(img.tobytes())
+        subprocess.run([str(jpeg_harness), str(src), str(dst), str(w), str(h), str(quality)], check=True)
+        got = np.fromfile(dst, dtype=np.int16).reshape(-1, 3, 64)
+        assert np.array_equal(got, oracle.jpeg_coefficients(img, quality)), (h, w, kind)
 
 ANNEX_K_LUMA = [16, 11, 10, 16, 24, 40, 51, 61, 12, 12, 14, 19, 26, 58, 60, 55, 14, 13, 16, 24, 40, 57, 69, 56,
                 14, 17, 22, 29, 51, 87, 80, 62, 18, 22, 37, 56, 68, 109, 103, 77, 24, 35, 55, 64, 81, 104, 113, 92,
