@@ -19,7 +19,9 @@ reference workload set, each under its own key: the 3008x2008 Clip + AMaZE
 full-resolution render and the 24 MP develop with RCD and with MHC
 (`configs`), the 48-image uneven batch (`batched`), the served trace over
 16 mixed-size images under a 120 GB budget (`edit_latency`), the
-full-resolution output formats (`export`) and the 102 MP export stream
+full-resolution output formats with their PNG and JPEG files (`export`,
+`export.png`; the PNG leg beside the oracle's filter selection + zlib level
+6 on one core) and the 102 MP export stream
 (`export_stream`); then the CPU baseline, the oracle developing the very
 same mosaic on the host cores, whose outputs also give the per-stage parity
 of the GPU develop (`parity`).
