@@ -136,3 +136,21 @@ def test_png_bound_is_the_stored_worst_case():
         assert PngEncoder.bound(w, h, depth, icc, exif) == header + stream + 17 * segments + 6 + 12
     assert PngEncoder.bound(10, 10, 12) == 0
     assert PngEncoder.bound(0, 10, 8) == 0
+
+
+def test_runs_across_chunk_and_segment_boundaries(harness, tmp_path):
+    # A thread's tokens depend on runs that start or end in other threads'
+    # 32-byte chunks and stop at segment ends: runs of every length from 1 to
+    # 600 placed at every offset around a chunk boundary and a segment boundary.
+    rng = np.random.default_rng(11)
+    for anchor in (4 * 32, SEG - 40):
+        pieces = []
+        for length in list(range(1, 40)) + [255, 256, 257, 258, 259, 260, 261, 515, 516, 517, 600]:
+            for shift in range(0, 36, 5):
+                noise = rng.integers(0, 256, anchor - shift, dtype=np.uint8)
+                pieces.append(noise.tobytes() + bytes([rng.integers(0, 256)]) * length)
+        data = b"".join(pieces)
+        z, crc, adler, segments, _ = _deflate(harness, tmp_path, data)
+        assert zlib.decompress(z) == data
+        assert crc == zlib.crc32(data) and adler == zlib.adler32(data)
+

@@ -270,6 +270,21 @@ def test_export_files_are_validated_at_submission():
     s.close()
 
 
+def test_dry_export_files_are_charged_their_encoder():
+    # A file export holds the output rows, the file and the encoder's scratch:
+    # a budget that admits the rows-only export refuses the same output as a PNG.
+    layers, develop = _footprint(1024, 1024, 512, 512)
+    rows_export = 32 * 1024 * 1024 + 3 * 1024 * 1024 + 64 * MB
+    s = PreviewServer.dry(budget_bytes=layers + rows_export + MB, develop_us=1000, render_us=100)
+    _open(s, 0)
+    _results(s)
+    rid, _ = s.submit_export(0, 1, _edit(0.1), [OutputSpec(format="srgb8")])
+    assert {r["request_id"]: r for r in _results(s)}[rid]["status"] == RD_OK
+    rid, _, _ = s.submit_export_files(0, 2, _edit(0.1), [OutputSpec(format="srgb8")], [{"format": "png"}])
+    assert {r["request_id"]: r for r in _results(s)}[rid]["status"] == RD_OVER_BUDGET
+    s.close()
+
+
 @pytest.mark.gpu
 def test_served_export_files_match_the_direct_encoders(device):
     """Served PNG and JPEG exports equal the encoders run on the direct path's
