@@ -106,8 +106,18 @@ RD_JHD void dct8(const int* in, int* out, int shift) {
   }
 }
 
-// Rounded to the nearest multiple of q, halves away from zero.
-RD_JHD int quantize(int coef, int q) { return coef >= 0 ? (coef + q / 2) / q : -((-coef + q / 2) / q); }
+// m = ceil(2^31 / q) for a step q of 1..255: with m = (2^31 + e) / q,
+// 0 <= e < q, (n * m) >> 31 = floor(n / q + n e / (q 2^31)) = floor(n / q)
+// whenever n e < 2^31, which holds for every n below 2^23.
+RD_JHD uint32_t quant_reciprocal(int q) { return (uint32_t)(((1ull << 31) + (uint64_t)q - 1) / (uint64_t)q); }
+
+// coef / q rounded to the nearest integer, halves away from zero, with m the
+// step's reciprocal (|coef| stays far below 2^22 for 8-bit samples).
+RD_JHD int quantize(int coef, int q, uint32_t m) {
+  const uint32_t n = (uint32_t)(coef >= 0 ? coef : -coef) + (uint32_t)(q >> 1);
+  const int r = (int)(((uint64_t)n * m) >> 31);
+  return coef >= 0 ? r : -r;
+}
 
 // Magnitude category (T.81 F.1.2.1): bits of |v|, 0 for 0.
 RD_JHD int category(int v) {

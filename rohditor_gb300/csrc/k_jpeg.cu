@@ -54,6 +54,7 @@ struct CoefParams {
   int W, H, bw, bh;
   int16_t* coef;  // [block][component][64], zigzag order, blocks in raster order
   uint8_t quant[2][64];
+  uint32_t recip[2][64];  // quant_reciprocal of each step
   uint8_t zigzag_of[64];  // natural index -> zigzag position
 };
 
@@ -100,7 +101,8 @@ __global__ void __launch_bounds__(COEF_THREADS) jpeg_coef_kernel(const __grid_co
 #pragma unroll
     for (int v = 0; v < 8; ++v) {
       const int nat = v * 8 + u;
-      q[lane * COEF_STRIDE + c * 64 + P.zigzag_of[nat]] = (int16_t)quantize(f[v], P.quant[c == 0 ? 0 : 1][nat]);
+      const int tq = c == 0 ? 0 : 1;
+      q[lane * COEF_STRIDE + c * 64 + P.zigzag_of[nat]] = (int16_t)quantize(f[v], P.quant[tq][nat], P.recip[tq][nat]);
     }
   }
   __syncthreads();
@@ -448,6 +450,8 @@ Status run_jpeg_encode(Context& ctx, const uint8_t* d_rgb, int W, int H, int qua
   cp.coef = coef;
   quant_table(0, quality, cp.quant[0]);
   quant_table(1, quality, cp.quant[1]);
+  for (int t = 0; t < 2; ++t)
+    for (int i = 0; i < 64; ++i) cp.recip[t][i] = quant_reciprocal(cp.quant[t][i]);
   uint8_t zz[64];
   zigzag_order(zz);
   for (int k = 0; k < 64; ++k) cp.zigzag_of[zz[k]] = (uint8_t)k;

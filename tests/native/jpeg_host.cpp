@@ -57,8 +57,9 @@ int main(int argc, char** argv) {
           dct8(col, fv, 15);
           for (int v = 0; v < 8; ++v) {
             const int nat = v * 8 + u;
+            const int q = quant[c == 0 ? 0 : 1][nat];
             coef[(((size_t)by * bw + bx) * 3 + c) * 64 + zigzag_of[nat]] =
-                (int16_t)quantize(fv[v], quant[c == 0 ? 0 : 1][nat]);
+                (int16_t)quantize(fv[v], q, quant_reciprocal(q));
           }
         }
     }

@@ -54,6 +54,15 @@ def _smooth(rng, h, w):
     return np.clip(img, 0, 255).astype(np.uint8)
 
 
+def test_quantisation_reciprocals_divide_exactly():
+    # floor(n / q) == (n * ceil(2^31 / q)) >> 31 for every step and every
+    # numerator the encoder can meet (|coefficient| + q / 2 stays below 2^11).
+    n = np.arange(0, 1 << 14, dtype=np.uint64)
+    for q in range(1, 256):
+        m = np.uint64(((1 << 31) + q - 1) // q)
+        assert np.array_equal((n * m) >> np.uint64(31), n // np.uint64(q)), q
+
+
 def test_oracle_coefficients_follow_the_float_fdct(oracle):
     rng = np.random.default_rng(1)
     img = _smooth(rng, 16, 24)
