@@ -136,6 +136,17 @@ def test_png_bound_is_the_stored_worst_case():
         assert PngEncoder.bound(w, h, depth, icc, exif) == header + stream + 17 * segments + 6 + 12
     assert PngEncoder.bound(10, 10, 12) == 0
     assert PngEncoder.bound(0, 10, 8) == 0
+    assert PngEncoder.bound(10, 10, 8, 1 << 40, 0) == 0  # metadata past a chunk's 31-bit length
+    assert PngEncoder.bound(10, 10, 8, 0, 1 << 40) == 0
+
+
+def test_jpeg_bound_limits():
+    from rohditor_gb300 import JpegEncoder
+
+    assert JpegEncoder.bound(6048, 4024) > 0
+    assert JpegEncoder.bound(65535, 1) > 0 and JpegEncoder.bound(65536, 1) == 0
+    assert JpegEncoder.bound(16, 16, 0, 65527) > 0 and JpegEncoder.bound(16, 16, 0, 65528) == 0  # one APP1
+    assert JpegEncoder.bound(16, 16, 255 * 65519, 0) > 0 and JpegEncoder.bound(16, 16, 255 * 65519 + 1, 0) == 0
 
 
 def test_runs_across_chunk_and_segment_boundaries(harness, tmp_path):

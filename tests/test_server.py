@@ -262,6 +262,7 @@ def test_export_files_are_validated_at_submission():
         ([OutputSpec(format="extended_f16", headroom=2.0)], [{"format": "png"}]),  # PNG takes display rows
         ([OutputSpec(format="srgb8")], [{"format": "jpeg", "quality": 0}]),
         ([OutputSpec(format="srgb8")], [{"format": "jpeg", "quality": 101}]),
+        ([OutputSpec(format="srgb8")], [{"format": "jpeg", "exif": bytes(65528)}]),  # more than one APP1
     ]
     for specs, files in bad:
         with pytest.raises(GpuPreviewError) as err:
